@@ -1,0 +1,209 @@
+/*
+ * snac_gpu.h -- C ABI of snac_gb300, a GB300 (sm_103a) implementation of
+ * SNaC's per-time-step hot path.
+ *
+ * Every entry point is plain C (extern "C", pointers and sizes, no C++ or
+ * torch types) so that SNaC's Fortran driver can bind it with
+ * iso_c_binding.  Each declaration names the reference interface it replaces
+ * (paths relative to the SNaC source tree).
+ *
+ * Two layers:
+ *   1. Reference-signature calls (snac_rk_mom, snac_fillps, ...): the same
+ *      argument lists as the Fortran subroutines, one block at a time, on the
+ *      caller's host arrays.  Arrays registered with snac_register() are used
+ *      through their device mirror without copies; unregistered arrays are
+ *      copied to the device and back around the call.
+ *   2. Domain calls (snac_init, snac_*_all, snac_step): all blocks of a case
+ *      resident in HBM, the block-to-block halo exchange done on the device,
+ *      the Poisson solve, and whole RK3 steps driven by the library.
+ *
+ * Array conventions follow the reference's Fortran declarations:
+ *   halo'd field   f(lo(1)-1:hi(1)+1, lo(2)-1:hi(2)+1, lo(3)-1:hi(3)+1), x fastest;
+ *   RK storage     dudtrko(lo(1):hi(1), lo(2):hi(2), lo(3):hi(3));
+ *   1-D metrics    dxc(lo(1)-1:hi(1)+1), passed as a pointer to element lo(1)-1;
+ *   BC planes      rhsx(lo(2):hi(2),lo(3):hi(3),0:1), rhsy(lo(1):hi(1),lo(3):hi(3),0:1),
+ *                  rhsz(lo(1):hi(1),lo(2):hi(2),0:1);
+ *   logical(0:1,3) arguments are int[3][2] (side fastest), 0 = .false.
+ *
+ * Errors: every function returns SNAC_OK (0) or one of the SNAC_ERR_* codes;
+ * snac_last_error() returns a message for the last failure.  There is no CPU
+ * fallback: without a usable CUDA device the calls fail with SNAC_ERR_CUDA.
+ */
+#ifndef SNAC_GPU_H
+#define SNAC_GPU_H
+#include <stddef.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SNAC_MAX_SCAL 4
+
+enum {
+  SNAC_OK = 0,
+  SNAC_ERR_ARG = 1,            /* invalid argument or inconsistent input */
+  SNAC_ERR_CUDA = 2,           /* CUDA runtime error (no device, launch failure, ...) */
+  SNAC_ERR_NOT_CONVERGED = 3,  /* a Poisson/Helmholtz solve hit maxiter above tolerance */
+  SNAC_ERR_NAN = 4,            /* NaN/Inf detected in a reduction */
+  SNAC_ERR_TIMEOUT = 5,        /* a bounded device-side wait gave up */
+  SNAC_ERR_BOUNDS = 6,         /* a device-side bounds check fired */
+  SNAC_ERR_STATE = 7,          /* call out of order (e.g. snac_step before snac_init) */
+  SNAC_ERR_UNSUPPORTED = 8,    /* input the library does not implement */
+  SNAC_ERR_NOMEM = 9           /* device allocation failed */
+};
+
+/* field identifiers for the domain layer */
+enum {
+  SNAC_U = 0, SNAC_V = 1, SNAC_W = 2, SNAC_P = 3, SNAC_PP = 4, SNAC_PO = 5,
+  SNAC_DUDTRKO = 6, SNAC_DVDTRKO = 7, SNAC_DWDTRKO = 8,
+  SNAC_S0 = 9,                       /* scalar s: SNAC_S0 + s, s < SNAC_MAX_SCAL */
+  SNAC_DSDTRKO0 = 20                 /* scalar RK storage: SNAC_DSDTRKO0 + s */
+};
+
+/* grid arrays for snac_get_grid */
+enum { SNAC_G_DXC = 0, SNAC_G_DXF = 1, SNAC_G_XC = 2, SNAC_G_XF = 3 };
+
+/* r2r transform kinds, FFTW's unnormalised definitions (fftw.f90:9-29) */
+enum { SNAC_R2HC = 0, SNAC_HC2R = 1, SNAC_REDFT00 = 3, SNAC_REDFT01 = 4, SNAC_REDFT10 = 5,
+       SNAC_REDFT11 = 6, SNAC_RODFT00 = 7, SNAC_RODFT01 = 8, SNAC_RODFT10 = 9, SNAC_RODFT11 = 10 };
+
+/* One entry of the &blocks namelist (param.f90:332-360, docs/INFO_INPUT.md).
+ * cbcvel[comp][dir][side] = block_cbcvel(side,dir,comp,ib); a friend link 'F'
+ * carries the 1-based id of the neighbouring block in the value array. */
+typedef struct snac_block_desc {
+  int    ng[3];
+  double lmin[3], lmax[3];
+  int    gt[3];
+  double gr[3];
+  char   cbcvel[3][3][2];
+  double bcvel[3][3][2];
+  char   cbcpre[3][2];
+  double bcpre[3][2];
+  char   cbcscal[SNAC_MAX_SCAL][3][2];
+  double bcscal[SNAC_MAX_SCAL][3][2];
+  const double *grid_file[3];  /* optional grid/grid_?_b_###.bin: rf,rc,drf,drc over lo..hi (4*ng) */
+} snac_block_desc;
+
+/* &dns, &scalar and &hypre namelists (param.f90:342-355) plus the build flags */
+typedef struct snac_case {
+  int    nblocks;
+  double visci, cfl, dtmax, dt_f;
+  double bforce[3], gacc[3], beta;
+  int    nscal;
+  double alphai[SNAC_MAX_SCAL], ssource[SNAC_MAX_SCAL], scalf[SNAC_MAX_SCAL];
+  int    is_sforced[SNAC_MAX_SCAL];
+  int    icheck;
+  int    fft_axis;    /* 0: 3-D solve; 1,2,3: FFT_AXIS (transform along x/y/z) */
+  int    impdiff;     /* _IMPDIFF */
+  int    boussinesq;  /* _BOUSSINESQ_BUOYANCY */
+  double tol;         /* relative residual ||r||/||b|| of every solve (hypre_tol) */
+  int    maxiter;     /* iteration cap of every solve (hypre_maxiter) */
+} snac_case;
+
+/* Library options with no counterpart in the reference. */
+typedef struct snac_options {
+  int precision;      /* 0: FP64 multigrid-preconditioned CG; 1: FP32 V-cycles inside FP64 iterative refinement */
+  int use_graph;      /* 1: replay whole steps as CUDA graphs */
+  int nu;             /* smoothing sweeps before/after each coarse correction (0 = default 2) */
+  int device;         /* CUDA device ordinal */
+} snac_options;
+
+typedef struct snac_step_stats {
+  int    istep;
+  double time, dt;
+  int    solve_iters_max;     /* largest iteration count of the last step's solves */
+  double solve_residual_max;  /* largest final relative residual of the last step's solves */
+  int    solves;              /* solves run in the last step */
+} snac_step_stats;
+
+/* ---------------------------------------------------------------- errors */
+const char *snac_last_error(void);
+int snac_device_count(int *n);
+
+/* ---------------------------------------------------------------- host mirrors */
+/* Keep a device mirror of a host array of `bytes` bytes (contents uploaded). */
+int snac_register(void *host, size_t bytes);
+int snac_unregister(void *host);
+int snac_update_device(void *host);      /* host -> mirror */
+int snac_update_host(void *host);        /* mirror -> host */
+
+/* ---------------------------------------------------------------- reference-signature calls */
+/* rk.f90:7-128 (rk_mom) with mom.f90:112-386; s1 = scalars(1)%val (may be NULL unless boussinesq) */
+int snac_rk_mom(const double rkpar[2], const int lo[3], const int hi[3],
+                const double *dxc, const double *dxf, const double *dyc, const double *dyf,
+                const double *dzc, const double *dzf, double dt, const double bforce[3],
+                const double gacc[3], double beta, const double *s1, double visc,
+                double *u, double *v, double *w, const double *p,
+                double *dudtrko, double *dvdtrko, double *dwdtrko, int impdiff, int boussinesq);
+/* rk.f90:130-204 (rk_scal) with scal.f90:89-179; f receives scalf - bulk mean when is_forced */
+int snac_rk_scal(const double rkpar[2], const int lo[3], const int hi[3],
+                 const double *dxc, const double *dxf, const double *dyc, const double *dyf,
+                 const double *dzc, const double *dzf, double dt, double alpha, double vol_all,
+                 const double *u, const double *v, const double *w, int is_forced, double scalf,
+                 double ssource, double *dsdtrko, double *s, double *f, int impdiff);
+/* fillps.f90:7-54; fft_axis selects the _FFT_X/_Y/_Z weighting */
+int snac_fillps(const int lo[3], const int hi[3], const double *dxf, const double *dyf,
+                const double *dzf, double dt, const double *u, const double *v, const double *w,
+                double *p, int fft_axis);
+/* correc.f90:7-48 */
+int snac_correc(const int lo[3], const int hi[3], const double *dxc, const double *dyc,
+                const double *dzc, double dt, const double *p, double *u, double *v, double *w);
+/* updt_pressure.f90:7-47 */
+int snac_updt_pressure(const int lo[3], const int hi[3], const double *dxc, const double *dxf,
+                       const double *dyc, const double *dyf, const double *dzc, const double *dzf,
+                       double alpha, const double *pp, double *p, int impdiff);
+/* bound.f90:543-585 */
+int snac_updt_rhs(const int lo[3], const int hi[3], const int is_bound[3][2],
+                  const double *rhsx, const double *rhsy, const double *rhsz, double *p);
+/* chkdt.f90:8-56 for one block/rank; visc is the value passed by main.f90:660 (max(visc,alpha_max)) */
+int snac_chkdt(const int lo[3], const int hi[3], const double *dxc, const double *dxf,
+               const double *dyc, const double *dyf, const double *dzc, const double *dzf,
+               double visc, const double *u, const double *v, const double *w, int impdiff,
+               double *dtmax);
+/* chkdiv.f90:8-44 for one block/rank (the MPI reductions are the caller's when several blocks) */
+int snac_chkdiv(const int lo[3], const int hi[3], const double *dxf, const double *dyf,
+                const double *dzf, const double *u, const double *v, const double *w, double vol,
+                double *divtot, double *divmax);
+/* bound.f90:108-248 (set_bc) on one face of one halo'd array */
+int snac_set_bc(char ctype, int ibound, const int lo[3], const int hi[3], int idir, int centered,
+                double rvalue, double dr, double *p);
+/* fft.f90:85-94 (fft): in-place unnormalised r2r of kind along axis idir (1..3) of an
+ * interior array arr(n(1),n(2),n(3)), over the first n(idir)-q points (q = 0 or 1, fft.f90:32) */
+int snac_fft(int kind, int idir, const int n[3], int q, double *arr);
+/* fft.f90:96-149 and 151-189 */
+int snac_find_fft(const char bc[2], int is_centered, int *kind_fwd, int *kind_bwd, double norm[2]);
+int snac_eigenvalues(int n, const char bc[2], int is_centered, double *lambda);
+/* initgrid.f90:9-83: arrays over lo-1..hi+1 */
+int snac_initgrid(int lo, int hi, int gt, double gr, double lmin, double lmax,
+                  double *drc, double *drf, double *rc, double *rf);
+
+/* ---------------------------------------------------------------- domain layer */
+/* read_input + initmpi + initgrid/bound_grid + init_bc_rhs + solver set-up (main.f90:188-886) */
+int snac_init(const snac_case *c, const snac_block_desc *blocks, const snac_options *opt);
+int snac_finalize(void);
+int snac_block_geometry(int ib, int lo[3], int hi[3], int nb[3][2], int is_bound[3][2]);
+int snac_get_grid(int ib, int axis, int which, double *out);         /* (ng+2) values */
+int snac_set_field(int ib, int field, const double *host);
+int snac_get_field(int ib, int field, double *host);
+double snac_vol_all(void);
+/* the per-stage routines of main.f90:906-1043 on every block */
+int snac_rk_mom_all(int irk);                     /* rk_mom for all blocks with the current dt */
+int snac_bounduvw_all(int is_correc);             /* bound.f90:8-66 */
+int snac_boundp_all(int field);                   /* bound.f90:68-106 (SNAC_P, SNAC_PP, scalars) */
+int snac_fillps_all(double dtrk);                 /* fillps.f90 */
+int snac_updt_rhs_all(void);                      /* bound.f90:543-585 with the pressure BC planes */
+int snac_solve_pressure(void);                    /* fft + solve_n_helmholtz_2d + fft + normfft, or solve_helmholtz */
+int snac_correc_all(double dtrk);                 /* correc.f90 */
+int snac_updt_pressure_all(double alpha);         /* updt_pressure.f90 */
+int snac_chkdt_all(double *dt_cfl);               /* chkdt.f90 incl. the MPI reductions */
+int snac_chkdiv_all(double *divtot, double *divmax);
+int snac_kinetic_energy(double *ke);
+/* whole RK3 steps, main.f90:893-1069 (dt from chkdt every icheck steps) */
+int snac_step(int nsteps);
+int snac_get_stats(snac_step_stats *st);
+int snac_set_dt(double dt);
+int snac_get_dt(double *dt);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

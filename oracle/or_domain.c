@@ -1,0 +1,560 @@
+/*
+ * or_domain.c -- oracle restatement of the set-up and of one RK3 step with
+ * all blocks held by one process.  TEST INFRASTRUCTURE ONLY.
+ *
+ * The reference runs one MPI rank per block; MPI_SENDRECV halo exchanges
+ * (bound.f90:587-650) are restated as plane copies between the blocks'
+ * arrays, done direction by direction (x for every block, then y, then z)
+ * and before any physical boundary condition, which is the order the
+ * paired SENDRECVs impose.  Allreduce results are plain sums/maxima over
+ * blocks in block order.
+ */
+#include "or_internal.h"
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static const double PI = 3.14159265358979323846264338327950288;
+/* rkcoeff, param.f90:11-14 */
+static const double RKC[3][2] = {{32.0 / 60.0, 0.0}, {25.0 / 60.0, -17.0 / 60.0}, {45.0 / 60.0, -25.0 / 60.0}};
+
+void or_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+/* ---- initgrid.f90:171-287 (grid stretching functions) ---- */
+static double gp_one_end(double alpha, double r0) {
+  if (alpha != 0.0) return 1.0 * (1.0 + tanh((r0 - 1.0) * alpha) / tanh(alpha / 1.0));
+  return r0;
+}
+static double gp_geo_one_end(double alpha, double r0) {
+  const double power = 1.0 / 3.0;
+  if (r0 == 1.0) return r0;
+  return r0 * pow((1.0 - pow(r0, alpha)) / (1.0 - r0) / alpha, power);
+}
+static double gridpoint(int gt, double alpha, double r0) {
+  switch (gt) {
+    case 1: return gp_one_end(alpha, r0);
+    case 2:
+      if (alpha != 0.0) {
+        if (r0 <= 0.5) return 0.5 * (1.0 - 1.0 + tanh(2.0 * alpha * (r0 - 0.0)) / tanh(alpha));
+        return 0.5 * (1.0 + 1.0 + tanh(2.0 * alpha * (r0 - 1.0)) / tanh(alpha));
+      }
+      return r0;
+    case 3:
+      if (alpha != 0.0) return 1.0 - 1.0 * (1.0 + tanh((1.0 - r0 - 1.0) * alpha) / tanh(alpha / 1.0));
+      return r0;
+    case 4: return gp_geo_one_end(alpha, r0);
+    case 5: return 1.0 - gp_geo_one_end(alpha, 1.0 - r0);
+    case 6:
+      if (r0 <= 0.5) return gp_geo_one_end(alpha / 2.0, 2.0 * r0) / 2.0;
+      return 1.0 - gp_geo_one_end(alpha / 2.0, 2.0 * (1.0 - r0)) / 2.0;
+    case 7:
+      if (r0 <= 0.5) return (1.0 - gp_geo_one_end(alpha / 2.0, (0.5 - r0) * 2.0)) / 2.0;
+      return (1.0 + gp_geo_one_end(alpha / 2.0, (r0 - 0.5) * 2.0)) / 2.0;
+    default: /* 0: cluster_two_end, initgrid.f90:171-184 */
+      if (alpha != 0.0) return 0.5 * (1.0 + tanh((r0 - 0.5) * alpha) / tanh(alpha / 2.0));
+      return r0;
+  }
+}
+
+/* initgrid.f90:9-83; arrays hold lo-1..hi+1 */
+void or_initgrid(int lo, int hi, int gt, double gr, double lmin, double lmax,
+                 double *drc, double *drf, double *rc, double *rf) {
+#define AT(a, q) (a)[(q) - lo + 1]
+  int n = hi - lo + 1;
+  for (int q = lo; q <= hi; q++) {
+    double r0 = ((double)(q - lo + 1) - 0.0) / (1.0 * n);
+    AT(rf, q) = gridpoint(gt, gr, r0);
+    AT(rf, q) = lmin + AT(rf, q) * (lmax - lmin);
+  }
+  AT(rf, lo - 1) = lmin;
+  for (int q = lo; q <= hi; q++) AT(drf, q) = AT(rf, q) - AT(rf, q - 1);
+  AT(drf, lo - 1) = AT(drf, lo);
+  AT(drf, hi + 1) = AT(drf, hi);
+  for (int q = lo - 1; q <= hi; q++) AT(drc, q) = 0.5 * (AT(drf, q) + AT(drf, q + 1));
+  AT(drc, hi + 1) = AT(drc, hi);
+  AT(rc, lo - 1) = lmin - AT(drc, lo - 1) / 2.0;
+  AT(rf, lo - 1) = lmin;
+  for (int q = lo; q <= hi + 1; q++) {
+    AT(rc, q) = AT(rc, q - 1) + AT(drc, q - 1);
+    AT(rf, q) = AT(rf, q - 1) + AT(drf, q);
+  }
+#undef AT
+}
+
+/* initgrid.f90:144-165 (load_grid): file = rf,rc,drf,drc over lo..hi */
+static void load_grid(int lo, int hi, const double *file, double *rf, double *rc, double *drf, double *drc) {
+#define AT(a, q) (a)[(q) - lo + 1]
+  int n = hi - lo + 1;
+  for (int q = lo; q <= hi; q++) {
+    AT(rf, q) = file[q - lo];
+    AT(rc, q) = file[n + q - lo];
+    AT(drf, q) = file[2 * n + q - lo];
+    AT(drc, q) = file[3 * n + q - lo];
+  }
+  AT(drf, lo - 1) = AT(drf, lo);
+  AT(drf, hi + 1) = AT(drf, hi);
+  AT(drc, lo - 1) = AT(drf, lo);
+  AT(drc, hi + 1) = AT(drc, hi);
+  AT(rf, lo - 1) = AT(rf, lo) - AT(drf, lo);
+  AT(rf, hi + 1) = AT(rf, hi) + AT(drf, hi);
+  AT(rc, lo - 1) = AT(rc, lo) - AT(drc, lo - 1);
+  AT(rc, hi + 1) = AT(rc, hi) + AT(drc, hi);
+#undef AT
+}
+
+/* initmpi.f90:50-98: breadth-first placement of the blocks in a global index space */
+int or_place_blocks(int nblocks, const or_block_desc *bl, int (*lo)[3]) {
+  int *done = calloc(nblocks, sizeof(int)), *unl = calloc(nblocks, sizeof(int));
+  int iblock = 0, rc = 0;
+  for (int a = 0; a < 3; a++) lo[0][a] = 1;
+  unl[0] = 1;
+  for (;;) {
+    int all = 1;
+    for (int q = 0; q < nblocks; q++) if (!done[q]) all = 0;
+    if (all) break;
+    if (iblock < 0 || iblock >= nblocks) { rc = -1; break; }
+    for (int idir = 0; idir < 3; idir++) {
+      for (int inb = 0; inb < 2; inb++) {
+        if (bl[iblock].cbcpre[idir][inb] != 'F') continue;
+        int ifr = (int)lround(bl[iblock].bcpre[idir][inb]) - 1;
+        if (ifr < 0 || ifr >= nblocks) { rc = -2; goto out; }
+        if (unl[ifr]) continue;
+        if (inb == 0 && bl[ifr].lmin[idir] > bl[iblock].lmin[idir]) continue;
+        if (inb == 1 && bl[ifr].lmin[idir] < bl[iblock].lmin[idir]) continue;
+        int ioff = -(1 - inb) * bl[ifr].ng[idir] + inb * bl[iblock].ng[idir];
+        lo[ifr][idir] = lo[iblock][idir] + ioff;
+        for (int t = 0; t < 3; t++) if (t != idir) lo[ifr][t] = lo[iblock][t];
+        unl[ifr] = 1;
+      }
+    }
+    done[iblock] = 1;
+    iblock = -1;
+    for (int q = 0; q < nblocks; q++) if (!done[q] && unl[q]) { iblock = q; break; }
+  }
+out:
+  free(done); free(unl);
+  return rc;
+}
+
+static double *fld_alloc(const or_block *B, int halo) {
+  size_t n = halo ? (size_t)(B->ng[0] + 2) * (B->ng[1] + 2) * (B->ng[2] + 2) : (size_t)B->ng[0] * B->ng[1] * B->ng[2];
+  return calloc(n, sizeof(double));
+}
+
+or_domain *or_create(const or_case *c, const or_block_desc *blocks, char *err, int errlen) {
+  or_domain *d = calloc(1, sizeof(or_domain));
+  d->c = *c;
+  d->nblocks = c->nblocks;
+  d->b = calloc(d->nblocks, sizeof(or_block));
+  int (*lo)[3] = calloc(d->nblocks, sizeof(int[3]));
+  if (or_place_blocks(d->nblocks, blocks, lo)) { snprintf(err, errlen, "invalid block connectivity"); goto fail; }
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    B->desc = blocks[ib];
+    for (int a = 0; a < 3; a++) {
+      B->ng[a] = blocks[ib].ng[a];
+      B->lo[a] = lo[ib][a];
+      B->hi[a] = lo[ib][a] + B->ng[a] - 1;
+    }
+  }
+  /* param.f90:460-487 (is_periodic) and initmpi.f90:107-113 (periods) */
+  for (int q = 0; q < 3; q++) {
+    d->is_periodic[q] = 1;
+    int lmn = d->b[0].lo[q], hmx = d->b[0].hi[q];
+    for (int ib = 0; ib < d->nblocks; ib++) {
+      if (!(blocks[ib].cbcpre[q][0] == 'F' && blocks[ib].cbcpre[q][1] == 'F')) d->is_periodic[q] = 0;
+      if (d->b[ib].lo[q] < lmn) lmn = d->b[ib].lo[q];
+      if (d->b[ib].hi[q] > hmx) hmx = d->b[ib].hi[q];
+    }
+    d->periods[q] = d->is_periodic[q] ? hmx - lmn + 1 : 0;
+  }
+  /* neighbours (initmpi.f90:150-237, one rank per block) */
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    for (int q = 0; q < 3; q++)
+      for (int s = 0; s < 2; s++) {
+        B->nb[q][s] = -1;
+        if (blocks[ib].cbcpre[q][s] == 'F') {
+          int f = (int)lround(blocks[ib].bcpre[q][s]) - 1;
+          if (f < 0 || f >= d->nblocks) { snprintf(err, errlen, "block %d: friend %d does not exist", ib + 1, f + 1); goto fail; }
+          or_block *Fb = &d->b[f];
+          int ok = blocks[f].cbcpre[q][1 - s] == 'F' && (int)lround(blocks[f].bcpre[q][1 - s]) - 1 == ib;
+          for (int t = 0; t < 3; t++)
+            if (t != q) ok = ok && Fb->lo[t] == B->lo[t] && Fb->hi[t] == B->hi[t] &&
+                              blocks[f].lmin[t] == blocks[ib].lmin[t] && blocks[f].lmax[t] == blocks[ib].lmax[t] &&
+                              blocks[f].gr[t] == blocks[ib].gr[t] && blocks[f].gt[t] == blocks[ib].gt[t];
+          /* adjacency in the global index space, directly or through the periodic wrap */
+          if (s == 0) ok = ok && (Fb->hi[q] + 1 == B->lo[q] || (d->periods[q] && Fb->hi[q] - B->lo[q] + 1 == d->periods[q]));
+          else ok = ok && (B->hi[q] + 1 == Fb->lo[q] || (d->periods[q] && B->hi[q] - Fb->lo[q] + 1 == d->periods[q]));
+          if (!ok) { snprintf(err, errlen, "block %d: inconsistent connectivity with block %d", ib + 1, f + 1); goto fail; }
+          B->nb[q][s] = f;
+        }
+        B->is_bound[q][s] = B->nb[q][s] < 0;
+      }
+  }
+  /* grids: initgrid.f90:9-83, optional load_grid, distribute_grid, bound_grid (initgrid.f90:91-127) */
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    for (int a = 0; a < 3; a++) {
+      int n2 = B->ng[a] + 2;
+      for (int w = 0; w < 4; w++) B->g[a][w] = calloc(n2, sizeof(double));
+      or_initgrid(B->lo[a], B->hi[a], blocks[ib].gt[a], blocks[ib].gr[a], blocks[ib].lmin[a], blocks[ib].lmax[a],
+                  B->g[a][OR_G_DXC], B->g[a][OR_G_DXF], B->g[a][OR_G_XC], B->g[a][OR_G_XF]);
+      if (blocks[ib].grid_file[a])
+        load_grid(B->lo[a], B->hi[a], blocks[ib].grid_file[a], B->g[a][OR_G_XF], B->g[a][OR_G_XC], B->g[a][OR_G_DXF], B->g[a][OR_G_DXC]);
+    }
+  }
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    for (int a = 0; a < 3; a++) {
+      int n = B->ng[a];
+      double *df = B->g[a][OR_G_DXF], *dc = B->g[a][OR_G_DXC];
+      if (B->nb[a][0] >= 0) { or_block *N = &d->b[B->nb[a][0]]; df[0] = N->g[a][OR_G_DXF][N->ng[a]]; }
+      if (B->nb[a][1] >= 0) { or_block *N = &d->b[B->nb[a][1]]; df[n + 1] = N->g[a][OR_G_DXF][1]; }
+    }
+  }
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    for (int a = 0; a < 3; a++) {
+      int n = B->ng[a];
+      double *df = B->g[a][OR_G_DXF], *dc = B->g[a][OR_G_DXC];
+      dc[0] = (df[1] + df[0]) / 2.0;
+      dc[n] = (df[n + 1] + df[n]) / 2.0;
+      dc[n + 1] = dc[n];
+    }
+  }
+  /* vol_all, param.f90:493-494 */
+  d->vol_all = 0.0;
+  for (int ib = 0; ib < d->nblocks; ib++)
+    d->vol_all += (blocks[ib].lmax[0] - blocks[ib].lmin[0]) * (blocks[ib].lmax[1] - blocks[ib].lmin[1]) *
+                  (blocks[ib].lmax[2] - blocks[ib].lmin[2]);
+  /* fields */
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    for (int f = OR_U; f <= OR_PO; f++) B->fld[f] = fld_alloc(B, 1);
+    for (int f = OR_DUDTRKO; f <= OR_DWDTRKO; f++) B->fld[f] = fld_alloc(B, 0);
+    for (int s = 0; s < c->nscal; s++) { B->fld[OR_S0 + s] = fld_alloc(B, 1); B->fld[OR_DSDTRKO0 + s] = fld_alloc(B, 0); }
+    B->rhsp[0] = calloc((size_t)B->ng[1] * B->ng[2] * 2, sizeof(double));
+    B->rhsp[1] = calloc((size_t)B->ng[0] * B->ng[2] * 2, sizeof(double));
+    B->rhsp[2] = calloc((size_t)B->ng[0] * B->ng[1] * 2, sizeof(double));
+  }
+  /* pressure BC rhs, main.f90:725-731 (dl from the global grid, is_centered = T) */
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    double dl[3][2];
+    int cen[3] = {1, 1, 1};
+    for (int a = 0; a < 3; a++) {
+      double *drc = calloc(B->ng[a] + 2, sizeof(double)), *drf = calloc(B->ng[a] + 2, sizeof(double)),
+             *rc = calloc(B->ng[a] + 2, sizeof(double)), *rf = calloc(B->ng[a] + 2, sizeof(double));
+      or_initgrid(B->lo[a], B->hi[a], blocks[ib].gt[a], blocks[ib].gr[a], blocks[ib].lmin[a], blocks[ib].lmax[a], drc, drf, rc, rf);
+      if (blocks[ib].grid_file[a]) load_grid(B->lo[a], B->hi[a], blocks[ib].grid_file[a], rf, rc, drf, drc);
+      dl[a][0] = drc[0];
+      dl[a][1] = drc[B->ng[a]];
+      free(drc); free(drf); free(rc); free(rf);
+    }
+    or_init_bc_rhs(blocks[ib].cbcpre, blocks[ib].bcpre, (const double(*)[2])dl, (const int(*)[2])B->is_bound, cen,
+                   B->lo, B->hi, d->periods, B->g[0][0], B->g[0][1], B->g[1][0], B->g[1][1], B->g[2][0], B->g[2][1],
+                   B->rhsp[0], B->rhsp[1], B->rhsp[2], NULL, NULL, NULL, c->fft_axis);
+    if (ib == 0) {
+      d->fft_axis = c->fft_axis;
+      if (c->fft_axis) {
+        int idir = c->fft_axis - 1;
+        d->il = idir == 0 ? 1 : 0;
+        d->iu = idir == 2 ? 1 : 2;
+        int n = B->ng[idir];
+        double norm[2];
+        or_find_fft(blocks[0].cbcpre[idir], 1, &d->kind_fwd, &d->kind_bwd, norm);
+        if (d->kind_fwd < 0) { snprintf(err, errlen, "unsupported boundary pair along the transform direction"); goto fail; }
+        d->normfft = 1.0 / (norm[0] * (n + norm[1] - 0));
+        d->lambda = calloc(n, sizeof(double));
+        if (or_eigenvalues(n, blocks[0].cbcpre[idir], 1, d->lambda)) { snprintf(err, errlen, "no eigenvalues for this boundary pair"); goto fail; }
+        for (int l = 0; l < n; l++) d->lambda[l] = d->lambda[l] / (dl[idir][0] * dl[idir][0]);
+      }
+    }
+  }
+  {
+    int cen[3] = {1, 1, 1};
+    d->ps = or_poisson_create(d, cen, 0.0, d->lambda, err, errlen);
+    if (!d->ps) goto fail;
+    long nbox = d->ps->L[0].ncell * d->ps->nsys;
+    d->box_b = calloc(nbox, sizeof(double));
+    d->box_x = calloc(nbox, sizeof(double));
+  }
+  d->dt = 0.0;
+  free(lo);
+  return d;
+fail:
+  free(lo);
+  or_destroy(d);
+  return NULL;
+}
+
+void or_destroy(or_domain *d) {
+  if (!d) return;
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    for (int a = 0; a < 3; a++) for (int w = 0; w < 4; w++) free(B->g[a][w]);
+    for (int f = 0; f < OR_NFIELDS; f++) free(B->fld[f]);
+    for (int a = 0; a < 3; a++) free(B->rhsp[a]);
+  }
+  free(d->b);
+  free(d->lambda);
+  or_poisson_destroy(d->ps);
+  free(d->box_b); free(d->box_x);
+  free(d);
+}
+
+int or_block_geometry(const or_domain *d, int ib, int lo[3], int hi[3], int nb[3][2], int is_bound[3][2]) {
+  if (ib < 0 || ib >= d->nblocks) return -1;
+  const or_block *B = &d->b[ib];
+  for (int a = 0; a < 3; a++) {
+    lo[a] = B->lo[a]; hi[a] = B->hi[a];
+    for (int s = 0; s < 2; s++) { nb[a][s] = B->nb[a][s]; is_bound[a][s] = B->is_bound[a][s]; }
+  }
+  return 0;
+}
+double *or_field(or_domain *d, int ib, int kind) { return (ib >= 0 && ib < d->nblocks && kind >= 0 && kind < OR_NFIELDS) ? d->b[ib].fld[kind] : NULL; }
+double *or_grid(or_domain *d, int ib, int axis, int which) { return d->b[ib].g[axis][which]; }
+double or_vol_all(const or_domain *d) { return d->vol_all; }
+double or_dt(const or_domain *d) { return d->dt; }
+void or_set_dt(or_domain *d, double dt) { d->dt = dt; }
+int or_istep(const or_domain *d) { return d->istep; }
+double or_time(const or_domain *d) { return d->time; }
+int or_last_iterations(const or_domain *d) { return d->ps ? d->ps->last_iter : 0; }
+double or_last_residual(const or_domain *d) { return d->ps ? d->ps->last_res : 0.0; }
+
+/* ---- halo exchange: the MPI_SENDRECV pairs of bound.f90:587-650 as copies ---- */
+static void exchange_dir(or_domain *d, int kind, int a) {
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    long st[3] = {1, B->ng[0] + 2, (long)(B->ng[0] + 2) * (B->ng[1] + 2)};
+    int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+    for (int s = 0; s < 2; s++) {
+      int f = B->nb[a][s];
+      if (f < 0) continue;
+      or_block *N = &d->b[f];
+      long sn[3] = {1, N->ng[0] + 2, (long)(N->ng[0] + 2) * (N->ng[1] + 2)};
+      int dst = s ? B->ng[a] + 1 : 0;  /* ghost plane hi+1 (s=1) or lo-1 (s=0) */
+      int src = s ? 1 : N->ng[a];      /* friend's plane lo (s=1) or hi (s=0) */
+      for (int y = 0; y < B->ng[t2] + 2; y++)
+        for (int x = 0; x < B->ng[t1] + 2; x++)
+          B->fld[kind][dst * st[a] + x * st[t1] + y * st[t2]] = N->fld[kind][src * sn[a] + x * sn[t1] + y * sn[t2]];
+    }
+  }
+}
+
+/* bound.f90:8-66 */
+void or_bounduvw(or_domain *d, int is_correc) {
+  for (int comp = 0; comp < 3; comp++)
+    for (int a = 0; a < 3; a++) exchange_dir(d, OR_U + comp, a);
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    for (int a = 0; a < 3; a++)
+      for (int s = 0; s < 2; s++) {
+        if (!B->is_bound[a][s]) continue;
+        for (int comp = 0; comp < 3; comp++) {
+          int centered = comp != a;
+          if (!centered && is_correc) continue;
+          const double *dr = centered ? B->g[a][OR_G_DXC] : B->g[a][OR_G_DXF];
+          double drv = s ? dr[B->ng[a]] : dr[0];
+          or_set_bc(B->desc.cbcvel[comp][a][s], s, B->lo, B->hi, a + 1, centered, B->desc.bcvel[comp][a][s], drv,
+                    B->fld[OR_U + comp]);
+        }
+      }
+  }
+}
+
+/* bound.f90:68-106; scalars use their own cbc/bc (main.f90:936) */
+void or_boundp(or_domain *d, int kind) {
+  for (int a = 0; a < 3; a++) exchange_dir(d, kind, a);
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    for (int a = 0; a < 3; a++)
+      for (int s = 0; s < 2; s++) {
+        if (!B->is_bound[a][s]) continue;
+        char cb; double bv;
+        if (kind >= OR_S0 && kind <= OR_S3) { cb = B->desc.cbcscal[kind - OR_S0][a][s]; bv = B->desc.bcscal[kind - OR_S0][a][s]; }
+        else { cb = B->desc.cbcpre[a][s]; bv = B->desc.bcpre[a][s]; }
+        double drv = s ? B->g[a][OR_G_DXC][B->ng[a]] : B->g[a][OR_G_DXC][0];
+        or_set_bc(cb, s, B->lo, B->hi, a + 1, 1, bv, drv, B->fld[kind]);
+      }
+  }
+}
+
+void or_fillps_all(or_domain *d, double dtrk) {
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    or_fillps(B->lo, B->hi, B->g[0][1], B->g[1][1], B->g[2][1], dtrk, B->fld[OR_U], B->fld[OR_V], B->fld[OR_W],
+              B->fld[OR_PP], d->fft_axis);
+  }
+}
+
+void or_updt_rhs_all(or_domain *d) {
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    or_updt_rhs(B->lo, B->hi, (const int(*)[2])B->is_bound, B->rhsp[0], B->rhsp[1], B->rhsp[2], B->fld[OR_PP]);
+  }
+}
+
+/* transform the interior of pp of every block along the FFT axis (fft.f90:85-94) */
+static void transform_blocks(or_domain *d, int kind) {
+  int idir = d->fft_axis - 1;
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    int n[3] = {B->ng[0], B->ng[1], B->ng[2]};
+    long st[3] = {1, n[0] + 2, (long)(n[0] + 2) * (n[1] + 2)};
+    double *f = B->fld[OR_PP];
+    int t1 = idir == 0 ? 1 : 0, t2 = idir == 2 ? 1 : 2;
+    int nl = n[idir];
+#pragma omp parallel
+    {
+      double *in = malloc(sizeof(double) * nl), *out = malloc(sizeof(double) * nl);
+#pragma omp for collapse(2)
+      for (int y = 1; y <= n[t2]; y++)
+        for (int x = 1; x <= n[t1]; x++) {
+          long base = x * st[t1] + y * st[t2];
+          for (int q = 0; q < nl; q++) in[q] = f[base + (q + 1) * st[idir]];
+          or_r2r(kind, nl, in, out);
+          for (int q = 0; q < nl; q++) f[base + (q + 1) * st[idir]] = out[q];
+        }
+      free(in); free(out);
+    }
+  }
+}
+
+/* main.f90:1004-1022: transform, per-wavenumber (or 3-D) solves warm-started from po, back-transform + normfft */
+int or_solve_pressure(or_domain *d) {
+  if (d->fft_axis) transform_blocks(d, d->kind_fwd);
+  or_box_gather(d, d->ps, OR_PP, d->box_b);
+  int rc = or_poisson_solve(d->ps, d->box_b, d->box_x);
+  or_box_scatter(d, d->ps, d->box_x, OR_PP);
+  if (d->fft_axis) {
+    transform_blocks(d, d->kind_bwd);
+    for (int ib = 0; ib < d->nblocks; ib++) {
+      or_block *B = &d->b[ib];
+      int nx = B->ng[0], ny = B->ng[1];
+      for (int k = 1; k <= B->ng[2]; k++)
+        for (int j = 1; j <= ny; j++)
+          for (int i = 1; i <= nx; i++) B->fld[OR_PP][i + (long)(nx + 2) * (j + (long)(ny + 2) * k)] *= d->normfft;
+    }
+  }
+  return rc;
+}
+
+void or_correc_all(or_domain *d, double dtrk) {
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    or_correc(B->lo, B->hi, B->g[0][0], B->g[1][0], B->g[2][0], dtrk, B->fld[OR_PP], B->fld[OR_U], B->fld[OR_V], B->fld[OR_W]);
+  }
+}
+
+void or_updt_pressure_all(or_domain *d, double alpha) {
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    or_updt_pressure(B->lo, B->hi, B->g[0][0], B->g[0][1], B->g[1][0], B->g[1][1], B->g[2][0], B->g[2][1], alpha,
+                     B->fld[OR_PP], B->fld[OR_P], d->c.impdiff);
+  }
+}
+
+/* chkdt.f90:8-56 with the MPI reductions over blocks; max(visc, alpha_max) as main.f90:660 */
+double or_chkdt(or_domain *d) {
+  double dti = 0.0, dlmin = 1e300;
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    double t, m;
+    or_chkdt_local(B->lo, B->hi, B->g[0][0], B->g[0][1], B->g[1][0], B->g[1][1], B->g[2][0], B->g[2][1],
+                   B->fld[OR_U], B->fld[OR_V], B->fld[OR_W], &t, &m);
+    if (t > dti) dti = t;
+    if (m < dlmin) dlmin = m;
+  }
+  if (dti == 0.0) dti = 1.0;
+  double dtmax = sqrt(3.0) / dti;
+  if (!d->c.impdiff) {
+    double visc = 1.0 / d->c.visci, amax = 0.0;
+    for (int s = 0; s < d->c.nscal; s++) { double a = 1.0 / d->c.alphai[s]; if (a > amax) amax = a; }
+    double ve = visc > amax ? visc : amax;
+    double lim = 1.65 / 12.0 / ve * (dlmin * dlmin);
+    if (lim < dtmax) dtmax = lim;
+  }
+  return dtmax;
+}
+
+void or_chkdiv(or_domain *d, double *divtot, double *divmax) {
+  double tot = 0.0, mx = 0.0;
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    double t, m;
+    or_chkdiv_local(B->lo, B->hi, B->g[0][1], B->g[1][1], B->g[2][1], B->fld[OR_U], B->fld[OR_V], B->fld[OR_W],
+                    d->vol_all, &t, &m);
+    tot += t;
+    if (m > mx) mx = m;
+  }
+  *divtot = tot;
+  *divmax = mx;
+}
+
+/* kinetic energy 0.5*sum(u^2 dxc dyf dzf + v^2 dxf dyc dzf + w^2 dxf dyf dzc)/vol over interior faces */
+double or_kinetic_energy(or_domain *d) {
+  double ke = 0.0;
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    int nx = B->ng[0], ny = B->ng[1];
+    double *dxc = B->g[0][0], *dxf = B->g[0][1], *dyc = B->g[1][0], *dyf = B->g[1][1], *dzc = B->g[2][0], *dzf = B->g[2][1];
+    for (int k = 1; k <= B->ng[2]; k++)
+      for (int j = 1; j <= ny; j++)
+        for (int i = 1; i <= nx; i++) {
+          long c = i + (long)(nx + 2) * (j + (long)(ny + 2) * k);
+          double u = B->fld[OR_U][c], v = B->fld[OR_V][c], w = B->fld[OR_W][c];
+          ke += u * u * dxc[i] * dyf[j] * dzf[k] + v * v * dxf[i] * dyc[j] * dzf[k] + w * w * dxf[i] * dyf[j] * dzc[k];
+        }
+  }
+  return 0.5 * ke / d->vol_all;
+}
+
+static void set_dt_from_cfl(or_domain *d) {
+  double dt_cfl = or_chkdt(d);
+  d->dt = d->c.dt_f > 0.0 ? d->c.dt_f : (d->c.cfl * dt_cfl < d->c.dtmax ? d->c.cfl * dt_cfl : d->c.dtmax);
+}
+
+/* main.f90:893-1069 for the explicit-diffusion path (no scalars, no IMPDIFF) */
+int or_step(or_domain *d, int nsteps) {
+  if (d->c.impdiff || d->c.nscal > 0) return -10; /* not restated in the oracle driver */
+  if (d->dt == 0.0) set_dt_from_cfl(d);          /* main.f90:660-661 */
+  double visc = 1.0 / d->c.visci;
+  int rc = 0;
+  for (int st = 0; st < nsteps; st++) {
+    d->istep++;
+    d->time += d->dt;
+    for (int irk = 0; irk < 3; irk++) {
+      double dtrk = (RKC[irk][0] + RKC[irk][1]) * d->dt;
+      double alpha = -visc * dtrk / 2.0;
+      for (int ib = 0; ib < d->nblocks; ib++) {
+        or_block *B = &d->b[ib];
+        or_rk_mom(RKC[irk], B->lo, B->hi, B->g[0][0], B->g[0][1], B->g[1][0], B->g[1][1], B->g[2][0], B->g[2][1],
+                  d->dt, d->c.bforce, d->c.gacc, d->c.beta, NULL, visc, B->fld[OR_U], B->fld[OR_V], B->fld[OR_W],
+                  B->fld[OR_P], B->fld[OR_DUDTRKO], B->fld[OR_DVDTRKO], B->fld[OR_DWDTRKO], 0, 0);
+      }
+      or_bounduvw(d, 0);
+      or_fillps_all(d, dtrk);
+      or_updt_rhs_all(d);
+      rc |= or_solve_pressure(d);
+      or_boundp(d, OR_PP);
+      or_correc_all(d, dtrk);
+      or_bounduvw(d, 1);
+      or_updt_pressure_all(d, alpha);
+      or_boundp(d, OR_P);
+    }
+    if (d->c.icheck > 0 && d->istep % d->c.icheck == 0) set_dt_from_cfl(d); /* main.f90:1048-1053 */
+  }
+  return rc;
+}

@@ -1,0 +1,106 @@
+// snac_internal.h -- shared device structures of snac_gb300 (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <array>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "snac_gpu.h"
+
+namespace snac {
+
+void set_error(const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+#define SNAC_CUDA(x)                                                      \
+  do {                                                                    \
+    cudaError_t e_ = (x);                                                 \
+    if (e_ != cudaSuccess) return snac::cuda_fail(e_, #x, __FILE__, __LINE__); \
+  } while (0)
+#define SNAC_TRY(x)                  \
+  do {                               \
+    int r_ = (x);                    \
+    if (r_ != SNAC_OK) return r_;    \
+  } while (0)
+
+// Per-axis stencil coefficients, all (n+2) long, element q+1 holds index q (q = -1..n).
+// The reference divides by the spacings in every cell (mom.f90, scal.f90); here
+// the divisions are hoisted into these 1-D tables so the FP64 pipe only sees
+// adds and FMAs in the 3-D loops.
+enum AxisArr {
+  AX_DC = 0,  // d?c (centre-to-centre spacing)
+  AX_DF,      // d?f (face-to-face spacing)
+  AX_RC,      // 1/dc
+  AX_RF,      // 1/df
+  AX_A,       // 0.25/dc
+  AX_E0,      // 0.25*df(q)/dc(q)
+  AX_E1,      // 0.25*df(q+1)/dc(q)
+  AX_SP,      // 1/(dc(q)*df(q+1))   staggered-component diffusion, + side
+  AX_SM,      // 1/(dc(q)*df(q))     staggered-component diffusion, - side
+  AX_CP,      // 1/(df(q)*dc(q))     centred-component diffusion, + side
+  AX_CM,      // 1/(df(q)*dc(q-1))   centred-component diffusion, - side
+  AX_NARR
+};
+
+struct DBlock {
+  int n[3];                    // interior extents
+  int lo[3];                   // global lower bounds (initmpi placement)
+  double *u, *v, *w, *p, *pp;  // halo'd (n+2)^3 arrays
+  double *s[SNAC_MAX_SCAL];    // halo'd scalars
+  double *ru, *rv, *rw;        // RK storage dudtrko.. (interior)
+  double *rs[SNAC_MAX_SCAL];   // dsdtrko (interior)
+  double *nu, *nv, *nw;        // interior scratch: new velocity of a stage before write-back
+  double *ns;                  // interior scratch for scalars
+  const double *ax[3];         // AxisArr tables per axis: ax[a][AX_*(n+2) + q + 1]
+};
+
+__host__ __device__ inline long hidx(int i, int j, int k, int nx, int ny) {
+  return (long)(i + 1) + (long)(nx + 2) * ((long)(j + 1) + (long)(ny + 2) * (long)(k + 1));
+}
+__host__ __device__ inline long iidx(int i, int j, int k, int nx, int ny) {
+  return (long)i + (long)nx * ((long)j + (long)ny * (long)k);
+}
+__device__ inline double AX(const DBlock &B, int a, int which, int q) {
+  return B.ax[a][which * (B.n[a] + 2) + q + 1];
+}
+
+// a tile of one block: x = block, y,z,w = i0,j0,k0 (0-based interior)
+typedef int4 Tile;
+
+struct RkMomParams {
+  double f1, f2, f12;
+  double bforce[3];
+  double gb[3];       // f12*gacc*beta*0.5 (Boussinesq)
+  double visc;
+  int impdiff, boussinesq;
+};
+
+struct RkScalParams {
+  double f1, f2, f12, alpha, ssource;
+  int impdiff, sidx;
+};
+
+// kernel launchers (k_stencil.cu)
+int launch_rk_mom(const DBlock *dB, const Tile *dT, int ntiles, const RkMomParams &prm, cudaStream_t st);
+int launch_rk_mom_writeback(const DBlock *dB, const Tile *dT, int ntiles, cudaStream_t st);
+int launch_rk_scal(const DBlock *dB, const Tile *dT, int ntiles, const RkScalParams &prm, cudaStream_t st);
+int launch_rk_scal_writeback(const DBlock *dB, const Tile *dT, int ntiles, int sidx, cudaStream_t st);
+int launch_fillps(const DBlock *dB, const Tile *dT, int ntiles, double dt, int fft_axis, cudaStream_t st);
+int launch_correc(const DBlock *dB, const Tile *dT, int ntiles, double dt, cudaStream_t st);
+int launch_updt_pressure(const DBlock *dB, const Tile *dT, int ntiles, double alpha, int impdiff, cudaStream_t st);
+// reductions: per-tile partials written to `part` (2 doubles per tile), then a fixed-order final pass
+int launch_chkdt_partial(const DBlock *dB, const Tile *dT, int ntiles, double *part, cudaStream_t st);
+int launch_chkdiv_partial(const DBlock *dB, const Tile *dT, int ntiles, double vol, double *part, cudaStream_t st);
+int launch_ke_partial(const DBlock *dB, const Tile *dT, int ntiles, double *part, cudaStream_t st);
+int launch_bulk_partial(const DBlock *dB, const Tile *dT, int ntiles, int sidx, double *part, cudaStream_t st);
+int launch_updt_rhs(int nx, int ny, int nz, const int isb[6], const double *rx, const double *ry, const double *rz,
+                    double *p, cudaStream_t st);
+int launch_reduce_final(const double *part, int ntiles, double *out, cudaStream_t st);  // out[0]=sum part[2t], out[1]=max part[2t+1]
+
+// tile shape of the stencil kernels
+constexpr int TX = 32, TY = 4, TZ = 2;
+std::vector<Tile> make_tiles(const std::vector<std::array<int, 3>> &sizes, int tx, int ty, int tz);
+
+}  // namespace snac
