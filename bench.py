@@ -1,0 +1,316 @@
+"""Benchmark: ms per RK3 step and Mcells/s of the four-block turbulent channel on one GB300.
+
+Workload (the configuration the headline metric is quoted on): four uneven blocks
+(x: 96|160, y: 64|80, z: 128) tiling 256x144x128 = 4.72M cells on a
+4pi x 2 x 4pi/3 box, periodic x and z through friend links, no-slip walls in y
+with a global tanh-stretched wall-normal grid (alpha = 1.8), Re_tau = 180,
+FFT along z, every Poisson solve to a relative residual of 1e-12.  Initial
+field: laminar Poiseuille profile scaled to U_b plus seeded uniform noise of
+0.1 U_b (synthetic; the reference publishes no dataset for this case).
+
+A "step" is one full RK3 step (3 stages: momentum, halo/BC, divergence,
+transform, 128 batched 2-D solves, back-transform, projection, pressure
+update; chkdt every icheck=10 steps).  `value` is the mixed path (FP32 V-cycles
+inside FP64 refinement), the plain FP64 path is reported beside it at the same
+solver tolerance.  Inputs (~0.5 GB of fields + solver vectors) exceed L2.
+
+--impl reference times the CPU restatement of the reference (the Fortran/HYPRE
+reference cannot be built on these machines) on the host cores, same case.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms per RK3 step & Mcells/s on 1 GB300, learned+mixed vs plain, equal |div u|"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+        self.th = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.th = threading.Thread(target=self._read, daemon=True)
+        self.th.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.th:
+            self.th.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for q, n in enumerate(names):
+                if len(r) > 5 + q and r[5 + q].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def init_channel(dom, case):
+    from snac_gb300 import capi, cases
+    ic = cases.channel_initial_condition(case, lambda ib: dom.grid(ib, 1, capi.G_XC))
+    for ib, (u, v, w) in ic.items():
+        dom.set(ib, capi.U, u)
+        dom.set(ib, capi.V, v)
+        dom.set(ib, capi.W, w)
+    dom.bounduvw(False)
+    dom.boundp(capi.P)
+
+
+# algorithmic bytes / FP64 flops per cell and launch of the profiled kernels (FP64 state)
+KERNEL_WORK = {
+    # kid: (name, bytes per cell, flops per cell, cells-per-launch key)
+    1: ("k_rk_mom", 104.0, 180.0, "cells"),
+    4: ("k_fft_fwd_box", 16.0, 22.0, "cells"),
+    2: ("k_rbgs<float>", 12.0, 0.0, "cells"),
+}
+
+
+def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0):
+    from snac_gb300 import capi
+    from snac_gb300.domain import Domain
+    case = case_fn()
+    dom = Domain(case, precision=precision, device=device)
+    try:
+        init_channel(dom, case)
+        dom.step(warmup, allow_not_converged=True)
+        L = capi.lib()
+        if profile_kid:
+            capi.check(L.snac_profile_kernel(profile_kid))
+        rc = dom.step(steps, allow_not_converged=True)
+        st = dom.stats()
+        prof = None
+        if profile_kid:
+            n = C.c_int(); tot = C.c_double()
+            capi.check(L.snac_profile_read(C.byref(n), C.byref(tot)))
+            capi.check(L.snac_profile_kernel(0))
+            prof = (n.value, tot.value)
+        divtot, divmax = dom.chkdiv()
+        ke = dom.kinetic_energy()
+        return dict(ms=st["device_ms"] / steps, iters=st["iters"], residual=st["residual"], divmax=divmax, ke=ke,
+                    rc=rc, prof=prof, ncell=case.ncell, dt=st["dt"])
+    finally:
+        dom.close()
+
+
+def run_e2e(case_fn, precision, steps, device):
+    """Through the C ABI with host buffers: upload u,v,w,p from pinned host memory, one step, read them back."""
+    import torch
+    from snac_gb300 import capi
+    from snac_gb300.domain import Domain
+    case = case_fn()
+    dom = Domain(case, precision=precision, device=device)
+    try:
+        init_channel(dom, case)
+        dom.step(1, allow_not_converged=True)
+        host = {}
+        for ib in range(dom.nblocks):
+            for k in (capi.U, capi.V, capi.W, capi.P):
+                shp = dom.shape(ib, k)
+                t = torch.empty(int(np.prod(shp)), dtype=torch.float64, pin_memory=True)
+                a = t.numpy().reshape(shp, order="F")
+                a[...] = dom.get(ib, k)
+                host[(ib, k)] = (t, a)
+        nbytes = sum(a.nbytes for (_, a) in host.values())
+        L = capi.lib()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            for (ib, k), (_, a) in host.items():
+                capi.check(L.snac_set_field(ib, k, capi.dptr(a)))
+            dom.step(1, allow_not_converged=True)
+            for (ib, k), (_, a) in host.items():
+                capi.check(L.snac_get_field(ib, k, capi.dptr(a)))
+        el = time.perf_counter() - t0
+        return dict(s_per_step=el / steps, h2d=nbytes, d2h=nbytes, ncell=case.ncell)
+    finally:
+        dom.close()
+
+
+def cpu_reference(case_fn, steps, warmup, budget_s=60.0):
+    """The oracle (CPU restatement of the reference) on all host cores, bounded to ~budget_s of stepping."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from snac_gb300 import cases
+    case = case_fn()
+    d = O.OracleDomain(case)
+    ic = cases.channel_initial_condition(case, lambda ib: d.grid(ib, 1, O.G_XC))
+    for ib, (u, v, w) in ic.items():
+        d.field(ib, O.U)[...] = u
+        d.field(ib, O.V)[...] = v
+        d.field(ib, O.W)[...] = w
+    d.bounduvw(False)
+    d.boundp(O.P)
+    t0 = time.perf_counter()
+    d.step(1)                       # warm-up (first-touch, dt) -- always one
+    first = time.perf_counter() - t0
+    nrun = max(1, min(steps, int(budget_s / max(first, 1e-3))))
+    t0 = time.perf_counter()
+    d.step(nrun)
+    el = time.perf_counter() - t0
+    d.close()
+    return dict(ms=1e3 * el / nrun, nrun=nrun, ncell=case.ncell, cores=os.cpu_count())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    from snac_gb300 import cases
+    case_fn = lambda: cases.channel_4block()
+    cfg = {"workload": "channel4 256x144x128 (4 uneven blocks 96|160 x 64|80 x 128), Re_tau=180, FFT along z",
+           "cells": cases.channel_4block().ncell, "solver_tol": 1e-12, "blocks": 4,
+           "l2_policy": "inputs larger than L2 (fields + solver vectors ~0.5 GB/step)"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        r = cpu_reference(case_fn, args.steps, args.warmup)
+        mcells = r["ncell"] / (r["ms"] * 1e-3) / 1e6
+        line = {"metric": METRIC, "impl": "reference", "value": mcells, "unit": "Mcells/s", "n_gpus": 0,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+                "cpu_baseline": {"value": mcells, "unit": "Mcells/s", "cores": r["cores"], "kind": "port",
+                                 "sample": f"{r['nrun']} RK3 step(s) of the full case after 1 warm-up step "
+                                           "(the Fortran/HYPRE reference cannot be built here; its C restatement "
+                                           "with OpenMP on all host cores)"},
+                "e2e": {"value": mcells, "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    if world > 1 and not torch.distributed.is_initialized():
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    device = local
+    sampler = ClockSampler(device)
+    # plain FP64 path
+    plain = run_gpu_path(case_fn, 0, args.steps, args.warmup, device)
+    # mixed path, the headline; clocks sampled over its timed region
+    sampler.start()
+    mixed = run_gpu_path(case_fn, 1, args.steps, args.warmup, device)
+    clocks = sampler.stop()
+    # live CUDA-event timing of the dominant kernel classes over a timed run
+    prof_rbgs = run_gpu_path(case_fn, 1, args.steps, args.warmup, device, profile_kid=2)["prof"]
+    prof_mom = run_gpu_path(case_fn, 1, args.steps, args.warmup, device, profile_kid=1)["prof"]
+    ms = mixed["ms"]
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{device}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ncell = mixed["ncell"]
+    value = world * ncell / (ms * 1e-3) / 1e6
+    e2e = None
+    if not args.no_e2e:
+        e = run_e2e(case_fn, 1, max(2, min(args.steps, 5)), device)
+        e2e = {"value": world * e["ncell"] / e["s_per_step"] / 1e6, "unit": "Mcells/s",
+               "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"],
+               "ms_per_step": 1e3 * e["s_per_step"]}
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    from snac_gb300 import capi
+    f64 = C.c_double(); f32 = C.c_double()
+    capi.check(capi.lib().snac_probe_peaks(C.byref(f64), C.byref(f32)))
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    # roofline of the k_rk_mom kernel (FP64 state, FP64-pipe bound on GB300)
+    n, tot = prof_mom
+    launch_ms = tot / max(n, 1)
+    mom_bytes = 104.0 * ncell
+    mom_flops = KERNEL_WORK[1][2] * ncell
+    roof = {"kernel": "k_rk_mom", "bound": "hbm", "achieved": mom_bytes / (launch_ms * 1e-3) / 1e9,
+            "peak": hbm_peak, "unit": "GB/s", "frac": None, "traffic": None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s",
+            "launch_ms": launch_ms, "launches": n,
+            "fp64": {"achieved_gflops": mom_flops / (launch_ms * 1e-3) / 1e9, "peak_gflops": f64.value,
+                     "frac": mom_flops / (launch_ms * 1e-3) / 1e9 / f64.value,
+                     "note": "FP64 FMA-stream peak measured on this GPU by snac_probe_peaks"}}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    nr, totr = prof_rbgs
+    rb_ms = totr / max(nr, 1)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        r = cpu_reference(case_fn, args.steps, args.warmup, budget_s=30.0)
+        cpu = {"value": r["ncell"] / (r["ms"] * 1e-3) / 1e6, "unit": "Mcells/s", "cores": r["cores"], "kind": "port",
+               "sample": f"{r['nrun']} RK3 step(s) of the same case after 1 warm-up step, C restatement with OpenMP",
+               "ms_per_step": r["ms"]}
+    line = {"metric": METRIC, "value": value, "unit": "Mcells/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+            "paths": {"mixed": {"ms_per_step": mixed["ms"], "max_div_u": mixed["divmax"],
+                                "solve_iters_max": mixed["iters"], "solve_residual_max": mixed["residual"],
+                                "kinetic_energy": mixed["ke"]},
+                      "plain_fp64": {"ms_per_step": plain["ms"], "max_div_u": plain["divmax"],
+                                     "solve_iters_max": plain["iters"], "solve_residual_max": plain["residual"],
+                                     "kinetic_energy": plain["ke"]},
+                      "speedup_mixed_vs_plain": plain["ms"] / mixed["ms"], "learned_guess": "not built"},
+            "roofline": roof,
+            "kernels": {"k_rbgs_mean_launch_ms": rb_ms, "k_rbgs_launches_per_step": nr / args.steps,
+                        "k_rk_mom_mean_launch_ms": launch_ms},
+            "peaks_measured_here": {"fp64_gflops": f64.value, "fp32_gflops": f32.value},
+            "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -113,11 +113,20 @@ typedef struct snac_step_stats {
   int    solve_iters_max;     /* largest iteration count of the last step's solves */
   double solve_residual_max;  /* largest final relative residual of the last step's solves */
   int    solves;              /* solves run in the last step */
+  double device_ms;           /* device time of the last snac_step call (CUDA events on the library stream) */
 } snac_step_stats;
 
-/* ---------------------------------------------------------------- errors */
+/* ---------------------------------------------------------------- errors, diagnostics */
 const char *snac_last_error(void);
 int snac_device_count(int *n);
+/* No counterpart in the reference: measured FMA throughput of the device (GFLOP/s, 2 flops per FMA),
+ * the compute roofline of the FP64 kernels. */
+int snac_probe_peaks(double *fp64_gflops, double *fp32_gflops);
+/* No counterpart in the reference: time every launch of one kernel class with CUDA events on the
+ * library stream (1 rk_mom, 2 red-black smoother, 3 residual+restriction, 4/5 forward/backward
+ * transform, 6 Krylov operator apply, 7 fillps, 8 correc; 0 = off).  Selecting resets the record. */
+int snac_profile_kernel(int kernel_class);
+int snac_profile_read(int *launches, double *total_ms);
 
 /* ---------------------------------------------------------------- host mirrors */
 /* Keep a device mirror of a host array of `bytes` bytes (contents uploaded). */
@@ -179,6 +188,10 @@ int snac_initgrid(int lo, int hi, int gt, double gr, double lmin, double lmax,
 /* ---------------------------------------------------------------- domain layer */
 /* read_input + initmpi + initgrid/bound_grid + init_bc_rhs + solver set-up (main.f90:188-886) */
 int snac_init(const snac_case *c, const snac_block_desc *blocks, const snac_options *opt);
+/* The host part of snac_init without a device (placement, grids, operator assembly, multigrid
+ * hierarchy): validates an input and returns the number of multigrid levels and the cells of the
+ * coarsest level.  Reference counterpart: the sanity checks of sanity.f90 / initmpi.f90:150-237. */
+int snac_check_case(const snac_case *c, const snac_block_desc *blocks, int *levels, long *coarse_cells);
 int snac_finalize(void);
 int snac_block_geometry(int ib, int lo[3], int hi[3], int nb[3][2], int is_bound[3][2]);
 int snac_get_grid(int ib, int axis, int which, double *out);         /* (ng+2) values */

@@ -445,23 +445,24 @@ or_poisson *or_poisson_create(or_domain *d, const int centered[3], double alpha,
   while (P->nlev < OR_MAXLEV) {
     or_level *F = &P->L[P->nlev - 1];
     if (F->ncell <= OR_DENSE_MAX) break;
-    /* semicoarsening (as PFMG does): only axes whose smallest spacing is within a
-       factor 2 of the smallest spacing of any coupled axis, i.e. the strongly coupled ones */
+    /* eligible axes keep even block offsets/extents (and even periodic rings); among them
+       only the strongly coupled ones (smallest spacing within a factor 2) are halved,
+       semicoarsening as PFMG does */
     double hmin[3] = {1e300, 1e300, 1e300}, hall = 1e300;
+    int elig[3] = {0, 0, 0};
     for (int a = 0; a < na; a++) {
-      if (F->n[a] < 2) continue;
+      if (F->n[a] < 2 || F->n[a] % 2) continue;
+      int ok = 1;
+      for (int ib = 0; ib < d->nblocks; ib++) if (boff[ib][a] % 2 || bext[ib][a] % 2) ok = 0;
+      if (P->periodic[a] && (F->n[a] / 2) % 2 && F->n[a] / 2 != 1) ok = 0;
+      if (!ok) continue;
+      elig[a] = 1;
       for (int q = 0; q < F->n[a]; q++) if (F->W[a][q] < hmin[a]) hmin[a] = F->W[a][q];
       if (hmin[a] < hall) hall = hmin[a];
     }
     int co[3] = {0, 0, 0}, any = 0;
-    for (int a = 0; a < na; a++) {
-      if (F->n[a] < 2 || F->n[a] % 2) continue;
-      if (hmin[a] > 2.0 * hall) continue;
-      int ok = 1;
-      for (int ib = 0; ib < d->nblocks; ib++) if (boff[ib][a] % 2 || bext[ib][a] % 2) ok = 0;
-      if (P->periodic[a] && (F->n[a] / 2) % 2 && F->n[a] / 2 != 1) ok = 0;
-      if (ok) { co[a] = 1; any = 1; }
-    }
+    for (int a = 0; a < na; a++)
+      if (elig[a] && hmin[a] <= 2.0 * hall) { co[a] = 1; any = 1; }
     if (!any) break;
     or_level *C = &P->L[P->nlev];
     for (int a = 0; a < 3; a++) { C->n[a] = co[a] ? F->n[a] / 2 : F->n[a]; C->coarsened[a] = co[a]; }

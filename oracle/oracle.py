@@ -94,6 +94,18 @@ def lib():
         L.or_find_fft.argtypes = [C.c_char_p, C.c_int, ip, ip, dp]
         L.or_eigenvalues.argtypes = [C.c_int, C.c_char_p, C.c_int, dp]
         L.or_initgrid.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, dp, dp, dp, dp]
+        d = C.c_double
+        i = C.c_int
+        L.or_rk_mom.argtypes = [dp, ip, ip, dp, dp, dp, dp, dp, dp, d, dp, dp, d, dp, d, dp, dp, dp, dp, dp, dp, dp, i, i]
+        L.or_rk_scal.argtypes = [dp, ip, ip, dp, dp, dp, dp, dp, dp, d, d, d, dp, dp, dp, i, d, d, dp, dp, dp, i]
+        L.or_fillps.argtypes = [ip, ip, dp, dp, dp, d, dp, dp, dp, dp, i]
+        L.or_correc.argtypes = [ip, ip, dp, dp, dp, d, dp, dp, dp, dp]
+        L.or_updt_pressure.argtypes = [ip, ip, dp, dp, dp, dp, dp, dp, d, dp, dp, i]
+        L.or_chkdt_local.argtypes = [ip, ip, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
+        L.or_chkdiv_local.argtypes = [ip, ip, dp, dp, dp, dp, dp, dp, d, dp, dp]
+        L.or_updt_rhs.argtypes = [ip, ip, ip, dp, dp, dp, dp]
+        L.or_set_bc.argtypes = [C.c_char, i, ip, ip, i, i, d, d, dp]
+        L.or_r2r_lines.argtypes = [i, i, i, C.c_long, C.c_long, dp]
         _lib = L
     return _lib
 

@@ -237,6 +237,44 @@ def splitmix64_uniform(seed: int, n: int) -> np.ndarray:
     return out
 
 
+def channel_bulk_velocity(case: Case) -> float:
+    """Bulk velocity of the turbulent-channel estimate of initflow.f90 ('pdc', is_wallturb):
+    u_tau = sqrt(bforce*h), Re_b = (Re_tau/0.09)**(1/0.88), U_b = Re_b*visc/(2h), h = half height = 1."""
+    lref = 1.0
+    uref = math.sqrt(case.bforce[0] * lref)
+    visc = 1.0 / case.visci
+    retau = uref * lref / visc
+    reb = (retau / 0.09) ** (1.0 / 0.88)
+    return reb * visc / (2.0 * lref)
+
+
+def channel_initial_condition(case: Case, yc_of_block, seed: int = 0x5EED, amp: float = 0.1):
+    """Laminar Poiseuille profile in y scaled to U_b plus uniform noise in [-amp, amp]*U_b on u, v, w.
+
+    yc_of_block(ib) returns the (ng+2) cell-centre y coordinates of block ib.  Noise values are drawn
+    from one splitmix64 stream, block by block, component by component, Fortran order of the interior.
+    Returns {ib: (u, v, w)} halo'd arrays (ghosts zero)."""
+    ub = channel_bulk_velocity(case)
+    out = {}
+    offset = 0
+    for ib, b in enumerate(case.blocks):
+        n = [int(x) for x in b.ng]
+        ncell = n[0] * n[1] * n[2]
+        yc = yc_of_block(ib)[1:-1]
+        prof = 1.5 * ub * yc * (2.0 - yc)
+        comps = []
+        for c in range(3):
+            r = splitmix64_uniform_fast(seed + offset, ncell).reshape(n, order="F")
+            offset += ncell
+            f = np.zeros([x + 2 for x in n], order="F")
+            f[1:-1, 1:-1, 1:-1] = 2.0 * (r - 0.5) * amp * ub
+            if c == 0:
+                f[1:-1, 1:-1, 1:-1] += prof[None, :, None]
+            comps.append(f)
+        out[ib] = tuple(comps)
+    return out
+
+
 def splitmix64_uniform_fast(seed: int, n: int) -> np.ndarray:
     """Vectorised splitmix64 (identical output to splitmix64_uniform)."""
     with np.errstate(over="ignore"):

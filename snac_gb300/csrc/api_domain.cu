@@ -1,0 +1,773 @@
+// api_domain.cu -- domain layer of the C ABI: all blocks resident in HBM.
+//
+// snac_init restates the set-up of main.f90:188-886 that the hot path needs:
+// block placement in the global index space (initmpi.f90:50-98), neighbours
+// (initmpi.f90:150-237), grids (initgrid.f90:9-165 with bound_grid), the
+// pressure BC planes (solver.f90:44-157) and the solver set-up.  snac_step
+// runs the RK3 loop of main.f90:893-1069.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "snac_host.h"
+
+namespace snac {
+
+static const double RKC[3][2] = {{32.0 / 60.0, 0.0}, {25.0 / 60.0, -17.0 / 60.0}, {45.0 / 60.0, -25.0 / 60.0}};
+
+static Domain *g_dom = nullptr;
+Domain *domain() { return g_dom; }
+
+void *Domain::alloc(size_t bytes) {
+  void *p = nullptr;
+  if (cudaMalloc(&p, bytes ? bytes : 8) != cudaSuccess) return nullptr;
+  cudaMemset(p, 0, bytes ? bytes : 8);
+  allocs.push_back(p);
+  return p;
+}
+Domain::~Domain() {
+  ps.reset();
+  for (void *p : allocs) cudaFree(p);
+  if (h_red) cudaFreeHost(h_red);
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
+  if (st) cudaStreamDestroy(st);
+}
+
+// ---- initgrid.f90:171-287 ----
+static double gp_geo_one_end(double alpha, double r0) {
+  if (r0 == 1.0) return r0;
+  return r0 * std::pow((1.0 - std::pow(r0, alpha)) / (1.0 - r0) / alpha, 1.0 / 3.0);
+}
+static double gridpoint(int gt, double alpha, double r0) {
+  switch (gt) {
+    case 1: return alpha != 0.0 ? 1.0 * (1.0 + std::tanh((r0 - 1.0) * alpha) / std::tanh(alpha / 1.0)) : r0;
+    case 2:
+      if (alpha == 0.0) return r0;
+      if (r0 <= 0.5) return 0.5 * (1.0 - 1.0 + std::tanh(2.0 * alpha * (r0 - 0.0)) / std::tanh(alpha));
+      return 0.5 * (1.0 + 1.0 + std::tanh(2.0 * alpha * (r0 - 1.0)) / std::tanh(alpha));
+    case 3: return alpha != 0.0 ? 1.0 - 1.0 * (1.0 + std::tanh((1.0 - r0 - 1.0) * alpha) / std::tanh(alpha / 1.0)) : r0;
+    case 4: return gp_geo_one_end(alpha, r0);
+    case 5: return 1.0 - gp_geo_one_end(alpha, 1.0 - r0);
+    case 6:
+      if (r0 <= 0.5) return gp_geo_one_end(alpha / 2.0, 2.0 * r0) / 2.0;
+      return 1.0 - gp_geo_one_end(alpha / 2.0, 2.0 * (1.0 - r0)) / 2.0;
+    case 7:
+      if (r0 <= 0.5) return (1.0 - gp_geo_one_end(alpha / 2.0, (0.5 - r0) * 2.0)) / 2.0;
+      return (1.0 + gp_geo_one_end(alpha / 2.0, (r0 - 0.5) * 2.0)) / 2.0;
+    default: return alpha != 0.0 ? 0.5 * (1.0 + std::tanh((r0 - 0.5) * alpha) / std::tanh(alpha / 2.0)) : r0;
+  }
+}
+
+// initgrid.f90:9-83
+void initgrid(int lo, int hi, int gt, double gr, double lmin, double lmax, double *drc, double *drf, double *rc,
+              double *rf) {
+  auto at = [&](double *a, int q) -> double & { return a[q - lo + 1]; };
+  const int n = hi - lo + 1;
+  for (int q = lo; q <= hi; q++) {
+    const double r0 = ((double)(q - lo + 1) - 0.0) / (1.0 * n);
+    at(rf, q) = gridpoint(gt, gr, r0);
+    at(rf, q) = lmin + at(rf, q) * (lmax - lmin);
+  }
+  at(rf, lo - 1) = lmin;
+  for (int q = lo; q <= hi; q++) at(drf, q) = at(rf, q) - at(rf, q - 1);
+  at(drf, lo - 1) = at(drf, lo);
+  at(drf, hi + 1) = at(drf, hi);
+  for (int q = lo - 1; q <= hi; q++) at(drc, q) = 0.5 * (at(drf, q) + at(drf, q + 1));
+  at(drc, hi + 1) = at(drc, hi);
+  at(rc, lo - 1) = lmin - at(drc, lo - 1) / 2.0;
+  at(rf, lo - 1) = lmin;
+  for (int q = lo; q <= hi + 1; q++) {
+    at(rc, q) = at(rc, q - 1) + at(drc, q - 1);
+    at(rf, q) = at(rf, q - 1) + at(drf, q);
+  }
+}
+
+// initgrid.f90:144-165 (load_grid)
+static void load_grid(int lo, int hi, const double *file, double *rf, double *rc, double *drf, double *drc) {
+  auto at = [&](double *a, int q) -> double & { return a[q - lo + 1]; };
+  const int n = hi - lo + 1;
+  for (int q = lo; q <= hi; q++) {
+    at(rf, q) = file[q - lo];
+    at(rc, q) = file[n + q - lo];
+    at(drf, q) = file[2 * n + q - lo];
+    at(drc, q) = file[3 * n + q - lo];
+  }
+  at(drf, lo - 1) = at(drf, lo);
+  at(drf, hi + 1) = at(drf, hi);
+  at(drc, lo - 1) = at(drf, lo);
+  at(drc, hi + 1) = at(drc, hi);
+  at(rf, lo - 1) = at(rf, lo) - at(drf, lo);
+  at(rf, hi + 1) = at(rf, hi) + at(drf, hi);
+  at(rc, lo - 1) = at(rc, lo) - at(drc, lo - 1);
+  at(rc, hi + 1) = at(rc, hi) + at(drc, hi);
+}
+
+// fft.f90:96-149
+void find_fft(char a, char b, int is_centered, int *kf, int *kb, double norm[2]) {
+  *kf = *kb = -1;
+  norm[0] = norm[1] = 0.0;
+  auto set = [&](int f, int bw, double n0, double n1) { *kf = f; *kb = bw; norm[0] = n0; norm[1] = n1; };
+  if (is_centered) {
+    if (a == 'F' && b == 'F') set(SNAC_R2HC, SNAC_HC2R, 1, 0);
+    else if (a == 'N' && b == 'N') set(SNAC_REDFT10, SNAC_REDFT01, 2, 0);
+    else if (a == 'D' && b == 'D') set(SNAC_RODFT10, SNAC_RODFT01, 2, 0);
+    else if (a == 'N' && b == 'D') set(SNAC_REDFT11, SNAC_REDFT11, 2, 0);
+    else if (a == 'D' && b == 'N') set(SNAC_RODFT11, SNAC_RODFT11, 2, 0);
+  } else {
+    if (a == 'F' && b == 'F') set(SNAC_R2HC, SNAC_HC2R, 1, 0);
+    else if (a == 'N' && b == 'N') set(SNAC_REDFT00, SNAC_REDFT00, 2, -1);
+    else if (a == 'D' && b == 'D') set(SNAC_RODFT00, SNAC_RODFT00, 2, 1);
+    else if (a == 'N' && b == 'D') set(SNAC_REDFT10, SNAC_REDFT01, 2, 0);
+    else if (a == 'D' && b == 'N') set(SNAC_RODFT01, SNAC_RODFT10, 2, 0);
+  }
+}
+
+// fft.f90:151-189; the reference defines no 'DN' case (returns -1 here)
+int eigenvalues(int n, char a, char b, int is_centered, double *lambda) {
+  const double PI = 3.14159265358979323846264338327950288;
+  auto s2 = [](double x) { const double s = std::sin(x); return -4.0 * s * s; };
+  if (a == 'F' && b == 'F') for (int l = 1; l <= n; l++) lambda[l - 1] = s2((1.0 * (l - 1)) * PI / (1.0 * n));
+  else if (a == 'N' && b == 'N') {
+    if (is_centered) for (int l = 1; l <= n; l++) lambda[l - 1] = s2((1.0 * (l - 1)) * PI / (2.0 * n));
+    else for (int l = 1; l <= n; l++) lambda[l - 1] = s2((1.0 * (l - 1)) * PI / (2.0 * (n - 1 + 1)));
+  } else if (a == 'D' && b == 'D') {
+    if (is_centered) for (int l = 1; l <= n; l++) lambda[l - 1] = s2((1.0 * (l - 0)) * PI / (2.0 * n));
+    else { for (int l = 1; l <= n - 1; l++) lambda[l - 1] = s2((1.0 * (l - 0)) * PI / (2.0 * (n + 1 - 1))); lambda[n - 1] = 0.0; }
+  } else if (a == 'N' && b == 'D') for (int l = 1; l <= n; l++) lambda[l - 1] = s2((1.0 * (2 * l - 1)) * PI / (4.0 * n));
+  else return -1;
+  return 0;
+}
+
+// solver.f90:44-157 (init_bc_rhs) for the pressure, centred in every direction
+static void init_bc_rhs_p(const HostBlock &H, const int periods[3], int fft_axis, std::vector<double> rhs[3]) {
+  const int nx = H.ng[0], ny = H.ng[1], nz = H.ng[2];
+  rhs[0].assign((size_t)ny * nz * 2, 0.0);
+  rhs[1].assign((size_t)nx * nz * 2, 0.0);
+  rhs[2].assign((size_t)nx * ny * 2, 0.0);
+  double factor[3][2];
+  for (int q = 0; q < 3; q++)
+    for (int s = 0; s < 2; s++) {
+      factor[q][s] = 0.0;
+      if (!H.is_bound[q][s]) continue;
+      const char cb = H.desc.cbcpre[q][s];
+      const double bc = H.desc.bcpre[q][s];
+      if (cb == 'N') { factor[q][s] = 1.0 * H.dl[q][s] * bc; if (s == 1) factor[q][s] = -factor[q][s]; }
+      else if (cb == 'D') factor[q][s] = -2.0 * bc;
+    }
+  const double *dx1 = H.g[0][0].data(), *dx2 = H.g[0][1].data(), *dy1 = H.g[1][0].data(), *dy2 = H.g[1][1].data(),
+               *dz1 = H.g[2][0].data(), *dz2 = H.g[2][1].data();
+  auto W = [&](int i, int j, int k) {  // local 1-based indices into (n+2) arrays
+    switch (fft_axis) {
+      case 1: return dy2[j] * dz2[k];
+      case 2: return dx2[i] * dz2[k];
+      case 3: return dx2[i] * dy2[j];
+      default: return dx2[i] * dy2[j] * dz2[k];
+    }
+  };
+  for (int idir = 0; idir < 3; idir++) {
+    if (periods[idir] != 0) continue;
+    const int n = H.ng[idir];
+    const int sides = n > 1 ? 2 : 1;
+    for (int sd = 0; sd < sides; sd++) {
+      const int ib = sd;
+      if (!H.is_bound[idir][ib]) continue;
+      const int cface = ib ? n : 1;  // local 1-based index of the boundary cell
+      if (idir == 0)
+        for (int k = 1; k <= nz; k++)
+          for (int j = 1; j <= ny; j++)
+            rhs[0][(j - 1) + (size_t)ny * ((k - 1) + (size_t)nz * ib)] = factor[0][ib] * W(cface, j, k) / (dx1[cface - (1 - ib)] * dx2[cface]);
+      else if (idir == 1)
+        for (int k = 1; k <= nz; k++)
+          for (int i = 1; i <= nx; i++)
+            rhs[1][(i - 1) + (size_t)nx * ((k - 1) + (size_t)nz * ib)] = factor[1][ib] * W(i, cface, k) / (dy1[cface - (1 - ib)] * dy2[cface]);
+      else
+        for (int j = 1; j <= ny; j++)
+          for (int i = 1; i <= nx; i++)
+            rhs[2][(i - 1) + (size_t)nx * ((j - 1) + (size_t)ny * ib)] = factor[2][ib] * W(i, j, cface) / (dz1[cface - (1 - ib)] * dz2[cface]);
+    }
+  }
+}
+
+static int build_domain(Domain &d, const snac_case *c, const snac_block_desc *blocks) {
+  d.c = *c;
+  d.nblocks = c->nblocks;
+  if (d.nblocks < 1) { set_error("nblocks must be >= 1"); return SNAC_ERR_ARG; }
+  if (c->nscal < 0 || c->nscal > SNAC_MAX_SCAL) { set_error("nscal out of range"); return SNAC_ERR_ARG; }
+  if (c->impdiff || c->nscal > 0) { set_error("IMPDIFF and scalar transport are not wired into snac_step yet"); return SNAC_ERR_UNSUPPORTED; }
+  d.hb.resize(d.nblocks);
+  // placement (initmpi.f90:50-98)
+  std::vector<int> done(d.nblocks, 0), unl(d.nblocks, 0);
+  for (int a = 0; a < 3; a++) d.hb[0].lo[a] = 1;
+  unl[0] = 1;
+  int ib = 0;
+  while (true) {
+    bool all = true;
+    for (int q = 0; q < d.nblocks; q++) if (!done[q]) all = false;
+    if (all) break;
+    if (ib < 0) { set_error("invalid block connectivity (unreachable block)"); return SNAC_ERR_ARG; }
+    for (int idir = 0; idir < 3; idir++)
+      for (int inb = 0; inb < 2; inb++) {
+        if (blocks[ib].cbcpre[idir][inb] != 'F') continue;
+        const int f = (int)std::lround(blocks[ib].bcpre[idir][inb]) - 1;
+        if (f < 0 || f >= d.nblocks) { set_error("block %d: friend block %d does not exist", ib + 1, f + 1); return SNAC_ERR_ARG; }
+        if (unl[f]) continue;
+        if (inb == 0 && blocks[f].lmin[idir] > blocks[ib].lmin[idir]) continue;
+        if (inb == 1 && blocks[f].lmin[idir] < blocks[ib].lmin[idir]) continue;
+        const int ioff = -(1 - inb) * blocks[f].ng[idir] + inb * blocks[ib].ng[idir];
+        d.hb[f].lo[idir] = d.hb[ib].lo[idir] + ioff;
+        for (int t = 0; t < 3; t++) if (t != idir) d.hb[f].lo[t] = d.hb[ib].lo[t];
+        unl[f] = 1;
+      }
+    done[ib] = 1;
+    ib = -1;
+    for (int q = 0; q < d.nblocks; q++) if (!done[q] && unl[q]) { ib = q; break; }
+  }
+  for (int b = 0; b < d.nblocks; b++) {
+    HostBlock &H = d.hb[b];
+    H.desc = blocks[b];
+    for (int a = 0; a < 3; a++) {
+      H.ng[a] = blocks[b].ng[a];
+      if (H.ng[a] < 1) { set_error("block %d: ng must be >= 1", b + 1); return SNAC_ERR_ARG; }
+      H.hi[a] = H.lo[a] + H.ng[a] - 1;
+    }
+  }
+  for (int q = 0; q < 3; q++) {
+    d.is_periodic[q] = 1;
+    int lmn = d.hb[0].lo[q], hmx = d.hb[0].hi[q];
+    for (int b = 0; b < d.nblocks; b++) {
+      if (!(blocks[b].cbcpre[q][0] == 'F' && blocks[b].cbcpre[q][1] == 'F')) d.is_periodic[q] = 0;
+      lmn = std::min(lmn, d.hb[b].lo[q]);
+      hmx = std::max(hmx, d.hb[b].hi[q]);
+    }
+    d.periods[q] = d.is_periodic[q] ? hmx - lmn + 1 : 0;
+  }
+  for (int b = 0; b < d.nblocks; b++) {
+    HostBlock &H = d.hb[b];
+    for (int q = 0; q < 3; q++)
+      for (int s = 0; s < 2; s++) {
+        H.nb[q][s] = -1;
+        if (blocks[b].cbcpre[q][s] == 'F') {
+          const int f = (int)std::lround(blocks[b].bcpre[q][s]) - 1;
+          const HostBlock &F = d.hb[f];
+          bool ok = blocks[f].cbcpre[q][1 - s] == 'F' && (int)std::lround(blocks[f].bcpre[q][1 - s]) - 1 == b;
+          for (int t = 0; t < 3; t++)
+            if (t != q)
+              ok = ok && F.lo[t] == H.lo[t] && F.hi[t] == H.hi[t] && blocks[f].lmin[t] == blocks[b].lmin[t] &&
+                   blocks[f].lmax[t] == blocks[b].lmax[t] && blocks[f].gr[t] == blocks[b].gr[t] &&
+                   blocks[f].gt[t] == blocks[b].gt[t];
+          if (s == 0) ok = ok && (F.hi[q] + 1 == H.lo[q] || (d.periods[q] && F.hi[q] - H.lo[q] + 1 == d.periods[q]));
+          else ok = ok && (H.hi[q] + 1 == F.lo[q] || (d.periods[q] && H.hi[q] - F.lo[q] + 1 == d.periods[q]));
+          if (!ok) { set_error("block %d: inconsistent connectivity with block %d", b + 1, f + 1); return SNAC_ERR_ARG; }
+          H.nb[q][s] = f;
+        }
+        H.is_bound[q][s] = H.nb[q][s] < 0;
+      }
+  }
+  // grids
+  for (int b = 0; b < d.nblocks; b++) {
+    HostBlock &H = d.hb[b];
+    for (int a = 0; a < 3; a++) {
+      for (int w = 0; w < 4; w++) H.g[a][w].assign(H.ng[a] + 2, 0.0);
+      initgrid(H.lo[a], H.hi[a], blocks[b].gt[a], blocks[b].gr[a], blocks[b].lmin[a], blocks[b].lmax[a],
+               H.g[a][0].data(), H.g[a][1].data(), H.g[a][2].data(), H.g[a][3].data());
+      if (blocks[b].grid_file[a])
+        load_grid(H.lo[a], H.hi[a], blocks[b].grid_file[a], H.g[a][3].data(), H.g[a][2].data(), H.g[a][1].data(),
+                  H.g[a][0].data());
+      // dl(0:1,a) = drc_g(lo_g-1), drc_g(hi_g) of the block's own (unexchanged) grid, main.f90:725-727
+      H.dl[a] = {H.g[a][0][0], H.g[a][0][H.ng[a]]};
+    }
+  }
+  // bound_grid (initgrid.f90:91-127)
+  std::vector<HostBlock> orig = d.hb;
+  for (int b = 0; b < d.nblocks; b++) {
+    HostBlock &H = d.hb[b];
+    for (int a = 0; a < 3; a++) {
+      const int n = H.ng[a];
+      if (H.nb[a][0] >= 0) H.g[a][1][0] = orig[H.nb[a][0]].g[a][1][orig[H.nb[a][0]].ng[a]];
+      if (H.nb[a][1] >= 0) H.g[a][1][n + 1] = orig[H.nb[a][1]].g[a][1][1];
+      auto &df = H.g[a][1];
+      auto &dc = H.g[a][0];
+      dc[0] = (df[1] + df[0]) / 2.0;
+      dc[n] = (df[n + 1] + df[n]) / 2.0;
+      dc[n + 1] = dc[n];
+    }
+  }
+  d.vol_all = 0.0;
+  for (int b = 0; b < d.nblocks; b++)
+    d.vol_all += (blocks[b].lmax[0] - blocks[b].lmin[0]) * (blocks[b].lmax[1] - blocks[b].lmin[1]) *
+                 (blocks[b].lmax[2] - blocks[b].lmin[2]);
+  for (int b = 0; b < d.nblocks; b++) init_bc_rhs_p(d.hb[b], d.periods, c->fft_axis, d.hb[b].rhsp);
+  return SNAC_OK;
+}
+
+static int upload_domain(Domain &d) {
+  SNAC_CUDA(cudaStreamCreateWithFlags(&d.st, cudaStreamNonBlocking));
+  d.db.resize(d.nblocks);
+  std::vector<std::array<int, 3>> sz, szh;
+  size_t rh = 0;
+  for (int b = 0; b < d.nblocks; b++) {
+    HostBlock &H = d.hb[b];
+    DBlock &B = d.db[b];
+    memset(&B, 0, sizeof(B));
+    for (int a = 0; a < 3; a++) { B.n[a] = H.ng[a]; B.lo[a] = H.lo[a]; }
+    const size_t nh = (size_t)(H.ng[0] + 2) * (H.ng[1] + 2) * (H.ng[2] + 2) * sizeof(double);
+    const size_t ni = (size_t)H.ng[0] * H.ng[1] * H.ng[2] * sizeof(double);
+    B.u = (double *)d.alloc(nh); B.v = (double *)d.alloc(nh); B.w = (double *)d.alloc(nh);
+    B.p = (double *)d.alloc(nh); B.pp = (double *)d.alloc(nh);
+    B.ru = (double *)d.alloc(ni); B.rv = (double *)d.alloc(ni); B.rw = (double *)d.alloc(ni);
+    B.nu = (double *)d.alloc(ni); B.nv = (double *)d.alloc(ni); B.nw = (double *)d.alloc(ni);
+    if (!B.u || !B.v || !B.w || !B.p || !B.pp || !B.ru || !B.nu || !B.nw) { set_error("device allocation failed (fields)"); return SNAC_ERR_NOMEM; }
+    for (int a = 0; a < 3; a++) {
+      auto t = axis_tables(H.g[a][0].data(), H.g[a][1].data(), H.ng[a]);
+      double *p = (double *)d.alloc(t.size() * sizeof(double));
+      if (!p) return SNAC_ERR_NOMEM;
+      SNAC_CUDA(cudaMemcpy(p, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice));
+      B.ax[a] = p;
+    }
+    sz.push_back({H.ng[0], H.ng[1], H.ng[2]});
+    szh.push_back({H.ng[0] + 2, H.ng[1] + 2, H.ng[2] + 2});
+    d.rhsp_off.push_back(rh);
+    rh += H.rhsp[0].size() + H.rhsp[1].size() + H.rhsp[2].size();
+  }
+  d.d_db = (DBlock *)d.alloc(d.nblocks * sizeof(DBlock));
+  SNAC_CUDA(cudaMemcpy(d.d_db, d.db.data(), d.nblocks * sizeof(DBlock), cudaMemcpyHostToDevice));
+  auto tl = make_tiles(sz, TX, TY, TZ), th = make_tiles(szh, TX, TY, TZ);
+  d.ntiles = (int)tl.size();
+  d.ntiles_halo = (int)th.size();
+  d.d_tiles = (Tile *)d.alloc(tl.size() * sizeof(Tile));
+  d.d_tiles_halo = (Tile *)d.alloc(th.size() * sizeof(Tile));
+  SNAC_CUDA(cudaMemcpy(d.d_tiles, tl.data(), tl.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+  SNAC_CUDA(cudaMemcpy(d.d_tiles_halo, th.data(), th.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+  // pressure BC planes
+  std::vector<double> allr;
+  for (int b = 0; b < d.nblocks; b++)
+    for (int a = 0; a < 3; a++) allr.insert(allr.end(), d.hb[b].rhsp[a].begin(), d.hb[b].rhsp[a].end());
+  d.d_rhsp = (double *)d.alloc(allr.size() * sizeof(double));
+  SNAC_CUDA(cudaMemcpy(d.d_rhsp, allr.data(), allr.size() * sizeof(double), cudaMemcpyHostToDevice));
+  // halo links
+  for (int a = 0; a < 3; a++) {
+    std::vector<FaceLink> fl;
+    const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+    int mp = 0;
+    for (int b = 0; b < d.nblocks; b++) {
+      for (int s = 0; s < 2; s++)
+        if (d.hb[b].nb[a][s] >= 0) fl.push_back({b, d.hb[b].nb[a][s], s, 0});
+      mp = std::max(mp, (d.hb[b].ng[t1] + 2) * (d.hb[b].ng[t2] + 2));
+    }
+    d.nlinks[a] = (int)fl.size();
+    d.maxplane[a] = mp;
+    d.d_links[a] = (FaceLink *)d.alloc(std::max<size_t>(1, fl.size()) * sizeof(FaceLink));
+    if (!fl.empty()) SNAC_CUDA(cudaMemcpy(d.d_links[a], fl.data(), fl.size() * sizeof(FaceLink), cudaMemcpyHostToDevice));
+  }
+  int flds[5 + SNAC_MAX_SCAL];
+  for (int q = 0; q < 5 + SNAC_MAX_SCAL; q++) flds[q] = q;
+  d.d_flds = (int *)d.alloc(sizeof(flds));
+  SNAC_CUDA(cudaMemcpy(d.d_flds, flds, sizeof(flds), cudaMemcpyHostToDevice));
+  // boundary-condition tables (bound.f90:36-105)
+  for (int kind = 0; kind < 4; kind++)
+    for (int a = 0; a < 3; a++) {
+      std::vector<BcEntry> E;
+      for (int b = 0; b < d.nblocks; b++) {
+        const HostBlock &H = d.hb[b];
+        const int nf = kind < 2 ? 3 : 1;
+        for (int fi = 0; fi < nf; fi++) {
+          BcEntry e;
+          memset(&e, 0, sizeof(e));
+          e.b = b;
+          e.f = kind < 2 ? fi : (kind == 2 ? 3 : 4);
+          bool any = false;
+          for (int s = 0; s < 2; s++) {
+            e.mode[s] = BC_NONE;
+            if (!H.is_bound[a][s]) continue;
+            char ct;
+            double val, dr;
+            int centered;
+            if (kind < 2) {
+              centered = fi != a;
+              if (!centered && kind == 1) continue;  // is_correc skips the wall-normal component
+              ct = H.desc.cbcvel[fi][a][s];
+              val = H.desc.bcvel[fi][a][s];
+              dr = centered ? H.g[a][0][s ? H.ng[a] : 0] : H.g[a][1][s ? H.ng[a] : 0];
+            } else {
+              centered = 1;
+              ct = H.desc.cbcpre[a][s];
+              val = H.desc.bcpre[a][s];
+              dr = H.g[a][0][s ? H.ng[a] : 0];
+            }
+            bc_mode(ct, s, centered, val, dr, &e.mode[s], &e.factor[s], &e.sgn[s]);
+            any = any || e.mode[s] != BC_NONE;
+          }
+          if (any) E.push_back(e);
+        }
+      }
+      d.nbc[kind][a] = (int)E.size();
+      d.d_bc[kind][a] = (BcEntry *)d.alloc(std::max<size_t>(1, E.size()) * sizeof(BcEntry));
+      if (!E.empty()) SNAC_CUDA(cudaMemcpy(d.d_bc[kind][a], E.data(), E.size() * sizeof(BcEntry), cudaMemcpyHostToDevice));
+    }
+  d.d_part = (double *)d.alloc((size_t)std::max(d.ntiles, 1) * 2 * sizeof(double));
+  d.d_red = (double *)d.alloc(4 * sizeof(double));
+  SNAC_CUDA(cudaMallocHost(&d.h_red, 4 * sizeof(double)));
+  return SNAC_OK;
+}
+
+static int bound_uvw(Domain &d, int is_correc) {
+  for (int a = 0; a < 3; a++)
+    SNAC_TRY(launch_exchange(d.d_db, d.d_links[a], d.nlinks[a], d.d_flds, 3, a, d.maxplane[a], d.st));
+  for (int a = 0; a < 3; a++) SNAC_TRY(launch_setbc(d.d_db, d.d_bc[is_correc ? 1 : 0][a], d.nbc[is_correc ? 1 : 0][a], a, d.maxplane[a], d.st));
+  return SNAC_OK;
+}
+
+static int bound_p(Domain &d, int field) {
+  const int fsel = field == SNAC_P ? 3 : 4;
+  const int kind = field == SNAC_P ? 2 : 3;
+  for (int a = 0; a < 3; a++) SNAC_TRY(launch_exchange(d.d_db, d.d_links[a], d.nlinks[a], d.d_flds + fsel, 1, a, d.maxplane[a], d.st));
+  for (int a = 0; a < 3; a++) SNAC_TRY(launch_setbc(d.d_db, d.d_bc[kind][a], d.nbc[kind][a], a, d.maxplane[a], d.st));
+  return SNAC_OK;
+}
+
+static int updt_rhs_all(Domain &d) {
+  for (int b = 0; b < d.nblocks; b++) {
+    const HostBlock &H = d.hb[b];
+    int isb[6];
+    for (int a = 0; a < 3; a++) for (int s = 0; s < 2; s++) isb[2 * a + s] = H.is_bound[a][s];
+    const double *rx = d.d_rhsp + d.rhsp_off[b];
+    const double *ry = rx + H.rhsp[0].size();
+    const double *rz = ry + H.rhsp[1].size();
+    SNAC_TRY(launch_updt_rhs(H.ng[0], H.ng[1], H.ng[2], isb, rx, ry, rz, d.db[b].pp, d.st));
+  }
+  return SNAC_OK;
+}
+
+static int rk_mom_all(Domain &d, int irk) {
+  RkMomParams prm;
+  prm.f1 = RKC[irk][0] * d.dt;
+  prm.f2 = RKC[irk][1] * d.dt;
+  prm.f12 = prm.f1 + prm.f2;
+  for (int a = 0; a < 3; a++) { prm.bforce[a] = d.c.bforce[a]; prm.gb[a] = 0.0; }
+  prm.visc = 1.0 / d.c.visci;
+  prm.impdiff = 0;
+  prm.boussinesq = 0;
+  SNAC_TRY(launch_rk_mom(d.d_db, d.d_tiles, d.ntiles, prm, d.st));
+  SNAC_TRY(launch_rk_mom_writeback(d.d_db, d.d_tiles, d.ntiles, d.st));
+  return SNAC_OK;
+}
+
+static int reduce(Domain &d, int which, double out[2]) {
+  if (which == 0) SNAC_TRY(launch_chkdt_partial(d.d_db, d.d_tiles, d.ntiles, d.d_part, d.st));
+  else if (which == 1) SNAC_TRY(launch_chkdiv_partial(d.d_db, d.d_tiles, d.ntiles, d.vol_all, d.d_part, d.st));
+  else SNAC_TRY(launch_ke_partial(d.d_db, d.d_tiles, d.ntiles, d.d_part, d.st));
+  SNAC_TRY(launch_reduce_final(d.d_part, d.ntiles, d.d_red, d.st));
+  SNAC_CUDA(cudaMemcpyAsync(d.h_red, d.d_red, 2 * sizeof(double), cudaMemcpyDeviceToHost, d.st));
+  SNAC_CUDA(cudaStreamSynchronize(d.st));
+  out[0] = d.h_red[0];
+  out[1] = d.h_red[1];
+  return SNAC_OK;
+}
+
+// chkdt.f90 incl. reductions; the caller's visc is max(visc, alpha_max) (main.f90:660)
+static int chkdt_all(Domain &d, double *dt_cfl) {
+  double r[2];
+  SNAC_TRY(reduce(d, 0, r));
+  double dti = r[1];
+  if (std::isinf(dti)) { set_error("chkdt: non-finite velocity"); return SNAC_ERR_NAN; }
+  if (dti == 0.0) dti = 1.0;
+  double dtmax = std::sqrt(3.0) / dti;
+  if (!d.c.impdiff) {
+    double dlmin = 1e300;
+    for (auto &H : d.hb)
+      for (int a = 0; a < 3; a++)
+        for (double v : H.g[a][1]) dlmin = std::min(dlmin, v);
+    double visc = 1.0 / d.c.visci, amax = 0.0;
+    for (int s = 0; s < d.c.nscal; s++) amax = std::max(amax, 1.0 / d.c.alphai[s]);
+    dtmax = std::min(dtmax, 1.65 / 12.0 / std::max(visc, amax) * (dlmin * dlmin));
+  }
+  *dt_cfl = dtmax;
+  return SNAC_OK;
+}
+
+static int set_dt_from_cfl(Domain &d) {
+  double dt_cfl;
+  SNAC_TRY(chkdt_all(d, &dt_cfl));
+  d.dt = d.c.dt_f > 0.0 ? d.c.dt_f : std::min(d.c.cfl * dt_cfl, d.c.dtmax);
+  return SNAC_OK;
+}
+
+static int one_stage(Domain &d, int irk) {
+  const double dtrk = (RKC[irk][0] + RKC[irk][1]) * d.dt;
+  const double alpha = -(1.0 / d.c.visci) * dtrk / 2.0;
+  SNAC_TRY(rk_mom_all(d, irk));
+  SNAC_TRY(bound_uvw(d, 0));
+  SNAC_TRY(launch_fillps(d.d_db, d.d_tiles, d.ntiles, dtrk, d.c.fft_axis, d.st));
+  SNAC_TRY(updt_rhs_all(d));
+  int rc = solver_solve_pressure(d, *d.ps);
+  if (rc != SNAC_OK && rc != SNAC_ERR_NOT_CONVERGED) return rc;
+  d.last_solve_iters = std::max(d.last_solve_iters, d.ps->last_iters);
+  d.last_solve_res = std::max(d.last_solve_res, d.ps->last_res);
+  d.solves++;
+  SNAC_TRY(bound_p(d, SNAC_PP));
+  SNAC_TRY(launch_correc(d.d_db, d.d_tiles_halo, d.ntiles_halo, dtrk, d.st));
+  SNAC_TRY(bound_uvw(d, 1));
+  SNAC_TRY(launch_updt_pressure(d.d_db, d.d_tiles, d.ntiles, alpha, d.c.impdiff, d.st));
+  SNAC_TRY(bound_p(d, SNAC_P));
+  return rc;
+}
+
+static int field_ptr(Domain &d, int ib, int field, double **p, size_t *bytes) {
+  if (ib < 0 || ib >= d.nblocks) { set_error("block index out of range"); return SNAC_ERR_ARG; }
+  DBlock &B = d.db[ib];
+  const size_t nh = (size_t)(B.n[0] + 2) * (B.n[1] + 2) * (B.n[2] + 2) * sizeof(double);
+  const size_t ni = (size_t)B.n[0] * B.n[1] * B.n[2] * sizeof(double);
+  switch (field) {
+    case SNAC_U: *p = B.u; *bytes = nh; break;
+    case SNAC_V: *p = B.v; *bytes = nh; break;
+    case SNAC_W: *p = B.w; *bytes = nh; break;
+    case SNAC_P: *p = B.p; *bytes = nh; break;
+    case SNAC_PP: *p = B.pp; *bytes = nh; break;
+    case SNAC_DUDTRKO: *p = B.ru; *bytes = ni; break;
+    case SNAC_DVDTRKO: *p = B.rv; *bytes = ni; break;
+    case SNAC_DWDTRKO: *p = B.rw; *bytes = ni; break;
+    default: set_error("unknown field %d", field); return SNAC_ERR_ARG;
+  }
+  return SNAC_OK;
+}
+
+}  // namespace snac
+
+using namespace snac;
+
+#define NEED_DOMAIN                                                         \
+  Domain *d = domain();                                                     \
+  if (!d) { set_error("snac_init has not been called"); return SNAC_ERR_STATE; }
+
+extern "C" {
+
+int snac_initgrid(int lo, int hi, int gt, double gr, double lmin, double lmax, double *drc, double *drf, double *rc,
+                  double *rf) {
+  if (hi < lo) { set_error("hi < lo"); return SNAC_ERR_ARG; }
+  initgrid(lo, hi, gt, gr, lmin, lmax, drc, drf, rc, rf);
+  return SNAC_OK;
+}
+
+int snac_find_fft(const char bc[2], int is_centered, int *kind_fwd, int *kind_bwd, double norm[2]) {
+  find_fft(bc[0], bc[1], is_centered, kind_fwd, kind_bwd, norm);
+  if (*kind_fwd < 0) { set_error("no transform for this boundary pair"); return SNAC_ERR_ARG; }
+  return SNAC_OK;
+}
+
+int snac_eigenvalues(int n, const char bc[2], int is_centered, double *lambda) {
+  if (eigenvalues(n, bc[0], bc[1], is_centered, lambda)) { set_error("the reference defines no eigenvalues for this pair"); return SNAC_ERR_UNSUPPORTED; }
+  return SNAC_OK;
+}
+
+int snac_fft(int kind, int idir, const int n[3], int q, double *arr) {
+  if (idir < 1 || idir > 3 || q < 0 || q > 1) { set_error("snac_fft: bad idir or q"); return SNAC_ERR_ARG; }
+  ArgArray A;
+  SNAC_TRY(A.bind(arr, (size_t)n[0] * n[1] * n[2] * sizeof(double), true, true));
+  SNAC_TRY(r2r_array(kind, idir, n, q, (double *)A.dev, 0));
+  SNAC_TRY(A.finish());
+  return SNAC_OK;
+}
+
+int snac_init(const snac_case *c, const snac_block_desc *blocks, const snac_options *opt) {
+  if (!c || !blocks) { set_error("snac_init: null argument"); return SNAC_ERR_ARG; }
+  snac_finalize();
+  auto *d = new Domain();
+  if (opt) d->opt = *opt;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { delete d; set_error("no CUDA device"); return SNAC_ERR_CUDA; }
+  if (cudaSetDevice(d->opt.device) != cudaSuccess) { delete d; set_error("cannot select device %d", d->opt.device); return SNAC_ERR_CUDA; }
+  int rc = build_domain(*d, c, blocks);
+  if (rc == SNAC_OK) rc = upload_domain(*d);
+  if (rc == SNAC_OK) {
+    d->ps.reset(new PoissonSolver());
+    rc = solver_create(*d, *d->ps);
+  }
+  if (rc != SNAC_OK) { delete d; return rc; }
+  g_dom = d;
+  return SNAC_OK;
+}
+
+int snac_check_case(const snac_case *c, const snac_block_desc *blocks, int *levels, long *coarse_cells) {
+  if (!c || !blocks) { set_error("snac_check_case: null argument"); return SNAC_ERR_ARG; }
+  Domain d;
+  SNAC_TRY(build_domain(d, c, blocks));
+  PoissonSolver S;
+  SNAC_TRY(solver_create(d, S, false));
+  if (levels) *levels = S.host_levels;
+  if (coarse_cells) *coarse_cells = S.host_coarse_cells;
+  return SNAC_OK;
+}
+
+int snac_finalize(void) {
+  if (g_dom) {
+    cudaDeviceSynchronize();
+    delete g_dom;
+    g_dom = nullptr;
+  }
+  return SNAC_OK;
+}
+
+int snac_block_geometry(int ib, int lo[3], int hi[3], int nb[3][2], int is_bound[3][2]) {
+  NEED_DOMAIN
+  if (ib < 0 || ib >= d->nblocks) { set_error("block index out of range"); return SNAC_ERR_ARG; }
+  const HostBlock &H = d->hb[ib];
+  for (int a = 0; a < 3; a++) {
+    lo[a] = H.lo[a]; hi[a] = H.hi[a];
+    for (int s = 0; s < 2; s++) { nb[a][s] = H.nb[a][s]; is_bound[a][s] = H.is_bound[a][s]; }
+  }
+  return SNAC_OK;
+}
+
+int snac_get_grid(int ib, int axis, int which, double *out) {
+  NEED_DOMAIN
+  if (ib < 0 || ib >= d->nblocks || axis < 0 || axis > 2 || which < 0 || which > 3) { set_error("bad grid request"); return SNAC_ERR_ARG; }
+  const auto &g = d->hb[ib].g[axis][which];
+  std::copy(g.begin(), g.end(), out);
+  return SNAC_OK;
+}
+
+double snac_vol_all(void) { return domain() ? domain()->vol_all : 0.0; }
+
+int snac_set_field(int ib, int field, const double *host) {
+  NEED_DOMAIN
+  double *p; size_t bytes;
+  SNAC_TRY(field_ptr(*d, ib, field, &p, &bytes));
+  SNAC_CUDA(cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, d->st));
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  return SNAC_OK;
+}
+
+int snac_get_field(int ib, int field, double *host) {
+  NEED_DOMAIN
+  double *p; size_t bytes;
+  SNAC_TRY(field_ptr(*d, ib, field, &p, &bytes));
+  SNAC_CUDA(cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, d->st));
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  return SNAC_OK;
+}
+
+int snac_rk_mom_all(int irk) {
+  NEED_DOMAIN
+  if (irk < 0 || irk > 2) { set_error("irk must be 0..2"); return SNAC_ERR_ARG; }
+  SNAC_TRY(rk_mom_all(*d, irk));
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  return SNAC_OK;
+}
+int snac_bounduvw_all(int is_correc) {
+  NEED_DOMAIN
+  SNAC_TRY(bound_uvw(*d, is_correc));
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  return SNAC_OK;
+}
+int snac_boundp_all(int field) {
+  NEED_DOMAIN
+  if (field != SNAC_P && field != SNAC_PP) { set_error("snac_boundp_all: field must be SNAC_P or SNAC_PP"); return SNAC_ERR_ARG; }
+  SNAC_TRY(bound_p(*d, field));
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  return SNAC_OK;
+}
+int snac_fillps_all(double dtrk) {
+  NEED_DOMAIN
+  SNAC_TRY(launch_fillps(d->d_db, d->d_tiles, d->ntiles, dtrk, d->c.fft_axis, d->st));
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  return SNAC_OK;
+}
+int snac_updt_rhs_all(void) {
+  NEED_DOMAIN
+  SNAC_TRY(updt_rhs_all(*d));
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  return SNAC_OK;
+}
+int snac_solve_pressure(void) {
+  NEED_DOMAIN
+  const int rc = solver_solve_pressure(*d, *d->ps);
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  return rc;
+}
+int snac_correc_all(double dtrk) {
+  NEED_DOMAIN
+  SNAC_TRY(launch_correc(d->d_db, d->d_tiles_halo, d->ntiles_halo, dtrk, d->st));
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  return SNAC_OK;
+}
+int snac_updt_pressure_all(double alpha) {
+  NEED_DOMAIN
+  SNAC_TRY(launch_updt_pressure(d->d_db, d->d_tiles, d->ntiles, alpha, d->c.impdiff, d->st));
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  return SNAC_OK;
+}
+int snac_chkdt_all(double *dt_cfl) {
+  NEED_DOMAIN
+  return chkdt_all(*d, dt_cfl);
+}
+int snac_chkdiv_all(double *divtot, double *divmax) {
+  NEED_DOMAIN
+  double r[2];
+  SNAC_TRY(reduce(*d, 1, r));
+  *divtot = r[0];
+  *divmax = r[1];
+  if (std::isinf(r[1]) || r[0] != r[0]) { set_error("chkdiv: non-finite divergence"); return SNAC_ERR_NAN; }
+  return SNAC_OK;
+}
+int snac_kinetic_energy(double *ke) {
+  NEED_DOMAIN
+  double r[2];
+  SNAC_TRY(reduce(*d, 2, r));
+  *ke = 0.5 * r[0] / d->vol_all;
+  return SNAC_OK;
+}
+
+int snac_step(int nsteps) {
+  NEED_DOMAIN
+  if (d->dt == 0.0) SNAC_TRY(set_dt_from_cfl(*d));
+  int rc_all = SNAC_OK;
+  if (!d->ev0) {
+    SNAC_CUDA(cudaEventCreate(&d->ev0));
+    SNAC_CUDA(cudaEventCreate(&d->ev1));
+  }
+  SNAC_CUDA(cudaEventRecord(d->ev0, d->st));
+  for (int s = 0; s < nsteps; s++) {
+    d->istep++;
+    d->time += d->dt;
+    d->last_solve_iters = 0;
+    d->last_solve_res = 0.0;
+    d->solves = 0;
+    for (int irk = 0; irk < 3; irk++) {
+      const int rc = one_stage(*d, irk);
+      if (rc == SNAC_ERR_NOT_CONVERGED) rc_all = rc;
+      else if (rc != SNAC_OK) return rc;
+    }
+    if (d->c.icheck > 0 && d->istep % d->c.icheck == 0) SNAC_TRY(set_dt_from_cfl(*d));
+  }
+  SNAC_CUDA(cudaEventRecord(d->ev1, d->st));
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  float ms = 0.f;
+  SNAC_CUDA(cudaEventElapsedTime(&ms, d->ev0, d->ev1));
+  d->device_ms = ms;
+  return rc_all;
+}
+
+int snac_get_stats(snac_step_stats *st) {
+  NEED_DOMAIN
+  st->istep = d->istep;
+  st->time = d->time;
+  st->dt = d->dt;
+  st->solve_iters_max = d->last_solve_iters;
+  st->solve_residual_max = d->last_solve_res;
+  st->solves = d->solves;
+  st->device_ms = d->device_ms;
+  return SNAC_OK;
+}
+int snac_set_dt(double dt) {
+  NEED_DOMAIN
+  d->dt = dt;
+  return SNAC_OK;
+}
+int snac_get_dt(double *dt) {
+  NEED_DOMAIN
+  *dt = d->dt;
+  return SNAC_OK;
+}
+
+}  // extern "C"

@@ -22,6 +22,18 @@ void set_error(const char *fmt, ...) {
   g_err = buf;
 }
 
+void trace(const char *what, cudaStream_t st) {
+  static int on = -1;
+  if (on < 0) {
+    const char *e = getenv("SNAC_DEBUG");
+    on = (e && e[0] && e[0] != '0') ? 1 : 0;
+  }
+  if (!on) return;
+  cudaError_t e = cudaStreamSynchronize(st);
+  fprintf(stderr, "[snac] %s: %s\n", what, cudaGetErrorString(e));
+  fflush(stderr);
+}
+
 int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
   set_error("CUDA error %s (%d) in %s at %s:%d", cudaGetErrorString(e), (int)e, what, file, line);
   return SNAC_ERR_CUDA;
@@ -283,22 +295,22 @@ int snac_rk_scal(const double rkpar[2], const int lo[3], const int hi[3], const 
   prm.ssource = ssource;
   prm.impdiff = impdiff;
   prm.sidx = 0;
-  SNAC_TRY(launch_rk_scal(ob.dblk, ob.dtiles, ob.ntiles, prm, 0));
+  // bulk_mean_s (scal.f90:156-179) is fused into the update kernel as per-tile partial sums
+  double *part = nullptr, *res = nullptr, r[2] = {0.0, 0.0};
+  if (is_forced && f) {
+    SNAC_TRY(ob.scratch((size_t)ob.ntiles * 2 * sizeof(double), &part));
+    SNAC_TRY(ob.scratch(2 * sizeof(double), &res));
+  }
+  SNAC_TRY(launch_rk_scal(ob.dblk, ob.dtiles, ob.ntiles, prm, part, 0));
   SNAC_TRY(launch_rk_scal_writeback(ob.dblk, ob.dtiles, ob.ntiles, 0, 0));
+  if (part) {
+    SNAC_TRY(launch_reduce_final(part, ob.ntiles, res, 0));
+    SNAC_CUDA(cudaMemcpy(r, res, 2 * sizeof(double), cudaMemcpyDeviceToHost));
+  }
   SNAC_CUDA(cudaDeviceSynchronize());
   SNAC_TRY(S.finish());
   SNAC_TRY(RS.finish());
-  if (f) *f = 0.0;
-  if (is_forced && f) {
-    // bulk_mean_s (scal.f90:156-179) of the updated scalar, on the device
-    double *part = nullptr, *res = nullptr, r[2];
-    SNAC_TRY(ob.scratch((size_t)ob.ntiles * 2 * sizeof(double), &part));
-    SNAC_TRY(ob.scratch(2 * sizeof(double), &res));
-    SNAC_TRY(launch_bulk_partial(ob.dblk, ob.dtiles, ob.ntiles, 0, part, 0));
-    SNAC_TRY(launch_reduce_final(part, ob.ntiles, res, 0));
-    SNAC_CUDA(cudaMemcpy(r, res, 2 * sizeof(double), cudaMemcpyDeviceToHost));
-    *f = scalf - r[0] / vol_all;
-  }
+  if (f) *f = (is_forced ? scalf - r[0] / vol_all : 0.0);
   return SNAC_OK;
 }
 

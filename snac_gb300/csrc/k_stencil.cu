@@ -10,6 +10,7 @@
 // One CTA covers one TX x TY x TZ tile of one block (tile lists make uneven
 // multi-block layouts a single launch).
 #include "snac_internal.h"
+#include "snac_prof.h"
 
 namespace snac {
 
@@ -132,7 +133,9 @@ k_rk_mom_writeback(const DBlock *__restrict__ Bs, const Tile *__restrict__ T) {
 
 int launch_rk_mom(const DBlock *dB, const Tile *dT, int ntiles, const RkMomParams &prm, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
+  prof_begin(KID_RK_MOM, st);
   k_rk_mom<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, prm);
+  prof_end(KID_RK_MOM, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -145,9 +148,20 @@ int launch_rk_mom_writeback(const DBlock *dB, const Tile *dT, int ntiles, cudaSt
 
 // ---------------------------------------------------------------- rk_scal
 // rk.f90:130-204 with scal_d (scal.f90:89-121) and scal_a (scal.f90:123-154)
+template <int OP>
+__device__ inline void tile_reduce(double s, double m, double *part);
+
+// `part` (optional): per-tile sums of s*dxf*dyf*dzf of the updated scalar before the
+// IMPDIFF correction -- the bulk mean of rk.f90:185-189, which precedes rk.f90:196-202.
 __global__ void __launch_bounds__(TX * TY * TZ)
-k_rk_scal(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, RkScalParams prm) {
-  TILE_SETUP
+k_rk_scal(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, RkScalParams prm, double *part) {
+  const Tile t = T[blockIdx.x];
+  const DBlock &B = Bs[t.x];
+  const int nx = B.n[0], ny = B.n[1], nz = B.n[2];
+  const int i = t.y + (int)threadIdx.x, j = t.z + (int)threadIdx.y, k = t.w + (int)threadIdx.z;
+  const bool valid = i < nx && j < ny && k < nz;
+  double msum = 0.0;
+  if (valid) {
   const long sy = nx + 2, sz = (long)(nx + 2) * (ny + 2);
   const long c = hidx(i, j, k, nx, ny), ci = iidx(i, j, k, nx, ny);
   const double *__restrict__ s = B.s[prm.sidx];
@@ -168,8 +182,11 @@ k_rk_scal(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, RkScalParam
   double sn = fma(prm.f12, prm.ssource, fma(prm.f2, ro[ci], fma(prm.f1, r, s0)));
   if (prm.impdiff) sn = fma(prm.f12, rd, sn);
   ro[ci] = r;
+  msum = sn * AX(B, 0, AX_DF, i) * AX(B, 1, AX_DF, j) * AX(B, 2, AX_DF, k);
   if (prm.impdiff) sn = fma(-0.5 * prm.f12, rd, sn);
   B.ns[ci] = sn;
+  }
+  if (part) tile_reduce<4>(msum, 0.0, part);
 }
 
 __global__ void __launch_bounds__(TX * TY * TZ)
@@ -178,9 +195,10 @@ k_rk_scal_writeback(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, i
   B.s[sidx][hidx(i, j, k, nx, ny)] = B.ns[iidx(i, j, k, nx, ny)];
 }
 
-int launch_rk_scal(const DBlock *dB, const Tile *dT, int ntiles, const RkScalParams &prm, cudaStream_t st) {
+int launch_rk_scal(const DBlock *dB, const Tile *dT, int ntiles, const RkScalParams &prm, double *part,
+                   cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
-  k_rk_scal<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, prm);
+  k_rk_scal<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, prm, part);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -211,7 +229,9 @@ k_fillps(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, double rdt, 
 
 int launch_fillps(const DBlock *dB, const Tile *dT, int ntiles, double dt, int fft_axis, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
+  prof_begin(KID_FILLPS, st);
   k_fillps<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, 1.0 / dt, fft_axis);
+  prof_end(KID_FILLPS, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -235,7 +255,9 @@ k_correc(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, double dt) {
 
 int launch_correc(const DBlock *dB, const Tile *dT, int ntiles, double dt, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
+  prof_begin(KID_CORREC, st);
   k_correc<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, dt);
+  prof_end(KID_CORREC, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

@@ -1,0 +1,131 @@
+// snac_host.h -- host-side state of snac_gb300 (not part of the C ABI).
+#pragma once
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "snac_bound.h"
+#include "snac_mgk.h"
+#include "snac_solver.h"
+
+namespace snac {
+
+// device view of one host argument of a reference-signature call
+struct ArgArray {
+  const void *host = nullptr;
+  void *dev = nullptr;
+  size_t bytes = 0;
+  bool owned = false, copy_out = false;
+  int bind(const void *h, size_t nbytes, bool in, bool out);
+  int finish();
+  ~ArgArray();
+};
+
+// one block given by reference arguments (lo, hi, metric arrays)
+struct OneBlock {
+  DBlock hb{};
+  DBlock *dblk = nullptr;
+  double *dax = nullptr;
+  Tile *dtiles = nullptr;
+  int ntiles = 0;
+  std::vector<void *> temps;
+  int setup(const int lo[3], const int hi[3], const double *dxc, const double *dxf, const double *dyc,
+            const double *dyf, const double *dzc, const double *dzf, bool halo_tiles);
+  int upload();
+  int scratch(size_t bytes, double **p);
+  size_t halo_bytes() const;
+  size_t interior_bytes() const;
+  ~OneBlock();
+};
+
+std::vector<double> axis_tables(const double *dc, const double *df, int n);
+
+// set-up results for one block (initmpi + initgrid + bound_grid + init_bc_rhs)
+struct HostBlock {
+  int ng[3], lo[3], hi[3];
+  int nb[3][2], is_bound[3][2];
+  snac_block_desc desc;
+  std::vector<double> g[3][4];   // per axis: dc, df, c, f over lo-1..hi+1
+  std::vector<double> rhsp[3];   // pressure BC planes
+  std::vector<double> dl[3];     // dl(0:1,idir) of main.f90:725-727
+};
+
+// the device multigrid problem plus its host-side construction data
+struct PoissonSolver {
+  int mode3d = 0, ax[3] = {0, 1, 2}, periodic[3] = {0, 0, 0}, nsys = 1, lo_min[3] = {0, 0, 0};
+  int fft_axis = 0, nfft = 0, kind_fwd = -1, kind_bwd = -1;
+  double normfft = 1.0;
+  int use_fft = 0;                   // 1: radix-2 FFT path for R2HC/HC2R; 0: dense r2r matrices
+  double *d_tw = nullptr;            // FFT twiddles exp(-2 pi i k/n), k < n/2 (complex)
+  double *d_mat_fwd = nullptr, *d_mat_bwd = nullptr;  // dense r2r matrices (n x n)
+  std::vector<double> lambda;
+  int precision = 0;
+  double tol = 1e-12;
+  int maxiter = 200;
+  MgProblem P{};
+  long ncell0 = 0, nact0 = 0;
+  double *box_b = nullptr, *box_x = nullptr;  // rhs, solution / warm start (po)
+  CgWork W64{}, W32{};
+  int *active_outer = nullptr;
+  SysScal *sc_outer = nullptr;
+  double *r64 = nullptr;
+  float *box_b32 = nullptr, *box_e32 = nullptr;
+  std::vector<void *> allocs;
+  int last_iters = 0;
+  double last_res = 0.0;
+  int host_levels = 0;
+  long host_coarse_cells = 0;
+  ~PoissonSolver();
+  void *alloc(size_t bytes);
+};
+
+struct Domain {
+  snac_case c{};
+  snac_options opt{};
+  int nblocks = 0;
+  std::vector<HostBlock> hb;
+  int periods[3] = {0, 0, 0}, is_periodic[3] = {0, 0, 0};
+  double vol_all = 0.0;
+  std::vector<DBlock> db;
+  DBlock *d_db = nullptr;
+  Tile *d_tiles = nullptr, *d_tiles_halo = nullptr;
+  int ntiles = 0, ntiles_halo = 0;
+  FaceLink *d_links[3] = {nullptr, nullptr, nullptr};
+  int nlinks[3] = {0, 0, 0}, maxplane[3] = {0, 0, 0};
+  // boundary-condition tables: [kind][axis]; kinds 0 bounduvw, 1 bounduvw(is_correc), 2 p, 3 pp, 4+s scalar s
+  BcEntry *d_bc[4 + SNAC_MAX_SCAL][3] = {};
+  int nbc[4 + SNAC_MAX_SCAL][3] = {};
+  int *d_flds = nullptr;             // field lists: [0..2] = u,v,w; [3] = p; [4] = pp; [5+s] = scalar s
+  double *d_rhsp = nullptr;          // concatenated pressure BC planes
+  std::vector<size_t> rhsp_off;      // per block: offsets of x,y,z planes
+  double *d_part = nullptr, *d_red = nullptr, *h_red = nullptr;
+  std::unique_ptr<PoissonSolver> ps;
+  double dt = 0.0, time = 0.0;
+  int istep = 0;
+  int last_solve_iters = 0, solves = 0;
+  double last_solve_res = 0.0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double device_ms = 0.0;
+  std::vector<void *> allocs;
+  void *alloc(size_t bytes);
+  ~Domain();
+};
+
+Domain *domain();
+int solver_create(Domain &d, PoissonSolver &S, bool upload = true);
+int solver_solve_pressure(Domain &d, PoissonSolver &S);
+
+// transforms (k_fft.cu)
+int fft_forward_to_box(Domain &d, PoissonSolver &S, cudaStream_t st);
+int fft_backward_from_box(Domain &d, PoissonSolver &S, cudaStream_t st);
+int box_gather(Domain &d, PoissonSolver &S, cudaStream_t st);
+int box_scatter(Domain &d, PoissonSolver &S, cudaStream_t st);
+int r2r_array(int kind, int idir, const int nn[3], int q, double *darr, cudaStream_t st);
+std::vector<double> r2r_matrix(int kind, int n);
+void find_fft(char a, char b, int is_centered, int *kf, int *kb, double norm[2]);
+int eigenvalues(int n, char a, char b, int is_centered, double *lambda);
+void initgrid(int lo, int hi, int gt, double gr, double lmin, double lmax, double *drc, double *drf, double *rc,
+              double *rf);
+
+}  // namespace snac

@@ -13,6 +13,8 @@ namespace snac {
 
 void set_error(const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+// SNAC_DEBUG=1 in the environment: every traced phase syncs the device and logs to stderr
+void trace(const char *what, cudaStream_t st);
 
 #define SNAC_CUDA(x)                                                      \
   do {                                                                    \
@@ -85,7 +87,8 @@ struct RkScalParams {
 // kernel launchers (k_stencil.cu)
 int launch_rk_mom(const DBlock *dB, const Tile *dT, int ntiles, const RkMomParams &prm, cudaStream_t st);
 int launch_rk_mom_writeback(const DBlock *dB, const Tile *dT, int ntiles, cudaStream_t st);
-int launch_rk_scal(const DBlock *dB, const Tile *dT, int ntiles, const RkScalParams &prm, cudaStream_t st);
+int launch_rk_scal(const DBlock *dB, const Tile *dT, int ntiles, const RkScalParams &prm, double *part,
+                   cudaStream_t st);
 int launch_rk_scal_writeback(const DBlock *dB, const Tile *dT, int ntiles, int sidx, cudaStream_t st);
 int launch_fillps(const DBlock *dB, const Tile *dT, int ntiles, double dt, int fft_axis, cudaStream_t st);
 int launch_correc(const DBlock *dB, const Tile *dT, int ntiles, double dt, cudaStream_t st);

@@ -1,0 +1,48 @@
+// snac_solver.h -- batched multigrid solver and transforms (device side).
+//
+// The linear systems are the ones solver.f90 assembles for HYPRE
+// (init_matrix_3d, init_matrix_2d + init_n_2d_matrices): all blocks placed in
+// the global index space of initmpi.f90:50-103, which is the solver "box"
+// (cells outside every block are inactive).  In plane mode (FFT_AXIS set) the
+// box holds one 2-D system per wavenumber, stored [system][i1][i0], i0 fastest;
+// in 3-D mode it holds one system [i2][i1][i0].
+#pragma once
+#include "snac_internal.h"
+
+namespace snac {
+
+constexpr int MG_MAXLEV = 16;
+constexpr int MG_DENSE_MAX = 256;    // coarsest level solved with a dense inverse when it has at most this many cells
+constexpr int MG_CHUNK = 256;        // cells of one system per CTA in level-0 vector kernels
+
+// one multigrid level, device pointers; real-typed arrays exist in FP64 and FP32
+struct MgLevelD {
+  int n[3];
+  long ncell;
+  int coarsened[3];                  // axes halved from the previous (finer) level
+  const unsigned short *code;        // per cell: bit 15 inactive; bits (2*(2a+s)).. fold type of face (a,s)
+  const double *cc, *cp[3], *W[3];
+  const float *ccf, *cpf[3], *Wf[3];
+  double *x, *b, *r;                 // ncell*nsys, FP64 path
+  float *xf, *bf, *rf;               // ncell*nsys, FP32 path
+  const double *dinv;                // coarsest: ncell^2 per system
+  const float *dinvf;
+};
+
+struct MgProblem {
+  int mode3d;
+  int periodic[3];
+  int nsys;
+  int nlev;
+  int nu;
+  MgLevelD L[MG_MAXLEV];
+  const double *shift;               // per system (lambda_k), device
+  const float *shiftf;
+  const int *singular;               // per system, device
+};
+
+// kernels (k_mg.cu) -- T = double or float
+template <typename T> int mg_vcycle(const MgProblem &P, int l, const int *active, cudaStream_t st);
+template <typename T> int mg_apply(const MgProblem &P, const T *x, T *y, double *part, const int *active, cudaStream_t st);
+
+}  // namespace snac

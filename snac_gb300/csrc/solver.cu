@@ -1,0 +1,578 @@
+// solver.cu -- set-up and driver of the batched Poisson/Helmholtz solve.
+//
+// Assembly follows solver.f90:158-372 (init_matrix_3d) and 687-842 + 981-1020
+// (init_matrix_2d, init_n_2d_matrices): 7- or 5-point operators weighted by the
+// cell volume/area, boundary folding with sgn = +1 (N), -1 (centred D),
+// 0 (staggered D), and lambda(k)*dl1_2*dl2_2 on the diagonal of wavenumber k.
+// The hierarchy is built here once: axes are halved only where every block
+// keeps an even extent and offset and where the coupling is strong
+// (semicoarsening as PFMG does); coarse operators are rediscretised from the
+// summed cell widths; the coarsest level is inverted densely per system.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "snac_host.h"
+
+namespace snac {
+
+int fft_setup(PoissonSolver &S);
+void forget_fft_tables(const PoissonSolver *S);
+
+void *PoissonSolver::alloc(size_t bytes) {
+  void *p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+  cudaMemset(p, 0, bytes);
+  allocs.push_back(p);
+  return p;
+}
+PoissonSolver::~PoissonSolver() {
+  forget_fft_tables(this);
+  for (void *p : allocs) cudaFree(p);
+  if (W64.h_count) cudaFreeHost(W64.h_count);
+  if (W32.h_count) cudaFreeHost(W32.h_count);
+}
+
+namespace {
+
+struct HLevel {
+  int n[3] = {1, 1, 1};
+  long ncell = 1;
+  int coarsened[3] = {0, 0, 0};
+  std::vector<double> W[3];
+  std::vector<unsigned short> code;
+  std::vector<double> cc, cp[3];
+  std::vector<double> dinv;
+};
+
+inline int fold_type(char cbc, int centered) {
+  if (cbc == 'N') return 1;
+  if (cbc == 'D') return centered ? 2 : 3;
+  return 0;
+}
+inline double fold_sgn(int t) { return t == 1 ? 1.0 : (t == 2 ? -1.0 : 0.0); }
+
+struct Builder {
+  PoissonSolver &S;
+  std::vector<HLevel> L;
+  int na;
+  explicit Builder(PoissonSolver &s) : S(s), na(s.mode3d ? 3 : 2) {}
+
+  long nbr(const HLevel &l, int i, int j, int k, int a, int s) const {
+    int c[3] = {i, j, k};
+    c[a] += s ? 1 : -1;
+    if (c[a] < 0 || c[a] >= l.n[a]) {
+      if (!S.periodic[a]) return -1;
+      c[a] = c[a] < 0 ? c[a] + l.n[a] : c[a] - l.n[a];
+    }
+    return c[0] + (long)l.n[0] * (c[1] + (long)l.n[1] * c[2]);
+  }
+
+  void alloc_level(HLevel &l) {
+    l.ncell = (long)l.n[0] * l.n[1] * l.n[2];
+    for (int a = 0; a < 3; a++) { l.W[a].assign(l.n[a], 0.0); l.cp[a].assign(l.ncell, 0.0); }
+    l.code.assign(l.ncell, 0x8000);
+    l.cc.assign(l.ncell, 0.0);
+  }
+
+  // rediscretised operator of a coarse level
+  void coarse_operator(HLevel &l, double alpha) {
+    for (int k = 0; k < l.n[2]; k++)
+      for (int j = 0; j < l.n[1]; j++)
+        for (int i = 0; i < l.n[0]; i++) {
+          const long c = i + (long)l.n[0] * (j + (long)l.n[1] * k);
+          const int idx[3] = {i, j, k};
+          for (int a = 0; a < 3; a++) l.cp[a][c] = 0.0;
+          l.cc[c] = 0.0;
+          if (l.code[c] & 0x8000) continue;
+          double weight = 1.0;
+          for (int a = 0; a < na; a++) weight *= l.W[a][idx[a]];
+          double cm[3] = {0, 0, 0}, cpv[3] = {0, 0, 0}, sum = 0.0;
+          for (int a = 0; a < na; a++) {
+            if (S.periodic[a] && l.n[a] == 1) continue;
+            double wt = 1.0;
+            for (int b = 0; b < na; b++)
+              if (b != a) wt *= l.W[b][idx[b]];
+            const int n = l.n[a], q = idx[a];
+            const double Wq = l.W[a][q];
+            const double Wm = q > 0 ? l.W[a][q - 1] : (S.periodic[a] ? l.W[a][n - 1] : Wq);
+            const double Wp = q < n - 1 ? l.W[a][q + 1] : (S.periodic[a] ? l.W[a][0] : Wq);
+            const int tm = (l.code[c] >> (2 * (2 * a))) & 3, tp = (l.code[c] >> (2 * (2 * a + 1))) & 3;
+            const double dm = tm ? Wq : 0.5 * (Wm + Wq);
+            const double dp = tp ? Wq : 0.5 * (Wq + Wp);
+            cm[a] = 1.0 / dm * wt;
+            cpv[a] = 1.0 / dp * wt;
+            sum += cm[a] + cpv[a];
+          }
+          double cc = -sum + alpha * weight;
+          for (int a = 0; a < na; a++) {
+            const int tm = (l.code[c] >> (2 * (2 * a))) & 3, tp = (l.code[c] >> (2 * (2 * a + 1))) & 3;
+            if (tm) { cc += fold_sgn(tm) * cm[a]; cm[a] = 0; }
+            if (tp) { cc += fold_sgn(tp) * cpv[a]; cpv[a] = 0; }
+            l.cp[a][c] = cpv[a];
+          }
+          l.cc[c] = cc;
+        }
+  }
+
+  double diag(const HLevel &l, long c, int i, int j, int s) const {
+    if (S.mode3d) return l.cc[c];
+    return l.cc[c] + S.lambda[s] * l.W[0][i] * l.W[1][j];
+  }
+
+  // dense inverse of the coarsest operator of system s (Cholesky of -A, +11^T when singular)
+  bool dense(const HLevel &l, int s, bool singular, double *M) const {
+    const long n = l.ncell;
+    std::vector<double> A((size_t)n * n, 0.0);
+    for (int k = 0; k < l.n[2]; k++)
+      for (int j = 0; j < l.n[1]; j++)
+        for (int i = 0; i < l.n[0]; i++) {
+          const long c = i + (long)l.n[0] * (j + (long)l.n[1] * k);
+          if (l.code[c] & 0x8000) continue;
+          A[c * n + c] -= diag(l, c, i, j, s);
+          for (int a = 0; a < na; a++) {
+            if (S.periodic[a] && l.n[a] == 1) continue;
+            const long p = nbr(l, i, j, k, a, 1), m = nbr(l, i, j, k, a, 0);
+            if (p >= 0) A[c * n + p] -= l.cp[a][c];
+            if (m >= 0) A[c * n + m] -= l.cp[a][m];
+          }
+        }
+    long nact = 0;
+    double dsum = 0.0;
+    for (long c = 0; c < n; c++) {
+      if (l.code[c] & 0x8000) { A[c * n + c] = 1.0; continue; }
+      nact++;
+      dsum += A[c * n + c];
+    }
+    if (singular && nact > 0) {
+      const double sh = dsum / nact;
+      for (long r = 0; r < n; r++)
+        for (long c = 0; c < n; c++)
+          if (!(l.code[r] & 0x8000) && !(l.code[c] & 0x8000)) A[r * n + c] += sh;
+    }
+    for (long j = 0; j < n; j++) {
+      double d = A[j * n + j];
+      for (long k = 0; k < j; k++) d -= A[j * n + k] * A[j * n + k];
+      if (d <= 0.0) return false;
+      d = std::sqrt(d);
+      A[j * n + j] = d;
+      for (long i = j + 1; i < n; i++) {
+        double v = A[i * n + j];
+        for (long k = 0; k < j; k++) v -= A[i * n + k] * A[j * n + k];
+        A[i * n + j] = v / d;
+      }
+    }
+    std::vector<double> e(n);
+    for (long c = 0; c < n; c++) {
+      std::fill(e.begin(), e.end(), 0.0);
+      e[c] = 1.0;
+      for (long i = 0; i < n; i++) { double v = e[i]; for (long k = 0; k < i; k++) v -= A[i * n + k] * e[k]; e[i] = v / A[i * n + i]; }
+      for (long i = n - 1; i >= 0; i--) { double v = e[i]; for (long k = i + 1; k < n; k++) v -= A[k * n + i] * e[k]; e[i] = v / A[i * n + i]; }
+      for (long r = 0; r < n; r++) M[r * n + c] = ((l.code[r] & 0x8000) || (l.code[c] & 0x8000)) ? 0.0 : -e[r];
+    }
+    return true;
+  }
+};
+
+}  // namespace
+
+// build the box problem of the pressure (centred in every direction, alpha = 0)
+int solver_create(Domain &d, PoissonSolver &S, bool upload) {
+  const snac_case &c = d.c;
+  S.precision = d.opt.precision;
+  S.tol = c.tol;
+  S.maxiter = c.maxiter;
+  S.fft_axis = c.fft_axis;
+  S.mode3d = c.fft_axis == 0;
+  if (S.mode3d) { S.ax[0] = 0; S.ax[1] = 1; S.ax[2] = 2; }
+  else {
+    const int idir = c.fft_axis - 1;
+    S.ax[0] = idir == 0 ? 1 : 0;
+    S.ax[1] = idir == 2 ? 1 : 2;
+    S.ax[2] = idir;
+  }
+  int lo_min[3], hi_max[3];
+  for (int p = 0; p < 3; p++) {
+    lo_min[p] = d.hb[0].lo[p];
+    hi_max[p] = d.hb[0].hi[p];
+    for (int b = 1; b < d.nblocks; b++) {
+      lo_min[p] = std::min(lo_min[p], d.hb[b].lo[p]);
+      hi_max[p] = std::max(hi_max[p], d.hb[b].hi[p]);
+    }
+    S.lo_min[p] = lo_min[p];
+  }
+  Builder B(S);
+  const int na = B.na;
+  B.L.reserve(MG_MAXLEV);  // levels are appended below while references to level 0 are held
+  B.L.resize(1);
+  HLevel &L0 = B.L[0];
+  for (int a = 0; a < 3; a++) {
+    const int p = S.ax[a];
+    L0.n[a] = a < na ? hi_max[p] - lo_min[p] + 1 : 1;
+    S.periodic[a] = a < na ? (d.periods[p] != 0) : 0;
+  }
+  if (!S.mode3d) {
+    const int pf = S.ax[2];
+    S.nsys = hi_max[pf] - lo_min[pf] + 1;
+    for (int b = 0; b < d.nblocks; b++)
+      if (d.hb[b].lo[pf] != lo_min[pf] || d.hb[b].hi[pf] != hi_max[pf]) {
+        set_error("every block must span the whole transform direction");
+        return SNAC_ERR_UNSUPPORTED;
+      }
+    // fft.f90 set-up: kinds, normfft (fftini, fft.f90:68), eigenvalues/dl^2 (init_fft_reduction)
+    S.nfft = S.nsys;
+    double norm[2];
+    const char *bc = d.hb[0].desc.cbcpre[pf];
+    find_fft(bc[0], bc[1], 1, &S.kind_fwd, &S.kind_bwd, norm);
+    if (S.kind_fwd < 0) { set_error("unsupported boundary pair along the transform direction"); return SNAC_ERR_UNSUPPORTED; }
+    S.normfft = 1.0 / (norm[0] * (S.nfft + norm[1] - 0));
+    S.lambda.assign(S.nfft, 0.0);
+    if (eigenvalues(S.nfft, bc[0], bc[1], 1, S.lambda.data())) {
+      set_error("no eigenvalues for this boundary pair (the reference defines none)");
+      return SNAC_ERR_UNSUPPORTED;
+    }
+    const double dl0 = d.hb[0].dl[pf][0];
+    for (auto &v : S.lambda) v = v / (dl0 * dl0);
+    if (upload) SNAC_TRY(fft_setup(S));
+  } else {
+    S.nsys = 1;
+    S.lambda.assign(1, 0.0);
+  }
+  B.alloc_level(L0);
+  const double alpha = 0.0;
+  const int centered[3] = {1, 1, 1};
+  std::vector<double> cmv_all[3];
+  for (int a = 0; a < 3; a++) cmv_all[a].assign(L0.ncell, 0.0);
+  std::vector<char> have[3];
+  for (int a = 0; a < 3; a++) have[a].assign(L0.n[a], 0);
+  for (int b = 0; b < d.nblocks; b++) {
+    const HostBlock &H = d.hb[b];
+    const double *d1[3], *d2[3];
+    int q3[3];
+    for (int p = 0; p < 3; p++) {
+      d1[p] = centered[p] ? H.g[p][0].data() : H.g[p][1].data();
+      d2[p] = centered[p] ? H.g[p][1].data() : H.g[p][0].data();
+      q3[p] = centered[p] ? 0 : 1;
+    }
+    auto LOC = [&](int p, int g) { return g - H.lo[p] + 1; };
+    int loc[3], hic[3];
+    for (int a = 0; a < 3; a++) {
+      const int p = S.ax[a];
+      loc[a] = a < na ? H.lo[p] : 0;
+      hic[a] = a < na ? H.hi[p] : 0;
+    }
+    for (int g2 = loc[2]; g2 <= hic[2]; g2++)
+      for (int g1 = loc[1]; g1 <= hic[1]; g1++)
+        for (int g0 = loc[0]; g0 <= hic[0]; g0++) {
+          const int gg[3] = {g0, g1, g2};
+          int idx[3];
+          for (int a = 0; a < 3; a++) idx[a] = a < na ? gg[a] - lo_min[S.ax[a]] : 0;
+          const long cidx = idx[0] + (long)L0.n[0] * (idx[1] + (long)L0.n[1] * idx[2]);
+          if (!(L0.code[cidx] & 0x8000)) { set_error("overlapping blocks in the solver box"); return SNAC_ERR_ARG; }
+          for (int a = 0; a < na; a++) {
+            const int p = S.ax[a];
+            const double wv = d2[p][LOC(p, gg[a])];
+            if (have[a][idx[a]] && L0.W[a][idx[a]] != wv) {
+              set_error("inconsistent grid spacing along axis %d at global index %d", p + 1, gg[a]);
+              return SNAC_ERR_ARG;
+            }
+            L0.W[a][idx[a]] = wv;
+            have[a][idx[a]] = 1;
+          }
+          double weight, cmv[3] = {0, 0, 0}, cpv[3] = {0, 0, 0}, cc;
+          if (S.mode3d) {
+            const double dx2 = d2[0][LOC(0, g0)], dy2 = d2[1][LOC(1, g1)], dz2 = d2[2][LOC(2, g2)];
+            weight = dx2 * dy2 * dz2;
+            cmv[0] = 1.0 / (d1[0][LOC(0, g0 - 1 + q3[0])]) * dy2 * dz2;
+            cpv[0] = 1.0 / (d1[0][LOC(0, g0 + q3[0])]) * dy2 * dz2;
+            cmv[1] = 1.0 / (d1[1][LOC(1, g1 - 1 + q3[1])]) * dx2 * dz2;
+            cpv[1] = 1.0 / (d1[1][LOC(1, g1 + q3[1])]) * dx2 * dz2;
+            cmv[2] = 1.0 / (d1[2][LOC(2, g2 - 1 + q3[2])]) * dx2 * dy2;
+            cpv[2] = 1.0 / (d1[2][LOC(2, g2 + q3[2])]) * dx2 * dy2;
+            cc = 0.0;
+            cc = cc - (cmv[0] + cpv[0] + cmv[1] + cpv[1] + cmv[2] + cpv[2]) + alpha * weight;
+          } else {
+            const int p1 = S.ax[0], p2 = S.ax[1];
+            const double w1 = d2[p1][LOC(p1, g0)], w2 = d2[p2][LOC(p2, g1)];
+            weight = w1 * w2;
+            cmv[0] = 1.0 / (d1[p1][LOC(p1, g0 - 1 + q3[p1])]) * w2;
+            cpv[0] = 1.0 / (d1[p1][LOC(p1, g0 + q3[p1])]) * w2;
+            cmv[1] = 1.0 / (d1[p2][LOC(p2, g1 - 1 + q3[p2])]) * w1;
+            cpv[1] = 1.0 / (d1[p2][LOC(p2, g1 + q3[p2])]) * w1;
+            cc = -(cmv[0] + cpv[0] + cmv[1] + cpv[1]) + alpha * weight;
+          }
+          unsigned short code = 0;
+          for (int a = 0; a < na; a++) {
+            const int p = S.ax[a];
+            if (d.periods[p] != 0) continue;
+            if (H.is_bound[p][0] && gg[a] == H.lo[p]) {
+              const int t = fold_type(H.desc.cbcpre[p][0], centered[p]);
+              cc = cc + fold_sgn(t) * cmv[a];
+              cmv[a] = 0.0;
+              code |= (unsigned short)(t << (2 * (2 * a)));
+            }
+            if (H.is_bound[p][1] && gg[a] == H.hi[p]) {
+              const int t = fold_type(H.desc.cbcpre[p][1], centered[p]);
+              cc = cc + fold_sgn(t) * cpv[a];
+              cpv[a] = 0.0;
+              code |= (unsigned short)(t << (2 * (2 * a + 1)));
+            }
+          }
+          L0.code[cidx] = code;
+          L0.cc[cidx] = cc;
+          for (int a = 0; a < na; a++) { L0.cp[a][cidx] = cpv[a]; cmv_all[a][cidx] = cmv[a]; }
+        }
+  }
+  // coupling consistency: cm(c) == cp(c - e_a) for coupled faces
+  for (int k = 0; k < L0.n[2]; k++)
+    for (int j = 0; j < L0.n[1]; j++)
+      for (int i = 0; i < L0.n[0]; i++) {
+        const long cidx = i + (long)L0.n[0] * (j + (long)L0.n[1] * k);
+        if (L0.code[cidx] & 0x8000) continue;
+        for (int a = 0; a < na; a++) {
+          const long m = B.nbr(L0, i, j, k, a, 0);
+          const int tm = (L0.code[cidx] >> (2 * (2 * a))) & 3;
+          if (m < 0 || (L0.code[m] & 0x8000)) {
+            if (!tm) { set_error("unfolded block face on the solver box boundary"); return SNAC_ERR_ARG; }
+            continue;
+          }
+          const int tpn = (L0.code[m] >> (2 * (2 * a + 1))) & 3;
+          if (tm && tpn) continue;
+          if (tm || tpn || cmv_all[a][cidx] != L0.cp[a][m]) {
+            set_error("inconsistent coupling between adjacent cells along axis %d", S.ax[a] + 1);
+            return SNAC_ERR_ARG;
+          }
+        }
+      }
+  bool has_dir = false;
+  long nact = 0;
+  for (long q = 0; q < L0.ncell; q++) {
+    if (L0.code[q] & 0x8000) continue;
+    nact++;
+    for (int f = 0; f < 6; f++) {
+      const int t = (L0.code[q] >> (2 * f)) & 3;
+      if (t == 2 || t == 3) has_dir = true;
+    }
+  }
+  S.nact0 = nact;
+  std::vector<int> singular(S.nsys);
+  for (int s = 0; s < S.nsys; s++) singular[s] = (!has_dir && alpha == 0.0 && S.lambda[s] == 0.0) ? 1 : 0;
+  // hierarchy
+  std::vector<std::array<int, 3>> boff(d.nblocks), bext(d.nblocks);
+  for (int b = 0; b < d.nblocks; b++)
+    for (int a = 0; a < 3; a++) {
+      const int p = S.ax[a];
+      boff[b][a] = a < na ? d.hb[b].lo[p] - lo_min[p] : 0;
+      bext[b][a] = a < na ? d.hb[b].hi[p] - d.hb[b].lo[p] + 1 : 1;
+    }
+  while ((int)B.L.size() < MG_MAXLEV) {
+    const HLevel &F = B.L.back();
+    if (F.ncell <= MG_DENSE_MAX) break;
+    // eligible axes: every block keeps an even offset and extent, periodic rings stay even (or 1);
+    // among them halve only the strongly coupled ones (smallest spacing within a factor 2), as PFMG does
+    double hmin[3] = {1e300, 1e300, 1e300}, hall = 1e300;
+    bool elig[3] = {false, false, false};
+    for (int a = 0; a < na; a++) {
+      if (F.n[a] < 2 || F.n[a] % 2) continue;
+      bool ok = true;
+      for (int b = 0; b < d.nblocks; b++)
+        if (boff[b][a] % 2 || bext[b][a] % 2) ok = false;
+      if (S.periodic[a] && (F.n[a] / 2) % 2 && F.n[a] / 2 != 1) ok = false;
+      if (!ok) continue;
+      elig[a] = true;
+      for (int q = 0; q < F.n[a]; q++) hmin[a] = std::min(hmin[a], F.W[a][q]);
+      hall = std::min(hall, hmin[a]);
+    }
+    int co[3] = {0, 0, 0}, any = 0;
+    for (int a = 0; a < na; a++)
+      if (elig[a] && hmin[a] <= 2.0 * hall) { co[a] = 1; any = 1; }
+    if (!any) break;
+    HLevel C;
+    for (int a = 0; a < 3; a++) { C.n[a] = co[a] ? F.n[a] / 2 : F.n[a]; C.coarsened[a] = co[a]; }
+    B.alloc_level(C);
+    for (int a = 0; a < 3; a++)
+      for (int q = 0; q < C.n[a]; q++) C.W[a][q] = co[a] ? F.W[a][2 * q] + F.W[a][2 * q + 1] : F.W[a][q];
+    for (int k = 0; k < C.n[2]; k++)
+      for (int j = 0; j < C.n[1]; j++)
+        for (int i = 0; i < C.n[0]; i++) {
+          const long cidx = i + (long)C.n[0] * (j + (long)C.n[1] * k);
+          const int f0[3] = {co[0] ? 2 * i : i, co[1] ? 2 * j : j, co[2] ? 2 * k : k};
+          const long fc = f0[0] + (long)F.n[0] * (f0[1] + (long)F.n[1] * f0[2]);
+          unsigned short code = F.code[fc];
+          if (!(code & 0x8000)) {
+            for (int a = 0; a < 3; a++) {
+              if (!co[a]) continue;
+              int f1[3] = {f0[0], f0[1], f0[2]};
+              f1[a] += 1;
+              const long fc1 = f1[0] + (long)F.n[0] * (f1[1] + (long)F.n[1] * f1[2]);
+              const int tp = (F.code[fc1] >> (2 * (2 * a + 1))) & 3;
+              code = (unsigned short)((code & ~(3u << (2 * (2 * a + 1)))) | (tp << (2 * (2 * a + 1))));
+            }
+          }
+          C.code[cidx] = code;
+        }
+    B.coarse_operator(C, alpha);
+    for (int b = 0; b < d.nblocks; b++)
+      for (int a = 0; a < 3; a++)
+        if (co[a]) { boff[b][a] /= 2; bext[b][a] /= 2; }
+    B.L.push_back(std::move(C));
+  }
+  HLevel &Lc = B.L.back();
+  if (Lc.ncell <= MG_DENSE_MAX) {
+    Lc.dinv.assign((size_t)Lc.ncell * Lc.ncell * S.nsys, 0.0);
+    for (int s = 0; s < S.nsys; s++)
+      if (!B.dense(Lc, s, singular[s] != 0, Lc.dinv.data() + (size_t)Lc.ncell * Lc.ncell * s)) {
+        set_error("coarsest operator of system %d is not definite", s);
+        return SNAC_ERR_ARG;
+      }
+  }
+  S.host_levels = (int)B.L.size();
+  S.host_coarse_cells = B.L.back().ncell;
+  if (!upload) return SNAC_OK;
+  // upload
+  MgProblem &P = S.P;
+  P.mode3d = S.mode3d;
+  for (int a = 0; a < 3; a++) P.periodic[a] = S.periodic[a];
+  P.nsys = S.nsys;
+  P.nlev = (int)B.L.size();
+  P.nu = d.opt.nu > 0 ? d.opt.nu : 2;
+  auto up = [&](const void *src, size_t bytes) -> void * {
+    void *p = S.alloc(bytes ? bytes : 8);
+    if (p && bytes) cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
+    return p;
+  };
+  auto upf = [&](const std::vector<double> &v) -> float * {
+    std::vector<float> f(v.begin(), v.end());
+    return (float *)up(f.data(), f.size() * sizeof(float));
+  };
+  for (int l = 0; l < P.nlev; l++) {
+    const HLevel &h = B.L[l];
+    MgLevelD &D = P.L[l];
+    for (int a = 0; a < 3; a++) { D.n[a] = h.n[a]; D.coarsened[a] = h.coarsened[a]; }
+    D.ncell = h.ncell;
+    D.code = (const unsigned short *)up(h.code.data(), h.code.size() * sizeof(unsigned short));
+    D.cc = (const double *)up(h.cc.data(), h.cc.size() * sizeof(double));
+    D.ccf = upf(h.cc);
+    for (int a = 0; a < 3; a++) {
+      D.cp[a] = (const double *)up(h.cp[a].data(), h.cp[a].size() * sizeof(double));
+      D.cpf[a] = upf(h.cp[a]);
+      D.W[a] = (const double *)up(h.W[a].data(), h.W[a].size() * sizeof(double));
+      D.Wf[a] = upf(h.W[a]);
+    }
+    const size_t nv = (size_t)h.ncell * S.nsys;
+    D.x = (double *)S.alloc(nv * sizeof(double));
+    D.b = (double *)S.alloc(nv * sizeof(double));
+    D.xf = (float *)S.alloc(nv * sizeof(float));
+    D.bf = (float *)S.alloc(nv * sizeof(float));
+    if (!h.dinv.empty()) {
+      D.dinv = (const double *)up(h.dinv.data(), h.dinv.size() * sizeof(double));
+      D.dinvf = upf(h.dinv);
+    }
+    if (!D.code || !D.cc || !D.x || !D.xf) { set_error("device allocation failed for multigrid level %d", l); return SNAC_ERR_NOMEM; }
+  }
+  P.shift = (const double *)up(S.lambda.data(), S.lambda.size() * sizeof(double));
+  P.shiftf = upf(S.lambda);
+  P.singular = (const int *)up(singular.data(), singular.size() * sizeof(int));
+  S.ncell0 = L0.ncell;
+  const size_t nv0 = (size_t)L0.ncell * S.nsys;
+  const int nchunk = (int)((L0.ncell + 255) / 256);
+  S.box_b = (double *)S.alloc(nv0 * sizeof(double));
+  S.box_x = (double *)S.alloc(nv0 * sizeof(double));
+  S.r64 = (double *)S.alloc(nv0 * sizeof(double));
+  S.box_b32 = (float *)S.alloc(nv0 * sizeof(float));
+  S.box_e32 = (float *)S.alloc(nv0 * sizeof(float));
+  S.active_outer = (int *)S.alloc(S.nsys * sizeof(int));
+  S.sc_outer = (SysScal *)S.alloc(S.nsys * sizeof(SysScal));
+  for (CgWork *W : {&S.W64, &S.W32}) {
+    const size_t es = W == &S.W64 ? sizeof(double) : sizeof(float);
+    W->r = S.alloc(nv0 * es);
+    W->z = S.alloc(nv0 * es);
+    W->p = S.alloc(nv0 * es);
+    W->q = S.alloc(nv0 * es);
+    W->part0 = (double *)S.alloc((size_t)nchunk * S.nsys * sizeof(double));
+    W->part1 = (double *)S.alloc((size_t)nchunk * S.nsys * sizeof(double));
+    W->sc = (SysScal *)S.alloc(S.nsys * sizeof(SysScal));
+    W->active = (int *)S.alloc(S.nsys * sizeof(int));
+    W->d_count = (int *)S.alloc(sizeof(int));
+    SNAC_CUDA(cudaMallocHost(&W->h_count, sizeof(int)));
+    if (!W->r || !W->p || !W->part0 || !W->sc) { set_error("device allocation failed for Krylov vectors"); return SNAC_ERR_NOMEM; }
+  }
+  return SNAC_OK;
+}
+
+// FP64: PCG with FP64 V-cycles.  Mixed: FP64 residual / FP32 PCG with FP32 V-cycles / FP64 update.
+static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *res_out) {
+  MgProblem &P = S.P;
+  SNAC_TRY(mg_project_singular(P, S.W64, S.box_b, st));
+  trace("solve: projection of singular systems", st);
+  int iters = 0;
+  if (S.precision == 0) {
+    SNAC_TRY(mg_set_active(P.nsys, S.W64.active, nullptr, st));
+    SNAC_TRY(mg_pcg<double>(P, S.W64, S.box_x, S.box_b, S.maxiter, S.tol, true, &iters, st));
+    // final residual report
+    std::vector<SysScal> sc(P.nsys);
+    SNAC_CUDA(cudaMemcpyAsync(sc.data(), S.W64.sc, P.nsys * sizeof(SysScal), cudaMemcpyDeviceToHost, st));
+    SNAC_CUDA(cudaStreamSynchronize(st));
+    double worst = 0.0;
+    for (auto &v : sc) worst = std::max(worst, v.rel);
+    *iters_out = iters;
+    *res_out = worst;
+    return (worst > S.tol && iters >= S.maxiter) ? SNAC_ERR_NOT_CONVERGED : SNAC_OK;
+  }
+  // mixed precision: iterative refinement in FP64 around FP32 Krylov solves
+  const int inner = 4;
+  const double inner_tol = 1e-5;
+  int outer = 0, total_inner = 0;
+  CgWork Wr = S.W64;  // residual-only use of the FP64 work area
+  Wr.active = S.active_outer;
+  Wr.sc = S.sc_outer;
+  SNAC_TRY(mg_set_active(P.nsys, S.active_outer, nullptr, st));
+  double worst = 0.0;
+  for (outer = 0; outer < S.maxiter; outer++) {
+    int it0 = 0;
+    // r64 = b - A x64 with norms/convergence (0 Krylov iterations)
+    Wr.r = S.r64;
+    SNAC_TRY(mg_pcg<double>(P, Wr, S.box_x, S.box_b, 0, S.tol, false, &it0, st));
+    SNAC_CUDA(cudaMemcpyAsync(Wr.h_count, Wr.d_count, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SNAC_CUDA(cudaStreamSynchronize(st));
+    if (*Wr.h_count == 0) break;
+    SNAC_TRY(mg_ir_down(P, Wr, S.r64, S.box_b32, S.box_e32, S.nact0, st));
+    SNAC_TRY(mg_set_active(P.nsys, S.W32.active, S.active_outer, st));
+    int it1 = 0;
+    SNAC_TRY(mg_pcg<float>(P, S.W32, S.box_e32, S.box_b32, inner, inner_tol, false, &it1, st));
+    total_inner += it1;
+    SNAC_TRY(mg_ir_up(P, Wr, S.box_e32, S.box_x, st));
+  }
+  std::vector<SysScal> sc(P.nsys);
+  SNAC_CUDA(cudaMemcpyAsync(sc.data(), S.sc_outer, P.nsys * sizeof(SysScal), cudaMemcpyDeviceToHost, st));
+  SNAC_CUDA(cudaStreamSynchronize(st));
+  for (auto &v : sc) worst = std::max(worst, v.rel);
+  *iters_out = outer;
+  *res_out = worst;
+  (void)total_inner;
+  return (outer >= S.maxiter && worst > S.tol) ? SNAC_ERR_NOT_CONVERGED : SNAC_OK;
+}
+
+// main.f90:1004-1022: transform (or gather), solve every system warm-started from po, back-transform + normfft
+int solver_solve_pressure(Domain &d, PoissonSolver &S) {
+  cudaStream_t st = d.st;
+  trace("solve: start", st);
+  if (S.fft_axis) SNAC_TRY(fft_forward_to_box(d, S, st));
+  else SNAC_TRY(box_gather(d, S, st));
+  trace("solve: forward transform / gather", st);
+  int it = 0;
+  double res = 0.0;
+  const int rc = solve_box(S, st, &it, &res);
+  trace("solve: box solve", st);
+  if (rc != SNAC_OK && rc != SNAC_ERR_NOT_CONVERGED) return rc;
+  if (S.fft_axis) SNAC_TRY(fft_backward_from_box(d, S, st));
+  else SNAC_TRY(box_scatter(d, S, st));
+  trace("solve: backward transform / scatter", st);
+  S.last_iters = it;
+  S.last_res = res;
+  if (rc == SNAC_ERR_NOT_CONVERGED)
+    set_error("pressure solve stopped at maxiter=%d with relative residual %.3e > tol %.3e", S.maxiter, res, S.tol);
+  return rc;
+}
+
+}  // namespace snac

@@ -1,0 +1,127 @@
+"""All blocks of a case resident on the GPU: the domain layer of the C ABI.
+
+``Domain(case)`` runs the set-up of main.f90:188-886 (placement, grids, BC
+planes, solver set-up) in the library; the per-stage routines and whole RK3
+steps (main.f90:893-1069) then run on the device without host round trips.
+Only one domain exists at a time (the library keeps module-level state, like
+the reference's Fortran modules).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import check, dptr
+
+
+class Domain:
+    def __init__(self, case, precision: int = 0, nu: int = 0, device: int = 0):
+        L = capi.lib()
+        self.case = case
+        c, arr, keep = capi.fill_descs(case)
+        opt = capi.Options(precision=int(precision), use_graph=0, nu=int(nu), device=int(device))
+        check(L.snac_init(C.byref(c), arr, C.byref(opt)))
+        self._keep = keep
+        self.nblocks = len(case.blocks)
+        self.geom = [self.geometry(ib) for ib in range(self.nblocks)]
+
+    def close(self):
+        capi.lib().snac_finalize()
+
+    def geometry(self, ib):
+        lo = (C.c_int * 3)(); hi = (C.c_int * 3)(); nb = (C.c_int * 6)(); isb = (C.c_int * 6)()
+        check(capi.lib().snac_block_geometry(ib, lo, hi, nb, isb))
+        return dict(lo=tuple(lo), hi=tuple(hi), nb=[[nb[2 * a], nb[2 * a + 1]] for a in range(3)],
+                    is_bound=[[isb[2 * a], isb[2 * a + 1]] for a in range(3)])
+
+    def shape(self, ib, kind):
+        lo, hi = self.geom[ib]["lo"], self.geom[ib]["hi"]
+        n = [hi[a] - lo[a] + 1 for a in range(3)]
+        if capi.DUDTRKO <= kind <= capi.DWDTRKO:
+            return tuple(n)
+        return tuple(x + 2 for x in n)
+
+    def get(self, ib, kind) -> np.ndarray:
+        a = np.zeros(self.shape(ib, kind), order="F")
+        check(capi.lib().snac_get_field(ib, kind, dptr(a)))
+        return a
+
+    def set(self, ib, kind, a: np.ndarray):
+        a = np.asfortranarray(a, dtype=np.float64)
+        assert a.shape == self.shape(ib, kind)
+        check(capi.lib().snac_set_field(ib, kind, dptr(a)))
+
+    def grid(self, ib, axis, which):
+        lo, hi = self.geom[ib]["lo"], self.geom[ib]["hi"]
+        out = np.zeros(hi[axis] - lo[axis] + 3)
+        check(capi.lib().snac_get_grid(ib, axis, which, dptr(out)))
+        return out
+
+    @property
+    def vol_all(self):
+        return capi.lib().snac_vol_all()
+
+    # per-stage routines (every block)
+    def rk_mom(self, irk):
+        check(capi.lib().snac_rk_mom_all(int(irk)))
+
+    def bounduvw(self, is_correc=False):
+        check(capi.lib().snac_bounduvw_all(int(is_correc)))
+
+    def boundp(self, kind=capi.P):
+        check(capi.lib().snac_boundp_all(int(kind)))
+
+    def fillps(self, dtrk):
+        check(capi.lib().snac_fillps_all(float(dtrk)))
+
+    def updt_rhs(self):
+        check(capi.lib().snac_updt_rhs_all())
+
+    def solve_pressure(self):
+        return capi.lib().snac_solve_pressure()
+
+    def correc(self, dtrk):
+        check(capi.lib().snac_correc_all(float(dtrk)))
+
+    def updt_pressure(self, alpha):
+        check(capi.lib().snac_updt_pressure_all(float(alpha)))
+
+    def chkdt(self):
+        out = C.c_double()
+        check(capi.lib().snac_chkdt_all(C.byref(out)))
+        return out.value
+
+    def chkdiv(self):
+        a = C.c_double(); b = C.c_double()
+        check(capi.lib().snac_chkdiv_all(C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def kinetic_energy(self):
+        out = C.c_double()
+        check(capi.lib().snac_kinetic_energy(C.byref(out)))
+        return out.value
+
+    def step(self, n=1, allow_not_converged=False):
+        rc = capi.lib().snac_step(int(n))
+        if rc == capi.ERR_NOT_CONVERGED and allow_not_converged:
+            return rc
+        check(rc)
+        return rc
+
+    def stats(self):
+        s = capi.StepStats()
+        check(capi.lib().snac_get_stats(C.byref(s)))
+        return dict(istep=s.istep, time=s.time, dt=s.dt, iters=s.solve_iters_max, residual=s.solve_residual_max,
+                    solves=s.solves, device_ms=s.device_ms)
+
+    @property
+    def dt(self):
+        out = C.c_double()
+        check(capi.lib().snac_get_dt(C.byref(out)))
+        return out.value
+
+    @dt.setter
+    def dt(self, v):
+        check(capi.lib().snac_set_dt(float(v)))

@@ -1,0 +1,193 @@
+"""Domain-level parity on the GPU: every block resident in HBM against the oracle.
+
+Covers the multi-block halo exchange and boundary conditions (bit-identical
+copies), the Poisson solve (FP64 and FP32-in-FP64), and whole RK3 steps on
+the reference's LDC test layout (3-D solve and FFT along x), the Taylor-Green
+vortex (FFT along z) and the uneven four-block channel.  The reference's own
+golden vector is checked with the reference's tolerance.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from snac_gb300 import capi, cases
+from snac_gb300.domain import Domain
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ldc_re1000_profile.txt")
+
+
+def seed_fields(case, oracle_dom, dom, seed=0, amp=1.0):
+    """Same random velocity/pressure on both sides (then the reference's initial bounduvw/boundp)."""
+    O = oracle_dom
+    rng = np.random.default_rng(seed)
+    for ib in range(len(case.blocks)):
+        for k in (capi.U, capi.V, capi.W, capi.P):
+            f = O.field(ib, k)
+            f[...] = amp * rng.standard_normal(f.shape)
+            dom.set(ib, k, f)
+
+
+def weighted_mean_free(p, ib, grid):
+    dxf, dyf, dzf = (grid(ib, a)[1:-1] for a in range(3))
+    w = dxf[:, None, None] * dyf[None, :, None] * dzf[None, None, :]
+    return w
+
+
+def compare_fields(case, O, dom, kinds, rtol, mean_free_p=False):
+    worst = 0.0
+    if mean_free_p:
+        num = den = 0.0
+        numo = 0.0
+        for ib in range(len(case.blocks)):
+            w = weighted_mean_free(None, ib, lambda b, a: O.grid(b, a, 1))
+            num += np.sum(w * dom.get(ib, capi.P)[1:-1, 1:-1, 1:-1])
+            numo += np.sum(w * O.field(ib, capi.P)[1:-1, 1:-1, 1:-1])
+            den += np.sum(w)
+        mg, mo = num / den, numo / den
+    for ib in range(len(case.blocks)):
+        for k in kinds:
+            g = dom.get(ib, k)[1:-1, 1:-1, 1:-1] if k != capi.DUDTRKO else dom.get(ib, k)
+            r = O.field(ib, k)[1:-1, 1:-1, 1:-1] if k != capi.DUDTRKO else O.field(ib, k)
+            if k == capi.P and mean_free_p:
+                g = g - mg
+                r = r - mo
+            scale = max(np.max(np.abs(r)), 1e-300)
+            err = np.max(np.abs(g - r)) / scale
+            worst = max(worst, err)
+            assert err <= rtol, (ib, k, err)
+    return worst
+
+
+@pytest.fixture
+def ldc3d(snac_lib, oracle_mod):
+    case = cases.ldc_reference_test(fft_axis=0)
+    O = oracle_mod.OracleDomain(case)
+    d = Domain(case)
+    yield case, O, d
+    d.close()
+
+
+def test_geometry_matches_oracle(ldc3d):
+    case, O, d = ldc3d
+    for ib in range(len(case.blocks)):
+        assert d.geom[ib] == O.geom[ib]
+        for a in range(3):
+            for w in range(4):
+                np.testing.assert_array_equal(d.grid(ib, a, w), O.grid(ib, a, w))
+
+
+def test_bound_exchange_and_bc_bitwise(ldc3d):
+    """bound.f90:8-106 on four blocks: ghost planes, edges and corners equal the oracle's exactly."""
+    case, O, d = ldc3d
+    seed_fields(case, O, d, seed=1)
+    for is_correc in (False, True):
+        O.bounduvw(is_correc)
+        d.bounduvw(is_correc)
+        for ib in range(4):
+            for k in (capi.U, capi.V, capi.W):
+                np.testing.assert_array_equal(d.get(ib, k), O.field(ib, k))
+    O.boundp(capi.P)
+    d.boundp(capi.P)
+    for ib in range(4):
+        np.testing.assert_array_equal(d.get(ib, capi.P), O.field(ib, capi.P))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_solve_pressure_matches_oracle(snac_lib, oracle_mod, precision):
+    """fillps + updt_rhs + solve + boundp on the four-block channel (FFT along z, stretched y)."""
+    case = cases.channel_4block(nx=(16, 32), ny=(8, 16), nz=16)
+    O = oracle_mod.OracleDomain(case)
+    d = Domain(case, precision=precision)
+    try:
+        seed_fields(case, O, d, seed=2)
+        O.bounduvw(False)
+        d.bounduvw(False)
+        L = oracle_mod.lib()
+        L.or_fillps_all(O.h, 0.01)
+        L.or_updt_rhs_all(O.h)
+        d.fillps(0.01)
+        d.updt_rhs()
+        for ib in range(4):
+            np.testing.assert_allclose(d.get(ib, capi.PP), O.field(ib, capi.PP), rtol=0,
+                                       atol=1e-12 * np.max(np.abs(O.field(ib, capi.PP))))
+        L.or_solve_pressure(O.h)
+        rc = d.solve_pressure()
+        assert rc == 0, capi.lib().snac_last_error()
+        O.boundp(capi.PP)
+        d.boundp(capi.PP)
+        # x periodic, y walls with N pressure, z periodic -> wavenumber 0 singular: compare mean-free
+        for ib in range(4):
+            g = d.get(ib, capi.PP)[1:-1, 1:-1, 1:-1]
+            r = O.field(ib, capi.PP)[1:-1, 1:-1, 1:-1]
+            scale = np.max(np.abs(r))
+            assert np.max(np.abs((g - g.mean()) - (r - r.mean()))) <= 2e-9 * scale
+    finally:
+        d.close()
+
+
+def _run_both(case, oracle_mod, nsteps, precision=0, seed=3, amp=0.1):
+    O = oracle_mod.OracleDomain(case)
+    d = Domain(case, precision=precision)
+    seed_fields(case, O, d, seed=seed, amp=amp)
+    O.bounduvw(False)
+    O.boundp(capi.P)
+    d.bounduvw(False)
+    d.boundp(capi.P)
+    O.step(nsteps)
+    d.step(nsteps)
+    return O, d
+
+
+@pytest.mark.parametrize("fft_axis", [0, 1])
+def test_steps_ldc_layout(snac_lib, oracle_mod, fft_axis):
+    case = cases.ldc_reference_test(fft_axis=fft_axis)
+    O, d = _run_both(case, oracle_mod, 5)
+    try:
+        assert abs(d.dt - O.dt) <= 1e-15 * O.dt
+        compare_fields(case, O, d, (capi.U, capi.V, capi.W), 1e-10)
+        compare_fields(case, O, d, (capi.P,), 1e-9, mean_free_p=True)
+        assert d.chkdiv()[1] < 1e-10
+    finally:
+        d.close()
+
+
+def test_steps_tgv(snac_lib, oracle_mod):
+    case = cases.taylor_green(16)
+    O, d = _run_both(case, oracle_mod, 3, amp=0.5)
+    try:
+        compare_fields(case, O, d, (capi.U, capi.V, capi.W), 1e-10)
+        compare_fields(case, O, d, (capi.P,), 1e-9, mean_free_p=True)
+    finally:
+        d.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_steps_channel(snac_lib, oracle_mod, precision):
+    case = cases.channel_4block(nx=(16, 32), ny=(8, 16), nz=16)
+    O, d = _run_both(case, oracle_mod, 3, precision=precision, amp=0.2)
+    try:
+        compare_fields(case, O, d, (capi.U, capi.V, capi.W), 1e-10)
+        compare_fields(case, O, d, (capi.P,), 1e-9, mean_free_p=True)
+        ke_o, ke_g = O.kinetic_energy(), d.kinetic_energy()
+        assert abs(ke_g - ke_o) <= 1e-12 * ke_o
+    finally:
+        d.close()
+
+
+@pytest.mark.parametrize("fft_axis", [0, 1])
+def test_gpu_ldc_golden(snac_lib, fft_axis):
+    """The reference's regression (tests/lid_driven_cavity/test.py) on the GPU path, with its tolerance."""
+    from test_oracle_golden import ldc_profile
+    case = cases.ldc_reference_test(fft_axis=fft_axis)
+    d = Domain(case)
+    try:
+        d.bounduvw(False)
+        d.boundp(capi.P)
+        d.step(1500)
+        prof = ldc_profile(lambda ib: d.get(ib, capi.V))
+        ref = np.loadtxt(GOLDEN)
+        np.testing.assert_allclose(prof, ref[:, 1], rtol=1e-7, atol=5e-8)
+    finally:
+        d.close()

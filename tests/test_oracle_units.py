@@ -1,0 +1,108 @@
+"""Oracle building blocks against independent definitions (numpy / scipy)."""
+import numpy as np
+import pytest
+import scipy.fft as sfft
+
+from snac_gb300 import cases
+
+
+def test_r2hc_matches_numpy(oracle_mod):
+    O = oracle_mod
+    rng = np.random.default_rng(1)
+    for n in (1, 2, 5, 8, 16, 33):
+        x = rng.standard_normal(n)
+        y = O.r2r(O.R2HC, x)
+        X = np.fft.rfft(x)
+        hc = np.zeros(n)
+        hc[: n // 2 + 1] = X.real
+        for k in range(1, (n + 1) // 2):
+            hc[n - k] = X[k].imag
+        np.testing.assert_allclose(y, hc, atol=1e-12 * max(1, n))
+        np.testing.assert_allclose(O.r2r(O.HC2R, y), n * x, atol=1e-11 * n)
+
+
+@pytest.mark.parametrize("kind,stype,sk", [("REDFT10", "dct", 2), ("REDFT01", "dct", 3), ("REDFT11", "dct", 4),
+                                           ("RODFT10", "dst", 2), ("RODFT01", "dst", 3), ("RODFT11", "dst", 4),
+                                           ("REDFT00", "dct", 1), ("RODFT00", "dst", 1)])
+def test_dct_dst_match_scipy(oracle_mod, kind, stype, sk):
+    """FFTW's unnormalised kinds equal scipy's type-1..4 DCT/DST with norm=None."""
+    O = oracle_mod
+    rng = np.random.default_rng(2)
+    for n in (2, 3, 8, 12):
+        x = rng.standard_normal(n)
+        y = O.r2r(getattr(O, kind), x)
+        ref = (sfft.dct if stype == "dct" else sfft.dst)(x, type=sk)
+        np.testing.assert_allclose(y, ref, atol=1e-11 * n)
+
+
+@pytest.mark.parametrize("bc", ["FF", "NN", "DD", "ND"])
+def test_eigenvalues_diagonalise_1d_operator(oracle_mod, bc):
+    """fft.f90:151-189: the modified wavenumbers of the centred 1-D operator with the BC folding of solver.f90."""
+    O = oracle_mod
+    n = 12
+    lam = O.eigenvalues(n, bc, True)
+    # 1-D operator with unit spacing, folded boundaries (N: +1, centred D: -1) or periodic
+    A = np.zeros((n, n))
+    for i in range(n):
+        A[i, i] = -2.0
+        if i > 0: A[i, i - 1] = 1.0
+        if i < n - 1: A[i, i + 1] = 1.0
+    if bc == "FF":
+        A[0, -1] = A[-1, 0] = 1.0
+    else:
+        s = {"N": 1.0, "D": -1.0}
+        A[0, 0] += s[bc[0]]
+        A[-1, -1] += s[bc[1]]
+    ev = np.sort(np.linalg.eigvalsh(A))
+    np.testing.assert_allclose(np.sort(lam), ev, atol=1e-12)
+
+
+def test_dn_pair_has_no_eigenvalues(oracle_mod):
+    """The reference's eigenvalues() has no 'DN' case (fft.f90:159-188)."""
+    with pytest.raises(ValueError):
+        oracle_mod.eigenvalues(8, "DN", True)
+
+
+def test_initgrid_matches_python(oracle_mod):
+    import ctypes as C
+    O = oracle_mod
+    n = 40
+    drc, drf, rc, rf = (np.zeros(n + 2) for _ in range(4))
+    P = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    O.lib().or_initgrid(1, n, 0, 1.8, 0.0, 2.0, P(drc), P(drf), P(rc), P(rf))
+    g = cases.global_axis_grid(n, 0.0, 2.0, 1.8)
+    np.testing.assert_allclose(rf, g[0], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(drf, g[2], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(drc, g[3], rtol=0, atol=1e-15)
+
+
+def test_block_placement_channel(oracle_mod):
+    d = oracle_mod.OracleDomain(cases.channel_4block(nx=(8, 16), ny=(4, 8), nz=8))
+    assert [g["lo"] for g in d.geom] == [(1, 1, 1), (9, 1, 1), (1, 5, 1), (9, 5, 1)]
+    assert d.geom[0]["nb"] == [[1, 1], [-1, 2], [0, 0]]
+    assert d.geom[3]["is_bound"] == [[0, 0], [0, 1], [0, 0]]
+
+
+def test_bad_connectivity_rejected(oracle_mod):
+    c = cases.ldc_reference_test()
+    c.blocks[0].bcpre[1][1] = 3.0  # y+ friend of block 1 points at block 3, which does not point back
+    with pytest.raises(RuntimeError):
+        oracle_mod.OracleDomain(c)
+
+
+def test_oracle_solver_exact_on_manufactured(oracle_mod):
+    """A divergence-free projection: after one pressure solve + correction the divergence vanishes."""
+    O = oracle_mod
+    d = O.OracleDomain(cases.lid_driven_cavity(16))
+    rng = np.random.default_rng(3)
+    for k in (O.U, O.V, O.W):
+        f = d.field(0, k)
+        f[...] = rng.standard_normal(f.shape)
+    d.bounduvw(False)
+    O.lib().or_fillps_all(d.h, 0.1)
+    O.lib().or_updt_rhs_all(d.h)
+    O.lib().or_solve_pressure(d.h)
+    d.boundp(O.PP)
+    O.lib().or_correc_all(d.h, 0.1)
+    d.bounduvw(True)
+    assert d.chkdiv()[1] < 1e-9
