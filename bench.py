@@ -209,6 +209,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--only", choices=["mixed", "plain"], default=None,
+                    help="run one path once and print its timing only (used for ncu launch lists)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     from snac_gb300 import cases
@@ -237,6 +239,12 @@ def main():
     if world > 1 and not torch.distributed.is_initialized():
         torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     device = local
+    if args.only:
+        r = run_gpu_path(case_fn, 1 if args.only == "mixed" else 0, args.steps, args.warmup, device)
+        if rank == 0:
+            print(json.dumps({"path": args.only, "ms_per_step": r["ms"], "max_div_u": r["divmax"],
+                              "solve_iters_max": r["iters"]}), flush=True)
+        return
     sampler = ClockSampler(device)
     # plain FP64 path
     plain = run_gpu_path(case_fn, 0, args.steps, args.warmup, device)
