@@ -172,6 +172,18 @@ int snac_chkdt(const int lo[3], const int hi[3], const double *dxc, const double
 int snac_chkdiv(const int lo[3], const int hi[3], const double *dxf, const double *dyf,
                 const double *dzf, const double *u, const double *v, const double *w, double vol,
                 double *divtot, double *divmax);
+/* No counterpart in the reference.  snac_chkdiv for callers that must not allocate device memory
+ * (e.g. a driver whose fields were placed on the GPU up front and that checks the divergence inside
+ * its time loop, where cudaMalloc/cudaFree would synchronise the device or fail on a full GPU):
+ * u, v, w (halo'd) and dxf, dyf, dzf ((n+2) entries) are DEVICE pointers, stream is a cudaStream_t
+ * (NULL = default stream), divtot/divmax are host pointers.  Scratch is a fixed 128 KiB device array
+ * owned by the library (held on every GPU that loads it until exit); blocks above 2^31-1 cells are
+ * rejected with SNAC_ERR_ARG.  The first call on a device resolves the array's address with that
+ * device current -- make it before any stream capture; calls that overlap on the GPU race on the
+ * shared array. */
+int snac_chkdiv_noalloc(const int lo[3], const int hi[3], const double *dxf, const double *dyf,
+                        const double *dzf, const double *u, const double *v, const double *w, double vol,
+                        void *stream, double *divtot, double *divmax);
 /* bound.f90:108-248 (set_bc) on one face of one halo'd array */
 int snac_set_bc(char ctype, int ibound, const int lo[3], const int hi[3], int idir, int centered,
                 double rvalue, double dr, double *p);

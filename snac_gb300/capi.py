@@ -80,6 +80,8 @@ PROTOTYPES = {
     "snac_updt_rhs": (C.c_int, [IP, IP, IP, DP, DP, DP, DP]),
     "snac_chkdt": (C.c_int, [IP, IP, DP, DP, DP, DP, DP, DP, C.c_double, DP, DP, DP, C.c_int, DP]),
     "snac_chkdiv": (C.c_int, [IP, IP, DP, DP, DP, DP, DP, DP, C.c_double, DP, DP]),
+    "snac_chkdiv_noalloc": (C.c_int, [IP, IP, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_double, C.c_void_p, DP, DP]),
     "snac_set_bc": (C.c_int, [C.c_char, C.c_int, IP, IP, C.c_int, C.c_int, C.c_double, C.c_double, DP]),
     "snac_fft": (C.c_int, [C.c_int, C.c_int, IP, C.c_int, DP]),
     "snac_find_fft": (C.c_int, [C.c_char_p, C.c_int, IP, IP, DP]),
