@@ -12,65 +12,10 @@
 #include "snac_solver.h"
 #include "snac_mgk.h"
 #include "snac_prof.h"
+#include "snac_mgdev.h"
 
 namespace snac {
 
-template <typename T> struct LA;
-template <> struct LA<double> {
-  static __host__ __device__ __forceinline__ const double *cc(const MgLevelD &L) { return L.cc; }
-  static __host__ __device__ __forceinline__ const double *cp(const MgLevelD &L, int a) { return L.cp[a]; }
-  static __host__ __device__ __forceinline__ const double *W(const MgLevelD &L, int a) { return L.W[a]; }
-  static __host__ __device__ __forceinline__ double *x(const MgLevelD &L) { return L.x; }
-  static __host__ __device__ __forceinline__ double *b(const MgLevelD &L) { return L.b; }
-  static __host__ __device__ __forceinline__ const double *dinv(const MgLevelD &L) { return L.dinv; }
-};
-template <> struct LA<float> {
-  static __host__ __device__ __forceinline__ const float *cc(const MgLevelD &L) { return L.ccf; }
-  static __host__ __device__ __forceinline__ const float *cp(const MgLevelD &L, int a) { return L.cpf[a]; }
-  static __host__ __device__ __forceinline__ const float *W(const MgLevelD &L, int a) { return L.Wf[a]; }
-  static __host__ __device__ __forceinline__ float *x(const MgLevelD &L) { return L.xf; }
-  static __host__ __device__ __forceinline__ float *b(const MgLevelD &L) { return L.bf; }
-  static __host__ __device__ __forceinline__ const float *dinv(const MgLevelD &L) { return L.dinvf; }
-};
-
-__device__ __forceinline__ long nbr_idx(const MgLevelD &L, const MgGeom &G, int i, int j, int k, int a, int s) {
-  int c[3] = {i, j, k};
-  c[a] += s ? 1 : -1;
-  if (c[a] < 0 || c[a] >= L.n[a]) {
-    if (!G.periodic[a]) return -1;
-    c[a] = c[a] < 0 ? c[a] + L.n[a] : c[a] - L.n[a];
-  }
-  return c[0] + (long)L.n[0] * (c[1] + (long)L.n[1] * c[2]);
-}
-
-template <typename T>
-__device__ __forceinline__ T diag_of(const MgLevelD &L, const MgGeom &G, const T *shift, long c, int i, int j, int s) {
-  const T d = LA<T>::cc(L)[c];
-  if (G.mode3d) return d;
-  return d + shift[s] * LA<T>::W(L, 0)[i] * LA<T>::W(L, 1)[j];
-}
-
-// sum over coupled neighbours of coefficient * v(neighbour)
-template <typename T>
-__device__ __forceinline__ T offdiag(const MgLevelD &L, const MgGeom &G, const T *v, long off, long c, int i, int j,
-                                     int k) {
-  T acc = 0;
-  const int na = G.mode3d ? 3 : 2;
-  for (int a = 0; a < na; a++) {
-    if (G.periodic[a] && L.n[a] == 1) continue;
-    const long cpn = nbr_idx(L, G, i, j, k, a, 1), cmn = nbr_idx(L, G, i, j, k, a, 0);
-    if (cpn >= 0) acc += LA<T>::cp(L, a)[c] * v[off + cpn];
-    if (cmn >= 0) acc += LA<T>::cp(L, a)[cmn] * v[off + cmn];
-  }
-  return acc;
-}
-
-__device__ __forceinline__ void decompose(const MgLevelD &L, long c, int &i, int &j, int &k) {
-  i = (int)(c % L.n[0]);
-  const long r = c / L.n[0];
-  j = (int)(r % L.n[1]);
-  k = (int)(r / L.n[1]);
-}
 
 // ---------------------------------------------------------------- smoothing / transfer
 template <typename T>
@@ -164,6 +109,19 @@ int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, c
   T *b = LA<T>::b(L);
   const dim3 g = grid_for(L.ncell, P.nsys);
   trace("vcycle: enter level", st);
+  if (P.fused && l >= P.cta_level[sizeof(T) == 8 ? 1 : 0]) return launch_vcycle_coarse<T>(P, G, l, shift, active, x, b, st);
+  const bool tile = P.fused && !P.mode3d && L.n[0] >= 32 && L.n[1] >= 16 && 2 * P.nu <= 4;
+  if (tile && l < P.nlev - 1) {
+    const MgLevelD &C = P.L[l + 1];
+    SNAC_TRY(launch_rbgs_tile2d<T>(P, l, shift, active, 0, 0, x, b, (const T *)nullptr, st));
+    prof_begin(KID_RESTRICT, st);
+    k_resid_restrict<T><<<grid_for(C.ncell, P.nsys), 256, 0, st>>>(L, C, G, shift, active, x, b, LA<T>::b(C),
+                                                                   LA<T>::x(C));
+    prof_end(KID_RESTRICT, st);
+    SNAC_CUDA(cudaGetLastError());
+    SNAC_TRY(mg_vcycle_impl<T>(P, G, l + 1, shift, active, st));
+    return launch_rbgs_tile2d<T>(P, l, shift, active, 1, 1, x, b, (const T *)LA<T>::x(C), st);
+  }
   if (l == P.nlev - 1) {
     if (LA<T>::dinv(L)) {
       k_dense<T><<<P.nsys, 256, 0, st>>>(L, active, x, b);
@@ -248,33 +206,43 @@ __global__ void k_cg_dot(long n, const int *active, const T *a, const T *b, doub
   if (threadIdx.x == 0) part[(long)s * nchunk + blockIdx.x] = v;
 }
 
-__device__ __forceinline__ double sum_parts(const double *part, int s, int nchunk) {
+// Per-system sum of the chunk partials by one warp: lane-strided, then a shuffle tree (fixed order).
+__device__ __forceinline__ double warp_sum_parts(const double *part, int s, int nchunk) {
+  const int l = threadIdx.x & 31;
   double acc = 0.0;
-  for (int q = 0; q < nchunk; q++) acc += part[(long)s * nchunk + q];
-  return acc;
+  for (int q = l; q < nchunk; q += 32) acc += part[(long)s * nchunk + q];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  return __shfl_sync(0xffffffffu, acc, 0);
 }
 
-// p = z + beta p with beta = rz_new/rz_old (0 on the first iteration); stores rz_new
+// rz_new = r.z; beta = rz_new/rz_old (0 on the first iteration); one warp per system
+__global__ void k_cg_beta(int nsys, const int *active, SysScal *sc, const double *part_rz, int nchunk) {
+  const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (s >= nsys || (active && !active[s])) return;
+  const double rz = warp_sum_parts(part_rz, s, nchunk);
+  if ((threadIdx.x & 31) == 0) {
+    sc[s].beta = sc[s].first ? 0.0 : rz / sc[s].rz;
+    sc[s].rz = rz;
+    sc[s].first = 0;
+  }
+}
+
+// alpha = rz/pq; one warp per system
+__global__ void k_cg_alpha(int nsys, const int *active, SysScal *sc, const double *part_pq, int nchunk) {
+  const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (s >= nsys || (active && !active[s])) return;
+  const double pq = warp_sum_parts(part_pq, s, nchunk);
+  if ((threadIdx.x & 31) == 0) sc[s].alpha = sc[s].rz / pq;
+}
+
+// p = z + beta p
 template <typename T>
-__global__ void k_cg_p(long n, const int *active, SysScal *sc, const double *part_rz, int nchunk, const T *z, T *p) {
+__global__ void k_cg_p(long n, const int *active, const SysScal *sc, const T *z, T *p) {
   const int s = blockIdx.y;
   if (active && !active[s]) return;
-  __shared__ double beta_s;
-  if (threadIdx.x == 0) {
-    const double rz = sum_parts(part_rz, s, nchunk);
-    beta_s = sc[s].first ? 0.0 : rz / sc[s].rz;
-  }
-  __syncthreads();
+  const T beta = (T)sc[s].beta;
   const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < n) p[n * s + c] = z[n * s + c] + (T)beta_s * p[n * s + c];
-}
-
-// store rz and clear `first` (one thread per system, after k_cg_p)
-__global__ void k_cg_rz_store(int nsys, const int *active, SysScal *sc, const double *part_rz, int nchunk) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nsys || (active && !active[s])) return;
-  sc[s].rz = sum_parts(part_rz, s, nchunk);
-  sc[s].first = 0;
+  if (c < n) p[n * s + c] = z[n * s + c] + beta * p[n * s + c];
 }
 
 // q = A p ; partial p.q
@@ -302,13 +270,11 @@ __global__ void k_cg_apply(MgLevelD L, MgGeom G, const T *shift, const int *acti
 
 // alpha = rz/pq; x += alpha p; r -= alpha q; partial r.r
 template <typename T>
-__global__ void k_cg_xr(long n, const int *active, const SysScal *sc, const double *part_pq, int nchunk, const T *p,
-                        const T *q, T *x, T *r, double *part_rr) {
+__global__ void k_cg_xr(long n, const int *active, const SysScal *sc, const T *p, const T *q, T *x, T *r,
+                        double *part_rr) {
   const int s = blockIdx.y;
   if (active && !active[s]) return;
-  __shared__ double alpha_s;
-  if (threadIdx.x == 0) alpha_s = sc[s].rz / sum_parts(part_pq, s, nchunk);
-  __syncthreads();
+  const double alpha_s = sc[s].alpha;
   const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
   double v = 0.0;
   if (c < n) {
@@ -319,29 +285,26 @@ __global__ void k_cg_xr(long n, const int *active, const SysScal *sc, const doub
     v = (double)rv * (double)rv;
   }
   v = block_sum(v);
-  if (threadIdx.x == 0) part_rr[(long)s * nchunk + blockIdx.x] = v;
+  if (threadIdx.x == 0) part_rr[(long)s * gridDim.x + blockIdx.x] = v;
 }
 
-// finalize residual norms: rel = sqrt(rr/bb); update active flags; count still-active systems
+// finalize residual norms: rel = sqrt(rr/bb); update active flags; count still-active systems.
+// One warp per system; `count` must be zero on entry (cleared by the caller).
 __global__ void k_cg_norms(int nsys, int *active, SysScal *sc, const double *part_rr, const double *part_bb,
                            int nchunk, double tol, int set_bb, int *count) {
-  __shared__ int cnt;
-  if (threadIdx.x == 0) cnt = 0;
-  __syncthreads();
-  for (int s = threadIdx.x; s < nsys; s += blockDim.x) {
-    if (!active[s]) continue;
-    const double rr = sum_parts(part_rr, s, nchunk);
-    if (set_bb) { sc[s].bb = sum_parts(part_bb, s, nchunk); sc[s].first = 1; sc[s].zero_rhs = 0; }
-    sc[s].rr = rr;
-    const double bb = sc[s].bb;
-    const double rel = bb > 0.0 ? sqrt(rr / bb) : 0.0;
-    sc[s].rel = rel;
-    if (bb == 0.0) { sc[s].zero_rhs = 1; active[s] = 0; }
-    else if (rel <= tol) active[s] = 0;
-    else atomicAdd(&cnt, 1);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) *count = cnt;
+  const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (s >= nsys || !active[s]) return;
+  const double rr = warp_sum_parts(part_rr, s, nchunk);
+  const double bbn = set_bb ? warp_sum_parts(part_bb, s, nchunk) : 0.0;
+  if ((threadIdx.x & 31) != 0) return;
+  if (set_bb) { sc[s].bb = bbn; sc[s].first = 1; sc[s].zero_rhs = 0; }
+  sc[s].rr = rr;
+  const double bb = sc[s].bb;
+  const double rel = bb > 0.0 ? sqrt(rr / bb) : 0.0;
+  sc[s].rel = rel;
+  if (bb == 0.0) { sc[s].zero_rhs = 1; active[s] = 0; }
+  else if (rel <= tol) active[s] = 0;
+  else atomicAdd(count, 1);
 }
 
 // systems with an all-zero right-hand side get x = 0 (as HYPRE does)
@@ -370,9 +333,10 @@ __global__ void k_sub_mean(MgLevelD L, const int *singular, T *b, const double *
   const int s = blockIdx.y;
   if (!singular[s]) return;
   __shared__ double mean;
-  if (threadIdx.x == 0) {
-    const double na = sum_parts(partn, s, nchunk);
-    mean = na > 0.0 ? sum_parts(part, s, nchunk) / na : 0.0;
+  if (threadIdx.x < 32) {
+    const double na = warp_sum_parts(partn, s, nchunk);
+    const double sm = warp_sum_parts(part, s, nchunk);
+    if (threadIdx.x == 0) mean = na > 0.0 ? sm / na : 0.0;
   }
   __syncthreads();
   const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -412,10 +376,9 @@ __global__ void k_ir_up(long n, const int *active, const SysScal *sc, const floa
   template __global__ void k_cg_resid<T>(MgLevelD, MgGeom, const T *, const int *, const T *, const T *, T *,       \
                                          double *, double *, int);                                                  \
   template __global__ void k_cg_dot<T>(long, const int *, const T *, const T *, double *, int);                     \
-  template __global__ void k_cg_p<T>(long, const int *, SysScal *, const double *, int, const T *, T *);            \
+  template __global__ void k_cg_p<T>(long, const int *, const SysScal *, const T *, T *);                           \
   template __global__ void k_cg_apply<T>(MgLevelD, MgGeom, const T *, const int *, const T *, T *, double *, int);  \
-  template __global__ void k_cg_xr<T>(long, const int *, const SysScal *, const double *, int, const T *,           \
-                                      const T *, T *, T *, double *);                                               \
+  template __global__ void k_cg_xr<T>(long, const int *, const SysScal *, const T *, const T *, T *, T *, double *); \
   template __global__ void k_zero_rhs_systems<T>(long, const SysScal *, T *);                                      \
   template __global__ void k_sum_active<T>(MgLevelD, const int *, const T *, double *, double *, int);              \
   template __global__ void k_sub_mean<T>(MgLevelD, const int *, T *, const double *, const double *, int);
@@ -450,8 +413,10 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, T *b, int maxiter, double tol, b
   const int nchunk = (int)((n + 255) / 256);
   const dim3 g(nchunk, P.nsys);
   T *r = (T *)W.r, *z = (T *)W.z, *p = (T *)W.p, *q = (T *)W.q;
+  const unsigned gsys = (unsigned)((P.nsys + 7) / 8);  // one warp per system, 8 per CTA
   k_cg_resid<T><<<g, 256, 0, st>>>(L0, G, shift, W.active, x, b, r, W.part0, W.part1, nchunk);
-  k_cg_norms<<<1, 256, 0, st>>>(P.nsys, W.active, W.sc, W.part0, W.part1, nchunk, tol, 1, W.d_count);
+  SNAC_CUDA(cudaMemsetAsync(W.d_count, 0, sizeof(int), st));
+  k_cg_norms<<<gsys, 256, 0, st>>>(P.nsys, W.active, W.sc, W.part0, W.part1, nchunk, tol, 1, W.d_count);
   SNAC_CUDA(cudaGetLastError());
   k_zero_rhs_systems<T><<<g, 256, 0, st>>>(n, W.sc, x);
   trace(sizeof(T) == 8 ? "pcg64: initial residual" : "pcg32: initial residual", st);
@@ -469,13 +434,15 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, T *b, int maxiter, double tol, b
     SNAC_TRY(mg_vcycle_impl<T>(Pz, G, 0, shift, W.active, st));
     trace("pcg: V-cycle", st);
     k_cg_dot<T><<<g, 256, 0, st>>>(n, W.active, r, z, W.part0, nchunk);
-    k_cg_p<T><<<g, 256, 0, st>>>(n, W.active, W.sc, W.part0, nchunk, z, p);
-    k_cg_rz_store<<<(P.nsys + 127) / 128, 128, 0, st>>>(P.nsys, W.active, W.sc, W.part0, nchunk);
+    k_cg_beta<<<gsys, 256, 0, st>>>(P.nsys, W.active, W.sc, W.part0, nchunk);
+    k_cg_p<T><<<g, 256, 0, st>>>(n, W.active, W.sc, z, p);
     prof_begin(KID_CG_APPLY, st);
     k_cg_apply<T><<<g, 256, 0, st>>>(L0, G, shift, W.active, p, q, W.part1, nchunk);
     prof_end(KID_CG_APPLY, st);
-    k_cg_xr<T><<<g, 256, 0, st>>>(n, W.active, W.sc, W.part1, nchunk, p, q, x, r, W.part0);
-    k_cg_norms<<<1, 256, 0, st>>>(P.nsys, W.active, W.sc, W.part0, nullptr, nchunk, tol, 0, W.d_count);
+    k_cg_alpha<<<gsys, 256, 0, st>>>(P.nsys, W.active, W.sc, W.part1, nchunk);
+    k_cg_xr<T><<<g, 256, 0, st>>>(n, W.active, W.sc, p, q, x, r, W.part0);
+    SNAC_CUDA(cudaMemsetAsync(W.d_count, 0, sizeof(int), st));
+    k_cg_norms<<<gsys, 256, 0, st>>>(P.nsys, W.active, W.sc, W.part0, nullptr, nchunk, tol, 0, W.d_count);
     SNAC_CUDA(cudaGetLastError());
     trace("pcg: iteration", st);
   }

@@ -11,7 +11,7 @@ struct MgGeom {
 
 // per-system scalars of one Krylov iteration
 struct SysScal {
-  double rz, rr, bb, rel, scale;
+  double rz, rr, bb, rel, scale, alpha, beta;
   int first, zero_rhs;
 };
 

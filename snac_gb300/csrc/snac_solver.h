@@ -39,7 +39,19 @@ struct MgProblem {
   const double *shift;               // per system (lambda_k), device
   const float *shiftf;
   const int *singular;               // per system, device
+  int fused;                         // 1: tiled smoother + one-CTA coarse tail; 0: one kernel per sweep
+  int cta_level[2];                  // first level run by k_vcycle_coarse ([0] FP32, [1] FP64); nlev = none
 };
+
+struct MgGeom;
+template <typename T>
+int launch_rbgs_tile2d(const MgProblem &P, int l, const T *shift, const int *active, int first_color, int mode,
+                       T *x, const T *b, const T *xc, cudaStream_t st);
+template <typename T>
+size_t coarse_smem_bytes(const MgProblem &P, int l0);
+template <typename T>
+int launch_vcycle_coarse(const MgProblem &P, const MgGeom &G, int l0, const T *shift, const int *active, T *x,
+                         const T *b, cudaStream_t st);
 
 // kernels (k_mg.cu) -- T = double or float
 template <typename T> int mg_vcycle(const MgProblem &P, int l, const int *active, cudaStream_t st);

@@ -470,6 +470,19 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
     }
     if (!D.code || !D.cc || !D.x || !D.xf) { set_error("device allocation failed for multigrid level %d", l); return SNAC_ERR_NOMEM; }
   }
+  // fused kernels: tiled plane smoother and a one-CTA coarse tail where its levels fit in shared memory
+  {
+    const char *e = getenv("SNAC_MG_UNFUSED");
+    P.fused = (e && e[0] && e[0] != '0') ? 0 : 1;
+    const size_t budget = 96 * 1024;
+    for (int prec = 0; prec < 2; prec++) {
+      P.cta_level[prec] = P.nlev;
+      for (int l = 1; l < P.nlev; l++) {
+        const size_t bytes = prec ? coarse_smem_bytes<double>(P, l) : coarse_smem_bytes<float>(P, l);
+        if (bytes <= budget) { P.cta_level[prec] = l; break; }
+      }
+    }
+  }
   P.shift = (const double *)up(S.lambda.data(), S.lambda.size() * sizeof(double));
   P.shiftf = upf(S.lambda);
   P.singular = (const int *)up(singular.data(), singular.size() * sizeof(int));

@@ -127,6 +127,33 @@ def test_solve_pressure_matches_oracle(snac_lib, oracle_mod, precision):
         d.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("which", ["channel", "ldc3d"])
+def test_fused_vcycle_matches_unfused(snac_lib, monkeypatch, precision, which):
+    """The tiled smoother / one-CTA coarse tail give the same solves as one kernel per sweep."""
+    case = (cases.channel_4block(nx=(32, 64), ny=(32, 48), nz=8) if which == "channel"
+            else cases.lid_driven_cavity(32))
+    out = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("SNAC_MG_UNFUSED", mode)
+        d = Domain(case, precision=precision)
+        try:
+            rng = np.random.default_rng(11)
+            for ib in range(len(case.blocks)):
+                for k in (capi.U, capi.V, capi.W):
+                    d.set(ib, k, rng.standard_normal(d.shape(ib, k)))
+            d.bounduvw(False)
+            d.fillps(0.01)
+            d.updt_rhs()
+            assert d.solve_pressure() == 0
+            out[mode] = [d.get(ib, capi.PP) for ib in range(len(case.blocks))]
+        finally:
+            d.close()
+    for a, b in zip(out["1"], out["0"]):
+        scale = np.max(np.abs(a))
+        assert np.max(np.abs(a - b)) <= 1e-12 * scale
+
+
 def _run_both(case, oracle_mod, nsteps, precision=0, seed=3, amp=0.1):
     O = oracle_mod.OracleDomain(case)
     d = Domain(case, precision=precision)
