@@ -69,7 +69,7 @@ struct PoissonSolver {
   int *active_outer = nullptr;
   SysScal *sc_outer = nullptr;
   double *r64 = nullptr;
-  float *box_b32 = nullptr, *box_e32 = nullptr;
+  float *box_e32 = nullptr;  // FP32 correction of the mixed path
   std::vector<void *> allocs;
   int last_iters = 0;
   double last_res = 0.0;

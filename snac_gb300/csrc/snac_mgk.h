@@ -15,21 +15,33 @@ struct SysScal {
   int first, zero_rhs;
 };
 
+// Partial sums: one row of `stride` doubles per system; a producer kernel writes one entry per CTA
+// and reports how many it wrote, the finalising kernel sums that many in a fixed order.
 struct CgWork {
-  void *r, *z, *p, *q;      // level-0 vectors (type of the running Krylov loop)
-  double *part0, *part1;    // nsys * nchunk partial sums
-  SysScal *sc;              // nsys
-  int *active;              // nsys flags of the running loop
-  int *d_count;             // still-active systems (device)
-  int *h_count;             // pinned host copy
+  void *r, *z, *p, *p2, *q;  // level-0 vectors (type of the running Krylov loop); p/p2 alternate
+  double *part0, *part1, *part2;
+  int stride;                // partial entries per system (capacity)
+  SysScal *sc;               // nsys
+  int *active;               // nsys flags of the running loop
+  int *d_count;              // [0] still-active systems, [1] systems with a zero right-hand side (device)
+  int *h_count;              // pinned host copy
 };
 
+// residual r = b - A x on level 0 with norms: sets rr (and bb, first, zero_rhs when set_bb), rel, active, count;
+// with want_scale also scale = RMS(r) over the nact active cells
 template <typename T>
-int mg_pcg(const MgProblem &P, CgWork &W, T *x, T *b, int maxiter, double tol, bool check_host, int *iters,
+int mg_residual(const MgProblem &P, CgWork &W, const T *x, const T *b, T *r, double tol, int set_bb, int want_scale,
+                long nact, cudaStream_t st);
+// preconditioned CG iterations on level 0, starting from the residual in W.r and the scalars set by
+// mg_residual / mg_ir_down; zero_x: x is taken as zero (overwritten on the first update)
+template <typename T>
+int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool zero_x, bool check_host, int *iters,
            cudaStream_t st);
 int mg_project_singular(const MgProblem &P, CgWork &W, double *b, cudaStream_t st);
-int mg_ir_down(const MgProblem &P, CgWork &W, const double *r64, float *r32, float *e32, long nact, cudaStream_t st);
-int mg_ir_up(const MgProblem &P, CgWork &W, const float *e32, double *x, cudaStream_t st);
-int mg_set_active(int nsys, int *active, const int *src, cudaStream_t st);
+// mixed path: r32 = r64 / scale, e32 = 0, inner norms (active copied from the outer loop)
+int mg_ir_down(const MgProblem &P, const CgWork &Wout, CgWork &W32, const double *r64, float *r32, float *e32,
+               double inner_tol, cudaStream_t st);
+int mg_ir_up(const MgProblem &P, const CgWork &Wout, const float *e32, double *x, cudaStream_t st);
+int mg_zero_rhs_systems(const MgProblem &P, const CgWork &W, double *x, cudaStream_t st);
 
 }  // namespace snac

@@ -14,6 +14,8 @@ enum KernelClass {
   KID_CG_APPLY = 6,      // k_cg_apply
   KID_FILLPS = 7,        // k_fillps
   KID_CORREC = 8,        // k_correc
+  KID_COARSE = 9,        // k_vcycle_coarse
+  KID_SOLVE = 10,        // one whole pressure solve (transforms + Krylov + V-cycles)
 };
 
 void prof_begin(int kid, cudaStream_t st);

@@ -23,6 +23,8 @@ struct MgLevelD {
   const unsigned short *code;        // per cell: bit 15 inactive; bits (2*(2a+s)).. fold type of face (a,s)
   const double *cc, *cp[3], *W[3];
   const float *ccf, *cpf[3], *Wf[3];
+  const double *w01;                 // plane mode: W0(i) * W1(j) per cell (weight of the wavenumber shift)
+  const float *w01f;
   double *x, *b, *r;                 // ncell*nsys, FP64 path
   float *xf, *bf, *rf;               // ncell*nsys, FP32 path
   const double *dinv;                // coarsest: ncell^2 per system
@@ -39,22 +41,27 @@ struct MgProblem {
   const double *shift;               // per system (lambda_k), device
   const float *shiftf;
   const int *singular;               // per system, device
-  int fused;                         // 1: tiled smoother + one-CTA coarse tail; 0: one kernel per sweep
+  int fused;                         // bits: 1/4 tiled plane smoother FP32/FP64, 2/8 one-CTA coarse tail FP32/FP64
   int cta_level[2];                  // first level run by k_vcycle_coarse ([0] FP32, [1] FP64); nlev = none
 };
 
 struct MgGeom;
+// fused kernels (k_mg_fused.cu)
+bool tile2d_ok(const MgProblem &P, int l, int prec);
+int tile2d_max_tiles(const MgLevelD &L);
 template <typename T>
 int launch_rbgs_tile2d(const MgProblem &P, int l, const T *shift, const int *active, int first_color, int mode,
-                       T *x, const T *b, const T *xc, cudaStream_t st);
+                       T *x, const T *b, const T *xc, double *part_bx, int part_stride, int *nchunk, cudaStream_t st);
 template <typename T>
 size_t coarse_smem_bytes(const MgProblem &P, int l0);
+constexpr size_t MG_COARSE_SMEM_MAX = 200 * 1024;
 template <typename T>
-int launch_vcycle_coarse(const MgProblem &P, const MgGeom &G, int l0, const T *shift, const int *active, T *x,
-                         const T *b, cudaStream_t st);
+int launch_vcycle_coarse(const MgProblem &P, int l0, const T *shift, const int *active, T *x, const T *b,
+                         cudaStream_t st);
 
 // kernels (k_mg.cu) -- T = double or float
 template <typename T> int mg_vcycle(const MgProblem &P, int l, const int *active, cudaStream_t st);
-template <typename T> int mg_apply(const MgProblem &P, const T *x, T *y, double *part, const int *active, cudaStream_t st);
+int mg_set_active(int nsys, int *active, const int *src, cudaStream_t st);
+int mg_partial_stride(const MgProblem &P);  // capacity of one system's row of partial sums
 
 }  // namespace snac

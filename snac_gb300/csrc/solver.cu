@@ -11,8 +11,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <cstdlib>
 
 #include "snac_host.h"
+#include "snac_prof.h"
 
 namespace snac {
 
@@ -428,6 +430,13 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
   }
   S.host_levels = (int)B.L.size();
   S.host_coarse_cells = B.L.back().ncell;
+  // launch limits of the level kernels: 32-bit cell index within a system, grid.y over rows / 8,
+  // grid.z over the systems (plane mode) or the k planes (3-D mode)
+  if (L0.ncell > 0x7fffffffL || (L0.n[1] + 7) / 8 > 65535 || (S.mode3d ? L0.n[2] : S.nsys) > 65535) {
+    set_error("solver box of %d x %d x %d cells (%d systems) exceeds the kernel launch limits", L0.n[0], L0.n[1],
+              L0.n[2], S.nsys);
+    return SNAC_ERR_UNSUPPORTED;
+  }
   if (!upload) return SNAC_OK;
   // upload
   MgProblem &P = S.P;
@@ -459,6 +468,13 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
       D.W[a] = (const double *)up(h.W[a].data(), h.W[a].size() * sizeof(double));
       D.Wf[a] = upf(h.W[a]);
     }
+    if (!S.mode3d) {
+      std::vector<double> w01(h.ncell);
+      for (int j = 0; j < h.n[1]; j++)
+        for (int i = 0; i < h.n[0]; i++) w01[i + (size_t)h.n[0] * j] = h.W[0][i] * h.W[1][j];
+      D.w01 = (const double *)up(w01.data(), w01.size() * sizeof(double));
+      D.w01f = upf(w01);
+    }
     const size_t nv = (size_t)h.ncell * S.nsys;
     D.x = (double *)S.alloc(nv * sizeof(double));
     D.b = (double *)S.alloc(nv * sizeof(double));
@@ -472,14 +488,16 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
   }
   // fused kernels: tiled plane smoother and a one-CTA coarse tail where its levels fit in shared memory
   {
+    // SNAC_MG_FUSE bit mask: 1 tiled smoother FP32, 2 coarse tail FP32, 4 tiled FP64, 8 coarse tail FP64.
+    // Default 11: the tile's redundant halo updates cost more than they save where FP64 arithmetic bounds.
     const char *e = getenv("SNAC_MG_UNFUSED");
-    P.fused = (e && e[0] && e[0] != '0') ? 0 : 1;
-    const size_t budget = 96 * 1024;
+    const char *m = getenv("SNAC_MG_FUSE");
+    P.fused = (e && e[0] && e[0] != '0') ? 0 : (m && m[0]) ? (int)strtol(m, nullptr, 0) & 15 : 11;
     for (int prec = 0; prec < 2; prec++) {
       P.cta_level[prec] = P.nlev;
-      for (int l = 1; l < P.nlev; l++) {
+      for (int l = 0; l < P.nlev && !S.mode3d; l++) {
         const size_t bytes = prec ? coarse_smem_bytes<double>(P, l) : coarse_smem_bytes<float>(P, l);
-        if (bytes <= budget) { P.cta_level[prec] = l; break; }
+        if (bytes <= MG_COARSE_SMEM_MAX) { P.cta_level[prec] = l; break; }
       }
     }
   }
@@ -488,11 +506,10 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
   P.singular = (const int *)up(singular.data(), singular.size() * sizeof(int));
   S.ncell0 = L0.ncell;
   const size_t nv0 = (size_t)L0.ncell * S.nsys;
-  const int nchunk = (int)((L0.ncell + 255) / 256);
+  const int stride = mg_partial_stride(P);
   S.box_b = (double *)S.alloc(nv0 * sizeof(double));
   S.box_x = (double *)S.alloc(nv0 * sizeof(double));
   S.r64 = (double *)S.alloc(nv0 * sizeof(double));
-  S.box_b32 = (float *)S.alloc(nv0 * sizeof(float));
   S.box_e32 = (float *)S.alloc(nv0 * sizeof(float));
   S.active_outer = (int *)S.alloc(S.nsys * sizeof(int));
   S.sc_outer = (SysScal *)S.alloc(S.nsys * sizeof(SysScal));
@@ -501,14 +518,19 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
     W->r = S.alloc(nv0 * es);
     W->z = S.alloc(nv0 * es);
     W->p = S.alloc(nv0 * es);
+    W->p2 = W == &S.W32 ? S.alloc(nv0 * es) : nullptr;
     W->q = S.alloc(nv0 * es);
-    W->part0 = (double *)S.alloc((size_t)nchunk * S.nsys * sizeof(double));
-    W->part1 = (double *)S.alloc((size_t)nchunk * S.nsys * sizeof(double));
+    W->stride = stride;
+    for (double **pp : {&W->part0, &W->part1, &W->part2}) *pp = (double *)S.alloc((size_t)stride * S.nsys * sizeof(double));
     W->sc = (SysScal *)S.alloc(S.nsys * sizeof(SysScal));
     W->active = (int *)S.alloc(S.nsys * sizeof(int));
-    W->d_count = (int *)S.alloc(sizeof(int));
-    SNAC_CUDA(cudaMallocHost(&W->h_count, sizeof(int)));
-    if (!W->r || !W->p || !W->part0 || !W->sc) { set_error("device allocation failed for Krylov vectors"); return SNAC_ERR_NOMEM; }
+    W->d_count = (int *)S.alloc(2 * sizeof(int));
+    SNAC_CUDA(cudaMallocHost(&W->h_count, 2 * sizeof(int)));
+    if (!W->r || !W->z || !W->p || !W->q || (W == &S.W32 && !W->p2) || !W->part0 || !W->part1 || !W->part2 || !W->sc ||
+        !W->active || !W->d_count) {
+      set_error("device allocation failed for Krylov vectors");
+      return SNAC_ERR_NOMEM;
+    }
   }
   return SNAC_OK;
 }
@@ -518,51 +540,50 @@ static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *
   MgProblem &P = S.P;
   SNAC_TRY(mg_project_singular(P, S.W64, S.box_b, st));
   trace("solve: projection of singular systems", st);
-  int iters = 0;
+  std::vector<SysScal> sc(P.nsys);
+  double worst = 0.0;
   if (S.precision == 0) {
-    SNAC_TRY(mg_set_active(P.nsys, S.W64.active, nullptr, st));
-    SNAC_TRY(mg_pcg<double>(P, S.W64, S.box_x, S.box_b, S.maxiter, S.tol, true, &iters, st));
-    // final residual report
-    std::vector<SysScal> sc(P.nsys);
-    SNAC_CUDA(cudaMemcpyAsync(sc.data(), S.W64.sc, P.nsys * sizeof(SysScal), cudaMemcpyDeviceToHost, st));
+    CgWork &W = S.W64;
+    int iters = 0;
+    SNAC_TRY(mg_set_active(P.nsys, W.active, nullptr, st));
+    SNAC_TRY(mg_residual<double>(P, W, S.box_x, S.box_b, (double *)W.r, S.tol, 1, 0, 0, st));
+    SNAC_CUDA(cudaMemcpyAsync(W.h_count, W.d_count, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     SNAC_CUDA(cudaStreamSynchronize(st));
-    double worst = 0.0;
+    if (W.h_count[1]) SNAC_TRY(mg_zero_rhs_systems(P, W, S.box_x, st));
+    trace("pcg64: initial residual", st);
+    if (W.h_count[0]) SNAC_TRY(mg_pcg<double>(P, W, S.box_x, S.maxiter, S.tol, false, true, &iters, st));
+    SNAC_CUDA(cudaMemcpyAsync(sc.data(), W.sc, P.nsys * sizeof(SysScal), cudaMemcpyDeviceToHost, st));
+    SNAC_CUDA(cudaStreamSynchronize(st));
     for (auto &v : sc) worst = std::max(worst, v.rel);
     *iters_out = iters;
     *res_out = worst;
     return (worst > S.tol && iters >= S.maxiter) ? SNAC_ERR_NOT_CONVERGED : SNAC_OK;
   }
-  // mixed precision: iterative refinement in FP64 around FP32 Krylov solves
+  // mixed precision: iterative refinement in FP64 around FP32 Krylov solves (zero initial guess)
   const int inner = 4;
   const double inner_tol = 1e-5;
-  int outer = 0, total_inner = 0;
+  int outer = 0;
   CgWork Wr = S.W64;  // residual-only use of the FP64 work area
   Wr.active = S.active_outer;
   Wr.sc = S.sc_outer;
   SNAC_TRY(mg_set_active(P.nsys, S.active_outer, nullptr, st));
-  double worst = 0.0;
   for (outer = 0; outer < S.maxiter; outer++) {
-    int it0 = 0;
-    // r64 = b - A x64 with norms/convergence (0 Krylov iterations)
-    Wr.r = S.r64;
-    SNAC_TRY(mg_pcg<double>(P, Wr, S.box_x, S.box_b, 0, S.tol, false, &it0, st));
-    SNAC_CUDA(cudaMemcpyAsync(Wr.h_count, Wr.d_count, sizeof(int), cudaMemcpyDeviceToHost, st));
+    // r64 = b - A x64 with norms, convergence and the scale of the FP32 residual
+    SNAC_TRY(mg_residual<double>(P, Wr, S.box_x, S.box_b, S.r64, S.tol, outer == 0 ? 1 : 0, 1, S.nact0, st));
+    SNAC_CUDA(cudaMemcpyAsync(Wr.h_count, Wr.d_count, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     SNAC_CUDA(cudaStreamSynchronize(st));
-    if (*Wr.h_count == 0) break;
-    SNAC_TRY(mg_ir_down(P, Wr, S.r64, S.box_b32, S.box_e32, S.nact0, st));
-    SNAC_TRY(mg_set_active(P.nsys, S.W32.active, S.active_outer, st));
+    if (outer == 0 && Wr.h_count[1]) SNAC_TRY(mg_zero_rhs_systems(P, Wr, S.box_x, st));
+    if (Wr.h_count[0] == 0) break;
+    SNAC_TRY(mg_ir_down(P, Wr, S.W32, S.r64, (float *)S.W32.r, S.box_e32, inner_tol, st));
     int it1 = 0;
-    SNAC_TRY(mg_pcg<float>(P, S.W32, S.box_e32, S.box_b32, inner, inner_tol, false, &it1, st));
-    total_inner += it1;
+    SNAC_TRY(mg_pcg<float>(P, S.W32, S.box_e32, inner, inner_tol, true, false, &it1, st));
     SNAC_TRY(mg_ir_up(P, Wr, S.box_e32, S.box_x, st));
   }
-  std::vector<SysScal> sc(P.nsys);
   SNAC_CUDA(cudaMemcpyAsync(sc.data(), S.sc_outer, P.nsys * sizeof(SysScal), cudaMemcpyDeviceToHost, st));
   SNAC_CUDA(cudaStreamSynchronize(st));
   for (auto &v : sc) worst = std::max(worst, v.rel);
   *iters_out = outer;
   *res_out = worst;
-  (void)total_inner;
   return (outer >= S.maxiter && worst > S.tol) ? SNAC_ERR_NOT_CONVERGED : SNAC_OK;
 }
 
@@ -570,6 +591,7 @@ static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *
 int solver_solve_pressure(Domain &d, PoissonSolver &S) {
   cudaStream_t st = d.st;
   trace("solve: start", st);
+  prof_begin(KID_SOLVE, st);
   if (S.fft_axis) SNAC_TRY(fft_forward_to_box(d, S, st));
   else SNAC_TRY(box_gather(d, S, st));
   trace("solve: forward transform / gather", st);
@@ -580,6 +602,7 @@ int solver_solve_pressure(Domain &d, PoissonSolver &S) {
   if (rc != SNAC_OK && rc != SNAC_ERR_NOT_CONVERGED) return rc;
   if (S.fft_axis) SNAC_TRY(fft_backward_from_box(d, S, st));
   else SNAC_TRY(box_scatter(d, S, st));
+  prof_end(KID_SOLVE, st);
   trace("solve: backward transform / scatter", st);
   S.last_iters = it;
   S.last_res = res;

@@ -130,12 +130,18 @@ def test_solve_pressure_matches_oracle(snac_lib, oracle_mod, precision):
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("which", ["channel", "ldc3d"])
 def test_fused_vcycle_matches_unfused(snac_lib, monkeypatch, precision, which):
-    """The tiled smoother / one-CTA coarse tail give the same solves as one kernel per sweep."""
+    """The tiled smoother / one-CTA coarse tail give the same solves as one kernel per sweep.
+
+    The V-cycles agree term by term; r.z is summed in a different order (tile partials against
+    flat partials), so the two converged solutions agree to the solver tolerance, not bitwise.
+    """
     case = (cases.channel_4block(nx=(32, 64), ny=(32, 48), nz=8) if which == "channel"
             else cases.lid_driven_cavity(32))
     out = {}
     for mode in ("1", "0"):
+        # "1": one kernel per sweep; "0": every fused kernel of both precisions (mask 15)
         monkeypatch.setenv("SNAC_MG_UNFUSED", mode)
+        monkeypatch.setenv("SNAC_MG_FUSE", "15")
         d = Domain(case, precision=precision)
         try:
             rng = np.random.default_rng(11)
@@ -150,8 +156,10 @@ def test_fused_vcycle_matches_unfused(snac_lib, monkeypatch, precision, which):
         finally:
             d.close()
     for a, b in zip(out["1"], out["0"]):
+        a, b = a[1:-1, 1:-1, 1:-1], b[1:-1, 1:-1, 1:-1]
+        a, b = a - a.mean(), b - b.mean()  # both cases have a singular (mean-free) wavenumber
         scale = np.max(np.abs(a))
-        assert np.max(np.abs(a - b)) <= 1e-12 * scale
+        assert np.max(np.abs(a - b)) <= 1e-9 * scale
 
 
 def _run_both(case, oracle_mod, nsteps, precision=0, seed=3, amp=0.1):
