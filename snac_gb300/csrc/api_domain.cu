@@ -683,6 +683,8 @@ int snac_solve_pressure(void) {
   NEED_DOMAIN
   const int rc = solver_solve_pressure(*d, *d->ps);
   SNAC_CUDA(cudaStreamSynchronize(d->st));
+  d->last_solve_iters = d->ps->last_iters;  // the statistics then describe this solve
+  d->last_solve_res = d->ps->last_res;
   return rc;
 }
 int snac_correc_all(double dtrk) {

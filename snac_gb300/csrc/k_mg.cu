@@ -38,9 +38,11 @@ inline dim3 grid_cell(const MgProblem &P, const MgLevelD &L) {
 inline dim3 grid_red(const MgProblem &P, const MgLevelD &L) {
   return dim3((unsigned)((L.n[0] + 31) / 32), (unsigned)((L.n[1] + 31) / 32), zdim(P, L));
 }
+// partials per system of the reducing stencil kernels (generic 3-D ones, or the plane ones)
 inline int nchunk_red(const MgProblem &P, const MgLevelD &L) {
+  if (!P.mode3d) return plane_nchunk(L);
   const dim3 g = grid_red(P, L);
-  return (int)(g.x * g.y * (P.mode3d ? g.z : 1u));
+  return (int)(g.x * g.y * g.z);
 }
 inline dim3 grid_flat(long n, int nsys) { return dim3((unsigned)((n + FLAT - 1) / FLAT), (unsigned)nsys); }
 const dim3 BLK(32, 8);
@@ -70,7 +72,7 @@ __global__ void __launch_bounds__(256) k_rbgs(MgLevelD L, MgGeom G, const T *shi
   T *__restrict__ xs = x + off;
   const T d = diag_of<T>(L, G, G.mode3d ? T(0) : shift[s], c);
   const T acc = offdiag<T>(L, G, [&](int e) { return xs[e]; }, c, i, j, k);
-  xs[c] = (b[off + c] - acc) * (T(1) / d);
+  xs[c] = (b[off + c] - acc) * rcpt(d);
 }
 
 // coarse b <- sum over children of (b - A x) on the fine level; coarse x <- 0
@@ -162,25 +164,35 @@ int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, c
       const dim3 g((unsigned)((L.ncell + 255) / 256), P.nsys);
       k_zero<T><<<g, 256, 0, st>>>(L.ncell, x, P.nsys, active);
       for (int it = 0; it < 40; it++)
-        for (int col : {0, 1, 1, 0}) k_rbgs<T><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, col, x, b);
+        for (int col : {0, 1, 1, 0}) {
+          if (P.mode3d) k_rbgs<T><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, col, x, b);
+          else SNAC_TRY(plane_sweep<T>(P, l, shift, active, col, x, b, st));
+        }
     }
     SNAC_CUDA(cudaGetLastError());
     return SNAC_OK;
   }
   const MgLevelD &C = P.L[l + 1];
   if ((fuse & 1) && tile2d_ok(P, l, prec)) {
-    SNAC_TRY(launch_rbgs_tile2d<T>(P, l, shift, active, 0, 0, x, b, (const T *)nullptr, nullptr, 0, nullptr, st));
-    prof_begin(KID_RESTRICT, st);
-    k_resid_restrict<T><<<grid_cell(P, C), BLK, 0, st>>>(L, C, G, shift, active, x, b, LA<T>::b(C), LA<T>::x(C));
-    prof_end(KID_RESTRICT, st);
-    SNAC_CUDA(cudaGetLastError());
+    T *xp = LA<T>::xp(P.L[l]);  // pre-smoothed x (the post-smoother reads it while writing x)
+    SNAC_TRY(launch_rbgs_tile2d<T>(P, l, active, 0, 0, xp, b, (const T *)nullptr, (const T *)nullptr, nullptr, 0,
+                                   nullptr, st));
+    SNAC_TRY(plane_restrict<T>(P, l, shift, active, xp, b, LA<T>::b(C), LA<T>::x(C), st));
     SNAC_TRY(mg_vcycle_impl<T>(P, G, l + 1, shift, active, nullptr, 0, nullptr, st));
-    return launch_rbgs_tile2d<T>(P, l, shift, active, 1, 1, x, b, (const T *)LA<T>::x(C), part_bx, part_stride,
-                                 nchunk_bx, st);
+    return launch_rbgs_tile2d<T>(P, l, active, 1, 1, x, b, (const T *)xp, (const T *)LA<T>::x(C), part_bx,
+                                 part_stride, nchunk_bx, st);
   }
   if (l == 0) {  // coarse x is zeroed by the restriction
     const dim3 g((unsigned)((L.ncell + 255) / 256), P.nsys);
     k_zero<T><<<g, 256, 0, st>>>(L.ncell, x, P.nsys, active);
+  }
+  if (!P.mode3d) {  // plane systems: kernels batched over systems
+    for (int it = 0; it < 2 * P.nu; it++) SNAC_TRY(plane_sweep<T>(P, l, shift, active, it & 1, x, b, st));
+    SNAC_TRY(plane_restrict<T>(P, l, shift, active, x, b, LA<T>::b(C), LA<T>::x(C), st));
+    SNAC_TRY(mg_vcycle_impl<T>(P, G, l + 1, shift, active, nullptr, 0, nullptr, st));
+    SNAC_TRY(plane_prolong<T>(P, l, active, x, LA<T>::x(C), st));
+    for (int it = 0; it < 2 * P.nu; it++) SNAC_TRY(plane_sweep<T>(P, l, shift, active, 1 - (it & 1), x, b, st));
+    return SNAC_OK;
   }
   for (int it = 0; it < 2 * P.nu; it++) {
     prof_begin(KID_RBGS, st);
@@ -525,8 +537,11 @@ int mg_residual(const MgProblem &P, CgWork &W, const T *x, const T *b, T *r, dou
                 long nact, cudaStream_t st) {
   const MgGeom G = geom_of(P);
   const MgLevelD &L0 = P.L[0];
-  k_cg_resid<T><<<grid_red(P, L0), BLK, 0, st>>>(L0, G, shift_of<T>(P), W.active, x, b, r, W.part0,
-                                                 set_bb ? W.part1 : nullptr, W.stride);
+  if (P.mode3d)
+    k_cg_resid<T><<<grid_red(P, L0), BLK, 0, st>>>(L0, G, shift_of<T>(P), W.active, x, b, r, W.part0,
+                                                   set_bb ? W.part1 : nullptr, W.stride);
+  else
+    SNAC_TRY(plane_resid<T>(P, shift_of<T>(P), W.active, x, b, r, W.part0, set_bb ? W.part1 : nullptr, W.stride, st));
   SNAC_CUDA(cudaMemsetAsync(W.d_count, 0, 2 * sizeof(int), st));
   k_cg_norms<<<P.nsys, 256, 0, st>>>(W.active, nullptr, W.sc, W.part0, W.part1, W.stride, nchunk_red(P, L0), tol,
                                      set_bb, want_scale, nact, W.d_count);
@@ -579,13 +594,19 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
     k_cg_beta<<<P.nsys, 256, 0, st>>>(W.active, W.sc, W.part2, W.stride, nrz);
     prof_begin(KID_CG_APPLY, st);
     if constexpr (fusep) {
-      k_cg_apply<T, true><<<grid_red(P, L0), BLK, 0, st>>>(L0, G, shift, W.active, W.sc, z, p, pn, q, W.part1,
-                                                           W.stride);
+      if (P.mode3d)
+        k_cg_apply<T, true><<<grid_red(P, L0), BLK, 0, st>>>(L0, G, shift, W.active, W.sc, z, p, pn, q, W.part1,
+                                                             W.stride);
+      else
+        SNAC_TRY((plane_apply<T, true>(P, shift, W.active, W.sc, z, p, pn, q, W.part1, W.stride, st)));
       std::swap(p, pn);
     } else {
       k_cg_p<T><<<gf, 256, 0, st>>>(n, W.active, W.sc, z, p);
-      k_cg_apply<T, false><<<grid_red(P, L0), BLK, 0, st>>>(L0, G, shift, W.active, W.sc, z, p, nullptr, q, W.part1,
-                                                            W.stride);
+      if (P.mode3d)
+        k_cg_apply<T, false><<<grid_red(P, L0), BLK, 0, st>>>(L0, G, shift, W.active, W.sc, z, p, nullptr, q,
+                                                              W.part1, W.stride);
+      else
+        SNAC_TRY((plane_apply<T, false>(P, shift, W.active, W.sc, z, p, nullptr, q, W.part1, W.stride, st)));
     }
     prof_end(KID_CG_APPLY, st);
     k_cg_alpha<<<P.nsys, 256, 0, st>>>(W.active, W.sc, W.part1, W.stride, nred);

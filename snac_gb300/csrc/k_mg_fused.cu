@@ -11,7 +11,9 @@
 //   can differ from a global sweep, so the output cells are exact after TH.
 //   The pre-smoother starts from x = 0 without reading x; the post-smoother adds
 //   the coarse-grid correction while loading (prolongation fused) and can emit
-//   the partials of b.x (r.z of the Krylov iteration).
+//   the partials of b.x (r.z of the Krylov iteration).  Tiles overlap, so a
+//   launch never reads the array it writes: the pre-smoother writes xp and the
+//   post-smoother reads xp + correction and writes x.
 // k_vcycle_coarse: one CTA of 1024 threads per system runs the V-cycle from
 //   level l0 down to the coarsest solve and back, with x, b, the diagonal and
 //   the couplings of every level in shared memory.
@@ -19,6 +21,8 @@
 // term by term, so fused and unfused V-cycles give identical results.
 #include <algorithm>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "snac_solver.h"
 #include "snac_mgk.h"
@@ -31,21 +35,24 @@ namespace {
 constexpr int TH = 4;              // tile halo = most half-sweeps per launch (2 nu with nu <= 2)
 constexpr int TSW = 64;            // tile width
 constexpr int TBX = TSW - 2 * TH;  // output columns per tile
-inline int tile_by(int R) { return 8 * R - 2 * TH; }
-inline int tiles_for(const MgLevelD &L, int R) {
-  return ((L.n[0] + TBX - 1) / TBX) * ((L.n[1] + tile_by(R) - 1) / tile_by(R));
+// tile shapes: NW warps x R rows per warp = tile height SH (output rows SH - 2 TH)
+struct TileShape { int nw, r; };
+const TileShape SHAPES_F[] = {{8, 2}, {8, 3}, {16, 2}, {16, 3}};
+const TileShape SHAPES_D[] = {{8, 2}};
+inline int tile_by(TileShape t) { return t.nw * t.r - 2 * TH; }
+inline int tiles_for(const MgLevelD &L, TileShape t) {
+  return ((L.n[0] + TBX - 1) / TBX) * ((L.n[1] + tile_by(t) - 1) / tile_by(t));
 }
-// rows per warp: the choice that processes the fewest tile rows (ties: the smaller tile)
-int choose_rows(const MgLevelD &L, int prec) {
-  static const int rf[] = {2, 3, 4, 6}, rd[] = {2, 3};
-  const int *opts = prec ? rd : rf;
-  const int nopt = prec ? 2 : 4;
-  int best = opts[0];
+// the shape that processes the fewest tile rows (ties: the smaller tile)
+TileShape choose_shape(const MgLevelD &L, int prec) {
+  const TileShape *opts = prec ? SHAPES_D : SHAPES_F;
+  const int nopt = prec ? 1 : 4;
+  TileShape best = opts[0];
   long bestc = -1;
   for (int q = 0; q < nopt; q++) {
-    const int R = opts[q];
-    const long cost = (long)((L.n[1] + tile_by(R) - 1) / tile_by(R)) * 8 * R;
-    if (bestc < 0 || cost < bestc) { bestc = cost; best = R; }
+    const TileShape t = opts[q];
+    const long cost = (long)((L.n[1] + tile_by(t) - 1) / tile_by(t)) * t.nw * t.r;
+    if (bestc < 0 || cost < bestc) { bestc = cost; best = t; }
   }
   return best;
 }
@@ -56,123 +63,189 @@ __device__ __forceinline__ int wrap(int g, int n) {
 }
 }  // namespace
 
-int tile2d_max_tiles(const MgLevelD &L) { return tiles_for(L, 2); }
+int tile2d_max_tiles(const MgLevelD &L) { return tiles_for(L, TileShape{8, 2}); }
 
 bool tile2d_ok(const MgProblem &P, int l, int prec) {
   (void)prec;
   if (P.mode3d || l >= P.nlev - 1 || 2 * P.nu > TH) return false;
   const MgLevelD &L = P.L[l];
+  if (!L.xp || !L.xpf || !L.invd || !L.invdf) return false;
+  if (L.n[0] & 1) return false;  // column pairs are copied as one aligned unit
   for (int a = 0; a < 2; a++)
     if (P.periodic[a] && L.n[a] > 1 && (L.n[a] & 1)) return false;  // red-black colouring must wrap consistently
   return true;
 }
 
-template <typename T, int R>
-__global__ void __launch_bounds__(256) k_rbgs_tile2d(MgLevelD L, MgLevelD C, int per0, int per1,
-                                                     const T *__restrict__ shift, const int *__restrict__ active,
-                                                     int first_color, int nhalf, int mode, T *__restrict__ x,
-                                                     const T *__restrict__ b, const T *__restrict__ xc,
-                                                     double *__restrict__ part_bx, int part_stride) {
-  constexpr int SH = 8 * R, BY = SH - 2 * TH;
-  __shared__ T xe[SH][32], xo[SH][32];
-  const int s = blockIdx.y;
-  if (active && !active[s]) return;
+// dynamic shared memory of one tile CTA: the even/odd x tile and two stages of the staged inputs
+// (b and 1/d; in mode 1 also the pre-smoothed x and the coarse correction), [stage][array][row][64]
+template <typename T>
+inline size_t tile_smem_bytes(int sh, int mode) {
+  return (2 * (size_t)sh * 32 + 2 * (size_t)(mode == 1 ? 4 : 2) * sh * 64) * sizeof(T);
+}
+
+template <typename T, int NW, int R>
+__global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C, int per0, int per1,
+                                                         const int *__restrict__ active, int nsys, int sb,
+                                                         int first_color, int nhalf, int mode, T *__restrict__ x,
+                                                         const T *__restrict__ b, const T *__restrict__ xin,
+                                                         const T *__restrict__ xc, double *__restrict__ part_bx,
+                                                         int part_stride) {
+  constexpr int SH = NW * R, BY = SH - 2 * TH;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T(*xe)[32] = reinterpret_cast<T(*)[32]>(smem_raw);
+  T(*xo)[32] = xe + SH;
+  T *const stg = reinterpret_cast<T *>(smem_raw) + 2 * SH * 32;
+  const int NA = mode == 1 ? 4 : 2;
+  auto S = [&](int k, int a, int r) -> T * { return stg + ((size_t)(k * NA + a) * SH + r) * 64; };
   const int n0 = L.n[0], n1 = L.n[1];
   const int ntx = (n0 + TBX - 1) / TBX;
   const int i0 = (int)(blockIdx.x % ntx) * TBX - TH, j0 = (int)(blockIdx.x / ntx) * BY - TH;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const long off = L.ncell * s;
-  const T sh = shift[s];
   const bool skip0 = per0 && n0 == 1, skip1 = per1 && n1 == 1;
-  const T *__restrict__ cc = LA<T>::cc(L);
-  const T *__restrict__ w01 = LA<T>::w01(L);
-  const T *__restrict__ cp0 = LA<T>::cp(L, 0);
-  const T *__restrict__ cp1 = LA<T>::cp(L, 1);
-  T bv[R][2], iv[R][2], ce[R][2], cw[R][2], cn[R][2], cs[R][2];
+  // wrapped global coordinates of the owned cells (-1: outside a non-periodic boundary); with n0 even
+  // and i0 even the pair (2 lane, 2 lane + 1) is never split by a boundary or a wrap
+  int gi0, gj[R];
+  {
+    const int g = i0 + 2 * lane;
+    gi0 = (g >= 0 && g < n0) ? g : (per0 ? wrap(g, n0) : -1);
+  }
 #pragma unroll
   for (int q = 0; q < R; q++) {
-    const int r = w + 8 * q;
+    const int g = j0 + w + NW * q;
+    gj[q] = (g >= 0 && g < n1) ? g : (per1 ? wrap(g, n1) : -1);
+  }
+  // couplings of the owned cells, the same for every system; bit 2q+p of `live`: active cell
+  const T *__restrict__ cp0 = LA<T>::cp(L, 0);
+  const T *__restrict__ cp1 = LA<T>::cp(L, 1);
+  const T *__restrict__ invd = LA<T>::invd(L);
+  T ce[R][2], cw[R][2], cn[R][2], cs[R][2];
+  unsigned live = 0;
+#pragma unroll
+  for (int q = 0; q < R; q++) {
 #pragma unroll
     for (int p = 0; p < 2; p++) {
-      int gi = i0 + 2 * lane + p, gj = j0 + r;
-      bool in = true;
-      if (gi < 0 || gi >= n0) { if (per0) gi = wrap(gi, n0); else in = false; }
-      if (gj < 0 || gj >= n1) { if (per1) gj = wrap(gj, n1); else in = false; }
-      T b_ = 0, i_ = 0, e_ = 0, w_ = 0, n_ = 0, s_ = 0, x_ = 0;
-      if (in) {
-        const int c = gi + n0 * gj;
+      T e_ = 0, w_ = 0, n_ = 0, s_ = 0;
+      if (gi0 >= 0 && gj[q] >= 0) {
+        const int ii = gi0 + p, jj = gj[q], c = ii + n0 * jj;
         if (!(L.code[c] & 0x8000)) {
-          i_ = T(1) / fmat(sh, w01[c], cc[c]);
-          b_ = b[off + c];
+          live |= 1u << (2 * q + p);
           if (!skip0) {
             e_ = cp0[c];
-            w_ = gi > 0 ? cp0[c - 1] : (per0 ? cp0[c + n0 - 1] : T(0));
+            w_ = ii > 0 ? cp0[c - 1] : (per0 ? cp0[c + n0 - 1] : T(0));
           }
           if (!skip1) {
             n_ = cp1[c];
-            s_ = gj > 0 ? cp1[c - n0] : (per1 ? cp1[c + n0 * (n1 - 1)] : T(0));
-          }
-          if (mode == 1) {
-            const int I = C.coarsened[0] ? gi / 2 : gi, J = C.coarsened[1] ? gj / 2 : gj;
-            x_ = x[off + c] + xc[C.ncell * s + I + C.n[0] * J];
+            s_ = jj > 0 ? cp1[c - n0] : (per1 ? cp1[c + n0 * (n1 - 1)] : T(0));
           }
         }
       }
-      bv[q][p] = b_;
-      iv[q][p] = i_;
       ce[q][p] = e_;
       cw[q][p] = w_;
       cn[q][p] = n_;
       cs[q][p] = s_;
-      if (p) xo[r][lane] = x_;
-      else xe[r][lane] = x_;
     }
   }
-  for (int t = 0; t < nhalf; t++) {
-    __syncthreads();
-    const int color = (first_color + t) & 1;
+  // stage the inputs of system `sys` (each thread copies exactly the cells it owns)
+  const bool xhalf = C.coarsened[0] != 0, yhalf = C.coarsened[1] != 0;
+  auto issue = [&](int sys, int k) {
+    const long off = L.ncell * (long)sys, offc = C.ncell * (long)sys;
 #pragma unroll
     for (int q = 0; q < R; q++) {
-      const int r = w + 8 * q;
-      if (r == 0 || r == SH - 1) continue;
-      if (((color + i0 + j0 + r) & 1) == 0) {  // even column 2*lane: E = odd(lane), W = odd(lane-1)
-        const T xE = xo[r][lane];
-        const T xW = lane > 0 ? xo[r][lane - 1] : T(0);
-        T acc = fmat(ce[q][0], xE, T(0));
-        acc = fmat(cw[q][0], xW, acc);
-        acc = fmat(cn[q][0], xe[r + 1][lane], acc);
-        acc = fmat(cs[q][0], xe[r - 1][lane], acc);
-        if (lane > 0) xe[r][lane] = (bv[q][0] - acc) * iv[q][0];
-      } else {                                  // odd column 2*lane+1: E = even(lane+1), W = even(lane)
-        const T xE = lane < 31 ? xe[r][lane + 1] : T(0);
-        const T xW = xe[r][lane];
-        T acc = fmat(ce[q][1], xE, T(0));
-        acc = fmat(cw[q][1], xW, acc);
-        acc = fmat(cn[q][1], xo[r + 1][lane], acc);
-        acc = fmat(cs[q][1], xo[r - 1][lane], acc);
-        if (lane < 31) xo[r][lane] = (bv[q][1] - acc) * iv[q][1];
+      const int r = w + NW * q;
+      const bool in = gi0 >= 0 && gj[q] >= 0;
+      const long c = in ? (long)gi0 + (long)n0 * gj[q] : 0;
+      cp_async_zfill<2 * sizeof(T)>(S(k, 0, r) + 2 * lane, b + off + c, in);
+      cp_async_zfill<2 * sizeof(T)>(S(k, 1, r) + 2 * lane, invd + off + c, in);
+      if (mode == 1) {
+        cp_async_zfill<2 * sizeof(T)>(S(k, 2, r) + 2 * lane, xin + off + c, in);
+        const long cc = in ? (long)(xhalf ? gi0 / 2 : gi0) + (long)C.n[0] * (yhalf ? gj[q] / 2 : gj[q]) : 0;
+        if (xhalf) cp_async_zfill<sizeof(T)>(S(k, 3, r) + 2 * lane, xc + offc + cc, in);
+        else cp_async_zfill<2 * sizeof(T)>(S(k, 3, r) + 2 * lane, xc + offc + cc, in);
       }
     }
-  }
-  // every thread stores only cells it updated itself: no barrier needed
-  T bx = 0;
-#pragma unroll
-  for (int q = 0; q < R; q++) {
-    const int r = w + 8 * q;
-#pragma unroll
-    for (int p = 0; p < 2; p++) {
-      const int col = 2 * lane + p;
-      if (r < TH || r >= TH + BY || col < TH || col >= TH + TBX) continue;
-      const int gi = i0 + col, gj = j0 + r;
-      if (gi >= n0 || gj >= n1 || iv[q][p] == T(0)) continue;
-      const T v = p ? xo[r][lane] : xe[r][lane];
-      x[off + gi + n0 * gj] = v;
-      bx = fmat(bv[q][p], v, bx);
+    cp_async_commit();
+  };
+  const int s1 = min(nsys, (int)(blockIdx.y + 1) * sb);
+  auto next_active = [&](int from) {
+    for (int q = from; q < s1; q++)
+      if (!active || active[q]) return q;
+    return -1;
+  };
+  int cur = next_active((int)blockIdx.y * sb), k = 0;
+  if (cur >= 0) issue(cur, 0);
+  while (cur >= 0) {
+    const int nxt = next_active(cur + 1);
+    if (nxt >= 0) {
+      issue(nxt, k ^ 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
     }
-  }
-  if (part_bx) {
-    const double t = block_sum1<T>(bx);
-    if (threadIdx.x == 0) part_bx[(long)s * part_stride + blockIdx.x] = t;
+    __syncthreads();  // the previous system's sweeps have finished with the x tile
+    T bv[R][2], iv[R][2];
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+      const int r = w + NW * q;
+#pragma unroll
+      for (int p = 0; p < 2; p++) {
+        const bool lv = live >> (2 * q + p) & 1;
+        bv[q][p] = lv ? S(k, 0, r)[2 * lane + p] : T(0);
+        iv[q][p] = lv ? S(k, 1, r)[2 * lane + p] : T(0);
+        T x_ = 0;
+        if (mode == 1 && lv) x_ = S(k, 2, r)[2 * lane + p] + S(k, 3, r)[2 * lane + (xhalf ? 0 : p)];
+        if (p) xo[r][lane] = x_;
+        else xe[r][lane] = x_;
+      }
+    }
+    for (int t = 0; t < nhalf; t++) {
+      __syncthreads();
+      const int color = (first_color + t) & 1;
+#pragma unroll
+      for (int q = 0; q < R; q++) {
+        const int r = w + NW * q;
+        if (r == 0 || r == SH - 1) continue;
+        if (((color + i0 + j0 + r) & 1) == 0) {  // even column 2*lane: E = odd(lane), W = odd(lane-1)
+          const T xE = xo[r][lane];
+          const T xW = lane > 0 ? xo[r][lane - 1] : T(0);
+          T acc = fmat(ce[q][0], xE, T(0));
+          acc = fmat(cw[q][0], xW, acc);
+          acc = fmat(cn[q][0], xe[r + 1][lane], acc);
+          acc = fmat(cs[q][0], xe[r - 1][lane], acc);
+          if (lane > 0) xe[r][lane] = (bv[q][0] - acc) * iv[q][0];
+        } else {                                  // odd column 2*lane+1: E = even(lane+1), W = even(lane)
+          const T xE = lane < 31 ? xe[r][lane + 1] : T(0);
+          const T xW = xe[r][lane];
+          T acc = fmat(ce[q][1], xE, T(0));
+          acc = fmat(cw[q][1], xW, acc);
+          acc = fmat(cn[q][1], xo[r + 1][lane], acc);
+          acc = fmat(cs[q][1], xo[r - 1][lane], acc);
+          if (lane < 31) xo[r][lane] = (bv[q][1] - acc) * iv[q][1];
+        }
+      }
+    }
+    // every thread stores only cells it updated itself: no barrier needed here
+    const long off = L.ncell * (long)cur;
+    T bx = 0;
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+      const int r = w + NW * q;
+#pragma unroll
+      for (int p = 0; p < 2; p++) {
+        const int col = 2 * lane + p;
+        if (r < TH || r >= TH + BY || col < TH || col >= TH + TBX) continue;
+        const int ui = i0 + col, uj = j0 + r;  // unwrapped: each global cell is stored by one tile only
+        if (ui >= n0 || uj >= n1 || !(live >> (2 * q + p) & 1)) continue;
+        const T v = p ? xo[r][lane] : xe[r][lane];
+        x[off + ui + n0 * uj] = v;
+        bx = fmat(bv[q][p], v, bx);
+      }
+    }
+    if (part_bx) {
+      const double t = block_sum1<T>(bx);
+      if (threadIdx.x == 0) part_bx[(long)cur * part_stride + blockIdx.x] = t;
+    }
+    cur = nxt;
+    k ^= 1;
   }
 }
 
@@ -189,7 +262,7 @@ __device__ __forceinline__ void cta_sweep_xy(int n0, int n1, int per0, int per1,
     const T dv = d[c];
     if (dv == T(0)) continue;
     const T acc = offdiag_xy<T>(n0, n1, per0, per1, c0, c1, [&](int e) { return x[e]; }, c, i, j);
-    x[c] = (b[c] - acc) * (T(1) / dv);
+    x[c] = (b[c] - acc) * rcpt(dv);
   }
   __syncthreads();
 }
@@ -311,32 +384,60 @@ __global__ void __launch_bounds__(1024, 1) k_vcycle_coarse(MgProblem P, int l0, 
 }
 
 // ---------------------------------------------------------------- launchers
+// opt in to more than 48 KB of dynamic shared memory, once per kernel and device
+static int allow_smem(const void *fn, size_t bytes) {
+  if (bytes <= 48 * 1024) return SNAC_OK;
+  static std::mutex mu;
+  static std::vector<std::pair<const void *, int>> done;
+  int dev = 0;
+  SNAC_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  for (auto &e : done)
+    if (e.first == fn && e.second == dev) return SNAC_OK;
+  SNAC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MG_COARSE_SMEM_MAX));
+  done.push_back({fn, dev});
+  return SNAC_OK;
+}
+
+template <typename T, int NW, int R>
+static int launch_tile(const MgProblem &P, const MgLevelD &L, const MgLevelD &C, int nt, const int *active,
+                       int first_color, int mode, T *x, const T *b, const T *xin, const T *xc, double *part_bx,
+                       int part_stride, cudaStream_t st) {
+  const size_t smem = tile_smem_bytes<T>(NW * R, mode);
+  SNAC_TRY(allow_smem((const void *)k_rbgs_tile2d<T, NW, R>, smem));
+  const int sb = plane_batch(P, nt, NW == 16 ? 2 : 4);
+  const dim3 g((unsigned)nt, (unsigned)((P.nsys + sb - 1) / sb));
+  k_rbgs_tile2d<T, NW, R><<<g, NW * 32, smem, st>>>(L, C, P.periodic[0], P.periodic[1], active, P.nsys, sb,
+                                                    first_color, 2 * P.nu, mode, x, b, xin, xc, part_bx, part_stride);
+  SNAC_CUDA(cudaGetLastError());
+  return SNAC_OK;
+}
+
 template <typename T>
-int launch_rbgs_tile2d(const MgProblem &P, int l, const T *shift, const int *active, int first_color, int mode,
-                       T *x, const T *b, const T *xc, double *part_bx, int part_stride, int *nchunk, cudaStream_t st) {
+int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_color, int mode, T *x, const T *b,
+                       const T *xin, const T *xc, double *part_bx, int part_stride, int *nchunk, cudaStream_t st) {
+  if (mode == 1 && (xin == x || !xin || !xc)) { set_error("tiled post-smoother needs separate input and output"); return SNAC_ERR_ARG; }
   const MgLevelD &L = P.L[l];
   const MgLevelD &C = l + 1 < P.nlev ? P.L[l + 1] : P.L[l];
-  const int R = choose_rows(L, sizeof(T) == 8 ? 1 : 0);
-  const int nt = tiles_for(L, R);
+  const TileShape t = choose_shape(L, sizeof(T) == 8 ? 1 : 0);
+  const int nt = tiles_for(L, t);
   if (part_bx && nt > part_stride) { set_error("partial-sum area too small for the tiled smoother"); return SNAC_ERR_ARG; }
-  const dim3 g((unsigned)nt, (unsigned)P.nsys);
-  const int nh = 2 * P.nu;
   prof_begin(KID_RBGS, st);
-#define SNAC_TILE_LAUNCH(RR)                                                                                        \
-  k_rbgs_tile2d<T, RR><<<g, 256, 0, st>>>(L, C, P.periodic[0], P.periodic[1], shift, active, first_color, nh, mode, \
-                                          x, b, xc, part_bx, part_stride)
+  int rc;
   if constexpr (sizeof(T) == 8) {
-    if (R == 2) SNAC_TILE_LAUNCH(2);
-    else SNAC_TILE_LAUNCH(3);
+    rc = launch_tile<T, 8, 2>(P, L, C, nt, active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
   } else {
-    if (R == 2) SNAC_TILE_LAUNCH(2);
-    else if (R == 3) SNAC_TILE_LAUNCH(3);
-    else if (R == 4) SNAC_TILE_LAUNCH(4);
-    else SNAC_TILE_LAUNCH(6);
+    if (t.nw == 8 && t.r == 2)
+      rc = launch_tile<T, 8, 2>(P, L, C, nt, active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
+    else if (t.nw == 16 && t.r == 2)
+      rc = launch_tile<T, 16, 2>(P, L, C, nt, active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
+    else if (t.nw == 8)
+      rc = launch_tile<T, 8, 3>(P, L, C, nt, active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
+    else
+      rc = launch_tile<T, 16, 3>(P, L, C, nt, active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
   }
-#undef SNAC_TILE_LAUNCH
   prof_end(KID_RBGS, st);
-  SNAC_CUDA(cudaGetLastError());
+  SNAC_TRY(rc);
   if (nchunk) *nchunk = part_bx ? nt : 0;
   return SNAC_OK;
 }
@@ -355,19 +456,7 @@ int launch_vcycle_coarse(const MgProblem &P, int l0, const T *shift, const int *
                          cudaStream_t st) {
   const size_t smem = coarse_smem_bytes<T>(P, l0);
   if (smem > MG_COARSE_SMEM_MAX) { set_error("coarse levels exceed the shared-memory budget"); return SNAC_ERR_ARG; }
-  if (smem > 48 * 1024) {
-    // the opt-in limit is a per-device function attribute: set it once for every device used
-    static std::mutex mu;
-    static unsigned long long done = 0;
-    int dev = 0;
-    SNAC_CUDA(cudaGetDevice(&dev));
-    std::lock_guard<std::mutex> lk(mu);
-    if (dev >= 64 || !(done >> dev & 1ull)) {
-      SNAC_CUDA(cudaFuncSetAttribute((const void *)k_vcycle_coarse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)MG_COARSE_SMEM_MAX));
-      if (dev < 64) done |= 1ull << dev;
-    }
-  }
+  SNAC_TRY(allow_smem((const void *)k_vcycle_coarse<T>, smem));
   prof_begin(KID_COARSE, st);
   k_vcycle_coarse<T><<<P.nsys, 1024, smem, st>>>(P, l0, shift, active, x, b);
   prof_end(KID_COARSE, st);
@@ -375,9 +464,9 @@ int launch_vcycle_coarse(const MgProblem &P, int l0, const T *shift, const int *
   return SNAC_OK;
 }
 
-template int launch_rbgs_tile2d<double>(const MgProblem &, int, const double *, const int *, int, int, double *,
+template int launch_rbgs_tile2d<double>(const MgProblem &, int, const int *, int, int, double *, const double *,
                                         const double *, const double *, double *, int, int *, cudaStream_t);
-template int launch_rbgs_tile2d<float>(const MgProblem &, int, const float *, const int *, int, int, float *,
+template int launch_rbgs_tile2d<float>(const MgProblem &, int, const int *, int, int, float *, const float *,
                                        const float *, const float *, double *, int, int *, cudaStream_t);
 template size_t coarse_smem_bytes<double>(const MgProblem &, int);
 template size_t coarse_smem_bytes<float>(const MgProblem &, int);

@@ -60,6 +60,8 @@ struct PoissonSolver {
   double *d_mat_fwd = nullptr, *d_mat_bwd = nullptr;  // dense r2r matrices (n x n)
   std::vector<double> lambda;
   int precision = 0;
+  int inner_iters = 5;               // mixed path: FP32 Krylov iterations per refinement step
+  double inner_tol = 1e-6;           // mixed path: relative tolerance of the FP32 solve
   double tol = 1e-12;
   int maxiter = 200;
   MgProblem P{};

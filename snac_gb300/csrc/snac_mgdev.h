@@ -4,7 +4,7 @@
 // one-CTA kernels) forms the same sums in the same order with explicit FMAs:
 //   diagonal  d   = fma(lambda_s, w01, cc)          (plane mode; cc alone in 3-D)
 //   couplings acc = +x, -x, +y, -y (, +z, -z) terms, each acc = fma(c, v, acc)
-//   smoother  x   = (b - acc) * (1 / d)
+//   smoother  x   = (b - acc) * rcpt(d)
 //   residual  r   = b - fma(d, x, acc)
 // so fused and unfused V-cycles produce identical iterates.
 #pragma once
@@ -20,7 +20,9 @@ template <> struct LA<double> {
   static __host__ __device__ __forceinline__ const double *w01(const MgLevelD &L) { return L.w01; }
   static __host__ __device__ __forceinline__ double *x(const MgLevelD &L) { return L.x; }
   static __host__ __device__ __forceinline__ double *b(const MgLevelD &L) { return L.b; }
+  static __host__ __device__ __forceinline__ double *xp(const MgLevelD &L) { return L.xp; }
   static __host__ __device__ __forceinline__ const double *dinv(const MgLevelD &L) { return L.dinv; }
+  static __host__ __device__ __forceinline__ const double *invd(const MgLevelD &L) { return L.invd; }
 };
 template <> struct LA<float> {
   static __host__ __device__ __forceinline__ const float *cc(const MgLevelD &L) { return L.ccf; }
@@ -29,11 +31,16 @@ template <> struct LA<float> {
   static __host__ __device__ __forceinline__ const float *w01(const MgLevelD &L) { return L.w01f; }
   static __host__ __device__ __forceinline__ float *x(const MgLevelD &L) { return L.xf; }
   static __host__ __device__ __forceinline__ float *b(const MgLevelD &L) { return L.bf; }
+  static __host__ __device__ __forceinline__ float *xp(const MgLevelD &L) { return L.xpf; }
   static __host__ __device__ __forceinline__ const float *dinv(const MgLevelD &L) { return L.dinvf; }
+  static __host__ __device__ __forceinline__ const float *invd(const MgLevelD &L) { return L.invdf; }
 };
 
 __device__ __forceinline__ float fmat(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fmat(double a, double b, double c) { return __fma_rn(a, b, c); }
+// correctly rounded reciprocal (the value of 1/d); every smoother uses it for 1/diagonal
+__device__ __forceinline__ float rcpt(float d) { return __frcp_rn(d); }
+__device__ __forceinline__ double rcpt(double d) { return __drcp_rn(d); }
 
 template <typename T>
 __device__ __forceinline__ T diag_of(const MgLevelD &L, const MgGeom &G, T sh, int c) {
@@ -79,13 +86,64 @@ __device__ __forceinline__ T offdiag(const MgLevelD &L, const MgGeom &G, V v, in
   return acc;
 }
 
+// One cell of the plane operator: neighbour indices and couplings in the order +x, -x, +y, -y.  A
+// neighbour that does not exist gets index c and coupling 0, which leaves the FMA chain unchanged.
+template <typename T>
+struct PlaneCell {
+  int c, ie, iw, in, is;
+  T ce, cw, cn, cs;
+};
+template <typename T>
+__device__ __forceinline__ PlaneCell<T> plane_cell(const MgLevelD &L, int per0, int per1, int i, int j) {
+  const int n0 = L.n[0], n1 = L.n[1];
+  const T *__restrict__ cp0 = LA<T>::cp(L, 0);
+  const T *__restrict__ cp1 = LA<T>::cp(L, 1);
+  PlaneCell<T> P;
+  const int c = i + n0 * j;
+  P.c = P.ie = P.iw = P.in = P.is = c;
+  P.ce = P.cw = P.cn = P.cs = T(0);
+  if (!(per0 && n0 == 1)) {
+    if (i + 1 < n0) { P.ie = c + 1; P.ce = cp0[c]; }
+    else if (per0) { P.ie = c + 1 - n0; P.ce = cp0[c]; }
+    if (i > 0) { P.iw = c - 1; P.cw = cp0[c - 1]; }
+    else if (per0) { P.iw = c + n0 - 1; P.cw = cp0[c + n0 - 1]; }
+  }
+  if (!(per1 && n1 == 1)) {
+    if (j + 1 < n1) { P.in = c + n0; P.cn = cp1[c]; }
+    else if (per1) { P.in = c + n0 - n0 * n1; P.cn = cp1[c]; }
+    if (j > 0) { P.is = c - n0; P.cs = cp1[c - n0]; }
+    else if (per1) { P.is = c + n0 * (n1 - 1); P.cs = cp1[c + n0 * (n1 - 1)]; }
+  }
+  return P;
+}
+template <typename T, typename V>
+__device__ __forceinline__ T plane_acc(const PlaneCell<T> &P, V v) {
+  T acc = fmat(P.ce, v(P.ie), T(0));
+  acc = fmat(P.cw, v(P.iw), acc);
+  acc = fmat(P.cn, v(P.in), acc);
+  return fmat(P.cs, v(P.is), acc);
+}
+
 // Level kernels run on (32, 8) blocks: grid.z is the system (plane mode) or the k plane (3-D mode).
 __device__ __forceinline__ void zpos(const MgGeom &G, int &k, int &s) {
   if (G.mode3d) { k = blockIdx.z; s = 0; }
   else { k = 0; s = blockIdx.z; }
 }
 
+// Asynchronous global -> shared copies of N bytes (4, 8 or 16), zero-filled when !valid (then nothing is
+// read); a thread may read what it copied itself after cp_async_wait.
+template <int N>
+__device__ __forceinline__ void cp_async_zfill(void *dst, const void *src, bool valid) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  const int sz = valid ? N : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(d), "l"(src), "n"(N), "r"(sz) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 // Block-wide sums of per-thread accumulators (any block shape); thread 0 receives the totals.
+// Every thread of the block must call them (they contain barriers).
 template <typename A>
 __device__ __forceinline__ void block_sum2(A a, A b, double &ta, double &tb) {
   __shared__ double sa[32], sb[32];
@@ -100,6 +158,7 @@ __device__ __forceinline__ void block_sum2(A a, A b, double &ta, double &tb) {
   ta = tb = 0.0;
   if (t == 0)
     for (int q = 0; q < nw; q++) { ta += sa[q]; tb += sb[q]; }
+  __syncthreads();  // sa/sb may be reused by the next call
 }
 template <typename A>
 __device__ __forceinline__ double block_sum1(A a) {
@@ -112,6 +171,7 @@ __device__ __forceinline__ double block_sum1(A a) {
   double ta = 0.0;
   if (t == 0)
     for (int q = 0; q < nw; q++) ta += sa[q];
+  __syncthreads();  // sa may be reused by the next call
   return ta;
 }
 

@@ -44,4 +44,12 @@ int mg_ir_down(const MgProblem &P, const CgWork &Wout, CgWork &W32, const double
 int mg_ir_up(const MgProblem &P, const CgWork &Wout, const float *e32, double *x, cudaStream_t st);
 int mg_zero_rhs_systems(const MgProblem &P, const CgWork &W, double *x, cudaStream_t st);
 
+// plane-mode level-0 Krylov kernels batched over systems (k_mg_plane.cu); partials per 32 x 32 patch
+template <typename T>
+int plane_resid(const MgProblem &P, const T *shift, const int *active, const T *x, const T *b, T *r, double *part_rr,
+                double *part_bb, int stride, cudaStream_t st);
+template <typename T, bool FUSEP>
+int plane_apply(const MgProblem &P, const T *shift, const int *active, const SysScal *sc, const T *z, const T *po,
+                T *pn, T *q, double *part, int stride, cudaStream_t st);
+
 }  // namespace snac

@@ -27,8 +27,12 @@ struct MgLevelD {
   const float *w01f;
   double *x, *b, *r;                 // ncell*nsys, FP64 path
   float *xf, *bf, *rf;               // ncell*nsys, FP32 path
+  double *xp;                        // plane mode: pre-smoothed x of the tiled smoother (read while x is written)
+  float *xpf;
   const double *dinv;                // coarsest: ncell^2 per system
   const float *dinvf;
+  const double *invd;                // plane mode: 1 / diagonal per system and cell (0 for inactive cells)
+  const float *invdf;
 };
 
 struct MgProblem {
@@ -43,6 +47,7 @@ struct MgProblem {
   const int *singular;               // per system, device
   int fused;                         // bits: 1/4 tiled plane smoother FP32/FP64, 2/8 one-CTA coarse tail FP32/FP64
   int cta_level[2];                  // first level run by k_vcycle_coarse ([0] FP32, [1] FP64); nlev = none
+  int nsm;                           // multiprocessors of the device (sizes the system batches)
 };
 
 struct MgGeom;
@@ -50,14 +55,25 @@ struct MgGeom;
 bool tile2d_ok(const MgProblem &P, int l, int prec);
 int tile2d_max_tiles(const MgLevelD &L);
 template <typename T>
-int launch_rbgs_tile2d(const MgProblem &P, int l, const T *shift, const int *active, int first_color, int mode,
-                       T *x, const T *b, const T *xc, double *part_bx, int part_stride, int *nchunk, cudaStream_t st);
+int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_color, int mode, T *x, const T *b,
+                       const T *xin, const T *xc, double *part_bx, int part_stride, int *nchunk, cudaStream_t st);
 template <typename T>
 size_t coarse_smem_bytes(const MgProblem &P, int l0);
 constexpr size_t MG_COARSE_SMEM_MAX = 200 * 1024;
 template <typename T>
 int launch_vcycle_coarse(const MgProblem &P, int l0, const T *shift, const int *active, T *x, const T *b,
                          cudaStream_t st);
+
+// plane-mode kernels batched over systems (k_mg_plane.cu)
+int plane_batch(const MgProblem &P, long ctas_per_system, int per_sm);
+int plane_nchunk(const MgLevelD &L);
+template <typename T> int plane_sweep(const MgProblem &P, int l, const T *shift, const int *active, int color, T *x,
+                                      const T *b, cudaStream_t st);
+template <typename T> int plane_restrict(const MgProblem &P, int l, const T *shift, const int *active, const T *xf,
+                                         const T *bf, T *bc, T *xc, cudaStream_t st);
+template <typename T> int plane_prolong(const MgProblem &P, int l, const int *active, T *xf, const T *xc,
+                                        cudaStream_t st);
+int plane_make_invd(MgProblem &P, double *const *out, float *const *outf, cudaStream_t st);
 
 // kernels (k_mg.cu) -- T = double or float
 template <typename T> int mg_vcycle(const MgProblem &P, int l, const int *active, cudaStream_t st);

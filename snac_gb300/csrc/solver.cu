@@ -182,6 +182,8 @@ struct Builder {
 int solver_create(Domain &d, PoissonSolver &S, bool upload) {
   const snac_case &c = d.c;
   S.precision = d.opt.precision;
+  if (const char *e = getenv("SNAC_MG_INNER")) S.inner_iters = std::max(1, atoi(e));
+  if (const char *e = getenv("SNAC_MG_INNER_TOL")) S.inner_tol = atof(e);
   S.tol = c.tol;
   S.maxiter = c.maxiter;
   S.fft_axis = c.fft_axis;
@@ -480,6 +482,11 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
     D.b = (double *)S.alloc(nv * sizeof(double));
     D.xf = (float *)S.alloc(nv * sizeof(float));
     D.bf = (float *)S.alloc(nv * sizeof(float));
+    if (!S.mode3d && l + 1 < P.nlev) {
+      D.xp = (double *)S.alloc(nv * sizeof(double));
+      D.xpf = (float *)S.alloc(nv * sizeof(float));
+      if (!D.xp || !D.xpf) { set_error("device allocation failed for multigrid level %d", l); return SNAC_ERR_NOMEM; }
+    }
     if (!h.dinv.empty()) {
       D.dinv = (const double *)up(h.dinv.data(), h.dinv.size() * sizeof(double));
       D.dinvf = upf(h.dinv);
@@ -504,6 +511,22 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
   P.shift = (const double *)up(S.lambda.data(), S.lambda.size() * sizeof(double));
   P.shiftf = upf(S.lambda);
   P.singular = (const int *)up(singular.data(), singular.size() * sizeof(int));
+  {
+    int dev = 0;
+    SNAC_CUDA(cudaGetDevice(&dev));
+    SNAC_CUDA(cudaDeviceGetAttribute(&P.nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  if (!S.mode3d) {  // smoothers: 1 / diagonal per system and cell, made once
+    double *tabs[MG_MAXLEV];
+    float *tabsf[MG_MAXLEV];
+    for (int l = 0; l < P.nlev; l++) {
+      tabs[l] = (double *)S.alloc((size_t)P.L[l].ncell * S.nsys * sizeof(double));
+      tabsf[l] = (float *)S.alloc((size_t)P.L[l].ncell * S.nsys * sizeof(float));
+      if (!tabs[l] || !tabsf[l]) { set_error("device allocation failed for the diagonal tables"); return SNAC_ERR_NOMEM; }
+    }
+    SNAC_TRY(plane_make_invd(P, tabs, tabsf, 0));
+    SNAC_CUDA(cudaStreamSynchronize(0));
+  }
   S.ncell0 = L0.ncell;
   const size_t nv0 = (size_t)L0.ncell * S.nsys;
   const int stride = mg_partial_stride(P);
@@ -560,8 +583,8 @@ static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *
     return (worst > S.tol && iters >= S.maxiter) ? SNAC_ERR_NOT_CONVERGED : SNAC_OK;
   }
   // mixed precision: iterative refinement in FP64 around FP32 Krylov solves (zero initial guess)
-  const int inner = 4;
-  const double inner_tol = 1e-5;
+  const int inner = S.inner_iters;
+  const double inner_tol = S.inner_tol;
   int outer = 0;
   CgWork Wr = S.W64;  // residual-only use of the FP64 work area
   Wr.active = S.active_outer;

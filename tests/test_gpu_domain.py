@@ -162,6 +162,36 @@ def test_fused_vcycle_matches_unfused(snac_lib, monkeypatch, precision, which):
         assert np.max(np.abs(a - b)) <= 1e-9 * scale
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_fused_vcycle_iterations_multiwave(snac_lib, monkeypatch, precision):
+    """Fused and unfused V-cycles are the same preconditioner, also when the tiled kernels run in
+    several waves (tiles of one launch then read and write neighbouring cells at different times)."""
+    case = cases.channel_4block(nx=(96, 160), ny=(64, 80), nz=32)
+    res = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("SNAC_MG_UNFUSED", mode)
+        monkeypatch.setenv("SNAC_MG_FUSE", "15")
+        d = Domain(case, precision=precision)
+        try:
+            ic = cases.channel_initial_condition(case, lambda ib: d.grid(ib, 1, capi.G_XC))
+            for ib, (u, v, w) in ic.items():
+                d.set(ib, capi.U, u)
+                d.set(ib, capi.V, v)
+                d.set(ib, capi.W, w)
+            d.bounduvw(False)
+            d.fillps(1e-3)
+            d.updt_rhs()
+            assert d.solve_pressure() == 0
+            st = d.stats()
+            res[mode] = (st["iters"], [d.get(ib, capi.PP)[1:-1, 1:-1, 1:-1] for ib in range(len(case.blocks))])
+        finally:
+            d.close()
+    assert res["0"][0] == res["1"][0], (res["0"][0], res["1"][0])
+    for a, b in zip(res["0"][1], res["1"][1]):
+        a, b = a - a.mean(), b - b.mean()
+        assert np.max(np.abs(a - b)) <= 1e-9 * np.max(np.abs(a))
+
+
 def _run_both(case, oracle_mod, nsteps, precision=0, seed=3, amp=0.1):
     O = oracle_mod.OracleDomain(case)
     d = Domain(case, precision=precision)
