@@ -127,7 +127,11 @@ def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0):
         L = capi.lib()
         if profile_kid:
             capi.check(L.snac_profile_kernel(profile_kid))
+        n0 = C.c_longlong()
+        capi.check(L.snac_launch_count(C.byref(n0)))
         rc = dom.step(steps, allow_not_converged=True)
+        n1 = C.c_longlong()
+        capi.check(L.snac_launch_count(C.byref(n1)))
         st = dom.stats()
         prof = None
         if profile_kid:
@@ -138,9 +142,39 @@ def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0):
         divtot, divmax = dom.chkdiv()
         ke = dom.kinetic_energy()
         return dict(ms=st["device_ms"] / steps, iters=st["iters"], residual=st["residual"], divmax=divmax, ke=ke,
-                    rc=rc, prof=prof, ncell=case.ncell, dt=st["dt"])
+                    rc=rc, prof=prof, ncell=case.ncell, dt=st["dt"], launches=n1.value - n0.value)
     finally:
         dom.close()
+
+
+def bench_smoother(case_fn, device, levels=(0, 1, 2), reps=20):
+    """CUDA-event timing of the FP32 tiled pre-smoother (the dominant kernel) on the bench workload,
+    inputs resident in HBM, all systems active: ms and algorithmic bytes per launch per level."""
+    from snac_gb300 import capi
+    from snac_gb300.domain import Domain
+    case = case_fn()
+    dom = Domain(case, precision=1, device=device)
+    out = {}
+    try:
+        init_channel(dom, case)
+        dom.step(1, allow_not_converged=True)
+        L = capi.lib()
+        for lev in levels:
+            ms = C.c_double(); nb = C.c_double()
+            if L.snac_bench_smoother(lev, reps, C.byref(ms), C.byref(nb)) == 0:
+                out[lev] = (ms.value, nb.value)
+    finally:
+        dom.close()
+    return out
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary (None when absent)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            return json.load(f).get(kernel, {}).get("dram_bytes_per_launch")
+    except (OSError, ValueError):
+        return None
 
 
 def run_e2e(case_fn, precision, steps, device):
@@ -252,9 +286,15 @@ def main():
     sampler.start()
     mixed = run_gpu_path(case_fn, 1, args.steps, args.warmup, device)
     clocks = sampler.stop()
-    # live CUDA-event timing of the dominant kernel classes over a timed run
-    prof_rbgs = run_gpu_path(case_fn, 1, args.steps, args.warmup, device, profile_kid=2)["prof"]
-    prof_mom = run_gpu_path(case_fn, 1, args.steps, args.warmup, device, profile_kid=1)["prof"]
+    # live CUDA-event timing of the kernel classes over timed runs of the mixed path
+    shares = {}
+    for kid, name in ((10, "pressure_solve"), (2, "smoother"), (9, "coarse_vcycle"), (3, "restriction"),
+                      (6, "operator_apply"), (1, "k_rk_mom"), (4, "fft_forward_box")):
+        n, tot = run_gpu_path(case_fn, 1, args.steps, args.warmup, device, profile_kid=kid)["prof"]
+        shares[name] = {"launches_per_step": n / args.steps, "ms_per_step": tot / args.steps,
+                        "mean_launch_ms": tot / max(n, 1)}
+    prof_mom = (shares["k_rk_mom"]["launches_per_step"] * args.steps, shares["k_rk_mom"]["ms_per_step"] * args.steps)
+    smoother = bench_smoother(case_fn, device)
     ms = mixed["ms"]
     if world > 1:
         t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{device}")
@@ -282,16 +322,27 @@ def main():
     launch_ms = tot / max(n, 1)
     mom_bytes = 104.0 * ncell
     mom_flops = KERNEL_WORK[1][2] * ncell
-    roof = {"kernel": "k_rk_mom", "bound": "hbm", "achieved": mom_bytes / (launch_ms * 1e-3) / 1e9,
-            "peak": hbm_peak, "unit": "GB/s", "frac": None, "traffic": None,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s",
-            "launch_ms": launch_ms, "launches": n,
-            "fp64": {"achieved_gflops": mom_flops / (launch_ms * 1e-3) / 1e9, "peak_gflops": f64.value,
-                     "frac": mom_flops / (launch_ms * 1e-3) / 1e9 / f64.value,
-                     "note": "FP64 FMA-stream peak measured on this GPU by snac_probe_peaks"}}
-    roof["frac"] = roof["achieved"] / roof["peak"]
-    nr, totr = prof_rbgs
-    rb_ms = totr / max(nr, 1)
+    peak_src = "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s"
+    roof_mom = {"kernel": "k_rk_mom", "bound": "fp64", "achieved": mom_bytes / (launch_ms * 1e-3) / 1e9,
+                "peak": hbm_peak, "unit": "GB/s", "frac": None, "traffic": ncu_traffic("k_rk_mom"),
+                "peak_source": peak_src, "launch_ms": launch_ms, "launches": n,
+                "fp64": {"achieved_gflops": mom_flops / (launch_ms * 1e-3) / 1e9, "peak_gflops": f64.value,
+                         "frac": mom_flops / (launch_ms * 1e-3) / 1e9 / f64.value,
+                         "note": "FP64 FMA-stream peak measured on this GPU by snac_probe_peaks"}}
+    roof_mom["frac"] = roof_mom["achieved"] / roof_mom["peak"]
+    # dominant kernel: the FP32 tiled red-black smoother of the pressure solve (level-0 pre-smoother)
+    roof = None
+    if 0 in smoother:
+        sm_ms, sm_bytes = smoother[0]
+        name = "k_rbgs_tile2d<float> level 0 pre-smoother"
+        roof = {"kernel": name, "bound": "hbm", "achieved": sm_bytes / (sm_ms * 1e-3) / 1e9, "peak": hbm_peak,
+                "unit": "GB/s", "frac": None, "traffic": ncu_traffic(name), "peak_source": peak_src,
+                "launch_ms": sm_ms, "bytes_per_launch": sm_bytes,
+                "algorithmic_bytes": "12 B per cell and system: b and 1/diagonal read, x written (FP32)",
+                "share_of_step": shares["smoother"]["ms_per_step"] / mixed["ms"],
+                "levels": {str(k): {"launch_ms": v[0], "achieved_gbs": v[1] / (v[0] * 1e-3) / 1e9}
+                           for k, v in smoother.items()}}
+        roof["frac"] = roof["achieved"] / roof["peak"]
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         r = cpu_reference(case_fn, args.steps, args.warmup, budget_s=30.0)
@@ -308,9 +359,9 @@ def main():
                                      "solve_iters_max": plain["iters"], "solve_residual_max": plain["residual"],
                                      "kinetic_energy": plain["ke"]},
                       "speedup_mixed_vs_plain": plain["ms"] / mixed["ms"], "learned_guess": "not built"},
-            "roofline": roof,
-            "kernels": {"k_rbgs_mean_launch_ms": rb_ms, "k_rbgs_launches_per_step": nr / args.steps,
-                        "k_rk_mom_mean_launch_ms": launch_ms},
+            "roofline": roof if roof else roof_mom, "roofline_rk_mom": roof_mom,
+            "gpu_launches": mixed["launches"], "gpu_launches_per_step": mixed["launches"] / args.steps,
+            "kernels": shares,
             "peaks_measured_here": {"fp64_gflops": f64.value, "fp32_gflops": f32.value},
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
     if rank == 0:

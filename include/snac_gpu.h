@@ -124,9 +124,18 @@ int snac_device_count(int *n);
 int snac_probe_peaks(double *fp64_gflops, double *fp32_gflops);
 /* No counterpart in the reference: time every launch of one kernel class with CUDA events on the
  * library stream (1 rk_mom, 2 red-black smoother, 3 residual+restriction, 4/5 forward/backward
- * transform, 6 Krylov operator apply, 7 fillps, 8 correc; 0 = off).  Selecting resets the record. */
+ * transform, 6 Krylov operator apply, 7 fillps, 8 correc, 9 one-CTA coarse V-cycle, 10 whole pressure
+ * solve; 0 = off).  Selecting resets the record. */
 int snac_profile_kernel(int kernel_class);
 int snac_profile_read(int *launches, double *total_ms);
+/* No counterpart in the reference: number of kernels this library has launched since it was loaded
+ * (a host-side counter incremented at every launch site). */
+int snac_launch_count(long long *n);
+/* No counterpart in the reference: time `reps` launches of the FP32 tiled pre-smoother on level `level`
+ * of the pressure solver of the current domain, all systems active, with CUDA events on the library
+ * stream.  Returns the mean time per launch and its algorithmic bytes (b, 1/diagonal read, x written:
+ * 12 bytes per cell and system).  The solver's level buffers are overwritten. */
+int snac_bench_smoother(int level, int reps, double *ms_per_launch, double *bytes_per_launch);
 
 /* ---------------------------------------------------------------- host mirrors */
 /* Keep a device mirror of a host array of `bytes` bytes (contents uploaded). */

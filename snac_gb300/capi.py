@@ -66,6 +66,8 @@ PROTOTYPES = {
     "snac_probe_peaks": (C.c_int, [DP, DP]),
     "snac_profile_kernel": (C.c_int, [C.c_int]),
     "snac_profile_read": (C.c_int, [IP, DP]),
+    "snac_launch_count": (C.c_int, [C.POINTER(C.c_longlong)]),
+    "snac_bench_smoother": (C.c_int, [C.c_int, C.c_int, DP, DP]),
     "snac_register": (C.c_int, [C.c_void_p, C.c_size_t]),
     "snac_unregister": (C.c_int, [C.c_void_p]),
     "snac_update_device": (C.c_int, [C.c_void_p]),

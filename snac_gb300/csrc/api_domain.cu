@@ -679,6 +679,36 @@ int snac_updt_rhs_all(void) {
   SNAC_CUDA(cudaStreamSynchronize(d->st));
   return SNAC_OK;
 }
+int snac_bench_smoother(int level, int reps, double *ms_per_launch, double *bytes_per_launch) {
+  NEED_DOMAIN
+  if (!ms_per_launch || !bytes_per_launch || reps < 1) { set_error("snac_bench_smoother: bad arguments"); return SNAC_ERR_ARG; }
+  const MgProblem &P = d->ps->P;
+  if (level < 0 || level >= P.nlev - 1 || !tile2d_ok(P, level, 0)) {
+    set_error("snac_bench_smoother: level %d has no tiled smoother (plane systems only)", level);
+    return SNAC_ERR_UNSUPPORTED;
+  }
+  const MgLevelD &L = P.L[level];
+  cudaEvent_t e0, e1;
+  SNAC_CUDA(cudaEventCreate(&e0));
+  SNAC_CUDA(cudaEventCreate(&e1));
+  int rc = SNAC_OK;
+  for (int q = 0; q < 2 + reps && rc == SNAC_OK; q++) {
+    if (q == 2) cudaEventRecord(e0, d->st);
+    rc = launch_rbgs_tile2d<float>(P, level, nullptr, 0, 0, L.xpf, L.bf, nullptr, nullptr, nullptr, 0, nullptr, d->st);
+  }
+  cudaEventRecord(e1, d->st);
+  float ms = 0.f;
+  if (rc == SNAC_OK) {
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = SNAC_ERR_CUDA;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  SNAC_TRY(rc);
+  *ms_per_launch = ms / reps;
+  *bytes_per_launch = 12.0 * (double)L.ncell * (double)P.nsys;
+  return SNAC_OK;
+}
+
 int snac_solve_pressure(void) {
   NEED_DOMAIN
   const int rc = solver_solve_pressure(*d, *d->ps);

@@ -85,7 +85,7 @@ int launch_exchange(const DBlock *dB, const FaceLink *dF, int nlinks, const int 
                     int maxplane, cudaStream_t st) {
   if (nlinks <= 0 || nflds <= 0) return SNAC_OK;
   dim3 g((maxplane + 255) / 256, nlinks, nflds);
-  k_exchange<<<g, 256, 0, st>>>(dB, dF, dflds, a);
+  k_exchange<<<g, 256, 0, st>>>(dB, dF, dflds, a), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -93,7 +93,7 @@ int launch_exchange(const DBlock *dB, const FaceLink *dF, int nlinks, const int 
 int launch_setbc(const DBlock *dB, const BcEntry *dE, int nent, int a, int maxplane, cudaStream_t st) {
   if (nent <= 0) return SNAC_OK;
   dim3 g((maxplane + 255) / 256, nent);
-  k_setbc<<<g, 256, 0, st>>>(dB, dE, a);
+  k_setbc<<<g, 256, 0, st>>>(dB, dE, a), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

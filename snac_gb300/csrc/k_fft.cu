@@ -347,7 +347,7 @@ int fft_forward_to_box(Domain &d, PoissonSolver &S, cudaStream_t st) {
   SNAC_TRY(prep_launch(g.n, L, (const void *)k_fft_fwd_box));
   prof_begin(KID_FFT_FWD, st);
   k_fft_fwd_box<<<g_tabs.nlt, 256, L.smem, st>>>(d.d_db, g_tabs.d_lt, g_tabs.d_boff, g, (const double2 *)S.d_tw,
-                                                 S.d_mat_fwd, S.box_b);
+                                                 S.d_mat_fwd, S.box_b), ::snac::count_launch();
   prof_end(KID_FFT_FWD, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -360,7 +360,7 @@ int fft_backward_from_box(Domain &d, PoissonSolver &S, cudaStream_t st) {
   SNAC_TRY(prep_launch(g.n, L, (const void *)k_fft_bwd_box));
   prof_begin(KID_FFT_BWD, st);
   k_fft_bwd_box<<<g_tabs.nlt, 256, L.smem, st>>>(d.d_db, g_tabs.d_lt, g_tabs.d_boff, g, (const double2 *)S.d_tw,
-                                                 S.d_mat_bwd, S.box_x, S.normfft);
+                                                 S.d_mat_bwd, S.box_x, S.normfft), ::snac::count_launch();
   prof_end(KID_FFT_BWD, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -369,7 +369,7 @@ int fft_backward_from_box(Domain &d, PoissonSolver &S, cudaStream_t st) {
 int box_gather(Domain &d, PoissonSolver &S, cudaStream_t st) {
   SNAC_TRY(ensure_tables(d, S));
   k_box_io<<<d.ntiles, dim3(TX, TY, TZ), 0, st>>>(d.d_db, d.d_tiles, g_tabs.d_boff3, S.P.L[0].n[0], S.P.L[0].n[1],
-                                                  S.box_b, 1);
+                                                  S.box_b, 1), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -377,7 +377,7 @@ int box_gather(Domain &d, PoissonSolver &S, cudaStream_t st) {
 int box_scatter(Domain &d, PoissonSolver &S, cudaStream_t st) {
   SNAC_TRY(ensure_tables(d, S));
   k_box_io<<<d.ntiles, dim3(TX, TY, TZ), 0, st>>>(d.d_db, d.d_tiles, g_tabs.d_boff3, S.P.L[0].n[0], S.P.L[0].n[1],
-                                                  S.box_x, 0);
+                                                  S.box_x, 0), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -427,7 +427,7 @@ int r2r_array(int kind, int idir, const int nn[3], int q, double *darr, cudaStre
   const int nlines = nn[t1] * nn[t2];
   if (rc == SNAC_OK) {
     k_r2r_strided<<<(nlines + L.lp - 1) / L.lp, 256, L.smem, st>>>(darr, nn[t1], str[t1], str[t2], str[a], nlines, g,
-                                                                    (const double2 *)dtw, dmat);
+                                                                    (const double2 *)dtw, dmat), ::snac::count_launch();
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) rc = cuda_fail(e, "k_r2r_strided", __FILE__, __LINE__);

@@ -159,13 +159,13 @@ int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, c
   if ((fuse & 2) && !P.mode3d && l >= P.cta_level[prec]) return launch_vcycle_coarse<T>(P, l, shift, active, x, b, st);
   if (l == P.nlev - 1) {
     if (LA<T>::dinv(L)) {
-      k_dense<T><<<P.nsys, 256, 0, st>>>(L, active, x, b);
+      k_dense<T><<<P.nsys, 256, 0, st>>>(L, active, x, b), ::snac::count_launch();
     } else {
       const dim3 g((unsigned)((L.ncell + 255) / 256), P.nsys);
-      k_zero<T><<<g, 256, 0, st>>>(L.ncell, x, P.nsys, active);
+      k_zero<T><<<g, 256, 0, st>>>(L.ncell, x, P.nsys, active), ::snac::count_launch();
       for (int it = 0; it < 40; it++)
         for (int col : {0, 1, 1, 0}) {
-          if (P.mode3d) k_rbgs<T><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, col, x, b);
+          if (P.mode3d) k_rbgs<T><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, col, x, b), ::snac::count_launch();
           else SNAC_TRY(plane_sweep<T>(P, l, shift, active, col, x, b, st));
         }
     }
@@ -184,7 +184,7 @@ int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, c
   }
   if (l == 0) {  // coarse x is zeroed by the restriction
     const dim3 g((unsigned)((L.ncell + 255) / 256), P.nsys);
-    k_zero<T><<<g, 256, 0, st>>>(L.ncell, x, P.nsys, active);
+    k_zero<T><<<g, 256, 0, st>>>(L.ncell, x, P.nsys, active), ::snac::count_launch();
   }
   if (!P.mode3d) {  // plane systems: kernels batched over systems
     for (int it = 0; it < 2 * P.nu; it++) SNAC_TRY(plane_sweep<T>(P, l, shift, active, it & 1, x, b, st));
@@ -196,18 +196,18 @@ int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, c
   }
   for (int it = 0; it < 2 * P.nu; it++) {
     prof_begin(KID_RBGS, st);
-    k_rbgs<T><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, it & 1, x, b);
+    k_rbgs<T><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, it & 1, x, b), ::snac::count_launch();
     prof_end(KID_RBGS, st);
   }
   prof_begin(KID_RESTRICT, st);
-  k_resid_restrict<T><<<grid_cell(P, C), BLK, 0, st>>>(L, C, G, shift, active, x, b, LA<T>::b(C), LA<T>::x(C));
+  k_resid_restrict<T><<<grid_cell(P, C), BLK, 0, st>>>(L, C, G, shift, active, x, b, LA<T>::b(C), LA<T>::x(C)), ::snac::count_launch();
   prof_end(KID_RESTRICT, st);
   SNAC_CUDA(cudaGetLastError());
   SNAC_TRY(mg_vcycle_impl<T>(P, G, l + 1, shift, active, nullptr, 0, nullptr, st));
-  k_prolong<T><<<grid_cell(P, L), BLK, 0, st>>>(L, C, G, active, x, LA<T>::x(C));
+  k_prolong<T><<<grid_cell(P, L), BLK, 0, st>>>(L, C, G, active, x, LA<T>::x(C)), ::snac::count_launch();
   for (int it = 0; it < 2 * P.nu; it++) {
     prof_begin(KID_RBGS, st);
-    k_rbgs<T><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, 1 - (it & 1), x, b);
+    k_rbgs<T><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, 1 - (it & 1), x, b), ::snac::count_launch();
     prof_end(KID_RBGS, st);
   }
   SNAC_CUDA(cudaGetLastError());
@@ -527,7 +527,7 @@ template int mg_vcycle<double>(const MgProblem &, int, const int *, cudaStream_t
 template int mg_vcycle<float>(const MgProblem &, int, const int *, cudaStream_t);
 
 int mg_set_active(int nsys, int *active, const int *src, cudaStream_t st) {
-  k_set_active<<<(nsys + 127) / 128, 128, 0, st>>>(nsys, active, src);
+  k_set_active<<<(nsys + 127) / 128, 128, 0, st>>>(nsys, active, src), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -539,12 +539,12 @@ int mg_residual(const MgProblem &P, CgWork &W, const T *x, const T *b, T *r, dou
   const MgLevelD &L0 = P.L[0];
   if (P.mode3d)
     k_cg_resid<T><<<grid_red(P, L0), BLK, 0, st>>>(L0, G, shift_of<T>(P), W.active, x, b, r, W.part0,
-                                                   set_bb ? W.part1 : nullptr, W.stride);
+                                                   set_bb ? W.part1 : nullptr, W.stride), ::snac::count_launch();
   else
     SNAC_TRY(plane_resid<T>(P, shift_of<T>(P), W.active, x, b, r, W.part0, set_bb ? W.part1 : nullptr, W.stride, st));
   SNAC_CUDA(cudaMemsetAsync(W.d_count, 0, 2 * sizeof(int), st));
   k_cg_norms<<<P.nsys, 256, 0, st>>>(W.active, nullptr, W.sc, W.part0, W.part1, W.stride, nchunk_red(P, L0), tol,
-                                     set_bb, want_scale, nact, W.d_count);
+                                     set_bb, want_scale, nact, W.d_count), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -555,7 +555,7 @@ template int mg_residual<float>(const MgProblem &, CgWork &, const float *, cons
 
 int mg_zero_rhs_systems(const MgProblem &P, const CgWork &W, double *x, cudaStream_t st) {
   const long n = P.L[0].ncell;
-  k_zero_rhs_systems<double><<<dim3((unsigned)((n + 255) / 256), P.nsys), 256, 0, st>>>(n, W.sc, x);
+  k_zero_rhs_systems<double><<<dim3((unsigned)((n + 255) / 256), P.nsys), 256, 0, st>>>(n, W.sc, x), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -588,32 +588,32 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
     SNAC_TRY(mg_vcycle_impl<T>(Pz, G, 0, shift, W.active, W.part2, W.stride, &nrz, st));
     trace("pcg: V-cycle", st);
     if (nrz == 0) {
-      k_cg_dot<T><<<gf, 256, 0, st>>>(n, W.active, r, z, W.part2, W.stride);
+      k_cg_dot<T><<<gf, 256, 0, st>>>(n, W.active, r, z, W.part2, W.stride), ::snac::count_launch();
       nrz = nflat;
     }
-    k_cg_beta<<<P.nsys, 256, 0, st>>>(W.active, W.sc, W.part2, W.stride, nrz);
+    k_cg_beta<<<P.nsys, 256, 0, st>>>(W.active, W.sc, W.part2, W.stride, nrz), ::snac::count_launch();
     prof_begin(KID_CG_APPLY, st);
     if constexpr (fusep) {
       if (P.mode3d)
         k_cg_apply<T, true><<<grid_red(P, L0), BLK, 0, st>>>(L0, G, shift, W.active, W.sc, z, p, pn, q, W.part1,
-                                                             W.stride);
+                                                             W.stride), ::snac::count_launch();
       else
         SNAC_TRY((plane_apply<T, true>(P, shift, W.active, W.sc, z, p, pn, q, W.part1, W.stride, st)));
       std::swap(p, pn);
     } else {
-      k_cg_p<T><<<gf, 256, 0, st>>>(n, W.active, W.sc, z, p);
+      k_cg_p<T><<<gf, 256, 0, st>>>(n, W.active, W.sc, z, p), ::snac::count_launch();
       if (P.mode3d)
         k_cg_apply<T, false><<<grid_red(P, L0), BLK, 0, st>>>(L0, G, shift, W.active, W.sc, z, p, nullptr, q,
-                                                              W.part1, W.stride);
+                                                              W.part1, W.stride), ::snac::count_launch();
       else
         SNAC_TRY((plane_apply<T, false>(P, shift, W.active, W.sc, z, p, nullptr, q, W.part1, W.stride, st)));
     }
     prof_end(KID_CG_APPLY, st);
-    k_cg_alpha<<<P.nsys, 256, 0, st>>>(W.active, W.sc, W.part1, W.stride, nred);
-    k_cg_xr<T><<<gf, 256, 0, st>>>(n, W.active, W.sc, p, q, x, r, W.part0, W.stride, (zero_x && it == 1) ? 1 : 0);
+    k_cg_alpha<<<P.nsys, 256, 0, st>>>(W.active, W.sc, W.part1, W.stride, nred), ::snac::count_launch();
+    k_cg_xr<T><<<gf, 256, 0, st>>>(n, W.active, W.sc, p, q, x, r, W.part0, W.stride, (zero_x && it == 1) ? 1 : 0), ::snac::count_launch();
     SNAC_CUDA(cudaMemsetAsync(W.d_count, 0, 2 * sizeof(int), st));
     k_cg_norms<<<P.nsys, 256, 0, st>>>(W.active, nullptr, W.sc, W.part0, nullptr, W.stride, nflat, tol, 0, 0, 0,
-                                       W.d_count);
+                                       W.d_count), ::snac::count_launch();
     SNAC_CUDA(cudaGetLastError());
     trace("pcg: iteration", st);
   }
@@ -627,8 +627,8 @@ template int mg_pcg<float>(const MgProblem &, CgWork &, float *, int, double, bo
 int mg_project_singular(const MgProblem &P, CgWork &W, double *b, cudaStream_t st) {
   const long n = P.L[0].ncell;
   const dim3 g = grid_flat(n, P.nsys);
-  k_sum_active<double><<<g, 256, 0, st>>>(P.L[0], P.singular, b, W.part0, W.part1, W.stride);
-  k_sub_mean<double><<<g, 256, 0, st>>>(P.L[0], P.singular, b, W.part0, W.part1, W.stride, (int)g.x);
+  k_sum_active<double><<<g, 256, 0, st>>>(P.L[0], P.singular, b, W.part0, W.part1, W.stride), ::snac::count_launch();
+  k_sub_mean<double><<<g, 256, 0, st>>>(P.L[0], P.singular, b, W.part0, W.part1, W.stride, (int)g.x), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -637,16 +637,16 @@ int mg_ir_down(const MgProblem &P, const CgWork &Wout, CgWork &W32, const double
                double inner_tol, cudaStream_t st) {
   const long n = P.L[0].ncell;
   const dim3 gf = grid_flat(n, P.nsys);
-  k_ir_down<<<gf, 256, 0, st>>>(n, Wout.active, Wout.sc, r64, r32, e32, W32.part0, W32.stride);
+  k_ir_down<<<gf, 256, 0, st>>>(n, Wout.active, Wout.sc, r64, r32, e32, W32.part0, W32.stride), ::snac::count_launch();
   SNAC_CUDA(cudaMemsetAsync(W32.d_count, 0, 2 * sizeof(int), st));
   k_cg_norms<<<P.nsys, 256, 0, st>>>(W32.active, Wout.active, W32.sc, W32.part0, W32.part0, W32.stride, (int)gf.x,
-                                     inner_tol, 1, 0, 0, W32.d_count);
+                                     inner_tol, 1, 0, 0, W32.d_count), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
 int mg_ir_up(const MgProblem &P, const CgWork &Wout, const float *e32, double *x, cudaStream_t st) {
   const long n = P.L[0].ncell;
-  k_ir_up<<<grid_flat(n, P.nsys), 256, 0, st>>>(n, Wout.active, Wout.sc, e32, x);
+  k_ir_up<<<grid_flat(n, P.nsys), 256, 0, st>>>(n, Wout.active, Wout.sc, e32, x), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

@@ -408,7 +408,7 @@ static int launch_tile(const MgProblem &P, const MgLevelD &L, const MgLevelD &C,
   const int sb = plane_batch(P, nt, NW == 16 ? 2 : 4);
   const dim3 g((unsigned)nt, (unsigned)((P.nsys + sb - 1) / sb));
   k_rbgs_tile2d<T, NW, R><<<g, NW * 32, smem, st>>>(L, C, P.periodic[0], P.periodic[1], active, P.nsys, sb,
-                                                    first_color, 2 * P.nu, mode, x, b, xin, xc, part_bx, part_stride);
+                                                    first_color, 2 * P.nu, mode, x, b, xin, xc, part_bx, part_stride), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -458,7 +458,7 @@ int launch_vcycle_coarse(const MgProblem &P, int l0, const T *shift, const int *
   if (smem > MG_COARSE_SMEM_MAX) { set_error("coarse levels exceed the shared-memory budget"); return SNAC_ERR_ARG; }
   SNAC_TRY(allow_smem((const void *)k_vcycle_coarse<T>, smem));
   prof_begin(KID_COARSE, st);
-  k_vcycle_coarse<T><<<P.nsys, 1024, smem, st>>>(P, l0, shift, active, x, b);
+  k_vcycle_coarse<T><<<P.nsys, 1024, smem, st>>>(P, l0, shift, active, x, b), ::snac::count_launch();
   prof_end(KID_COARSE, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;

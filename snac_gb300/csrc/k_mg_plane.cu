@@ -254,7 +254,7 @@ int plane_sweep(const MgProblem &P, int l, const T *shift, const int *active, in
   const int sb = plane_batch(P, (long)g.x * g.y, 8);
   const dim3 gz(g.x, g.y, (unsigned)((P.nsys + sb - 1) / sb));
   prof_begin(KID_RBGS, st);
-  k_p_rbgs<T><<<gz, BLK, 0, st>>>(L, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, color, x, b);
+  k_p_rbgs<T><<<gz, BLK, 0, st>>>(L, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, color, x, b), ::snac::count_launch();
   prof_end(KID_RBGS, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -270,13 +270,13 @@ int plane_restrict(const MgProblem &P, int l, const T *shift, const int *active,
   prof_begin(KID_RESTRICT, st);
   const int e0 = C.coarsened[0] ? 2 : 1, e1 = C.coarsened[1] ? 2 : 1;
   if (e0 == 1 && e1 == 2)
-    k_p_restrict<T, 1, 2><<<gz, BLK, 0, st>>>(F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc);
+    k_p_restrict<T, 1, 2><<<gz, BLK, 0, st>>>(F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc), ::snac::count_launch();
   else if (e0 == 2 && e1 == 1)
-    k_p_restrict<T, 2, 1><<<gz, BLK, 0, st>>>(F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc);
+    k_p_restrict<T, 2, 1><<<gz, BLK, 0, st>>>(F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc), ::snac::count_launch();
   else if (e0 == 2 && e1 == 2)
-    k_p_restrict<T, 2, 2><<<gz, BLK, 0, st>>>(F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc);
+    k_p_restrict<T, 2, 2><<<gz, BLK, 0, st>>>(F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc), ::snac::count_launch();
   else
-    k_p_restrict<T, 1, 1><<<gz, BLK, 0, st>>>(F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc);
+    k_p_restrict<T, 1, 1><<<gz, BLK, 0, st>>>(F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc), ::snac::count_launch();
   prof_end(KID_RESTRICT, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -288,7 +288,7 @@ int plane_prolong(const MgProblem &P, int l, const int *active, T *xf, const T *
   const dim3 g((unsigned)((F.n[0] + 31) / 32), (unsigned)((F.n[1] + 7) / 8), 1);
   const int sb = plane_batch(P, (long)g.x * g.y, 8);
   const dim3 gz(g.x, g.y, (unsigned)((P.nsys + sb - 1) / sb));
-  k_p_prolong<T><<<gz, BLK, 0, st>>>(F, C, active, P.nsys, sb, xf, xc);
+  k_p_prolong<T><<<gz, BLK, 0, st>>>(F, C, active, P.nsys, sb, xf, xc), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -297,8 +297,8 @@ int plane_make_invd(MgProblem &P, double *const *out, float *const *outf, cudaSt
   for (int l = 0; l < P.nlev; l++) {
     const MgLevelD &L = P.L[l];
     const dim3 g((unsigned)((L.ncell + 255) / 256), (unsigned)P.nsys);
-    k_p_invd<double><<<g, 256, 0, st>>>(L, P.shift, out[l]);
-    k_p_invd<float><<<g, 256, 0, st>>>(L, P.shiftf, outf[l]);
+    k_p_invd<double><<<g, 256, 0, st>>>(L, P.shift, out[l]), ::snac::count_launch();
+    k_p_invd<float><<<g, 256, 0, st>>>(L, P.shiftf, outf[l]), ::snac::count_launch();
     SNAC_CUDA(cudaGetLastError());
     P.L[l].invd = out[l];
     P.L[l].invdf = outf[l];
@@ -320,7 +320,7 @@ int plane_resid(const MgProblem &P, const T *shift, const int *active, const T *
   const int sb = red_batch(P, (long)g.x * g.y);
   const dim3 gz(g.x, g.y, (unsigned)((P.nsys + sb - 1) / sb));
   k_p_resid<T><<<gz, BLK, 0, st>>>(L, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, x, b, r, part_rr,
-                                   part_bb, stride);
+                                   part_bb, stride), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -333,7 +333,7 @@ int plane_apply(const MgProblem &P, const T *shift, const int *active, const Sys
   const int sb = red_batch(P, (long)g.x * g.y);
   const dim3 gz(g.x, g.y, (unsigned)((P.nsys + sb - 1) / sb));
   k_p_apply<T, FUSEP><<<gz, BLK, 0, st>>>(L, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, sc, z, po, pn,
-                                          q, part, stride);
+                                          q, part, stride), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

@@ -29,11 +29,11 @@ static int probe(double *gflops) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  k_fma_stream<T><<<blocks, threads>>>(out, iters / 16, (T)0.999999, (T)1e-7);  // warm-up
+  k_fma_stream<T><<<blocks, threads>>>(out, iters / 16, (T)0.999999, (T)1e-7), ::snac::count_launch();  // warm-up
   float best = 1e30f;
   for (int r = 0; r < 3; r++) {
     cudaEventRecord(e0);
-    k_fma_stream<T><<<blocks, threads>>>(out, iters, (T)0.999999, (T)1e-7);
+    k_fma_stream<T><<<blocks, threads>>>(out, iters, (T)0.999999, (T)1e-7), ::snac::count_launch();
     cudaEventRecord(e1);
     cudaEventSynchronize(e1);
     float ms = 0.f;

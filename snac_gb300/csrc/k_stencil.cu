@@ -134,14 +134,14 @@ k_rk_mom_writeback(const DBlock *__restrict__ Bs, const Tile *__restrict__ T) {
 int launch_rk_mom(const DBlock *dB, const Tile *dT, int ntiles, const RkMomParams &prm, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
   prof_begin(KID_RK_MOM, st);
-  k_rk_mom<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, prm);
+  k_rk_mom<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, prm), ::snac::count_launch();
   prof_end(KID_RK_MOM, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
 int launch_rk_mom_writeback(const DBlock *dB, const Tile *dT, int ntiles, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
-  k_rk_mom_writeback<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT);
+  k_rk_mom_writeback<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -198,13 +198,13 @@ k_rk_scal_writeback(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, i
 int launch_rk_scal(const DBlock *dB, const Tile *dT, int ntiles, const RkScalParams &prm, double *part,
                    cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
-  k_rk_scal<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, prm, part);
+  k_rk_scal<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, prm, part), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
 int launch_rk_scal_writeback(const DBlock *dB, const Tile *dT, int ntiles, int sidx, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
-  k_rk_scal_writeback<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, sidx);
+  k_rk_scal_writeback<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, sidx), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -230,7 +230,7 @@ k_fillps(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, double rdt, 
 int launch_fillps(const DBlock *dB, const Tile *dT, int ntiles, double dt, int fft_axis, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
   prof_begin(KID_FILLPS, st);
-  k_fillps<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, 1.0 / dt, fft_axis);
+  k_fillps<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, 1.0 / dt, fft_axis), ::snac::count_launch();
   prof_end(KID_FILLPS, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -256,7 +256,7 @@ k_correc(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, double dt) {
 int launch_correc(const DBlock *dB, const Tile *dT, int ntiles, double dt, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
   prof_begin(KID_CORREC, st);
-  k_correc<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, dt);
+  k_correc<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, dt), ::snac::count_launch();
   prof_end(KID_CORREC, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -282,7 +282,7 @@ k_updt_pressure(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, doubl
 
 int launch_updt_pressure(const DBlock *dB, const Tile *dT, int ntiles, double alpha, int impdiff, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
-  k_updt_pressure<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, alpha, impdiff);
+  k_updt_pressure<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, alpha, impdiff), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -422,15 +422,15 @@ int launch_updt_rhs(int nx, int ny, int nz, const int isb[6], const double *rx, 
                     double *p, cudaStream_t st) {
   if (isb[0] || isb[1]) {
     k_updt_rhs<<<(ny * nz + 255) / 256, 256, 0, st>>>(nx, ny, nz, make_int4(isb[0], isb[1], 0, 0), make_int2(0, 0),
-                                                      rx, ry, rz, p);
+                                                      rx, ry, rz, p), ::snac::count_launch();
     SNAC_CUDA(cudaGetLastError());
   }
   if (isb[2] || isb[3]) {
-    k_updt_rhs_y<<<(nx * nz + 255) / 256, 256, 0, st>>>(nx, ny, nz, isb[2], isb[3], ry, p);
+    k_updt_rhs_y<<<(nx * nz + 255) / 256, 256, 0, st>>>(nx, ny, nz, isb[2], isb[3], ry, p), ::snac::count_launch();
     SNAC_CUDA(cudaGetLastError());
   }
   if (isb[4] || isb[5]) {
-    k_updt_rhs_z<<<(nx * ny + 255) / 256, 256, 0, st>>>(nx, ny, nz, isb[4], isb[5], rz, p);
+    k_updt_rhs_z<<<(nx * ny + 255) / 256, 256, 0, st>>>(nx, ny, nz, isb[4], isb[5], rz, p), ::snac::count_launch();
     SNAC_CUDA(cudaGetLastError());
   }
   return SNAC_OK;
@@ -438,7 +438,7 @@ int launch_updt_rhs(int nx, int ny, int nz, const int isb[6], const double *rx, 
 
 int launch_bulk_partial(const DBlock *dB, const Tile *dT, int ntiles, int sidx, double *part, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
-  k_bulk<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, sidx, part);
+  k_bulk<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, sidx, part), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -457,24 +457,24 @@ __global__ void k_reduce_final(const double *part, int n, double *out) {
 
 int launch_chkdt_partial(const DBlock *dB, const Tile *dT, int ntiles, double *part, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
-  k_chkdt<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, part);
+  k_chkdt<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, part), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
 int launch_chkdiv_partial(const DBlock *dB, const Tile *dT, int ntiles, double vol, double *part, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
-  k_chkdiv<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, 1.0 / vol, part);
+  k_chkdiv<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, 1.0 / vol, part), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
 int launch_ke_partial(const DBlock *dB, const Tile *dT, int ntiles, double *part, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
-  k_ke<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, part);
+  k_ke<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, part), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
 int launch_reduce_final(const double *part, int ntiles, double *out, cudaStream_t st) {
-  k_reduce_final<<<1, 32, 0, st>>>(part, ntiles, out);
+  k_reduce_final<<<1, 32, 0, st>>>(part, ntiles, out), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

@@ -138,10 +138,10 @@ extern "C" int snac_chkdiv_noalloc(const int lo[3], const int hi[3], const doubl
   SNAC_TRY(scratch_address(&scratch));
   cudaStream_t st = (cudaStream_t)stream;
   k_chkdiv_noalloc<<<nparts, dim3(NTX, NTY, NTZ), 0, st>>>((int)nx, (int)ny, (int)nz, tx, ty, ntiles, u, v, w, dxf, dyf,
-                                                            dzf, 1.0 / vol, scratch);
+                                                            dzf, 1.0 / vol, scratch), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   double *fin = scratch + 2 * NCTA;
-  k_chkdiv_noalloc_final<<<1, 32, 0, st>>>(scratch, nparts, fin);
+  k_chkdiv_noalloc_final<<<1, 32, 0, st>>>(scratch, nparts, fin), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   double r[2];
   SNAC_CUDA(cudaMemcpyAsync(r, fin, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -1,4 +1,5 @@
 // prof.cu -- CUDA-event timing of one selected kernel class on the launching stream.
+#include <atomic>
 #include <vector>
 
 #include "snac_prof.h"
@@ -15,6 +16,9 @@ struct Prof {
 Prof g_prof;
 constexpr int PROF_MAX = 8192;
 }  // namespace
+
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void prof_begin(int kid, cudaStream_t st) {
   if (g_prof.kid != kid || g_prof.n >= PROF_MAX) return;
@@ -55,5 +59,11 @@ extern "C" int snac_profile_read(int *launches, double *total_ms) {
   }
   *launches = snac::g_prof.n;
   *total_ms = tot;
+  return SNAC_OK;
+}
+
+extern "C" int snac_launch_count(long long *n) {
+  if (!n) return SNAC_ERR_ARG;
+  *n = snac::g_launches.load(std::memory_order_relaxed);
   return SNAC_OK;
 }

@@ -11,6 +11,9 @@
 
 namespace snac {
 
+// every kernel launch site appends ", count_launch()" to its launch expression
+void count_launch();
+
 void set_error(const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
 // SNAC_DEBUG=1 in the environment: every traced phase syncs the device and logs to stderr
