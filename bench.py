@@ -36,6 +36,33 @@ sys.path.insert(0, ROOT)
 METRIC = "ms per RK3 step & Mcells/s on 1 GB300, learned+mixed vs plain, equal |div u|"
 
 
+def max_over_ranks(x, device=0):
+    """Largest value of x over the ranks of the job (x itself when not distributed)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return x
+    on_gpu = dist.get_backend() == "nccl"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=f"cuda:{device}" if on_gpu else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def rank_barrier(device=0):
+    """Barrier over the job's ranks, with the device drained on both sides."""
+    import torch
+    import torch.distributed as dist
+    if torch.cuda.is_available():
+        torch.cuda.synchronize(device)
+    if dist.is_available() and dist.is_initialized():
+        if dist.get_backend() == "nccl":
+            dist.barrier(device_ids=[device])
+        else:
+            dist.barrier()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize(device)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -129,7 +156,9 @@ def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0):
             capi.check(L.snac_profile_kernel(profile_kid))
         n0 = C.c_longlong()
         capi.check(L.snac_launch_count(C.byref(n0)))
+        rank_barrier(device)
         rc = dom.step(steps, allow_not_converged=True)
+        rank_barrier(device)
         n1 = C.c_longlong()
         capi.check(L.snac_launch_count(C.byref(n1)))
         st = dom.stats()
@@ -243,15 +272,22 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--case", choices=["channel", "small"], default="channel",
+                    help="channel: the benchmark workload; small: the same layout at test size")
     ap.add_argument("--only", choices=["mixed", "plain"], default=None,
                     help="run one path once and print its timing only (used for ncu launch lists)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     from snac_gb300 import cases
-    case_fn = lambda: cases.channel_4block()
-    cfg = {"workload": "channel4 256x144x128 (4 uneven blocks 96|160 x 64|80 x 128), Re_tau=180, FFT along z",
-           "cells": cases.channel_4block().ncell, "solver_tol": 1e-12, "blocks": 4,
-           "l2_policy": "inputs larger than L2 (fields + solver vectors ~0.5 GB/step)"}
+    if args.case == "small":  # the same four-block layout at 48x24x16 (tests of the multi-rank logic)
+        case_fn = lambda: cases.channel_4block(nx=(16, 32), ny=(8, 16), nz=16)
+        cfg = {"workload": "channel4 48x24x16 (4 uneven blocks 16|32 x 8|16 x 16), FFT along z",
+               "cells": case_fn().ncell, "solver_tol": 1e-12, "blocks": 4, "l2_policy": "fits in L2 (test size)"}
+    else:
+        case_fn = lambda: cases.channel_4block()
+        cfg = {"workload": "channel4 256x144x128 (4 uneven blocks 96|160 x 64|80 x 128), Re_tau=180, FFT along z",
+               "cells": cases.channel_4block().ncell, "solver_tol": 1e-12, "blocks": 4,
+               "l2_policy": "inputs larger than L2 (fields + solver vectors ~1.3 GB)"}
 
     if args.impl == "reference":
         if rank != 0:
@@ -296,10 +332,7 @@ def main():
     prof_mom = (shares["k_rk_mom"]["launches_per_step"] * args.steps, shares["k_rk_mom"]["ms_per_step"] * args.steps)
     smoother = bench_smoother(case_fn, device)
     ms = mixed["ms"]
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{device}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, device)
     ncell = mixed["ncell"]
     value = world * ncell / (ms * 1e-3) / 1e6
     e2e = None
