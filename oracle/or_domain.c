@@ -526,9 +526,32 @@ static void set_dt_from_cfl(or_domain *d) {
   d->dt = d->c.dt_f > 0.0 ? d->c.dt_f : (d->c.cfl * dt_cfl < d->c.dtmax ? d->c.cfl * dt_cfl : d->c.dtmax);
 }
 
-/* main.f90:893-1069 for the explicit-diffusion path (no scalars, no IMPDIFF) */
+/* main.f90:907-936 for the explicit-diffusion path: rk_scal on every block, the bulk mean summed over
+ * blocks as the MPI_ALLREDUCE of scal.f90:175 sums it over ranks, bulk_forcing_s, boundp of the scalar */
+static void scalar_stage(or_domain *d, int irk) {
+  for (int s = 0; s < d->c.nscal; s++) {
+    const int forced = d->c.is_sforced[s];
+    double msum = 0.0;
+    for (int ib = 0; ib < d->nblocks; ib++) {
+      or_block *B = &d->b[ib];
+      double fb = 0.0;
+      or_rk_scal(RKC[irk], B->lo, B->hi, B->g[0][0], B->g[0][1], B->g[1][0], B->g[1][1], B->g[2][0], B->g[2][1],
+                 d->dt, 1.0 / d->c.alphai[s], d->vol_all, B->fld[OR_U], B->fld[OR_V], B->fld[OR_W], forced,
+                 d->c.scalf[s], d->c.ssource[s], B->fld[OR_DSDTRKO0 + s], B->fld[OR_S0 + s], &fb, d->c.impdiff);
+      if (forced) msum += d->c.scalf[s] - fb; /* this block's share of the bulk mean */
+    }
+    const double f = forced ? d->c.scalf[s] - msum : 0.0;
+    for (int ib = 0; ib < d->nblocks; ib++) {
+      or_block *B = &d->b[ib];
+      or_bulk_forcing_s(B->lo, B->hi, forced, f, B->fld[OR_S0 + s]);
+    }
+    or_boundp(d, OR_S0 + s);
+  }
+}
+
+/* main.f90:893-1069 for the explicit-diffusion path (scalars and Boussinesq buoyancy included) */
 int or_step(or_domain *d, int nsteps) {
-  if (d->c.impdiff || d->c.nscal > 0) return -10; /* not restated in the oracle driver */
+  if (d->c.impdiff) return -10; /* the IMPDIFF Helmholtz solves are not restated in the oracle driver */
   if (d->dt == 0.0) set_dt_from_cfl(d);          /* main.f90:660-661 */
   double visc = 1.0 / d->c.visci;
   int rc = 0;
@@ -538,11 +561,14 @@ int or_step(or_domain *d, int nsteps) {
     for (int irk = 0; irk < 3; irk++) {
       double dtrk = (RKC[irk][0] + RKC[irk][1]) * d->dt;
       double alpha = -visc * dtrk / 2.0;
+      scalar_stage(d, irk);
+      const int bq = d->c.boussinesq && d->c.nscal > 0;
       for (int ib = 0; ib < d->nblocks; ib++) {
         or_block *B = &d->b[ib];
         or_rk_mom(RKC[irk], B->lo, B->hi, B->g[0][0], B->g[0][1], B->g[1][0], B->g[1][1], B->g[2][0], B->g[2][1],
-                  d->dt, d->c.bforce, d->c.gacc, d->c.beta, NULL, visc, B->fld[OR_U], B->fld[OR_V], B->fld[OR_W],
-                  B->fld[OR_P], B->fld[OR_DUDTRKO], B->fld[OR_DVDTRKO], B->fld[OR_DWDTRKO], 0, 0);
+                  d->dt, d->c.bforce, d->c.gacc, d->c.beta, bq ? B->fld[OR_S0] : NULL, visc, B->fld[OR_U],
+                  B->fld[OR_V], B->fld[OR_W], B->fld[OR_P], B->fld[OR_DUDTRKO], B->fld[OR_DVDTRKO],
+                  B->fld[OR_DWDTRKO], 0, bq);
       }
       or_bounduvw(d, 0);
       or_fillps_all(d, dtrk);

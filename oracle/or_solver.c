@@ -515,6 +515,17 @@ fail:
   return NULL;
 }
 
+/* singular systems: the preconditioned residual is taken orthogonal to the null space (the constant
+ * over the active cells), so that the search directions carry no constant and x - x0 stays mean-free;
+ * without it the smoother's constant drift accumulates in x and swamps the residual in cancellation */
+static void remove_mean(const or_level *L, int s, double *v) {
+  long n = L->ncell, off = n * s, na = 0;
+  double sum = 0.0;
+  for (long c = 0; c < n; c++) if (!(L->code[c] & 0x8000)) { sum += v[off + c]; na++; }
+  double mean = na ? sum / na : 0.0;
+  for (long c = 0; c < n; c++) if (!(L->code[c] & 0x8000)) v[off + c] -= mean;
+}
+
 /* Solve A x = b for every system; x holds the initial guess on entry. */
 int or_poisson_solve(or_poisson *P, double *b, double *x) {
   or_level *L = &P->L[0];
@@ -539,12 +550,18 @@ int or_poisson_solve(or_poisson *P, double *b, double *x) {
     apply_A(P, L, s, x, q);
     for (long c = 0; c < n; c++) z[off + c] = b[off + c] - q[off + c];
     double rr = dot(L, s, z, z);
+    if (rr > bb) { /* a warm start worse than zero is dropped: x = 0, r = b */
+      for (long c = 0; c < n; c++) { x[off + c] = 0.0; z[off + c] = b[off + c]; }
+      rr = bb;
+    }
+    if (P->singular[s]) { remove_mean(L, s, z); rr = dot(L, s, z, z); } /* consistent correction equation */
     int it = 0;
     double rel = sqrt(rr / bb);
     if (rel > P->tol) {
       /* V-cycle on the residual: L->b <- r, M r in L->x */
       memcpy(L->b + off, z + off, sizeof(double) * n);
       vcycle(P, 0, s);
+      if (P->singular[s]) remove_mean(L, s, L->x);
       for (long c = 0; c < n; c++) p[off + c] = L->x[off + c];
       double rz = dot(L, s, z, L->x);
       for (it = 1; it <= P->maxiter; it++) {
@@ -557,6 +574,7 @@ int or_poisson_solve(or_poisson *P, double *b, double *x) {
         if (rel <= P->tol) break;
         memcpy(L->b + off, z + off, sizeof(double) * n);
         vcycle(P, 0, s);
+        if (P->singular[s]) remove_mean(L, s, L->x);
         double rzn = dot(L, s, z, L->x);
         double beta = rzn / rz;
         rz = rzn;

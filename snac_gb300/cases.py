@@ -205,6 +205,54 @@ def channel_4block(nx=(96, 160), ny=(64, 80), nz: int = 128, stretch: float = 1.
     return Case(name="channel4", blocks=blocks, visci=180.0, cfl=0.95, bforce=(1.0, 0.0, 0.0), fft_axis=3, tol=tol)
 
 
+def channel_4block_scalar(nx=(16, 32), ny=(8, 16), nz: int = 16, pr: float = 0.71, tol: float = 1e-12) -> Case:
+    """The four-block channel with one passive scalar: T = 0 / 1 on the lower / upper wall, friend links
+    elsewhere (as the velocity), bulk-forced to a mean of 0.5 (is_sforced, scal.f90:156-199)."""
+    c = channel_4block(nx=nx, ny=ny, nz=nz, tol=tol)
+    for b in c.blocks:
+        cs = [list(f) for f in b.cbcpre]
+        vs = [list(f) for f in b.bcpre]
+        for side in range(2):
+            if cs[1][side] == "N":  # a wall of the channel
+                cs[1][side] = "D"
+                vs[1][side] = 0.0 if side == 0 else 1.0
+        b.cbcscal = [cs]
+        b.bcscal = [vs]
+    c.name = "channel4_scalar"
+    c.nscal = 1
+    c.alphai = (c.visci * pr,)
+    c.ssource = (0.0,)
+    c.scalf = (0.5,)
+    c.is_sforced = (1,)
+    return c
+
+
+def dhc_reference_test() -> Case:
+    """tests/differentially_heated_cavity/{dns,blocks}.nml: one 32x2x32 block, y periodic (FFT along y),
+    no-slip walls in x and z, T = -0.5 / +0.5 on x- / x+, adiabatic z, Boussinesq buoyancy with
+    gacc = (0, 0, -1), beta = 1, Ra = 1e8-like visci/alphai, fixed dt = 1e-3, explicit diffusion."""
+    b = Block(ng=(32, 2, 32), lmin=(0.0, 0.0, 0.0), lmax=(1.0, 0.0625, 1.0),
+              cbcvel=[bc6("DDFFDD")] * 3, bcvel=[val6([0, 0, 1, 1, 0, 0])] * 3,
+              cbcpre=bc6("NNFFNN"), bcpre=val6([0, 0, 1, 1, 0, 0]),
+              cbcscal=[bc6("DDFFNN")], bcscal=[val6([-0.5, 0.5, 1, 1, 0, 0])])
+    return Case(name="dhc_reference_test", blocks=[b], visci=1186.78165819, cfl=0.95, dtmax=1e9, dt_f=1e-3,
+                gacc=(0.0, 0.0, -1.0), beta=1.0, nscal=1, alphai=(842.614977318,), ssource=(0.0,), scalf=(0.0,),
+                is_sforced=(0,), icheck=10, fft_axis=2, boussinesq=1, tol=1e-12)
+
+
+def dhc_initial_scalar(case: Case, xc_of_block):
+    """initflow.f90:247-256 ('dhc'): T linear in x between the two wall values, on every cell incl. halo."""
+    out = {}
+    for ib, b in enumerate(case.blocks):
+        xc = np.asarray(xc_of_block(ib))          # (nx+2) cell centres lo-1..hi+1
+        lx = b.lmax[0] - b.lmin[0]
+        t0, t1 = b.bcscal[0][0][0], b.bcscal[0][0][1]
+        xx = xc / lx
+        prof = (1.0 - xx) * t0 + xx * t1
+        out[ib] = np.broadcast_to(prof[:, None, None], (b.ng[0] + 2, b.ng[1] + 2, b.ng[2] + 2)).copy()
+    return out
+
+
 def l_shaped_box(n: int = 144, nz: int = 96, tol: float = 1e-12) -> Case:
     """Config 4: closed L-shaped box of three n x n x nz blocks (corner, +x leg, +y leg), lid u=1 on z+."""
     h = 1.0

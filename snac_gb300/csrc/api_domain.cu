@@ -194,7 +194,9 @@ static int build_domain(Domain &d, const snac_case *c, const snac_block_desc *bl
   d.nblocks = c->nblocks;
   if (d.nblocks < 1) { set_error("nblocks must be >= 1"); return SNAC_ERR_ARG; }
   if (c->nscal < 0 || c->nscal > SNAC_MAX_SCAL) { set_error("nscal out of range"); return SNAC_ERR_ARG; }
-  if (c->impdiff || c->nscal > 0) { set_error("IMPDIFF and scalar transport are not wired into snac_step yet"); return SNAC_ERR_UNSUPPORTED; }
+  if (c->impdiff) { set_error("IMPDIFF (implicit diffusion) is not wired into snac_step yet"); return SNAC_ERR_UNSUPPORTED; }
+  for (int q = 0; q < c->nscal; q++)
+    if (!(c->alphai[q] > 0.0)) { set_error("alphai of scalar %d must be positive", q + 1); return SNAC_ERR_ARG; }
   d.hb.resize(d.nblocks);
   // placement (initmpi.f90:50-98)
   std::vector<int> done(d.nblocks, 0), unl(d.nblocks, 0);
@@ -318,6 +320,12 @@ static int upload_domain(Domain &d) {
     B.ru = (double *)d.alloc(ni); B.rv = (double *)d.alloc(ni); B.rw = (double *)d.alloc(ni);
     B.nu = (double *)d.alloc(ni); B.nv = (double *)d.alloc(ni); B.nw = (double *)d.alloc(ni);
     if (!B.u || !B.v || !B.w || !B.p || !B.pp || !B.ru || !B.nu || !B.nw) { set_error("device allocation failed (fields)"); return SNAC_ERR_NOMEM; }
+    for (int q = 0; q < d.c.nscal; q++) {
+      B.s[q] = (double *)d.alloc(nh);
+      B.rs[q] = (double *)d.alloc(ni);
+      if (!B.s[q] || !B.rs[q]) { set_error("device allocation failed (scalars)"); return SNAC_ERR_NOMEM; }
+    }
+    if (d.c.nscal > 0 && !(B.ns = (double *)d.alloc(ni))) { set_error("device allocation failed (scalars)"); return SNAC_ERR_NOMEM; }
     for (int a = 0; a < 3; a++) {
       auto t = axis_tables(H.g[a][0].data(), H.g[a][1].data(), H.ng[a]);
       double *p = (double *)d.alloc(t.size() * sizeof(double));
@@ -365,7 +373,7 @@ static int upload_domain(Domain &d) {
   d.d_flds = (int *)d.alloc(sizeof(flds));
   SNAC_CUDA(cudaMemcpy(d.d_flds, flds, sizeof(flds), cudaMemcpyHostToDevice));
   // boundary-condition tables (bound.f90:36-105)
-  for (int kind = 0; kind < 4; kind++)
+  for (int kind = 0; kind < 4 + d.c.nscal; kind++)
     for (int a = 0; a < 3; a++) {
       std::vector<BcEntry> E;
       for (int b = 0; b < d.nblocks; b++) {
@@ -375,7 +383,7 @@ static int upload_domain(Domain &d) {
           BcEntry e;
           memset(&e, 0, sizeof(e));
           e.b = b;
-          e.f = kind < 2 ? fi : (kind == 2 ? 3 : 4);
+          e.f = kind < 2 ? fi : (kind == 2 ? 3 : (kind == 3 ? 4 : 5 + (kind - 4)));
           bool any = false;
           for (int s = 0; s < 2; s++) {
             e.mode[s] = BC_NONE;
@@ -389,10 +397,15 @@ static int upload_domain(Domain &d) {
               ct = H.desc.cbcvel[fi][a][s];
               val = H.desc.bcvel[fi][a][s];
               dr = centered ? H.g[a][0][s ? H.ng[a] : 0] : H.g[a][1][s ? H.ng[a] : 0];
-            } else {
+            } else if (kind < 4) {
               centered = 1;
               ct = H.desc.cbcpre[a][s];
               val = H.desc.bcpre[a][s];
+              dr = H.g[a][0][s ? H.ng[a] : 0];
+            } else {  // scalar kind-4: its own cbc/bc (main.f90:936, boundp(s%cbc, ..., s%bc, ...))
+              centered = 1;
+              ct = H.desc.cbcscal[kind - 4][a][s];
+              val = H.desc.bcscal[kind - 4][a][s];
               dr = H.g[a][0][s ? H.ng[a] : 0];
             }
             bc_mode(ct, s, centered, val, dr, &e.mode[s], &e.factor[s], &e.sgn[s]);
@@ -419,8 +432,9 @@ static int bound_uvw(Domain &d, int is_correc) {
 }
 
 static int bound_p(Domain &d, int field) {
-  const int fsel = field == SNAC_P ? 3 : 4;
-  const int kind = field == SNAC_P ? 2 : 3;
+  const bool scal = field >= SNAC_S0 && field < SNAC_S0 + d.c.nscal;
+  const int fsel = field == SNAC_P ? 3 : (scal ? 5 + (field - SNAC_S0) : 4);
+  const int kind = field == SNAC_P ? 2 : (scal ? 4 + (field - SNAC_S0) : 3);
   for (int a = 0; a < 3; a++) SNAC_TRY(launch_exchange(d.d_db, d.d_links[a], d.nlinks[a], d.d_flds + fsel, 1, a, d.maxplane[a], d.st));
   for (int a = 0; a < 3; a++) SNAC_TRY(launch_setbc(d.d_db, d.d_bc[kind][a], d.nbc[kind][a], a, d.maxplane[a], d.st));
   return SNAC_OK;
@@ -447,9 +461,36 @@ static int rk_mom_all(Domain &d, int irk) {
   for (int a = 0; a < 3; a++) { prm.bforce[a] = d.c.bforce[a]; prm.gb[a] = 0.0; }
   prm.visc = 1.0 / d.c.visci;
   prm.impdiff = 0;
-  prm.boussinesq = 0;
+  prm.boussinesq = d.c.boussinesq && d.c.nscal > 0;  // rk.f90:104-108 with scalars(1)
+  if (prm.boussinesq)
+    for (int a = 0; a < 3; a++) prm.gb[a] = prm.f12 * d.c.gacc[a] * d.c.beta * 0.5;
   SNAC_TRY(launch_rk_mom(d.d_db, d.d_tiles, d.ntiles, prm, d.st));
   SNAC_TRY(launch_rk_mom_writeback(d.d_db, d.d_tiles, d.ntiles, d.st));
+  return SNAC_OK;
+}
+
+// main.f90:907-936 (explicit diffusion): rk_scal on every block with the bulk mean of all blocks
+// (the MPI_ALLREDUCE of scal.f90:175), bulk_forcing_s with f = scalf - mean, then boundp of the scalar.
+// The mean stays on the device: the forcing kernel reads it there.
+static int rk_scal_all(Domain &d, int irk) {
+  for (int q = 0; q < d.c.nscal; q++) {
+    RkScalParams prm;
+    prm.f1 = RKC[irk][0] * d.dt;
+    prm.f2 = RKC[irk][1] * d.dt;
+    prm.f12 = prm.f1 + prm.f2;
+    prm.alpha = 1.0 / d.c.alphai[q];
+    prm.ssource = d.c.ssource[q];
+    prm.impdiff = d.c.impdiff;
+    prm.sidx = q;
+    const bool forced = d.c.is_sforced[q] != 0;
+    SNAC_TRY(launch_rk_scal(d.d_db, d.d_tiles, d.ntiles, prm, forced ? d.d_part : nullptr, d.st));
+    SNAC_TRY(launch_rk_scal_writeback(d.d_db, d.d_tiles, d.ntiles, q, d.st));
+    if (forced) {
+      SNAC_TRY(launch_reduce_final(d.d_part, d.ntiles, d.d_red, d.st));
+      SNAC_TRY(launch_bulk_forcing_s(d.d_db, d.d_tiles, d.ntiles, q, d.c.scalf[q], 1.0 / d.vol_all, d.d_red, d.st));
+    }
+    SNAC_TRY(bound_p(d, SNAC_S0 + q));
+  }
   return SNAC_OK;
 }
 
@@ -496,6 +537,7 @@ static int set_dt_from_cfl(Domain &d) {
 static int one_stage(Domain &d, int irk) {
   const double dtrk = (RKC[irk][0] + RKC[irk][1]) * d.dt;
   const double alpha = -(1.0 / d.c.visci) * dtrk / 2.0;
+  SNAC_TRY(rk_scal_all(d, irk));
   SNAC_TRY(rk_mom_all(d, irk));
   SNAC_TRY(bound_uvw(d, 0));
   SNAC_TRY(launch_fillps(d.d_db, d.d_tiles, d.ntiles, dtrk, d.c.fft_axis, d.st));
@@ -527,7 +569,15 @@ static int field_ptr(Domain &d, int ib, int field, double **p, size_t *bytes) {
     case SNAC_DUDTRKO: *p = B.ru; *bytes = ni; break;
     case SNAC_DVDTRKO: *p = B.rv; *bytes = ni; break;
     case SNAC_DWDTRKO: *p = B.rw; *bytes = ni; break;
-    default: set_error("unknown field %d", field); return SNAC_ERR_ARG;
+    default:
+      if (field >= SNAC_S0 && field < SNAC_S0 + d.c.nscal) { *p = B.s[field - SNAC_S0]; *bytes = nh; break; }
+      if (field >= SNAC_DSDTRKO0 && field < SNAC_DSDTRKO0 + d.c.nscal) {
+        *p = B.rs[field - SNAC_DSDTRKO0];
+        *bytes = ni;
+        break;
+      }
+      set_error("unknown field %d", field);
+      return SNAC_ERR_ARG;
   }
   return SNAC_OK;
 }
@@ -662,7 +712,10 @@ int snac_bounduvw_all(int is_correc) {
 }
 int snac_boundp_all(int field) {
   NEED_DOMAIN
-  if (field != SNAC_P && field != SNAC_PP) { set_error("snac_boundp_all: field must be SNAC_P or SNAC_PP"); return SNAC_ERR_ARG; }
+  if (field != SNAC_P && field != SNAC_PP && !(field >= SNAC_S0 && field < SNAC_S0 + d->c.nscal)) {
+    set_error("snac_boundp_all: field must be SNAC_P, SNAC_PP or a scalar");
+    return SNAC_ERR_ARG;
+  }
   SNAC_TRY(bound_p(*d, field));
   SNAC_CUDA(cudaStreamSynchronize(d->st));
   return SNAC_OK;

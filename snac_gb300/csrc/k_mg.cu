@@ -383,10 +383,18 @@ __global__ void k_cg_norms(int *active, const int *src_active, SysScal *sc, cons
     __syncthreads();
   }
   if (!active[s]) return;
-  const double rr = cta_sum_parts(part_rr, s, stride, n);
+  double rr = cta_sum_parts(part_rr, s, stride, n);
   const double bbn = set_bb ? cta_sum_parts(part_bb, s, stride, n) : 0.0;
   if (threadIdx.x != 0) return;
-  if (set_bb) { sc[s].bb = bbn; sc[s].first = 1; sc[s].zero_rhs = 0; }
+  if (set_bb) {
+    sc[s].bb = bbn;
+    sc[s].first = 1;
+    sc[s].zero_rhs = 0;
+    // a warm start worse than zero (||b - A x0|| > ||b||) is dropped: the solve then starts from x = 0,
+    // r = b, which also avoids the cancellation of a large A x0 against a small b
+    sc[s].restart = (bbn > 0.0 && rr > bbn) ? 1 : 0;
+    if (sc[s].restart) rr = bbn;
+  }
   sc[s].rr = rr;
   if (want_scale) {
     const double v = sqrt(rr / (double)(nact > 0 ? nact : 1));
@@ -398,6 +406,15 @@ __global__ void k_cg_norms(int *active, const int *src_active, SysScal *sc, cons
   if (bb == 0.0) { sc[s].zero_rhs = 1; active[s] = 0; atomicAdd(count + 1, 1); }
   else if (rel <= tol) active[s] = 0;
   else atomicAdd(count, 1);
+}
+
+// systems flagged by k_cg_norms: x = 0, r = b
+template <typename T>
+__global__ void k_restart_systems(long n, const SysScal *sc, T *x, const T *b, T *r) {
+  const int s = blockIdx.y;
+  if (!sc[s].restart) return;
+  const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) { x[n * s + c] = 0; r[n * s + c] = b[n * s + c]; }
 }
 
 // systems with an all-zero right-hand side get x = 0 (as HYPRE does)
@@ -553,6 +570,13 @@ template int mg_residual<double>(const MgProblem &, CgWork &, const double *, co
 template int mg_residual<float>(const MgProblem &, CgWork &, const float *, const float *, float *, double, int, int,
                                 long, cudaStream_t);
 
+int mg_restart_bad_guess(const MgProblem &P, CgWork &W, double *x, const double *b, double *r, cudaStream_t st) {
+  const long n = P.L[0].ncell;
+  k_restart_systems<double><<<dim3((unsigned)((n + 255) / 256), P.nsys), 256, 0, st>>>(n, W.sc, x, b, r), ::snac::count_launch();
+  SNAC_CUDA(cudaGetLastError());
+  return SNAC_OK;
+}
+
 int mg_zero_rhs_systems(const MgProblem &P, const CgWork &W, double *x, cudaStream_t st) {
   const long n = P.L[0].ncell;
   k_zero_rhs_systems<double><<<dim3((unsigned)((n + 255) / 256), P.nsys), 256, 0, st>>>(n, W.sc, x), ::snac::count_launch();
@@ -584,9 +608,18 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
     MgProblem Pz = P;
     if constexpr (sizeof(T) == 8) { Pz.L[0].b = (double *)r; Pz.L[0].x = (double *)z; }
     else { Pz.L[0].bf = (float *)r; Pz.L[0].xf = (float *)z; }
+    // with singular systems r.z is taken after the projection below, so the V-cycle's own partials are
+    // not asked for
     int nrz = 0;
-    SNAC_TRY(mg_vcycle_impl<T>(Pz, G, 0, shift, W.active, W.part2, W.stride, &nrz, st));
+    SNAC_TRY(mg_vcycle_impl<T>(Pz, G, 0, shift, W.active, P.any_singular ? nullptr : W.part2, W.stride, &nrz, st));
     trace("pcg: V-cycle", st);
+    if (P.any_singular) {
+      // singular systems: z is taken orthogonal to the constant (the null space), so the search
+      // directions carry no constant and x - x0 stays mean-free.  r.z must use the projected z: r's
+      // mean is zero only up to rounding, and the V-cycle's constant drift can be large.
+      k_sum_active<T><<<gf, 256, 0, st>>>(L0, P.singular, z, W.part0, W.part1, W.stride), ::snac::count_launch();
+      k_sub_mean<T><<<gf, 256, 0, st>>>(L0, P.singular, z, W.part0, W.part1, W.stride, nflat), ::snac::count_launch();
+    }
     if (nrz == 0) {
       k_cg_dot<T><<<gf, 256, 0, st>>>(n, W.active, r, z, W.part2, W.stride), ::snac::count_launch();
       nrz = nflat;
@@ -625,6 +658,7 @@ template int mg_pcg<double>(const MgProblem &, CgWork &, double *, int, double, 
 template int mg_pcg<float>(const MgProblem &, CgWork &, float *, int, double, bool, bool, int *, cudaStream_t);
 
 int mg_project_singular(const MgProblem &P, CgWork &W, double *b, cudaStream_t st) {
+  if (!P.any_singular) return SNAC_OK;
   const long n = P.L[0].ncell;
   const dim3 g = grid_flat(n, P.nsys);
   k_sum_active<double><<<g, 256, 0, st>>>(P.L[0], P.singular, b, W.part0, W.part1, W.stride), ::snac::count_launch();

@@ -209,6 +209,22 @@ int launch_rk_scal_writeback(const DBlock *dB, const Tile *dT, int ntiles, int s
   return SNAC_OK;
 }
 
+// bulk_forcing_s (scal.f90:181-199) with f = scalf - mean, mean = red[0] * inv_vol read on the device
+__global__ void __launch_bounds__(TX * TY * TZ)
+k_bulk_forcing_s(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, int sidx, double scalf, double inv_vol,
+                 const double *__restrict__ red) {
+  TILE_SETUP
+  const double f = scalf - red[0] * inv_vol;
+  B.s[sidx][hidx(i, j, k, nx, ny)] += f;
+}
+int launch_bulk_forcing_s(const DBlock *dB, const Tile *dT, int ntiles, int sidx, double scalf, double inv_vol,
+                          const double *red, cudaStream_t st) {
+  if (ntiles <= 0) return SNAC_OK;
+  k_bulk_forcing_s<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, sidx, scalf, inv_vol, red), ::snac::count_launch();
+  SNAC_CUDA(cudaGetLastError());
+  return SNAC_OK;
+}
+
 // ---------------------------------------------------------------- fillps (fillps.f90:27-53)
 __global__ void __launch_bounds__(TX * TY * TZ)
 k_fillps(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, double rdt, int fft_axis) {

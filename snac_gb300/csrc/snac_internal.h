@@ -93,6 +93,8 @@ int launch_rk_mom_writeback(const DBlock *dB, const Tile *dT, int ntiles, cudaSt
 int launch_rk_scal(const DBlock *dB, const Tile *dT, int ntiles, const RkScalParams &prm, double *part,
                    cudaStream_t st);
 int launch_rk_scal_writeback(const DBlock *dB, const Tile *dT, int ntiles, int sidx, cudaStream_t st);
+int launch_bulk_forcing_s(const DBlock *dB, const Tile *dT, int ntiles, int sidx, double scalf, double inv_vol,
+                          const double *red, cudaStream_t st);
 int launch_fillps(const DBlock *dB, const Tile *dT, int ntiles, double dt, int fft_axis, cudaStream_t st);
 int launch_correc(const DBlock *dB, const Tile *dT, int ntiles, double dt, cudaStream_t st);
 int launch_updt_pressure(const DBlock *dB, const Tile *dT, int ntiles, double alpha, int impdiff, cudaStream_t st);

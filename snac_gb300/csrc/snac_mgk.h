@@ -13,6 +13,7 @@ struct MgGeom {
 struct SysScal {
   double rz, rr, bb, rel, scale, alpha, beta;
   int first, zero_rhs;
+  int restart;  // the warm start was worse than zero (rel > 1): the solve restarts from x = 0
 };
 
 // Partial sums: one row of `stride` doubles per system; a producer kernel writes one entry per CTA
@@ -43,6 +44,8 @@ int mg_ir_down(const MgProblem &P, const CgWork &Wout, CgWork &W32, const double
                double inner_tol, cudaStream_t st);
 int mg_ir_up(const MgProblem &P, const CgWork &Wout, const float *e32, double *x, cudaStream_t st);
 int mg_zero_rhs_systems(const MgProblem &P, const CgWork &W, double *x, cudaStream_t st);
+// systems whose warm start is worse than zero (set by mg_residual with set_bb): x = 0, r = b
+int mg_restart_bad_guess(const MgProblem &P, CgWork &W, double *x, const double *b, double *r, cudaStream_t st);
 
 // plane-mode level-0 Krylov kernels batched over systems (k_mg_plane.cu); partials per 32 x 32 patch
 template <typename T>

@@ -48,6 +48,7 @@ struct MgProblem {
   int fused;                         // bits: 1/4 tiled plane smoother FP32/FP64, 2/8 one-CTA coarse tail FP32/FP64
   int cta_level[2];                  // first level run by k_vcycle_coarse ([0] FP32, [1] FP64); nlev = none
   int nsm;                           // multiprocessors of the device (sizes the system batches)
+  int any_singular;                  // some system is singular (pure Neumann, zero shift)
 };
 
 struct MgGeom;

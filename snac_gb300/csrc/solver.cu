@@ -511,6 +511,8 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
   P.shift = (const double *)up(S.lambda.data(), S.lambda.size() * sizeof(double));
   P.shiftf = upf(S.lambda);
   P.singular = (const int *)up(singular.data(), singular.size() * sizeof(int));
+  P.any_singular = 0;
+  for (int v : singular) P.any_singular |= v;
   {
     int dev = 0;
     SNAC_CUDA(cudaGetDevice(&dev));
@@ -570,6 +572,10 @@ static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *
     int iters = 0;
     SNAC_TRY(mg_set_active(P.nsys, W.active, nullptr, st));
     SNAC_TRY(mg_residual<double>(P, W, S.box_x, S.box_b, (double *)W.r, S.tol, 1, 0, 0, st));
+    SNAC_TRY(mg_restart_bad_guess(P, W, S.box_x, S.box_b, (double *)W.r, st));
+    // singular systems: r = b - A x0 keeps its zero mean only up to rounding; CG cannot remove a
+    // null-space part, so it is projected out
+    SNAC_TRY(mg_project_singular(P, W, (double *)W.r, st));
     SNAC_CUDA(cudaMemcpyAsync(W.h_count, W.d_count, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     SNAC_CUDA(cudaStreamSynchronize(st));
     if (W.h_count[1]) SNAC_TRY(mg_zero_rhs_systems(P, W, S.box_x, st));
@@ -593,9 +599,11 @@ static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *
   for (outer = 0; outer < S.maxiter; outer++) {
     // r64 = b - A x64 with norms, convergence and the scale of the FP32 residual
     SNAC_TRY(mg_residual<double>(P, Wr, S.box_x, S.box_b, S.r64, S.tol, outer == 0 ? 1 : 0, 1, S.nact0, st));
+    SNAC_TRY(mg_project_singular(P, Wr, S.r64, st));  // as in the FP64 path: the correction equation stays consistent
     SNAC_CUDA(cudaMemcpyAsync(Wr.h_count, Wr.d_count, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     SNAC_CUDA(cudaStreamSynchronize(st));
     if (outer == 0 && Wr.h_count[1]) SNAC_TRY(mg_zero_rhs_systems(P, Wr, S.box_x, st));
+    if (outer == 0) SNAC_TRY(mg_restart_bad_guess(P, Wr, S.box_x, S.box_b, S.r64, st));
     if (Wr.h_count[0] == 0) break;
     SNAC_TRY(mg_ir_down(P, Wr, S.W32, S.r64, (float *)S.W32.r, S.box_e32, inner_tol, st));
     int it1 = 0;

@@ -39,7 +39,7 @@ class Domain:
     def shape(self, ib, kind):
         lo, hi = self.geom[ib]["lo"], self.geom[ib]["hi"]
         n = [hi[a] - lo[a] + 1 for a in range(3)]
-        if capi.DUDTRKO <= kind <= capi.DWDTRKO:
+        if capi.DUDTRKO <= kind <= capi.DWDTRKO or kind >= capi.DSDTRKO0:
             return tuple(n)
         return tuple(x + 2 for x in n)
 

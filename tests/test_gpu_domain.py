@@ -241,6 +241,57 @@ def test_steps_channel(snac_lib, oracle_mod, precision):
         d.close()
 
 
+def test_steps_dhc_scalar_buoyancy(snac_lib, oracle_mod):
+    """The reference's differentially-heated-cavity layout (tests/differentially_heated_cavity): one
+    scalar advected and diffused by rk_scal, Boussinesq buoyancy in rk_mom, FFT along y, fixed dt."""
+    case = cases.dhc_reference_test()
+    O = oracle_mod.OracleDomain(case)
+    d = Domain(case)
+    try:
+        s0 = cases.dhc_initial_scalar(case, lambda ib: O.grid(ib, 0, oracle_mod.G_XC))
+        rng = np.random.default_rng(5)
+        for ib in range(len(case.blocks)):
+            O.field(ib, capi.S0)[...] = s0[ib] + 1e-3 * rng.standard_normal(s0[ib].shape)
+            d.set(ib, capi.S0, O.field(ib, capi.S0))
+        for X in (O, d):
+            X.bounduvw(False)
+            X.boundp(capi.P)
+            X.boundp(capi.S0)
+        O.step(20)
+        d.step(20)
+        compare_fields(case, O, d, (capi.U, capi.V, capi.W, capi.S0), 1e-10)
+        compare_fields(case, O, d, (capi.P,), 1e-9, mean_free_p=True)
+        assert np.max(np.abs(d.get(0, capi.W))) > 1e-6  # buoyancy has set the fluid in motion
+    finally:
+        d.close()
+
+
+def test_steps_channel_forced_scalar(snac_lib, oracle_mod):
+    """Four uneven blocks with a bulk-forced scalar: the bulk mean of rk_scal is taken over all blocks and
+    the scalar's ghost planes come through the friend links."""
+    case = cases.channel_4block_scalar()
+    O = oracle_mod.OracleDomain(case)
+    d = Domain(case)
+    try:
+        seed_fields(case, O, d, seed=3, amp=0.2)
+        for X in (O, d):
+            X.bounduvw(False)
+            X.boundp(capi.P)
+        rng = np.random.default_rng(9)
+        for ib in range(len(case.blocks)):
+            f = O.field(ib, capi.S0)
+            f[...] = 0.5 + 0.1 * rng.standard_normal(f.shape)
+            d.set(ib, capi.S0, f)
+        O.boundp(capi.S0)
+        d.boundp(capi.S0)
+        O.step(3)
+        d.step(3)
+        compare_fields(case, O, d, (capi.U, capi.V, capi.W, capi.S0), 1e-10)
+        compare_fields(case, O, d, (capi.P,), 1e-9, mean_free_p=True)
+    finally:
+        d.close()
+
+
 @pytest.mark.parametrize("fft_axis", [0, 1])
 def test_gpu_ldc_golden(snac_lib, fft_axis):
     """The reference's regression (tests/lid_driven_cavity/test.py) on the GPU path, with its tolerance."""
