@@ -114,6 +114,8 @@ typedef struct snac_step_stats {
   double solve_residual_max;  /* largest final relative residual of the last step's solves */
   int    solves;              /* solves run in the last step */
   double device_ms;           /* device time of the last snac_step call (CUDA events on the library stream) */
+  int    helm_iters_max;      /* IMPDIFF: largest iteration count of the last step's Helmholtz solves */
+  double helm_residual_max;   /* IMPDIFF: largest final relative residual of those solves */
 } snac_step_stats;
 
 /* ---------------------------------------------------------------- errors, diagnostics */

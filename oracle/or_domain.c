@@ -283,12 +283,63 @@ or_domain *or_create(const or_case *c, const or_block_desc *blocks, char *err, i
     }
   }
   {
-    int cen[3] = {1, 1, 1};
-    d->ps = or_poisson_create(d, cen, 0.0, d->lambda, err, errlen);
+    d->ps = or_poisson_create(d, OR_HF_P, 0.0, d->lambda, err, errlen);
     if (!d->ps) goto fail;
     long nbox = d->ps->L[0].ncell * d->ps->nsys;
     d->box_b = calloc(nbox, sizeof(double));
     d->box_x = calloc(nbox, sizeof(double));
+  }
+  /* IMPDIFF (main.f90:771-839): BC planes and a Helmholtz problem for u, v, w and every scalar */
+  if (c->impdiff) {
+    if (c->fft_axis) { snprintf(err, errlen, "IMPDIFF with an FFT axis is not restated in the oracle"); goto fail; }
+    for (int hf = OR_HF_U; hf < OR_HF_S0 + c->nscal; hf++) {
+      for (int ib = 0; ib < d->nblocks; ib++) {
+        or_block *B = &d->b[ib];
+        double dl[3][2];
+        int cen[3], hif[3];
+        char cb[3][2];
+        double bv[3][2];
+        for (int a = 0; a < 3; a++) {
+          cen[a] = or_field_centered(hf, a);
+          hif[a] = or_field_hi(B, hf, a);
+          for (int sd = 0; sd < 2; sd++) { cb[a][sd] = or_field_cbc(B, hf, a, sd); bv[a][sd] = or_field_bc(B, hf, a, sd); }
+          /* dl of main.f90:771-773 (dxf at lo and hi along a staggered axis, dxc at lo-1 and hi otherwise),
+             from the block's own grid */
+          double *drc = calloc(B->ng[a] + 2, sizeof(double)), *drf = calloc(B->ng[a] + 2, sizeof(double)),
+                 *rc = calloc(B->ng[a] + 2, sizeof(double)), *rf = calloc(B->ng[a] + 2, sizeof(double));
+          or_initgrid(B->lo[a], B->hi[a], blocks[ib].gt[a], blocks[ib].gr[a], blocks[ib].lmin[a], blocks[ib].lmax[a], drc, drf, rc, rf);
+          if (blocks[ib].grid_file[a]) load_grid(B->lo[a], B->hi[a], blocks[ib].grid_file[a], rf, rc, drf, drc);
+          dl[a][0] = cen[a] ? drc[0] : drf[1];
+          dl[a][1] = cen[a] ? drc[B->ng[a]] : drf[B->ng[a]];
+          free(drc); free(drf); free(rc); free(rf);
+        }
+        const int nf[3] = {hif[0] - B->lo[0] + 1, hif[1] - B->lo[1] + 1, hif[2] - B->lo[2] + 1};
+        B->rhsh[hf][0] = calloc((size_t)nf[1] * nf[2] * 2, sizeof(double));
+        B->rhsh[hf][1] = calloc((size_t)nf[0] * nf[2] * 2, sizeof(double));
+        B->rhsh[hf][2] = calloc((size_t)nf[0] * nf[1] * 2, sizeof(double));
+        const double *d1[3], *d2[3];
+        for (int a = 0; a < 3; a++) { d1[a] = cen[a] ? B->g[a][0] : B->g[a][1]; d2[a] = cen[a] ? B->g[a][1] : B->g[a][0]; }
+        /* the velocity components pass bcu%x.. (main.f90:580-582: bcvel over each plane, no inflow) */
+        double *bcp[3] = {NULL, NULL, NULL};
+        if (hf < OR_HF_S0) {
+          const size_t np[3] = {(size_t)nf[1] * nf[2], (size_t)nf[0] * nf[2], (size_t)nf[0] * nf[1]};
+          for (int a = 0; a < 3; a++) {
+            bcp[a] = malloc(np[a] * 2 * sizeof(double));
+            for (int sd = 0; sd < 2; sd++)
+              for (size_t q = 0; q < np[a]; q++) bcp[a][q + np[a] * sd] = bv[a][sd];
+          }
+        }
+        or_init_bc_rhs((const char(*)[2])cb, (const double(*)[2])bv, (const double(*)[2])dl, (const int(*)[2])B->is_bound,
+                       cen, B->lo, hif, d->periods, d1[0], d2[0], d1[1], d2[1], d1[2], d2[2], B->rhsh[hf][0],
+                       B->rhsh[hf][1], B->rhsh[hf][2], bcp[0], bcp[1], bcp[2], 0);
+        for (int a = 0; a < 3; a++) free(bcp[a]);
+      }
+      d->ph[hf] = or_poisson_create(d, hf, 0.0, NULL, err, errlen);
+      if (!d->ph[hf]) goto fail;
+      long nbox = d->ph[hf]->L[0].ncell * d->ph[hf]->nsys;
+      d->hbox_b[hf] = calloc(nbox, sizeof(double));
+      d->hbox_x[hf] = calloc(nbox, sizeof(double));
+    }
   }
   d->dt = 0.0;
   free(lo);
@@ -306,11 +357,13 @@ void or_destroy(or_domain *d) {
     for (int a = 0; a < 3; a++) for (int w = 0; w < 4; w++) free(B->g[a][w]);
     for (int f = 0; f < OR_NFIELDS; f++) free(B->fld[f]);
     for (int a = 0; a < 3; a++) free(B->rhsp[a]);
+    for (int hf = 0; hf < 3 + OR_MAX_SCAL; hf++) for (int a = 0; a < 3; a++) free(B->rhsh[hf][a]);
   }
   free(d->b);
   free(d->lambda);
   or_poisson_destroy(d->ps);
   free(d->box_b); free(d->box_x);
+  for (int hf = 0; hf < 3 + OR_MAX_SCAL; hf++) { or_poisson_destroy(d->ph[hf]); free(d->hbox_b[hf]); free(d->hbox_x[hf]); }
   free(d);
 }
 
@@ -526,9 +579,55 @@ static void set_dt_from_cfl(or_domain *d) {
   d->dt = d->c.dt_f > 0.0 ? d->c.dt_f : (d->c.cfl * dt_cfl < d->c.dtmax ? d->c.cfl * dt_cfl : d->c.dtmax);
 }
 
+/* solve_impdiff_field_3d (solve_helmholtz.f90:109-138): phi <- alphai * phi * dx2 dy2 dz2 (the field's
+ * control volume), the BC planes added at the boundary cells (updt_rhs over lo..hif), then
+ * (A + alphai V) phi = rhs warm-started from the previous solution (phio) */
+static int helm_solve(or_domain *d, int hf, int kind, double alphai) {
+  or_poisson *P = d->ph[hf];
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    int hif[3], cen[3];
+    const double *d2[3];
+    for (int a = 0; a < 3; a++) {
+      hif[a] = or_field_hi(B, hf, a);
+      cen[a] = or_field_centered(hf, a);
+      d2[a] = cen[a] ? B->g[a][1] : B->g[a][0];
+    }
+    const int nx = B->ng[0], ny = B->ng[1];
+    const int nf[3] = {hif[0] - B->lo[0] + 1, hif[1] - B->lo[1] + 1, hif[2] - B->lo[2] + 1};
+    double *f = B->fld[kind];
+#define FI(i, j, k) f[(i) + (size_t)(nx + 2) * ((j) + (size_t)(ny + 2) * (k))]
+    /* solve_helmholtz.f90:123-129 scales over lo..hi, including a wall face that the solve leaves alone */
+    for (int k = 1; k <= B->ng[2]; k++)
+      for (int j = 1; j <= B->ng[1]; j++)
+        for (int i = 1; i <= B->ng[0]; i++) FI(i, j, k) = FI(i, j, k) * alphai * d2[0][i] * d2[1][j] * d2[2][k];
+    const double *rx = B->rhsh[hf][0], *ry = B->rhsh[hf][1], *rz = B->rhsh[hf][2];
+    /* bound.f90:543-585 with hi = hif, in its order x0, x1, y0, y1, z0, z1 (an edge cell takes two planes) */
+    for (int sd = 0; sd < 2; sd++)
+      if (B->is_bound[0][sd])
+        for (int k = 1; k <= nf[2]; k++)
+          for (int j = 1; j <= nf[1]; j++) FI(sd ? nf[0] : 1, j, k) += rx[(j - 1) + (size_t)nf[1] * ((k - 1) + (size_t)nf[2] * sd)];
+    for (int sd = 0; sd < 2; sd++)
+      if (B->is_bound[1][sd])
+        for (int k = 1; k <= nf[2]; k++)
+          for (int i = 1; i <= nf[0]; i++) FI(i, sd ? nf[1] : 1, k) += ry[(i - 1) + (size_t)nf[0] * ((k - 1) + (size_t)nf[2] * sd)];
+    for (int sd = 0; sd < 2; sd++)
+      if (B->is_bound[2][sd])
+        for (int j = 1; j <= nf[1]; j++)
+          for (int i = 1; i <= nf[0]; i++) FI(i, j, sd ? nf[2] : 1) += rz[(i - 1) + (size_t)nf[0] * ((j - 1) + (size_t)nf[1] * sd)];
+#undef FI
+  }
+  P->shift[0] = alphai;
+  or_box_gather(d, P, kind, d->hbox_b[hf]);
+  int rc = or_poisson_solve(P, d->hbox_b[hf], d->hbox_x[hf]);
+  or_box_scatter(d, P, d->hbox_x[hf], kind);
+  return rc;
+}
+
 /* main.f90:907-936 for the explicit-diffusion path: rk_scal on every block, the bulk mean summed over
  * blocks as the MPI_ALLREDUCE of scal.f90:175 sums it over ranks, bulk_forcing_s, boundp of the scalar */
-static void scalar_stage(or_domain *d, int irk) {
+static int scalar_stage(or_domain *d, int irk) {
+  int rc = 0;
   for (int s = 0; s < d->c.nscal; s++) {
     const int forced = d->c.is_sforced[s];
     double msum = 0.0;
@@ -545,13 +644,19 @@ static void scalar_stage(or_domain *d, int irk) {
       or_block *B = &d->b[ib];
       or_bulk_forcing_s(B->lo, B->hi, forced, f, B->fld[OR_S0 + s]);
     }
+    if (d->c.impdiff) { /* main.f90:914-934: alpha = -s%alpha*dtrk/2 */
+      const double dtrk = (RKC[irk][0] + RKC[irk][1]) * d->dt;
+      const double alpha = -(1.0 / d->c.alphai[s]) * dtrk / 2.0;
+      rc |= helm_solve(d, OR_HF_S0 + s, OR_S0 + s, 1.0 / alpha);
+    }
     or_boundp(d, OR_S0 + s);
   }
+  return rc;
 }
 
-/* main.f90:893-1069 for the explicit-diffusion path (scalars and Boussinesq buoyancy included) */
+/* main.f90:893-1069 with scalars, Boussinesq buoyancy and IMPDIFF (3-D solves) */
 int or_step(or_domain *d, int nsteps) {
-  if (d->c.impdiff) return -10; /* the IMPDIFF Helmholtz solves are not restated in the oracle driver */
+  if (d->c.impdiff && d->c.fft_axis) return -10; /* IMPDIFF with an FFT axis is not restated */
   if (d->dt == 0.0) set_dt_from_cfl(d);          /* main.f90:660-661 */
   double visc = 1.0 / d->c.visci;
   int rc = 0;
@@ -561,15 +666,17 @@ int or_step(or_domain *d, int nsteps) {
     for (int irk = 0; irk < 3; irk++) {
       double dtrk = (RKC[irk][0] + RKC[irk][1]) * d->dt;
       double alpha = -visc * dtrk / 2.0;
-      scalar_stage(d, irk);
+      rc |= scalar_stage(d, irk);
       const int bq = d->c.boussinesq && d->c.nscal > 0;
       for (int ib = 0; ib < d->nblocks; ib++) {
         or_block *B = &d->b[ib];
         or_rk_mom(RKC[irk], B->lo, B->hi, B->g[0][0], B->g[0][1], B->g[1][0], B->g[1][1], B->g[2][0], B->g[2][1],
                   d->dt, d->c.bforce, d->c.gacc, d->c.beta, bq ? B->fld[OR_S0] : NULL, visc, B->fld[OR_U],
                   B->fld[OR_V], B->fld[OR_W], B->fld[OR_P], B->fld[OR_DUDTRKO], B->fld[OR_DVDTRKO],
-                  B->fld[OR_DWDTRKO], 0, bq);
+                  B->fld[OR_DWDTRKO], d->c.impdiff, bq);
       }
+      if (d->c.impdiff) /* main.f90:947-995: the three Helmholtz solves of u, v, w with alphai = 1/alpha */
+        for (int comp = 0; comp < 3; comp++) rc |= helm_solve(d, OR_HF_U + comp, OR_U + comp, 1.0 / alpha);
       or_bounduvw(d, 0);
       or_fillps_all(d, dtrk);
       or_updt_rhs_all(d);

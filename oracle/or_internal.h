@@ -13,6 +13,7 @@ typedef struct or_block {
   double *g[3][4];            /* per axis: [dc, df, c, f], (n+2) entries for lo-1..hi+1 */
   double *fld[OR_NFIELDS];
   double *rhsp[3];            /* init_bc_rhs planes for the pressure (rhsp%x/y/z) */
+  double *rhsh[3 + OR_MAX_SCAL][3]; /* IMPDIFF: init_bc_rhs planes of u, v, w and the scalars (rhsu%x, ...) */
 } or_block;
 
 /* one multigrid level of a box problem */
@@ -28,7 +29,13 @@ typedef struct or_level {
   int coarsened[3];
 } or_level;
 
+/* the field a box problem solves for: the pressure, or (IMPDIFF Helmholtz problems) velocity
+ * component c (OR_HF_U + c) or scalar s (OR_HF_S0 + s) */
+enum { OR_HF_P = -1, OR_HF_U = 0, OR_HF_S0 = 3 };
+
 typedef struct or_poisson {
+  int field;                  /* OR_HF_P, OR_HF_U + c or OR_HF_S0 + s */
+  int helm;                   /* Helmholtz problem: never singular, iterative coarsest level */
   int mode3d;                 /* 1: one 3-D system; 0: 2-D planes batched along the transform axis */
   int ax[3];                  /* box axis -> physical axis (ax[2] = transform axis in plane mode) */
   int periodic[3];            /* per box axis */
@@ -57,11 +64,18 @@ struct or_domain {
   double *lambda;             /* eigenvalues/dl^2 along the transform axis */
   or_poisson *ps;
   double *box_b, *box_x;      /* gathered rhs and warm start (po in transformed space) */
+  /* IMPDIFF Helmholtz problems of u, v, w and the scalars (3-D mode), with their warm starts */
+  or_poisson *ph[3 + OR_MAX_SCAL];
+  double *hbox_b[3 + OR_MAX_SCAL], *hbox_x[3 + OR_MAX_SCAL];
 };
 
 /* solver module */
-or_poisson *or_poisson_create(or_domain *d, const int centered[3], double alpha,
-                              const double *lambda, char *err, int errlen);
+or_poisson *or_poisson_create(or_domain *d, int field, double alpha, const double *lambda, char *err, int errlen);
+/* the field's boundary letter, centring and last solved index of block B along physical axis p */
+char or_field_cbc(const or_block *B, int field, int p, int side);
+double or_field_bc(const or_block *B, int field, int p, int side);
+int  or_field_centered(int field, int p);
+int  or_field_hi(const or_block *B, int field, int p);
 void or_poisson_destroy(or_poisson *P);
 int  or_poisson_solve(or_poisson *P, double *b, double *x);
 void or_box_gather(or_domain *d, or_poisson *P, int kind, double *box);

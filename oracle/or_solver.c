@@ -114,9 +114,31 @@ static void build_coarse_operator(or_poisson *P, or_level *L, double alpha) {
       }
 }
 
-/* diagonal entry for system s (plane mode adds (lambda*W0)*W1, solver.f90:1010-1017) */
+/* field descriptors: main.f90:771-805 (velocity: cbcvel(:,:,c), is_centered false along c, hi - 1
+ * at a wall along c), main.f90:830-838 (scalars: s%cbc, centred) and the pressure */
+char or_field_cbc(const or_block *B, int field, int p, int side) {
+  if (field == OR_HF_P) return B->desc.cbcpre[p][side];
+  if (field < OR_HF_S0) return B->desc.cbcvel[field][p][side];
+  return B->desc.cbcscal[field - OR_HF_S0][p][side];
+}
+double or_field_bc(const or_block *B, int field, int p, int side) {
+  if (field == OR_HF_P) return B->desc.bcpre[p][side];
+  if (field < OR_HF_S0) return B->desc.bcvel[field][p][side];
+  return B->desc.bcscal[field - OR_HF_S0][p][side];
+}
+int or_field_centered(int field, int p) { return !(field >= OR_HF_U && field < OR_HF_S0 && field == p); }
+int or_field_hi(const or_block *B, int field, int p) {
+  return B->hi[p] - ((!or_field_centered(field, p) && B->is_bound[p][1]) ? 1 : 0);
+}
+
+/* diagonal entry for system s: plane mode adds (lambda*W0)*W1 (solver.f90:1010-1017); a 3-D Helmholtz
+ * problem adds alphai*W0*W1*W2 (add_weighted_constant_to_diagonal, solve_helmholtz.f90:134) */
 static inline double diag_of(const or_poisson *P, const or_level *L, long c, int i, int j, int s) {
-  if (P->mode3d) return L->cc[c];
+  if (P->mode3d) {
+    if (P->shift[s] == 0.0) return L->cc[c];
+    int k = (int)(c / ((long)L->n[0] * L->n[1]));
+    return L->cc[c] + P->shift[s] * (L->W[0][i] * L->W[1][j] * L->W[2][k]);
+  }
   return L->cc[c] + P->shift[s] * L->W[0][i] * L->W[1][j];
 }
 
@@ -277,9 +299,12 @@ static int build_dense(or_poisson *P, or_level *L, int s, double *M) {
   return 0;
 }
 
-or_poisson *or_poisson_create(or_domain *d, const int centered[3], double alpha,
-                              const double *lambda, char *err, int errlen) {
+or_poisson *or_poisson_create(or_domain *d, int field, double alpha, const double *lambda, char *err, int errlen) {
   or_poisson *P = calloc(1, sizeof(or_poisson));
+  int centered[3];
+  for (int p = 0; p < 3; p++) centered[p] = or_field_centered(field, p);
+  P->field = field;
+  P->helm = field != OR_HF_P;
   P->mode3d = d->fft_axis == 0;
   if (P->mode3d) { P->ax[0] = 0; P->ax[1] = 1; P->ax[2] = 2; }
   else { P->ax[0] = d->il; P->ax[1] = d->iu; P->ax[2] = d->fft_axis - 1; }
@@ -288,10 +313,10 @@ or_poisson *or_poisson_create(or_domain *d, const int centered[3], double alpha,
   P->nu = 2;
   int lo_min[3], hi_max[3];
   for (int p = 0; p < 3; p++) {
-    lo_min[p] = d->b[0].lo[p]; hi_max[p] = d->b[0].hi[p];
+    lo_min[p] = d->b[0].lo[p]; hi_max[p] = or_field_hi(&d->b[0], field, p);
     for (int ib = 1; ib < d->nblocks; ib++) {
       if (d->b[ib].lo[p] < lo_min[p]) lo_min[p] = d->b[ib].lo[p];
-      if (d->b[ib].hi[p] > hi_max[p]) hi_max[p] = d->b[ib].hi[p];
+      if (or_field_hi(&d->b[ib], field, p) > hi_max[p]) hi_max[p] = or_field_hi(&d->b[ib], field, p);
     }
     P->lo_min[p] = lo_min[p];
   }
@@ -330,11 +355,12 @@ or_poisson *or_poisson_create(or_domain *d, const int centered[3], double alpha,
       d2[p] = centered[p] ? B->g[p][1] : B->g[p][0];
       q3[p] = centered[p] ? 0 : 1;
     }
-    int loc[3], hic[3];
+    int loc[3], hic[3], bhi[3];
+    for (int p = 0; p < 3; p++) bhi[p] = or_field_hi(B, field, p);
     for (int a = 0; a < 3; a++) {
       int p = P->ax[a];
       loc[a] = (a < na) ? B->lo[p] : 0;
-      hic[a] = (a < na) ? B->hi[p] : 0;
+      hic[a] = (a < na) ? bhi[p] : 0;
     }
     for (int g2 = loc[2]; g2 <= hic[2]; g2++)
       for (int g1 = loc[1]; g1 <= hic[1]; g1++)
@@ -386,13 +412,13 @@ or_poisson *or_poisson_create(or_domain *d, const int centered[3], double alpha,
             int p = P->ax[a];
             if (d->periods[p] != 0) continue;
             if (B->is_bound[p][0] && gg[a] == B->lo[p]) {
-              int t = fold_type(B->desc.cbcpre[p][0], centered[p]);
+              int t = fold_type(or_field_cbc(B, field, p, 0), centered[p]);
               cc = cc + fold_sgn(t) * cmv[a];
               cmv[a] = 0.0;
               code |= (unsigned short)(t << (2 * (2 * a)));
             }
-            if (B->is_bound[p][1] && gg[a] == B->hi[p]) {
-              int t = fold_type(B->desc.cbcpre[p][1], centered[p]);
+            if (B->is_bound[p][1] && gg[a] == bhi[p]) {
+              int t = fold_type(or_field_cbc(B, field, p, 1), centered[p]);
               cc = cc + fold_sgn(t) * cpv[a];
               cpv[a] = 0.0;
               code |= (unsigned short)(t << (2 * (2 * a + 1)));
@@ -431,7 +457,7 @@ or_poisson *or_poisson_create(or_domain *d, const int centered[3], double alpha,
     if (L->code[c] & 0x8000) continue;
     for (int f = 0; f < 6; f++) { int t = (L->code[c] >> (2 * f)) & 3; if (t == 2 || t == 3) has_dir = 1; }
   }
-  for (int s = 0; s < P->nsys; s++) P->singular[s] = (!has_dir && alpha == 0.0 && P->shift[s] == 0.0);
+  for (int s = 0; s < P->nsys; s++) P->singular[s] = !P->helm && (!has_dir && alpha == 0.0 && P->shift[s] == 0.0);
   /* hierarchy: coarsen an axis while every block keeps an even offset and extent */
   int boff[64][3], bext[64][3];
   if (d->nblocks > 64) { snprintf(err, errlen, "too many blocks for the oracle solver"); goto fail; }
@@ -439,7 +465,7 @@ or_poisson *or_poisson_create(or_domain *d, const int centered[3], double alpha,
     for (int a = 0; a < 3; a++) {
       int p = P->ax[a];
       boff[ib][a] = (a < na) ? d->b[ib].lo[p] - lo_min[p] : 0;
-      bext[ib][a] = (a < na) ? d->b[ib].hi[p] - d->b[ib].lo[p] + 1 : 1;
+      bext[ib][a] = (a < na) ? or_field_hi(&d->b[ib], field, p) - d->b[ib].lo[p] + 1 : 1;
     }
   P->nlev = 1;
   while (P->nlev < OR_MAXLEV) {
@@ -496,7 +522,9 @@ or_poisson *or_poisson_create(or_domain *d, const int centered[3], double alpha,
   }
   {
     or_level *C = &P->L[P->nlev - 1];
-    if (C->ncell <= OR_DENSE_MAX) {
+    /* Helmholtz problems: the dense inverse would depend on the shift; their coarsest level is
+       diagonally dominant and is smoothed instead */
+    if (C->ncell <= OR_DENSE_MAX && !P->helm) {
       C->dinv = calloc((size_t)C->ncell * C->ncell * P->nsys, sizeof(double));
       for (int s = 0; s < P->nsys; s++)
         if (build_dense(P, C, s, C->dinv + (size_t)C->ncell * C->ncell * s)) {
@@ -599,9 +627,10 @@ void or_box_gather(or_domain *d, or_poisson *P, int kind, double *box) {
     or_block *B = &d->b[ib];
     int nx = B->hi[0] - B->lo[0] + 1, ny = B->hi[1] - B->lo[1] + 1;
     double *f = B->fld[kind];
-    for (int k = B->lo[2]; k <= B->hi[2]; k++)
-      for (int j = B->lo[1]; j <= B->hi[1]; j++)
-        for (int i = B->lo[0]; i <= B->hi[0]; i++) {
+    int h0 = or_field_hi(B, P->field, 0), h1 = or_field_hi(B, P->field, 1), h2 = or_field_hi(B, P->field, 2);
+    for (int k = B->lo[2]; k <= h2; k++)
+      for (int j = B->lo[1]; j <= h1; j++)
+        for (int i = B->lo[0]; i <= h0; i++) {
           int g[3] = {i, j, k};
           long c, s;
           int a0 = g[P->ax[0]] - P->lo_min[P->ax[0]], a1 = g[P->ax[1]] - P->lo_min[P->ax[1]];
@@ -619,9 +648,10 @@ void or_box_scatter(or_domain *d, or_poisson *P, double *box, int kind) {
     or_block *B = &d->b[ib];
     int nx = B->hi[0] - B->lo[0] + 1, ny = B->hi[1] - B->lo[1] + 1;
     double *f = B->fld[kind];
-    for (int k = B->lo[2]; k <= B->hi[2]; k++)
-      for (int j = B->lo[1]; j <= B->hi[1]; j++)
-        for (int i = B->lo[0]; i <= B->hi[0]; i++) {
+    int h0 = or_field_hi(B, P->field, 0), h1 = or_field_hi(B, P->field, 1), h2 = or_field_hi(B, P->field, 2);
+    for (int k = B->lo[2]; k <= h2; k++)
+      for (int j = B->lo[1]; j <= h1; j++)
+        for (int i = B->lo[0]; i <= h0; i++) {
           int g[3] = {i, j, k};
           long c, s;
           int a0 = g[P->ax[0]] - P->lo_min[P->ax[0]], a1 = g[P->ax[1]] - P->lo_min[P->ax[1]];

@@ -52,7 +52,8 @@ class Options(C.Structure):
 
 class StepStats(C.Structure):
     _fields_ = [("istep", C.c_int), ("time", C.c_double), ("dt", C.c_double), ("solve_iters_max", C.c_int),
-                ("solve_residual_max", C.c_double), ("solves", C.c_int), ("device_ms", C.c_double)]
+                ("solve_residual_max", C.c_double), ("solves", C.c_int), ("device_ms", C.c_double),
+                ("helm_iters_max", C.c_int), ("helm_residual_max", C.c_double)]
 
 
 _lib = None

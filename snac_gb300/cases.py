@@ -240,6 +240,22 @@ def dhc_reference_test() -> Case:
                 is_sforced=(0,), icheck=10, fft_axis=2, boussinesq=1, tol=1e-12)
 
 
+def heated_cavity(n=(512, 512, 256), stretch: float = 1.5, ra: float = 1e8, pr: float = 0.71, impdiff: int = 1,
+                  tol: float = 1e-12, dt_f: float = -1.0) -> Case:
+    """Config 5: differentially heated cavity, one block on the unit box (n cells), tanh-stretched towards
+    every wall (gt = 0, the two-end clustering of initgrid.f90, with gr = stretch), no-slip walls, T = +0.5 / -0.5
+    on x- / x+ (hot / cold), adiabatic elsewhere, Boussinesq buoyancy with gacc = (0, 0, -1), beta = 1,
+    visci = sqrt(Ra/Pr), alphai = sqrt(Ra Pr) (the convention of tests/differentially_heated_cavity),
+    3-D pressure solve, implicit diffusion when impdiff (IMPDIFF)."""
+    gr = max(stretch, 0.0)
+    b = Block(ng=tuple(n), lmin=(0.0, 0.0, 0.0), lmax=(1.0, 1.0, 1.0), gt=(0, 0, 0), gr=(gr, gr, gr),
+              cbcvel=[bc6("DDDDDD")] * 3, bcvel=[val6([0] * 6)] * 3, cbcpre=bc6("NNNNNN"), bcpre=val6([0] * 6),
+              cbcscal=[bc6("DDNNNN")], bcscal=[val6([0.5, -0.5, 0, 0, 0, 0])])
+    return Case(name=f"dhc{n[0]}x{n[1]}x{n[2]}", blocks=[b], visci=math.sqrt(ra / pr), cfl=0.95, dtmax=1e9,
+                dt_f=dt_f, gacc=(0.0, 0.0, -1.0), beta=1.0, nscal=1, alphai=(math.sqrt(ra * pr),), ssource=(0.0,),
+                scalf=(0.0,), is_sforced=(0,), icheck=10, fft_axis=0, impdiff=impdiff, boussinesq=1, tol=tol)
+
+
 def dhc_initial_scalar(case: Case, xc_of_block):
     """initflow.f90:247-256 ('dhc'): T linear in x between the two wall values, on every cell incl. halo."""
     out = {}

@@ -27,6 +27,7 @@ void *Domain::alloc(size_t bytes) {
 }
 Domain::~Domain() {
   ps.reset();
+  for (auto &h : hs) h.reset();
   for (void *p : allocs) cudaFree(p);
   if (h_red) cudaFreeHost(h_red);
   if (ev0) cudaEventDestroy(ev0);
@@ -194,7 +195,10 @@ static int build_domain(Domain &d, const snac_case *c, const snac_block_desc *bl
   d.nblocks = c->nblocks;
   if (d.nblocks < 1) { set_error("nblocks must be >= 1"); return SNAC_ERR_ARG; }
   if (c->nscal < 0 || c->nscal > SNAC_MAX_SCAL) { set_error("nscal out of range"); return SNAC_ERR_ARG; }
-  if (c->impdiff) { set_error("IMPDIFF (implicit diffusion) is not wired into snac_step yet"); return SNAC_ERR_UNSUPPORTED; }
+  if (c->impdiff && c->fft_axis) {
+    set_error("IMPDIFF with an FFT-reduced pressure solve (_FFT_X/_Y/_Z) is not built: use fft_axis = 0");
+    return SNAC_ERR_UNSUPPORTED;
+  }
   for (int q = 0; q < c->nscal; q++)
     if (!(c->alphai[q] > 0.0)) { set_error("alphai of scalar %d must be positive", q + 1); return SNAC_ERR_ARG; }
   d.hb.resize(d.nblocks);
@@ -453,6 +457,16 @@ static int updt_rhs_all(Domain &d) {
   return SNAC_OK;
 }
 
+// one Helmholtz solve; the largest iteration count and residual of the step are kept with the pressure's
+static int helm_step(Domain &d, PoissonSolver &S, double alphai) {
+  const int rc = solver_solve_helmholtz(d, S, alphai);
+  if (rc != SNAC_OK && rc != SNAC_ERR_NOT_CONVERGED) return rc;
+  d.last_helm_iters = std::max(d.last_helm_iters, S.last_iters);
+  d.last_helm_res = std::max(d.last_helm_res, S.last_res);
+  if (rc == SNAC_ERR_NOT_CONVERGED) d.helm_not_converged = true;  // reported by snac_step like the pressure's
+  return SNAC_OK;
+}
+
 static int rk_mom_all(Domain &d, int irk) {
   RkMomParams prm;
   prm.f1 = RKC[irk][0] * d.dt;
@@ -460,12 +474,16 @@ static int rk_mom_all(Domain &d, int irk) {
   prm.f12 = prm.f1 + prm.f2;
   for (int a = 0; a < 3; a++) { prm.bforce[a] = d.c.bforce[a]; prm.gb[a] = 0.0; }
   prm.visc = 1.0 / d.c.visci;
-  prm.impdiff = 0;
+  prm.impdiff = d.c.impdiff;
   prm.boussinesq = d.c.boussinesq && d.c.nscal > 0;  // rk.f90:104-108 with scalars(1)
   if (prm.boussinesq)
     for (int a = 0; a < 3; a++) prm.gb[a] = prm.f12 * d.c.gacc[a] * d.c.beta * 0.5;
   SNAC_TRY(launch_rk_mom(d.d_db, d.d_tiles, d.ntiles, prm, d.st));
   SNAC_TRY(launch_rk_mom_writeback(d.d_db, d.d_tiles, d.ntiles, d.st));
+  if (d.c.impdiff) {  // main.f90:947-995: u, v, w Helmholtz solves with alphai = 1/(-visc*dtrk/2)
+    const double alpha = -prm.visc * ((RKC[irk][0] + RKC[irk][1]) * d.dt) / 2.0;
+    for (int comp = 0; comp < 3; comp++) SNAC_TRY(helm_step(d, *d.hs[HF_U + comp], 1.0 / alpha));
+  }
   return SNAC_OK;
 }
 
@@ -488,6 +506,10 @@ static int rk_scal_all(Domain &d, int irk) {
     if (forced) {
       SNAC_TRY(launch_reduce_final(d.d_part, d.ntiles, d.d_red, d.st));
       SNAC_TRY(launch_bulk_forcing_s(d.d_db, d.d_tiles, d.ntiles, q, d.c.scalf[q], 1.0 / d.vol_all, d.d_red, d.st));
+    }
+    if (d.c.impdiff) {  // main.f90:914-934: alpha = -s%alpha*dtrk/2, the scalar's Helmholtz solve
+      const double alpha = -prm.alpha * ((RKC[irk][0] + RKC[irk][1]) * d.dt) / 2.0;
+      SNAC_TRY(helm_step(d, *d.hs[HF_S0 + q], 1.0 / alpha));
     }
     SNAC_TRY(bound_p(d, SNAC_S0 + q));
   }
@@ -632,6 +654,11 @@ int snac_init(const snac_case *c, const snac_block_desc *blocks, const snac_opti
   if (rc == SNAC_OK) {
     d->ps.reset(new PoissonSolver());
     rc = solver_create(*d, *d->ps);
+  }
+  // IMPDIFF (main.f90:771-869): one Helmholtz solver per velocity component and scalar
+  for (int f = HF_U; rc == SNAC_OK && c->impdiff && f < HF_S0 + c->nscal; f++) {
+    d->hs[f].reset(new PoissonSolver());
+    rc = solver_create(*d, *d->hs[f], true, f);
   }
   if (rc != SNAC_OK) { delete d; return rc; }
   g_dom = d;
@@ -817,10 +844,13 @@ int snac_step(int nsteps) {
     d->time += d->dt;
     d->last_solve_iters = 0;
     d->last_solve_res = 0.0;
+    d->last_helm_iters = 0;
+    d->last_helm_res = 0.0;
     d->solves = 0;
     for (int irk = 0; irk < 3; irk++) {
+      d->helm_not_converged = false;
       const int rc = one_stage(*d, irk);
-      if (rc == SNAC_ERR_NOT_CONVERGED) rc_all = rc;
+      if (rc == SNAC_ERR_NOT_CONVERGED || (rc == SNAC_OK && d->helm_not_converged)) rc_all = SNAC_ERR_NOT_CONVERGED;
       else if (rc != SNAC_OK) return rc;
     }
     if (d->c.icheck > 0 && d->istep % d->c.icheck == 0) SNAC_TRY(set_dt_from_cfl(*d));
@@ -842,6 +872,8 @@ int snac_get_stats(snac_step_stats *st) {
   st->solve_residual_max = d->last_solve_res;
   st->solves = d->solves;
   st->device_ms = d->device_ms;
+  st->helm_iters_max = d->last_helm_iters;
+  st->helm_residual_max = d->last_helm_res;
   return SNAC_OK;
 }
 int snac_set_dt(double dt) {

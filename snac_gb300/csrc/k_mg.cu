@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(256) k_rbgs(MgLevelD L, MgGeom G, const T *shi
   if (L.code[c] & 0x8000) return;
   const long off = L.ncell * s;
   T *__restrict__ xs = x + off;
-  const T d = diag_of<T>(L, G, G.mode3d ? T(0) : shift[s], c);
+  const T d = diag_of<T>(L, G, shift[s], c);
   const T acc = offdiag<T>(L, G, [&](int e) { return xs[e]; }, c, i, j, k);
   xs[c] = (b[off + c] - acc) * rcpt(d);
 }
@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(256) k_resid_restrict(MgLevelD F, MgLevelD C, 
   const int cc = I + C.n[0] * (J + C.n[1] * K);
   const long offf = F.ncell * s, offc = C.ncell * s;
   const T *__restrict__ xs = xf + offf;
-  const T sh = G.mode3d ? T(0) : shift[s];
+  const T sh = shift[s];
   T sum = 0;
   const int e0 = C.coarsened[0] ? 2 : 1, e1 = C.coarsened[1] ? 2 : 1, e2 = C.coarsened[2] ? 2 : 1;
   for (int dk = 0; dk < e2; dk++)
@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(256) k_cg_resid(MgLevelD L, MgGeom G, const T 
   if (active && !active[s]) return;
   const long off = L.ncell * s;
   const T *__restrict__ xs = x + off;
-  const T sh = G.mode3d ? T(0) : shift[s];
+  const T sh = shift[s];
   const int i = blockIdx.x * 32 + threadIdx.x;
   T rr = 0, bb = 0;
   for (int q = 0; q < RROWS; q++) {
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(256) k_cg_apply(MgLevelD L, MgGeom G, const T 
   const T *__restrict__ zs = z + off;
   const T *__restrict__ ps = po + off;
   const T beta = FUSEP ? (T)sc[s].beta : T(0);
-  const T sh = G.mode3d ? T(0) : shift[s];
+  const T sh = shift[s];
   auto pv = [&](int e) -> T { return FUSEP ? fmat(beta, ps[e], zs[e]) : ps[e]; };
   const int i = blockIdx.x * 32 + threadIdx.x;
   T pq = 0;

@@ -50,8 +50,24 @@ struct HostBlock {
   std::vector<double> dl[3];     // dl(0:1,idir) of main.f90:725-727
 };
 
+// the field a solver is built for: the pressure, or (IMPDIFF Helmholtz problems) velocity component c
+// (HF_U + c) or scalar s (HF_S0 + s)
+enum { HF_P = -1, HF_U = 0, HF_S0 = 3 };
+char field_cbc(const HostBlock &H, int field, int p, int side);
+double field_bc(const HostBlock &H, int field, int p, int side);
+inline int field_centered(int field, int p) { return !(field >= HF_U && field < HF_S0 && field == p); }
+// last solved index along p: one less at a wall along a velocity component's own direction
+inline int field_hi(const HostBlock &H, int field, int p) {
+  return H.hi[p] - ((!field_centered(field, p) && H.is_bound[p][1]) ? 1 : 0);
+}
+
+struct HelmBlk;  // per-block tables of a Helmholtz solver (k_helm.cu)
+
 // the device multigrid problem plus its host-side construction data
 struct PoissonSolver {
+  int field = HF_P;                  // what the solver is built for
+  int helm = 0;                      // Helmholtz problem: never singular, iterative coarsest level
+  HelmBlk *d_hb = nullptr;           // Helmholtz solvers: per-block extents, offsets and BC planes (device)
   int mode3d = 0, ax[3] = {0, 1, 2}, periodic[3] = {0, 0, 0}, nsys = 1, lo_min[3] = {0, 0, 0};
   int fft_axis = 0, nfft = 0, kind_fwd = -1, kind_bwd = -1;
   double normfft = 1.0;
@@ -102,10 +118,14 @@ struct Domain {
   std::vector<size_t> rhsp_off;      // per block: offsets of x,y,z planes
   double *d_part = nullptr, *d_red = nullptr, *h_red = nullptr;
   std::unique_ptr<PoissonSolver> ps;
+  std::unique_ptr<PoissonSolver> hs[3 + SNAC_MAX_SCAL];  // IMPDIFF: Helmholtz solvers of u, v, w, scalars
   double dt = 0.0, time = 0.0;
   int istep = 0;
   int last_solve_iters = 0, solves = 0;
   double last_solve_res = 0.0;
+  int last_helm_iters = 0;
+  double last_helm_res = 0.0;
+  bool helm_not_converged = false;
   cudaStream_t st = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double device_ms = 0.0;
@@ -115,7 +135,12 @@ struct Domain {
 };
 
 Domain *domain();
-int solver_create(Domain &d, PoissonSolver &S, bool upload = true);
+int solver_create(Domain &d, PoissonSolver &S, bool upload = true, int field = HF_P);
+// IMPDIFF (solve_helmholtz.f90:109-138): S.field <- solution of (A + alphai V) x = alphai V field + BC planes
+int solver_solve_helmholtz(Domain &d, PoissonSolver &S, double alphai);
+int helm_upload_tables(Domain &d, PoissonSolver &S, const std::vector<std::vector<double>> (&planes)[3]);
+int helm_rhs(Domain &d, PoissonSolver &S, double alphai, cudaStream_t st);
+int helm_io(Domain &d, PoissonSolver &S, double *box, int to_box, cudaStream_t st);
 int solver_solve_pressure(Domain &d, PoissonSolver &S);
 
 // transforms (k_fft.cu)

@@ -2,7 +2,7 @@
 //
 // Every kernel that applies the operator (smoothers, residuals, the tiled and the
 // one-CTA kernels) forms the same sums in the same order with explicit FMAs:
-//   diagonal  d   = fma(lambda_s, w01, cc)          (plane mode; cc alone in 3-D)
+//   diagonal  d   = fma(shift_s, w01, cc)           (w01: area in plane mode, volume in 3-D)
 //   couplings acc = +x, -x, +y, -y (, +z, -z) terms, each acc = fma(c, v, acc)
 //   smoother  x   = (b - acc) * rcpt(d)
 //   residual  r   = b - fma(d, x, acc)
@@ -42,9 +42,11 @@ __device__ __forceinline__ double fmat(double a, double b, double c) { return __
 __device__ __forceinline__ float rcpt(float d) { return __frcp_rn(d); }
 __device__ __forceinline__ double rcpt(double d) { return __drcp_rn(d); }
 
+// diagonal of cell c for a system with shift sh: cc + sh * w01 (w01 = area in plane mode, where sh is the
+// wavenumber's eigenvalue; volume in 3-D mode, where sh is 0 for the pressure and alphai for IMPDIFF)
 template <typename T>
 __device__ __forceinline__ T diag_of(const MgLevelD &L, const MgGeom &G, T sh, int c) {
-  if (G.mode3d) return LA<T>::cc(L)[c];
+  (void)G;
   return fmat(sh, LA<T>::w01(L)[c], LA<T>::cc(L)[c]);
 }
 

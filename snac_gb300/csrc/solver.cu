@@ -178,9 +178,86 @@ struct Builder {
 
 }  // namespace
 
-// build the box problem of the pressure (centred in every direction, alpha = 0)
-int solver_create(Domain &d, PoissonSolver &S, bool upload) {
+char field_cbc(const HostBlock &H, int field, int p, int side) {
+  if (field == HF_P) return H.desc.cbcpre[p][side];
+  if (field < HF_S0) return H.desc.cbcvel[field][p][side];
+  return H.desc.cbcscal[field - HF_S0][p][side];
+}
+double field_bc(const HostBlock &H, int field, int p, int side) {
+  if (field == HF_P) return H.desc.bcpre[p][side];
+  if (field < HF_S0) return H.desc.bcvel[field][p][side];
+  return H.desc.bcscal[field - HF_S0][p][side];
+}
+
+// init_bc_rhs (solver.f90:44-157) of a field in 3-D mode over lo..hif, with the field's centring,
+// spacings and boundary values; dl is dxc at lo-1 and hi along a centred axis, dxf at lo and hi along a
+// staggered one (main.f90:725-727, 771-773).  Planes rhs?(.., .., 0:1) over the solved extents.  The
+// velocity components pass the boundary-value planes bcu%x.. (main.f90:580-582, uniform bcvel without an
+// inflow), which scale a plane by bcval/bc where bc is nonzero (solver.f90:122-123); the scalars do not.
+static void init_bc_rhs_field(const HostBlock &H, int field, const int periods[3], std::vector<double> rhs[3]) {
+  int nf[3], cen[3], q3[3];
+  const double *d1[3], *d2[3];
+  double factor[3][2];
+  for (int a = 0; a < 3; a++) {
+    nf[a] = field_hi(H, field, a) - H.lo[a] + 1;
+    cen[a] = field_centered(field, a);
+    q3[a] = cen[a] ? 0 : 1;
+    d1[a] = cen[a] ? H.g[a][0].data() : H.g[a][1].data();
+    d2[a] = cen[a] ? H.g[a][1].data() : H.g[a][0].data();
+    for (int s = 0; s < 2; s++) {
+      factor[a][s] = 0.0;
+      if (!H.is_bound[a][s]) continue;
+      const char cb = field_cbc(H, field, a, s);
+      const double bc = field_bc(H, field, a, s);
+      const double dl = cen[a] ? H.dl[a][s] : H.g[a][1][s ? H.ng[a] : 1];
+      if (cb == 'N') { factor[a][s] = 1.0 * dl * bc; if (s == 1) factor[a][s] = -factor[a][s]; }
+      else if (cb == 'D') factor[a][s] = cen[a] ? -2.0 * bc : -1.0 * bc;
+    }
+  }
+  rhs[0].assign((size_t)nf[1] * nf[2] * 2, 0.0);
+  rhs[1].assign((size_t)nf[0] * nf[2] * 2, 0.0);
+  rhs[2].assign((size_t)nf[0] * nf[1] * 2, 0.0);
+  auto W = [&](int i, int j, int k) { return d2[0][i] * d2[1][j] * d2[2][k]; };  // local 1-based indices
+  const bool has_bcval = field >= HF_U && field < HF_S0;
+  auto scale = [&](double r, int a, int sd) {
+    const double bc = field_bc(H, field, a, sd);
+    return (has_bcval && bc != 0.0) ? r * bc / bc : r;
+  };
+  for (int idir = 0; idir < 3; idir++) {
+    if (periods[idir] != 0) continue;
+    const int n = nf[idir];
+    for (int sd = 0; sd < (n > 1 ? 2 : 1); sd++) {
+      if (!H.is_bound[idir][sd]) continue;
+      const int cf = sd ? n : 1;  // boundary cell (local, 1-based)
+      const double *a1 = d1[idir], *a2 = d2[idir];
+      const double den = a1[cf - (1 - sd) + q3[idir]] * a2[cf];
+      if (idir == 0)
+        for (int k = 1; k <= nf[2]; k++)
+          for (int j = 1; j <= nf[1]; j++)
+            rhs[0][(j - 1) + (size_t)nf[1] * ((k - 1) + (size_t)nf[2] * sd)] = scale(factor[0][sd] * W(cf, j, k) / den, 0, sd);
+      else if (idir == 1)
+        for (int k = 1; k <= nf[2]; k++)
+          for (int i = 1; i <= nf[0]; i++)
+            rhs[1][(i - 1) + (size_t)nf[0] * ((k - 1) + (size_t)nf[2] * sd)] = scale(factor[1][sd] * W(i, cf, k) / den, 1, sd);
+      else
+        for (int j = 1; j <= nf[1]; j++)
+          for (int i = 1; i <= nf[0]; i++)
+            rhs[2][(i - 1) + (size_t)nf[0] * ((j - 1) + (size_t)nf[1] * sd)] = scale(factor[2][sd] * W(i, j, cf) / den, 2, sd);
+    }
+  }
+}
+
+// Build the box problem of a field: the pressure (centred in every direction, alpha = 0), or for
+// IMPDIFF a velocity component (staggered along its own direction, one unknown fewer at a wall there,
+// main.f90:771-826) or a scalar (centred), with the field's own boundary conditions.
+int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
   const snac_case &c = d.c;
+  S.field = field;
+  S.helm = field != HF_P;
+  if (S.helm && c.fft_axis) {
+    set_error("IMPDIFF Helmholtz solves are implemented for the 3-D solve (FFT_AXIS 0) only");
+    return SNAC_ERR_UNSUPPORTED;
+  }
   S.precision = d.opt.precision;
   if (const char *e = getenv("SNAC_MG_INNER")) S.inner_iters = std::max(1, atoi(e));
   if (const char *e = getenv("SNAC_MG_INNER_TOL")) S.inner_tol = atof(e);
@@ -198,10 +275,10 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
   int lo_min[3], hi_max[3];
   for (int p = 0; p < 3; p++) {
     lo_min[p] = d.hb[0].lo[p];
-    hi_max[p] = d.hb[0].hi[p];
+    hi_max[p] = field_hi(d.hb[0], field, p);
     for (int b = 1; b < d.nblocks; b++) {
       lo_min[p] = std::min(lo_min[p], d.hb[b].lo[p]);
-      hi_max[p] = std::max(hi_max[p], d.hb[b].hi[p]);
+      hi_max[p] = std::max(hi_max[p], field_hi(d.hb[b], field, p));
     }
     S.lo_min[p] = lo_min[p];
   }
@@ -244,7 +321,8 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
   }
   B.alloc_level(L0);
   const double alpha = 0.0;
-  const int centered[3] = {1, 1, 1};
+  int centered[3];
+  for (int p = 0; p < 3; p++) centered[p] = field_centered(field, p);
   std::vector<double> cmv_all[3];
   for (int a = 0; a < 3; a++) cmv_all[a].assign(L0.ncell, 0.0);
   std::vector<char> have[3];
@@ -259,11 +337,12 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
       q3[p] = centered[p] ? 0 : 1;
     }
     auto LOC = [&](int p, int g) { return g - H.lo[p] + 1; };
-    int loc[3], hic[3];
+    int loc[3], hic[3], bhi[3];
+    for (int p = 0; p < 3; p++) bhi[p] = field_hi(H, field, p);
     for (int a = 0; a < 3; a++) {
       const int p = S.ax[a];
       loc[a] = a < na ? H.lo[p] : 0;
-      hic[a] = a < na ? H.hi[p] : 0;
+      hic[a] = a < na ? bhi[p] : 0;
     }
     for (int g2 = loc[2]; g2 <= hic[2]; g2++)
       for (int g1 = loc[1]; g1 <= hic[1]; g1++)
@@ -310,13 +389,13 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
             const int p = S.ax[a];
             if (d.periods[p] != 0) continue;
             if (H.is_bound[p][0] && gg[a] == H.lo[p]) {
-              const int t = fold_type(H.desc.cbcpre[p][0], centered[p]);
+              const int t = fold_type(field_cbc(H, field, p, 0), centered[p]);
               cc = cc + fold_sgn(t) * cmv[a];
               cmv[a] = 0.0;
               code |= (unsigned short)(t << (2 * (2 * a)));
             }
-            if (H.is_bound[p][1] && gg[a] == H.hi[p]) {
-              const int t = fold_type(H.desc.cbcpre[p][1], centered[p]);
+            if (H.is_bound[p][1] && gg[a] == bhi[p]) {
+              const int t = fold_type(field_cbc(H, field, p, 1), centered[p]);
               cc = cc + fold_sgn(t) * cpv[a];
               cpv[a] = 0.0;
               code |= (unsigned short)(t << (2 * (2 * a + 1)));
@@ -360,14 +439,14 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
   }
   S.nact0 = nact;
   std::vector<int> singular(S.nsys);
-  for (int s = 0; s < S.nsys; s++) singular[s] = (!has_dir && alpha == 0.0 && S.lambda[s] == 0.0) ? 1 : 0;
+  for (int s = 0; s < S.nsys; s++) singular[s] = (!S.helm && !has_dir && alpha == 0.0 && S.lambda[s] == 0.0) ? 1 : 0;
   // hierarchy
   std::vector<std::array<int, 3>> boff(d.nblocks), bext(d.nblocks);
   for (int b = 0; b < d.nblocks; b++)
     for (int a = 0; a < 3; a++) {
       const int p = S.ax[a];
       boff[b][a] = a < na ? d.hb[b].lo[p] - lo_min[p] : 0;
-      bext[b][a] = a < na ? d.hb[b].hi[p] - d.hb[b].lo[p] + 1 : 1;
+      bext[b][a] = a < na ? field_hi(d.hb[b], field, p) - d.hb[b].lo[p] + 1 : 1;
     }
   while ((int)B.L.size() < MG_MAXLEV) {
     const HLevel &F = B.L.back();
@@ -422,7 +501,9 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
     B.L.push_back(std::move(C));
   }
   HLevel &Lc = B.L.back();
-  if (Lc.ncell <= MG_DENSE_MAX) {
+  // Helmholtz problems: the dense inverse would depend on the shift; their coarsest level is
+  // diagonally dominant and is smoothed instead
+  if (Lc.ncell <= MG_DENSE_MAX && !S.helm) {
     Lc.dinv.assign((size_t)Lc.ncell * Lc.ncell * S.nsys, 0.0);
     for (int s = 0; s < S.nsys; s++)
       if (!B.dense(Lc, s, singular[s] != 0, Lc.dinv.data() + (size_t)Lc.ncell * Lc.ncell * s)) {
@@ -470,10 +551,13 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
       D.W[a] = (const double *)up(h.W[a].data(), h.W[a].size() * sizeof(double));
       D.Wf[a] = upf(h.W[a]);
     }
-    if (!S.mode3d) {
+    {  // weight of the per-system diagonal shift: area W0 W1 (plane mode), volume W0 W1 W2 (3-D mode)
       std::vector<double> w01(h.ncell);
-      for (int j = 0; j < h.n[1]; j++)
-        for (int i = 0; i < h.n[0]; i++) w01[i + (size_t)h.n[0] * j] = h.W[0][i] * h.W[1][j];
+      for (int k = 0; k < h.n[2]; k++)
+        for (int j = 0; j < h.n[1]; j++)
+          for (int i = 0; i < h.n[0]; i++)
+            w01[i + (size_t)h.n[0] * (j + (size_t)h.n[1] * k)] =
+                S.mode3d ? h.W[0][i] * h.W[1][j] * h.W[2][k] : h.W[0][i] * h.W[1][j];
       D.w01 = (const double *)up(w01.data(), w01.size() * sizeof(double));
       D.w01f = upf(w01);
     }
@@ -557,6 +641,16 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload) {
       return SNAC_ERR_NOMEM;
     }
   }
+  if (S.helm) {
+    std::vector<std::vector<double>> planes[3];
+    for (int a = 0; a < 3; a++) planes[a].resize(d.nblocks);
+    for (int b = 0; b < d.nblocks; b++) {
+      std::vector<double> r[3];
+      init_bc_rhs_field(d.hb[b], field, d.periods, r);
+      for (int a = 0; a < 3; a++) planes[a][b] = std::move(r[a]);
+    }
+    SNAC_TRY(helm_upload_tables(d, S, planes));
+  }
   return SNAC_OK;
 }
 
@@ -616,6 +710,25 @@ static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *
   *iters_out = outer;
   *res_out = worst;
   return (outer >= S.maxiter && worst > S.tol) ? SNAC_ERR_NOT_CONVERGED : SNAC_OK;
+}
+
+// solve_impdiff_field_3d (solve_helmholtz.f90:109-138): right-hand side alphai V phi + BC planes, the
+// shift alphai on the diagonal, the solve warm-started from the previous solution, the field overwritten
+int solver_solve_helmholtz(Domain &d, PoissonSolver &S, double alphai) {
+  cudaStream_t st = d.st;
+  if (!S.helm) { set_error("not a Helmholtz solver"); return SNAC_ERR_STATE; }
+  SNAC_TRY(helm_rhs(d, S, alphai, st));
+  SNAC_TRY(helm_io(d, S, S.box_b, 1, st));
+  int it = 0;
+  double res = 0.0;
+  const int rc = solve_box(S, st, &it, &res);
+  if (rc != SNAC_OK && rc != SNAC_ERR_NOT_CONVERGED) return rc;
+  SNAC_TRY(helm_io(d, S, S.box_x, 0, st));
+  S.last_iters = it;
+  S.last_res = res;
+  if (rc == SNAC_ERR_NOT_CONVERGED)
+    set_error("Helmholtz solve stopped at maxiter=%d with relative residual %.3e > tol %.3e", S.maxiter, res, S.tol);
+  return rc;
 }
 
 // main.f90:1004-1022: transform (or gather), solve every system warm-started from po, back-transform + normfft

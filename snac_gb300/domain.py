@@ -114,7 +114,8 @@ class Domain:
         s = capi.StepStats()
         check(capi.lib().snac_get_stats(C.byref(s)))
         return dict(istep=s.istep, time=s.time, dt=s.dt, iters=s.solve_iters_max, residual=s.solve_residual_max,
-                    solves=s.solves, device_ms=s.device_ms)
+                    solves=s.solves, device_ms=s.device_ms, helm_iters=s.helm_iters_max,
+                    helm_residual=s.helm_residual_max)
 
     @property
     def dt(self):

@@ -266,6 +266,46 @@ def test_steps_dhc_scalar_buoyancy(snac_lib, oracle_mod):
         d.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_steps_dhc_impdiff(snac_lib, oracle_mod, precision):
+    """IMPDIFF on the stretched heated cavity: the Helmholtz solves of u, v, w (staggered along their own
+    axis, hif = hi - 1 at a wall) and of the scalar, with the 3-D pressure solve."""
+    case = cases.heated_cavity(n=(16, 16, 8), stretch=1.2, ra=1e5, impdiff=1, tol=1e-12, dt_f=2e-3)
+    O = oracle_mod.OracleDomain(case)
+    d = Domain(case, precision=precision)
+    try:
+        s0 = cases.dhc_initial_scalar(case, lambda ib: O.grid(ib, 0, oracle_mod.G_XC))
+        rng = np.random.default_rng(11)
+        O.field(0, capi.S0)[...] = s0[0] + 1e-2 * rng.standard_normal(s0[0].shape)
+        d.set(0, capi.S0, O.field(0, capi.S0))
+        for X in (O, d):
+            X.bounduvw(False)
+            X.boundp(capi.P)
+            X.boundp(capi.S0)
+        O.step(5)
+        d.step(5)
+        st = d.stats()
+        assert 0 < st["helm_iters"] and st["helm_residual"] <= case.tol
+        compare_fields(case, O, d, (capi.U, capi.V, capi.W, capi.S0), 1e-9)
+        compare_fields(case, O, d, (capi.P,), 1e-8, mean_free_p=True)
+        assert np.max(np.abs(d.get(0, capi.V))) > 1e-8
+    finally:
+        d.close()
+
+
+def test_steps_lshape_impdiff(snac_lib, oracle_mod):
+    """IMPDIFF across block interfaces: the L-shaped box of three blocks, where a velocity component's
+    Helmholtz box runs through the friend faces (hif = hi there) and stops short of the walls."""
+    import dataclasses
+    case = dataclasses.replace(cases.l_shaped_box(n=16, nz=8), impdiff=1, dt_f=1e-3)
+    O, d = _run_both(case, oracle_mod, 3, amp=0.2)
+    try:
+        compare_fields(case, O, d, (capi.U, capi.V, capi.W), 1e-9)
+        compare_fields(case, O, d, (capi.P,), 1e-8, mean_free_p=True)
+    finally:
+        d.close()
+
+
 def test_steps_channel_forced_scalar(snac_lib, oracle_mod):
     """Four uneven blocks with a bulk-forced scalar: the bulk mean of rk_scal is taken over all blocks and
     the scalar's ghost planes come through the friend links."""

@@ -106,3 +106,28 @@ def test_oracle_solver_exact_on_manufactured(oracle_mod):
     O.lib().or_correc_all(d.h, 0.1)
     d.bounduvw(True)
     assert d.chkdiv()[1] < 1e-9
+
+
+def test_oracle_impdiff_matches_explicit_small_dt(oracle_mod):
+    """IMPDIFF (Crank-Nicolson diffusion through the Helmholtz solves) and explicit RK3 diffusion are two
+    discretisations of the same equations: at a small dt their solutions differ at second order in dt.
+    Checks the BC planes, the staggered extents hif and the shift of the oracle's Helmholtz problems."""
+    from snac_gb300 import capi
+    out = {}
+    for imp in (0, 1):
+        case = cases.heated_cavity(n=(12, 12, 8), stretch=1.2, ra=1e5, impdiff=imp, tol=1e-13, dt_f=1e-5)
+        O = oracle_mod.OracleDomain(case)
+        try:
+            s0 = cases.dhc_initial_scalar(case, lambda ib: O.grid(ib, 0, oracle_mod.G_XC))
+            O.field(0, capi.S0)[...] = s0[0]
+            O.bounduvw(False)
+            O.boundp(capi.P)
+            O.boundp(capi.S0)
+            O.step(10)
+            out[imp] = {k: O.field(0, k)[1:-1, 1:-1, 1:-1].copy() for k in (capi.U, capi.W, capi.S0)}
+        finally:
+            O.close()
+    for k in out[0]:
+        a, b = out[0][k], out[1][k]
+        assert np.max(np.abs(a)) > 0
+        assert np.max(np.abs(a - b)) <= 1e-6 * np.max(np.abs(a)), k
