@@ -81,6 +81,8 @@ typedef struct snac_block_desc {
   char   cbcscal[SNAC_MAX_SCAL][3][2];
   double bcscal[SNAC_MAX_SCAL][3][2];
   const double *grid_file[3];  /* optional grid/grid_?_b_###.bin: rf,rc,drf,drc over lo..hi (4*ng) */
+  int    inflow_type[3][2];    /* block_inflow_type (param.f90:84): 0 none, 1 Poiseuille, 2 Kovasznay; active on a
+                                  physical boundary whose normal velocity component is 'D' (main.f90:596) */
 } snac_block_desc;
 
 /* &dns, &scalar and &hypre namelists (param.f90:342-355) plus the build flags */
@@ -224,7 +226,10 @@ double snac_vol_all(void);
 /* the per-stage routines of main.f90:906-1043 on every block */
 int snac_rk_mom_all(int irk);                     /* rk_mom for all blocks with the current dt */
 int snac_bounduvw_all(int is_correc);             /* bound.f90:8-66 */
-int snac_boundp_all(int field);                   /* bound.f90:68-106 (SNAC_P, SNAC_PP, scalars) */
+int snac_boundp_all(int field);
+/* inflow (bound.f90:438-477) on every block's inflow faces: the normal component set on the boundary face
+ * (skipped when is_correc), the tangential ones mirrored about the face value */
+int snac_inflow_all(int is_correc);                   /* bound.f90:68-106 (SNAC_P, SNAC_PP, scalars) */
 int snac_fillps_all(double dtrk);                 /* fillps.f90 */
 int snac_updt_rhs_all(void);                      /* bound.f90:543-585 with the pressure BC planes */
 int snac_solve_pressure(void);                    /* fft + solve_n_helmholtz_2d + fft + normfft, or solve_helmholtz */

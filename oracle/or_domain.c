@@ -289,6 +289,49 @@ or_domain *or_create(const or_case *c, const or_block_desc *blocks, char *err, i
     d->box_b = calloc(nbox, sizeof(double));
     d->box_x = calloc(nbox, sizeof(double));
   }
+  /* inflow BCs (main.f90:592-632 with init_inflow, initflow.f90:369-429); chk_inflow (sanity.f90:173-189) */
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    for (int a = 0; a < 3; a++)
+      for (int s = 0; s < 2; s++) {
+        const int type = blocks[ib].inflow_type[a][s];
+        if (type < 0 || type > 2) { snprintf(err, errlen, "block %d: inflow_type must be 0, 1 or 2", ib + 1); goto fail; }
+        if (type > 0 && d->periods[a] != 0) {
+          snprintf(err, errlen, "block %d: periodicity and inflow BCs cannot be combined", ib + 1);
+          goto fail;
+        }
+        B->inflow[a][s] = B->is_bound[a][s] && type > 0 && blocks[ib].cbcvel[a][a][s] == 'D';
+        if (!B->inflow[a][s]) continue;
+        const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+        const int n1 = B->ng[t1] + 2, n2 = B->ng[t2] + 2;
+        for (int comp = 0; comp < 3; comp++) B->vin[a][s][comp] = calloc((size_t)n1 * n2, sizeof(double));
+        double *veln = B->vin[a][s][a], *velt2 = B->vin[a][s][t2];
+        const double uref = blocks[ib].bcvel[a][a][s], lref = 1.0, visc = 1.0 / c->visci;
+        const double *x1c = B->g[t1][OR_G_XC], *x2c = B->g[t2][OR_G_XC], *x2f = B->g[t2][OR_G_XF];
+        const double pi = acos(-1.0);
+        if (type == 1) {
+          const int q1 = d->periods[t1] == 0, q2 = d->periods[t2] == 0;
+          const double l10 = blocks[ib].lmin[t1], l11 = blocks[ib].lmax[t1];
+          const double l20 = blocks[ib].lmin[t2], l21 = blocks[ib].lmax[t2];
+          for (int i2 = 0; i2 < n2; i2++)
+            for (int i1 = 0; i1 < n1; i1++) {
+              /* poiseuille_square (initflow.f90:353-367) raised to q = 0 (periodic) or 1 */
+              const double r1 = (x1c[i1] - l10) / (l11 - l10), r2 = (x2c[i2] - l20) / (l21 - l20);
+              const double p1 = q1 ? 6.0 * (r1 * (1.0 - r1)) : 1.0, p2 = q2 ? 6.0 * (r2 * (1.0 - r2)) : 1.0;
+              veln[i1 + (size_t)n1 * i2] = uref * p1 * p2;
+            }
+        } else {
+          const double reb = uref * lref / visc;
+          const double lambda = reb / 2.0 - sqrt(reb * reb / 4.0 + 4.0 * (pi * pi));
+          const double x0 = -0.5;
+          for (int i2 = 0; i2 < n2; i2++)
+            for (int i1 = 0; i1 < n1; i1++) {
+              veln[i1 + (size_t)n1 * i2] = 1.0 - exp(lambda * x0) * cos(2.0 * pi * x2c[i2]);
+              velt2[i1 + (size_t)n1 * i2] = lambda / (2.0 * pi) * exp(lambda * x0) * sin(2.0 * pi * x2f[i2]);
+            }
+        }
+      }
+  }
   /* IMPDIFF (main.f90:771-839): BC planes and a Helmholtz problem for u, v, w and every scalar */
   if (c->impdiff) {
     if (c->fft_axis) { snprintf(err, errlen, "IMPDIFF with an FFT axis is not restated in the oracle"); goto fail; }
@@ -319,14 +362,21 @@ or_domain *or_create(const or_case *c, const or_block_desc *blocks, char *err, i
         B->rhsh[hf][2] = calloc((size_t)nf[0] * nf[1] * 2, sizeof(double));
         const double *d1[3], *d2[3];
         for (int a = 0; a < 3; a++) { d1[a] = cen[a] ? B->g[a][0] : B->g[a][1]; d2[a] = cen[a] ? B->g[a][1] : B->g[a][0]; }
-        /* the velocity components pass bcu%x.. (main.f90:580-582: bcvel over each plane, no inflow) */
+        /* the velocity components pass bcu%x.. (main.f90:580-582, 605-625): bcvel over each plane, or
+           the interior of the inflow plane on an inflow face */
         double *bcp[3] = {NULL, NULL, NULL};
         if (hf < OR_HF_S0) {
-          const size_t np[3] = {(size_t)nf[1] * nf[2], (size_t)nf[0] * nf[2], (size_t)nf[0] * nf[1]};
           for (int a = 0; a < 3; a++) {
-            bcp[a] = malloc(np[a] * 2 * sizeof(double));
+            const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+            const int m1 = nf[t1], m2 = nf[t2];
+            const size_t np = (size_t)m1 * m2;
+            bcp[a] = malloc(np * 2 * sizeof(double));
             for (int sd = 0; sd < 2; sd++)
-              for (size_t q = 0; q < np[a]; q++) bcp[a][q + np[a] * sd] = bv[a][sd];
+              for (int i2 = 0; i2 < m2; i2++)
+                for (int i1 = 0; i1 < m1; i1++)
+                  bcp[a][i1 + (size_t)m1 * i2 + np * sd] =
+                      B->inflow[a][sd] ? B->vin[a][sd][hf - OR_HF_U][(i1 + 1) + (size_t)(B->ng[t1] + 2) * (i2 + 1)]
+                                       : bv[a][sd];
           }
         }
         or_init_bc_rhs((const char(*)[2])cb, (const double(*)[2])bv, (const double(*)[2])dl, (const int(*)[2])B->is_bound,
@@ -358,6 +408,7 @@ void or_destroy(or_domain *d) {
     for (int f = 0; f < OR_NFIELDS; f++) free(B->fld[f]);
     for (int a = 0; a < 3; a++) free(B->rhsp[a]);
     for (int hf = 0; hf < 3 + OR_MAX_SCAL; hf++) for (int a = 0; a < 3; a++) free(B->rhsh[hf][a]);
+    for (int a = 0; a < 3; a++) for (int s = 0; s < 2; s++) for (int q = 0; q < 3; q++) free(B->vin[a][s][q]);
   }
   free(d->b);
   free(d->lambda);
@@ -422,6 +473,41 @@ void or_bounduvw(or_domain *d, int is_correc) {
           double drv = s ? dr[B->ng[a]] : dr[0];
           or_set_bc(B->desc.cbcvel[comp][a][s], s, B->lo, B->hi, a + 1, centered, B->desc.bcvel[comp][a][s], drv,
                     B->fld[OR_U + comp]);
+        }
+      }
+  }
+}
+
+/* bound.f90:438-477 on every block, faces x0, x1, y0, y1, z0, z1; local indices 1..n, halo 0 and n+1 */
+void or_inflow(or_domain *d, int is_correc) {
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    const int nx = B->ng[0], ny = B->ng[1];
+    for (int a = 0; a < 3; a++)
+      for (int s = 0; s < 2; s++) {
+        if (!B->inflow[a][s]) continue;
+        const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+        const int n1 = B->ng[t1] + 2, n2 = B->ng[t2] + 2;
+        const int qn = s ? B->ng[a] : 0, qt = s ? B->ng[a] + 1 : 0, dq = s ? -1 : 1;
+        for (int comp = 0; comp < 3; comp++) {
+          if (comp == a && is_correc) continue;
+          double *f = B->fld[OR_U + comp];
+          const double *in = B->vin[a][s][comp];
+          for (int i2 = 0; i2 < n2; i2++)
+            for (int i1 = 0; i1 < n1; i1++) {
+              int c[3];
+              c[t1] = i1; c[t2] = i2;
+              const double vin = in[i1 + (size_t)n1 * i2];
+#define FI(p) f[(p)[0] + (size_t)(nx + 2) * ((p)[1] + (size_t)(ny + 2) * (p)[2])]
+              if (comp == a) { c[a] = qn; FI(c) = vin; }
+              else {
+                c[a] = qt + dq;
+                const double inner = FI(c);
+                c[a] = qt;
+                FI(c) = -inner + 2.0 * vin;
+              }
+#undef FI
+            }
         }
       }
   }
@@ -678,12 +764,14 @@ int or_step(or_domain *d, int nsteps) {
       if (d->c.impdiff) /* main.f90:947-995: the three Helmholtz solves of u, v, w with alphai = 1/alpha */
         for (int comp = 0; comp < 3; comp++) rc |= helm_solve(d, OR_HF_U + comp, OR_U + comp, 1.0 / alpha);
       or_bounduvw(d, 0);
+      or_inflow(d, 0);
       or_fillps_all(d, dtrk);
       or_updt_rhs_all(d);
       rc |= or_solve_pressure(d);
       or_boundp(d, OR_PP);
       or_correc_all(d, dtrk);
       or_bounduvw(d, 1);
+      or_inflow(d, 1);
       or_updt_pressure_all(d, alpha);
       or_boundp(d, OR_P);
     }

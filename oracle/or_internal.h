@@ -14,6 +14,8 @@ typedef struct or_block {
   double *fld[OR_NFIELDS];
   double *rhsp[3];            /* init_bc_rhs planes for the pressure (rhsp%x/y/z) */
   double *rhsh[3 + OR_MAX_SCAL][3]; /* IMPDIFF: init_bc_rhs planes of u, v, w and the scalars (rhsu%x, ...) */
+  int inflow[3][2];           /* is_bound_inflow (main.f90:596) */
+  double *vin[3][2][3];       /* u_in%x.. per axis, side, component over (lo-1:hi+1)^2 of the in-plane axes */
 } or_block;
 
 /* one multigrid level of a box problem */

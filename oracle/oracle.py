@@ -35,7 +35,7 @@ class BlockDesc(C.Structure):
                 ("gr", C.c_double * 3), ("cbcvel", ((C.c_char * 2) * 3) * 3), ("bcvel", ((C.c_double * 2) * 3) * 3),
                 ("cbcpre", (C.c_char * 2) * 3), ("bcpre", (C.c_double * 2) * 3),
                 ("cbcscal", ((C.c_char * 2) * 3) * MAX_SCAL), ("bcscal", ((C.c_double * 2) * 3) * MAX_SCAL),
-                ("grid_file", C.POINTER(C.c_double) * 3)]
+                ("grid_file", C.POINTER(C.c_double) * 3), ("inflow_type", (C.c_int * 2) * 3)]
 
 
 class CaseDesc(C.Structure):
@@ -67,7 +67,7 @@ def lib():
         L.or_block_geometry.argtypes = [C.c_void_p, C.c_int, ip, ip, ip, ip]
         L.or_vol_all.restype = C.c_double
         L.or_vol_all.argtypes = [C.c_void_p]
-        for n in ("or_bounduvw", "or_boundp"):
+        for n in ("or_bounduvw", "or_boundp", "or_inflow"):
             getattr(L, n).argtypes = [C.c_void_p, C.c_int]
         L.or_fillps_all.argtypes = [C.c_void_p, C.c_double]
         L.or_updt_rhs_all.argtypes = [C.c_void_p]
@@ -138,6 +138,8 @@ def fill_descs(case, block_cls=BlockDesc, case_cls=CaseDesc):
                     else:
                         d.cbcscal[sc][a][s] = b"N"
                         d.bcscal[sc][a][s] = 0.0
+            for s in range(2):
+                d.inflow_type[a][s] = int(b.inflow_type[a][s])
             gf = b.grid_file[a]
             if gf is not None:
                 g = np.ascontiguousarray(gf, dtype=np.float64)
@@ -220,6 +222,9 @@ class OracleDomain:
 
     def bounduvw(self, is_correc=False):
         lib().or_bounduvw(self.h, int(is_correc))
+
+    def inflow(self, is_correc=False):
+        lib().or_inflow(self.h, int(is_correc))
 
     def boundp(self, kind=P):
         lib().or_boundp(self.h, kind)

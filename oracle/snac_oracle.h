@@ -48,6 +48,7 @@ typedef struct or_block_desc {
   char   cbcscal[OR_MAX_SCAL][3][2];
   double bcscal[OR_MAX_SCAL][3][2];
   const double *grid_file[3];      /* optional grid/grid_?_b_###.bin contents: rf,rc,drf,drc (4*ng) */
+  int    inflow_type[3][2];        /* block_inflow_type(0:1,1:3,ib): 0 none, 1 Poiseuille, 2 Kovasznay */
 } or_block_desc;
 
 /* global input, mirrors &dns/&scalar/&hypre (param.f90:342-355) + build flags */
@@ -136,6 +137,7 @@ double *or_grid(or_domain *d, int ib, int axis, int which); /* (n+2) entries, lo
 double  or_vol_all(const or_domain *d);
 void   or_bounduvw(or_domain *d, int is_correc);
 void   or_boundp(or_domain *d, int kind);
+void   or_inflow(or_domain *d, int is_correc);              /* bound.f90:438-477 on every inflow face */
 void   or_fillps_all(or_domain *d, double dtrk);
 void   or_updt_rhs_all(or_domain *d);
 int    or_solve_pressure(or_domain *d);                   /* pp <- solution, po updated */

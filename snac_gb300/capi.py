@@ -34,7 +34,7 @@ class BlockDesc(C.Structure):
                 ("gr", C.c_double * 3), ("cbcvel", ((C.c_char * 2) * 3) * 3), ("bcvel", ((C.c_double * 2) * 3) * 3),
                 ("cbcpre", (C.c_char * 2) * 3), ("bcpre", (C.c_double * 2) * 3),
                 ("cbcscal", ((C.c_char * 2) * 3) * MAX_SCAL), ("bcscal", ((C.c_double * 2) * 3) * MAX_SCAL),
-                ("grid_file", C.POINTER(C.c_double) * 3)]
+                ("grid_file", C.POINTER(C.c_double) * 3), ("inflow_type", (C.c_int * 2) * 3)]
 
 
 class CaseDesc(C.Structure):
@@ -101,6 +101,7 @@ PROTOTYPES = {
     "snac_rk_mom_all": (C.c_int, [C.c_int]),
     "snac_bounduvw_all": (C.c_int, [C.c_int]),
     "snac_boundp_all": (C.c_int, [C.c_int]),
+    "snac_inflow_all": (C.c_int, [C.c_int]),
     "snac_fillps_all": (C.c_int, [C.c_double]),
     "snac_updt_rhs_all": (C.c_int, []),
     "snac_solve_pressure": (C.c_int, []),
@@ -190,6 +191,8 @@ def fill_descs(case):
                     else:
                         d.cbcscal[sc][a][s] = b"N"
                         d.bcscal[sc][a][s] = 0.0
+            for s in range(2):
+                d.inflow_type[a][s] = int(b.inflow_type[a][s])
             gf = b.grid_file[a]
             if gf is not None:
                 g = np.ascontiguousarray(gf, dtype=np.float64)

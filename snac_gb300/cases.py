@@ -54,6 +54,8 @@ class Block:
     bcscal: Optional[List[List[List[float]]]] = None
     # optional axis grid files grid/grid_?_b_###.bin: rf, rc, drf, drc over lo..hi (4*ng doubles)
     grid_file: List[Optional[np.ndarray]] = dataclasses.field(default_factory=lambda: [None, None, None])
+    # block_inflow_type(0:1,1:3): 0 none, 1 Poiseuille, 2 Kovasznay (param.f90:84)
+    inflow_type: List[List[int]] = dataclasses.field(default_factory=lambda: [[0, 0], [0, 0], [0, 0]])
 
     @property
     def ncell(self) -> int:
@@ -267,6 +269,31 @@ def dhc_initial_scalar(case: Case, xc_of_block):
         prof = (1.0 - xx) * t0 + xx * t1
         out[ib] = np.broadcast_to(prof[:, None, None], (b.ng[0] + 2, b.ng[1] + 2, b.ng[2] + 2)).copy()
     return out
+
+
+def developing_duct(n=(32, 16, 16), inflow_type: int = 1, impdiff: int = 0, fft_axis: int = 0,
+                    tol: float = 1e-12, dt_f: float = -1.0) -> Case:
+    """The layout of examples/developing_duct: a square duct [0,1] x [0,1.5] x [0,1] with walls in y and z,
+    an inflow on x- (inflow_type 1: the Poiseuille square-duct profile of init_inflow scaled to u = 1),
+    zero-gradient velocity and p = 0 on x+, visci = 1000."""
+    b = Block(ng=tuple(n), lmin=(0.0, 0.0, 0.0), lmax=(1.0, 1.5, 1.0),
+              cbcvel=[bc6("DNDDDD"), bc6("NNDDDD"), bc6("NNDDDD")],
+              bcvel=[val6([1, 0, 0, 0, 0, 0]), val6([0] * 6), val6([0] * 6)],
+              cbcpre=bc6("NDNNNN"), bcpre=val6([0] * 6), inflow_type=[[inflow_type, 0], [0, 0], [0, 0]])
+    return Case(name=f"duct{n[0]}x{n[1]}x{n[2]}", blocks=[b], visci=1000.0, cfl=0.95, dtmax=1e5, dt_f=dt_f,
+                fft_axis=fft_axis, impdiff=impdiff, tol=tol)
+
+
+def kovasznay(n=(40, 2, 16), visci: float = 40.0, impdiff: int = 0, tol: float = 1e-12, dt_f: float = -1.0) -> Case:
+    """The layout of examples/__MULTI_BLOCK_GEOMETRY/kovasznay_flow: [-0.5,4.5] x [0,1/32] x [-0.5,0.5],
+    periodic in y and z (self-friend faces), the Kovasznay inflow (inflow_type 2) on x-, zero-gradient
+    velocity and p = 0 on x+; Re = visci (here 40, the classical case)."""
+    b = Block(ng=tuple(n), lmin=(-0.5, 0.0, -0.5), lmax=(4.5, 0.03125, 0.5),
+              cbcvel=[bc6("DNFFFF")] * 3,
+              bcvel=[val6([1, 0, 1, 1, 1, 1]), val6([0, 0, 1, 1, 1, 1]), val6([0, 0, 1, 1, 1, 1])],
+              cbcpre=bc6("NDFFFF"), bcpre=val6([0, 0, 1, 1, 1, 1]), inflow_type=[[2, 0], [0, 0], [0, 0]])
+    return Case(name=f"kovasznay{n[0]}x{n[1]}x{n[2]}", blocks=[b], visci=visci, cfl=0.95, dtmax=1e5, dt_f=dt_f,
+                fft_axis=0, impdiff=impdiff, tol=tol)
 
 
 def l_shaped_box(n: int = 144, nz: int = 96, tol: float = 1e-12) -> Case:

@@ -190,6 +190,69 @@ static void init_bc_rhs_p(const HostBlock &H, const int periods[3], int fft_axis
   }
 }
 
+// init_inflow (initflow.f90:369-429) on one face: the normal component veln and the tangential ones of the
+// two in-plane axes (velt1, velt2) over (lo-1:hi+1)^2, from the block's own centre/face coordinates
+static void init_inflow_face(int type, const int per[2], const int n[2], const double lmin[2], const double lmax[2],
+                             const double *x1c, const double *x2c, const double *x2f, double uref, double lref,
+                             double visc, std::vector<double> &veln, std::vector<double> &velt1,
+                             std::vector<double> &velt2) {
+  const int n1 = n[0] + 2, n2 = n[1] + 2;
+  veln.assign((size_t)n1 * n2, 0.0);
+  velt1.assign((size_t)n1 * n2, 0.0);
+  velt2.assign((size_t)n1 * n2, 0.0);
+  // poiseuille_square (initflow.f90:353-367): 6 rr (1 - rr) on [lmin, lmax]
+  auto pois = [](double r, double l0, double l1) {
+    const double rr = (r - l0) / (l1 - l0);
+    return 6.0 * (rr * (1.0 - rr));
+  };
+  const double pi = std::acos(-1.0);
+  if (type == 1) {  // the profile does not vary along a periodic axis (an integer power 0)
+    for (int i2 = 0; i2 < n2; i2++)
+      for (int i1 = 0; i1 < n1; i1++) {
+        const double f1 = per[0] == 0 ? pois(x1c[i1], lmin[0], lmax[0]) : 1.0;
+        const double f2 = per[1] == 0 ? pois(x2c[i2], lmin[1], lmax[1]) : 1.0;
+        veln[i1 + (size_t)n1 * i2] = uref * f1 * f2;
+      }
+  } else if (type == 2) {  // Kovasznay flow at x0 = -0.5
+    const double reb = uref * lref / visc;
+    const double lambda = reb / 2.0 - std::sqrt(reb * reb / 4.0 + 4.0 * (pi * pi));
+    const double x0 = -0.5;
+    for (int i2 = 0; i2 < n2; i2++)
+      for (int i1 = 0; i1 < n1; i1++) {
+        veln[i1 + (size_t)n1 * i2] = 1.0 - std::exp(lambda * x0) * std::cos(2.0 * pi * x2c[i2]);
+        velt2[i1 + (size_t)n1 * i2] = lambda / (2.0 * pi) * std::exp(lambda * x0) * std::sin(2.0 * pi * x2f[i2]);
+      }
+  }
+}
+
+// inflow set-up of main.f90:592-632: a face is an inflow face when it is a physical boundary, its
+// inflow_type is positive and the normal velocity component is 'D'; periodic axes reject an inflow
+// (chk_inflow, sanity.f90:173-189)
+static int init_inflow_planes(Domain &d, const snac_block_desc *blocks) {
+  for (int b = 0; b < d.nblocks; b++) {
+    HostBlock &H = d.hb[b];
+    for (int a = 0; a < 3; a++)
+      for (int s = 0; s < 2; s++) {
+        const int type = blocks[b].inflow_type[a][s];
+        if (type < 0 || type > 2) { set_error("block %d: inflow_type must be 0, 1 or 2", b + 1); return SNAC_ERR_ARG; }
+        if (type > 0 && d.periods[a] != 0) {
+          set_error("block %d: periodicity and inflow BCs cannot be combined", b + 1);
+          return SNAC_ERR_ARG;
+        }
+        H.inflow[a][s] = H.is_bound[a][s] && type > 0 && blocks[b].cbcvel[a][a][s] == 'D';
+        if (!H.inflow[a][s]) continue;
+        const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+        const int per[2] = {d.periods[t1], d.periods[t2]}, n[2] = {H.ng[t1], H.ng[t2]};
+        const double lmin[2] = {blocks[b].lmin[t1], blocks[b].lmin[t2]};
+        const double lmax[2] = {blocks[b].lmax[t1], blocks[b].lmax[t2]};
+        init_inflow_face(type, per, n, lmin, lmax, H.g[t1][2].data(), H.g[t2][2].data(), H.g[t2][3].data(),
+                         blocks[b].bcvel[a][a][s], 1.0, 1.0 / d.c.visci, H.vin[a][s][a], H.vin[a][s][t1],
+                         H.vin[a][s][t2]);
+      }
+  }
+  return SNAC_OK;
+}
+
 static int build_domain(Domain &d, const snac_case *c, const snac_block_desc *blocks) {
   d.c = *c;
   d.nblocks = c->nblocks;
@@ -304,6 +367,7 @@ static int build_domain(Domain &d, const snac_case *c, const snac_block_desc *bl
     d.vol_all += (blocks[b].lmax[0] - blocks[b].lmin[0]) * (blocks[b].lmax[1] - blocks[b].lmin[1]) *
                  (blocks[b].lmax[2] - blocks[b].lmin[2]);
   for (int b = 0; b < d.nblocks; b++) init_bc_rhs_p(d.hb[b], d.periods, c->fft_axis, d.hb[b].rhsp);
+  SNAC_TRY(init_inflow_planes(d, blocks));
   return SNAC_OK;
 }
 
@@ -372,6 +436,31 @@ static int upload_domain(Domain &d) {
     d.d_links[a] = (FaceLink *)d.alloc(std::max<size_t>(1, fl.size()) * sizeof(FaceLink));
     if (!fl.empty()) SNAC_CUDA(cudaMemcpy(d.d_links[a], fl.data(), fl.size() * sizeof(FaceLink), cudaMemcpyHostToDevice));
   }
+  // inflow faces per axis and side
+  for (int a = 0; a < 3; a++)
+    for (int s = 0; s < 2; s++) {
+      std::vector<InflowFace> fc;
+      const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+      for (int b = 0; b < d.nblocks; b++) {
+        HostBlock &H = d.hb[b];
+        if (!H.inflow[a][s]) continue;
+        InflowFace F{b, 0, {nullptr, nullptr, nullptr}};
+        for (int comp = 0; comp < 3; comp++) {
+          const auto &v = H.vin[a][s][comp];
+          double *p = (double *)d.alloc(v.size() * sizeof(double));
+          if (!p) { set_error("device allocation failed (inflow planes)"); return SNAC_ERR_NOMEM; }
+          SNAC_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice));
+          F.pl[comp] = p;
+        }
+        fc.push_back(F);
+        d.inflow_plane[a][s] = std::max(d.inflow_plane[a][s], (H.ng[t1] + 2) * (H.ng[t2] + 2));
+      }
+      d.ninflow[a][s] = (int)fc.size();
+      if (fc.empty()) continue;
+      d.d_inflow[a][s] = (InflowFace *)d.alloc(fc.size() * sizeof(InflowFace));
+      if (!d.d_inflow[a][s]) { set_error("device allocation failed (inflow faces)"); return SNAC_ERR_NOMEM; }
+      SNAC_CUDA(cudaMemcpy(d.d_inflow[a][s], fc.data(), fc.size() * sizeof(InflowFace), cudaMemcpyHostToDevice));
+    }
   int flds[5 + SNAC_MAX_SCAL];
   for (int q = 0; q < 5 + SNAC_MAX_SCAL; q++) flds[q] = q;
   d.d_flds = (int *)d.alloc(sizeof(flds));
@@ -432,6 +521,14 @@ static int bound_uvw(Domain &d, int is_correc) {
   for (int a = 0; a < 3; a++)
     SNAC_TRY(launch_exchange(d.d_db, d.d_links[a], d.nlinks[a], d.d_flds, 3, a, d.maxplane[a], d.st));
   for (int a = 0; a < 3; a++) SNAC_TRY(launch_setbc(d.d_db, d.d_bc[is_correc ? 1 : 0][a], d.nbc[is_correc ? 1 : 0][a], a, d.maxplane[a], d.st));
+  return SNAC_OK;
+}
+
+// inflow (bound.f90:438-477) on every inflow face, x0, x1, y0, y1, z0, z1
+static int inflow_all(Domain &d, int is_correc) {
+  for (int a = 0; a < 3; a++)
+    for (int s = 0; s < 2; s++)
+      SNAC_TRY(launch_inflow(d.d_db, d.d_inflow[a][s], d.ninflow[a][s], a, s, d.inflow_plane[a][s], is_correc, d.st));
   return SNAC_OK;
 }
 
@@ -562,6 +659,7 @@ static int one_stage(Domain &d, int irk) {
   SNAC_TRY(rk_scal_all(d, irk));
   SNAC_TRY(rk_mom_all(d, irk));
   SNAC_TRY(bound_uvw(d, 0));
+  SNAC_TRY(inflow_all(d, 0));
   SNAC_TRY(launch_fillps(d.d_db, d.d_tiles, d.ntiles, dtrk, d.c.fft_axis, d.st));
   SNAC_TRY(updt_rhs_all(d));
   int rc = solver_solve_pressure(d, *d.ps);
@@ -572,6 +670,7 @@ static int one_stage(Domain &d, int irk) {
   SNAC_TRY(bound_p(d, SNAC_PP));
   SNAC_TRY(launch_correc(d.d_db, d.d_tiles_halo, d.ntiles_halo, dtrk, d.st));
   SNAC_TRY(bound_uvw(d, 1));
+  SNAC_TRY(inflow_all(d, 1));
   SNAC_TRY(launch_updt_pressure(d.d_db, d.d_tiles, d.ntiles, alpha, d.c.impdiff, d.st));
   SNAC_TRY(bound_p(d, SNAC_P));
   return rc;
@@ -734,6 +833,12 @@ int snac_rk_mom_all(int irk) {
 int snac_bounduvw_all(int is_correc) {
   NEED_DOMAIN
   SNAC_TRY(bound_uvw(*d, is_correc));
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  return SNAC_OK;
+}
+int snac_inflow_all(int is_correc) {
+  NEED_DOMAIN
+  SNAC_TRY(inflow_all(*d, is_correc));
   SNAC_CUDA(cudaStreamSynchronize(d->st));
   return SNAC_OK;
 }

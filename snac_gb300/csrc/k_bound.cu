@@ -98,6 +98,48 @@ int launch_setbc(const DBlock *dB, const BcEntry *dE, int nent, int a, int maxpl
   return SNAC_OK;
 }
 
+// inflow (bound.f90:438-477), one face of every listed block: the normal component on the boundary face
+// (qn = lo-1 | hi) unless is_correc, the tangential ones at qt = lo-1 | hi+1 mirrored about the inflow value
+// (-f(qt+dq) + 2 f_in), over the whole halo'd plane.  The faces of one block run in the reference's order
+// (x0, x1, y0, y1, z0, z1), one launch each, so edge ghosts end up as in the reference.
+__global__ void k_inflow(const DBlock *__restrict__ dB, const InflowFace *__restrict__ dI, int a, int side,
+                         int is_correc) {
+  const InflowFace F = dI[blockIdx.y];
+  const DBlock &B = dB[F.b];
+  const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+  const int n1 = B.n[t1] + 2, n2 = B.n[t2] + 2;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n1 * n2) return;
+  int c[3];
+  c[t1] = q % n1 - 1;
+  c[t2] = q / n1 - 1;
+  const int na = B.n[a];
+  const int qn = side ? na - 1 : -1, qt = side ? na : -1, dq = side ? -1 : 1;
+  double *f[3] = {B.u, B.v, B.w};
+  for (int comp = 0; comp < 3; comp++) {
+    const double vin = F.pl[comp][q];
+    if (comp == a) {
+      if (is_correc) continue;
+      c[a] = qn;
+      f[comp][hidx(c[0], c[1], c[2], B.n[0], B.n[1])] = vin;
+    } else {
+      c[a] = qt + dq;
+      const double inner = f[comp][hidx(c[0], c[1], c[2], B.n[0], B.n[1])];
+      c[a] = qt;
+      f[comp][hidx(c[0], c[1], c[2], B.n[0], B.n[1])] = -inner + 2.0 * vin;
+    }
+  }
+}
+
+int launch_inflow(const DBlock *dB, const InflowFace *dI, int nface, int a, int side, int maxplane, int is_correc,
+                  cudaStream_t st) {
+  if (nface <= 0) return SNAC_OK;
+  dim3 g((maxplane + 255) / 256, nface);
+  k_inflow<<<g, 256, 0, st>>>(dB, dI, a, side, is_correc), ::snac::count_launch();
+  SNAC_CUDA(cudaGetLastError());
+  return SNAC_OK;
+}
+
 // set_bc parameters of one face, bound.f90:121-133
 void bc_mode(char ctype, int ibound, int centered, double rvalue, double dr, int *mode, double *factor, double *sgn) {
   *mode = BC_NONE;

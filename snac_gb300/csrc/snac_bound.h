@@ -19,9 +19,18 @@ struct BcEntry {
   double factor[2], sgn[2];
 };
 
+// one inflow face of one block (bound.f90:438-477): the planes u_in, v_in, w_in over (lo-1:hi+1) of the
+// two tangential axes (the lower one fastest)
+struct InflowFace {
+  int b, pad;
+  const double *pl[3];
+};
+
 void bc_mode(char ctype, int ibound, int centered, double rvalue, double dr, int *mode, double *factor, double *sgn);
 int launch_exchange(const DBlock *dB, const FaceLink *dF, int nlinks, const int *dflds, int nflds, int a,
                     int maxplane, cudaStream_t st);
 int launch_setbc(const DBlock *dB, const BcEntry *dE, int nent, int a, int maxplane, cudaStream_t st);
+int launch_inflow(const DBlock *dB, const InflowFace *dI, int nface, int a, int side, int maxplane, int is_correc,
+                  cudaStream_t st);
 
 }  // namespace snac

@@ -48,6 +48,8 @@ struct HostBlock {
   std::vector<double> g[3][4];   // per axis: dc, df, c, f over lo-1..hi+1
   std::vector<double> rhsp[3];   // pressure BC planes
   std::vector<double> dl[3];     // dl(0:1,idir) of main.f90:725-727
+  int inflow[3][2] = {};         // is_bound_inflow (main.f90:596)
+  std::vector<double> vin[3][2][3];  // inflow planes u_in%x.. per axis, side, component over the halo'd plane
 };
 
 // the field a solver is built for: the pressure, or (IMPDIFF Helmholtz problems) velocity component c
@@ -109,6 +111,8 @@ struct Domain {
   Tile *d_tiles = nullptr, *d_tiles_halo = nullptr;
   int ntiles = 0, ntiles_halo = 0;
   FaceLink *d_links[3] = {nullptr, nullptr, nullptr};
+  InflowFace *d_inflow[3][2] = {};   // inflow faces per axis and side, blocks in order
+  int ninflow[3][2] = {}, inflow_plane[3][2] = {};
   int nlinks[3] = {0, 0, 0}, maxplane[3] = {0, 0, 0};
   // boundary-condition tables: [kind][axis]; kinds 0 bounduvw, 1 bounduvw(is_correc), 2 p, 3 pp, 4+s scalar s
   BcEntry *d_bc[4 + SNAC_MAX_SCAL][3] = {};

@@ -192,8 +192,9 @@ double field_bc(const HostBlock &H, int field, int p, int side) {
 // init_bc_rhs (solver.f90:44-157) of a field in 3-D mode over lo..hif, with the field's centring,
 // spacings and boundary values; dl is dxc at lo-1 and hi along a centred axis, dxf at lo and hi along a
 // staggered one (main.f90:725-727, 771-773).  Planes rhs?(.., .., 0:1) over the solved extents.  The
-// velocity components pass the boundary-value planes bcu%x.. (main.f90:580-582, uniform bcvel without an
-// inflow), which scale a plane by bcval/bc where bc is nonzero (solver.f90:122-123); the scalars do not.
+// velocity components pass the boundary-value planes bcu%x.. (main.f90:580-582: uniform bcvel, or the
+// inflow planes on an inflow face), which scale a plane by bcval/bc where bc is nonzero (solver.f90:122-123);
+// the scalars do not.
 static void init_bc_rhs_field(const HostBlock &H, int field, const int periods[3], std::vector<double> rhs[3]) {
   int nf[3], cen[3], q3[3];
   const double *d1[3], *d2[3];
@@ -219,9 +220,17 @@ static void init_bc_rhs_field(const HostBlock &H, int field, const int periods[3
   rhs[2].assign((size_t)nf[0] * nf[1] * 2, 0.0);
   auto W = [&](int i, int j, int k) { return d2[0][i] * d2[1][j] * d2[2][k]; };  // local 1-based indices
   const bool has_bcval = field >= HF_U && field < HF_S0;
-  auto scale = [&](double r, int a, int sd) {
+  // bcval at local (1-based) in-plane indices p1, p2: the inflow plane on an inflow face (main.f90:605-625),
+  // else the uniform bc
+  auto scale = [&](double r, int a, int sd, int p1, int p2) {
     const double bc = field_bc(H, field, a, sd);
-    return (has_bcval && bc != 0.0) ? r * bc / bc : r;
+    if (!has_bcval || bc == 0.0) return r;
+    double bv = bc;
+    if (H.inflow[a][sd]) {
+      const int t1 = a == 0 ? 1 : 0;
+      bv = H.vin[a][sd][field - HF_U][p1 + (size_t)(H.ng[t1] + 2) * p2];
+    }
+    return r * bv / bc;
   };
   for (int idir = 0; idir < 3; idir++) {
     if (periods[idir] != 0) continue;
@@ -234,15 +243,15 @@ static void init_bc_rhs_field(const HostBlock &H, int field, const int periods[3
       if (idir == 0)
         for (int k = 1; k <= nf[2]; k++)
           for (int j = 1; j <= nf[1]; j++)
-            rhs[0][(j - 1) + (size_t)nf[1] * ((k - 1) + (size_t)nf[2] * sd)] = scale(factor[0][sd] * W(cf, j, k) / den, 0, sd);
+            rhs[0][(j - 1) + (size_t)nf[1] * ((k - 1) + (size_t)nf[2] * sd)] = scale(factor[0][sd] * W(cf, j, k) / den, 0, sd, j, k);
       else if (idir == 1)
         for (int k = 1; k <= nf[2]; k++)
           for (int i = 1; i <= nf[0]; i++)
-            rhs[1][(i - 1) + (size_t)nf[0] * ((k - 1) + (size_t)nf[2] * sd)] = scale(factor[1][sd] * W(i, cf, k) / den, 1, sd);
+            rhs[1][(i - 1) + (size_t)nf[0] * ((k - 1) + (size_t)nf[2] * sd)] = scale(factor[1][sd] * W(i, cf, k) / den, 1, sd, i, k);
       else
         for (int j = 1; j <= nf[1]; j++)
           for (int i = 1; i <= nf[0]; i++)
-            rhs[2][(i - 1) + (size_t)nf[0] * ((j - 1) + (size_t)nf[1] * sd)] = scale(factor[2][sd] * W(i, j, cf) / den, 2, sd);
+            rhs[2][(i - 1) + (size_t)nf[0] * ((j - 1) + (size_t)nf[1] * sd)] = scale(factor[2][sd] * W(i, j, cf) / den, 2, sd, i, j);
     }
   }
 }

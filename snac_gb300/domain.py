@@ -70,6 +70,9 @@ class Domain:
     def bounduvw(self, is_correc=False):
         check(capi.lib().snac_bounduvw_all(int(is_correc)))
 
+    def inflow(self, is_correc=False):
+        check(capi.lib().snac_inflow_all(int(is_correc)))
+
     def boundp(self, kind=capi.P):
         check(capi.lib().snac_boundp_all(int(kind)))
 

@@ -131,3 +131,44 @@ def test_oracle_impdiff_matches_explicit_small_dt(oracle_mod):
         a, b = out[0][k], out[1][k]
         assert np.max(np.abs(a)) > 0
         assert np.max(np.abs(a - b)) <= 1e-6 * np.max(np.abs(a)), k
+
+
+@pytest.mark.parametrize("which", ["duct", "kovasznay"])
+def test_oracle_inflow_planes(oracle_mod, which):
+    """init_inflow (initflow.f90:369-429) and inflow (bound.f90:438-477), restated in numpy: the normal
+    component on the inflow face, the tangential ones mirrored about the inflow value into the ghost."""
+    from snac_gb300 import capi
+    case = cases.developing_duct() if which == "duct" else cases.kovasznay()
+    O = oracle_mod.OracleDomain(case)
+    try:
+        rng = np.random.default_rng(4)
+        for k in (capi.U, capi.V, capi.W):
+            O.field(0, k)[...] = rng.standard_normal(O.field(0, k).shape)
+        O.bounduvw(False)
+        O.inflow(False)
+        b = case.blocks[0]
+        yc = O.grid(0, 1, oracle_mod.G_XC)
+        zc, zf = O.grid(0, 2, oracle_mod.G_XC), O.grid(0, 2, oracle_mod.G_XF)
+        if which == "duct":
+            def pois(r, l0, l1):
+                rr = (r - l0) / (l1 - l0)
+                return 6.0 * (rr * (1.0 - rr))
+            un = (1.0 * pois(yc, b.lmin[1], b.lmax[1]))[:, None] * pois(zc, b.lmin[2], b.lmax[2])[None, :]
+            vt = np.zeros_like(un)
+            wt = np.zeros_like(un)
+        else:
+            reb = 1.0 * 1.0 / (1.0 / case.visci)
+            lam = reb / 2 - np.sqrt(reb * reb / 4 + 4 * (np.pi * np.pi))
+            un = np.broadcast_to(1.0 - np.exp(lam * -0.5) * np.cos(2 * np.pi * zc)[None, :], (len(yc), len(zc)))
+            vt = np.zeros_like(un)
+            wt = np.broadcast_to(lam / (2 * np.pi) * np.exp(lam * -0.5) * np.sin(2 * np.pi * zf)[None, :], un.shape)
+        u, v, w = (O.field(0, k) for k in (capi.U, capi.V, capi.W))
+        np.testing.assert_allclose(u[0], un, rtol=1e-14, atol=1e-14)
+        np.testing.assert_allclose(v[0], -v[1] + 2.0 * vt, rtol=1e-14, atol=1e-14)
+        np.testing.assert_allclose(w[0], -w[1] + 2.0 * wt, rtol=1e-14, atol=1e-14)
+        # is_correc leaves the normal component alone
+        u[0] = 7.0
+        O.inflow(True)
+        assert np.all(u[0] == 7.0)
+    finally:
+        O.close()
