@@ -15,8 +15,9 @@
 //   launch never reads the array it writes: the pre-smoother writes xp and the
 //   post-smoother reads xp + correction and writes x.
 // k_vcycle_coarse: one CTA of 1024 threads per system runs the V-cycle from
-//   level l0 down to the coarsest solve and back, with x, b, the diagonal and
-//   the couplings of every level in shared memory.
+//   level l0 down to the coarsest solve and back, with x, b and 1/d of every
+//   level in shared memory, and the couplings too where they fit (the top
+//   level's may stay in global memory, shared by all systems and held in L2).
 // Both follow the arithmetic of k_rbgs / k_resid_restrict / k_prolong / k_dense
 // term by term, so fused and unfused V-cycles give identical results.
 #include <algorithm>
@@ -250,62 +251,118 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
 }
 
 // ---------------------------------------------------------------- whole coarse V-cycle in one CTA
-// one half-sweep of a level held in shared memory (inactive cells have d = 0)
+constexpr int COARSE_THREADS = 1024;
+
+// where the coarse V-cycle kernel keeps each level: x, b and 1/d in shared memory; the couplings too when
+// they fit (else they are read from global memory, where every system shares them and L2 holds them)
+struct CoarseLev {
+  int ox, ob, oi;  // shared-memory offsets (elements) of x, b, 1/d
+  int oc;          // couplings c0 | c1 at oc, oc + ncell; -1: global memory
+  int hdj, hdi;    // walker steps over the half rows of a colour: COARSE_THREADS / h0, % h0 (h0 = (n0+1)/2)
+  int fdj, fdi;    // walker steps over full rows: COARSE_THREADS / n0, % n0
+};
+struct CoarsePlan {
+  CoarseLev lev[MG_MAXLEV];
+};
+
+// the layout for levels l0.. : x, b and 1/d of every level (the dense coarsest level only x and b) in
+// shared memory, then the couplings of as many levels as still fit, the finest (most used) first; false
+// when even x, b and 1/d do not fit
 template <typename T>
-__device__ __forceinline__ void cta_sweep_xy(int n0, int n1, int per0, int per1, T *x, const T *b, const T *d,
-                                             const T *c0, const T *c1, int color) {
-  const int h0 = (n0 + 1) >> 1, half = h0 * n1;
-  for (int q = threadIdx.x; q < half; q += blockDim.x) {
-    const int j = q / h0, i = 2 * (q - j * h0) + ((color + j) & 1);
-    if (i >= n0) continue;
-    const int c = i + n0 * j;
-    const T dv = d[c];
-    if (dv == T(0)) continue;
-    const T acc = offdiag_xy<T>(n0, n1, per0, per1, c0, c1, [&](int e) { return x[e]; }, c, i, j);
-    x[c] = (b[c] - acc) * rcpt(dv);
+static bool coarse_plan(const MgProblem &P, int l0, CoarsePlan *plan, size_t *bytes) {
+  const int last = P.nlev - 1;
+  const bool dense = LA<T>::dinv(P.L[last]) != nullptr;
+  size_t o = 0;
+  CoarsePlan pl{};
+  for (int l = l0; l < P.nlev; l++) {
+    const MgLevelD &L = P.L[l];
+    const int n = (int)L.ncell, n0 = L.n[0], h0 = (n0 + 1) / 2;
+    CoarseLev &e = pl.lev[l];
+    e.hdj = COARSE_THREADS / h0;
+    e.hdi = COARSE_THREADS % h0;
+    e.fdj = COARSE_THREADS / n0;
+    e.fdi = COARSE_THREADS % n0;
+    e.ox = (int)o;
+    e.ob = (int)o + n;
+    o += 2 * (size_t)n;
+    e.oi = e.oc = -1;
+    if (l == last && dense) continue;
+    e.oi = (int)o;
+    o += n;
+  }
+  if (o * sizeof(T) > MG_COARSE_SMEM_MAX) return false;
+  for (int l = l0; l < P.nlev; l++) {
+    if (l == last && dense) break;
+    const size_t need = 2 * (size_t)P.L[l].ncell;
+    if ((o + need) * sizeof(T) > MG_COARSE_SMEM_MAX) continue;
+    pl.lev[l].oc = (int)o;
+    o += need;
+  }
+  if (plan) *plan = pl;
+  if (bytes) *bytes = o * sizeof(T);
+  return true;
+}
+
+// one half-sweep of a level held in shared memory (inactive cells have 1/d = 0); the walker visits the
+// cells of one colour without a division per cell
+template <typename T>
+__device__ __forceinline__ void cta_sweep_xy(int n0, int n1, int per0, int per1, T *x, const T *b, const T *id,
+                                             const T *c0, const T *c1, int color, int hdj, int hdi) {
+  const int h0 = (n0 + 1) >> 1;
+  int j = (int)threadIdx.x / h0, ih = (int)threadIdx.x - j * h0;
+  while (j < n1) {
+    const int i = 2 * ih + ((color + j) & 1);
+    if (i < n0) {
+      const int c = i + n0 * j;
+      const T iv = id[c];
+      if (iv != T(0)) {
+        const T acc = offdiag_xy<T>(n0, n1, per0, per1, c0, c1, [&](int e) { return x[e]; }, c, i, j);
+        x[c] = (b[c] - acc) * iv;
+      }
+    }
+    ih += hdi;
+    j += hdj;
+    if (ih >= h0) { ih -= h0; j++; }
   }
   __syncthreads();
 }
 
 template <typename T>
-__global__ void __launch_bounds__(1024, 1) k_vcycle_coarse(MgProblem P, int l0, const T *__restrict__ shift,
-                                                           const int *__restrict__ active, T *__restrict__ xout,
-                                                           const T *__restrict__ bin) {
+__global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P, CoarsePlan plan, int l0,
+                                                                     const T *__restrict__ shift,
+                                                                     const int *__restrict__ active,
+                                                                     T *__restrict__ xout, const T *__restrict__ bin) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int s = blockIdx.x;
   if (active && !active[s]) return;
   const int last = P.nlev - 1;
   const bool dense = LA<T>::dinv(P.L[last]) != nullptr;
   const int per0 = P.periodic[0], per1 = P.periodic[1];
-  // level l occupies [x | b | d | c0 | c1] (the dense coarsest level only [x | b]) from offset lo[l]
-  __shared__ int lo[MG_MAXLEV];
-  if (threadIdx.x == 0) {
-    int o = 0;
-    for (int l = l0; l < P.nlev; l++) {
-      lo[l] = o;
-      o += ((l == last && dense) ? 2 : 5) * (int)P.L[l].ncell;
-    }
-  }
-  __syncthreads();
   T *const base = (T *)smem_raw;
-  auto X = [&](int l) { return base + lo[l]; };
-  auto B = [&](int l) { return base + lo[l] + (int)P.L[l].ncell; };
-  auto D = [&](int l) { return base + lo[l] + 2 * (int)P.L[l].ncell; };
-  auto C0 = [&](int l) { return base + lo[l] + 3 * (int)P.L[l].ncell; };
-  auto C1 = [&](int l) { return base + lo[l] + 4 * (int)P.L[l].ncell; };
+  auto X = [&](int l) { return base + plan.lev[l].ox; };
+  auto B = [&](int l) { return base + plan.lev[l].ob; };
+  auto ID = [&](int l) { return base + plan.lev[l].oi; };
+  auto C0 = [&](int l) -> const T * { return plan.lev[l].oc >= 0 ? base + plan.lev[l].oc : LA<T>::cp(P.L[l], 0); };
+  auto C1 = [&](int l) -> const T * {
+    return plan.lev[l].oc >= 0 ? base + plan.lev[l].oc + (int)P.L[l].ncell : LA<T>::cp(P.L[l], 1);
+  };
   const T sh = shift[s];
   for (int l = l0; l < P.nlev; l++) {
     if (l == last && dense) break;
     const MgLevelD &L = P.L[l];
     const int n = (int)L.ncell;
-    const T *__restrict__ cc = LA<T>::cc(L);
-    const T *__restrict__ w01 = LA<T>::w01(L);
+    const T *__restrict__ invd = LA<T>::invd(L) + (long)n * s;
     const T *__restrict__ cp0 = LA<T>::cp(L, 0);
     const T *__restrict__ cp1 = LA<T>::cp(L, 1);
+    T *id = ID(l);
+    const bool cs = plan.lev[l].oc >= 0;
+    T *c0 = base + plan.lev[l].oc, *c1 = c0 + n;
     for (int c = threadIdx.x; c < n; c += blockDim.x) {
-      D(l)[c] = (L.code[c] & 0x8000) ? T(0) : fmat(sh, w01[c], cc[c]);
-      C0(l)[c] = cp0[c];
-      C1(l)[c] = cp1[c];
+      id[c] = invd[c];
+      if (cs) {
+        c0[c] = cp0[c];
+        c1[c] = cp1[c];
+      }
     }
   }
   {
@@ -320,26 +377,33 @@ __global__ void __launch_bounds__(1024, 1) k_vcycle_coarse(MgProblem P, int l0, 
   for (int l = l0; l < last; l++) {
     const MgLevelD &L = P.L[l];
     const MgLevelD &C = P.L[l + 1];
+    const CoarseLev &E = plan.lev[l], &EC = plan.lev[l + 1];
     const int n0 = L.n[0], n1 = L.n[1];
     T *x = X(l);
-    const T *b = B(l), *d = D(l), *c0 = C0(l), *c1 = C1(l);
-    for (int it = 0; it < 2 * P.nu; it++) cta_sweep_xy<T>(n0, n1, per0, per1, x, b, d, c0, c1, it & 1);
-    const int cn0 = C.n[0], nc = (int)C.ncell;
+    const T *b = B(l), *id = ID(l), *c0 = C0(l), *c1 = C1(l);
+    const T *__restrict__ cc = LA<T>::cc(L);
+    const T *__restrict__ w01 = LA<T>::w01(L);
+    for (int it = 0; it < 2 * P.nu; it++) cta_sweep_xy<T>(n0, n1, per0, per1, x, b, id, c0, c1, it & 1, E.hdj, E.hdi);
+    const int cn0 = C.n[0], cn1 = C.n[1];
     const int e0 = C.coarsened[0] ? 2 : 1, e1 = C.coarsened[1] ? 2 : 1;
-    for (int q = threadIdx.x; q < nc; q += blockDim.x) {
-      const int J = q / cn0, I = q - J * cn0;
+    T *bc = B(l + 1), *xc = X(l + 1);
+    int J = (int)threadIdx.x / cn0, I = (int)threadIdx.x - J * cn0;
+    while (J < cn1) {
       T sum = 0;
       for (int dj = 0; dj < e1; dj++)
         for (int di = 0; di < e0; di++) {
           const int i = C.coarsened[0] ? 2 * I + di : I, j = C.coarsened[1] ? 2 * J + dj : J;
           const int c = i + n0 * j;
-          const T dv = d[c];
-          if (dv == T(0)) continue;
+          if (id[c] == T(0)) continue;
+          const T dv = fmat(sh, w01[c], cc[c]);  // the diagonal of the unfused residual, term by term
           const T acc = offdiag_xy<T>(n0, n1, per0, per1, c0, c1, [&](int e) { return x[e]; }, c, i, j);
           sum += b[c] - fmat(dv, x[c], acc);
         }
-      B(l + 1)[q] = sum;
-      X(l + 1)[q] = 0;
+      bc[I + cn0 * J] = sum;
+      xc[I + cn0 * J] = 0;
+      I += EC.fdi;
+      J += EC.fdj;
+      if (I >= cn0) { I -= cn0; J++; }
     }
     __syncthreads();
   }
@@ -356,28 +420,35 @@ __global__ void __launch_bounds__(1024, 1) k_vcycle_coarse(MgProblem P, int l0, 
       }
       __syncthreads();
     } else {
+      const CoarseLev &E = plan.lev[last];
       for (int it = 0; it < 40; it++)
         for (int col = 0; col < 4; col++)
-          cta_sweep_xy<T>(L.n[0], L.n[1], per0, per1, X(last), B(last), D(last), C0(last), C1(last),
-                          (col == 1 || col == 2) ? 1 : 0);
+          cta_sweep_xy<T>(L.n[0], L.n[1], per0, per1, X(last), B(last), ID(last), C0(last), C1(last),
+                          (col == 1 || col == 2) ? 1 : 0, E.hdj, E.hdi);
     }
   }
   // up: prolongation and post-smoothing
   for (int l = last - 1; l >= l0; l--) {
     const MgLevelD &L = P.L[l];
     const MgLevelD &C = P.L[l + 1];
-    const int n0 = L.n[0], n1 = L.n[1], n = (int)L.ncell, cn0 = C.n[0];
+    const CoarseLev &E = plan.lev[l];
+    const int n0 = L.n[0], n1 = L.n[1], cn0 = C.n[0];
     T *x = X(l);
-    const T *xc = X(l + 1), *d = D(l);
-    for (int c = threadIdx.x; c < n; c += blockDim.x) {
-      if (d[c] == T(0)) continue;
-      const int j = c / n0, i = c - j * n0;
-      const int I = C.coarsened[0] ? i / 2 : i, J = C.coarsened[1] ? j / 2 : j;
-      x[c] += xc[I + cn0 * J];
+    const T *xc = X(l + 1), *id = ID(l);
+    int j = (int)threadIdx.x / n0, i = (int)threadIdx.x - j * n0;
+    while (j < n1) {
+      const int c = i + n0 * j;
+      if (id[c] != T(0)) {
+        const int I = C.coarsened[0] ? i / 2 : i, J = C.coarsened[1] ? j / 2 : j;
+        x[c] += xc[I + cn0 * J];
+      }
+      i += E.fdi;
+      j += E.fdj;
+      if (i >= n0) { i -= n0; j++; }
     }
     __syncthreads();
     for (int it = 0; it < 2 * P.nu; it++)
-      cta_sweep_xy<T>(n0, n1, per0, per1, x, B(l), d, C0(l), C1(l), 1 - (it & 1));
+      cta_sweep_xy<T>(n0, n1, per0, per1, x, B(l), id, C0(l), C1(l), 1 - (it & 1), E.hdj, E.hdi);
   }
   const int n = (int)P.L[l0].ncell;
   for (int c = threadIdx.x; c < n; c += blockDim.x) xout[(long)n * s + c] = X(l0)[c];
@@ -444,21 +515,24 @@ int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_c
 
 template <typename T>
 size_t coarse_smem_bytes(const MgProblem &P, int l0) {
-  const int last = P.nlev - 1;
-  const bool dense = LA<T>::dinv(P.L[last]) != nullptr;
-  size_t n = 0;
-  for (int l = l0; l < P.nlev; l++) n += (size_t)((l == last && dense) ? 2 : 5) * (size_t)P.L[l].ncell;
-  return n * sizeof(T);
+  size_t bytes = 0;
+  return coarse_plan<T>(P, l0, nullptr, &bytes) ? bytes : (size_t)-1;
 }
 
 template <typename T>
 int launch_vcycle_coarse(const MgProblem &P, int l0, const T *shift, const int *active, T *x, const T *b,
                          cudaStream_t st) {
-  const size_t smem = coarse_smem_bytes<T>(P, l0);
-  if (smem > MG_COARSE_SMEM_MAX) { set_error("coarse levels exceed the shared-memory budget"); return SNAC_ERR_ARG; }
+  CoarsePlan plan;
+  size_t smem = 0;
+  if (!coarse_plan<T>(P, l0, &plan, &smem)) { set_error("coarse levels exceed the shared-memory budget"); return SNAC_ERR_ARG; }
+  for (int l = l0; l < P.nlev; l++)
+    if (!LA<T>::invd(P.L[l]) && !(l == P.nlev - 1 && LA<T>::dinv(P.L[l]))) {
+      set_error("coarse V-cycle needs the 1/diagonal tables");
+      return SNAC_ERR_STATE;
+    }
   SNAC_TRY(allow_smem((const void *)k_vcycle_coarse<T>, smem));
   prof_begin(KID_COARSE, st);
-  k_vcycle_coarse<T><<<P.nsys, 1024, smem, st>>>(P, l0, shift, active, x, b), ::snac::count_launch();
+  k_vcycle_coarse<T><<<P.nsys, COARSE_THREADS, smem, st>>>(P, plan, l0, shift, active, x, b), ::snac::count_launch();
   prof_end(KID_COARSE, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;

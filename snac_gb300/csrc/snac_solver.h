@@ -60,7 +60,7 @@ int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_c
                        const T *xin, const T *xc, double *part_bx, int part_stride, int *nchunk, cudaStream_t st);
 template <typename T>
 size_t coarse_smem_bytes(const MgProblem &P, int l0);
-constexpr size_t MG_COARSE_SMEM_MAX = 200 * 1024;
+constexpr size_t MG_COARSE_SMEM_MAX = 226 * 1024;  // dynamic shared memory of the coarse V-cycle CTA (227 KB at most)
 template <typename T>
 int launch_vcycle_coarse(const MgProblem &P, int l0, const T *shift, const int *active, T *x, const T *b,
                          cudaStream_t st);
