@@ -334,8 +334,8 @@ or_domain *or_create(const or_case *c, const or_block_desc *blocks, char *err, i
   }
   /* IMPDIFF (main.f90:771-839): BC planes and a Helmholtz problem for u, v, w and every scalar */
   if (c->impdiff) {
-    if (c->fft_axis) { snprintf(err, errlen, "IMPDIFF with an FFT axis is not restated in the oracle"); goto fail; }
     for (int hf = OR_HF_U; hf < OR_HF_S0 + c->nscal; hf++) {
+      double dl_fft = 0.0; /* dl(0, idir) of the field (main.f90:771-773, 781) */
       for (int ib = 0; ib < d->nblocks; ib++) {
         or_block *B = &d->b[ib];
         double dl[3][2];
@@ -354,6 +354,7 @@ or_domain *or_create(const or_case *c, const or_block_desc *blocks, char *err, i
           if (blocks[ib].grid_file[a]) load_grid(B->lo[a], B->hi[a], blocks[ib].grid_file[a], rf, rc, drf, drc);
           dl[a][0] = cen[a] ? drc[0] : drf[1];
           dl[a][1] = cen[a] ? drc[B->ng[a]] : drf[B->ng[a]];
+          if (c->fft_axis && a == c->fft_axis - 1 && ib == 0) dl_fft = dl[a][0];
           free(drc); free(drf); free(rc); free(rf);
         }
         const int nf[3] = {hif[0] - B->lo[0] + 1, hif[1] - B->lo[1] + 1, hif[2] - B->lo[2] + 1};
@@ -381,11 +382,39 @@ or_domain *or_create(const or_case *c, const or_block_desc *blocks, char *err, i
         }
         or_init_bc_rhs((const char(*)[2])cb, (const double(*)[2])bv, (const double(*)[2])dl, (const int(*)[2])B->is_bound,
                        cen, B->lo, hif, d->periods, d1[0], d2[0], d1[1], d2[1], d1[2], d2[2], B->rhsh[hf][0],
-                       B->rhsh[hf][1], B->rhsh[hf][2], bcp[0], bcp[1], bcp[2], 0);
+                       B->rhsh[hf][1], B->rhsh[hf][2], bcp[0], bcp[1], bcp[2], c->fft_axis);
         for (int a = 0; a < 3; a++) free(bcp[a]);
       }
-      d->ph[hf] = or_poisson_create(d, hf, 0.0, NULL, err, errlen);
-      if (!d->ph[hf]) goto fail;
+      double *lam = NULL;
+      int kf = -1, kb = -1, nfft = 0;
+      double normfft = 1.0;
+      if (c->fft_axis) {
+        /* init_fft_reduction (solver.f90:1124-1138) with the field's boundary pair and centring along
+           the transform axis; fftini drops the last point (q = 1) of a staggered non-periodic axis */
+        const int pf = c->fft_axis - 1, cen_f = or_field_centered(hf, pf);
+        const or_block *B0 = &d->b[0];
+        const char bc2[2] = {or_field_cbc(B0, hf, pf, 0), or_field_cbc(B0, hf, pf, 1)};
+        const int n_full = B0->ng[pf], q = (bc2[0] == 'F' && bc2[1] == 'F') || cen_f ? 0 : 1;
+        double norm[2];
+        or_find_fft(bc2, cen_f, &kf, &kb, norm);
+        if (kf < 0) { snprintf(err, errlen, "unsupported boundary pair along the transform direction"); goto fail; }
+        nfft = n_full - q;
+        normfft = 1.0 / (norm[0] * (n_full + norm[1] - q));
+        lam = calloc(n_full, sizeof(double));
+        if (or_eigenvalues(n_full, bc2, cen_f, lam)) {
+          free(lam);
+          snprintf(err, errlen, "no eigenvalues for this boundary pair (the reference defines none)");
+          goto fail;
+        }
+        for (int l = 0; l < n_full; l++) lam[l] = lam[l] / (dl_fft * dl_fft);
+      }
+      d->ph[hf] = or_poisson_create(d, hf, 0.0, lam, err, errlen);
+      if (!d->ph[hf]) { free(lam); goto fail; }
+      d->ph[hf]->lam = lam;
+      d->ph[hf]->kind_fwd = kf;
+      d->ph[hf]->kind_bwd = kb;
+      d->ph[hf]->nfft = nfft;
+      d->ph[hf]->normfft = normfft;
       long nbox = d->ph[hf]->L[0].ncell * d->ph[hf]->nsys;
       d->hbox_b[hf] = calloc(nbox, sizeof(double));
       d->hbox_x[hf] = calloc(nbox, sizeof(double));
@@ -546,15 +575,17 @@ void or_updt_rhs_all(or_domain *d) {
 }
 
 /* transform the interior of pp of every block along the FFT axis (fft.f90:85-94) */
-static void transform_blocks(or_domain *d, int kind) {
+/* fft(plan, arr(lo:hi,...)) on every block: every line of the interior along the transform axis, its first
+   nl points (nl = 0: all) */
+static void transform_field(or_domain *d, int fkind, int kind, int nl_in) {
   int idir = d->fft_axis - 1;
   for (int ib = 0; ib < d->nblocks; ib++) {
     or_block *B = &d->b[ib];
     int n[3] = {B->ng[0], B->ng[1], B->ng[2]};
     long st[3] = {1, n[0] + 2, (long)(n[0] + 2) * (n[1] + 2)};
-    double *f = B->fld[OR_PP];
+    double *f = B->fld[fkind];
     int t1 = idir == 0 ? 1 : 0, t2 = idir == 2 ? 1 : 2;
-    int nl = n[idir];
+    int nl = nl_in > 0 ? nl_in : n[idir];
 #pragma omp parallel
     {
       double *in = malloc(sizeof(double) * nl), *out = malloc(sizeof(double) * nl);
@@ -573,12 +604,12 @@ static void transform_blocks(or_domain *d, int kind) {
 
 /* main.f90:1004-1022: transform, per-wavenumber (or 3-D) solves warm-started from po, back-transform + normfft */
 int or_solve_pressure(or_domain *d) {
-  if (d->fft_axis) transform_blocks(d, d->kind_fwd);
+  if (d->fft_axis) transform_field(d, OR_PP, d->kind_fwd, 0);
   or_box_gather(d, d->ps, OR_PP, d->box_b);
   int rc = or_poisson_solve(d->ps, d->box_b, d->box_x);
   or_box_scatter(d, d->ps, d->box_x, OR_PP);
   if (d->fft_axis) {
-    transform_blocks(d, d->kind_bwd);
+    transform_field(d, OR_PP, d->kind_bwd, 0);
     for (int ib = 0; ib < d->nblocks; ib++) {
       or_block *B = &d->b[ib];
       int nx = B->ng[0], ny = B->ng[1];
@@ -670,6 +701,7 @@ static void set_dt_from_cfl(or_domain *d) {
  * (A + alphai V) phi = rhs warm-started from the previous solution (phio) */
 static int helm_solve(or_domain *d, int hf, int kind, double alphai) {
   or_poisson *P = d->ph[hf];
+  const int pf = d->fft_axis - 1; /* solve_impdiff_field_fft: no weight along the transform axis */
   for (int ib = 0; ib < d->nblocks; ib++) {
     or_block *B = &d->b[ib];
     int hif[3], cen[3];
@@ -686,7 +718,13 @@ static int helm_solve(or_domain *d, int hf, int kind, double alphai) {
     /* solve_helmholtz.f90:123-129 scales over lo..hi, including a wall face that the solve leaves alone */
     for (int k = 1; k <= B->ng[2]; k++)
       for (int j = 1; j <= B->ng[1]; j++)
-        for (int i = 1; i <= B->ng[0]; i++) FI(i, j, k) = FI(i, j, k) * alphai * d2[0][i] * d2[1][j] * d2[2][k];
+        for (int i = 1; i <= B->ng[0]; i++) {
+          double v = FI(i, j, k) * alphai;
+          if (pf != 0) v = v * d2[0][i];
+          if (pf != 1) v = v * d2[1][j];
+          if (pf != 2) v = v * d2[2][k];
+          FI(i, j, k) = v;
+        }
     const double *rx = B->rhsh[hf][0], *ry = B->rhsh[hf][1], *rz = B->rhsh[hf][2];
     /* bound.f90:543-585 with hi = hif, in its order x0, x1, y0, y1, z0, z1 (an edge cell takes two planes) */
     for (int sd = 0; sd < 2; sd++)
@@ -703,10 +741,28 @@ static int helm_solve(or_domain *d, int hf, int kind, double alphai) {
           for (int i = 1; i <= nf[0]; i++) FI(i, j, sd ? nf[2] : 1) += rz[(i - 1) + (size_t)nf[0] * ((j - 1) + (size_t)nf[1] * sd)];
 #undef FI
   }
-  P->shift[0] = alphai;
+  if (pf < 0) {
+    P->shift[0] = alphai;
+    or_box_gather(d, P, kind, d->hbox_b[hf]);
+    int rc = or_poisson_solve(P, d->hbox_b[hf], d->hbox_x[hf]);
+    or_box_scatter(d, P, d->hbox_x[hf], kind);
+    return rc;
+  }
+  /* transform, per-wavenumber solves of (A + (lambda_k + alphai) w) x = rhs, back-transform, normfft over
+     the whole interior (solve_helmholtz.f90:86-101) */
+  for (int s = 0; s < P->nsys; s++) P->shift[s] = P->lam[s] + alphai;
+  transform_field(d, kind, P->kind_fwd, P->nfft);
   or_box_gather(d, P, kind, d->hbox_b[hf]);
   int rc = or_poisson_solve(P, d->hbox_b[hf], d->hbox_x[hf]);
   or_box_scatter(d, P, d->hbox_x[hf], kind);
+  transform_field(d, kind, P->kind_bwd, P->nfft);
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    const int nx = B->ng[0], ny = B->ng[1];
+    for (int k = 1; k <= B->ng[2]; k++)
+      for (int j = 1; j <= ny; j++)
+        for (int i = 1; i <= nx; i++) B->fld[kind][i + (long)(nx + 2) * (j + (long)(ny + 2) * k)] *= P->normfft;
+  }
   return rc;
 }
 
@@ -742,7 +798,7 @@ static int scalar_stage(or_domain *d, int irk) {
 
 /* main.f90:893-1069 with scalars, Boussinesq buoyancy and IMPDIFF (3-D solves) */
 int or_step(or_domain *d, int nsteps) {
-  if (d->c.impdiff && d->c.fft_axis) return -10; /* IMPDIFF with an FFT axis is not restated */
+
   if (d->dt == 0.0) set_dt_from_cfl(d);          /* main.f90:660-661 */
   double visc = 1.0 / d->c.visci;
   int rc = 0;

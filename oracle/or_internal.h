@@ -51,6 +51,11 @@ typedef struct or_poisson {
   int last_iter; double last_res;
   double tol; int maxiter;
   int nu;                     /* smoothing sweeps (red+black pairs) before and after */
+  /* IMPDIFF Helmholtz problems with a transform axis (solve_impdiff_field_fft): the field's own
+     transform (fftini with its centring), nfft = n - q points, and lambda_k / dl^2 of its wavenumbers */
+  int kind_fwd, kind_bwd, nfft;
+  double normfft;
+  double *lam;
 } or_poisson;
 
 struct or_domain {

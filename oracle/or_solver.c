@@ -57,7 +57,7 @@ static void free_level(or_level *L) {
 void or_poisson_destroy(or_poisson *P) {
   if (!P) return;
   for (int l = 0; l < P->nlev; l++) free_level(&P->L[l]);
-  free(P->shift); free(P->singular); free(P->p); free(P->q); free(P->z);
+  free(P->shift); free(P->singular); free(P->p); free(P->q); free(P->z); free(P->lam);
   free(P);
 }
 
@@ -331,7 +331,7 @@ or_poisson *or_poisson_create(or_domain *d, int field, double alpha, const doubl
     int pf = P->ax[2];
     P->nsys = hi_max[pf] - lo_min[pf] + 1;
     for (int ib = 0; ib < d->nblocks; ib++)
-      if (d->b[ib].lo[pf] != lo_min[pf] || d->b[ib].hi[pf] != hi_max[pf]) {
+      if (d->b[ib].lo[pf] != lo_min[pf] || or_field_hi(&d->b[ib], field, pf) != hi_max[pf]) {
         snprintf(err, errlen, "blocks must span the whole transform direction");
         or_poisson_destroy(P); return NULL;
       }

@@ -24,9 +24,8 @@ G_DXC, G_DXF, G_XC, G_XF = range(4)
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with its Makefile (gcc only)."""
-    if force or not os.path.exists(_LIB_PATH):
-        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    """Compile the oracle with its Makefile (gcc only; make rebuilds only what changed)."""
+    subprocess.run(["make", "-s", "-C", _HERE] + (["-B"] if force else []), check=True)
     return _LIB_PATH
 
 

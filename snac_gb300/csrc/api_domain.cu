@@ -258,10 +258,6 @@ static int build_domain(Domain &d, const snac_case *c, const snac_block_desc *bl
   d.nblocks = c->nblocks;
   if (d.nblocks < 1) { set_error("nblocks must be >= 1"); return SNAC_ERR_ARG; }
   if (c->nscal < 0 || c->nscal > SNAC_MAX_SCAL) { set_error("nscal out of range"); return SNAC_ERR_ARG; }
-  if (c->impdiff && c->fft_axis) {
-    set_error("IMPDIFF with an FFT-reduced pressure solve (_FFT_X/_Y/_Z) is not built: use fft_axis = 0");
-    return SNAC_ERR_UNSUPPORTED;
-  }
   for (int q = 0; q < c->nscal; q++)
     if (!(c->alphai[q] > 0.0)) { set_error("alphai of scalar %d must be positive", q + 1); return SNAC_ERR_ARG; }
   d.hb.resize(d.nblocks);

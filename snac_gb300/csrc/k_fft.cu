@@ -108,16 +108,29 @@ struct LineGeom {
   int n, logn, use_fft, kind, lp;
   long ncell;          // box cells per system (plane mode)
   int n0;              // box extent along t1
+  int field;           // HF_P: pp; HF_U + c: u, v, w; HF_S0 + s: scalar s
 };
 
-// forward: pp interior lines of all blocks -> box[q][i1][i0]
+__device__ __forceinline__ double *line_field(const DBlock &B, int field) {
+  if (field == HF_P) return B.pp;
+  if (field == HF_U) return B.u;
+  if (field == HF_U + 1) return B.v;
+  if (field == HF_U + 2) return B.w;
+  return B.s[field - HF_S0];
+}
+
+// forward: the field's interior lines of all blocks (their first n points along the transform axis) ->
+// box[q][i1][i0]; a line outside the solved extents (a wall face of a staggered component) is transformed
+// in place, as fft() transforms the whole interior (solve_helmholtz.f90:86)
 __global__ void k_fft_fwd_box(const DBlock *__restrict__ Bs, const int2 *__restrict__ LT, const int2 *__restrict__ boff,
-                              LineGeom g, const double2 *__restrict__ tw, const double *__restrict__ mat,
-                              double *__restrict__ box) {
+                              const int2 *__restrict__ lext, LineGeom g, const double2 *__restrict__ tw,
+                              const double *__restrict__ mat, double *__restrict__ box) {
   extern __shared__ double smem[];
   const int2 lt = LT[blockIdx.x];
   const DBlock &B = Bs[lt.x];
   const int n1 = B.n[g.t1], nlines = B.n[g.t1] * B.n[g.t2];
+  const int2 ex = lext[lt.x];
+  double *__restrict__ f = line_field(B, g.field);
   double *s = smem;
   double2 *zb = (double2 *)(smem + g.lp * g.n);
   const int n = g.n;
@@ -128,7 +141,7 @@ __global__ void k_fft_fwd_box(const DBlock *__restrict__ Bs, const int2 *__restr
     if (line < nlines) {
       int c[3];
       c[g.a] = q; c[g.t1] = line % n1; c[g.t2] = line / n1;
-      v = B.pp[hidx(c[0], c[1], c[2], B.n[0], B.n[1])];
+      v = f[hidx(c[0], c[1], c[2], B.n[0], B.n[1])];
     }
     s[l * n + q] = v;
   }
@@ -138,19 +151,29 @@ __global__ void k_fft_fwd_box(const DBlock *__restrict__ Bs, const int2 *__restr
     const int l = t % g.lp, q = t / g.lp;
     const int line = lt.y + l;
     if (line >= nlines) continue;
-    const long cell = (long)(line % n1 + o.x) + (long)g.n0 * (line / n1 + o.y);
-    box[cell + g.ncell * q] = s[l * n + q];
+    const int x1 = line % n1, x2 = line / n1;
+    if (x1 < ex.x && x2 < ex.y) {
+      const long cell = (long)(x1 + o.x) + (long)g.n0 * (x2 + o.y);
+      box[cell + g.ncell * q] = s[l * n + q];
+    } else {
+      int c[3];
+      c[g.a] = q; c[g.t1] = x1; c[g.t2] = x2;
+      f[hidx(c[0], c[1], c[2], B.n[0], B.n[1])] = s[l * n + q];
+    }
   }
 }
 
-// backward: box -> pp interior lines, times normfft
+// backward: box (or, outside the solved extents, the field) -> field interior lines, times normfft; points
+// of a line beyond the transform length (a wall face along the transform axis) are scaled by normfft too
 __global__ void k_fft_bwd_box(const DBlock *__restrict__ Bs, const int2 *__restrict__ LT, const int2 *__restrict__ boff,
-                              LineGeom g, const double2 *__restrict__ tw, const double *__restrict__ mat,
-                              const double *__restrict__ box, double normfft) {
+                              const int2 *__restrict__ lext, LineGeom g, const double2 *__restrict__ tw,
+                              const double *__restrict__ mat, const double *__restrict__ box, double normfft) {
   extern __shared__ double smem[];
   const int2 lt = LT[blockIdx.x];
   const DBlock &B = Bs[lt.x];
   const int n1 = B.n[g.t1], nlines = B.n[g.t1] * B.n[g.t2];
+  const int2 ex = lext[lt.x];
+  double *__restrict__ f = line_field(B, g.field);
   double *s = smem;
   double2 *zb = (double2 *)(smem + g.lp * g.n);
   const int n = g.n;
@@ -160,19 +183,28 @@ __global__ void k_fft_bwd_box(const DBlock *__restrict__ Bs, const int2 *__restr
     const int line = lt.y + l;
     double v = 0.0;
     if (line < nlines) {
-      const long cell = (long)(line % n1 + o.x) + (long)g.n0 * (line / n1 + o.y);
-      v = box[cell + g.ncell * q];
+      const int x1 = line % n1, x2 = line / n1;
+      if (x1 < ex.x && x2 < ex.y) {
+        const long cell = (long)(x1 + o.x) + (long)g.n0 * (x2 + o.y);
+        v = box[cell + g.ncell * q];
+      } else {
+        int c[3];
+        c[g.a] = q; c[g.t1] = x1; c[g.t2] = x2;
+        v = f[hidx(c[0], c[1], c[2], B.n[0], B.n[1])];
+      }
     }
     s[l * n + q] = v;
   }
   transform_smem(g.kind, n, g.use_fft, g.logn, tw, mat, s, zb, g.lp);
-  for (int t = threadIdx.x; t < g.lp * n; t += blockDim.x) {
+  const int na = B.n[g.a];
+  for (int t = threadIdx.x; t < g.lp * na; t += blockDim.x) {
     const int l = t % g.lp, q = t / g.lp;
     const int line = lt.y + l;
     if (line >= nlines) continue;
     int c[3];
     c[g.a] = q; c[g.t1] = line % n1; c[g.t2] = line / n1;
-    B.pp[hidx(c[0], c[1], c[2], B.n[0], B.n[1])] = s[l * n + q] * normfft;
+    double *p = &f[hidx(c[0], c[1], c[2], B.n[0], B.n[1])];
+    *p = (q < n ? s[l * n + q] : *p) * normfft;
   }
 }
 
@@ -283,46 +315,39 @@ static int prep_launch(int n, FftLaunch &L, const void *fn) {
   return SNAC_OK;
 }
 
-// tables of line tiles and box offsets, cached on the solver
-struct FftTables {
-  int2 *d_lt = nullptr, *d_boff = nullptr;
-  int nlt = 0, lp = 0;
-  int4 *d_boff3 = nullptr;
-};
-static FftTables g_tabs;  // rebuilt for each solver (one domain at a time)
-static const PoissonSolver *g_tabs_owner = nullptr;
-
+// tables of line tiles, box offsets and solved line extents, built once per solver
 static int ensure_tables(Domain &d, PoissonSolver &S) {
-  if (g_tabs_owner == &S) return SNAC_OK;
+  if (S.tabs_ready) return SNAC_OK;
   const int a = S.fft_axis ? S.fft_axis - 1 : 0;
   const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
-  g_tabs.lp = lines_per_cta(S.fft_axis ? S.nfft : 1);
-  std::vector<int2> lt, bo;
+  S.lt_lp = lines_per_cta(S.fft_axis ? S.nfft : 1);
+  std::vector<int2> lt, bo, ex;
   std::vector<int4> bo3;
   for (int b = 0; b < d.nblocks; b++) {
     const HostBlock &H = d.hb[b];
     if (S.fft_axis) {
       const int nl = H.ng[t1] * H.ng[t2];
-      for (int l = 0; l < nl; l += g_tabs.lp) lt.push_back(make_int2(b, l));
+      for (int l = 0; l < nl; l += S.lt_lp) lt.push_back(make_int2(b, l));
       bo.push_back(make_int2(H.lo[t1] - S.lo_min[t1], H.lo[t2] - S.lo_min[t2]));
+      ex.push_back(make_int2(field_hi(H, S.field, t1) - H.lo[t1] + 1, field_hi(H, S.field, t2) - H.lo[t2] + 1));
     }
     bo3.push_back(make_int4(H.lo[0] - S.lo_min[0], H.lo[1] - S.lo_min[1], H.lo[2] - S.lo_min[2], 0));
   }
-  g_tabs.nlt = (int)lt.size();
+  S.nlt = (int)lt.size();
   if (!lt.empty()) {
-    g_tabs.d_lt = (int2 *)S.alloc(lt.size() * sizeof(int2));
-    g_tabs.d_boff = (int2 *)S.alloc(bo.size() * sizeof(int2));
-    SNAC_CUDA(cudaMemcpy(g_tabs.d_lt, lt.data(), lt.size() * sizeof(int2), cudaMemcpyHostToDevice));
-    SNAC_CUDA(cudaMemcpy(g_tabs.d_boff, bo.data(), bo.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    S.d_lt = (int2 *)S.alloc(lt.size() * sizeof(int2));
+    S.d_boff = (int2 *)S.alloc(bo.size() * sizeof(int2));
+    S.d_lext = (int2 *)S.alloc(ex.size() * sizeof(int2));
+    if (!S.d_lt || !S.d_boff || !S.d_lext) { set_error("device allocation failed (transform tables)"); return SNAC_ERR_NOMEM; }
+    SNAC_CUDA(cudaMemcpy(S.d_lt, lt.data(), lt.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    SNAC_CUDA(cudaMemcpy(S.d_boff, bo.data(), bo.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    SNAC_CUDA(cudaMemcpy(S.d_lext, ex.data(), ex.size() * sizeof(int2), cudaMemcpyHostToDevice));
   }
-  g_tabs.d_boff3 = (int4 *)S.alloc(bo3.size() * sizeof(int4));
-  SNAC_CUDA(cudaMemcpy(g_tabs.d_boff3, bo3.data(), bo3.size() * sizeof(int4), cudaMemcpyHostToDevice));
-  g_tabs_owner = &S;
+  S.d_boff3 = (int4 *)S.alloc(bo3.size() * sizeof(int4));
+  if (!S.d_boff3) { set_error("device allocation failed (box offsets)"); return SNAC_ERR_NOMEM; }
+  SNAC_CUDA(cudaMemcpy(S.d_boff3, bo3.data(), bo3.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  S.tabs_ready = 1;
   return SNAC_OK;
-}
-
-void forget_fft_tables(const PoissonSolver *S) {
-  if (g_tabs_owner == S) { g_tabs_owner = nullptr; g_tabs = FftTables(); }
 }
 
 static LineGeom line_geom(const PoissonSolver &S, int kind) {
@@ -334,9 +359,10 @@ static LineGeom line_geom(const PoissonSolver &S, int kind) {
   g.logn = ilog2(S.nfft);
   g.use_fft = S.use_fft;
   g.kind = kind;
-  g.lp = g_tabs.lp;
+  g.lp = S.lt_lp;
   g.ncell = S.ncell0;
   g.n0 = S.P.L[0].n[0];
+  g.field = S.field;
   return g;
 }
 
@@ -346,8 +372,8 @@ int fft_forward_to_box(Domain &d, PoissonSolver &S, cudaStream_t st) {
   FftLaunch L;
   SNAC_TRY(prep_launch(g.n, L, (const void *)k_fft_fwd_box));
   prof_begin(KID_FFT_FWD, st);
-  k_fft_fwd_box<<<g_tabs.nlt, 256, L.smem, st>>>(d.d_db, g_tabs.d_lt, g_tabs.d_boff, g, (const double2 *)S.d_tw,
-                                                 S.d_mat_fwd, S.box_b), ::snac::count_launch();
+  k_fft_fwd_box<<<S.nlt, 256, L.smem, st>>>(d.d_db, S.d_lt, S.d_boff, S.d_lext, g, (const double2 *)S.d_tw,
+                                            S.d_mat_fwd, S.box_b), ::snac::count_launch();
   prof_end(KID_FFT_FWD, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -359,8 +385,8 @@ int fft_backward_from_box(Domain &d, PoissonSolver &S, cudaStream_t st) {
   FftLaunch L;
   SNAC_TRY(prep_launch(g.n, L, (const void *)k_fft_bwd_box));
   prof_begin(KID_FFT_BWD, st);
-  k_fft_bwd_box<<<g_tabs.nlt, 256, L.smem, st>>>(d.d_db, g_tabs.d_lt, g_tabs.d_boff, g, (const double2 *)S.d_tw,
-                                                 S.d_mat_bwd, S.box_x, S.normfft), ::snac::count_launch();
+  k_fft_bwd_box<<<S.nlt, 256, L.smem, st>>>(d.d_db, S.d_lt, S.d_boff, S.d_lext, g, (const double2 *)S.d_tw,
+                                            S.d_mat_bwd, S.box_x, S.normfft), ::snac::count_launch();
   prof_end(KID_FFT_BWD, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -368,7 +394,7 @@ int fft_backward_from_box(Domain &d, PoissonSolver &S, cudaStream_t st) {
 
 int box_gather(Domain &d, PoissonSolver &S, cudaStream_t st) {
   SNAC_TRY(ensure_tables(d, S));
-  k_box_io<<<d.ntiles, dim3(TX, TY, TZ), 0, st>>>(d.d_db, d.d_tiles, g_tabs.d_boff3, S.P.L[0].n[0], S.P.L[0].n[1],
+  k_box_io<<<d.ntiles, dim3(TX, TY, TZ), 0, st>>>(d.d_db, d.d_tiles, S.d_boff3, S.P.L[0].n[0], S.P.L[0].n[1],
                                                   S.box_b, 1), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -376,7 +402,7 @@ int box_gather(Domain &d, PoissonSolver &S, cudaStream_t st) {
 
 int box_scatter(Domain &d, PoissonSolver &S, cudaStream_t st) {
   SNAC_TRY(ensure_tables(d, S));
-  k_box_io<<<d.ntiles, dim3(TX, TY, TZ), 0, st>>>(d.d_db, d.d_tiles, g_tabs.d_boff3, S.P.L[0].n[0], S.P.L[0].n[1],
+  k_box_io<<<d.ntiles, dim3(TX, TY, TZ), 0, st>>>(d.d_db, d.d_tiles, S.d_boff3, S.P.L[0].n[0], S.P.L[0].n[1],
                                                   S.box_x, 0), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;

@@ -19,6 +19,7 @@ struct HelmBlk {
   int isb[6];                  // is_bound, side fastest
   int boff[3];                 // offset of the block in the solver box
   int cen[3];                  // centred along each axis (else staggered)
+  int wskip;                   // transform axis, left out of the weight (-1: 3-D solve)
 };
 
 __device__ inline double *helm_field(const DBlock &B, int field) {
@@ -39,9 +40,9 @@ k_helm_rhs(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, const Helm
   double *__restrict__ f = helm_field(B, field);
   const long c = hidx(i, j, k, B.n[0], B.n[1]);
   double v = f[c] * alphai;
-  v = v * AX(B, 0, H.cen[0] ? AX_DF : AX_DC, i);
-  v = v * AX(B, 1, H.cen[1] ? AX_DF : AX_DC, j);
-  v = v * AX(B, 2, H.cen[2] ? AX_DF : AX_DC, k);
+  if (H.wskip != 0) v = v * AX(B, 0, H.cen[0] ? AX_DF : AX_DC, i);
+  if (H.wskip != 1) v = v * AX(B, 1, H.cen[1] ? AX_DF : AX_DC, j);
+  if (H.wskip != 2) v = v * AX(B, 2, H.cen[2] ? AX_DF : AX_DC, k);
   const int n0 = H.nf[0], n1 = H.nf[1], n2 = H.nf[2];
   if (i >= n0 || j >= n1 || k >= n2) { f[c] = v; return; }  // the planes only over lo..hif
   if (H.isb[0] && i == 0) v += H.rx[j + (long)n1 * (k + (long)n2 * 0)];
@@ -69,9 +70,13 @@ k_helm_io(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, const HelmB
   else f[c] = box[cell];
 }
 
-__global__ void k_set_shift(double *shift, float *shiftf, double v) {
-  shift[0] = v;
-  shiftf[0] = (float)v;
+// shift of every system: alphai (3-D) or lambda_k + alphai (per wavenumber)
+__global__ void k_set_shift(double *shift, float *shiftf, const double *lambda, int nsys, double alphai) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nsys) return;
+  const double v = lambda ? lambda[k] + alphai : alphai;
+  shift[k] = v;
+  shiftf[k] = (float)v;
 }
 
 int helm_upload_tables(Domain &d, PoissonSolver &S, const std::vector<std::vector<double>> (&planes)[3]) {
@@ -83,6 +88,7 @@ int helm_upload_tables(Domain &d, PoissonSolver &S, const std::vector<std::vecto
       e.nf[a] = field_hi(H, S.field, a) - H.lo[a] + 1;
       e.boff[a] = H.lo[a] - S.lo_min[a];
       e.cen[a] = field_centered(S.field, a);
+      e.wskip = S.fft_axis ? S.fft_axis - 1 : -1;
       for (int s = 0; s < 2; s++) e.isb[2 * a + s] = H.is_bound[a][s];
     }
     const double **dst[3] = {&e.rx, &e.ry, &e.rz};
@@ -102,8 +108,18 @@ int helm_upload_tables(Domain &d, PoissonSolver &S, const std::vector<std::vecto
 
 int helm_rhs(Domain &d, PoissonSolver &S, double alphai, cudaStream_t st) {
   k_helm_rhs<<<d.ntiles, dim3(TX, TY, TZ), 0, st>>>(d.d_db, d.d_tiles, S.d_hb, S.field, alphai), ::snac::count_launch();
-  k_set_shift<<<1, 1, 0, st>>>(const_cast<double *>(S.P.shift), const_cast<float *>(S.P.shiftf), alphai), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
+  return SNAC_OK;
+}
+
+// the diagonal shift of this solve (add_weighted_constant_to_diagonal / _n_diagonals): the 1/diagonal
+// tables of the plane smoothers follow it
+int helm_shift(PoissonSolver &S, double alphai, cudaStream_t st) {
+  const int ns = S.nsys;
+  k_set_shift<<<(ns + 127) / 128, 128, 0, st>>>(const_cast<double *>(S.P.shift), const_cast<float *>(S.P.shiftf),
+                                                S.fft_axis ? S.d_lambda : nullptr, ns, alphai), ::snac::count_launch();
+  SNAC_CUDA(cudaGetLastError());
+  if (!S.mode3d) SNAC_TRY(plane_make_invd(S.P, S.invd_tab, S.invd_tabf, st));
   return SNAC_OK;
 }
 

@@ -76,6 +76,16 @@ struct PoissonSolver {
   int use_fft = 0;                   // 1: radix-2 FFT path for R2HC/HC2R; 0: dense r2r matrices
   double *d_tw = nullptr;            // FFT twiddles exp(-2 pi i k/n), k < n/2 (complex)
   double *d_mat_fwd = nullptr, *d_mat_bwd = nullptr;  // dense r2r matrices (n x n)
+  // transform line tiles (k_fft.cu), built once per solver: (block, first line) per CTA, box offsets of the
+  // blocks, per block the solved extents along the two other axes (lines outside them are transformed in
+  // place but not solved) and, 3-D mode, the box offsets
+  int2 *d_lt = nullptr, *d_boff = nullptr;
+  int2 *d_lext = nullptr;
+  int4 *d_boff3 = nullptr;
+  int nlt = 0, lt_lp = 0, tabs_ready = 0;
+  double *invd_tab[MG_MAXLEV] = {};  // plane mode: 1/diagonal tables (remade when a Helmholtz shift changes)
+  float *invd_tabf[MG_MAXLEV] = {};
+  double *d_lambda = nullptr;        // Helmholtz with a transform: lambda_k / dl^2 (the shift is lambda_k + alphai)
   std::vector<double> lambda;
   int precision = 0;
   int inner_iters = 5;               // mixed path: FP32 Krylov iterations per refinement step
@@ -144,6 +154,7 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload = true, int field = H
 int solver_solve_helmholtz(Domain &d, PoissonSolver &S, double alphai);
 int helm_upload_tables(Domain &d, PoissonSolver &S, const std::vector<std::vector<double>> (&planes)[3]);
 int helm_rhs(Domain &d, PoissonSolver &S, double alphai, cudaStream_t st);
+int helm_shift(PoissonSolver &S, double alphai, cudaStream_t st);
 int helm_io(Domain &d, PoissonSolver &S, double *box, int to_box, cudaStream_t st);
 int solver_solve_pressure(Domain &d, PoissonSolver &S);
 

@@ -19,7 +19,6 @@
 namespace snac {
 
 int fft_setup(PoissonSolver &S);
-void forget_fft_tables(const PoissonSolver *S);
 
 void *PoissonSolver::alloc(size_t bytes) {
   void *p = nullptr;
@@ -29,7 +28,6 @@ void *PoissonSolver::alloc(size_t bytes) {
   return p;
 }
 PoissonSolver::~PoissonSolver() {
-  forget_fft_tables(this);
   for (void *p : allocs) cudaFree(p);
   if (W64.h_count) cudaFreeHost(W64.h_count);
   if (W32.h_count) cudaFreeHost(W32.h_count);
@@ -195,7 +193,8 @@ double field_bc(const HostBlock &H, int field, int p, int side) {
 // velocity components pass the boundary-value planes bcu%x.. (main.f90:580-582: uniform bcvel, or the
 // inflow planes on an inflow face), which scale a plane by bcval/bc where bc is nonzero (solver.f90:122-123);
 // the scalars do not.
-static void init_bc_rhs_field(const HostBlock &H, int field, const int periods[3], std::vector<double> rhs[3]) {
+static void init_bc_rhs_field(const HostBlock &H, int field, const int periods[3], int fft_axis,
+                              std::vector<double> rhs[3]) {
   int nf[3], cen[3], q3[3];
   const double *d1[3], *d2[3];
   double factor[3][2];
@@ -218,7 +217,13 @@ static void init_bc_rhs_field(const HostBlock &H, int field, const int periods[3
   rhs[0].assign((size_t)nf[1] * nf[2] * 2, 0.0);
   rhs[1].assign((size_t)nf[0] * nf[2] * 2, 0.0);
   rhs[2].assign((size_t)nf[0] * nf[1] * 2, 0.0);
-  auto W = [&](int i, int j, int k) { return d2[0][i] * d2[1][j] * d2[2][k]; };  // local 1-based indices
+  // local 1-based indices; with a transform axis the weight leaves it out (solver.f90:98-106)
+  auto W = [&](int i, int j, int k) {
+    if (fft_axis == 1) return d2[1][j] * d2[2][k];
+    if (fft_axis == 2) return d2[0][i] * d2[2][k];
+    if (fft_axis == 3) return d2[0][i] * d2[1][j];
+    return d2[0][i] * d2[1][j] * d2[2][k];
+  };
   const bool has_bcval = field >= HF_U && field < HF_S0;
   // bcval at local (1-based) in-plane indices p1, p2: the inflow plane on an inflow face (main.f90:605-625),
   // else the uniform bc
@@ -263,10 +268,6 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
   const snac_case &c = d.c;
   S.field = field;
   S.helm = field != HF_P;
-  if (S.helm && c.fft_axis) {
-    set_error("IMPDIFF Helmholtz solves are implemented for the 3-D solve (FFT_AXIS 0) only");
-    return SNAC_ERR_UNSUPPORTED;
-  }
   S.precision = d.opt.precision;
   if (const char *e = getenv("SNAC_MG_INNER")) S.inner_iters = std::max(1, atoi(e));
   if (const char *e = getenv("SNAC_MG_INNER_TOL")) S.inner_tol = atof(e);
@@ -305,23 +306,31 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
     const int pf = S.ax[2];
     S.nsys = hi_max[pf] - lo_min[pf] + 1;
     for (int b = 0; b < d.nblocks; b++)
-      if (d.hb[b].lo[pf] != lo_min[pf] || d.hb[b].hi[pf] != hi_max[pf]) {
+      if (d.hb[b].lo[pf] != lo_min[pf] || field_hi(d.hb[b], field, pf) != hi_max[pf]) {
         set_error("every block must span the whole transform direction");
         return SNAC_ERR_UNSUPPORTED;
       }
-    // fft.f90 set-up: kinds, normfft (fftini, fft.f90:68), eigenvalues/dl^2 (init_fft_reduction)
-    S.nfft = S.nsys;
+    // fft.f90 set-up with the field's boundary pair and centring along the transform axis: kinds, the
+    // transform length n - q (fftini drops the wall face of a staggered non-periodic component), normfft,
+    // eigenvalues(n)/dl^2 (init_fft_reduction, solver.f90:1124-1138) of which the first nsys are used
+    const HostBlock &H0 = d.hb[0];
+    const int cen_f = field_centered(field, pf), n_full = H0.ng[pf];
+    const char bc[2] = {field_cbc(H0, field, pf, 0), field_cbc(H0, field, pf, 1)};
+    const int q = ((bc[0] == 'F' && bc[1] == 'F') || cen_f) ? 0 : 1;
     double norm[2];
-    const char *bc = d.hb[0].desc.cbcpre[pf];
-    find_fft(bc[0], bc[1], 1, &S.kind_fwd, &S.kind_bwd, norm);
+    find_fft(bc[0], bc[1], cen_f, &S.kind_fwd, &S.kind_bwd, norm);
     if (S.kind_fwd < 0) { set_error("unsupported boundary pair along the transform direction"); return SNAC_ERR_UNSUPPORTED; }
-    S.normfft = 1.0 / (norm[0] * (S.nfft + norm[1] - 0));
-    S.lambda.assign(S.nfft, 0.0);
-    if (eigenvalues(S.nfft, bc[0], bc[1], 1, S.lambda.data())) {
+    S.nfft = n_full - q;
+    if (S.nfft != S.nsys) { set_error("transform length and solved extent differ along the transform direction"); return SNAC_ERR_UNSUPPORTED; }
+    S.normfft = 1.0 / (norm[0] * (n_full + norm[1] - q));
+    std::vector<double> lam(n_full, 0.0);
+    if (eigenvalues(n_full, bc[0], bc[1], cen_f, lam.data())) {
       set_error("no eigenvalues for this boundary pair (the reference defines none)");
       return SNAC_ERR_UNSUPPORTED;
     }
-    const double dl0 = d.hb[0].dl[pf][0];
+    // dl(0, idir): dxc(lo-1) along a centred axis, dxf(lo) along a staggered one (main.f90:725, 771-773)
+    const double dl0 = cen_f ? H0.dl[pf][0] : H0.g[pf][1][1];
+    S.lambda.assign(lam.begin(), lam.begin() + S.nsys);
     for (auto &v : S.lambda) v = v / (dl0 * dl0);
     if (upload) SNAC_TRY(fft_setup(S));
   } else {
@@ -621,6 +630,11 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
     }
     SNAC_TRY(plane_make_invd(P, tabs, tabsf, 0));
     SNAC_CUDA(cudaStreamSynchronize(0));
+    for (int l = 0; l < P.nlev; l++) { S.invd_tab[l] = tabs[l]; S.invd_tabf[l] = tabsf[l]; }
+    if (S.helm) {  // the shift of each wavenumber is lambda_k + alphai, set per solve
+      S.d_lambda = (double *)up(S.lambda.data(), S.lambda.size() * sizeof(double));
+      if (!S.d_lambda) { set_error("device allocation failed (eigenvalues)"); return SNAC_ERR_NOMEM; }
+    }
   }
   S.ncell0 = L0.ncell;
   const size_t nv0 = (size_t)L0.ncell * S.nsys;
@@ -655,7 +669,7 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
     for (int a = 0; a < 3; a++) planes[a].resize(d.nblocks);
     for (int b = 0; b < d.nblocks; b++) {
       std::vector<double> r[3];
-      init_bc_rhs_field(d.hb[b], field, d.periods, r);
+      init_bc_rhs_field(d.hb[b], field, d.periods, c.fft_axis, r);
       for (int a = 0; a < 3; a++) planes[a][b] = std::move(r[a]);
     }
     SNAC_TRY(helm_upload_tables(d, S, planes));
@@ -723,16 +737,22 @@ static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *
 
 // solve_impdiff_field_3d (solve_helmholtz.f90:109-138): right-hand side alphai V phi + BC planes, the
 // shift alphai on the diagonal, the solve warm-started from the previous solution, the field overwritten
+// solve_impdiff_field_fft (solve_helmholtz.f90:32-102) with a transform axis: the same right-hand side
+// weighted by the in-plane area, the forward transform of the field, per-wavenumber solves with the shift
+// lambda_k + alphai, the backward transform and normfft.
 int solver_solve_helmholtz(Domain &d, PoissonSolver &S, double alphai) {
   cudaStream_t st = d.st;
   if (!S.helm) { set_error("not a Helmholtz solver"); return SNAC_ERR_STATE; }
   SNAC_TRY(helm_rhs(d, S, alphai, st));
-  SNAC_TRY(helm_io(d, S, S.box_b, 1, st));
+  SNAC_TRY(helm_shift(S, alphai, st));
+  if (S.fft_axis) SNAC_TRY(fft_forward_to_box(d, S, st));
+  else SNAC_TRY(helm_io(d, S, S.box_b, 1, st));
   int it = 0;
   double res = 0.0;
   const int rc = solve_box(S, st, &it, &res);
   if (rc != SNAC_OK && rc != SNAC_ERR_NOT_CONVERGED) return rc;
-  SNAC_TRY(helm_io(d, S, S.box_x, 0, st));
+  if (S.fft_axis) SNAC_TRY(fft_backward_from_box(d, S, st));
+  else SNAC_TRY(helm_io(d, S, S.box_x, 0, st));
   S.last_iters = it;
   S.last_res = res;
   if (rc == SNAC_ERR_NOT_CONVERGED)

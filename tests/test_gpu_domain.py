@@ -293,6 +293,44 @@ def test_steps_dhc_impdiff(snac_lib, oracle_mod, precision):
         d.close()
 
 
+@pytest.mark.parametrize("which,precision", [("ldc_x", 0), ("ldc_x", 1), ("channel_z", 0), ("channel_z", 1),
+                                             ("dhc_y", 0)])
+def test_steps_impdiff_fft(snac_lib, oracle_mod, which, precision):
+    """IMPDIFF with a transform axis (solve_impdiff_field_fft): each field's own transform, per-wavenumber
+    Helmholtz solves with the shift lambda_k + alphai.  LDC along x has walls on the transform axis (u is
+    staggered there: the transform drops its wall face), the channel is periodic along z, the heated cavity
+    (FFT along y) adds the scalar's Helmholtz solve and buoyancy."""
+    import dataclasses
+    if which == "ldc_x":
+        case = dataclasses.replace(cases.ldc_reference_test(fft_axis=1), impdiff=1, dt_f=2e-3)
+    elif which == "channel_z":
+        case = dataclasses.replace(cases.channel_4block(nx=(16, 32), ny=(8, 16), nz=16), impdiff=1, dt_f=2e-3)
+    else:
+        case = dataclasses.replace(cases.dhc_reference_test(), impdiff=1, dt_f=5e-3)
+    O = oracle_mod.OracleDomain(case)
+    d = Domain(case, precision=precision)
+    try:
+        seed_fields(case, O, d, seed=8, amp=0.1)
+        if which == "dhc_y":
+            s0 = cases.dhc_initial_scalar(case, lambda ib: O.grid(ib, 0, oracle_mod.G_XC))
+            O.field(0, capi.S0)[...] = s0[0]
+            d.set(0, capi.S0, s0[0])
+        for X in (O, d):
+            X.bounduvw(False)
+            X.boundp(capi.P)
+            if which == "dhc_y":
+                X.boundp(capi.S0)
+        O.step(3)
+        d.step(3)
+        st = d.stats()
+        assert st["helm_iters"] > 0 and st["helm_residual"] <= case.tol
+        kinds = (capi.U, capi.V, capi.W) + ((capi.S0,) if which == "dhc_y" else ())
+        compare_fields(case, O, d, kinds, 1e-9)
+        compare_fields(case, O, d, (capi.P,), 1e-8, mean_free_p=True)
+    finally:
+        d.close()
+
+
 def test_steps_lshape_impdiff(snac_lib, oracle_mod):
     """IMPDIFF across block interfaces: the L-shaped box of three blocks, where a velocity component's
     Helmholtz box runs through the friend faces (hif = hi there) and stops short of the walls."""

@@ -172,3 +172,41 @@ def test_oracle_inflow_planes(oracle_mod, which):
         assert np.all(u[0] == 7.0)
     finally:
         O.close()
+
+
+@pytest.mark.parametrize("which", ["ldc_x", "channel_z"])
+def test_oracle_impdiff_fft_matches_3d(oracle_mod, which):
+    """solve_impdiff_field_fft and solve_impdiff_field_3d solve the same discrete Helmholtz problems where
+    the transform axis is uniform: the field's own transform (the staggered kinds and eigenvalues along a
+    wall-bounded axis for LDC along x, the periodic ones for the channel along z) diagonalises it exactly,
+    so whole IMPDIFF steps agree to the solver tolerance."""
+    import dataclasses
+    from snac_gb300 import capi
+
+    def run(case):
+        O = oracle_mod.OracleDomain(case)
+        try:
+            rng = np.random.default_rng(3)
+            for ib in range(len(case.blocks)):
+                for k in (capi.U, capi.V, capi.W, capi.P):
+                    f = O.field(ib, k)
+                    f[...] = 0.1 * rng.standard_normal(f.shape)
+            O.bounduvw(False)
+            O.boundp(capi.P)
+            O.step(3)
+            return [[O.field(ib, k)[1:-1, 1:-1, 1:-1].copy() for k in (capi.U, capi.V, capi.W)]
+                    for ib in range(len(case.blocks))]
+        finally:
+            O.close()
+
+    if which == "ldc_x":
+        mk = lambda fa: cases.ldc_reference_test(fft_axis=fa)
+        fa = 1
+    else:
+        mk = lambda fa: dataclasses.replace(cases.channel_4block(nx=(16, 32), ny=(8, 16), nz=16), fft_axis=fa)
+        fa = 3
+    a = run(dataclasses.replace(mk(0), impdiff=1, dt_f=2e-3, tol=1e-13))
+    b = run(dataclasses.replace(mk(fa), impdiff=1, dt_f=2e-3, tol=1e-13))
+    for fa_, fb_ in zip(a, b):
+        for x, y in zip(fa_, fb_):
+            assert np.max(np.abs(x - y)) <= 1e-11 * np.max(np.abs(x))
