@@ -48,7 +48,8 @@ enum {
   SNAC_ERR_BOUNDS = 6,         /* a device-side bounds check fired */
   SNAC_ERR_STATE = 7,          /* call out of order (e.g. snac_step before snac_init) */
   SNAC_ERR_UNSUPPORTED = 8,    /* input the library does not implement */
-  SNAC_ERR_NOMEM = 9           /* device allocation failed */
+  SNAC_ERR_NOMEM = 9,          /* device allocation failed */
+  SNAC_ERR_IO = 10             /* a checkpoint file could not be opened, read or written, or has the wrong size */
 };
 
 /* field identifiers for the domain layer */
@@ -238,6 +239,15 @@ int snac_updt_pressure_all(double alpha);         /* updt_pressure.f90 */
 int snac_chkdt_all(double *dt_cfl);               /* chkdt.f90 incl. the MPI reductions */
 int snac_chkdiv_all(double *divtot, double *divmax);
 int snac_kinetic_energy(double *ke);
+/* checkpoints, load_one (load.f90:92-160) as main.f90:544-553 (read) and 1107-1115 (write) call it: for
+ * block b (1-based) and field f the file "<prefix>_b_<b as %03d>_<f>.bin", f = u, v, w, p, s_001..,
+ * each the block's interior ng(1) x ng(2) x ng(3) FP64 values in Fortran order followed by
+ * [time, istep] as two FP64 values.  prefix is e.g. "data/fld" (is_overwrite_save) or "data/fld_0001000".
+ * Loading checks every file's size (the reference's abort becomes SNAC_ERR_IO), replaces the interiors
+ * and sets time and istep; ghost cells are left to the caller's bounduvw/boundp, as in main.f90:562-568. */
+int snac_checkpoint_save(const char *prefix);
+int snac_checkpoint_load(const char *prefix);
+
 /* whole RK3 steps, main.f90:893-1069 (dt from chkdt every icheck steps) */
 int snac_step(int nsteps);
 int snac_get_stats(snac_step_stats *st);

@@ -542,6 +542,78 @@ void or_inflow(or_domain *d, int is_correc) {
   }
 }
 
+/* load_one (load.f90:92-160): the interior of one field in Fortran order, then [time, istep] */
+static void ckpt_name(char *buf, size_t len, const char *prefix, int ib, int kind) {
+  if (kind >= OR_S0 && kind <= OR_S3) snprintf(buf, len, "%s_b_%03d_s_%03d.bin", prefix, ib + 1, kind - OR_S0 + 1);
+  else snprintf(buf, len, "%s_b_%03d_%c.bin", prefix, ib + 1, "uvwp"[kind - OR_U]);
+}
+
+int or_checkpoint_save(or_domain *d, const char *prefix) {
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    const int nx = B->ng[0], ny = B->ng[1], nz = B->ng[2];
+    double *out = malloc(sizeof(double) * ((size_t)nx * ny * nz + 2));
+    for (int f = 0; f < 4 + d->c.nscal; f++) {
+      const int kind = f < 4 ? OR_U + f : OR_S0 + (f - 4);
+      const double *fl = B->fld[kind];
+      size_t q = 0;
+      for (int k = 1; k <= nz; k++)
+        for (int j = 1; j <= ny; j++)
+          for (int i = 1; i <= nx; i++) out[q++] = fl[i + (size_t)(nx + 2) * (j + (size_t)(ny + 2) * k)];
+      out[q++] = d->time;
+      out[q++] = 1.0 * d->istep;
+      char name[4096];
+      ckpt_name(name, sizeof(name), prefix, ib, kind);
+      FILE *fp = fopen(name, "wb");
+      if (!fp) { free(out); return -1; }
+      const size_t nw = fwrite(out, sizeof(double), q, fp);
+      if (fclose(fp) != 0 || nw != q) { free(out); return -1; }
+    }
+    free(out);
+  }
+  return 0;
+}
+
+int or_checkpoint_load(or_domain *d, const char *prefix) {
+  double info[2] = {0.0, 0.0};
+  for (int ib = 0; ib < d->nblocks; ib++) {
+    or_block *B = &d->b[ib];
+    const int nx = B->ng[0], ny = B->ng[1], nz = B->ng[2];
+    const size_t n = (size_t)nx * ny * nz + 2;
+    double *in = malloc(sizeof(double) * n);
+    for (int f = 0; f < 4 + d->c.nscal; f++) {
+      const int kind = f < 4 ? OR_U + f : OR_S0 + (f - 4);
+      char name[4096];
+      ckpt_name(name, sizeof(name), prefix, ib, kind);
+      FILE *fp = fopen(name, "rb");
+      if (!fp) { free(in); return -1; }
+      fseek(fp, 0, SEEK_END);
+      const long size = ftell(fp);
+      fseek(fp, 0, SEEK_SET);
+      if (size < 0 || (size_t)size != n * sizeof(double)) { fclose(fp); free(in); return -2; }
+      const size_t nr = fread(in, sizeof(double), n, fp);
+      fclose(fp);
+      if (nr != n) { free(in); return -1; }
+      double *fl = B->fld[kind];
+      size_t q = 0;
+      for (int k = 1; k <= nz; k++)
+        for (int j = 1; j <= ny; j++)
+          for (int i = 1; i <= nx; i++) fl[i + (size_t)(nx + 2) * (j + (size_t)(ny + 2) * k)] = in[q++];
+      info[0] = in[q];
+      info[1] = in[q + 1];
+    }
+    free(in);
+  }
+  d->time = info[0];
+  d->istep = (int)lround(info[1]);
+  return 0;
+}
+
+void or_time_istep(const or_domain *d, double *time, int *istep) {
+  *time = d->time;
+  *istep = d->istep;
+}
+
 /* bound.f90:68-106; scalars use their own cbc/bc (main.f90:936) */
 void or_boundp(or_domain *d, int kind) {
   for (int a = 0; a < 3; a++) exchange_dir(d, kind, a);

@@ -66,6 +66,10 @@ def lib():
         L.or_block_geometry.argtypes = [C.c_void_p, C.c_int, ip, ip, ip, ip]
         L.or_vol_all.restype = C.c_double
         L.or_vol_all.argtypes = [C.c_void_p]
+        for n in ("or_checkpoint_save", "or_checkpoint_load"):
+            getattr(L, n).argtypes = [C.c_void_p, C.c_char_p]
+            getattr(L, n).restype = C.c_int
+        L.or_time_istep.argtypes = [C.c_void_p, dp, C.POINTER(C.c_int)]
         for n in ("or_bounduvw", "or_boundp", "or_inflow"):
             getattr(L, n).argtypes = [C.c_void_p, C.c_int]
         L.or_fillps_all.argtypes = [C.c_void_p, C.c_double]
@@ -224,6 +228,22 @@ class OracleDomain:
 
     def inflow(self, is_correc=False):
         lib().or_inflow(self.h, int(is_correc))
+
+    def checkpoint_save(self, prefix):
+        rc = lib().or_checkpoint_save(self.h, str(prefix).encode())
+        if rc:
+            raise IOError(f"oracle checkpoint save failed ({rc})")
+
+    def checkpoint_load(self, prefix):
+        rc = lib().or_checkpoint_load(self.h, str(prefix).encode())
+        if rc:
+            raise IOError(f"oracle checkpoint load failed ({rc})")
+
+    @property
+    def time_istep(self):
+        t = C.c_double(); i = C.c_int()
+        lib().or_time_istep(self.h, C.byref(t), C.byref(i))
+        return t.value, i.value
 
     def boundp(self, kind=P):
         lib().or_boundp(self.h, kind)

@@ -138,6 +138,11 @@ double  or_vol_all(const or_domain *d);
 void   or_bounduvw(or_domain *d, int is_correc);
 void   or_boundp(or_domain *d, int kind);
 void   or_inflow(or_domain *d, int is_correc);              /* bound.f90:438-477 on every inflow face */
+/* load_one (load.f90:92-160) per block and field: "<prefix>_b_%03d_{u,v,w,p,s_%03d}.bin"; 0 ok, -1 i/o error,
+   -2 a file of the wrong size */
+int    or_checkpoint_save(or_domain *d, const char *prefix);
+int    or_checkpoint_load(or_domain *d, const char *prefix);
+void   or_time_istep(const or_domain *d, double *time, int *istep);
 void   or_fillps_all(or_domain *d, double dtrk);
 void   or_updt_rhs_all(or_domain *d);
 int    or_solve_pressure(or_domain *d);                   /* pp <- solution, po updated */

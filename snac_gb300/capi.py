@@ -16,7 +16,7 @@ import numpy as np
 from . import _build
 
 MAX_SCAL = 4
-OK, ERR_ARG, ERR_CUDA, ERR_NOT_CONVERGED, ERR_NAN, ERR_TIMEOUT, ERR_BOUNDS, ERR_STATE, ERR_UNSUPPORTED, ERR_NOMEM = range(10)
+OK, ERR_ARG, ERR_CUDA, ERR_NOT_CONVERGED, ERR_NAN, ERR_TIMEOUT, ERR_BOUNDS, ERR_STATE, ERR_UNSUPPORTED, ERR_NOMEM, ERR_IO = range(11)
 U, V, W, P, PP, PO, DUDTRKO, DVDTRKO, DWDTRKO = range(9)
 S0, DSDTRKO0 = 9, 20
 G_DXC, G_DXF, G_XC, G_XF = range(4)
@@ -111,6 +111,8 @@ PROTOTYPES = {
     "snac_chkdiv_all": (C.c_int, [DP, DP]),
     "snac_kinetic_energy": (C.c_int, [DP]),
     "snac_step": (C.c_int, [C.c_int]),
+    "snac_checkpoint_save": (C.c_int, [C.c_char_p]),
+    "snac_checkpoint_load": (C.c_int, [C.c_char_p]),
     "snac_get_stats": (C.c_int, [C.POINTER(StepStats)]),
     "snac_set_dt": (C.c_int, [C.c_double]),
     "snac_get_dt": (C.c_int, [DP]),

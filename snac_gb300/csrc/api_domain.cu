@@ -7,7 +7,9 @@
 // runs the RK3 loop of main.f90:893-1069.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <string>
 
 #include "snac_host.h"
 
@@ -800,6 +802,93 @@ int snac_get_grid(int ib, int axis, int which, double *out) {
 }
 
 double snac_vol_all(void) { return domain() ? domain()->vol_all : 0.0; }
+
+// ---------------------------------------------------------------- checkpoints (load.f90:92-160)
+static std::string ckpt_name(const char *prefix, int ib, int field) {
+  char buf[64];
+  if (field >= SNAC_S0) snprintf(buf, sizeof(buf), "_b_%03d_s_%03d.bin", ib + 1, field - SNAC_S0 + 1);
+  else snprintf(buf, sizeof(buf), "_b_%03d_%c.bin", ib + 1, "uvwp"[field - SNAC_U]);
+  return std::string(prefix) + buf;
+}
+
+static int ckpt_fields(const Domain &d, std::vector<int> &f) {
+  f = {SNAC_U, SNAC_V, SNAC_W, SNAC_P};
+  for (int q = 0; q < d.c.nscal; q++) f.push_back(SNAC_S0 + q);
+  return SNAC_OK;
+}
+
+int snac_checkpoint_save(const char *prefix) {
+  NEED_DOMAIN
+  if (!prefix) { set_error("snac_checkpoint_save: null prefix"); return SNAC_ERR_ARG; }
+  std::vector<int> fl;
+  ckpt_fields(*d, fl);
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  for (int b = 0; b < d->nblocks; b++) {
+    const int nx = d->hb[b].ng[0], ny = d->hb[b].ng[1], nz = d->hb[b].ng[2];
+    std::vector<double> halo((size_t)(nx + 2) * (ny + 2) * (nz + 2)), out((size_t)nx * ny * nz + 2);
+    for (int f : fl) {
+      double *p; size_t bytes;
+      SNAC_TRY(field_ptr(*d, b, f, &p, &bytes));
+      SNAC_CUDA(cudaMemcpy(halo.data(), p, bytes, cudaMemcpyDeviceToHost));
+      size_t q = 0;
+      for (int k = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++)
+          for (int i = 0; i < nx; i++) out[q++] = halo[hidx(i, j, k, nx, ny)];
+      out[q++] = d->time;
+      out[q++] = 1.0 * d->istep;
+      const std::string name = ckpt_name(prefix, b, f);
+      FILE *fp = fopen(name.c_str(), "wb");
+      if (!fp) { set_error("cannot create checkpoint file %s", name.c_str()); return SNAC_ERR_IO; }
+      const size_t nw = fwrite(out.data(), sizeof(double), out.size(), fp);
+      const int cl = fclose(fp);
+      if (nw != out.size() || cl != 0) { set_error("cannot write checkpoint file %s", name.c_str()); return SNAC_ERR_IO; }
+    }
+  }
+  return SNAC_OK;
+}
+
+int snac_checkpoint_load(const char *prefix) {
+  NEED_DOMAIN
+  if (!prefix) { set_error("snac_checkpoint_load: null prefix"); return SNAC_ERR_ARG; }
+  std::vector<int> fl;
+  ckpt_fields(*d, fl);
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  double info[2] = {0.0, 0.0};
+  for (int b = 0; b < d->nblocks; b++) {
+    const int nx = d->hb[b].ng[0], ny = d->hb[b].ng[1], nz = d->hb[b].ng[2];
+    const size_t good = ((size_t)nx * ny * nz + 2) * sizeof(double);
+    std::vector<double> halo((size_t)(nx + 2) * (ny + 2) * (nz + 2)), in((size_t)nx * ny * nz + 2);
+    for (int f : fl) {
+      const std::string name = ckpt_name(prefix, b, f);
+      FILE *fp = fopen(name.c_str(), "rb");
+      if (!fp) { set_error("cannot open checkpoint file %s", name.c_str()); return SNAC_ERR_IO; }
+      fseek(fp, 0, SEEK_END);
+      const long size = ftell(fp);
+      fseek(fp, 0, SEEK_SET);
+      if (size < 0 || (size_t)size != good) {
+        fclose(fp);
+        set_error("checkpoint file with incorrect size: %s | expected size: %zu | actual size: %ld", name.c_str(), good, size);
+        return SNAC_ERR_IO;
+      }
+      const size_t nr = fread(in.data(), sizeof(double), in.size(), fp);
+      fclose(fp);
+      if (nr != in.size()) { set_error("cannot read checkpoint file %s", name.c_str()); return SNAC_ERR_IO; }
+      double *p; size_t bytes;
+      SNAC_TRY(field_ptr(*d, b, f, &p, &bytes));
+      SNAC_CUDA(cudaMemcpy(halo.data(), p, bytes, cudaMemcpyDeviceToHost));
+      size_t q = 0;
+      for (int k = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++)
+          for (int i = 0; i < nx; i++) halo[hidx(i, j, k, nx, ny)] = in[q++];
+      SNAC_CUDA(cudaMemcpy(p, halo.data(), bytes, cudaMemcpyHostToDevice));
+      info[0] = in[q];
+      info[1] = in[q + 1];
+    }
+  }
+  d->time = info[0];
+  d->istep = (int)std::lround(info[1]);
+  return SNAC_OK;
+}
 
 int snac_set_field(int ib, int field, const double *host) {
   NEED_DOMAIN

@@ -128,10 +128,12 @@ __global__ void k_dense(MgLevelD L, const int *active, T *x, const T *b) {
   const long off = (long)n * s;
   for (int q = threadIdx.x; q < n; q += blockDim.x) sb[q] = b[off + q];
   __syncthreads();
+  // the inverse is stored by columns (M[c n + r]): a warp's loads of one step are contiguous
   const T *M = LA<T>::dinv(L) + (size_t)n * n * s;
   for (int r = threadIdx.x; r < n; r += blockDim.x) {
     T acc = 0;
-    for (int c = 0; c < n; c++) acc = fmat(M[(size_t)r * n + c], sb[c], acc);
+#pragma unroll 8
+    for (int c = 0; c < n; c++) acc = fmat(M[(size_t)c * n + r], sb[c], acc);
     x[off + r] = acc;
   }
 }

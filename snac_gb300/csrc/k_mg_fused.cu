@@ -166,16 +166,18 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
     }
     cp_async_commit();
   };
-  const int s1 = min(nsys, (int)(blockIdx.y + 1) * sb);
+  // systems strided over the CTA groups: systems still active late in a solve (often neighbouring
+  // wavenumbers) spread over many CTAs instead of queueing in one
+  const int sstep = (int)gridDim.y;
   auto next_active = [&](int from) {
-    for (int q = from; q < s1; q++)
+    for (int q = from; q < nsys; q += sstep)
       if (!active || active[q]) return q;
     return -1;
   };
-  int cur = next_active((int)blockIdx.y * sb), k = 0;
+  int cur = next_active((int)blockIdx.y), k = 0;
   if (cur >= 0) issue(cur, 0);
   while (cur >= 0) {
-    const int nxt = next_active(cur + 1);
+    const int nxt = next_active(cur + sstep);
     if (nxt >= 0) {
       issue(nxt, k ^ 1);
       cp_async_wait<1>();
@@ -413,9 +415,10 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P
     const int n = (int)L.ncell;
     if (dense) {
       const T *__restrict__ M = LA<T>::dinv(L) + (size_t)n * n * s;
-      for (int r = threadIdx.x; r < n; r += blockDim.x) {
+      for (int r = threadIdx.x; r < n; r += blockDim.x) {  // the inverse is stored by columns (as k_dense)
         T acc = 0;
-        for (int c = 0; c < n; c++) acc = fmat(M[(size_t)r * n + c], B(last)[c], acc);
+#pragma unroll 8
+        for (int c = 0; c < n; c++) acc = fmat(M[(size_t)c * n + r], B(last)[c], acc);
         X(last)[r] = acc;
       }
       __syncthreads();

@@ -56,8 +56,7 @@ __global__ void __launch_bounds__(256) k_p_rbgs(MgLevelD L, int per0, int per1, 
   const PlaneCell<T> pc = plane_cell<T>(L, per0, per1, i, j);
   const T cc = LA<T>::cc(L)[c], wt = LA<T>::w01(L)[c];
   const T *__restrict__ invd = LA<T>::invd(L);
-  const int s0 = blockIdx.z * sb, s1 = min(nsys, s0 + sb);
-  for (int s = s0; s < s1; s++) {
+  for (int s = (int)blockIdx.z; s < nsys; s += (int)gridDim.z) {  // systems strided over the CTA groups
     if (active && !active[s]) continue;
     const long off = L.ncell * (long)s;
     const T *xs = x + off;
@@ -92,8 +91,7 @@ __global__ void __launch_bounds__(256) k_p_restrict(MgLevelD F, MgLevelD C, int 
     }
   }
   const int cq = I + C.n[0] * J;
-  const int s0 = blockIdx.z * sb, s1 = min(nsys, s0 + sb);
-  for (int s = s0; s < s1; s++) {
+  for (int s = (int)blockIdx.z; s < nsys; s += (int)gridDim.z) {  // systems strided over the CTA groups
     if (active && !active[s]) continue;
     const long offf = F.ncell * (long)s, offc = C.ncell * (long)s;
     const T *__restrict__ xs = xf + offf;
@@ -118,8 +116,7 @@ __global__ void __launch_bounds__(256) k_p_prolong(MgLevelD F, MgLevelD C, const
   const int c = i + F.n[0] * j;
   if (F.code[c] & 0x8000) return;
   const int pc = (C.coarsened[0] ? i / 2 : i) + C.n[0] * (C.coarsened[1] ? j / 2 : j);
-  const int s0 = blockIdx.z * sb, s1 = min(nsys, s0 + sb);
-  for (int s = s0; s < s1; s++) {
+  for (int s = (int)blockIdx.z; s < nsys; s += (int)gridDim.z) {  // systems strided over the CTA groups
     if (active && !active[s]) continue;
     xf[F.ncell * (long)s + c] += xc[C.ncell * (long)s + pc];
   }
@@ -162,8 +159,7 @@ __global__ void __launch_bounds__(256) k_p_resid(MgLevelD L, int per0, int per1,
     }
   }
   const long chunk = blockIdx.x + (long)gridDim.x * blockIdx.y;
-  const int s0 = blockIdx.z * sb, s1 = min(nsys, s0 + sb);
-  for (int s = s0; s < s1; s++) {
+  for (int s = (int)blockIdx.z; s < nsys; s += (int)gridDim.z) {  // systems strided over the CTA groups
     if (active && !active[s]) continue;
     const long off = L.ncell * (long)s;
     const T *__restrict__ xs = x + off;
@@ -219,8 +215,7 @@ __global__ void __launch_bounds__(256) k_p_apply(MgLevelD L, int per0, int per1,
     }
   }
   const long chunk = blockIdx.x + (long)gridDim.x * blockIdx.y;
-  const int s0 = blockIdx.z * sb, s1 = min(nsys, s0 + sb);
-  for (int s = s0; s < s1; s++) {
+  for (int s = (int)blockIdx.z; s < nsys; s += (int)gridDim.z) {  // systems strided over the CTA groups
     if (active && !active[s]) continue;
     const long off = L.ncell * (long)s;
     const T *__restrict__ zs = z + off;

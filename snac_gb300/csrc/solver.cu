@@ -168,7 +168,8 @@ struct Builder {
       e[c] = 1.0;
       for (long i = 0; i < n; i++) { double v = e[i]; for (long k = 0; k < i; k++) v -= A[i * n + k] * e[k]; e[i] = v / A[i * n + i]; }
       for (long i = n - 1; i >= 0; i--) { double v = e[i]; for (long k = i + 1; k < n; k++) v -= A[k * n + i] * e[k]; e[i] = v / A[i * n + i]; }
-      for (long r = 0; r < n; r++) M[r * n + c] = ((l.code[r] & 0x8000) || (l.code[c] & 0x8000)) ? 0.0 : -e[r];
+      // stored by columns, M[c n + r] = inverse(r, c): a warp of consecutive rows reads contiguous memory
+      for (long r = 0; r < n; r++) M[c * n + r] = ((l.code[r] & 0x8000) || (l.code[c] & 0x8000)) ? 0.0 : -e[r];
     }
     return true;
   }

@@ -113,6 +113,13 @@ class Domain:
         check(rc)
         return rc
 
+    def checkpoint_save(self, prefix):
+        """load_one('w') of every field of every block: <prefix>_b_###_{u,v,w,p,s_###}.bin"""
+        check(capi.lib().snac_checkpoint_save(str(prefix).encode()))
+
+    def checkpoint_load(self, prefix):
+        check(capi.lib().snac_checkpoint_load(str(prefix).encode()))
+
     def stats(self):
         s = capi.StepStats()
         check(capi.lib().snac_get_stats(C.byref(s)))

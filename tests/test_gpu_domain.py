@@ -430,3 +430,42 @@ def test_gpu_ldc_golden(snac_lib, fft_axis):
         np.testing.assert_allclose(prof, ref[:, 1], rtol=1e-7, atol=5e-8)
     finally:
         d.close()
+
+
+def test_checkpoint_bytes_match_oracle(snac_lib, oracle_mod, tmp_path):
+    """Checkpoints written from device state are byte-identical to the oracle's load_one files of the same
+    fields, and loading the oracle's files restores the device interiors exactly (with time and istep)."""
+    case = cases.channel_4block_scalar()
+    O = oracle_mod.OracleDomain(case)
+    d = Domain(case)
+    try:
+        rng = np.random.default_rng(13)
+        for ib in range(len(case.blocks)):
+            for k in (capi.U, capi.V, capi.W, capi.P, capi.S0):
+                f = O.field(ib, k)
+                f[...] = rng.standard_normal(f.shape)
+                d.set(ib, k, f)
+        pg, po = str(tmp_path / "gpu"), str(tmp_path / "orc")
+        d.checkpoint_save(pg)
+        O.checkpoint_save(po)
+        for ib in range(len(case.blocks)):
+            for tag in ("u", "v", "w", "p", "s_001"):
+                a = open(f"{pg}_b_{ib + 1:03d}_{tag}.bin", "rb").read()
+                b = open(f"{po}_b_{ib + 1:03d}_{tag}.bin", "rb").read()
+                assert a == b, (ib, tag)
+        # the oracle advances one step and writes; the device loads the oracle's files
+        O.bounduvw(False)
+        O.boundp(capi.P)
+        O.step(1)
+        O.checkpoint_save(po)
+        d.checkpoint_load(po)
+        st = d.stats()
+        assert (st["time"], st["istep"]) == O.time_istep
+        for ib in range(len(case.blocks)):
+            for k in (capi.U, capi.V, capi.W, capi.P, capi.S0):
+                np.testing.assert_array_equal(d.get(ib, k)[1:-1, 1:-1, 1:-1], O.field(ib, k)[1:-1, 1:-1, 1:-1])
+        with open(f"{po}_b_001_u.bin", "ab") as f:
+            f.write(b"\0" * 8)
+        assert capi.lib().snac_checkpoint_load(po.encode()) == capi.ERR_IO
+    finally:
+        d.close()

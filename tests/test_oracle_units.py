@@ -210,3 +210,43 @@ def test_oracle_impdiff_fft_matches_3d(oracle_mod, which):
     for fa_, fb_ in zip(a, b):
         for x, y in zip(fa_, fb_):
             assert np.max(np.abs(x - y)) <= 1e-11 * np.max(np.abs(x))
+
+
+def test_oracle_checkpoint_format(oracle_mod, tmp_path):
+    """load_one (load.f90:92-160): each file is the block's interior in Fortran order followed by
+    [time, istep] in FP64; loading restores the interiors exactly and rejects a file of the wrong size."""
+    from snac_gb300 import capi
+    case = cases.channel_4block_scalar()
+    O = oracle_mod.OracleDomain(case)
+    O2 = oracle_mod.OracleDomain(case)
+    try:
+        rng = np.random.default_rng(12)
+        for ib in range(len(case.blocks)):
+            for k in (capi.U, capi.V, capi.W, capi.P, capi.S0):
+                O.field(ib, k)[...] = rng.standard_normal(O.field(ib, k).shape)
+        O.bounduvw(False)
+        O.step(1)
+        prefix = str(tmp_path / "fld")
+        O.checkpoint_save(prefix)
+        t, istep = O.time_istep
+        assert istep == 1
+        for ib, b in enumerate(case.blocks):
+            for k, tag in ((capi.U, "u"), (capi.V, "v"), (capi.W, "w"), (capi.P, "p"), (capi.S0, "s_001")):
+                raw = np.fromfile(f"{prefix}_b_{ib + 1:03d}_{tag}.bin", dtype=np.float64)
+                n = int(np.prod(b.ng))
+                assert raw.size == n + 2
+                interior = O.field(ib, k)[1:-1, 1:-1, 1:-1]
+                np.testing.assert_array_equal(raw[:n].reshape(tuple(b.ng), order="F"), interior)
+                assert raw[n] == t and raw[n + 1] == float(istep)
+        O2.checkpoint_load(prefix)
+        assert O2.time_istep == (t, istep)
+        for ib in range(len(case.blocks)):
+            for k in (capi.U, capi.V, capi.W, capi.P, capi.S0):
+                np.testing.assert_array_equal(O2.field(ib, k)[1:-1, 1:-1, 1:-1], O.field(ib, k)[1:-1, 1:-1, 1:-1])
+        with open(f"{prefix}_b_002_v.bin", "ab") as f:
+            f.write(b"\0" * 8)
+        with pytest.raises(IOError):
+            O2.checkpoint_load(prefix)
+    finally:
+        O.close()
+        O2.close()
