@@ -248,6 +248,16 @@ int snac_kinetic_energy(double *ke);
 int snac_checkpoint_save(const char *prefix);
 int snac_checkpoint_load(const char *prefix);
 
+/* out1d (output.f90:34-125) as out1d.h90 calls it: the average of field f of block ib over the planes
+ * normal to idir (1..3), each field with its own spacings and coordinates (u: dxc,dyf,dzf at xf,yc,zc;
+ * v: dxf,dyc,dzf at xc,yf,zc; w: dxf,dyf,dzc at xc,yc,zf; p, pp and scalars: dxf,dyf,dzf at xc,yc,zc),
+ * divided by the block's lengths.  coord and prof receive ng(idir) values. */
+int snac_out1d(int ib, int field, int idir, double *coord, double *prof);
+/* the same profile written as the reference's text file: one line per index in format (2E15.7) */
+int snac_out1d_write(const char *fname, int ib, int field, int idir);
+/* out3d (output.f90:227-257): the interior of field f of block ib in Fortran order, FP64, no header */
+int snac_out3d_write(const char *fname, int ib, int field);
+
 /* whole RK3 steps, main.f90:893-1069 (dt from chkdt every icheck steps) */
 int snac_step(int nsteps);
 int snac_get_stats(snac_step_stats *st);

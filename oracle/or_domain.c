@@ -609,6 +609,70 @@ int or_checkpoint_load(or_domain *d, const char *prefix) {
   return 0;
 }
 
+/* Fortran's E15.7 edit descriptor: 0.ddddddd with 7 significant digits (correctly rounded, as printf's
+   %.6e), then E+ee, or +eee beyond two exponent digits, right-justified in 15 columns */
+void or_fortran_e15_7(double v, char *out) {
+  char mant[40], expo[24], body[96];
+  int e10 = 0;
+  const int neg = signbit(v) && v != 0.0;
+  if (v == 0.0) snprintf(mant, sizeof(mant), "0.0000000");
+  else {
+    char buf[40];
+    snprintf(buf, sizeof(buf), "%.6e", fabs(v));
+    e10 = atoi(buf + 9) + 1;
+    snprintf(mant, sizeof(mant), "0.%c%.6s", buf[0], buf + 2);
+  }
+  if (e10 >= -99 && e10 <= 99) snprintf(expo, sizeof(expo), "E%c%02d", e10 < 0 ? '-' : '+', abs(e10));
+  else snprintf(expo, sizeof(expo), "%c%03d", e10 < 0 ? '-' : '+', abs(e10));
+  snprintf(body, sizeof(body), "%s%s%s", neg ? "-" : "", mant, expo);
+  snprintf(out, 128, "%15s", body);
+}
+
+int or_out1d(or_domain *d, int ib, int kind, int idir, double *coord, double *prof, const char *fname) {
+  if (ib < 0 || ib >= d->nblocks || idir < 1 || idir > 3) return -1;
+  or_block *B = &d->b[ib];
+  const int nx = B->ng[0], ny = B->ng[1], nz = B->ng[2];
+  const double *f = B->fld[kind];
+  /* out1d.h90: u uses dxc,dyf,dzf at xf,yc,zc; v dxf,dyc,dzf at xc,yf,zc; w dxf,dyf,dzc at xc,yc,zf; p dxf.. */
+  const double *dl[3], *xg[3];
+  double l[3];
+  for (int a = 0; a < 3; a++) {
+    const int stag = kind >= OR_U && kind <= OR_W && kind - OR_U == a;
+    dl[a] = stag ? B->g[a][OR_G_DXC] : B->g[a][OR_G_DXF];
+    xg[a] = stag ? B->g[a][OR_G_XF] : B->g[a][OR_G_XC];
+    l[a] = B->desc.lmax[a] - B->desc.lmin[a];
+  }
+#define F(i, j, k) f[(i) + (size_t)(nx + 2) * ((j) + (size_t)(ny + 2) * (k))]
+  const int a = idir - 1, n = B->ng[a];
+  for (int q = 0; q < n; q++) prof[q] = 0.0;
+  if (idir == 3)
+    for (int k = 1; k <= nz; k++)
+      for (int j = 1; j <= ny; j++)
+        for (int i = 1; i <= nx; i++) prof[k - 1] = prof[k - 1] + F(i, j, k) * dl[0][i] * dl[1][j] / (l[0] * l[1]);
+  else if (idir == 2)
+    for (int j = 1; j <= ny; j++)
+      for (int k = 1; k <= nz; k++)
+        for (int i = 1; i <= nx; i++) prof[j - 1] = prof[j - 1] + F(i, j, k) * dl[0][i] * dl[2][k] / (l[0] * l[2]);
+  else
+    for (int i = 1; i <= nx; i++)
+      for (int k = 1; k <= nz; k++)
+        for (int j = 1; j <= ny; j++) prof[i - 1] = prof[i - 1] + F(i, j, k) * dl[1][j] * dl[2][k] / (l[1] * l[2]);
+#undef F
+  for (int q = 0; q < n; q++) coord[q] = xg[a][q + 1];
+  if (fname) {
+    FILE *fp = fopen(fname, "w");
+    if (!fp) return -1;
+    char s1[128], s2[128];
+    for (int q = 0; q < n; q++) {
+      or_fortran_e15_7(coord[q], s1);
+      or_fortran_e15_7(prof[q], s2);
+      fprintf(fp, "%s%s\n", s1, s2);
+    }
+    if (fclose(fp) != 0) return -1;
+  }
+  return 0;
+}
+
 void or_time_istep(const or_domain *d, double *time, int *istep) {
   *time = d->time;
   *istep = d->istep;

@@ -70,6 +70,9 @@ def lib():
             getattr(L, n).argtypes = [C.c_void_p, C.c_char_p]
             getattr(L, n).restype = C.c_int
         L.or_time_istep.argtypes = [C.c_void_p, dp, C.POINTER(C.c_int)]
+        L.or_out1d.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, dp, dp, C.c_char_p]
+        L.or_out1d.restype = C.c_int
+        L.or_fortran_e15_7.argtypes = [C.c_double, C.c_char_p]
         for n in ("or_bounduvw", "or_boundp", "or_inflow"):
             getattr(L, n).argtypes = [C.c_void_p, C.c_int]
         L.or_fillps_all.argtypes = [C.c_void_p, C.c_double]
@@ -239,6 +242,16 @@ class OracleDomain:
         if rc:
             raise IOError(f"oracle checkpoint load failed ({rc})")
 
+    def out1d(self, ib, kind, idir, fname=None):
+        n = self.case.blocks[ib].ng[idir - 1]
+        x = np.zeros(n); p = np.zeros(n)
+        dpp = C.POINTER(C.c_double)
+        rc = lib().or_out1d(self.h, int(ib), int(kind), int(idir), x.ctypes.data_as(dpp), p.ctypes.data_as(dpp),
+                            None if fname is None else str(fname).encode())
+        if rc:
+            raise IOError("oracle out1d failed")
+        return x, p
+
     @property
     def time_istep(self):
         t = C.c_double(); i = C.c_int()
@@ -308,3 +321,10 @@ def find_fft(bc: str, centered: bool):
     kf = C.c_int(); kb = C.c_int(); norm = np.zeros(2)
     lib().or_find_fft(bc.encode(), int(centered), C.byref(kf), C.byref(kb), _ptr(norm))
     return kf.value, kb.value, norm
+
+
+def fortran_e15_7(v: float) -> str:
+    """The oracle's Fortran E15.7 formatter (output.f90's '(2E15.7)' fields)."""
+    out = C.create_string_buffer(128)
+    lib().or_fortran_e15_7(float(v), out)
+    return out.value.decode()

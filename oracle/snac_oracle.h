@@ -143,6 +143,10 @@ void   or_inflow(or_domain *d, int is_correc);              /* bound.f90:438-477
 int    or_checkpoint_save(or_domain *d, const char *prefix);
 int    or_checkpoint_load(or_domain *d, const char *prefix);
 void   or_time_istep(const or_domain *d, double *time, int *istep);
+/* out1d (output.f90:34-125) with out1d.h90's spacings/coordinates per field; writes n(idir) values, and
+   the reference's text file when fname is not NULL (format 2E15.7) */
+int    or_out1d(or_domain *d, int ib, int kind, int idir, double *coord, double *prof, const char *fname);
+void   or_fortran_e15_7(double v, char *out);  /* Fortran Ew.d, w = 15, d = 7 */
 void   or_fillps_all(or_domain *d, double dtrk);
 void   or_updt_rhs_all(or_domain *d);
 int    or_solve_pressure(or_domain *d);                   /* pp <- solution, po updated */

@@ -113,6 +113,9 @@ PROTOTYPES = {
     "snac_step": (C.c_int, [C.c_int]),
     "snac_checkpoint_save": (C.c_int, [C.c_char_p]),
     "snac_checkpoint_load": (C.c_int, [C.c_char_p]),
+    "snac_out1d": (C.c_int, [C.c_int, C.c_int, C.c_int, DP, DP]),
+    "snac_out1d_write": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int]),
+    "snac_out3d_write": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
     "snac_get_stats": (C.c_int, [C.POINTER(StepStats)]),
     "snac_set_dt": (C.c_int, [C.c_double]),
     "snac_get_dt": (C.c_int, [DP]),

@@ -890,6 +890,108 @@ int snac_checkpoint_load(const char *prefix) {
   return SNAC_OK;
 }
 
+// ---------------------------------------------------------------- output (output.f90)
+// spacing and coordinate tables of a field along axis a: staggered along a (u along x, ...) -> d?c and the
+// face coordinates, else d?f and the centres (out1d.h90)
+static bool out_staggered(int field, int a) { return field >= SNAC_U && field <= SNAC_W && field - SNAC_U == a; }
+
+// Fortran's Ew.d edit descriptor for w = 15, d = 7 with the default scale factor: [-]0.ddddddd followed by
+// E+ee (or +eee when |exponent| > 99), right-justified; the digits are the value rounded to 7 significant
+// figures, as printf's %.6e rounds them
+static void fortran_e15_7(double v, char out[128]) {
+  char mant[32];
+  int e10 = 0;
+  const bool neg = std::signbit(v) && v != 0.0;
+  if (v == 0.0) {
+    std::snprintf(mant, sizeof(mant), "0.0000000");
+  } else {
+    char buf[32];
+    std::snprintf(buf, sizeof(buf), "%.6e", std::fabs(v));  // d.dddddde[+-]xx
+    e10 = std::atoi(buf + 9) + 1;
+    std::snprintf(mant, sizeof(mant), "0.%c%.6s", buf[0], buf + 2);
+  }
+  char expo[24];
+  if (e10 >= -99 && e10 <= 99) std::snprintf(expo, sizeof(expo), "E%c%02d", e10 < 0 ? '-' : '+', std::abs(e10));
+  else std::snprintf(expo, sizeof(expo), "%c%03d", e10 < 0 ? '-' : '+', std::abs(e10));
+  char body[96];
+  std::snprintf(body, sizeof(body), "%s%s%s", neg ? "-" : "", mant, expo);
+  std::snprintf(out, 128, "%15s", body);
+}
+
+int snac_out1d(int ib, int field, int idir, double *coord, double *prof) {
+  NEED_DOMAIN
+  if (ib < 0 || ib >= d->nblocks) { set_error("block index out of range"); return SNAC_ERR_ARG; }
+  if (idir < 1 || idir > 3) { set_error("idir must be 1, 2 or 3"); return SNAC_ERR_ARG; }
+  if (!coord || !prof) { set_error("snac_out1d: null output"); return SNAC_ERR_ARG; }
+  double *f; size_t bytes;
+  SNAC_TRY(field_ptr(*d, ib, field, &f, &bytes));
+  if (field == SNAC_DUDTRKO || field == SNAC_DVDTRKO || field == SNAC_DWDTRKO ||
+      (field >= SNAC_DSDTRKO0 && field < SNAC_DSDTRKO0 + SNAC_MAX_SCAL)) {
+    set_error("snac_out1d: halo'd fields only");
+    return SNAC_ERR_ARG;
+  }
+  const HostBlock &H = d->hb[ib];
+  const DBlock &B = d->db[ib];
+  const int a = idir - 1, ta = a == 0 ? 1 : 0, tb = a == 2 ? 1 : 2;
+  // device weight tables: the interior entries of B.ax[axis][which]
+  auto wtab = [&](int ax) {
+    const int which = out_staggered(field, ax) ? AX_DC : AX_DF;
+    return B.ax[ax] + (size_t)which * (B.n[ax] + 2) + 1;
+  };
+  const double lprod = (H.desc.lmax[ta] - H.desc.lmin[ta]) * (H.desc.lmax[tb] - H.desc.lmin[tb]);
+  double *dprof = (double *)d->alloc((size_t)H.ng[a] * sizeof(double));
+  if (!dprof) { set_error("device allocation failed (profile)"); return SNAC_ERR_NOMEM; }
+  SNAC_TRY(launch_out1d(f, H.ng, a, wtab(ta), wtab(tb), lprod, dprof, d->st));
+  SNAC_CUDA(cudaMemcpyAsync(prof, dprof, (size_t)H.ng[a] * sizeof(double), cudaMemcpyDeviceToHost, d->st));
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  d->allocs.pop_back();
+  SNAC_CUDA(cudaFree(dprof));
+  const std::vector<double> &x = H.g[a][out_staggered(field, a) ? 3 : 2];
+  for (int q = 0; q < H.ng[a]; q++) coord[q] = x[q + 1];
+  return SNAC_OK;
+}
+
+int snac_out1d_write(const char *fname, int ib, int field, int idir) {
+  NEED_DOMAIN
+  if (!fname) { set_error("snac_out1d_write: null file name"); return SNAC_ERR_ARG; }
+  if (ib < 0 || ib >= d->nblocks || idir < 1 || idir > 3) { set_error("block or direction out of range"); return SNAC_ERR_ARG; }
+  const int n = d->hb[ib].ng[idir - 1];
+  std::vector<double> x(n), p(n);
+  SNAC_TRY(snac_out1d(ib, field, idir, x.data(), p.data()));
+  FILE *fp = fopen(fname, "w");
+  if (!fp) { set_error("cannot create %s", fname); return SNAC_ERR_IO; }
+  char a[128], b[128];
+  for (int q = 0; q < n; q++) {
+    fortran_e15_7(x[q], a);
+    fortran_e15_7(p[q], b);
+    fprintf(fp, "%s%s\n", a, b);
+  }
+  if (fclose(fp) != 0) { set_error("cannot write %s", fname); return SNAC_ERR_IO; }
+  return SNAC_OK;
+}
+
+int snac_out3d_write(const char *fname, int ib, int field) {
+  NEED_DOMAIN
+  if (!fname) { set_error("snac_out3d_write: null file name"); return SNAC_ERR_ARG; }
+  if (ib < 0 || ib >= d->nblocks) { set_error("block index out of range"); return SNAC_ERR_ARG; }
+  double *p; size_t bytes;
+  SNAC_TRY(field_ptr(*d, ib, field, &p, &bytes));
+  const int nx = d->hb[ib].ng[0], ny = d->hb[ib].ng[1], nz = d->hb[ib].ng[2];
+  if (bytes != (size_t)(nx + 2) * (ny + 2) * (nz + 2) * sizeof(double)) { set_error("snac_out3d_write: halo'd fields only"); return SNAC_ERR_ARG; }
+  std::vector<double> halo((size_t)(nx + 2) * (ny + 2) * (nz + 2)), out((size_t)nx * ny * nz);
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  SNAC_CUDA(cudaMemcpy(halo.data(), p, bytes, cudaMemcpyDeviceToHost));
+  size_t q = 0;
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) out[q++] = halo[hidx(i, j, k, nx, ny)];
+  FILE *fp = fopen(fname, "wb");
+  if (!fp) { set_error("cannot create %s", fname); return SNAC_ERR_IO; }
+  const size_t nw = fwrite(out.data(), sizeof(double), out.size(), fp);
+  if (fclose(fp) != 0 || nw != out.size()) { set_error("cannot write %s", fname); return SNAC_ERR_IO; }
+  return SNAC_OK;
+}
+
 int snac_set_field(int ib, int field, const double *host) {
   NEED_DOMAIN
   double *p; size_t bytes;

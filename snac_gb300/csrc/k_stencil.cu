@@ -10,6 +10,7 @@
 // One CTA covers one TX x TY x TZ tile of one block (tile lists make uneven
 // multi-block layouts a single launch).
 #include "snac_internal.h"
+#include "snac_mgdev.h"
 #include "snac_prof.h"
 
 namespace snac {
@@ -502,6 +503,38 @@ std::vector<Tile> make_tiles(const std::vector<std::array<int, 3>> &sizes, int t
       for (int j = 0; j < sizes[b][1]; j += ty)
         for (int i = 0; i < sizes[b][0]; i += tx) t.push_back(make_int4((int)b, i, j, k));
   return t;
+}
+
+}  // namespace snac
+
+namespace snac {
+
+// out1d (output.f90:34-125): one CTA per index along idir sums p * w_a * w_b / (l_a l_b) over its plane,
+// with the field's weight tables wa (along axis ta) and wb (along tb) on the device
+__global__ void __launch_bounds__(256) k_out1d(const double *__restrict__ f, int nx, int ny, int nz, int idir,
+                                               const double *__restrict__ wa, const double *__restrict__ wb,
+                                               double lprod, double *__restrict__ prof) {
+  const int q = blockIdx.x;
+  const int n[3] = {nx, ny, nz};
+  const int ta = idir == 0 ? 1 : 0, tb = idir == 2 ? 1 : 2;
+  const long npl = (long)n[ta] * n[tb];
+  double acc = 0.0;
+  for (long e = threadIdx.x; e < npl; e += blockDim.x) {
+    int c[3];
+    c[idir] = q;
+    c[ta] = (int)(e % n[ta]);
+    c[tb] = (int)(e / n[ta]);
+    acc += f[hidx(c[0], c[1], c[2], nx, ny)] * wa[c[ta]] * wb[c[tb]] / lprod;
+  }
+  const double t = block_sum1<double>(acc);
+  if (threadIdx.x == 0) prof[q] = t;
+}
+
+int launch_out1d(const double *f, const int n[3], int idir, const double *wa, const double *wb, double lprod,
+                 double *prof, cudaStream_t st) {
+  k_out1d<<<n[idir], 256, 0, st>>>(f, n[0], n[1], n[2], idir, wa, wb, lprod, prof), ::snac::count_launch();
+  SNAC_CUDA(cudaGetLastError());
+  return SNAC_OK;
 }
 
 }  // namespace snac

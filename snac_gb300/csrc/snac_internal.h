@@ -102,6 +102,8 @@ int launch_updt_pressure(const DBlock *dB, const Tile *dT, int ntiles, double al
 int launch_chkdt_partial(const DBlock *dB, const Tile *dT, int ntiles, double *part, cudaStream_t st);
 int launch_chkdiv_partial(const DBlock *dB, const Tile *dT, int ntiles, double vol, double *part, cudaStream_t st);
 int launch_ke_partial(const DBlock *dB, const Tile *dT, int ntiles, double *part, cudaStream_t st);
+int launch_out1d(const double *f, const int n[3], int idir, const double *wa, const double *wb, double lprod,
+                 double *prof, cudaStream_t st);
 int launch_bulk_partial(const DBlock *dB, const Tile *dT, int ntiles, int sidx, double *part, cudaStream_t st);
 int launch_updt_rhs(int nx, int ny, int nz, const int isb[6], const double *rx, const double *ry, const double *rz,
                     double *p, cudaStream_t st);

@@ -120,6 +120,13 @@ class Domain:
     def checkpoint_load(self, prefix):
         check(capi.lib().snac_checkpoint_load(str(prefix).encode()))
 
+    def out1d(self, ib, kind, idir):
+        """(coordinates, profile) of out1d along idir (1..3)"""
+        n = self.case.blocks[ib].ng[idir - 1]
+        x = np.zeros(n); p = np.zeros(n)
+        check(capi.lib().snac_out1d(int(ib), int(kind), int(idir), x.ctypes.data_as(capi.DP), p.ctypes.data_as(capi.DP)))
+        return x, p
+
     def stats(self):
         s = capi.StepStats()
         check(capi.lib().snac_get_stats(C.byref(s)))

@@ -469,3 +469,33 @@ def test_checkpoint_bytes_match_oracle(snac_lib, oracle_mod, tmp_path):
         assert capi.lib().snac_checkpoint_load(po.encode()) == capi.ERR_IO
     finally:
         d.close()
+
+
+def test_out1d_out3d_match_oracle(snac_lib, oracle_mod, tmp_path):
+    """out1d profiles reduced on the device agree with the oracle's serial sums (their order differs: 1e-13),
+    the text files carry the same coordinates and 7-digit values, and out3d dumps are byte-identical."""
+    case = cases.channel_4block(nx=(16, 32), ny=(8, 16), nz=16)
+    O = oracle_mod.OracleDomain(case)
+    d = Domain(case)
+    try:
+        seed_fields(case, O, d, seed=15)
+        for ib in range(len(case.blocks)):
+            for k in (capi.U, capi.V, capi.W, capi.P):
+                for idir in (1, 2, 3):
+                    xg, pg = d.out1d(ib, k, idir)
+                    xo, po = O.out1d(ib, k, idir, fname=tmp_path / "o.out")
+                    np.testing.assert_array_equal(xg, xo)
+                    np.testing.assert_allclose(pg, po, rtol=1e-13, atol=1e-13 * np.max(np.abs(po)))
+                    assert capi.lib().snac_out1d_write(str(tmp_path / "g.out").encode(), ib, k, idir) == 0
+                    lg = open(tmp_path / "g.out").read().splitlines()
+                    lo = open(tmp_path / "o.out").read().splitlines()
+                    assert len(lg) == len(lo)
+                    for a, b in zip(lg, lo):
+                        assert a[:15] == b[:15]
+                        assert abs(float(a[15:]) - float(b[15:])) <= 1e-6 * max(abs(float(b[15:])), 1e-30)
+            assert capi.lib().snac_out3d_write(str(tmp_path / "f.bin").encode(), ib, capi.W) == 0
+            raw = np.fromfile(tmp_path / "f.bin", dtype=np.float64)
+            interior = O.field(ib, capi.W)[1:-1, 1:-1, 1:-1]
+            np.testing.assert_array_equal(raw, interior.ravel(order="F"))
+    finally:
+        d.close()

@@ -250,3 +250,52 @@ def test_oracle_checkpoint_format(oracle_mod, tmp_path):
     finally:
         O.close()
         O2.close()
+
+
+def test_fortran_e15_7_format(oracle_mod):
+    """output.f90 writes profiles with '(2E15.7)': 0.ddddddd mantissa, E+ee exponent, 15 columns."""
+    f = oracle_mod.fortran_e15_7
+    assert f(1.0) == "  0.1000000E+01"
+    assert f(-2.5e-3) == " -0.2500000E-02"
+    assert f(0.0) == "  0.0000000E+00"
+    assert f(123456789.0) == "  0.1234568E+09"
+    assert f(9.99999996) == "  0.1000000E+02"   # rounding carries into the exponent
+    assert f(1.5e-120) == "  0.1500000-119"   # three exponent digits drop the E
+    rng = np.random.default_rng(0)
+    for v in rng.standard_normal(200) * 10.0 ** rng.integers(-30, 30, 200):
+        s = f(v)
+        assert len(s) == 15
+        assert abs(float(s.replace("E", "e")) - v) <= 5.1e-7 * abs(v)  # 7 significant digits
+
+
+def test_oracle_out1d_matches_numpy(oracle_mod, tmp_path):
+    """out1d (output.f90:34-125): plane averages with the field's spacings (out1d.h90) over the block
+    lengths, against a numpy restatement, and the text file they are written to."""
+    from snac_gb300 import capi
+    case = cases.channel_4block(nx=(16, 32), ny=(8, 16), nz=16)
+    O = oracle_mod.OracleDomain(case)
+    try:
+        rng = np.random.default_rng(14)
+        for k in (capi.U, capi.V, capi.W, capi.P):
+            O.field(1, k)[...] = rng.standard_normal(O.field(1, k).shape)
+        b = case.blocks[1]
+        l = [b.lmax[a] - b.lmin[a] for a in range(3)]
+        for k in (capi.U, capi.V, capi.W, capi.P):
+            stag = [k - capi.U == a if k <= capi.W else False for a in range(3)]
+            dl = [O.grid(1, a, oracle_mod.G_DXC if stag[a] else oracle_mod.G_DXF)[1:-1] for a in range(3)]
+            xg = [O.grid(1, a, oracle_mod.G_XF if stag[a] else oracle_mod.G_XC)[1:-1] for a in range(3)]
+            f = O.field(1, k)[1:-1, 1:-1, 1:-1]
+            for idir in (1, 2, 3):
+                x, p = O.out1d(1, k, idir, fname=tmp_path / f"p{k}{idir}.out")
+                t = [a for a in range(3) if a != idir - 1]
+                wa = dl[t[0]].reshape([-1 if a == t[0] else 1 for a in range(3)])
+                wb = dl[t[1]].reshape([-1 if a == t[1] else 1 for a in range(3)])
+                ref = (f * wa * wb / (l[t[0]] * l[t[1]])).sum(axis=tuple(t))
+                np.testing.assert_allclose(p, ref, rtol=1e-12, atol=1e-14)
+                np.testing.assert_array_equal(x, xg[idir - 1])
+                lines = open(tmp_path / f"p{k}{idir}.out").read().splitlines()
+                assert len(lines) == len(p) and all(len(s) == 30 for s in lines)
+                vals = np.array([[float(s[:15]), float(s[15:])] for s in lines])
+                np.testing.assert_allclose(vals[:, 1], p, rtol=1e-6, atol=1e-7 * np.max(np.abs(p)))
+    finally:
+        O.close()
