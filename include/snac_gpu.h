@@ -121,6 +121,13 @@ typedef struct snac_step_stats {
   double helm_residual_max;   /* IMPDIFF: largest final relative residual of those solves */
 } snac_step_stats;
 
+/* param.f90:88-240: reads dns.nml (&dns, &scalar, &hypre) and blocks.nml (&blocks) with the reference's
+ * defaults into c and blocks[0..nblocks-1] (room for max_blocks).  The reference's build flags are
+ * arguments: fft_axis (FFT_AXIS 0..3), impdiff (_IMPDIFF), boussinesq (_BOUSSINESQ_BUOYANCY).  Host only;
+ * grid files and block_dims (the MPI split of a block) are not read. */
+int snac_read_namelists(const char *dns_path, const char *blocks_path, int fft_axis, int impdiff, int boussinesq,
+                        snac_case *c, snac_block_desc *blocks, int max_blocks);
+
 /* ---------------------------------------------------------------- errors, diagnostics */
 const char *snac_last_error(void);
 int snac_device_count(int *n);

@@ -111,6 +111,8 @@ PROTOTYPES = {
     "snac_chkdiv_all": (C.c_int, [DP, DP]),
     "snac_kinetic_energy": (C.c_int, [DP]),
     "snac_step": (C.c_int, [C.c_int]),
+    "snac_read_namelists": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.POINTER(CaseDesc),
+                                      C.POINTER(BlockDesc), C.c_int]),
     "snac_checkpoint_save": (C.c_int, [C.c_char_p]),
     "snac_checkpoint_load": (C.c_int, [C.c_char_p]),
     "snac_out1d": (C.c_int, [C.c_int, C.c_int, C.c_int, DP, DP]),
