@@ -159,6 +159,7 @@ int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, c
   if (nchunk_bx) *nchunk_bx = 0;
   trace("vcycle: enter level", st);
   if ((fuse & 2) && !P.mode3d && l >= P.cta_level[prec]) return launch_vcycle_coarse<T>(P, l, shift, active, x, b, st);
+  if ((fuse & 2) && P.mode3d && l >= P.cta_level[prec]) return launch_vcycle_coarse3d<T>(P, G, l, shift, active, x, b, st);
   if (l == P.nlev - 1) {
     if (LA<T>::dinv(L)) {
       k_dense<T><<<P.nsys, 256, 0, st>>>(L, active, x, b), ::snac::count_launch();

@@ -457,6 +457,139 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P
   for (int c = threadIdx.x; c < n; c += blockDim.x) xout[(long)n * s + c] = X(l0)[c];
 }
 
+// ---------------------------------------------------------------- 3-D coarse end of a V-cycle in one CTA
+// 3-D mode has one system, so its coarse levels (and the 160 half-sweeps of an iterative coarsest level)
+// would be launch after launch of a few hundred cells.  Here one CTA of 1024 threads runs the V-cycle from
+// level l0 down and back with x and b of every level in shared memory; the operator (shared by every
+// system, L2-resident) is read from global memory.  Same arithmetic as k_rbgs, k_resid_restrict,
+// k_prolong and k_dense, term by term.
+
+// cells of a 3-D index space of extents m[3] visited by COARSE_THREADS threads without a division per cell
+struct Walk3 {
+  int a[3], s[3], m[3];
+  __device__ void start(int m0, int m1, int m2) {
+    m[0] = m0; m[1] = m1; m[2] = m2;
+    const int t = threadIdx.x, S = COARSE_THREADS;
+    a[0] = t % m0; a[1] = (t / m0) % m1; a[2] = t / (m0 * m1);
+    s[0] = S % m0; s[1] = (S / m0) % m1; s[2] = S / (m0 * m1);
+  }
+  __device__ bool ok() const { return a[2] < m[2]; }
+  __device__ void next() {
+    a[0] += s[0];
+    if (a[0] >= m[0]) { a[0] -= m[0]; a[1]++; }
+    a[1] += s[1];
+    if (a[1] >= m[1]) { a[1] -= m[1]; a[2]++; }
+    a[2] += s[2];
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ void cta_sweep3(const MgLevelD &L, const MgGeom &G, T sh, T *x, const T *b, int color) {
+  const int n0 = L.n[0], h0 = (n0 + 1) >> 1;
+  Walk3 w;
+  for (w.start(h0, L.n[1], L.n[2]); w.ok(); w.next()) {
+    const int j = w.a[1], k = w.a[2], i = 2 * w.a[0] + ((color + j + k) & 1);
+    if (i >= n0) continue;
+    const int c = i + n0 * (j + L.n[1] * k);
+    if (L.code[c] & 0x8000) continue;
+    const T d = diag_of<T>(L, G, sh, c);
+    const T acc = offdiag<T>(L, G, [&](int e) { return x[e]; }, c, i, j, k);
+    x[c] = (b[c] - acc) * rcpt(d);
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse3d(MgProblem P, MgGeom G, int l0,
+                                                                       const T *__restrict__ shift,
+                                                                       const int *__restrict__ active,
+                                                                       T *__restrict__ xout, const T *__restrict__ bin) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int s = blockIdx.x;
+  if (active && !active[s]) return;
+  const int last = P.nlev - 1;
+  const bool dense = LA<T>::dinv(P.L[last]) != nullptr;
+  __shared__ int off[MG_MAXLEV];
+  if (threadIdx.x == 0) {
+    int o = 0;
+    for (int l = l0; l < P.nlev; l++) { off[l] = o; o += 2 * (int)P.L[l].ncell; }
+  }
+  __syncthreads();
+  T *const base = (T *)smem_raw;
+  auto X = [&](int l) { return base + off[l]; };
+  auto B = [&](int l) { return base + off[l] + (int)P.L[l].ncell; };
+  const T sh = shift[s];
+  {
+    const int n = (int)P.L[l0].ncell;
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+      B(l0)[c] = bin[(long)n * s + c];
+      X(l0)[c] = 0;
+    }
+  }
+  __syncthreads();
+  for (int l = l0; l < last; l++) {
+    const MgLevelD &F = P.L[l], &C = P.L[l + 1];
+    T *x = X(l);
+    const T *b = B(l);
+    for (int it = 0; it < 2 * P.nu; it++) cta_sweep3<T>(F, G, sh, x, b, it & 1);
+    const int e0 = C.coarsened[0] ? 2 : 1, e1 = C.coarsened[1] ? 2 : 1, e2 = C.coarsened[2] ? 2 : 1;
+    T *bc = B(l + 1), *xc = X(l + 1);
+    Walk3 w;
+    for (w.start(C.n[0], C.n[1], C.n[2]); w.ok(); w.next()) {
+      const int I = w.a[0], J = w.a[1], K = w.a[2];
+      T sum = 0;
+      for (int dk = 0; dk < e2; dk++)
+        for (int dj = 0; dj < e1; dj++)
+          for (int di = 0; di < e0; di++) {
+            const int i = C.coarsened[0] ? 2 * I + di : I, j = C.coarsened[1] ? 2 * J + dj : J,
+                      k = C.coarsened[2] ? 2 * K + dk : K;
+            const int c = i + F.n[0] * (j + F.n[1] * k);
+            if (F.code[c] & 0x8000) continue;
+            const T acc = offdiag<T>(F, G, [&](int e) { return x[e]; }, c, i, j, k);
+            sum += b[c] - fmat(diag_of<T>(F, G, sh, c), x[c], acc);
+          }
+      const int cc = I + C.n[0] * (J + C.n[1] * K);
+      bc[cc] = sum;
+      xc[cc] = 0;
+    }
+    __syncthreads();
+  }
+  {
+    const MgLevelD &L = P.L[last];
+    const int n = (int)L.ncell;
+    if (dense) {
+      const T *__restrict__ M = LA<T>::dinv(L) + (size_t)n * n * s;
+      for (int r = threadIdx.x; r < n; r += blockDim.x) {  // the inverse is stored by columns (as k_dense)
+        T acc = 0;
+#pragma unroll 8
+        for (int c = 0; c < n; c++) acc = fmat(M[(size_t)c * n + r], B(last)[c], acc);
+        X(last)[r] = acc;
+      }
+      __syncthreads();
+    } else {
+      for (int it = 0; it < 40; it++)
+        for (int col = 0; col < 4; col++) cta_sweep3<T>(L, G, sh, X(last), B(last), (col == 1 || col == 2) ? 1 : 0);
+    }
+  }
+  for (int l = last - 1; l >= l0; l--) {
+    const MgLevelD &F = P.L[l], &C = P.L[l + 1];
+    T *x = X(l);
+    const T *xc = X(l + 1);
+    Walk3 w;
+    for (w.start(F.n[0], F.n[1], F.n[2]); w.ok(); w.next()) {
+      const int i = w.a[0], j = w.a[1], k = w.a[2];
+      const int c = i + F.n[0] * (j + F.n[1] * k);
+      if (F.code[c] & 0x8000) continue;
+      const int I = C.coarsened[0] ? i / 2 : i, J = C.coarsened[1] ? j / 2 : j, K = C.coarsened[2] ? k / 2 : k;
+      x[c] += xc[I + C.n[0] * (J + C.n[1] * K)];
+    }
+    __syncthreads();
+    for (int it = 0; it < 2 * P.nu; it++) cta_sweep3<T>(F, G, sh, x, B(l), 1 - (it & 1));
+  }
+  const int n = (int)P.L[l0].ncell;
+  for (int c = threadIdx.x; c < n; c += blockDim.x) xout[(long)n * s + c] = X(l0)[c];
+}
+
 // ---------------------------------------------------------------- launchers
 // opt in to more than 48 KB of dynamic shared memory, once per kernel and device
 static int allow_smem(const void *fn, size_t bytes) {
@@ -540,6 +673,33 @@ int launch_vcycle_coarse(const MgProblem &P, int l0, const T *shift, const int *
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
+
+template <typename T>
+size_t coarse3d_smem_bytes(const MgProblem &P, int l0) {
+  size_t n = 0;
+  for (int l = l0; l < P.nlev; l++) n += 2 * (size_t)P.L[l].ncell;
+  return n * sizeof(T);
+}
+
+template <typename T>
+int launch_vcycle_coarse3d(const MgProblem &P, const MgGeom &G, int l0, const T *shift, const int *active, T *x,
+                           const T *b, cudaStream_t st) {
+  const size_t smem = coarse3d_smem_bytes<T>(P, l0);
+  if (smem > MG_COARSE_SMEM_MAX) { set_error("coarse levels exceed the shared-memory budget"); return SNAC_ERR_ARG; }
+  SNAC_TRY(allow_smem((const void *)k_vcycle_coarse3d<T>, smem));
+  prof_begin(KID_COARSE, st);
+  k_vcycle_coarse3d<T><<<P.nsys, COARSE_THREADS, smem, st>>>(P, G, l0, shift, active, x, b), ::snac::count_launch();
+  prof_end(KID_COARSE, st);
+  SNAC_CUDA(cudaGetLastError());
+  return SNAC_OK;
+}
+
+template size_t coarse3d_smem_bytes<double>(const MgProblem &, int);
+template size_t coarse3d_smem_bytes<float>(const MgProblem &, int);
+template int launch_vcycle_coarse3d<double>(const MgProblem &, const MgGeom &, int, const double *, const int *,
+                                            double *, const double *, cudaStream_t);
+template int launch_vcycle_coarse3d<float>(const MgProblem &, const MgGeom &, int, const float *, const int *, float *,
+                                           const float *, cudaStream_t);
 
 template int launch_rbgs_tile2d<double>(const MgProblem &, int, const int *, int, int, double *, const double *,
                                         const double *, const double *, double *, int, int *, cudaStream_t);

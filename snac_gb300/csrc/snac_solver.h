@@ -46,7 +46,7 @@ struct MgProblem {
   const float *shiftf;
   const int *singular;               // per system, device
   int fused;                         // bits: 1/4 tiled plane smoother FP32/FP64, 2/8 one-CTA coarse tail FP32/FP64
-  int cta_level[2];                  // first level run by k_vcycle_coarse ([0] FP32, [1] FP64); nlev = none
+  int cta_level[2];                  // first level run by k_vcycle_coarse / k_vcycle_coarse3d ([0] FP32, [1] FP64); nlev = none
   int nsm;                           // multiprocessors of the device (sizes the system batches)
   int any_singular;                  // some system is singular (pure Neumann, zero shift)
 };
@@ -60,6 +60,12 @@ int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_c
                        const T *xin, const T *xc, double *part_bx, int part_stride, int *nchunk, cudaStream_t st);
 template <typename T>
 size_t coarse_smem_bytes(const MgProblem &P, int l0);
+struct MgGeom;
+template <typename T>
+size_t coarse3d_smem_bytes(const MgProblem &P, int l0);
+template <typename T>
+int launch_vcycle_coarse3d(const MgProblem &P, const MgGeom &G, int l0, const T *shift, const int *active, T *x,
+                           const T *b, cudaStream_t st);
 constexpr size_t MG_COARSE_SMEM_MAX = 226 * 1024;  // dynamic shared memory of the coarse V-cycle CTA (227 KB at most)
 template <typename T>
 int launch_vcycle_coarse(const MgProblem &P, int l0, const T *shift, const int *active, T *x, const T *b,

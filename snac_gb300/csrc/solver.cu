@@ -605,8 +605,10 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
     P.fused = (e && e[0] && e[0] != '0') ? 0 : (m && m[0]) ? (int)strtol(m, nullptr, 0) & 15 : 11;
     for (int prec = 0; prec < 2; prec++) {
       P.cta_level[prec] = P.nlev;
-      for (int l = 0; l < P.nlev && !S.mode3d; l++) {
-        const size_t bytes = prec ? coarse_smem_bytes<double>(P, l) : coarse_smem_bytes<float>(P, l);
+      for (int l = 0; l < P.nlev; l++) {
+        size_t bytes;
+        if (S.mode3d) bytes = prec ? coarse3d_smem_bytes<double>(P, l) : coarse3d_smem_bytes<float>(P, l);
+        else bytes = prec ? coarse_smem_bytes<double>(P, l) : coarse_smem_bytes<float>(P, l);
         if (bytes <= MG_COARSE_SMEM_MAX) { P.cta_level[prec] = l; break; }
       }
     }
