@@ -431,10 +431,9 @@ __global__ void k_zero_rhs_systems(long n, const SysScal *sc, T *x) {
 
 // singular systems: b -= mean(b) over active cells (two passes, flat chunks)
 template <typename T>
-__global__ void __launch_bounds__(256) k_sum_active(MgLevelD L, const int *singular, const T *b, double *part,
+__global__ void __launch_bounds__(256) k_sum_active(MgLevelD L, const int *sing_list, const T *b, double *part,
                                                     double *partn, int stride) {
-  const int s = blockIdx.y;
-  if (!singular[s]) return;
+  const int s = sing_list[blockIdx.y];  // the singular systems only
   const long base = (long)blockIdx.x * FLAT + threadIdx.x, n = L.ncell;
   double v = 0.0, m = 0.0;
   for (int e = 0; e < FLAT / 256; e++) {
@@ -446,10 +445,9 @@ __global__ void __launch_bounds__(256) k_sum_active(MgLevelD L, const int *singu
   if (threadIdx.x == 0) { part[(long)s * stride + blockIdx.x] = tv; partn[(long)s * stride + blockIdx.x] = tm; }
 }
 template <typename T>
-__global__ void __launch_bounds__(256) k_sub_mean(MgLevelD L, const int *singular, T *b, const double *part,
+__global__ void __launch_bounds__(256) k_sub_mean(MgLevelD L, const int *sing_list, T *b, const double *part,
                                                   const double *partn, int stride, int nchunk) {
-  const int s = blockIdx.y;
-  if (!singular[s]) return;
+  const int s = sing_list[blockIdx.y];
   const double na = cta_sum_parts(partn, s, stride, nchunk);
   const double sm = cta_sum_parts(part, s, stride, nchunk);
   const double mean = na > 0.0 ? sm / na : 0.0;
@@ -611,8 +609,8 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
     MgProblem Pz = P;
     if constexpr (sizeof(T) == 8) { Pz.L[0].b = (double *)r; Pz.L[0].x = (double *)z; }
     else { Pz.L[0].bf = (float *)r; Pz.L[0].xf = (float *)z; }
-    // with singular systems r.z is taken after the projection below, so the V-cycle's own partials are
-    // not asked for
+    // with singular systems r.z is taken after the projection below, by one flat pass over all systems
+    // (cheaper on GB300 than the V-cycle's per-system block reductions of it)
     int nrz = 0;
     SNAC_TRY(mg_vcycle_impl<T>(Pz, G, 0, shift, W.active, P.any_singular ? nullptr : W.part2, W.stride, &nrz, st));
     trace("pcg: V-cycle", st);
@@ -620,8 +618,9 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
       // singular systems: z is taken orthogonal to the constant (the null space), so the search
       // directions carry no constant and x - x0 stays mean-free.  r.z must use the projected z: r's
       // mean is zero only up to rounding, and the V-cycle's constant drift can be large.
-      k_sum_active<T><<<gf, 256, 0, st>>>(L0, P.singular, z, W.part0, W.part1, W.stride), ::snac::count_launch();
-      k_sub_mean<T><<<gf, 256, 0, st>>>(L0, P.singular, z, W.part0, W.part1, W.stride, nflat), ::snac::count_launch();
+      const dim3 gs(gf.x, (unsigned)P.nsing);
+      k_sum_active<T><<<gs, 256, 0, st>>>(L0, P.sing_list, z, W.part0, W.part1, W.stride), ::snac::count_launch();
+      k_sub_mean<T><<<gs, 256, 0, st>>>(L0, P.sing_list, z, W.part0, W.part1, W.stride, nflat), ::snac::count_launch();
     }
     if (nrz == 0) {
       k_cg_dot<T><<<gf, 256, 0, st>>>(n, W.active, r, z, W.part2, W.stride), ::snac::count_launch();
@@ -663,9 +662,9 @@ template int mg_pcg<float>(const MgProblem &, CgWork &, float *, int, double, bo
 int mg_project_singular(const MgProblem &P, CgWork &W, double *b, cudaStream_t st) {
   if (!P.any_singular) return SNAC_OK;
   const long n = P.L[0].ncell;
-  const dim3 g = grid_flat(n, P.nsys);
-  k_sum_active<double><<<g, 256, 0, st>>>(P.L[0], P.singular, b, W.part0, W.part1, W.stride), ::snac::count_launch();
-  k_sub_mean<double><<<g, 256, 0, st>>>(P.L[0], P.singular, b, W.part0, W.part1, W.stride, (int)g.x), ::snac::count_launch();
+  const dim3 g(grid_flat(n, P.nsys).x, (unsigned)P.nsing);
+  k_sum_active<double><<<g, 256, 0, st>>>(P.L[0], P.sing_list, b, W.part0, W.part1, W.stride), ::snac::count_launch();
+  k_sub_mean<double><<<g, 256, 0, st>>>(P.L[0], P.sing_list, b, W.part0, W.part1, W.stride, (int)g.x), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

@@ -49,6 +49,8 @@ struct MgProblem {
   int cta_level[2];                  // first level run by k_vcycle_coarse / k_vcycle_coarse3d ([0] FP32, [1] FP64); nlev = none
   int nsm;                           // multiprocessors of the device (sizes the system batches)
   int any_singular;                  // some system is singular (pure Neumann, zero shift)
+  const int *sing_list;              // device: indices of the singular systems (nsing of them)
+  int nsing;
 };
 
 struct MgGeom;

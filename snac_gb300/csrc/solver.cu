@@ -619,6 +619,13 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
   P.any_singular = 0;
   for (int v : singular) P.any_singular |= v;
   {
+    std::vector<int> list;
+    for (int q = 0; q < S.nsys; q++)
+      if (singular[q]) list.push_back(q);
+    P.nsing = (int)list.size();
+    P.sing_list = list.empty() ? nullptr : (const int *)up(list.data(), list.size() * sizeof(int));
+  }
+  {
     int dev = 0;
     SNAC_CUDA(cudaGetDevice(&dev));
     SNAC_CUDA(cudaDeviceGetAttribute(&P.nsm, cudaDevAttrMultiProcessorCount, dev));
