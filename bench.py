@@ -143,11 +143,14 @@ KERNEL_WORK = {
 }
 
 
+USE_GRAPH = 1  # the mixed path replays its refinement steps as CUDA graphs (bench.py --no-graph: off)
+
+
 def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0):
     from snac_gb300 import capi
     from snac_gb300.domain import Domain
     case = case_fn()
-    dom = Domain(case, precision=precision, device=device)
+    dom = Domain(case, precision=precision, device=device, use_graph=USE_GRAPH if precision else 0)
     try:
         init_channel(dom, case)
         dom.step(warmup, allow_not_converged=True)
@@ -212,7 +215,7 @@ def run_e2e(case_fn, precision, steps, device):
     from snac_gb300 import capi
     from snac_gb300.domain import Domain
     case = case_fn()
-    dom = Domain(case, precision=precision, device=device)
+    dom = Domain(case, precision=precision, device=device, use_graph=USE_GRAPH if precision else 0)
     try:
         init_channel(dom, case)
         dom.step(1, allow_not_converged=True)
@@ -274,9 +277,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--case", choices=["channel", "small"], default="channel",
                     help="channel: the benchmark workload; small: the same layout at test size")
+    ap.add_argument("--no-graph", action="store_true", help="launch the refinement steps one kernel at a time")
     ap.add_argument("--only", choices=["mixed", "plain"], default=None,
                     help="run one path once and print its timing only (used for ncu launch lists)")
     args = ap.parse_args()
+    global USE_GRAPH
+    if args.no_graph:
+        USE_GRAPH = 0
     rank, world, local = dist_env()
     from snac_gb300 import cases
     if args.case == "small":  # the same four-block layout at 48x24x16 (tests of the multi-rank logic)

@@ -105,7 +105,8 @@ typedef struct snac_case {
 /* Library options with no counterpart in the reference. */
 typedef struct snac_options {
   int precision;      /* 0: FP64 multigrid-preconditioned CG; 1: FP32 V-cycles inside FP64 iterative refinement */
-  int use_graph;      /* 1: replay whole steps as CUDA graphs */
+  int use_graph;      /* 1: replay each mixed-precision refinement step (FP32 PCG with its V-cycles) as a
+                         CUDA graph captured once per solver */
   int nu;             /* smoothing sweeps before/after each coarse correction (0 = default 2) */
   int device;         /* CUDA device ordinal */
 } snac_options;

@@ -22,13 +22,17 @@ void set_error(const char *fmt, ...) {
   g_err = buf;
 }
 
-void trace(const char *what, cudaStream_t st) {
+bool trace_on() {
   static int on = -1;
   if (on < 0) {
     const char *e = getenv("SNAC_DEBUG");
     on = (e && e[0] && e[0] != '0') ? 1 : 0;
   }
-  if (!on) return;
+  return on != 0;
+}
+
+void trace(const char *what, cudaStream_t st) {
+  if (!trace_on()) return;
   cudaError_t e = cudaStreamSynchronize(st);
   fprintf(stderr, "[snac] %s: %s\n", what, cudaGetErrorString(e));
   fflush(stderr);

@@ -19,6 +19,8 @@ constexpr int PROF_MAX = 8192;
 
 static std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void add_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+bool prof_active() { return g_prof.kid != 0; }
 
 void prof_begin(int kid, cudaStream_t st) {
   if (g_prof.kid != kid || g_prof.n >= PROF_MAX) return;

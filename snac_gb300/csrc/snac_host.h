@@ -89,6 +89,9 @@ struct PoissonSolver {
   std::vector<double> lambda;
   int precision = 0;
   int inner_iters = 5;               // mixed path: FP32 Krylov iterations per refinement step
+  int use_graph = 0;                 // mixed path: replay each refinement step's FP32 solve as a CUDA graph
+  cudaGraphExec_t inner_exec = nullptr;
+  long long inner_nodes = 0;         // kernel launches in that graph
   double inner_tol = 1e-6;           // mixed path: relative tolerance of the FP32 solve
   double tol = 1e-12;
   int maxiter = 200;

@@ -20,5 +20,8 @@ enum KernelClass {
 
 void prof_begin(int kid, cudaStream_t st);
 void prof_end(int kid, cudaStream_t st);
+bool prof_active();                // a kernel class is being timed (graph replay is then not used)
+void add_launches(long long n);    // launches of a replayed CUDA graph (negative: undo captured ones)
+bool trace_on();                   // SNAC_DEBUG tracing synchronises after every phase (no capture then)
 
 }  // namespace snac

@@ -28,6 +28,7 @@ void *PoissonSolver::alloc(size_t bytes) {
   return p;
 }
 PoissonSolver::~PoissonSolver() {
+  if (inner_exec) cudaGraphExecDestroy(inner_exec);
   for (void *p : allocs) cudaFree(p);
   if (W64.h_count) cudaFreeHost(W64.h_count);
   if (W32.h_count) cudaFreeHost(W32.h_count);
@@ -272,6 +273,7 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
   S.precision = d.opt.precision;
   if (const char *e = getenv("SNAC_MG_INNER")) S.inner_iters = std::max(1, atoi(e));
   if (const char *e = getenv("SNAC_MG_INNER_TOL")) S.inner_tol = atof(e);
+  S.use_graph = d.opt.use_graph ? 1 : 0;
   S.tol = c.tol;
   S.maxiter = c.maxiter;
   S.fft_axis = c.fft_axis;
@@ -688,6 +690,41 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
 }
 
 // FP64: PCG with FP64 V-cycles.  Mixed: FP64 residual / FP32 PCG with FP32 V-cycles / FP64 update.
+// one refinement step of the mixed path: scaled FP32 residual, FP32 PCG with FP32 V-cycles, FP64 update.
+// It has no host synchronisation, so with use_graph it is captured once per solver as a CUDA graph and
+// replayed (every pointer and launch shape is fixed for the solver's lifetime).
+static int refine_step_body(PoissonSolver &S, const CgWork &Wr, cudaStream_t st) {
+  MgProblem &P = S.P;
+  SNAC_TRY(mg_ir_down(P, Wr, S.W32, S.r64, (float *)S.W32.r, S.box_e32, S.inner_tol, st));
+  int it1 = 0;
+  SNAC_TRY(mg_pcg<float>(P, S.W32, S.box_e32, S.inner_iters, S.inner_tol, true, false, &it1, st));
+  SNAC_TRY(mg_ir_up(P, Wr, S.box_e32, S.box_x, st));
+  return SNAC_OK;
+}
+
+static int refine_step(PoissonSolver &S, const CgWork &Wr, cudaStream_t st) {
+  if (!S.use_graph || prof_active() || trace_on()) return refine_step_body(S, Wr, st);
+  if (!S.inner_exec) {
+    long long c0 = 0, c1 = 0;
+    snac_launch_count(&c0);
+    SNAC_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    const int rc = refine_step_body(S, Wr, st);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(st, &g);
+    snac_launch_count(&c1);
+    add_launches(c0 - c1);  // captured, not run
+    if (rc != SNAC_OK) { if (g) cudaGraphDestroy(g); return rc; }
+    if (ce != cudaSuccess) { set_error("stream capture of the refinement step failed: %s", cudaGetErrorString(ce)); return SNAC_ERR_CUDA; }
+    const cudaError_t ie = cudaGraphInstantiate(&S.inner_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) { S.inner_exec = nullptr; set_error("graph instantiation failed: %s", cudaGetErrorString(ie)); return SNAC_ERR_CUDA; }
+    S.inner_nodes = c1 - c0;
+  }
+  SNAC_CUDA(cudaGraphLaunch(S.inner_exec, st));
+  add_launches(S.inner_nodes);
+  return SNAC_OK;
+}
+
 static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *res_out) {
   MgProblem &P = S.P;
   SNAC_TRY(mg_project_singular(P, S.W64, S.box_b, st));
@@ -716,8 +753,6 @@ static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *
     return (worst > S.tol && iters >= S.maxiter) ? SNAC_ERR_NOT_CONVERGED : SNAC_OK;
   }
   // mixed precision: iterative refinement in FP64 around FP32 Krylov solves (zero initial guess)
-  const int inner = S.inner_iters;
-  const double inner_tol = S.inner_tol;
   int outer = 0;
   CgWork Wr = S.W64;  // residual-only use of the FP64 work area
   Wr.active = S.active_outer;
@@ -732,10 +767,7 @@ static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *
     if (outer == 0 && Wr.h_count[1]) SNAC_TRY(mg_zero_rhs_systems(P, Wr, S.box_x, st));
     if (outer == 0) SNAC_TRY(mg_restart_bad_guess(P, Wr, S.box_x, S.box_b, S.r64, st));
     if (Wr.h_count[0] == 0) break;
-    SNAC_TRY(mg_ir_down(P, Wr, S.W32, S.r64, (float *)S.W32.r, S.box_e32, inner_tol, st));
-    int it1 = 0;
-    SNAC_TRY(mg_pcg<float>(P, S.W32, S.box_e32, inner, inner_tol, true, false, &it1, st));
-    SNAC_TRY(mg_ir_up(P, Wr, S.box_e32, S.box_x, st));
+    SNAC_TRY(refine_step(S, Wr, st));
   }
   SNAC_CUDA(cudaMemcpyAsync(sc.data(), S.sc_outer, P.nsys * sizeof(SysScal), cudaMemcpyDeviceToHost, st));
   SNAC_CUDA(cudaStreamSynchronize(st));
