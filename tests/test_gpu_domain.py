@@ -520,3 +520,57 @@ def test_graph_replay_bitwise(snac_lib):
             d.close()
     for a, b in zip(out[0], out[1]):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_100_steps_channel_against_oracle(snac_lib, oracle_mod, precision):
+    """The acceptance criteria on the uneven four-block channel layout (FFT along z, stretched walls):
+    after 100 RK3 steps the velocity and pressure fields are within 1e-10 relative of the oracle's,
+    max|div u| <= 1e-10, and the kinetic energy within 1e-8 relative; for the mixed path (FP32 V-cycles
+    in FP64 refinement) this also states its error against the FP64 path."""
+    case = cases.channel_4block(nx=(16, 32), ny=(8, 16), nz=16)
+    O = oracle_mod.OracleDomain(case)
+    d = Domain(case, precision=precision, use_graph=precision)
+    try:
+        ic = cases.channel_initial_condition(case, lambda ib: O.grid(ib, 1, oracle_mod.G_XC))
+        for ib, (u, v, w) in ic.items():
+            for k, f in ((capi.U, u), (capi.V, v), (capi.W, w)):
+                O.field(ib, k)[...] = f
+                d.set(ib, k, f)
+        for X in (O, d):
+            X.bounduvw(False)
+            X.boundp(capi.P)
+        O.step(100)
+        d.step(100)
+        err_v = compare_fields(case, O, d, (capi.U, capi.V, capi.W), 1e-10)
+        err_p = compare_fields(case, O, d, (capi.P,), 1e-10, mean_free_p=True)
+        assert d.chkdiv()[1] <= 1e-10
+        ke_o, ke_g = O.kinetic_energy(), d.kinetic_energy()
+        assert abs(ke_g - ke_o) <= 1e-8 * ke_o
+        print(f"precision {precision}: max rel. error velocity {err_v:.2e}, pressure {err_p:.2e}")
+    finally:
+        d.close()
+
+
+def test_100_steps_heated_cavity_impdiff_against_oracle(snac_lib, oracle_mod):
+    """100 steps of the stretched heated cavity with IMPDIFF, Boussinesq buoyancy and the 3-D solves
+    (the layout of the 512x512x256 configuration at 16x16x8): fields within 1e-10, divergence <= 1e-10."""
+    case = cases.heated_cavity(n=(16, 16, 8), stretch=1.5, ra=1e6, impdiff=1, tol=1e-12, dt_f=2e-3)
+    O = oracle_mod.OracleDomain(case)
+    d = Domain(case)
+    try:
+        s0 = cases.dhc_initial_scalar(case, lambda ib: O.grid(ib, 0, oracle_mod.G_XC))
+        rng = np.random.default_rng(21)
+        O.field(0, capi.S0)[...] = s0[0] + 1e-3 * rng.uniform(-1, 1, s0[0].shape)
+        d.set(0, capi.S0, O.field(0, capi.S0))
+        for X in (O, d):
+            X.bounduvw(False)
+            X.boundp(capi.P)
+            X.boundp(capi.S0)
+        O.step(100)
+        d.step(100)
+        compare_fields(case, O, d, (capi.U, capi.V, capi.W, capi.S0), 1e-10)
+        compare_fields(case, O, d, (capi.P,), 1e-10, mean_free_p=True)
+        assert d.chkdiv()[1] <= 1e-10
+    finally:
+        d.close()
