@@ -393,6 +393,9 @@ or_poisson *or_poisson_create(or_domain *d, int field, double alpha, const doubl
             cpv[1] = 1.0 / (d1[1][LOCAL(B, 1, g1 + q3[1])]) * dx2 * dz2;
             cmv[2] = 1.0 / (d1[2][LOCAL(B, 2, g2 - 1 + q3[2])]) * dx2 * dy2;
             cpv[2] = 1.0 / (d1[2][LOCAL(B, 2, g2 + q3[2])]) * dx2 * dy2;
+            /* a periodic axis of one cell couples each cell to itself (HYPRE's periodic wrap): the +/- terms cancel */
+            for (int a = 0; a < 3; a++)
+              if (P->periodic[a] && L->n[a] == 1) cmv[a] = cpv[a] = 0.0;
             cc = 0.0;
             cc = cc - (cmv[0] + cpv[0] + cmv[1] + cpv[1] + cmv[2] + cpv[2]) + alpha * weight;
           } else {
@@ -404,6 +407,8 @@ or_poisson *or_poisson_create(or_domain *d, int field, double alpha, const doubl
             cpv[0] = 1.0 / (d1[p1][LOCAL(B, p1, g0 + q3[p1])]) * w2;
             cmv[1] = 1.0 / (d1[p2][LOCAL(B, p2, g1 - 1 + q3[p2])]) * w1;
             cpv[1] = 1.0 / (d1[p2][LOCAL(B, p2, g1 + q3[p2])]) * w1;
+            for (int a = 0; a < 2; a++)
+              if (P->periodic[a] && L->n[a] == 1) cmv[a] = cpv[a] = 0.0;
             cc = -(cmv[0] + cpv[0] + cmv[1] + cpv[1]) + alpha * weight;
           }
           /* boundary folding, solver.f90:298-351 / 786-822 */

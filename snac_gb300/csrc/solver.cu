@@ -393,6 +393,9 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
             cpv[1] = 1.0 / (d1[1][LOC(1, g1 + q3[1])]) * dx2 * dz2;
             cmv[2] = 1.0 / (d1[2][LOC(2, g2 - 1 + q3[2])]) * dx2 * dy2;
             cpv[2] = 1.0 / (d1[2][LOC(2, g2 + q3[2])]) * dx2 * dy2;
+            // a periodic axis of one cell couples each cell to itself: its +/- terms cancel
+            for (int a = 0; a < 3; a++)
+              if (S.periodic[a] && L0.n[a] == 1) cmv[a] = cpv[a] = 0.0;
             cc = 0.0;
             cc = cc - (cmv[0] + cpv[0] + cmv[1] + cpv[1] + cmv[2] + cpv[2]) + alpha * weight;
           } else {
@@ -403,6 +406,8 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
             cpv[0] = 1.0 / (d1[p1][LOC(p1, g0 + q3[p1])]) * w2;
             cmv[1] = 1.0 / (d1[p2][LOC(p2, g1 - 1 + q3[p2])]) * w1;
             cpv[1] = 1.0 / (d1[p2][LOC(p2, g1 + q3[p2])]) * w1;
+            for (int a = 0; a < 2; a++)  // a periodic axis of one cell: the self-couplings cancel
+              if (S.periodic[a] && L0.n[a] == 1) cmv[a] = cpv[a] = 0.0;
             cc = -(cmv[0] + cpv[0] + cmv[1] + cpv[1]) + alpha * weight;
           }
           unsigned short code = 0;
