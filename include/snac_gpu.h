@@ -266,6 +266,12 @@ int snac_out1d_write(const char *fname, int ib, int field, int idir);
 /* out3d (output.f90:227-257): the interior of field f of block ib in Fortran order, FP64, no header */
 int snac_out3d_write(const char *fname, int ib, int field);
 
+/* No counterpart in the reference: one dense 3x3 convolution layer of the learned initial guess on the
+ * tensor cores (tcgen05, BF16 inputs, FP32 accumulation): y = act(bias + w * x) over nplanes images of
+ * 16 channels x H x W (x rounded to BF16, zero padding, act = ReLU when relu != 0), weights w[16][16][3][3]. */
+int snac_cnn_conv3x3(const float *x, int nplanes, int H, int W, const float *w, const float *bias, int relu,
+                     float *y);
+
 /* whole RK3 steps, main.f90:893-1069 (dt from chkdt every icheck steps) */
 int snac_step(int nsteps);
 int snac_get_stats(snac_step_stats *st);

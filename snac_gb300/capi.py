@@ -58,6 +58,7 @@ class StepStats(C.Structure):
 
 _lib = None
 DP = C.POINTER(C.c_double)
+FP = C.POINTER(C.c_float)
 IP = C.POINTER(C.c_int)
 
 # every entry point declared in include/snac_gpu.h with its ctypes signature
@@ -116,6 +117,7 @@ PROTOTYPES = {
     "snac_checkpoint_save": (C.c_int, [C.c_char_p]),
     "snac_checkpoint_load": (C.c_int, [C.c_char_p]),
     "snac_out1d": (C.c_int, [C.c_int, C.c_int, C.c_int, DP, DP]),
+    "snac_cnn_conv3x3": (C.c_int, [FP, C.c_int, C.c_int, C.c_int, FP, FP, C.c_int, FP]),
     "snac_out1d_write": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int]),
     "snac_out3d_write": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
     "snac_get_stats": (C.c_int, [C.POINTER(StepStats)]),
