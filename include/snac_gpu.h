@@ -272,6 +272,25 @@ int snac_out3d_write(const char *fname, int ib, int field);
 int snac_cnn_conv3x3(const float *x, int nplanes, int H, int W, const float *w, const float *bias, int relu,
                      float *y);
 
+/* No counterpart in the reference: forward and backward of the learned-guess network (three 3x3 layers of
+ * 16 channels, ReLU between them) on host data, for checking its gradients: x nb x 16 x H x W, target
+ * nb x H x W, params 3 x (16*16*9 weights + 16 biases); returns the loss
+ * (1/nb) sum_p |y_p - t_p|^2 / |t_p|^2 and its gradient with respect to every parameter. */
+int snac_guess_grad(const float *x, const float *target, int nb, int H, int W, const float *params, float *grads,
+                    double *loss);
+
+/* No counterpart in the reference: the learned initial guess of the plane-mode pressure solve.  mode 0 off;
+ * 1 every pressure solve of snac_step records its (residual of the previous solution, correction) pairs
+ * for training; 2 every solve starts from the previous solution plus the network's correction (the
+ * multigrid then iterates to the same tolerance).  Not available with the 3-D solve (SNAC_ERR_UNSUPPORTED). */
+int snac_guess_mode(int mode);
+/* trains the network on the recorded pairs on the GPU: iters Adam steps of 16-plane batches at learning
+ * rate lr; returns the mean batch loss of the first and last few steps and the number of recorded pairs */
+int snac_guess_train(int iters, double lr, double *loss_first, double *loss_last, int *pairs);
+/* with on != 0 every guided solve also measures |b - A x0| / |b - A x_prev| per non-singular system; returns
+ * the median and largest ratio of the last guided solve */
+int snac_guess_measure(int on, double *ratio_median, double *ratio_max);
+
 /* whole RK3 steps, main.f90:893-1069 (dt from chkdt every icheck steps) */
 int snac_step(int nsteps);
 int snac_get_stats(snac_step_stats *st);

@@ -118,6 +118,10 @@ PROTOTYPES = {
     "snac_checkpoint_load": (C.c_int, [C.c_char_p]),
     "snac_out1d": (C.c_int, [C.c_int, C.c_int, C.c_int, DP, DP]),
     "snac_cnn_conv3x3": (C.c_int, [FP, C.c_int, C.c_int, C.c_int, FP, FP, C.c_int, FP]),
+    "snac_guess_grad": (C.c_int, [FP, FP, C.c_int, C.c_int, C.c_int, FP, FP, DP]),
+    "snac_guess_mode": (C.c_int, [C.c_int]),
+    "snac_guess_train": (C.c_int, [C.c_int, C.c_double, DP, DP, IP]),
+    "snac_guess_measure": (C.c_int, [C.c_int, DP, DP]),
     "snac_out1d_write": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int]),
     "snac_out3d_write": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
     "snac_get_stats": (C.c_int, [C.POINTER(StepStats)]),

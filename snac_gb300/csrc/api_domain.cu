@@ -28,6 +28,7 @@ void *Domain::alloc(size_t bytes) {
   return p;
 }
 Domain::~Domain() {
+  if (guess) guess_destroy(guess);
   ps.reset();
   for (auto &h : hs) h.reset();
   for (void *p : allocs) cudaFree(p);

@@ -45,10 +45,11 @@ __device__ __forceinline__ int core_off(int r, int k) { return (((r >> 3) * 2 + 
 }  // namespace
 
 // y[p][co][h][w] = act(bias[co] + sum_{ci,dy,dx} w[co][ci][dy][dx] x[p][ci][h+dy-1][w+dx-1]) with zero
-// padding; x BF16, weights given in FP32 and rounded to BF16 here, y FP32 (and BF16 copy when yb)
+// padding; x BF16, weights given in FP32 and rounded to BF16 here; y FP32 for the first ny output channels
+// (none when y is null) and the BF16 copy of all 16 when yb
 __global__ void __launch_bounds__(CNN_M) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ x, int H, int W,
                                                       const float *__restrict__ wts, const float *__restrict__ bias,
-                                                      int relu, float *__restrict__ y,
+                                                      int relu, float *__restrict__ y, int ny,
                                                       __nv_bfloat16 *__restrict__ yb, int *__restrict__ err) {
   __shared__ __align__(128) unsigned char sa[CNN_TAPS * CNN_M * CNN_C * 2];  // 36 KB of A blocks
   __shared__ __align__(128) unsigned char sb[CNN_TAPS * CNN_C * CNN_C * 2];  // 4.5 KB of B blocks
@@ -127,7 +128,7 @@ __global__ void __launch_bounds__(CNN_M) k_conv3x3_tc(const __nv_bfloat16 *__res
         float v = __uint_as_float(r[n]) + bias[n];
         if (relu) v = fmaxf(v, 0.f);
         const long o = (long)p * CNN_C * plane + (long)n * plane + (long)h * W + ww;
-        y[o] = v;
+        if (y && n < ny) y[o] = v;
         if (yb) yb[o] = __float2bfloat16(v);
       }
     }
@@ -140,9 +141,9 @@ __global__ void __launch_bounds__(CNN_M) k_conv3x3_tc(const __nv_bfloat16 *__res
 }
 
 int launch_conv3x3_tc(const __nv_bfloat16 *x, int nplanes, int H, int W, const float *wts, const float *bias, int relu,
-                      float *y, __nv_bfloat16 *yb, int *err, cudaStream_t st) {
+                      float *y, int ny, __nv_bfloat16 *yb, int *err, cudaStream_t st) {
   const dim3 g((unsigned)((W + CNN_M - 1) / CNN_M), (unsigned)H, (unsigned)nplanes);
-  k_conv3x3_tc<<<g, CNN_M, 0, st>>>(x, H, W, wts, bias, relu, y, yb, err), ::snac::count_launch();
+  k_conv3x3_tc<<<g, CNN_M, 0, st>>>(x, H, W, wts, bias, relu, y, ny, yb, err), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -172,7 +173,7 @@ int snac_cnn_conv3x3(const float *x, int nplanes, int H, int W, const float *wts
     cudaMemcpy(dw, wts, 16 * 16 * 9 * 4, cudaMemcpyHostToDevice);
     cudaMemcpy(db, bias, 16 * 4, cudaMemcpyHostToDevice);
     cudaMemset(derr, 0, sizeof(int));
-    rc = launch_conv3x3_tc(dx, nplanes, H, W, dw, db, relu, dy, nullptr, derr, 0);
+    rc = launch_conv3x3_tc(dx, nplanes, H, W, dw, db, relu, dy, CNN_C, nullptr, derr, 0);
     if (rc == SNAC_OK) {
       if (cudaDeviceSynchronize() != cudaSuccess) fail(cudaGetErrorString(cudaGetLastError()));
       else {

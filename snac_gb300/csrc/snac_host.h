@@ -64,6 +64,8 @@ inline int field_hi(const HostBlock &H, int field, int p) {
 }
 
 struct HelmBlk;  // per-block tables of a Helmholtz solver (k_helm.cu)
+struct GuessState;  // the learned initial guess (k_guess.cu)
+void guess_destroy(GuessState *g);
 
 // the device multigrid problem plus its host-side construction data
 struct PoissonSolver {
@@ -136,6 +138,7 @@ struct Domain {
   double *d_part = nullptr, *d_red = nullptr, *h_red = nullptr;
   std::unique_ptr<PoissonSolver> ps;
   std::unique_ptr<PoissonSolver> hs[3 + SNAC_MAX_SCAL];  // IMPDIFF: Helmholtz solvers of u, v, w, scalars
+  GuessState *guess = nullptr;       // learned initial guess of the pressure solve (off unless requested)
   double dt = 0.0, time = 0.0;
   int istep = 0;
   int last_solve_iters = 0, solves = 0;
@@ -160,6 +163,8 @@ int helm_rhs(Domain &d, PoissonSolver &S, double alphai, cudaStream_t st);
 int helm_shift(PoissonSolver &S, double alphai, cudaStream_t st);
 int helm_io(Domain &d, PoissonSolver &S, double *box, int to_box, cudaStream_t st);
 int solver_solve_pressure(Domain &d, PoissonSolver &S);
+int guess_before(Domain &d, PoissonSolver &S, cudaStream_t st);
+int guess_after(Domain &d, PoissonSolver &S, cudaStream_t st);
 
 // transforms (k_fft.cu)
 int fft_forward_to_box(Domain &d, PoissonSolver &S, cudaStream_t st);

@@ -815,9 +815,11 @@ int solver_solve_pressure(Domain &d, PoissonSolver &S) {
   if (S.fft_axis) SNAC_TRY(fft_forward_to_box(d, S, st));
   else SNAC_TRY(box_gather(d, S, st));
   trace("solve: forward transform / gather", st);
+  if (d.guess) SNAC_TRY(guess_before(d, S, st));
   int it = 0;
   double res = 0.0;
   const int rc = solve_box(S, st, &it, &res);
+  if (d.guess && (rc == SNAC_OK || rc == SNAC_ERR_NOT_CONVERGED)) SNAC_TRY(guess_after(d, S, st));
   trace("solve: box solve", st);
   if (rc != SNAC_OK && rc != SNAC_ERR_NOT_CONVERGED) return rc;
   if (S.fft_axis) SNAC_TRY(fft_backward_from_box(d, S, st));
