@@ -21,6 +21,7 @@
 // Both follow the arithmetic of k_rbgs / k_resid_restrict / k_prolong / k_dense
 // term by term, so fused and unfused V-cycles give identical results.
 #include <algorithm>
+#include <cstdlib>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -44,8 +45,9 @@ inline int tile_by(TileShape t) { return t.nw * t.r - 2 * TH; }
 inline int tiles_for(const MgLevelD &L, TileShape t) {
   return ((L.n[0] + TBX - 1) / TBX) * ((L.n[1] + tile_by(t) - 1) / tile_by(t));
 }
-// the shape that processes the fewest tile rows (ties: the smaller tile)
+// the shape that processes the fewest tile rows (ties: the smaller tile; SNAC_MG_TILE_TALL=1: the taller)
 TileShape choose_shape(const MgLevelD &L, int prec) {
+  static const bool tall = [] { const char *e = getenv("SNAC_MG_TILE_TALL"); return e && e[0] == '1'; }();
   const TileShape *opts = prec ? SHAPES_D : SHAPES_F;
   const int nopt = prec ? 1 : 4;
   TileShape best = opts[0];
@@ -53,7 +55,7 @@ TileShape choose_shape(const MgLevelD &L, int prec) {
   for (int q = 0; q < nopt; q++) {
     const TileShape t = opts[q];
     const long cost = (long)((L.n[1] + tile_by(t) - 1) / tile_by(t)) * t.nw * t.r;
-    if (bestc < 0 || cost < bestc) { bestc = cost; best = t; }
+    if (bestc < 0 || cost < bestc || (tall && cost == bestc)) { bestc = cost; best = t; }
   }
   return best;
 }
@@ -77,57 +79,72 @@ bool tile2d_ok(const MgProblem &P, int l, int prec) {
   return true;
 }
 
-// dynamic shared memory of one tile CTA: the even/odd x tile and two stages of the staged inputs
-// (b and 1/d; in mode 1 also the pre-smoothed x and the coarse correction), [stage][array][row][64]
+// shared-memory row of the even/odd x tile: 32 column pairs plus a zero pad on each side, so that the
+// edge lanes read a zero neighbour instead of testing their lane
+constexpr int TRS = 34;
+
+// dynamic shared memory of one tile CTA: the even/odd x tile (SH rows plus a zero pad row above and
+// below) and two stages of the staged inputs (b and 1/d; in mode 1 also the pre-smoothed x and the coarse
+// correction), [stage][array][row][64]
 template <typename T>
 inline size_t tile_smem_bytes(int sh, int mode) {
-  return (2 * (size_t)sh * 32 + 2 * (size_t)(mode == 1 ? 4 : 2) * sh * 64) * sizeof(T);
+  return (2 * (size_t)(sh + 2) * TRS + 2 * (size_t)(mode == 1 ? 4 : 2) * sh * 64) * sizeof(T);
 }
 
-template <typename T, int NW, int R>
+// Every per-cell address, mask and coupling is set up once per CTA and reused for all its systems.  The
+// cells on the tile's outermost ring are updated with zero neighbours from the pads; like any cell within
+// TH of the tile edge they may differ from a global sweep, and none of them is stored.
+template <typename T, int NW, int R, int MODE>
 __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C, int per0, int per1,
                                                          const int *__restrict__ active, int nsys, int sb,
-                                                         int first_color, int nhalf, int mode, T *__restrict__ x,
+                                                         int first_color, int nhalf, T *__restrict__ x,
                                                          const T *__restrict__ b, const T *__restrict__ xin,
                                                          const T *__restrict__ xc, double *__restrict__ part_bx,
                                                          int part_stride) {
+  static_assert(NW % 2 == 0, "rows w + NW q of a thread must share their colour parity");
   constexpr int SH = NW * R, BY = SH - 2 * TH;
+  constexpr int NA = MODE == 1 ? 4 : 2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T(*xe)[32] = reinterpret_cast<T(*)[32]>(smem_raw);
-  T(*xo)[32] = xe + SH;
-  T *const stg = reinterpret_cast<T *>(smem_raw) + 2 * SH * 32;
-  const int NA = mode == 1 ? 4 : 2;
-  auto S = [&](int k, int a, int r) -> T * { return stg + ((size_t)(k * NA + a) * SH + r) * 64; };
+  T *const xe = reinterpret_cast<T *>(smem_raw);  // [SH + 2][TRS], tile row r at r + 1, pair l at l + 1
+  T *const xo = xe + (SH + 2) * TRS;
+  T *const stg = xo + (SH + 2) * TRS;
   const int n0 = L.n[0], n1 = L.n[1];
   const int ntx = (n0 + TBX - 1) / TBX;
   const int i0 = (int)(blockIdx.x % ntx) * TBX - TH, j0 = (int)(blockIdx.x / ntx) * BY - TH;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const bool skip0 = per0 && n0 == 1, skip1 = per1 && n1 == 1;
+  for (int e = threadIdx.x; e < 2 * (SH + 2) * TRS; e += NW * 32) xe[e] = T(0);  // pads stay zero
   // wrapped global coordinates of the owned cells (-1: outside a non-periodic boundary); with n0 even
   // and i0 even the pair (2 lane, 2 lane + 1) is never split by a boundary or a wrap
-  int gi0, gj[R];
+  int gi0;
   {
     const int g = i0 + 2 * lane;
     gi0 = (g >= 0 && g < n0) ? g : (per0 ? wrap(g, n0) : -1);
   }
-#pragma unroll
-  for (int q = 0; q < R; q++) {
-    const int g = j0 + w + NW * q;
-    gj[q] = (g >= 0 && g < n1) ? g : (per1 ? wrap(g, n1) : -1);
-  }
-  // couplings of the owned cells, the same for every system; bit 2q+p of `live`: active cell
+  int cidx[R];          // global index of the even cell of the owned pair of row q (0 when outside)
+  int cidxc[R];         // mode 1: index of the coarse cell of that pair
+  unsigned live = 0;    // bit 2q+p: active cell
+  unsigned inb = 0;     // bit q: the pair of row q lies inside the level (staged from global memory)
+  unsigned store = 0;   // bit 2q+p: an output cell of this tile
   const T *__restrict__ cp0 = LA<T>::cp(L, 0);
   const T *__restrict__ cp1 = LA<T>::cp(L, 1);
   const T *__restrict__ invd = LA<T>::invd(L);
+  const bool xhalf = C.coarsened[0] != 0, yhalf = C.coarsened[1] != 0;
   T ce[R][2], cw[R][2], cn[R][2], cs[R][2];
-  unsigned live = 0;
 #pragma unroll
   for (int q = 0; q < R; q++) {
+    const int r = w + NW * q;
+    const int g = j0 + r;
+    const int gj = (g >= 0 && g < n1) ? g : (per1 ? wrap(g, n1) : -1);
+    const bool in = gi0 >= 0 && gj >= 0;
+    cidx[q] = in ? gi0 + n0 * gj : 0;
+    cidxc[q] = in ? (xhalf ? gi0 / 2 : gi0) + C.n[0] * (yhalf ? gj / 2 : gj) : 0;
+    if (in) inb |= 1u << q;
 #pragma unroll
     for (int p = 0; p < 2; p++) {
       T e_ = 0, w_ = 0, n_ = 0, s_ = 0;
-      if (gi0 >= 0 && gj[q] >= 0) {
-        const int ii = gi0 + p, jj = gj[q], c = ii + n0 * jj;
+      if (in) {
+        const int ii = gi0 + p, c = cidx[q] + p;
         if (!(L.code[c] & 0x8000)) {
           live |= 1u << (2 * q + p);
           if (!skip0) {
@@ -136,7 +153,7 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
           }
           if (!skip1) {
             n_ = cp1[c];
-            s_ = jj > 0 ? cp1[c - n0] : (per1 ? cp1[c + n0 * (n1 - 1)] : T(0));
+            s_ = gj > 0 ? cp1[c - n0] : (per1 ? cp1[c + n0 * (n1 - 1)] : T(0));
           }
         }
       }
@@ -144,24 +161,31 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
       cw[q][p] = w_;
       cn[q][p] = n_;
       cs[q][p] = s_;
+      // unwrapped: each global cell is stored by one tile only (stored cells are never wrapped)
+      const int col = 2 * lane + p, ui = i0 + col, uj = j0 + r;
+      if (r >= TH && r < TH + BY && col >= TH && col < TH + TBX && ui < n0 && uj < n1 && (live >> (2 * q + p) & 1))
+        store |= 1u << (2 * q + p);
     }
   }
+  // this thread's cells in the tile and the staging area
+  const int tpos = (w + 1) * TRS + lane + 1;  // row q adds (NW * q) * TRS
+  const int spos = w * 64 + 2 * lane;         // row q adds (NW * q) * 64; array a of stage k adds (k * NA + a) * SH * 64
+  // parity of the even column of the owned pairs (the same for every row of this thread, NW being even)
+  const int par = (i0 + j0 + w) & 1;
   // stage the inputs of system `sys` (each thread copies exactly the cells it owns)
-  const bool xhalf = C.coarsened[0] != 0, yhalf = C.coarsened[1] != 0;
   auto issue = [&](int sys, int k) {
     const long off = L.ncell * (long)sys, offc = C.ncell * (long)sys;
+    T *sk = stg + (size_t)k * NA * SH * 64 + spos;
 #pragma unroll
     for (int q = 0; q < R; q++) {
-      const int r = w + NW * q;
-      const bool in = gi0 >= 0 && gj[q] >= 0;
-      const long c = in ? (long)gi0 + (long)n0 * gj[q] : 0;
-      cp_async_zfill<2 * sizeof(T)>(S(k, 0, r) + 2 * lane, b + off + c, in);
-      cp_async_zfill<2 * sizeof(T)>(S(k, 1, r) + 2 * lane, invd + off + c, in);
-      if (mode == 1) {
-        cp_async_zfill<2 * sizeof(T)>(S(k, 2, r) + 2 * lane, xin + off + c, in);
-        const long cc = in ? (long)(xhalf ? gi0 / 2 : gi0) + (long)C.n[0] * (yhalf ? gj[q] / 2 : gj[q]) : 0;
-        if (xhalf) cp_async_zfill<sizeof(T)>(S(k, 3, r) + 2 * lane, xc + offc + cc, in);
-        else cp_async_zfill<2 * sizeof(T)>(S(k, 3, r) + 2 * lane, xc + offc + cc, in);
+      const bool in = inb >> q & 1;
+      T *sq = sk + NW * q * 64;
+      cp_async_zfill<2 * sizeof(T)>(sq, b + off + cidx[q], in);
+      cp_async_zfill<2 * sizeof(T)>(sq + SH * 64, invd + off + cidx[q], in);
+      if (MODE == 1) {
+        cp_async_zfill<2 * sizeof(T)>(sq + 2 * SH * 64, xin + off + cidx[q], in);
+        if (xhalf) cp_async_zfill<sizeof(T)>(sq + 3 * SH * 64, xc + offc + cidxc[q], in);
+        else cp_async_zfill<2 * sizeof(T)>(sq + 3 * SH * 64, xc + offc + cidxc[q], in);
       }
     }
     cp_async_commit();
@@ -184,45 +208,47 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
     } else {
       cp_async_wait<0>();
     }
-    __syncthreads();  // the previous system's sweeps have finished with the x tile
+    __syncthreads();  // the staged inputs are complete and the previous system's sweeps are over
     T bv[R][2], iv[R][2];
+    {
+      const T *sk = stg + (size_t)k * NA * SH * 64 + spos;
 #pragma unroll
-    for (int q = 0; q < R; q++) {
-      const int r = w + NW * q;
+      for (int q = 0; q < R; q++) {
+        const T *sq = sk + NW * q * 64;
 #pragma unroll
-      for (int p = 0; p < 2; p++) {
-        const bool lv = live >> (2 * q + p) & 1;
-        bv[q][p] = lv ? S(k, 0, r)[2 * lane + p] : T(0);
-        iv[q][p] = lv ? S(k, 1, r)[2 * lane + p] : T(0);
-        T x_ = 0;
-        if (mode == 1 && lv) x_ = S(k, 2, r)[2 * lane + p] + S(k, 3, r)[2 * lane + (xhalf ? 0 : p)];
-        if (p) xo[r][lane] = x_;
-        else xe[r][lane] = x_;
+        for (int p = 0; p < 2; p++) {
+          const bool lv = live >> (2 * q + p) & 1;
+          bv[q][p] = lv ? sq[p] : T(0);
+          iv[q][p] = lv ? sq[SH * 64 + p] : T(0);
+          T x_ = 0;
+          if (MODE == 1 && lv) x_ = sq[2 * SH * 64 + p] + sq[3 * SH * 64 + (xhalf ? 0 : p)];
+          (p ? xo : xe)[tpos + NW * q * TRS] = x_;
+        }
       }
     }
     for (int t = 0; t < nhalf; t++) {
       __syncthreads();
-      const int color = (first_color + t) & 1;
+      if (((first_color + t + par) & 1) == 0) {  // even columns 2 lane: E = odd(lane), W = odd(lane - 1)
 #pragma unroll
-      for (int q = 0; q < R; q++) {
-        const int r = w + NW * q;
-        if (r == 0 || r == SH - 1) continue;
-        if (((color + i0 + j0 + r) & 1) == 0) {  // even column 2*lane: E = odd(lane), W = odd(lane-1)
-          const T xE = xo[r][lane];
-          const T xW = lane > 0 ? xo[r][lane - 1] : T(0);
-          T acc = fmat(ce[q][0], xE, T(0));
-          acc = fmat(cw[q][0], xW, acc);
-          acc = fmat(cn[q][0], xe[r + 1][lane], acc);
-          acc = fmat(cs[q][0], xe[r - 1][lane], acc);
-          if (lane > 0) xe[r][lane] = (bv[q][0] - acc) * iv[q][0];
-        } else {                                  // odd column 2*lane+1: E = even(lane+1), W = even(lane)
-          const T xE = lane < 31 ? xe[r][lane + 1] : T(0);
-          const T xW = xe[r][lane];
-          T acc = fmat(ce[q][1], xE, T(0));
-          acc = fmat(cw[q][1], xW, acc);
-          acc = fmat(cn[q][1], xo[r + 1][lane], acc);
-          acc = fmat(cs[q][1], xo[r - 1][lane], acc);
-          if (lane < 31) xo[r][lane] = (bv[q][1] - acc) * iv[q][1];
+        for (int q = 0; q < R; q++) {
+          T *o = xe + tpos + NW * q * TRS;
+          const T *e = xo + tpos + NW * q * TRS;
+          T acc = fmat(ce[q][0], e[0], T(0));
+          acc = fmat(cw[q][0], e[-1], acc);
+          acc = fmat(cn[q][0], o[TRS], acc);
+          acc = fmat(cs[q][0], o[-TRS], acc);
+          o[0] = (bv[q][0] - acc) * iv[q][0];
+        }
+      } else {                                   // odd columns 2 lane + 1: E = even(lane + 1), W = even(lane)
+#pragma unroll
+        for (int q = 0; q < R; q++) {
+          T *o = xo + tpos + NW * q * TRS;
+          const T *e = xe + tpos + NW * q * TRS;
+          T acc = fmat(ce[q][1], e[1], T(0));
+          acc = fmat(cw[q][1], e[0], acc);
+          acc = fmat(cn[q][1], o[TRS], acc);
+          acc = fmat(cs[q][1], o[-TRS], acc);
+          o[0] = (bv[q][1] - acc) * iv[q][1];
         }
       }
     }
@@ -231,15 +257,11 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
     T bx = 0;
 #pragma unroll
     for (int q = 0; q < R; q++) {
-      const int r = w + NW * q;
 #pragma unroll
       for (int p = 0; p < 2; p++) {
-        const int col = 2 * lane + p;
-        if (r < TH || r >= TH + BY || col < TH || col >= TH + TBX) continue;
-        const int ui = i0 + col, uj = j0 + r;  // unwrapped: each global cell is stored by one tile only
-        if (ui >= n0 || uj >= n1 || !(live >> (2 * q + p) & 1)) continue;
-        const T v = p ? xo[r][lane] : xe[r][lane];
-        x[off + ui + n0 * uj] = v;
+        if (!(store >> (2 * q + p) & 1)) continue;
+        const T v = (p ? xo : xe)[tpos + NW * q * TRS];
+        x[off + cidx[q] + p] = v;
         bx = fmat(bv[q][p], v, bx);
       }
     }
@@ -611,11 +633,17 @@ static int launch_tile(const MgProblem &P, const MgLevelD &L, const MgLevelD &C,
                        int first_color, int mode, T *x, const T *b, const T *xin, const T *xc, double *part_bx,
                        int part_stride, cudaStream_t st) {
   const size_t smem = tile_smem_bytes<T>(NW * R, mode);
-  SNAC_TRY(allow_smem((const void *)k_rbgs_tile2d<T, NW, R>, smem));
   const int sb = plane_batch(P, nt, NW == 16 ? 2 : 4);
   const dim3 g((unsigned)nt, (unsigned)((P.nsys + sb - 1) / sb));
-  k_rbgs_tile2d<T, NW, R><<<g, NW * 32, smem, st>>>(L, C, P.periodic[0], P.periodic[1], active, P.nsys, sb,
-                                                    first_color, 2 * P.nu, mode, x, b, xin, xc, part_bx, part_stride), ::snac::count_launch();
+  if (mode == 1) {
+    SNAC_TRY(allow_smem((const void *)k_rbgs_tile2d<T, NW, R, 1>, smem));
+    k_rbgs_tile2d<T, NW, R, 1><<<g, NW * 32, smem, st>>>(L, C, P.periodic[0], P.periodic[1], active, P.nsys, sb,
+                                                         first_color, 2 * P.nu, x, b, xin, xc, part_bx, part_stride), ::snac::count_launch();
+  } else {
+    SNAC_TRY(allow_smem((const void *)k_rbgs_tile2d<T, NW, R, 0>, smem));
+    k_rbgs_tile2d<T, NW, R, 0><<<g, NW * 32, smem, st>>>(L, C, P.periodic[0], P.periodic[1], active, P.nsys, sb,
+                                                         first_color, 2 * P.nu, x, b, xin, xc, part_bx, part_stride), ::snac::count_launch();
+  }
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

@@ -610,9 +610,12 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
     const char *e = getenv("SNAC_MG_UNFUSED");
     const char *m = getenv("SNAC_MG_FUSE");
     P.fused = (e && e[0] && e[0] != '0') ? 0 : (m && m[0]) ? (int)strtol(m, nullptr, 0) & 15 : 11;
+    // SNAC_MG_CTA_LEVEL: the finest level the one-CTA coarse tail may start at (default 0: the finest that fits)
+    const char *cl = getenv("SNAC_MG_CTA_LEVEL");
+    const int lmin = cl && cl[0] ? std::max(0, atoi(cl)) : 0;
     for (int prec = 0; prec < 2; prec++) {
       P.cta_level[prec] = P.nlev;
-      for (int l = 0; l < P.nlev; l++) {
+      for (int l = lmin; l < P.nlev; l++) {
         size_t bytes;
         if (S.mode3d) bytes = prec ? coarse3d_smem_bytes<double>(P, l) : coarse3d_smem_bytes<float>(P, l);
         else bytes = prec ? coarse_smem_bytes<double>(P, l) : coarse_smem_bytes<float>(P, l);
