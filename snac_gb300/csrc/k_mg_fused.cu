@@ -366,9 +366,15 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P
   auto X = [&](int l) { return base + plan.lev[l].ox; };
   auto B = [&](int l) { return base + plan.lev[l].ob; };
   auto ID = [&](int l) { return base + plan.lev[l].oi; };
-  auto C0 = [&](int l) -> const T * { return plan.lev[l].oc >= 0 ? base + plan.lev[l].oc : LA<T>::cp(P.L[l], 0); };
-  auto C1 = [&](int l) -> const T * {
-    return plan.lev[l].oc >= 0 ? base + plan.lev[l].oc + (int)P.L[l].ncell : LA<T>::cp(P.L[l], 1);
+  // f(c0, c1) with the couplings of level l: two inlined copies, one reading shared memory and one global
+  // memory, so that neither goes through generic loads
+  auto with_c = [&](int l, auto &&f) {
+    if (plan.lev[l].oc >= 0) {
+      const T *c0 = base + plan.lev[l].oc;
+      f(c0, c0 + (int)P.L[l].ncell);
+    } else {
+      f(LA<T>::cp(P.L[l], 0), LA<T>::cp(P.L[l], 1));
+    }
   };
   const T sh = shift[s];
   for (int l = l0; l < P.nlev; l++) {
@@ -404,31 +410,33 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P
     const CoarseLev &E = plan.lev[l], &EC = plan.lev[l + 1];
     const int n0 = L.n[0], n1 = L.n[1];
     T *x = X(l);
-    const T *b = B(l), *id = ID(l), *c0 = C0(l), *c1 = C1(l);
+    const T *b = B(l), *id = ID(l);
     const T *__restrict__ cc = LA<T>::cc(L);
     const T *__restrict__ w01 = LA<T>::w01(L);
-    for (int it = 0; it < 2 * P.nu; it++) cta_sweep_xy<T>(n0, n1, per0, per1, x, b, id, c0, c1, it & 1, E.hdj, E.hdi);
-    const int cn0 = C.n[0], cn1 = C.n[1];
-    const int e0 = C.coarsened[0] ? 2 : 1, e1 = C.coarsened[1] ? 2 : 1;
-    T *bc = B(l + 1), *xc = X(l + 1);
-    int J = (int)threadIdx.x / cn0, I = (int)threadIdx.x - J * cn0;
-    while (J < cn1) {
-      T sum = 0;
-      for (int dj = 0; dj < e1; dj++)
-        for (int di = 0; di < e0; di++) {
-          const int i = C.coarsened[0] ? 2 * I + di : I, j = C.coarsened[1] ? 2 * J + dj : J;
-          const int c = i + n0 * j;
-          if (id[c] == T(0)) continue;
-          const T dv = fmat(sh, w01[c], cc[c]);  // the diagonal of the unfused residual, term by term
-          const T acc = offdiag_xy<T>(n0, n1, per0, per1, c0, c1, [&](int e) { return x[e]; }, c, i, j);
-          sum += b[c] - fmat(dv, x[c], acc);
-        }
-      bc[I + cn0 * J] = sum;
-      xc[I + cn0 * J] = 0;
-      I += EC.fdi;
-      J += EC.fdj;
-      if (I >= cn0) { I -= cn0; J++; }
-    }
+    with_c(l, [&](const T *c0, const T *c1) {
+      for (int it = 0; it < 2 * P.nu; it++) cta_sweep_xy<T>(n0, n1, per0, per1, x, b, id, c0, c1, it & 1, E.hdj, E.hdi);
+      const int cn0 = C.n[0], cn1 = C.n[1];
+      const int e0 = C.coarsened[0] ? 2 : 1, e1 = C.coarsened[1] ? 2 : 1;
+      T *bc = B(l + 1), *xc = X(l + 1);
+      int J = (int)threadIdx.x / cn0, I = (int)threadIdx.x - J * cn0;
+      while (J < cn1) {
+        T sum = 0;
+        for (int dj = 0; dj < e1; dj++)
+          for (int di = 0; di < e0; di++) {
+            const int i = C.coarsened[0] ? 2 * I + di : I, j = C.coarsened[1] ? 2 * J + dj : J;
+            const int c = i + n0 * j;
+            if (id[c] == T(0)) continue;
+            const T dv = fmat(sh, w01[c], cc[c]);  // the diagonal of the unfused residual, term by term
+            const T acc = offdiag_xy<T>(n0, n1, per0, per1, c0, c1, [&](int e) { return x[e]; }, c, i, j);
+            sum += b[c] - fmat(dv, x[c], acc);
+          }
+        bc[I + cn0 * J] = sum;
+        xc[I + cn0 * J] = 0;
+        I += EC.fdi;
+        J += EC.fdj;
+        if (I >= cn0) { I -= cn0; J++; }
+      }
+    });
     __syncthreads();
   }
   // coarsest level
@@ -446,10 +454,12 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P
       __syncthreads();
     } else {
       const CoarseLev &E = plan.lev[last];
-      for (int it = 0; it < 40; it++)
-        for (int col = 0; col < 4; col++)
-          cta_sweep_xy<T>(L.n[0], L.n[1], per0, per1, X(last), B(last), ID(last), C0(last), C1(last),
-                          (col == 1 || col == 2) ? 1 : 0, E.hdj, E.hdi);
+      with_c(last, [&](const T *c0, const T *c1) {
+        for (int it = 0; it < 40; it++)
+          for (int col = 0; col < 4; col++)
+            cta_sweep_xy<T>(L.n[0], L.n[1], per0, per1, X(last), B(last), ID(last), c0, c1,
+                            (col == 1 || col == 2) ? 1 : 0, E.hdj, E.hdi);
+      });
     }
   }
   // up: prolongation and post-smoothing
@@ -472,8 +482,10 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P
       if (i >= n0) { i -= n0; j++; }
     }
     __syncthreads();
-    for (int it = 0; it < 2 * P.nu; it++)
-      cta_sweep_xy<T>(n0, n1, per0, per1, x, B(l), id, C0(l), C1(l), 1 - (it & 1), E.hdj, E.hdi);
+    with_c(l, [&](const T *c0, const T *c1) {
+      for (int it = 0; it < 2 * P.nu; it++)
+        cta_sweep_xy<T>(n0, n1, per0, per1, x, B(l), id, c0, c1, 1 - (it & 1), E.hdj, E.hdi);
+    });
   }
   const int n = (int)P.L[l0].ncell;
   for (int c = threadIdx.x; c < n; c += blockDim.x) xout[(long)n * s + c] = X(l0)[c];
