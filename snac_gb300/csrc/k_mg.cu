@@ -281,6 +281,45 @@ __device__ __forceinline__ double cta_sum_parts(const double *part, int s, int s
   return tot;
 }
 
+// partial dot a.b (flat) with the projection of b folded in: for a singular system b -= mean(b) over its
+// active cells first (the mean from the k_sum_active partials; the same rounding as k_sub_mean), written
+// back, and the dot taken with the projected b
+template <typename T>
+__global__ void __launch_bounds__(256) k_cg_dot_proj(MgLevelD L, const int *active, const int *singular,
+                                                     const T *a, T *b, double *part, int stride,
+                                                     const double *part_s, const double *part_n, int nchunk_s) {
+  const int s = blockIdx.y;
+  if (active && !active[s]) return;
+  const long n = L.ncell;
+  const long base = (long)blockIdx.x * FLAT + threadIdx.x, o = n * s;
+  T v = 0;
+  if (singular[s]) {
+    const double na = cta_sum_parts(part_n, s, stride, nchunk_s);
+    const double sm = cta_sum_parts(part_s, s, stride, nchunk_s);
+    const T mean = (T)(na > 0.0 ? sm / na : 0.0);
+#pragma unroll
+    for (int e = 0; e < FLAT / 256; e++) {
+      const long c = base + 256 * e;
+      if (c < n) {
+        T bv = b[o + c];
+        if (!(L.code[c] & 0x8000)) {
+          bv -= mean;
+          b[o + c] = bv;
+        }
+        v = fmat(a[o + c], bv, v);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < FLAT / 256; e++) {
+      const long c = base + 256 * e;
+      if (c < n) v = fmat(a[o + c], b[o + c], v);
+    }
+  }
+  const double t = block_sum1<T>(v);
+  if (threadIdx.x == 0) part[(long)s * stride + blockIdx.x] = t;
+}
+
 // rz = sum of the r.z partials; beta = rz / rz_old (0 on the first iteration); one CTA per system
 __global__ void k_cg_beta(const int *active, SysScal *sc, const double *part, int stride, int n) {
   const int s = blockIdx.x;
@@ -510,6 +549,8 @@ __global__ void k_set_active(int nsys, int *active, const int *src) {
   template __global__ void k_cg_resid<T>(MgLevelD, MgGeom, const T *, const int *, const T *, const T *, T *,        \
                                          double *, double *, int);                                                   \
   template __global__ void k_cg_dot<T>(long, const int *, const T *, const T *, double *, int);                      \
+  template __global__ void k_cg_dot_proj<T>(MgLevelD, const int *, const int *, const T *, T *, double *, int,      \
+                                            const double *, const double *, int);                                    \
   template __global__ void k_cg_p<T>(long, const int *, const SysScal *, const T *, T *);                            \
   template __global__ void k_cg_apply<T, true>(MgLevelD, MgGeom, const T *, const int *, const SysScal *, const T *, \
                                                const T *, T *, T *, double *, int);                                  \
@@ -618,9 +659,12 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
       // singular systems: z is taken orthogonal to the constant (the null space), so the search
       // directions carry no constant and x - x0 stays mean-free.  r.z must use the projected z: r's
       // mean is zero only up to rounding, and the V-cycle's constant drift can be large.
+      // (the subtraction itself is folded into the dot pass that follows)
       const dim3 gs(gf.x, (unsigned)P.nsing);
       k_sum_active<T><<<gs, 256, 0, st>>>(L0, P.sing_list, z, W.part0, W.part1, W.stride), ::snac::count_launch();
-      k_sub_mean<T><<<gs, 256, 0, st>>>(L0, P.sing_list, z, W.part0, W.part1, W.stride, nflat), ::snac::count_launch();
+      k_cg_dot_proj<T><<<gf, 256, 0, st>>>(L0, W.active, P.singular, r, z, W.part2, W.stride, W.part0, W.part1, nflat),
+          ::snac::count_launch();
+      nrz = nflat;
     }
     if (nrz == 0) {
       k_cg_dot<T><<<gf, 256, 0, st>>>(n, W.active, r, z, W.part2, W.stride), ::snac::count_launch();
