@@ -109,6 +109,8 @@ typedef struct snac_options {
                          CUDA graph captured once per solver */
   int nu;             /* smoothing sweeps before/after each coarse correction (0 = default 2) */
   int device;         /* CUDA device ordinal */
+  int nu_coarse;      /* smoothing sweeps per side on multigrid levels 2 and coarser (0 = default: 1 with a
+                         transform axis, nu for a 3-D solve) */
 } snac_options;
 
 typedef struct snac_step_stats {

@@ -47,7 +47,8 @@ class CaseDesc(C.Structure):
 
 
 class Options(C.Structure):
-    _fields_ = [("precision", C.c_int), ("use_graph", C.c_int), ("nu", C.c_int), ("device", C.c_int)]
+    _fields_ = [("precision", C.c_int), ("use_graph", C.c_int), ("nu", C.c_int), ("device", C.c_int),
+                ("nu_coarse", C.c_int)]
 
 
 class StepStats(C.Structure):

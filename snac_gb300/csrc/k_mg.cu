@@ -190,14 +190,14 @@ int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, c
     k_zero<T><<<g, 256, 0, st>>>(L.ncell, x, P.nsys, active), ::snac::count_launch();
   }
   if (!P.mode3d) {  // plane systems: kernels batched over systems
-    for (int it = 0; it < 2 * P.nu; it++) SNAC_TRY(plane_sweep<T>(P, l, shift, active, it & 1, x, b, st));
+    for (int it = 0; it < 2 * mg_nu(P, l); it++) SNAC_TRY(plane_sweep<T>(P, l, shift, active, it & 1, x, b, st));
     SNAC_TRY(plane_restrict<T>(P, l, shift, active, x, b, LA<T>::b(C), LA<T>::x(C), st));
     SNAC_TRY(mg_vcycle_impl<T>(P, G, l + 1, shift, active, nullptr, 0, nullptr, st));
     SNAC_TRY(plane_prolong<T>(P, l, active, x, LA<T>::x(C), st));
-    for (int it = 0; it < 2 * P.nu; it++) SNAC_TRY(plane_sweep<T>(P, l, shift, active, 1 - (it & 1), x, b, st));
+    for (int it = 0; it < 2 * mg_nu(P, l); it++) SNAC_TRY(plane_sweep<T>(P, l, shift, active, 1 - (it & 1), x, b, st));
     return SNAC_OK;
   }
-  for (int it = 0; it < 2 * P.nu; it++) {
+  for (int it = 0; it < 2 * mg_nu(P, l); it++) {
     prof_begin(KID_RBGS, st);
     k_rbgs<T><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, it & 1, x, b), ::snac::count_launch();
     prof_end(KID_RBGS, st);
@@ -208,7 +208,7 @@ int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, c
   SNAC_CUDA(cudaGetLastError());
   SNAC_TRY(mg_vcycle_impl<T>(P, G, l + 1, shift, active, nullptr, 0, nullptr, st));
   k_prolong<T><<<grid_cell(P, L), BLK, 0, st>>>(L, C, G, active, x, LA<T>::x(C)), ::snac::count_launch();
-  for (int it = 0; it < 2 * P.nu; it++) {
+  for (int it = 0; it < 2 * mg_nu(P, l); it++) {
     prof_begin(KID_RBGS, st);
     k_rbgs<T><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, 1 - (it & 1), x, b), ::snac::count_launch();
     prof_end(KID_RBGS, st);

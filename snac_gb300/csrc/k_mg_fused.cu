@@ -70,7 +70,7 @@ int tile2d_max_tiles(const MgLevelD &L) { return tiles_for(L, TileShape{8, 2}); 
 
 bool tile2d_ok(const MgProblem &P, int l, int prec) {
   (void)prec;
-  if (P.mode3d || l >= P.nlev - 1 || 2 * P.nu > TH) return false;
+  if (P.mode3d || l >= P.nlev - 1 || 2 * mg_nu(P, l) > TH) return false;
   const MgLevelD &L = P.L[l];
   if (!L.xp || !L.xpf || !L.invd || !L.invdf) return false;
   if (L.n[0] & 1) return false;  // column pairs are copied as one aligned unit
@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P
     const T *__restrict__ cc = LA<T>::cc(L);
     const T *__restrict__ w01 = LA<T>::w01(L);
     with_c(l, [&](const T *c0, const T *c1) {
-      for (int it = 0; it < 2 * P.nu; it++) cta_sweep_xy<T>(n0, n1, per0, per1, x, b, id, c0, c1, it & 1, E.hdj, E.hdi);
+      for (int it = 0; it < 2 * mg_nu(P, l); it++) cta_sweep_xy<T>(n0, n1, per0, per1, x, b, id, c0, c1, it & 1, E.hdj, E.hdi);
       const int cn0 = C.n[0], cn1 = C.n[1];
       const int e0 = C.coarsened[0] ? 2 : 1, e1 = C.coarsened[1] ? 2 : 1;
       T *bc = B(l + 1), *xc = X(l + 1);
@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P
     }
     __syncthreads();
     with_c(l, [&](const T *c0, const T *c1) {
-      for (int it = 0; it < 2 * P.nu; it++)
+      for (int it = 0; it < 2 * mg_nu(P, l); it++)
         cta_sweep_xy<T>(n0, n1, per0, per1, x, B(l), id, c0, c1, 1 - (it & 1), E.hdj, E.hdi);
     });
   }
@@ -565,7 +565,7 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse3d(MgProblem
     const MgLevelD &F = P.L[l], &C = P.L[l + 1];
     T *x = X(l);
     const T *b = B(l);
-    for (int it = 0; it < 2 * P.nu; it++) cta_sweep3<T>(F, G, sh, x, b, it & 1);
+    for (int it = 0; it < 2 * mg_nu(P, l); it++) cta_sweep3<T>(F, G, sh, x, b, it & 1);
     const int e0 = C.coarsened[0] ? 2 : 1, e1 = C.coarsened[1] ? 2 : 1, e2 = C.coarsened[2] ? 2 : 1;
     T *bc = B(l + 1), *xc = X(l + 1);
     Walk3 w;
@@ -618,7 +618,7 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse3d(MgProblem
       x[c] += xc[I + C.n[0] * (J + C.n[1] * K)];
     }
     __syncthreads();
-    for (int it = 0; it < 2 * P.nu; it++) cta_sweep3<T>(F, G, sh, x, B(l), 1 - (it & 1));
+    for (int it = 0; it < 2 * mg_nu(P, l); it++) cta_sweep3<T>(F, G, sh, x, B(l), 1 - (it & 1));
   }
   const int n = (int)P.L[l0].ncell;
   for (int c = threadIdx.x; c < n; c += blockDim.x) xout[(long)n * s + c] = X(l0)[c];
@@ -641,7 +641,7 @@ static int allow_smem(const void *fn, size_t bytes) {
 }
 
 template <typename T, int NW, int R>
-static int launch_tile(const MgProblem &P, const MgLevelD &L, const MgLevelD &C, int nt, const int *active,
+static int launch_tile(const MgProblem &P, const MgLevelD &L, const MgLevelD &C, int nt, int nhalf, const int *active,
                        int first_color, int mode, T *x, const T *b, const T *xin, const T *xc, double *part_bx,
                        int part_stride, cudaStream_t st) {
   const size_t smem = tile_smem_bytes<T>(NW * R, mode);
@@ -650,11 +650,11 @@ static int launch_tile(const MgProblem &P, const MgLevelD &L, const MgLevelD &C,
   if (mode == 1) {
     SNAC_TRY(allow_smem((const void *)k_rbgs_tile2d<T, NW, R, 1>, smem));
     k_rbgs_tile2d<T, NW, R, 1><<<g, NW * 32, smem, st>>>(L, C, P.periodic[0], P.periodic[1], active, P.nsys, sb,
-                                                         first_color, 2 * P.nu, x, b, xin, xc, part_bx, part_stride), ::snac::count_launch();
+                                                         first_color, nhalf, x, b, xin, xc, part_bx, part_stride), ::snac::count_launch();
   } else {
     SNAC_TRY(allow_smem((const void *)k_rbgs_tile2d<T, NW, R, 0>, smem));
     k_rbgs_tile2d<T, NW, R, 0><<<g, NW * 32, smem, st>>>(L, C, P.periodic[0], P.periodic[1], active, P.nsys, sb,
-                                                         first_color, 2 * P.nu, x, b, xin, xc, part_bx, part_stride), ::snac::count_launch();
+                                                         first_color, nhalf, x, b, xin, xc, part_bx, part_stride), ::snac::count_launch();
   }
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -672,16 +672,16 @@ int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_c
   prof_begin(KID_RBGS, st);
   int rc;
   if constexpr (sizeof(T) == 8) {
-    rc = launch_tile<T, 8, 2>(P, L, C, nt, active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
+    rc = launch_tile<T, 8, 2>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
   } else {
     if (t.nw == 8 && t.r == 2)
-      rc = launch_tile<T, 8, 2>(P, L, C, nt, active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
+      rc = launch_tile<T, 8, 2>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
     else if (t.nw == 16 && t.r == 2)
-      rc = launch_tile<T, 16, 2>(P, L, C, nt, active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
+      rc = launch_tile<T, 16, 2>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
     else if (t.nw == 8)
-      rc = launch_tile<T, 8, 3>(P, L, C, nt, active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
+      rc = launch_tile<T, 8, 3>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
     else
-      rc = launch_tile<T, 16, 3>(P, L, C, nt, active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
+      rc = launch_tile<T, 16, 3>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
   }
   prof_end(KID_RBGS, st);
   SNAC_TRY(rc);

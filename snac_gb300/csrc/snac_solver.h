@@ -40,7 +40,9 @@ struct MgProblem {
   int periodic[3];
   int nsys;
   int nlev;
-  int nu;
+  int nu;                            // smoothing sweeps per side on levels < lnu
+  int nu_coarse;                     // and on levels >= lnu
+  int lnu;
   MgLevelD L[MG_MAXLEV];
   const double *shift;               // per system (lambda_k), device
   const float *shiftf;
@@ -52,6 +54,9 @@ struct MgProblem {
   const int *sing_list;              // device: indices of the singular systems (nsing of them)
   int nsing;
 };
+// smoothing sweeps per side of the V-cycle on level l
+__host__ __device__ inline int mg_nu(const MgProblem &P, int l) { return l >= P.lnu ? P.nu_coarse : P.nu; }
+
 
 struct MgGeom;
 // fused kernels (k_mg_fused.cu)

@@ -554,6 +554,10 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
   P.nsys = S.nsys;
   P.nlev = (int)B.L.size();
   P.nu = d.opt.nu > 0 ? d.opt.nu : 2;
+  // levels from 2 down: one sweep per side in plane mode (the tiled levels 0 and 1 keep nu; on the
+  // channel this halves the one-CTA coarse V-cycle at the same refinement-step count), nu in 3-D mode
+  P.lnu = 2;
+  P.nu_coarse = d.opt.nu_coarse > 0 ? d.opt.nu_coarse : (S.mode3d ? P.nu : 1);
   auto up = [&](const void *src, size_t bytes) -> void * {
     void *p = S.alloc(bytes ? bytes : 8);
     if (p && bytes) cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);

@@ -17,11 +17,12 @@ from .capi import check, dptr
 
 
 class Domain:
-    def __init__(self, case, precision: int = 0, nu: int = 0, device: int = 0, use_graph: int = 0):
+    def __init__(self, case, precision: int = 0, nu: int = 0, device: int = 0, use_graph: int = 0, nu_coarse: int = 0):
         L = capi.lib()
         self.case = case
         c, arr, keep = capi.fill_descs(case)
-        opt = capi.Options(precision=int(precision), use_graph=int(use_graph), nu=int(nu), device=int(device))
+        opt = capi.Options(precision=int(precision), use_graph=int(use_graph), nu=int(nu), device=int(device),
+                           nu_coarse=int(nu_coarse))
         check(L.snac_init(C.byref(c), arr, C.byref(opt)))
         self._keep = keep
         self.nblocks = len(case.blocks)
