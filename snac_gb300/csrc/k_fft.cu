@@ -22,17 +22,18 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 
 __device__ __forceinline__ int bitrev(int q, int logn) { return (int)(__brev((unsigned)q) >> (32 - logn)); }
 
-// in-place radix-2 DIT FFT (exp(-i...)) of npair complex lines of length n held in bit-reversed order
+// in-place radix-2 DIT FFT (exp(-i...)) of npair complex lines of length n = 2^logn held in bit-reversed
+// order (index arithmetic by shifts and masks)
 __device__ void fft_pairs(double2 *zb, int npair, int n, int logn, const double2 *__restrict__ tw) {
-  const int half = n >> 1;
-  for (int h = 1; h < n; h <<= 1) {
+  const int half = n >> 1, lhalf = logn - 1;
+  for (int lh = 0; lh < logn; lh++) {
     __syncthreads();
-    const int step = n / (2 * h);
-    for (int t = threadIdx.x; t < npair * half; t += blockDim.x) {
-      const int p = t / half, b = t - p * half;
-      const int grp = b / h, k = b - grp * h;
-      const int i0 = grp * 2 * h + k, i1 = i0 + h;
-      const double2 w = tw[k * step];
+    const int h = 1 << lh, lstep = lhalf - lh;  // twiddle stride n / (2 h)
+    for (int t = threadIdx.x; t < (npair << lhalf); t += blockDim.x) {
+      const int p = t >> lhalf, b = t & (half - 1);
+      const int grp = b >> lh, k = b & (h - 1);
+      const int i0 = (grp << (lh + 1)) + k, i1 = i0 + h;
+      const double2 w = tw[k << lstep];
       double2 *z = zb + p * n;
       const double2 x0 = z[i0], t1 = cmul(w, z[i1]);
       z[i0] = make_double2(x0.x + t1.x, x0.y + t1.y);
@@ -66,12 +67,12 @@ __device__ void transform_smem(int kind, int n, int use_fft, int logn, const dou
   __syncthreads();
   if (kind == SNAC_R2HC) {
     for (int t = threadIdx.x; t < npair * n; t += blockDim.x) {
-      const int p = t / n, q = t - p * n;
+      const int p = t >> logn, q = t & (n - 1);
       zb[p * n + (logn ? bitrev(q, logn) : 0)] = make_double2(s[(2 * p) * n + q], s[(2 * p + 1) * n + q]);
     }
     fft_pairs(zb, npair, n, logn, tw);
     for (int t = threadIdx.x; t < npair * n; t += blockDim.x) {
-      const int p = t / n, m = t - p * n;
+      const int p = t >> logn, m = t & (n - 1);
       const double2 Zm = zb[p * n + m], Zc = zb[p * n + ((n - m) & (n - 1))];
       double a, b;
       if (2 * m <= n) { a = 0.5 * (Zm.x + Zc.x); b = 0.5 * (Zm.y + Zc.y); }
@@ -81,7 +82,7 @@ __device__ void transform_smem(int kind, int n, int use_fft, int logn, const dou
     }
   } else {  // HC2R
     for (int t = threadIdx.x; t < npair * n; t += blockDim.x) {
-      const int p = t / n, k = t - p * n;
+      const int p = t >> logn, k = t & (n - 1);
       const double *A = s + (2 * p) * n, *B = s + (2 * p + 1) * n;
       const int kk = (2 * k <= n) ? k : n - k;
       const double ra = A[kk], rb = B[kk];
@@ -94,7 +95,7 @@ __device__ void transform_smem(int kind, int n, int use_fft, int logn, const dou
     }
     fft_pairs(zb, npair, n, logn, tw);
     for (int t = threadIdx.x; t < npair * n; t += blockDim.x) {
-      const int p = t / n, q = t - p * n;
+      const int p = t >> logn, q = t & (n - 1);
       const double2 z = zb[p * n + q];
       s[(2 * p) * n + q] = z.x;
       s[(2 * p + 1) * n + q] = -z.y;
@@ -105,7 +106,7 @@ __device__ void transform_smem(int kind, int n, int use_fft, int logn, const dou
 
 struct LineGeom {
   int a, t1, t2;       // transform axis and the two other axes (t1 < t2)
-  int n, logn, use_fft, kind, lp;
+  int n, logn, use_fft, kind, lp, llp;  // lp = 2^llp lines per CTA
   long ncell;          // box cells per system (plane mode)
   int n0;              // box extent along t1
   int field;           // HF_P: pp; HF_U + c: u, v, w; HF_S0 + s: scalar s
@@ -134,32 +135,24 @@ __global__ void k_fft_fwd_box(const DBlock *__restrict__ Bs, const int2 *__restr
   double *s = smem;
   double2 *zb = (double2 *)(smem + g.lp * g.n);
   const int n = g.n;
-  for (int t = threadIdx.x; t < g.lp * n; t += blockDim.x) {
-    const int l = t % g.lp, q = t / g.lp;
-    const int line = lt.y + l;
-    double v = 0.0;
-    if (line < nlines) {
-      int c[3];
-      c[g.a] = q; c[g.t1] = line % n1; c[g.t2] = line / n1;
-      v = f[hidx(c[0], c[1], c[2], B.n[0], B.n[1])];
-    }
-    s[l * n + q] = v;
-  }
+  // the line of this thread is the same in every pass (blockDim.x is a multiple of lp = 2^llp)
+  const int l = threadIdx.x & (g.lp - 1), q0 = threadIdx.x >> g.llp, qs = blockDim.x >> g.llp;
+  const int line = lt.y + l;
+  const bool valid = line < nlines;
+  const int x1 = valid ? line % n1 : 0, x2 = valid ? line / n1 : 0;
+  int c[3];
+  c[g.a] = 0; c[g.t1] = x1; c[g.t2] = x2;
+  const long fb = hidx(c[0], c[1], c[2], B.n[0], B.n[1]);
+  const long fs = g.a == 0 ? 1 : g.a == 1 ? (long)(B.n[0] + 2) : (long)(B.n[0] + 2) * (B.n[1] + 2);
+  for (int q = q0; q < n; q += qs) s[l * n + q] = valid ? f[fb + fs * q] : 0.0;
   transform_smem(g.kind, n, g.use_fft, g.logn, tw, mat, s, zb, g.lp);
+  if (!valid) return;
   const int2 o = boff[lt.x];
-  for (int t = threadIdx.x; t < g.lp * n; t += blockDim.x) {
-    const int l = t % g.lp, q = t / g.lp;
-    const int line = lt.y + l;
-    if (line >= nlines) continue;
-    const int x1 = line % n1, x2 = line / n1;
-    if (x1 < ex.x && x2 < ex.y) {
-      const long cell = (long)(x1 + o.x) + (long)g.n0 * (x2 + o.y);
-      box[cell + g.ncell * q] = s[l * n + q];
-    } else {
-      int c[3];
-      c[g.a] = q; c[g.t1] = x1; c[g.t2] = x2;
-      f[hidx(c[0], c[1], c[2], B.n[0], B.n[1])] = s[l * n + q];
-    }
+  if (x1 < ex.x && x2 < ex.y) {
+    double *__restrict__ bx = box + (long)(x1 + o.x) + (long)g.n0 * (x2 + o.y);
+    for (int q = q0; q < n; q += qs) bx[g.ncell * q] = s[l * n + q];
+  } else {
+    for (int q = q0; q < n; q += qs) f[fb + fs * q] = s[l * n + q];
   }
 }
 
@@ -178,32 +171,22 @@ __global__ void k_fft_bwd_box(const DBlock *__restrict__ Bs, const int2 *__restr
   double2 *zb = (double2 *)(smem + g.lp * g.n);
   const int n = g.n;
   const int2 o = boff[lt.x];
-  for (int t = threadIdx.x; t < g.lp * n; t += blockDim.x) {
-    const int l = t % g.lp, q = t / g.lp;
-    const int line = lt.y + l;
-    double v = 0.0;
-    if (line < nlines) {
-      const int x1 = line % n1, x2 = line / n1;
-      if (x1 < ex.x && x2 < ex.y) {
-        const long cell = (long)(x1 + o.x) + (long)g.n0 * (x2 + o.y);
-        v = box[cell + g.ncell * q];
-      } else {
-        int c[3];
-        c[g.a] = q; c[g.t1] = x1; c[g.t2] = x2;
-        v = f[hidx(c[0], c[1], c[2], B.n[0], B.n[1])];
-      }
-    }
-    s[l * n + q] = v;
-  }
+  const int l = threadIdx.x & (g.lp - 1), q0 = threadIdx.x >> g.llp, qs = blockDim.x >> g.llp;
+  const int line = lt.y + l;
+  const bool valid = line < nlines;
+  const int x1 = valid ? line % n1 : 0, x2 = valid ? line / n1 : 0;
+  int c[3];
+  c[g.a] = 0; c[g.t1] = x1; c[g.t2] = x2;
+  const long fb = hidx(c[0], c[1], c[2], B.n[0], B.n[1]);
+  const long fs = g.a == 0 ? 1 : g.a == 1 ? (long)(B.n[0] + 2) : (long)(B.n[0] + 2) * (B.n[1] + 2);
+  const bool inbox = valid && x1 < ex.x && x2 < ex.y;
+  const double *__restrict__ bx = box + (long)(x1 + o.x) + (long)g.n0 * (x2 + o.y);
+  for (int q = q0; q < n; q += qs) s[l * n + q] = !valid ? 0.0 : inbox ? bx[g.ncell * q] : f[fb + fs * q];
   transform_smem(g.kind, n, g.use_fft, g.logn, tw, mat, s, zb, g.lp);
+  if (!valid) return;
   const int na = B.n[g.a];
-  for (int t = threadIdx.x; t < g.lp * na; t += blockDim.x) {
-    const int l = t % g.lp, q = t / g.lp;
-    const int line = lt.y + l;
-    if (line >= nlines) continue;
-    int c[3];
-    c[g.a] = q; c[g.t1] = line % n1; c[g.t2] = line / n1;
-    double *p = &f[hidx(c[0], c[1], c[2], B.n[0], B.n[1])];
+  for (int q = q0; q < na; q += qs) {
+    double *p = &f[fb + fs * q];
     *p = (q < n ? s[l * n + q] : *p) * normfft;
   }
 }
@@ -242,11 +225,12 @@ __global__ void k_r2r_strided(double *arr, int m1, long s1, long s2, long sa, in
   }
 }
 
+// a power of two from 2 to 16 (the kernels take a thread's line as threadIdx.x mod lp)
 static int lines_per_cta(int n) {
-  int lp = 6144 / (n > 0 ? n : 1);
-  if (lp > 16) lp = 16;
-  if (lp < 2) lp = 2;
-  return lp & ~1;
+  const int cap = 6144 / (n > 0 ? n : 1);
+  int lp = 2;
+  while (lp * 2 <= 16 && lp * 2 <= cap) lp *= 2;
+  return lp;
 }
 static size_t smem_bytes(int n, int lp) { return (size_t)lp * n * sizeof(double) * 2; }
 
@@ -360,6 +344,7 @@ static LineGeom line_geom(const PoissonSolver &S, int kind) {
   g.use_fft = S.use_fft;
   g.kind = kind;
   g.lp = S.lt_lp;
+  g.llp = ilog2(S.lt_lp);
   g.ncell = S.ncell0;
   g.n0 = S.P.L[0].n[0];
   g.field = S.field;
@@ -437,6 +422,7 @@ int r2r_array(int kind, int idir, const int nn[3], int q, double *darr, cudaStre
   g.a = a; g.t1 = t1; g.t2 = t2; g.n = n; g.logn = ilog2(n); g.kind = kind;
   g.use_fft = ((kind == SNAC_R2HC || kind == SNAC_HC2R) && pow2(n)) ? 1 : 0;
   g.lp = lines_per_cta(n);
+  g.llp = ilog2(g.lp);
   g.ncell = 0; g.n0 = 0;
   double *dtw = nullptr, *dmat = nullptr;
   if (g.use_fft) {

@@ -558,6 +558,7 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
   // channel this halves the one-CTA coarse V-cycle at the same refinement-step count), nu in 3-D mode
   P.lnu = 2;
   P.nu_coarse = d.opt.nu_coarse > 0 ? d.opt.nu_coarse : (S.mode3d ? P.nu : 1);
+  if (const char *e = getenv("SNAC_MG_LNU")) P.lnu = std::max(0, atoi(e));  // tuning: first level with nu_coarse
   auto up = [&](const void *src, size_t bytes) -> void * {
     void *p = S.alloc(bytes ? bytes : 8);
     if (p && bytes) cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
