@@ -94,6 +94,11 @@ struct PoissonSolver {
   int use_graph = 0;                 // mixed path: replay each refinement step's FP32 solve as a CUDA graph
   cudaGraphExec_t inner_exec = nullptr;
   long long inner_nodes = 0;         // kernel launches in that graph
+  // mixed path: refinement steps run without reading the active count back, up to the number the previous
+  // solve of this solver needed; each step's residual counts go to their own slot, read once at the end
+  static constexpr int SPEC_MAX = 8;
+  int spec_outer = 0;
+  int *d_ocount = nullptr, *h_ocount = nullptr;  // 2 * SPEC_MAX ints (device, pinned host)
   double inner_tol = 1e-6;           // mixed path: relative tolerance of the FP32 solve
   double tol = 1e-12;
   int maxiter = 200;

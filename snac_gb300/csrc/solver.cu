@@ -32,6 +32,7 @@ PoissonSolver::~PoissonSolver() {
   for (void *p : allocs) cudaFree(p);
   if (W64.h_count) cudaFreeHost(W64.h_count);
   if (W32.h_count) cudaFreeHost(W32.h_count);
+  if (h_ocount) cudaFreeHost(h_ocount);
 }
 
 namespace {
@@ -765,27 +766,59 @@ static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *
     *res_out = worst;
     return (worst > S.tol && iters >= S.maxiter) ? SNAC_ERR_NOT_CONVERGED : SNAC_OK;
   }
-  // mixed precision: iterative refinement in FP64 around FP32 Krylov solves (zero initial guess)
-  int outer = 0;
+  // mixed precision: iterative refinement in FP64 around FP32 Krylov solves (zero initial guess).  The
+  // first `spec` refinement steps run without a host round trip (converged systems are skipped on the
+  // device by their active flags); the counts of every step are read after step `spec`.
+  int outer = 0, needed = -1;
   CgWork Wr = S.W64;  // residual-only use of the FP64 work area
   Wr.active = S.active_outer;
   Wr.sc = S.sc_outer;
+  if (!S.d_ocount) {
+    S.d_ocount = (int *)S.alloc(2 * PoissonSolver::SPEC_MAX * sizeof(int));
+    SNAC_CUDA(cudaMallocHost(&S.h_ocount, 2 * PoissonSolver::SPEC_MAX * sizeof(int)));
+    if (!S.d_ocount) { set_error("device allocation failed (refinement counts)"); return SNAC_ERR_NOMEM; }
+  }
+  const int spec = std::min(S.spec_outer, PoissonSolver::SPEC_MAX - 1);
   SNAC_TRY(mg_set_active(P.nsys, S.active_outer, nullptr, st));
   for (outer = 0; outer < S.maxiter; outer++) {
+    CgWork Wo = Wr;
+    if (outer <= spec) Wo.d_count = S.d_ocount + 2 * outer;
     // r64 = b - A x64 with norms, convergence and the scale of the FP32 residual
-    SNAC_TRY(mg_residual<double>(P, Wr, S.box_x, S.box_b, S.r64, S.tol, outer == 0 ? 1 : 0, 1, S.nact0, st));
-    SNAC_TRY(mg_project_singular(P, Wr, S.r64, st));  // as in the FP64 path: the correction equation stays consistent
-    SNAC_CUDA(cudaMemcpyAsync(Wr.h_count, Wr.d_count, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
-    SNAC_CUDA(cudaStreamSynchronize(st));
-    if (outer == 0 && Wr.h_count[1]) SNAC_TRY(mg_zero_rhs_systems(P, Wr, S.box_x, st));
-    if (outer == 0) SNAC_TRY(mg_restart_bad_guess(P, Wr, S.box_x, S.box_b, S.r64, st));
-    if (Wr.h_count[0] == 0) break;
+    SNAC_TRY(mg_residual<double>(P, Wo, S.box_x, S.box_b, S.r64, S.tol, outer == 0 ? 1 : 0, 1, S.nact0, st));
+    SNAC_TRY(mg_project_singular(P, Wo, S.r64, st));  // as in the FP64 path: the correction equation stays consistent
+    if (outer < spec) {
+      if (outer == 0) {
+        SNAC_TRY(mg_zero_rhs_systems(P, Wo, S.box_x, st));  // a no-op for systems with a right-hand side
+        SNAC_TRY(mg_restart_bad_guess(P, Wo, S.box_x, S.box_b, S.r64, st));
+      }
+      SNAC_TRY(refine_step(S, Wr, st));
+      continue;
+    }
+    int cnt[2];
+    if (outer == spec) {
+      SNAC_CUDA(cudaMemcpyAsync(S.h_ocount, S.d_ocount, 2 * (spec + 1) * sizeof(int), cudaMemcpyDeviceToHost, st));
+      SNAC_CUDA(cudaStreamSynchronize(st));
+      for (int o = 0; o <= spec && needed < 0; o++)
+        if (S.h_ocount[2 * o] == 0) needed = o;
+      cnt[0] = S.h_ocount[2 * spec];
+      cnt[1] = S.h_ocount[2 * spec + 1];
+    } else {
+      SNAC_CUDA(cudaMemcpyAsync(Wo.h_count, Wo.d_count, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+      SNAC_CUDA(cudaStreamSynchronize(st));
+      cnt[0] = Wo.h_count[0];
+      cnt[1] = Wo.h_count[1];
+    }
+    if (outer == 0 && cnt[1]) SNAC_TRY(mg_zero_rhs_systems(P, Wo, S.box_x, st));
+    if (outer == 0) SNAC_TRY(mg_restart_bad_guess(P, Wo, S.box_x, S.box_b, S.r64, st));
+    if (cnt[0] == 0) break;
     SNAC_TRY(refine_step(S, Wr, st));
   }
+  if (needed < 0) needed = outer;
+  S.spec_outer = needed;
   SNAC_CUDA(cudaMemcpyAsync(sc.data(), S.sc_outer, P.nsys * sizeof(SysScal), cudaMemcpyDeviceToHost, st));
   SNAC_CUDA(cudaStreamSynchronize(st));
   for (auto &v : sc) worst = std::max(worst, v.rel);
-  *iters_out = outer;
+  *iters_out = needed;
   *res_out = worst;
   return (outer >= S.maxiter && worst > S.tol) ? SNAC_ERR_NOT_CONVERGED : SNAC_OK;
 }
