@@ -11,8 +11,10 @@ field: laminar Poiseuille profile scaled to U_b plus seeded uniform noise of
 A "step" is one full RK3 step (3 stages: momentum, halo/BC, divergence,
 transform, 128 batched 2-D solves, back-transform, projection, pressure
 update; chkdt every icheck=10 steps).  `value` is the mixed path (FP32 V-cycles
-inside FP64 refinement), the plain FP64 path is reported beside it at the same
-solver tolerance.  Inputs (~0.5 GB of fields + solver vectors) exceed L2.
+inside FP64 refinement); the plain FP64 path and the mixed path with the learned
+initial guess (pairs recorded from 8 steps, the network trained on the GPU, then
+timed) are reported beside it at the same solver tolerance.  Inputs (~0.5 GB of
+fields + solver vectors) exceed L2.
 
 --impl reference times the CPU restatement of the reference (the Fortran/HYPRE
 reference cannot be built on these machines) on the host cores, same case.
@@ -179,6 +181,42 @@ def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0):
         dom.close()
 
 
+def run_learned_path(case_fn, steps, warmup, device, record=8, train_iters=1500, lr=2e-3):
+    """Mixed path with the learned initial guess: pairs recorded from `record` steps after the warm-up, the
+    network trained on the GPU, then `steps` timed steps with the guess applied (and one more that measures
+    the residual it leaves relative to the previous solution's, per wavenumber system)."""
+    from snac_gb300 import capi
+    from snac_gb300.domain import Domain
+    case = case_fn()
+    L = capi.lib()
+    dom = Domain(case, precision=1, device=device, use_graph=USE_GRAPH)
+    try:
+        init_channel(dom, case)
+        dom.step(warmup, allow_not_converged=True)
+        capi.check(L.snac_guess_mode(1))
+        dom.step(record, allow_not_converged=True)
+        lf, ll, npairs = C.c_double(), C.c_double(), C.c_int()
+        t0 = time.time()
+        capi.check(L.snac_guess_train(train_iters, lr, C.byref(lf), C.byref(ll), C.byref(npairs)))
+        train_s = time.time() - t0
+        capi.check(L.snac_guess_mode(2))
+        dom.step(1, allow_not_converged=True)
+        dom.step(steps, allow_not_converged=True)
+        st = dom.stats()
+        capi.check(L.snac_guess_measure(1, None, None))
+        dom.step(1, allow_not_converged=True)
+        med, mx = C.c_double(), C.c_double()
+        capi.check(L.snac_guess_measure(0, C.byref(med), C.byref(mx)))
+        divtot, divmax = dom.chkdiv()
+        return {"ms_per_step": st["device_ms"] / steps, "solve_iters_max": st["iters"],
+                "solve_residual_max": st["residual"], "max_div_u": divmax, "pairs": npairs.value,
+                "train_iters": train_iters, "train_s": train_s, "loss_first": lf.value, "loss_last": ll.value,
+                "residual_ratio_median": med.value, "residual_ratio_max": mx.value}
+    finally:
+        L.snac_guess_mode(0)
+        dom.close()
+
+
 def bench_smoother(case_fn, device, levels=(0, 1, 2), reps=20):
     """CUDA-event timing of the FP32 tiled pre-smoother (the dominant kernel) on the bench workload,
     inputs resident in HBM, all systems active: ms and algorithmic bytes per launch per level."""
@@ -278,6 +316,7 @@ def main():
     ap.add_argument("--case", choices=["channel", "small"], default="channel",
                     help="channel: the benchmark workload; small: the same layout at test size")
     ap.add_argument("--no-graph", action="store_true", help="launch the refinement steps one kernel at a time")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess path (record, train, time)")
     ap.add_argument("--only", choices=["mixed", "plain"], default=None,
                     help="run one path once and print its timing only (used for ncu launch lists)")
     args = ap.parse_args()
@@ -337,6 +376,7 @@ def main():
         shares[name] = {"launches_per_step": n / args.steps, "ms_per_step": tot / args.steps,
                         "mean_launch_ms": tot / max(n, 1)}
     prof_mom = (shares["k_rk_mom"]["launches_per_step"] * args.steps, shares["k_rk_mom"]["ms_per_step"] * args.steps)
+    learned = run_learned_path(case_fn, args.steps, args.warmup, device) if not args.no_learned else None
     smoother = bench_smoother(case_fn, device)
     ms = mixed["ms"]
     ms = max_over_ranks(ms, device)
@@ -398,7 +438,10 @@ def main():
                       "plain_fp64": {"ms_per_step": plain["ms"], "max_div_u": plain["divmax"],
                                      "solve_iters_max": plain["iters"], "solve_residual_max": plain["residual"],
                                      "kinetic_energy": plain["ke"]},
-                      "speedup_mixed_vs_plain": plain["ms"] / mixed["ms"], "learned_guess": "not built"},
+                      "speedup_mixed_vs_plain": plain["ms"] / mixed["ms"],
+                      "learned_mixed": learned,
+                      "headline_path": "mixed (the learned guess is measured beside it and left off: it lowers "
+                                       "the starting residual but not the refinement-step count)"},
             "roofline": roof if roof else roof_mom, "roofline_rk_mom": roof_mom,
             "gpu_launches": mixed["launches"], "gpu_launches_per_step": mixed["launches"] / args.steps,
             "kernels": shares,
