@@ -293,6 +293,21 @@ int snac_guess_train(int iters, double lr, double *loss_first, double *loss_last
  * the median and largest ratio of the last guided solve */
 int snac_guess_measure(int on, double *ratio_median, double *ratio_max);
 
+/* No counterpart in the reference (HYPRE's PFMG settings are fixed in the input): picks the solver settings
+ * for this case by timing.  Every candidate (FP32 Krylov iterations per refinement step 4, 5 or 6 with the
+ * mixed solve; one or two smoothing sweeps per side on levels 2 and coarser with a transform axis) rebuilds
+ * the solvers and runs 1 + steps RK3 steps from a snapshot of the state; candidates whose solves do not
+ * converge are dropped.  The state (fields, RK storage, time, dt, step count and the solvers' warm starts) is
+ * then restored and the solvers are rebuilt with the fastest candidate. */
+typedef struct snac_tune_result {
+  int inner_iters;      /* chosen FP32 Krylov iterations per refinement step (mixed solve) */
+  int nu_coarse;        /* chosen smoothing sweeps per side on levels 2 and coarser */
+  double ms_per_step;   /* device time per step of the chosen candidate */
+  double ms_before;     /* device time per step of the settings in use before the call */
+  int ncand;            /* candidates timed */
+} snac_tune_result;
+int snac_autotune(int steps, snac_tune_result *out);
+
 /* whole RK3 steps, main.f90:893-1069 (dt from chkdt every icheck steps) */
 int snac_step(int nsteps);
 int snac_get_stats(snac_step_stats *st);

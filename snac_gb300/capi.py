@@ -51,6 +51,11 @@ class Options(C.Structure):
                 ("nu_coarse", C.c_int)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("inner_iters", C.c_int), ("nu_coarse", C.c_int), ("ms_per_step", C.c_double),
+                ("ms_before", C.c_double), ("ncand", C.c_int)]
+
+
 class StepStats(C.Structure):
     _fields_ = [("istep", C.c_int), ("time", C.c_double), ("dt", C.c_double), ("solve_iters_max", C.c_int),
                 ("solve_residual_max", C.c_double), ("solves", C.c_int), ("device_ms", C.c_double),
@@ -123,6 +128,7 @@ PROTOTYPES = {
     "snac_guess_mode": (C.c_int, [C.c_int]),
     "snac_guess_train": (C.c_int, [C.c_int, C.c_double, DP, DP, IP]),
     "snac_guess_measure": (C.c_int, [C.c_int, DP, DP]),
+    "snac_autotune": (C.c_int, [C.c_int, C.POINTER(TuneResult)]),
     "snac_out1d_write": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int]),
     "snac_out3d_write": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
     "snac_get_stats": (C.c_int, [C.POINTER(StepStats)]),

@@ -144,6 +144,7 @@ struct Domain {
   std::unique_ptr<PoissonSolver> ps;
   std::unique_ptr<PoissonSolver> hs[3 + SNAC_MAX_SCAL];  // IMPDIFF: Helmholtz solvers of u, v, w, scalars
   GuessState *guess = nullptr;       // learned initial guess of the pressure solve (off unless requested)
+  int tune_inner = 0;                // FP32 Krylov iterations per refinement step set by snac_autotune (0: default)
   double dt = 0.0, time = 0.0;
   int istep = 0;
   int last_solve_iters = 0, solves = 0;

@@ -272,6 +272,7 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
   S.field = field;
   S.helm = field != HF_P;
   S.precision = d.opt.precision;
+  if (d.tune_inner > 0) S.inner_iters = d.tune_inner;
   if (const char *e = getenv("SNAC_MG_INNER")) S.inner_iters = std::max(1, atoi(e));
   if (const char *e = getenv("SNAC_MG_INNER_TOL")) S.inner_tol = atof(e);
   S.use_graph = d.opt.use_graph ? 1 : 0;

@@ -1,0 +1,169 @@
+// tune.cu -- snac_autotune: the solver settings for the case at hand, chosen by timing RK3 steps.
+//
+// The candidates differ in the FP32 Krylov iterations per refinement step (mixed solve) and in the
+// smoothing sweeps per side on the coarse levels (transform-axis solve).  Each candidate rebuilds the
+// solvers and runs from the same snapshot of the state; the state is restored afterwards, including the
+// solvers' warm starts, so the run continues as if only the settings had changed.
+#include <vector>
+
+#include "snac_host.h"
+
+namespace snac {
+namespace {
+
+struct Snapshot {
+  std::vector<std::pair<double *, double *>> arrays;  // (live array, copy)
+  std::vector<std::pair<size_t, double *>> boxes;     // per solver slot (0 pressure, 1.. Helmholtz): size, copy
+  double dt = 0.0, time = 0.0;
+  int istep = 0;
+  ~Snapshot() {
+    for (auto &a : arrays) cudaFree(a.second);
+    for (auto &b : boxes) cudaFree(b.second);
+  }
+};
+
+int snap_array(Snapshot &s, double *live, size_t bytes, cudaStream_t st) {
+  if (!live) return SNAC_OK;
+  double *c = nullptr;
+  if (cudaMalloc(&c, bytes) != cudaSuccess) { set_error("snac_autotune: device allocation failed (snapshot)"); return SNAC_ERR_NOMEM; }
+  s.arrays.push_back({live, c});
+  SNAC_CUDA(cudaMemcpyAsync(c, live, bytes, cudaMemcpyDeviceToDevice, st));
+  return SNAC_OK;
+}
+
+std::vector<PoissonSolver *> solvers(Domain &d) {
+  std::vector<PoissonSolver *> v{d.ps.get()};
+  for (auto &h : d.hs) v.push_back(h.get());
+  return v;
+}
+
+size_t box_bytes(const PoissonSolver &S) { return (size_t)S.P.L[0].ncell * S.P.nsys * sizeof(double); }
+
+int take(Domain &d, Snapshot &s) {
+  cudaStream_t st = d.st;
+  for (int b = 0; b < d.nblocks; b++) {
+    const DBlock &B = d.db[b];
+    const size_t nh = (size_t)(B.n[0] + 2) * (B.n[1] + 2) * (B.n[2] + 2) * sizeof(double);
+    const size_t ni = (size_t)B.n[0] * B.n[1] * B.n[2] * sizeof(double);
+    for (double *p : {B.u, B.v, B.w, B.p, B.pp}) SNAC_TRY(snap_array(s, p, nh, st));
+    for (double *p : {B.ru, B.rv, B.rw}) SNAC_TRY(snap_array(s, p, ni, st));
+    for (int q = 0; q < d.c.nscal; q++) {
+      SNAC_TRY(snap_array(s, B.s[q], nh, st));
+      SNAC_TRY(snap_array(s, B.rs[q], ni, st));
+    }
+  }
+  for (PoissonSolver *S : solvers(d)) {
+    double *c = nullptr;
+    size_t n = 0;
+    if (S && S->box_x) {
+      n = box_bytes(*S);
+      if (cudaMalloc(&c, n) != cudaSuccess) { set_error("snac_autotune: device allocation failed (snapshot)"); return SNAC_ERR_NOMEM; }
+      SNAC_CUDA(cudaMemcpyAsync(c, S->box_x, n, cudaMemcpyDeviceToDevice, st));
+    }
+    s.boxes.push_back({n, c});
+  }
+  s.dt = d.dt;
+  s.time = d.time;
+  s.istep = d.istep;
+  SNAC_CUDA(cudaStreamSynchronize(st));
+  return SNAC_OK;
+}
+
+// rebuild the pressure solver and the Helmholtz solvers with the current settings
+int rebuild(Domain &d) {
+  SNAC_CUDA(cudaStreamSynchronize(d.st));
+  d.ps.reset(new PoissonSolver());
+  SNAC_TRY(solver_create(d, *d.ps));
+  for (int f = HF_U; d.c.impdiff && f < HF_S0 + d.c.nscal; f++) {
+    d.hs[f].reset(new PoissonSolver());
+    SNAC_TRY(solver_create(d, *d.hs[f], true, f));
+  }
+  return SNAC_OK;
+}
+
+int restore(Domain &d, const Snapshot &s, bool boxes) {
+  cudaStream_t st = d.st;
+  size_t k = 0;
+  for (int b = 0; b < d.nblocks; b++) {
+    const DBlock &B = d.db[b];
+    const size_t nh = (size_t)(B.n[0] + 2) * (B.n[1] + 2) * (B.n[2] + 2) * sizeof(double);
+    const size_t ni = (size_t)B.n[0] * B.n[1] * B.n[2] * sizeof(double);
+    std::vector<size_t> sizes{nh, nh, nh, nh, nh, ni, ni, ni};
+    for (int q = 0; q < d.c.nscal; q++) { sizes.push_back(nh); sizes.push_back(ni); }
+    for (size_t z : sizes) {
+      const auto &a = s.arrays[k++];
+      SNAC_CUDA(cudaMemcpyAsync(a.first, a.second, z, cudaMemcpyDeviceToDevice, st));
+    }
+  }
+  if (boxes) {
+    const auto sv = solvers(d);
+    for (size_t i = 0; i < sv.size() && i < s.boxes.size(); i++)
+      if (sv[i] && sv[i]->box_x && s.boxes[i].second && box_bytes(*sv[i]) == s.boxes[i].first)
+        SNAC_CUDA(cudaMemcpyAsync(sv[i]->box_x, s.boxes[i].second, s.boxes[i].first, cudaMemcpyDeviceToDevice, st));
+  }
+  d.dt = s.dt;
+  d.time = s.time;
+  d.istep = s.istep;
+  SNAC_CUDA(cudaStreamSynchronize(st));
+  return SNAC_OK;
+}
+
+}  // namespace
+}  // namespace snac
+
+using namespace snac;
+
+int snac_autotune(int steps, snac_tune_result *out) {
+  Domain *d = domain();
+  if (!d) { set_error("snac_autotune: no domain (call snac_init first)"); return SNAC_ERR_STATE; }
+  if (steps < 1) { set_error("snac_autotune: steps must be >= 1"); return SNAC_ERR_ARG; }
+  const int inner0 = d->tune_inner, nuc0 = d->opt.nu_coarse;
+  const bool plane = d->ps && !d->ps->mode3d;
+  const bool mixed = d->opt.precision == 1;
+  std::vector<std::pair<int, int>> cand;  // (inner iterations, nu_coarse); 0 = the solver's default
+  for (int inner : mixed ? std::vector<int>{4, 5, 6} : std::vector<int>{0})
+    for (int nuc : plane ? std::vector<int>{1, 2} : std::vector<int>{0}) cand.push_back({inner, nuc});
+  Snapshot snap;
+  SNAC_TRY(take(*d, snap));
+  // the settings in use: one warm-up step and `steps` timed steps from the snapshot
+  auto time_current = [&](double *ms) -> int {
+    SNAC_TRY(restore(*d, snap, true));
+    const int rc1 = snac_step(1);
+    if (rc1 != SNAC_OK) return rc1;
+    const int rc = snac_step(steps);
+    *ms = d->device_ms / steps;
+    return rc;
+  };
+  double ms_before = 0.0;
+  SNAC_TRY(time_current(&ms_before));
+  double best = 1e300;
+  int bi = -1, ntimed = 0;
+  for (size_t i = 0; i < cand.size(); i++) {
+    d->tune_inner = cand[i].first;
+    d->opt.nu_coarse = cand[i].second;
+    SNAC_TRY(rebuild(*d));
+    double ms = 0.0;
+    const int rc = time_current(&ms);
+    ntimed++;
+    if (rc == SNAC_ERR_NOT_CONVERGED) continue;  // this candidate does not reach the tolerance
+    SNAC_TRY(rc);
+    if (ms < best) { best = ms; bi = (int)i; }
+  }
+  if (bi < 0) {  // nothing converged: keep the settings that were in use
+    d->tune_inner = inner0;
+    d->opt.nu_coarse = nuc0;
+  } else {
+    d->tune_inner = cand[bi].first;
+    d->opt.nu_coarse = cand[bi].second;
+  }
+  SNAC_TRY(rebuild(*d));
+  SNAC_TRY(restore(*d, snap, true));
+  if (out) {
+    out->inner_iters = d->ps ? d->ps->inner_iters : 0;
+    out->nu_coarse = d->ps ? d->ps->P.nu_coarse : 0;
+    out->ms_per_step = bi < 0 ? ms_before : best;
+    out->ms_before = ms_before;
+    out->ncand = ntimed;
+  }
+  return SNAC_OK;
+}

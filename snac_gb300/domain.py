@@ -128,6 +128,14 @@ class Domain:
         check(capi.lib().snac_out1d(int(ib), int(kind), int(idir), x.ctypes.data_as(capi.DP), p.ctypes.data_as(capi.DP)))
         return x, p
 
+    def autotune(self, steps: int = 3):
+        """Time the solver-setting candidates from a snapshot of the state and keep the fastest (the state is
+        restored); returns the chosen settings and the times per step before and after."""
+        r = capi.TuneResult()
+        check(capi.lib().snac_autotune(int(steps), C.byref(r)))
+        return dict(inner_iters=r.inner_iters, nu_coarse=r.nu_coarse, ms_per_step=r.ms_per_step,
+                    ms_before=r.ms_before, candidates=r.ncand)
+
     def stats(self):
         s = capi.StepStats()
         check(capi.lib().snac_get_stats(C.byref(s)))

@@ -590,3 +590,42 @@ def test_steps_one_cell_periodic_axis(snac_lib, oracle_mod, fft_axis):
         assert d.chkdiv()[1] < 1e-10
     finally:
         d.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_autotune_restores_state(snac_lib, precision):
+    """snac_autotune times its candidates from a snapshot and then restores the state: the fields, time and
+    step count after the call are those before it, bit for bit, and stepping on with the chosen settings
+    converges to the same tolerance.  Against the same steps without tuning, the fields differ only by
+    what the solver tolerance allows."""
+    case = cases.channel_4block(nx=(16, 32), ny=(8, 16), nz=16)
+    runs = {}
+    for tune in (0, 1):
+        d = Domain(case, precision=precision, use_graph=precision)
+        try:
+            ic = cases.channel_initial_condition(case, lambda ib: d.grid(ib, 1, capi.G_XC))
+            for ib, (u, v, w) in ic.items():
+                d.set(ib, capi.U, u)
+                d.set(ib, capi.V, v)
+                d.set(ib, capi.W, w)
+            d.bounduvw(False)
+            d.step(3)
+            before = [d.get(ib, k) for ib in range(len(case.blocks)) for k in (capi.U, capi.V, capi.W, capi.P)]
+            st0 = d.stats()
+            if tune:
+                r = d.autotune(2)
+                assert r["candidates"] == (6 if precision else 2), r
+                assert r["inner_iters"] in ((4, 5, 6) if precision else (5,)) and r["nu_coarse"] in (1, 2), r
+                assert 0.0 < r["ms_per_step"] <= r["ms_before"] * 1.5, r
+                after = [d.get(ib, k) for ib in range(len(case.blocks)) for k in (capi.U, capi.V, capi.W, capi.P)]
+                for a, b in zip(before, after):
+                    np.testing.assert_array_equal(a, b)
+                st1 = d.stats()
+                assert st1["istep"] == st0["istep"] and st1["time"] == st0["time"] and st1["dt"] == st0["dt"]
+            assert d.step(3) == 0
+            assert d.stats()["residual"] <= case.tol and d.chkdiv()[1] < 1e-10
+            runs[tune] = [d.get(ib, k) for ib in range(len(case.blocks)) for k in (capi.U, capi.V, capi.W)]
+        finally:
+            d.close()
+    for a, b in zip(runs[0], runs[1]):
+        assert np.max(np.abs(a - b)) <= 1e-9 * np.max(np.abs(a))
