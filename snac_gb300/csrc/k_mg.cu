@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(256) k_cg_xr(long n, const int *active, const 
 // scale = RMS of the residual over nact cells.  src_active: flags are first copied from there.
 __global__ void k_cg_norms(int *active, const int *src_active, SysScal *sc, const double *part_rr,
                            const double *part_bb, int stride, int n, double tol, int set_bb, int want_scale,
-                           long nact, int *count) {
+                           long nact, int *count, const SysScal *outer, double outer_tol) {
   const int s = blockIdx.x;
   if (src_active) {
     if (threadIdx.x == 0) active[s] = src_active[s];
@@ -436,6 +436,10 @@ __global__ void k_cg_norms(int *active, const int *src_active, SysScal *sc, cons
     // r = b, which also avoids the cancellation of a large A x0 against a small b
     sc[s].restart = (bbn > 0.0 && rr > bbn) ? 1 : 0;
     if (sc[s].restart) rr = bbn;
+    // the start of an inner solve of iterative refinement: reduce this system's residual only as far as its
+    // outer residual needs (a tenth of outer_tol / its relative outer residual), never below tol
+    sc[s].tol = 0.0;
+    if (outer) sc[s].tol = fmin(0.5, fmax(tol, 0.1 * outer_tol / outer[s].rel));
   }
   sc[s].rr = rr;
   if (want_scale) {
@@ -445,8 +449,9 @@ __global__ void k_cg_norms(int *active, const int *src_active, SysScal *sc, cons
   const double bb = sc[s].bb;
   const double rel = bb > 0.0 ? sqrt(rr / bb) : 0.0;
   sc[s].rel = rel;
+  const double ts = sc[s].tol > 0.0 ? sc[s].tol : tol;
   if (bb == 0.0) { sc[s].zero_rhs = 1; active[s] = 0; atomicAdd(count + 1, 1); }
-  else if (rel <= tol) active[s] = 0;
+  else if (rel <= ts) active[s] = 0;
   else atomicAdd(count, 1);
 }
 
@@ -603,7 +608,7 @@ int mg_residual(const MgProblem &P, CgWork &W, const T *x, const T *b, T *r, dou
     SNAC_TRY(plane_resid<T>(P, shift_of<T>(P), W.active, x, b, r, W.part0, set_bb ? W.part1 : nullptr, W.stride, st));
   SNAC_CUDA(cudaMemsetAsync(W.d_count, 0, 2 * sizeof(int), st));
   k_cg_norms<<<P.nsys, 256, 0, st>>>(W.active, nullptr, W.sc, W.part0, W.part1, W.stride, nchunk_red(P, L0), tol,
-                                     set_bb, want_scale, nact, W.d_count), ::snac::count_launch();
+                                     set_bb, want_scale, nact, W.d_count, nullptr, 0.0), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -692,7 +697,7 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
     k_cg_xr<T><<<gf, 256, 0, st>>>(n, W.active, W.sc, p, q, x, r, W.part0, W.stride, (zero_x && it == 1) ? 1 : 0), ::snac::count_launch();
     SNAC_CUDA(cudaMemsetAsync(W.d_count, 0, 2 * sizeof(int), st));
     k_cg_norms<<<P.nsys, 256, 0, st>>>(W.active, nullptr, W.sc, W.part0, nullptr, W.stride, nflat, tol, 0, 0, 0,
-                                       W.d_count), ::snac::count_launch();
+                                       W.d_count, nullptr, 0.0), ::snac::count_launch();
     SNAC_CUDA(cudaGetLastError());
     trace("pcg: iteration", st);
   }
@@ -714,13 +719,14 @@ int mg_project_singular(const MgProblem &P, CgWork &W, double *b, cudaStream_t s
 }
 
 int mg_ir_down(const MgProblem &P, const CgWork &Wout, CgWork &W32, const double *r64, float *r32, float *e32,
-               double inner_tol, cudaStream_t st) {
+               double inner_tol, double outer_tol, cudaStream_t st) {
   const long n = P.L[0].ncell;
   const dim3 gf = grid_flat(n, P.nsys);
   k_ir_down<<<gf, 256, 0, st>>>(n, Wout.active, Wout.sc, r64, r32, e32, W32.part0, W32.stride), ::snac::count_launch();
   SNAC_CUDA(cudaMemsetAsync(W32.d_count, 0, 2 * sizeof(int), st));
   k_cg_norms<<<P.nsys, 256, 0, st>>>(W32.active, Wout.active, W32.sc, W32.part0, W32.part0, W32.stride, (int)gf.x,
-                                     inner_tol, 1, 0, 0, W32.d_count), ::snac::count_launch();
+                                     inner_tol, 1, 0, 0, W32.d_count, outer_tol > 0.0 ? Wout.sc : nullptr, outer_tol),
+      ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

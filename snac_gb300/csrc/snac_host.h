@@ -100,6 +100,8 @@ struct PoissonSolver {
   int spec_outer = 0;
   int *d_ocount = nullptr, *h_ocount = nullptr;  // 2 * SPEC_MAX ints (device, pinned host)
   double inner_tol = 1e-6;           // mixed path: relative tolerance of the FP32 solve
+  bool adapt_inner = true;           // mixed path: each system's inner solve stops once its outer residual
+                                     // would be within a tenth of the tolerance (never beyond inner_tol)
   double tol = 1e-12;
   int maxiter = 200;
   MgProblem P{};

@@ -14,6 +14,7 @@ struct SysScal {
   double rz, rr, bb, rel, scale, alpha, beta;
   int first, zero_rhs;
   int restart;  // the warm start was worse than zero (rel > 1): the solve restarts from x = 0
+  double tol;   // this system's own relative tolerance in the running loop (0: the loop's)
 };
 
 // Partial sums: one row of `stride` doubles per system; a producer kernel writes one entry per CTA
@@ -41,7 +42,7 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
 int mg_project_singular(const MgProblem &P, CgWork &W, double *b, cudaStream_t st);
 // mixed path: r32 = r64 / scale, e32 = 0, inner norms (active copied from the outer loop)
 int mg_ir_down(const MgProblem &P, const CgWork &Wout, CgWork &W32, const double *r64, float *r32, float *e32,
-               double inner_tol, cudaStream_t st);
+               double inner_tol, double outer_tol, cudaStream_t st);
 int mg_ir_up(const MgProblem &P, const CgWork &Wout, const float *e32, double *x, cudaStream_t st);
 int mg_zero_rhs_systems(const MgProblem &P, const CgWork &W, double *x, cudaStream_t st);
 // systems whose warm start is worse than zero (set by mg_residual with set_bb): x = 0, r = b

@@ -273,6 +273,8 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
   S.helm = field != HF_P;
   S.precision = d.opt.precision;
   if (d.tune_inner > 0) S.inner_iters = d.tune_inner;
+  // SNAC_MG_ADAPT=0: every inner solve reduces its residual by inner_tol, whatever the outer residual needs
+  if (const char *e = getenv("SNAC_MG_ADAPT")) S.adapt_inner = e[0] != '0';
   if (const char *e = getenv("SNAC_MG_INNER")) S.inner_iters = std::max(1, atoi(e));
   if (const char *e = getenv("SNAC_MG_INNER_TOL")) S.inner_tol = atof(e);
   S.use_graph = d.opt.use_graph ? 1 : 0;
@@ -710,7 +712,7 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
 // replayed (every pointer and launch shape is fixed for the solver's lifetime).
 static int refine_step_body(PoissonSolver &S, const CgWork &Wr, cudaStream_t st) {
   MgProblem &P = S.P;
-  SNAC_TRY(mg_ir_down(P, Wr, S.W32, S.r64, (float *)S.W32.r, S.box_e32, S.inner_tol, st));
+  SNAC_TRY(mg_ir_down(P, Wr, S.W32, S.r64, (float *)S.W32.r, S.box_e32, S.inner_tol, S.adapt_inner ? S.tol : 0.0, st));
   int it1 = 0;
   SNAC_TRY(mg_pcg<float>(P, S.W32, S.box_e32, S.inner_iters, S.inner_tol, true, false, &it1, st));
   SNAC_TRY(mg_ir_up(P, Wr, S.box_e32, S.box_x, st));
