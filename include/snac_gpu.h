@@ -294,12 +294,13 @@ int snac_guess_train(int iters, double lr, double *loss_first, double *loss_last
 int snac_guess_measure(int on, double *ratio_median, double *ratio_max);
 
 /* No counterpart in the reference (HYPRE's PFMG settings are fixed in the input): picks the solver settings
- * for this case by timing.  Every candidate (FP32 Krylov iterations per refinement step 4, 5 or 6 with the
- * mixed solve; one or two smoothing sweeps per side on levels 2 and coarser with a transform axis) rebuilds
- * the solvers and runs 1 + steps RK3 steps from a snapshot of the state; candidates whose solves do not
- * converge are dropped.  The state (fields, RK storage, time, dt, step count and the solvers' warm starts) is
+ * for this case by timing.  Every candidate (the plain FP64 solve, or the mixed solve with 4, 5 or 6 FP32
+ * Krylov iterations per refinement step; one or two smoothing sweeps per side on levels 2 and coarser with
+ * a transform axis) rebuilds the solvers and runs 1 + steps RK3 steps from a snapshot of the state; all
+ * solve to the same tolerance, and candidates whose solves do not converge are dropped.  The state (fields, RK storage, time, dt, step count and the solvers' warm starts) is
  * then restored and the solvers are rebuilt with the fastest candidate. */
 typedef struct snac_tune_result {
+  int precision;        /* chosen solve: 0 plain FP64, 1 mixed (as snac_options.precision) */
   int inner_iters;      /* chosen FP32 Krylov iterations per refinement step (mixed solve) */
   int nu_coarse;        /* chosen smoothing sweeps per side on levels 2 and coarser */
   double ms_per_step;   /* device time per step of the chosen candidate */

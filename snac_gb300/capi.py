@@ -52,7 +52,7 @@ class Options(C.Structure):
 
 
 class TuneResult(C.Structure):
-    _fields_ = [("inner_iters", C.c_int), ("nu_coarse", C.c_int), ("ms_per_step", C.c_double),
+    _fields_ = [("precision", C.c_int), ("inner_iters", C.c_int), ("nu_coarse", C.c_int), ("ms_per_step", C.c_double),
                 ("ms_before", C.c_double), ("ncand", C.c_int)]
 
 

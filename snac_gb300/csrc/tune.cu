@@ -1,7 +1,8 @@
 // tune.cu -- snac_autotune: the solver settings for the case at hand, chosen by timing RK3 steps.
 //
-// The candidates differ in the FP32 Krylov iterations per refinement step (mixed solve) and in the
-// smoothing sweeps per side on the coarse levels (transform-axis solve).  Each candidate rebuilds the
+// The candidates differ in the solve (plain FP64, or mixed with 4, 5 or 6 FP32 Krylov iterations per
+// refinement step) and in the smoothing sweeps per side on the coarse levels (transform-axis solve); all
+// solve to the same tolerance.  Each candidate rebuilds the
 // solvers and runs from the same snapshot of the state; the state is restored afterwards, including the
 // solvers' warm starts, so the run continues as if only the settings had changed.
 #include <vector>
@@ -117,12 +118,14 @@ int snac_autotune(int steps, snac_tune_result *out) {
   Domain *d = domain();
   if (!d) { set_error("snac_autotune: no domain (call snac_init first)"); return SNAC_ERR_STATE; }
   if (steps < 1) { set_error("snac_autotune: steps must be >= 1"); return SNAC_ERR_ARG; }
-  const int inner0 = d->tune_inner, nuc0 = d->opt.nu_coarse;
+  const int inner0 = d->tune_inner, nuc0 = d->opt.nu_coarse, prec0 = d->opt.precision;
   const bool plane = d->ps && !d->ps->mode3d;
-  const bool mixed = d->opt.precision == 1;
-  std::vector<std::pair<int, int>> cand;  // (inner iterations, nu_coarse); 0 = the solver's default
-  for (int inner : mixed ? std::vector<int>{4, 5, 6} : std::vector<int>{0})
-    for (int nuc : plane ? std::vector<int>{1, 2} : std::vector<int>{0}) cand.push_back({inner, nuc});
+  struct Cand { int prec, inner, nuc; };  // inner, nuc: 0 = the solver's default
+  std::vector<Cand> cand;
+  for (int nuc : plane ? std::vector<int>{1, 2} : std::vector<int>{0}) {
+    for (int inner : {4, 5, 6}) cand.push_back({1, inner, nuc});
+    cand.push_back({0, 0, nuc});
+  }
   Snapshot snap;
   SNAC_TRY(take(*d, snap));
   // the settings in use: one warm-up step and `steps` timed steps from the snapshot
@@ -139,8 +142,9 @@ int snac_autotune(int steps, snac_tune_result *out) {
   double best = 1e300;
   int bi = -1, ntimed = 0;
   for (size_t i = 0; i < cand.size(); i++) {
-    d->tune_inner = cand[i].first;
-    d->opt.nu_coarse = cand[i].second;
+    d->opt.precision = cand[i].prec;
+    d->tune_inner = cand[i].inner;
+    d->opt.nu_coarse = cand[i].nuc;
     SNAC_TRY(rebuild(*d));
     double ms = 0.0;
     const int rc = time_current(&ms);
@@ -150,15 +154,18 @@ int snac_autotune(int steps, snac_tune_result *out) {
     if (ms < best) { best = ms; bi = (int)i; }
   }
   if (bi < 0) {  // nothing converged: keep the settings that were in use
+    d->opt.precision = prec0;
     d->tune_inner = inner0;
     d->opt.nu_coarse = nuc0;
   } else {
-    d->tune_inner = cand[bi].first;
-    d->opt.nu_coarse = cand[bi].second;
+    d->opt.precision = cand[bi].prec;
+    d->tune_inner = cand[bi].inner;
+    d->opt.nu_coarse = cand[bi].nuc;
   }
   SNAC_TRY(rebuild(*d));
   SNAC_TRY(restore(*d, snap, true));
   if (out) {
+    out->precision = d->opt.precision;
     out->inner_iters = d->ps ? d->ps->inner_iters : 0;
     out->nu_coarse = d->ps ? d->ps->P.nu_coarse : 0;
     out->ms_per_step = bi < 0 ? ms_before : best;

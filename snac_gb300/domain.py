@@ -133,7 +133,7 @@ class Domain:
         restored); returns the chosen settings and the times per step before and after."""
         r = capi.TuneResult()
         check(capi.lib().snac_autotune(int(steps), C.byref(r)))
-        return dict(inner_iters=r.inner_iters, nu_coarse=r.nu_coarse, ms_per_step=r.ms_per_step,
+        return dict(precision=r.precision, inner_iters=r.inner_iters, nu_coarse=r.nu_coarse, ms_per_step=r.ms_per_step,
                     ms_before=r.ms_before, candidates=r.ncand)
 
     def stats(self):

@@ -614,8 +614,8 @@ def test_autotune_restores_state(snac_lib, precision):
             st0 = d.stats()
             if tune:
                 r = d.autotune(2)
-                assert r["candidates"] == (6 if precision else 2), r
-                assert r["inner_iters"] in ((4, 5, 6) if precision else (5,)) and r["nu_coarse"] in (1, 2), r
+                assert r["candidates"] == 8, r  # (mixed with 4, 5, 6 inner iterations, plain) x (1, 2 sweeps)
+                assert r["precision"] in (0, 1) and r["inner_iters"] in (4, 5, 6) and r["nu_coarse"] in (1, 2), r
                 assert 0.0 < r["ms_per_step"] <= r["ms_before"] * 1.5, r
                 after = [d.get(ib, k) for ib in range(len(case.blocks)) for k in (capi.U, capi.V, capi.W, capi.P)]
                 for a, b in zip(before, after):
