@@ -22,13 +22,39 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 
 __device__ __forceinline__ int bitrev(int q, int logn) { return (int)(__brev((unsigned)q) >> (32 - logn)); }
 
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+
 // in-place radix-2 DIT FFT (exp(-i...)) of npair complex lines of length n = 2^logn held in bit-reversed
-// order (index arithmetic by shifts and masks)
+// order (index arithmetic by shifts and masks).  Two consecutive stages (spans h and 2h) run as one pass:
+// a thread loads the 4 points of a group of 4h and applies the same butterflies and twiddles as the two
+// radix-2 stages would, so the results are those of the stage-by-stage form with half the passes over
+// shared memory and half the barriers.
 __device__ void fft_pairs(double2 *zb, int npair, int n, int logn, const double2 *__restrict__ tw) {
   const int half = n >> 1, lhalf = logn - 1;
-  for (int lh = 0; lh < logn; lh++) {
+  int lh = 0;
+  for (; lh + 1 < logn; lh += 2) {
     __syncthreads();
-    const int h = 1 << lh, lstep = lhalf - lh;  // twiddle stride n / (2 h)
+    const int h = 1 << lh, lq = logn - 2, quarter = n >> 2;
+    const int s1 = lhalf - lh, s2 = lhalf - lh - 1;  // twiddle strides n / (2h) and n / (4h)
+    for (int t = threadIdx.x; t < (npair << lq); t += blockDim.x) {
+      const int p = t >> lq, b = t & (quarter - 1);
+      const int grp = b >> lh, k = b & (h - 1);
+      double2 *z = zb + p * n + (grp << (lh + 2)) + k;
+      const double2 a0 = z[0], a1 = z[h], a2 = z[2 * h], a3 = z[3 * h];
+      const double2 w1 = tw[k << s1];
+      const double2 t1 = cmul(w1, a1), t3 = cmul(w1, a3);
+      const double2 b0 = cadd(a0, t1), b1 = csub(a0, t1), b2 = cadd(a2, t3), b3 = csub(a2, t3);
+      const double2 u2 = cmul(tw[k << s2], b2), u3 = cmul(tw[(k + h) << s2], b3);
+      z[0] = cadd(b0, u2);
+      z[2 * h] = csub(b0, u2);
+      z[h] = cadd(b1, u3);
+      z[3 * h] = csub(b1, u3);
+    }
+  }
+  if (lh < logn) {  // a last single stage (odd logn)
+    __syncthreads();
+    const int h = 1 << lh, lstep = lhalf - lh;
     for (int t = threadIdx.x; t < (npair << lhalf); t += blockDim.x) {
       const int p = t >> lhalf, b = t & (half - 1);
       const int grp = b >> lh, k = b & (h - 1);
@@ -36,8 +62,8 @@ __device__ void fft_pairs(double2 *zb, int npair, int n, int logn, const double2
       const double2 w = tw[k << lstep];
       double2 *z = zb + p * n;
       const double2 x0 = z[i0], t1 = cmul(w, z[i1]);
-      z[i0] = make_double2(x0.x + t1.x, x0.y + t1.y);
-      z[i1] = make_double2(x0.x - t1.x, x0.y - t1.y);
+      z[i0] = cadd(x0, t1);
+      z[i1] = csub(x0, t1);
     }
   }
   __syncthreads();
