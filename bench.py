@@ -248,7 +248,8 @@ def ncu_traffic(kernel):
 
 
 def run_e2e(case_fn, precision, steps, device):
-    """Through the C ABI with host buffers: upload u,v,w,p from pinned host memory, one step, read them back."""
+    """Through the C ABI with host buffers: upload u,v,w,p of every block from pinned host memory in one
+    snac_set_fields call, one step, read them back with snac_get_fields."""
     import torch
     from snac_gb300 import capi
     from snac_gb300.domain import Domain
@@ -266,14 +267,12 @@ def run_e2e(case_fn, precision, steps, device):
                 a[...] = dom.get(ib, k)
                 host[(ib, k)] = (t, a)
         nbytes = sum(a.nbytes for (_, a) in host.values())
-        L = capi.lib()
+        items = [(ib, k, a) for (ib, k), (_, a) in host.items()]
         t0 = time.perf_counter()
         for _ in range(steps):
-            for (ib, k), (_, a) in host.items():
-                capi.check(L.snac_set_field(ib, k, capi.dptr(a)))
+            dom.set_many(items)  # snac_set_fields: every field's copy issued, one synchronisation
             dom.step(1, allow_not_converged=True)
-            for (ib, k), (_, a) in host.items():
-                capi.check(L.snac_get_field(ib, k, capi.dptr(a)))
+            dom.get_many(items)  # snac_get_fields
         el = time.perf_counter() - t0
         return dict(s_per_step=el / steps, h2d=nbytes, d2h=nbytes, ncell=case.ncell)
     finally:

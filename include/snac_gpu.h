@@ -233,6 +233,10 @@ int snac_block_geometry(int ib, int lo[3], int hi[3], int nb[3][2], int is_bound
 int snac_get_grid(int ib, int axis, int which, double *out);         /* (ng+2) values */
 int snac_set_field(int ib, int field, const double *host);
 int snac_get_field(int ib, int field, double *host);
+/* n fields at once (block ib[q], field kind field[q], host array host[q]): the copies are issued on two
+ * streams (two copy engines) and the call returns when all are complete */
+int snac_set_fields(int n, const int *ib, const int *field, const double *const *host);
+int snac_get_fields(int n, const int *ib, const int *field, double *const *host);
 double snac_vol_all(void);
 /* the per-stage routines of main.f90:906-1043 on every block */
 int snac_rk_mom_all(int irk);                     /* rk_mom for all blocks with the current dt */

@@ -36,6 +36,7 @@ Domain::~Domain() {
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
   if (st) cudaStreamDestroy(st);
+  if (st_copy) cudaStreamDestroy(st_copy);
 }
 
 // ---- initgrid.f90:171-287 ----
@@ -1009,6 +1010,37 @@ int snac_get_field(int ib, int field, double *host) {
   SNAC_CUDA(cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, d->st));
   SNAC_CUDA(cudaStreamSynchronize(d->st));
   return SNAC_OK;
+}
+
+// batched host <-> device copies: alternate between the library stream and a second stream so that two
+// copy engines share the transfers; one synchronisation at the end
+static int copy_fields(Domain &d, int n, const int *ib, const int *field, void *const *host, bool to_device) {
+  if (n < 0 || (n > 0 && (!ib || !field || !host))) { set_error("batched field copy: bad argument"); return SNAC_ERR_ARG; }
+  if (!d.st_copy) SNAC_CUDA(cudaStreamCreateWithFlags(&d.st_copy, cudaStreamNonBlocking));
+  std::vector<std::pair<double *, size_t>> dev(n);
+  for (int q = 0; q < n; q++) {
+    SNAC_TRY(field_ptr(d, ib[q], field[q], &dev[q].first, &dev[q].second));
+    if (!host[q]) { set_error("batched field copy: null host array %d", q); return SNAC_ERR_ARG; }
+  }
+  SNAC_CUDA(cudaStreamSynchronize(d.st));  // the fields are not in use by queued work
+  for (int q = 0; q < n; q++) {
+    cudaStream_t s = (q & 1) ? d.st_copy : d.st;
+    if (to_device) SNAC_CUDA(cudaMemcpyAsync(dev[q].first, host[q], dev[q].second, cudaMemcpyHostToDevice, s));
+    else SNAC_CUDA(cudaMemcpyAsync(host[q], dev[q].first, dev[q].second, cudaMemcpyDeviceToHost, s));
+  }
+  SNAC_CUDA(cudaStreamSynchronize(d.st_copy));
+  SNAC_CUDA(cudaStreamSynchronize(d.st));
+  return SNAC_OK;
+}
+
+int snac_set_fields(int n, const int *ib, const int *field, const double *const *host) {
+  NEED_DOMAIN
+  return copy_fields(*d, n, ib, field, (void *const *)host, true);
+}
+
+int snac_get_fields(int n, const int *ib, const int *field, double *const *host) {
+  NEED_DOMAIN
+  return copy_fields(*d, n, ib, field, (void *const *)host, false);
 }
 
 int snac_rk_mom_all(int irk) {

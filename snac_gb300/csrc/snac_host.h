@@ -155,6 +155,7 @@ struct Domain {
   double last_helm_res = 0.0;
   bool helm_not_converged = false;
   cudaStream_t st = nullptr;
+  cudaStream_t st_copy = nullptr;   // second stream for batched host copies (created on first use)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double device_ms = 0.0;
   std::vector<void *> allocs;

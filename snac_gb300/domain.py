@@ -49,6 +49,30 @@ class Domain:
         check(capi.lib().snac_get_field(ib, kind, dptr(a)))
         return a
 
+    def set_many(self, items):
+        """items: (block, kind, Fortran-ordered float64 array) triples, copied to the device in one call."""
+        items = list(items)
+        n = len(items)
+        ib = (C.c_int * n)(*[i[0] for i in items])
+        kd = (C.c_int * n)(*[i[1] for i in items])
+        for _, _, a in items:
+            if not (a.flags.f_contiguous and a.dtype == np.float64):
+                raise ValueError("set_many needs Fortran-ordered float64 arrays")
+        hp = (C.c_void_p * n)(*[a.ctypes.data for _, _, a in items])
+        check(capi.lib().snac_set_fields(n, ib, kd, hp))
+
+    def get_many(self, items):
+        """items: (block, kind, Fortran-ordered float64 array) triples, filled from the device in one call."""
+        items = list(items)
+        n = len(items)
+        ib = (C.c_int * n)(*[i[0] for i in items])
+        kd = (C.c_int * n)(*[i[1] for i in items])
+        for _, _, a in items:
+            if not (a.flags.f_contiguous and a.dtype == np.float64 and a.flags.writeable):
+                raise ValueError("get_many needs writeable Fortran-ordered float64 arrays")
+        hp = (C.c_void_p * n)(*[a.ctypes.data for _, _, a in items])
+        check(capi.lib().snac_get_fields(n, ib, kd, hp))
+
     def set(self, ib, kind, a: np.ndarray):
         a = np.asfortranarray(a, dtype=np.float64)
         assert a.shape == self.shape(ib, kind)

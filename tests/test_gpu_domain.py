@@ -629,3 +629,27 @@ def test_autotune_restores_state(snac_lib, precision):
             d.close()
     for a, b in zip(runs[0], runs[1]):
         assert np.max(np.abs(a - b)) <= 1e-9 * np.max(np.abs(a))
+
+
+def test_batched_field_copies(snac_lib):
+    """snac_set_fields / snac_get_fields move the same bytes as the one-field calls (two streams, one
+    synchronisation)."""
+    case = cases.channel_4block(nx=(16, 32), ny=(8, 16), nz=16)
+    d = Domain(case, precision=1)
+    try:
+        rng = np.random.default_rng(5)
+        items = []
+        for ib in range(len(case.blocks)):
+            for k in (capi.U, capi.V, capi.W, capi.P):
+                items.append((ib, k, np.asfortranarray(rng.standard_normal(d.shape(ib, k)))))
+        d.set_many(items)
+        for ib, k, a in items:
+            np.testing.assert_array_equal(d.get(ib, k), a)
+        outs = [(ib, k, np.zeros(a.shape, order="F")) for ib, k, a in items]
+        d.get_many(outs)
+        for (_, _, a), (_, _, b) in zip(items, outs):
+            np.testing.assert_array_equal(a, b)
+        with pytest.raises(capi.SnacError):
+            d.set_many([(99, capi.U, items[0][2])])
+    finally:
+        d.close()
