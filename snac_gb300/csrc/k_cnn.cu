@@ -1,15 +1,21 @@
 // k_cnn.cu -- dense 3x3 convolutions on the 5th-generation tensor cores (tcgen05, sm_103a).
 //
-// The convolution of a 16-channel BF16 image with 16 output channels is an implicit GEMM per CTA:
+// The convolution of a 16-channel BF16 image with 16 output channels is an implicit GEMM per row segment:
 // 128 pixels of one image row (M = 128) times K = 9 x 16 (the 3x3 taps of 16 channels) times N = 16.
-// The CTA builds the nine 128 x 16 A blocks (im2col of its pixels) and the nine 16 x 16 B blocks (the
-// weights of one tap) in shared memory in the no-swizzle K-major core-matrix layout (8 rows x 16 bytes
-// per core matrix), one thread issues the nine tcgen05.mma.kind::f16 (BF16 inputs, FP32 accumulation)
-// into a 128-lane x 16-column TMEM accumulator, tcgen05.commit signals an mbarrier, and every warp
-// reads its 32 lanes back with tcgen05.ld for the epilogue (bias, optional ReLU).  The wait on the
-// mbarrier has an iteration limit; past it the kernel records an error and returns without reading TMEM.
+// Activations are stored per row as two 8-channel halves of 16-byte pixel records (act_idx), so the three
+// input rows a segment needs, staged in shared memory with 16-byte loads, already are the A operands of
+// the nine taps in the no-swizzle K-major core-matrix layout: a tap's horizontal offset is a 16-byte
+// offset of the descriptor's start address (rows of a core matrix are consecutive pixels, 16 bytes
+// apart; the two K halves are one staged half-row apart).  The weights (B, 16 x 16 per tap) are converted
+// to BF16 once per CTA; the CTAs are persistent and loop over row segments with one TMEM accumulator
+// (128 lanes x 16 columns), one elected thread issuing the nine tcgen05.mma.kind::f16 (BF16 inputs, FP32
+// accumulation) and tcgen05.commit signalling an mbarrier whose phase alternates per segment.  Every warp
+// reads its 32 lanes back with tcgen05.ld for the epilogue (bias, optional ReLU).  The mbarrier wait has
+// an iteration limit; past it the kernel records an error, waits (bounded) for the MMAs in flight, frees
+// its TMEM and returns.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <vector>
 
@@ -45,19 +51,31 @@ __device__ __forceinline__ int core_off(int r, int k) { return (((r >> 3) * 2 + 
 }  // namespace
 
 // y[p][co][h][w] = act(bias[co] + sum_{ci,dy,dx} w[co][ci][dy][dx] x[p][ci][h+dy-1][w+dx-1]) with zero
-// padding; x BF16, weights given in FP32 and rounded to BF16 here; y FP32 for the first ny output channels
-// (none when y is null) and the BF16 copy of all 16 when yb
-__global__ void __launch_bounds__(CNN_M) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ x, int H, int W,
+// padding; x BF16 in the act_idx layout, weights given in FP32 and rounded to BF16 here; y FP32 (planar
+// [p][co][h][w]) for the first ny output channels (none when y is null) and yb BF16 (act_idx) of all 16
+constexpr int CNN_ROW = (CNN_M + 2) * 16;  // bytes of one staged half-row (130 pixel records)
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  uint32_t done = 0;
+  for (long it = 0; it < (1L << 24) && !done; it++) {
+    asm volatile(
+        "{\n .reg .pred pw;\n mbarrier.try_wait.parity.shared::cta.b64 pw, [%1], %2;\n selp.u32 %0, 1, 0, pw;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity));
+  }
+  return done != 0;
+}
+
+__global__ void __launch_bounds__(CNN_M) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ x, int np, int H, int W,
                                                       const float *__restrict__ wts, const float *__restrict__ bias,
                                                       int relu, float *__restrict__ y, int ny,
                                                       __nv_bfloat16 *__restrict__ yb, int *__restrict__ err) {
-  __shared__ __align__(128) unsigned char sa[CNN_TAPS * CNN_M * CNN_C * 2];  // 36 KB of A blocks
+  __shared__ __align__(128) unsigned char sa[3 * 2 * CNN_ROW];               // 12.2 KB: rows h-1..h+1, halves
   __shared__ __align__(128) unsigned char sb[CNN_TAPS * CNN_C * CNN_C * 2];  // 4.5 KB of B blocks
+  __shared__ float sbias[CNN_C];
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const int w0 = blockIdx.x * CNN_M, h = blockIdx.y, p = blockIdx.z;
-  const long plane = (long)H * W;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                  "r"(TMEM_COLS));
@@ -67,74 +85,98 @@ __global__ void __launch_bounds__(CNN_M) k_conv3x3_tc(const __nv_bfloat16 *__res
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar)), "r"(1));
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
-  // B blocks: tap q = dy*3+dx, row n = output channel, k = input channel
+  // B blocks: tap q = dy*3+dx, row n = output channel, k = input channel (K-major core matrices)
   for (int e = t; e < CNN_TAPS * CNN_C * CNN_C; e += CNN_M) {
     const int k = e % CNN_C, n = (e / CNN_C) % CNN_C, q = e / (CNN_C * CNN_C);
     const float wv = wts[((n * CNN_C + k) * 3 + q / 3) * 3 + q % 3];
     *reinterpret_cast<__nv_bfloat16 *>(sb + q * (CNN_C * CNN_C * 2) + core_off(n, k)) = __float2bfloat16(wv);
   }
-  __syncthreads();
-  // A blocks: thread t fills row t (pixel w0 + t) of every tap, zero outside the image
-  for (int q = 0; q < CNN_TAPS; q++) {
-    const int hh = h + q / 3 - 1, ww = w0 + t + q % 3 - 1;
-    const bool in = hh >= 0 && hh < H && ww >= 0 && ww < W;
-    unsigned char *blk = sa + q * (CNN_M * CNN_C * 2);
-    for (int c = 0; c < CNN_C; c++) {
-      const __nv_bfloat16 v = in ? x[(long)p * CNN_C * plane + (long)c * plane + (long)hh * W + ww] : __float2bfloat16(0.f);
-      *reinterpret_cast<__nv_bfloat16 *>(blk + core_off(t, c)) = v;
-    }
-  }
-  // the operands were written by the generic proxy and are read by the tensor core (async proxy)
-  asm volatile("fence.proxy.async.shared::cta;");
+  if (t < CNN_C) sbias[t] = bias[t];
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
-  const uint32_t dtmem = tmem_base;
-  if (t == 0) {
-    constexpr uint32_t idesc = idesc_bf16(CNN_M, CNN_C);
-    for (int q = 0; q < CNN_TAPS; q++) {
-      const uint64_t ad = smem_desc(smem_u32(sa + q * (CNN_M * CNN_C * 2)), 128, 256);
-      const uint64_t bd = smem_desc(smem_u32(sb + q * (CNN_C * CNN_C * 2)), 128, 256);
-      const uint32_t acc = q > 0 ? 1u : 0u;
-      asm volatile(
-          "{\n .reg .pred pa;\n setp.ne.b32 pa, %4, 0;\n"
-          " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, pa;\n}\n" ::"r"(dtmem),
-          "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+  const uint32_t dtmem = tmem_base, bar = smem_u32(&mbar);
+  const int nseg = (W + CNN_M - 1) / CNN_M;
+  const long total = (long)np * H * nseg;
+  uint32_t phase = 0;
+  bool failed = false;
+  for (long seg = blockIdx.x; seg < total; seg += gridDim.x) {
+    const int ws = (int)(seg % nseg);
+    const long ph = seg / nseg;
+    const int h = (int)(ph % H), p = (int)(ph / H);
+    const int w0 = ws * CNN_M;
+    // stage rows h-1, h, h+1 (zero outside the image): 3 x 2 halves x 130 records of 16 bytes
+    for (int e = t; e < 3 * 2 * (CNN_M + 2); e += CNN_M) {
+      const int r = e / (2 * (CNN_M + 2)), rem = e - r * 2 * (CNN_M + 2);
+      const int kh = rem / (CNN_M + 2), q = rem - kh * (CNN_M + 2);
+      const int hh = h + r - 1, ww = w0 - 1 + q;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (hh >= 0 && hh < H && ww >= 0 && ww < W) v = *reinterpret_cast<const uint4 *>(x + act_idx(p, kh * 8, hh, ww, H, W));
+      *reinterpret_cast<uint4 *>(sa + (r * 2 + kh) * CNN_ROW + q * 16) = v;
     }
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&mbar)));
-  }
-  // bounded wait for the accumulator (phase 0)
-  uint32_t done = 0;
-  for (long it = 0; it < (1L << 24) && !done; it++) {
-    asm volatile(
-        "{\n .reg .pred pw;\n mbarrier.try_wait.parity.shared::cta.b64 pw, [%1], %2;\n selp.u32 %0, 1, 0, pw;\n}\n"
-        : "=r"(done)
-        : "r"(smem_u32(&mbar)), "r"(0));
-  }
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  done = __all_sync(0xffffffffu, done);  // tcgen05.ld is warp-collective
-  if (done) {
-    uint32_t r[16];
+    // the operands were written by the generic proxy and are read by the tensor core (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (t == 0) {
+      constexpr uint32_t idesc = idesc_bf16(CNN_M, CNN_C);
+      for (int q = 0; q < CNN_TAPS; q++) {
+        const int dy = q / 3, dx = q % 3;
+        // pixel rows 16 bytes apart (8-row core matrices 128 B apart), K halves one staged half-row apart
+        const uint64_t ad = smem_desc(smem_u32(sa + dy * 2 * CNN_ROW + dx * 16), CNN_ROW, 128);
+        const uint64_t bd = smem_desc(smem_u32(sb + q * (CNN_C * CNN_C * 2)), 128, 256);
+        const uint32_t acc = q > 0 ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred pa;\n setp.ne.b32 pa, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, pa;\n}\n" ::"r"(dtmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar));
+    }
+    const bool got = mbar_wait_bounded(bar, phase);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (!__syncthreads_and(got ? 1 : 0)) {  // the accumulator did not arrive in time
+      if (t == 0) atomicExch(err, 1);
+      failed = true;
+      break;
+    }
+    phase ^= 1u;
+    uint32_t rr[16];
     const uint32_t taddr = dtmem + ((uint32_t)(warp * 32) << 16);
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "=r"(rr[0]), "=r"(rr[1]), "=r"(rr[2]), "=r"(rr[3]), "=r"(rr[4]), "=r"(rr[5]), "=r"(rr[6]), "=r"(rr[7]),
+          "=r"(rr[8]), "=r"(rr[9]), "=r"(rr[10]), "=r"(rr[11]), "=r"(rr[12]), "=r"(rr[13]), "=r"(rr[14]), "=r"(rr[15])
         : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;");
-    const int m = warp * 32 + lane, ww = w0 + m;
+    const int ww = w0 + warp * 32 + lane;
     if (ww < W) {
+      float v[CNN_C];
+#pragma unroll
       for (int n = 0; n < CNN_C; n++) {
-        float v = __uint_as_float(r[n]) + bias[n];
-        if (relu) v = fmaxf(v, 0.f);
-        const long o = (long)p * CNN_C * plane + (long)n * plane + (long)h * W + ww;
-        if (y && n < ny) y[o] = v;
-        if (yb) yb[o] = __float2bfloat16(v);
+        v[n] = __uint_as_float(rr[n]) + sbias[n];
+        if (relu) v[n] = fmaxf(v[n], 0.f);
+      }
+      if (yb) {
+#pragma unroll
+        for (int kh = 0; kh < 2; kh++) {
+          __align__(16) __nv_bfloat16 o[8];
+#pragma unroll
+          for (int c = 0; c < 8; c++) o[c] = __float2bfloat16(v[kh * 8 + c]);
+          *reinterpret_cast<uint4 *>(yb + act_idx(p, kh * 8, h, ww, H, W)) = *reinterpret_cast<const uint4 *>(o);
+        }
+      }
+      if (y) {
+        const long plane = (long)H * W;
+        for (int n = 0; n < ny && n < CNN_C; n++) y[((long)p * CNN_C + n) * plane + (long)h * W + ww] = v[n];
       }
     }
-  } else if (lane == 0) {
-    atomicExch(err, 1);
+    // the next segment's MMAs overwrite the accumulator after the barrier that follows its staging
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();  // every thread has finished with the staged rows and the accumulator
   }
+  if (failed) mbar_wait_bounded(bar, phase);  // let the MMAs in flight finish (bounded) before freeing TMEM
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(dtmem), "r"(TMEM_COLS));
@@ -142,8 +184,15 @@ __global__ void __launch_bounds__(CNN_M) k_conv3x3_tc(const __nv_bfloat16 *__res
 
 int launch_conv3x3_tc(const __nv_bfloat16 *x, int nplanes, int H, int W, const float *wts, const float *bias, int relu,
                       float *y, int ny, __nv_bfloat16 *yb, int *err, cudaStream_t st) {
-  const dim3 g((unsigned)((W + CNN_M - 1) / CNN_M), (unsigned)H, (unsigned)nplanes);
-  k_conv3x3_tc<<<g, CNN_M, 0, st>>>(x, H, W, wts, bias, relu, y, ny, yb, err), ::snac::count_launch();
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    SNAC_CUDA(cudaGetDevice(&dev));
+    SNAC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const long total = (long)nplanes * H * ((W + CNN_M - 1) / CNN_M);
+  const int grid = (int)std::min<long>(total, (long)nsm * 8);  // persistent CTAs, 8 per SM
+  k_conv3x3_tc<<<grid, CNN_M, 0, st>>>(x, nplanes, H, W, wts, bias, relu, y, ny, yb, err), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -158,7 +207,11 @@ int snac_cnn_conv3x3(const float *x, int nplanes, int H, int W, const float *wts
   if (!x || !wts || !bias || !y || nplanes < 1 || H < 1 || W < 1) { set_error("snac_cnn_conv3x3: bad argument"); return SNAC_ERR_ARG; }
   const size_t n = (size_t)nplanes * 16 * H * W;
   std::vector<__nv_bfloat16> xb(n);
-  for (size_t i = 0; i < n; i++) xb[i] = __float2bfloat16(x[i]);
+  for (int p = 0; p < nplanes; p++)
+    for (int c = 0; c < 16; c++)
+      for (int h = 0; h < H; h++)
+        for (int w = 0; w < W; w++)
+          xb[act_idx(p, c, h, w, H, W)] = __float2bfloat16(x[(((size_t)p * 16 + c) * H + h) * W + w]);
   __nv_bfloat16 *dx = nullptr;
   float *dw = nullptr, *db = nullptr, *dy = nullptr;
   int *derr = nullptr;

@@ -39,8 +39,8 @@ constexpr int GB = 16;               // planes per training batch (snac_guess_tr
 __global__ void __launch_bounds__(256) k_gn_input(const double *__restrict__ r, const unsigned short *__restrict__ code,
                                                   const double *__restrict__ shift, double lam_scale,
                                                   const int *__restrict__ singular, const int *__restrict__ sys,
-                                                  long ncell, __nv_bfloat16 *__restrict__ x0, float *__restrict__ rms,
-                                                  float *__restrict__ xf) {
+                                                  long ncell, int H, int W, __nv_bfloat16 *__restrict__ x0,
+                                                  float *__restrict__ rms, float *__restrict__ xf) {
   const int p = blockIdx.x, s = sys[p];
   const double *rs = r + ncell * s;
   double acc = 0.0, cnt = 0.0;
@@ -58,10 +58,13 @@ __global__ void __launch_bounds__(256) k_gn_input(const double *__restrict__ r, 
     const bool live = m > 0.0 && !(code[c] & 0x8000);
     const float v = live ? (float)(rs[c] / m) : 0.f;
     if (x0) {
-      __nv_bfloat16 *o = x0 + (long)p * GC * ncell;
-      o[c] = __float2bfloat16(v);
-      o[ncell + c] = __float2bfloat16(live ? lam : 0.f);
-      for (int ch = 2; ch < GC; ch++) o[ch * ncell + c] = __float2bfloat16(0.f);
+      const int h = (int)(c / W), w = (int)(c - (long)h * W);
+      __nv_bfloat16 *o = x0 + act_idx(p, 0, h, w, H, W);
+      o[0] = __float2bfloat16(v);
+      o[1] = __float2bfloat16(live ? lam : 0.f);
+      for (int ch = 2; ch < 8; ch++) o[ch] = __float2bfloat16(0.f);
+      __nv_bfloat16 *o2 = x0 + act_idx(p, 8, h, w, H, W);
+      for (int ch = 0; ch < 8; ch++) o2[ch] = __float2bfloat16(0.f);
     }
     if (xf) xf[(long)p * ncell + c] = v;
   }
@@ -141,15 +144,18 @@ __global__ void __launch_bounds__(256) k_gn_target(const double *__restrict__ xn
 
 // BF16 network input of recorded planes idx[0..nb) (channel 0 the stored residual, channel 1 lambda)
 __global__ void k_gn_gather(const float *__restrict__ rec_x, const float *__restrict__ rec_lam, const int *__restrict__ idx,
-                            long ncell, __nv_bfloat16 *__restrict__ x0) {
+                            long ncell, int H, int W, __nv_bfloat16 *__restrict__ x0) {
   const int p = blockIdx.y, q = idx[p];
   const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncell) return;
   const float v = rec_x[(long)q * ncell + c];
-  __nv_bfloat16 *o = x0 + (long)p * GC * ncell;
-  o[c] = __float2bfloat16(v);
-  o[ncell + c] = __float2bfloat16(v != 0.f || rec_lam[q] != 0.f ? rec_lam[q] : 0.f);
-  for (int ch = 2; ch < GC; ch++) o[ch * ncell + c] = __float2bfloat16(0.f);
+  const int h = (int)(c / W), w = (int)(c - (long)h * W);
+  __nv_bfloat16 *o = x0 + act_idx(p, 0, h, w, H, W);
+  o[0] = __float2bfloat16(v);
+  o[1] = __float2bfloat16(v != 0.f || rec_lam[q] != 0.f ? rec_lam[q] : 0.f);
+  for (int ch = 2; ch < 8; ch++) o[ch] = __float2bfloat16(0.f);
+  __nv_bfloat16 *o2 = x0 + act_idx(p, 8, h, w, H, W);
+  for (int ch = 0; ch < 8; ch++) o2[ch] = __float2bfloat16(0.f);
 }
 
 // loss (1/B) sum_p |y3 - t|^2 / |t|^2 per plane and its gradient on channel 0 (other channels 0)
@@ -191,11 +197,10 @@ __global__ void __launch_bounds__(256) k_gn_dw(const float *__restrict__ d, cons
     const float g = d[(long)p * GC * plane + co * plane + px];
     if (g == 0.f) continue;
     accb += g;
-    const __nv_bfloat16 *xs = x + (long)p * GC * plane + (long)ci * plane;
 #pragma unroll
     for (int q = 0; q < 9; q++) {
       const int hh = h + q / 3 - 1, ww = w + q % 3 - 1;
-      if (hh >= 0 && hh < H && ww >= 0 && ww < W) acc[q] = fmaf(g, __bfloat162float(xs[(long)hh * W + ww]), acc[q]);
+      if (hh >= 0 && hh < H && ww >= 0 && ww < W) acc[q] = fmaf(g, __bfloat162float(x[act_idx(p, ci, hh, ww, H, W)]), acc[q]);
     }
   }
   for (int q = 0; q < 9; q++) {
@@ -357,7 +362,11 @@ int snac_guess_grad(const float *x, const float *target, int nb, int H, int W, c
   const long plane = (long)H * W, n = (long)nb * GC * plane;
   SNAC_CUDA(cudaMemcpy(net.par, params, GuessNet::NPAR * 4, cudaMemcpyHostToDevice));
   std::vector<__nv_bfloat16> xb(n);
-  for (long i = 0; i < n; i++) xb[i] = __float2bfloat16(x[i]);
+  for (int p = 0; p < nb; p++)
+    for (int c = 0; c < GC; c++)
+      for (int h = 0; h < H; h++)
+        for (int w = 0; w < W; w++)
+          xb[act_idx(p, c, h, w, H, W)] = __float2bfloat16(x[(((long)p * GC + c) * H + h) * W + w]);
   SNAC_CUDA(cudaMemcpy(net.xb[0], xb.data(), n * 2, cudaMemcpyHostToDevice));
   float *tg = (float *)net.alloc(nb * plane * 4), *tn = (float *)net.alloc(nb * 4);
   if (!tg || !tn) { set_error("device allocation failed"); return SNAC_ERR_NOMEM; }
@@ -479,8 +488,8 @@ int guess_before(Domain &d, PoissonSolver &S, cudaStream_t st) {
     SNAC_TRY(g->net.ensure(g->nsys, g->H, g->W));
     x0 = g->net.xb[0];
   }
-  k_gn_input<<<g->nsys, 256, 0, st>>>(g->r, P.L[0].code, P.shift, g->lam_scale, P.singular, g->sys, g->ncell, x0, g->rms,
-                                      g->mode == 1 ? g->xf : nullptr), ::snac::count_launch();
+  k_gn_input<<<g->nsys, 256, 0, st>>>(g->r, P.L[0].code, P.shift, g->lam_scale, P.singular, g->sys, g->ncell, g->H,
+                                      g->W, x0, g->rms, g->mode == 1 ? g->xf : nullptr), ::snac::count_launch();
   if (g->mode == 2) {
     SNAC_TRY(g->net.forward(g->nsys, false, st));
     const MgLevelD &L = P.L[0];
@@ -570,7 +579,7 @@ int snac_guess_train(int iters, double lr, double *loss_first, double *loss_last
     for (int q = 0; q < GB; q++) ids[q] = pick(g.rng);
     SNAC_CUDA(cudaMemcpyAsync(g.net.idx, ids, sizeof(ids), cudaMemcpyHostToDevice, st));
     k_gn_gather<<<dim3((unsigned)((g.ncell + 255) / 256), GB), 256, 0, st>>>(g.rec_x, g.rec_lam, g.net.idx, g.ncell,
-                                                                           g.net.xb[0]), ::snac::count_launch();
+                                                                           g.H, g.W, g.net.xb[0]), ::snac::count_launch();
     SNAC_TRY(g.net.forward(GB, true, st));
     k_gn_loss<<<GB, 256, 0, st>>>(g.net.y[GL - 1], g.rec_t, g.rec_tn, g.net.idx, GB, g.ncell, g.net.d[GL - 1], g.net.lpart), ::snac::count_launch();
     SNAC_TRY(g.net.backward(GB, st));

@@ -65,6 +65,11 @@ inline int field_hi(const HostBlock &H, int field, int p) {
 
 struct HelmBlk;  // per-block tables of a Helmholtz solver (k_helm.cu)
 struct GuessState;  // the learned initial guess (k_guess.cu)
+// BF16 activations of the guess network: plane p, row h, channel half c/8, pixel w, 8 channels of 2 bytes
+// (each pixel's half is one 16-byte record; the tensor-core convolution reads the records as its operands)
+__host__ __device__ inline long act_idx(int p, int c, int h, int w, int H, int W) {
+  return ((((long)p * H + h) * 2 + (c >> 3)) * W + w) * 8 + (c & 7);
+}
 void guess_destroy(GuessState *g);
 
 // the device multigrid problem plus its host-side construction data
