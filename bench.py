@@ -316,8 +316,9 @@ def main():
                     help="channel: the benchmark workload; small: the same layout at test size")
     ap.add_argument("--no-graph", action="store_true", help="launch the refinement steps one kernel at a time")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess path (record, train, time)")
-    ap.add_argument("--only", choices=["mixed", "plain"], default=None,
-                    help="run one path once and print its timing only (used for ncu launch lists)")
+    ap.add_argument("--only", choices=["mixed", "plain", "learned"], default=None,
+                    help="run one path once and print its timing only (used for ncu launch lists; learned: "
+                         "1 recorded step and 20 training iterations)")
     args = ap.parse_args()
     global USE_GRAPH
     if args.no_graph:
@@ -354,6 +355,11 @@ def main():
     if world > 1 and not torch.distributed.is_initialized():
         torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     device = local
+    if args.only == "learned":
+        r = run_learned_path(case_fn, args.steps, args.warmup, device, record=1, train_iters=20)
+        if rank == 0:
+            print(json.dumps({"path": "learned", **r}), flush=True)
+        return
     if args.only:
         r = run_gpu_path(case_fn, 1 if args.only == "mixed" else 0, args.steps, args.warmup, device)
         if rank == 0:
