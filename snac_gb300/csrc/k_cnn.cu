@@ -184,12 +184,9 @@ __global__ void __launch_bounds__(CNN_M) k_conv3x3_tc(const __nv_bfloat16 *__res
 
 int launch_conv3x3_tc(const __nv_bfloat16 *x, int nplanes, int H, int W, const float *wts, const float *bias, int relu,
                       float *y, int ny, __nv_bfloat16 *yb, int *err, cudaStream_t st) {
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    SNAC_CUDA(cudaGetDevice(&dev));
-    SNAC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  }
+  int dev = 0, nsm = 0;  // the current device's multiprocessors (an attribute query, no synchronisation)
+  SNAC_CUDA(cudaGetDevice(&dev));
+  SNAC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   const long total = (long)nplanes * H * ((W + CNN_M - 1) / CNN_M);
   const int grid = (int)std::min<long>(total, (long)nsm * 8);  // persistent CTAs, 8 per SM
   k_conv3x3_tc<<<grid, CNN_M, 0, st>>>(x, nplanes, H, W, wts, bias, relu, y, ny, yb, err), ::snac::count_launch();
