@@ -127,10 +127,13 @@ def test_solve_pressure_matches_oracle(snac_lib, oracle_mod, precision):
         d.close()
 
 
+@pytest.mark.parametrize("nu_coarse", [0, 2])
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("which", ["channel", "ldc3d"])
-def test_fused_vcycle_matches_unfused(snac_lib, monkeypatch, precision, which):
-    """The tiled smoother / one-CTA coarse tail give the same solves as one kernel per sweep.
+def test_fused_vcycle_matches_unfused(snac_lib, monkeypatch, precision, which, nu_coarse):
+    """The tiled smoother / one-CTA coarse tail give the same solves as one kernel per sweep, with the
+    default smoothing counts (one sweep per side on levels 2 and coarser with a transform axis) and with
+    two sweeps everywhere.
 
     The V-cycles agree term by term; r.z is summed in a different order (tile partials against
     flat partials), so the two converged solutions agree to the solver tolerance, not bitwise.
@@ -142,7 +145,7 @@ def test_fused_vcycle_matches_unfused(snac_lib, monkeypatch, precision, which):
         # "1": one kernel per sweep; "0": every fused kernel of both precisions (mask 15)
         monkeypatch.setenv("SNAC_MG_UNFUSED", mode)
         monkeypatch.setenv("SNAC_MG_FUSE", "15")
-        d = Domain(case, precision=precision)
+        d = Domain(case, precision=precision, nu_coarse=nu_coarse)
         try:
             rng = np.random.default_rng(11)
             for ib in range(len(case.blocks)):
