@@ -607,7 +607,8 @@ int mg_residual(const MgProblem &P, CgWork &W, const T *x, const T *b, T *r, dou
   else
     SNAC_TRY(plane_resid<T>(P, shift_of<T>(P), W.active, x, b, r, W.part0, set_bb ? W.part1 : nullptr, W.stride, st));
   SNAC_CUDA(cudaMemsetAsync(W.d_count, 0, 2 * sizeof(int), st));
-  k_cg_norms<<<P.nsys, 256, 0, st>>>(W.active, nullptr, W.sc, W.part0, W.part1, W.stride, nchunk_red(P, L0), tol,
+  const int nres = P.mode3d ? nchunk_red(P, L0) : plane_resid_nchunk(L0, sizeof(T) == 8 ? 1 : 0);
+  k_cg_norms<<<P.nsys, 256, 0, st>>>(W.active, nullptr, W.sc, W.part0, W.part1, W.stride, nres, tol,
                                      set_bb, want_scale, nact, W.d_count, nullptr, 0.0), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;

@@ -27,6 +27,11 @@ const dim3 BLK(32, 8);
 
 // partials per system written by plane_resid / plane_apply (one per 32 x 8*RROWS patch)
 int plane_nchunk(const MgLevelD &L) { return ((L.n[0] + 31) / 32) * ((L.n[1] + 8 * RROWS - 1) / (8 * RROWS)); }
+// partials per system written by plane_resid in FP64 (prec 1, 4 rows per thread) or FP32
+int plane_resid_nchunk(const MgLevelD &L, int prec) {
+  const int rr = prec ? 4 : RROWS;
+  return ((L.n[0] + 31) / 32) * ((L.n[1] + 8 * rr - 1) / (8 * rr));
+}
 
 // systems per CTA: enough CTAs for about `waves` waves of `per_sm` resident CTAs on every multiprocessor
 // (SNAC_MG_WAVES overrides the default of 2; a large value gives one system per CTA)
@@ -132,20 +137,22 @@ __global__ void k_p_invd(MgLevelD L, const T *__restrict__ shift, T *__restrict_
 }
 
 // ---------------------------------------------------------------- Krylov kernels
-// r = b - A x; partials of r.r (and b.b when part_bb); RROWS rows per thread
-template <typename T>
+// r = b - A x; partials of r.r (and b.b when part_bb); RR rows per thread.  FP64 arithmetic is the scarce
+// resource here: every FP64 add of the block reduction costs as much as a stencil FMA, so the FP64 residual
+// gives each thread 4 rows (one reduction tree per 4 cells) and reduces b.b only when it is asked for.
+template <typename T, int RR>
 __global__ void __launch_bounds__(256) k_p_resid(MgLevelD L, int per0, int per1, const T *__restrict__ shift,
                                                  const int *__restrict__ active, int nsys, int sb,
                                                  const T *__restrict__ x, const T *__restrict__ b,
                                                  T *__restrict__ r, double *__restrict__ part_rr,
                                                  double *__restrict__ part_bb, int stride) {
   const int i = blockIdx.x * 32 + threadIdx.x;
-  PlaneCell<T> pc[RROWS];
-  T ccv[RROWS], wtv[RROWS];
+  PlaneCell<T> pc[RR];
+  T ccv[RR], wtv[RR];
   unsigned inb = 0, live = 0;
 #pragma unroll
-  for (int q = 0; q < RROWS; q++) {
-    const int j = blockIdx.y * (8 * RROWS) + threadIdx.y + 8 * q;
+  for (int q = 0; q < RR; q++) {
+    const int j = blockIdx.y * (8 * RR) + threadIdx.y + 8 * q;
     ccv[q] = wtv[q] = T(0);
     pc[q] = PlaneCell<T>{0, 0, 0, 0, 0, T(0), T(0), T(0), T(0)};
     if (i < L.n[0] && j < L.n[1]) {
@@ -166,7 +173,7 @@ __global__ void __launch_bounds__(256) k_p_resid(MgLevelD L, int per0, int per1,
     const T sh = shift[s];
     T rr = 0, bb = 0;
 #pragma unroll
-    for (int q = 0; q < RROWS; q++) {
+    for (int q = 0; q < RR; q++) {
       if (!(inb >> q & 1)) continue;
       const int c = pc[q].c;
       T rv = 0;
@@ -179,8 +186,9 @@ __global__ void __launch_bounds__(256) k_p_resid(MgLevelD L, int per0, int per1,
       }
       r[off + c] = rv;
     }
-    double trr, tbb;
-    block_sum2<T>(rr, bb, trr, tbb);
+    double trr, tbb = 0.0;
+    if (part_bb) block_sum2<T>(rr, bb, trr, tbb);
+    else trr = block_sum1<T>(rr);
     if (threadIdx.x == 0 && threadIdx.y == 0) {
       part_rr[(long)s * stride + chunk] = trr;
       if (part_bb) part_bb[(long)s * stride + chunk] = tbb;
@@ -310,12 +318,13 @@ static int red_batch(const MgProblem &P, long ctas_per_system) {
 template <typename T>
 int plane_resid(const MgProblem &P, const T *shift, const int *active, const T *x, const T *b, T *r, double *part_rr,
                 double *part_bb, int stride, cudaStream_t st) {
+  constexpr int RR = sizeof(T) == 8 ? 4 : RROWS;
   const MgLevelD &L = P.L[0];
-  const dim3 g((unsigned)((L.n[0] + 31) / 32), (unsigned)((L.n[1] + 8 * RROWS - 1) / (8 * RROWS)), 1);
+  const dim3 g((unsigned)((L.n[0] + 31) / 32), (unsigned)((L.n[1] + 8 * RR - 1) / (8 * RR)), 1);
   const int sb = red_batch(P, (long)g.x * g.y);
   const dim3 gz(g.x, g.y, (unsigned)((P.nsys + sb - 1) / sb));
-  k_p_resid<T><<<gz, BLK, 0, st>>>(L, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, x, b, r, part_rr,
-                                   part_bb, stride), ::snac::count_launch();
+  k_p_resid<T, RR><<<gz, BLK, 0, st>>>(L, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, x, b, r, part_rr,
+                                       part_bb, stride), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

@@ -81,6 +81,7 @@ int launch_vcycle_coarse(const MgProblem &P, int l0, const T *shift, const int *
 // plane-mode kernels batched over systems (k_mg_plane.cu)
 int plane_batch(const MgProblem &P, long ctas_per_system, int per_sm);
 int plane_nchunk(const MgLevelD &L);
+int plane_resid_nchunk(const MgLevelD &L, int prec);
 template <typename T> int plane_sweep(const MgProblem &P, int l, const T *shift, const int *active, int color, T *x,
                                       const T *b, cudaStream_t st);
 template <typename T> int plane_restrict(const MgProblem &P, int l, const T *shift, const int *active, const T *xf,
