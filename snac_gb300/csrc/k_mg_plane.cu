@@ -141,7 +141,7 @@ __global__ void k_p_invd(MgLevelD L, const T *__restrict__ shift, T *__restrict_
 // resource here: every FP64 add of the block reduction costs as much as a stencil FMA, so the FP64 residual
 // gives each thread 4 rows (one reduction tree per 4 cells) and reduces b.b only when it is asked for.
 template <typename T, int RR>
-__global__ void __launch_bounds__(256) k_p_resid(MgLevelD L, int per0, int per1, const T *__restrict__ shift,
+__global__ void __launch_bounds__(256, (RR >= 4 ? 3 : 1)) k_p_resid(MgLevelD L, int per0, int per1, const T *__restrict__ shift,
                                                  const int *__restrict__ active, int nsys, int sb,
                                                  const T *__restrict__ x, const T *__restrict__ b,
                                                  T *__restrict__ r, double *__restrict__ part_rr,
