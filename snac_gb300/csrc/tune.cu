@@ -12,13 +12,17 @@
 namespace snac {
 namespace {
 
+struct SnapArray {
+  double *live, *copy;
+  size_t bytes;
+};
 struct Snapshot {
-  std::vector<std::pair<double *, double *>> arrays;  // (live array, copy)
+  std::vector<SnapArray> arrays;
   std::vector<std::pair<size_t, double *>> boxes;     // per solver slot (0 pressure, 1.. Helmholtz): size, copy
   double dt = 0.0, time = 0.0;
   int istep = 0;
   ~Snapshot() {
-    for (auto &a : arrays) cudaFree(a.second);
+    for (auto &a : arrays) cudaFree(a.copy);
     for (auto &b : boxes) cudaFree(b.second);
   }
 };
@@ -27,7 +31,7 @@ int snap_array(Snapshot &s, double *live, size_t bytes, cudaStream_t st) {
   if (!live) return SNAC_OK;
   double *c = nullptr;
   if (cudaMalloc(&c, bytes) != cudaSuccess) { set_error("snac_autotune: device allocation failed (snapshot)"); return SNAC_ERR_NOMEM; }
-  s.arrays.push_back({live, c});
+  s.arrays.push_back({live, c, bytes});
   SNAC_CUDA(cudaMemcpyAsync(c, live, bytes, cudaMemcpyDeviceToDevice, st));
   return SNAC_OK;
 }
@@ -84,18 +88,7 @@ int rebuild(Domain &d) {
 
 int restore(Domain &d, const Snapshot &s, bool boxes) {
   cudaStream_t st = d.st;
-  size_t k = 0;
-  for (int b = 0; b < d.nblocks; b++) {
-    const DBlock &B = d.db[b];
-    const size_t nh = (size_t)(B.n[0] + 2) * (B.n[1] + 2) * (B.n[2] + 2) * sizeof(double);
-    const size_t ni = (size_t)B.n[0] * B.n[1] * B.n[2] * sizeof(double);
-    std::vector<size_t> sizes{nh, nh, nh, nh, nh, ni, ni, ni};
-    for (int q = 0; q < d.c.nscal; q++) { sizes.push_back(nh); sizes.push_back(ni); }
-    for (size_t z : sizes) {
-      const auto &a = s.arrays[k++];
-      SNAC_CUDA(cudaMemcpyAsync(a.first, a.second, z, cudaMemcpyDeviceToDevice, st));
-    }
-  }
+  for (const SnapArray &a : s.arrays) SNAC_CUDA(cudaMemcpyAsync(a.live, a.copy, a.bytes, cudaMemcpyDeviceToDevice, st));
   if (boxes) {
     const auto sv = solvers(d);
     for (size_t i = 0; i < sv.size() && i < s.boxes.size(); i++)
