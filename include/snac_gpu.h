@@ -201,8 +201,8 @@ int snac_chkdiv(const int lo[3], const int hi[3], const double *dxf, const doubl
  * its time loop, where cudaMalloc/cudaFree would synchronise the device or fail on a full GPU):
  * u, v, w (halo'd) and dxf, dyf, dzf ((n+2) entries) are DEVICE pointers, stream is a cudaStream_t
  * (NULL = default stream), divtot/divmax are host pointers.  Scratch is a fixed 128 KiB device array
- * owned by the library (held on every GPU that loads it until exit); blocks above 2^31-1 cells are
- * rejected with SNAC_ERR_ARG.  The first call on a device resolves the array's address with that
+ * owned by the library (held on every GPU that loads it until exit); blocks above 2^31-1 cells, or
+ * above 2^31-65 cells along one axis, are rejected with SNAC_ERR_ARG.  The first call on a device resolves the array's address with that
  * device current -- make it before any stream capture; calls that overlap on the GPU race on the
  * shared array. */
 int snac_chkdiv_noalloc(const int lo[3], const int hi[3], const double *dxf, const double *dyf,
@@ -312,6 +312,11 @@ typedef struct snac_tune_result {
   int ncand;            /* candidates timed */
 } snac_tune_result;
 int snac_autotune(int steps, snac_tune_result *out);
+/* No counterpart in the reference: a host-side fault injector for testing snac_autotune's error paths.  The
+ * next snac_autotune call fails with SNAC_ERR_STATE right after rebuilding the solvers of candidate
+ * `candidate` (0-based; -1 clears), which must leave the settings, the solvers and the state as they were
+ * before the call.  Nothing on the device is made to fail. */
+int snac_tune_inject_failure(int candidate);
 
 /* whole RK3 steps, main.f90:893-1069 (dt from chkdt every icheck steps) */
 int snac_step(int nsteps);

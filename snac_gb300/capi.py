@@ -129,6 +129,7 @@ PROTOTYPES = {
     "snac_guess_train": (C.c_int, [C.c_int, C.c_double, DP, DP, IP]),
     "snac_guess_measure": (C.c_int, [C.c_int, DP, DP]),
     "snac_autotune": (C.c_int, [C.c_int, C.POINTER(TuneResult)]),
+    "snac_tune_inject_failure": (C.c_int, [C.c_int]),
     "snac_set_fields": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_void_p)]),
     "snac_get_fields": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_void_p)]),
     "snac_out1d_write": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int]),

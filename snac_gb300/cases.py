@@ -366,6 +366,26 @@ def channel_initial_condition(case: Case, yc_of_block, seed: int = 0x5EED, amp: 
     return out
 
 
+def tgv_initial_condition(case: Case, grid):
+    """Taylor-Green vortex on the MAC grid: u = sin x cos y cos z at the x faces, v = -cos x sin y cos z at the
+    y faces, w = 0, and the analytic pressure p = (cos 2x + cos 2y)(cos 2z + 2)/16 at the cell centres.
+
+    grid(ib, axis, which) returns the (ng+2) coordinates of block ib (which = G_XC centres, G_XF faces).
+    Returns {ib: (u, v, w, p)} halo'd arrays, ghosts included."""
+    from .capi import G_XC, G_XF
+    out = {}
+    for ib, _ in enumerate(case.blocks):
+        xc, yc, zc = (grid(ib, a, G_XC) for a in range(3))
+        xf, yf = grid(ib, 0, G_XF), grid(ib, 1, G_XF)
+        u = np.asfortranarray(np.sin(xf)[:, None, None] * np.cos(yc)[None, :, None] * np.cos(zc)[None, None, :])
+        v = np.asfortranarray(-np.cos(xc)[:, None, None] * np.sin(yf)[None, :, None] * np.cos(zc)[None, None, :])
+        w = np.zeros_like(u, order="F")
+        p = np.asfortranarray((np.cos(2 * xc)[:, None, None] + np.cos(2 * yc)[None, :, None])
+                              * (np.cos(2 * zc)[None, None, :] + 2.0) / 16.0)
+        out[ib] = (u, v, w, p)
+    return out
+
+
 def splitmix64_uniform_fast(seed: int, n: int) -> np.ndarray:
     """Vectorised splitmix64 (identical output to splitmix64_uniform)."""
     with np.errstate(over="ignore"):

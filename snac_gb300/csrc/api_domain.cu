@@ -1023,13 +1023,21 @@ static int copy_fields(Domain &d, int n, const int *ib, const int *field, void *
     if (!host[q]) { set_error("batched field copy: null host array %d", q); return SNAC_ERR_ARG; }
   }
   SNAC_CUDA(cudaStreamSynchronize(d.st));  // the fields are not in use by queued work
-  for (int q = 0; q < n; q++) {
+  // on a failed copy the copies already issued may still be reading or writing the caller's host arrays:
+  // both streams are drained before the first error is returned
+  cudaError_t first = cudaSuccess;
+  for (int q = 0; q < n && first == cudaSuccess; q++) {
     cudaStream_t s = (q & 1) ? d.st_copy : d.st;
-    if (to_device) SNAC_CUDA(cudaMemcpyAsync(dev[q].first, host[q], dev[q].second, cudaMemcpyHostToDevice, s));
-    else SNAC_CUDA(cudaMemcpyAsync(host[q], dev[q].first, dev[q].second, cudaMemcpyDeviceToHost, s));
+    first = to_device ? cudaMemcpyAsync(dev[q].first, host[q], dev[q].second, cudaMemcpyHostToDevice, s)
+                      : cudaMemcpyAsync(host[q], dev[q].first, dev[q].second, cudaMemcpyDeviceToHost, s);
   }
-  SNAC_CUDA(cudaStreamSynchronize(d.st_copy));
-  SNAC_CUDA(cudaStreamSynchronize(d.st));
+  const cudaError_t e1 = cudaStreamSynchronize(d.st_copy);
+  const cudaError_t e2 = cudaStreamSynchronize(d.st);
+  if (first != cudaSuccess)
+    return cuda_fail(first, to_device ? "cudaMemcpyAsync (host to device)" : "cudaMemcpyAsync (device to host)",
+                     __FILE__, __LINE__);
+  SNAC_CUDA(e1);
+  SNAC_CUDA(e2);
   return SNAC_OK;
 }
 

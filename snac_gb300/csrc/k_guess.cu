@@ -544,6 +544,13 @@ int guess_after(Domain &d, PoissonSolver &S, cudaStream_t st) {
 
 }  // namespace snac
 
+namespace snac {
+int guess_get_mode(const Domain &d) { return d.guess ? d.guess->mode : 0; }
+void guess_set_mode(Domain &d, int mode) {
+  if (d.guess) d.guess->mode = mode;
+}
+}  // namespace snac
+
 int snac_guess_mode(int mode) {
   Domain *d = domain();
   if (!d) { set_error("snac_guess_mode: no domain (call snac_init first)"); return SNAC_ERR_STATE; }

@@ -16,8 +16,8 @@
 //   * scratch: SNAC_NOALLOC_CTAS = 8192 (sum, max) pairs plus one final pair,
 //     128 KiB, resident on every GPU that loads the library until the process
 //     exits; each CTA walks its share of the block's 32x4x2 tiles in a fixed
-//     order, so any block works up to 2^31 - 1 interior cells; larger blocks
-//     are rejected with SNAC_ERR_ARG;
+//     order, so any block works up to 2^31 - 1 interior cells (and 2^31 - 65
+//     along one axis); larger blocks are rejected with SNAC_ERR_ARG;
 //   * the first call on a device looks the array's device address up with
 //     cudaGetSymbolAddress, with that device current; make the first call
 //     before any stream capture begins;
@@ -35,6 +35,7 @@ namespace {
 constexpr int NTX = 32, NTY = 4, NTZ = 2;      // tile of one CTA pass
 constexpr int NCTA = 8192;                      // SNAC_NOALLOC_CTAS
 constexpr long MAX_CELLS = 2147483647L;         // 2^31 - 1 interior cells per block
+constexpr long MAX_EXTENT = 2147483647L - 64;   // cells along one axis (the 1-D metric arrays have n + 2)
 
 static __device__ __align__(256) double g_scratch[2 * NCTA + 2];
 
@@ -67,13 +68,14 @@ k_chkdiv_noalloc(int nx, int ny, int nz, long tx, long ty, long ntiles, const do
                  const double *__restrict__ v, const double *__restrict__ w, const double *__restrict__ dxf,
                  const double *__restrict__ dyf, const double *__restrict__ dzf, double rvol,
                  double *__restrict__ part) {
-  const long sy = nx + 2, sz = (long)(nx + 2) * (ny + 2);
+  const long sy = (long)nx + 2, sz = ((long)nx + 2) * ((long)ny + 2);
   double s = 0.0, m = 0.0;
   for (long t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const long bx = t % tx, by = (t / tx) % ty, bz = t / (tx * ty);
-    const int i = (int)(bx * NTX) + threadIdx.x, j = (int)(by * NTY) + threadIdx.y, k = (int)(bz * NTZ) + threadIdx.z;
+    // cell coordinates and the halo'd index in 64-bit arithmetic: an extent near 2^31 stays exact
+    const long i = bx * NTX + threadIdx.x, j = by * NTY + threadIdx.y, k = bz * NTZ + threadIdx.z;
     if (i < nx && j < ny && k < nz) {
-      const long c = hidx(i, j, k, nx, ny);
+      const long c = (i + 1) + sy * (j + 1) + sz * (k + 1);
       const double div = (w[c] - w[c - sz]) / dzf[k + 1] + (v[c] - v[c - sy]) / dyf[j + 1] + (u[c] - u[c - 1]) / dxf[i + 1];
       double a = fabs(div);
       if (!(a == a)) a = __longlong_as_double(0x7ff0000000000000ll);  // NaN -> +Inf, survives fmax
@@ -126,9 +128,9 @@ extern "C" int snac_chkdiv_noalloc(const int lo[3], const int hi[3], const doubl
     set_error("snac_chkdiv_noalloc: hi < lo");
     return SNAC_ERR_ARG;
   }
-  if (nx * ny * nz > MAX_CELLS) {
-    set_error("snac_chkdiv_noalloc: block of %ld x %ld x %ld cells exceeds the limit of %ld cells; use snac_chkdiv",
-              nx, ny, nz, MAX_CELLS);
+  if (nx > MAX_EXTENT || ny > MAX_EXTENT || nz > MAX_EXTENT || nx * ny * nz > MAX_CELLS) {
+    set_error("snac_chkdiv_noalloc: block of %ld x %ld x %ld cells exceeds the limit of %ld cells (%ld along "
+              "one axis); use snac_chkdiv", nx, ny, nz, MAX_CELLS, MAX_EXTENT);
     return SNAC_ERR_ARG;
   }
   const long tx = (nx + NTX - 1) / NTX, ty = (ny + NTY - 1) / NTY, tz = (nz + NTZ - 1) / NTZ;

@@ -179,6 +179,9 @@ int helm_io(Domain &d, PoissonSolver &S, double *box, int to_box, cudaStream_t s
 int solver_solve_pressure(Domain &d, PoissonSolver &S);
 int guess_before(Domain &d, PoissonSolver &S, cudaStream_t st);
 int guess_after(Domain &d, PoissonSolver &S, cudaStream_t st);
+// mode of the learned guess (0 when it was never set up); set only changes an existing guess state
+int guess_get_mode(const Domain &d);
+void guess_set_mode(Domain &d, int mode);
 
 // transforms (k_fft.cu)
 int fft_forward_to_box(Domain &d, PoissonSolver &S, cudaStream_t st);

@@ -5,6 +5,7 @@
 // solve to the same tolerance.  Each candidate rebuilds the
 // solvers and runs from the same snapshot of the state; the state is restored afterwards, including the
 // solvers' warm starts, so the run continues as if only the settings had changed.
+#include <string>
 #include <vector>
 
 #include "snac_host.h"
@@ -102,10 +103,17 @@ int restore(Domain &d, const Snapshot &s, bool boxes) {
   return SNAC_OK;
 }
 
+int g_fail_candidate = -1;  // snac_tune_inject_failure
+
 }  // namespace
 }  // namespace snac
 
 using namespace snac;
+
+int snac_tune_inject_failure(int candidate) {
+  g_fail_candidate = candidate;
+  return SNAC_OK;
+}
 
 int snac_autotune(int steps, snac_tune_result *out) {
   Domain *d = domain();
@@ -119,8 +127,31 @@ int snac_autotune(int steps, snac_tune_result *out) {
     for (int inner : {4, 5, 6}) cand.push_back({1, inner, nuc});
     cand.push_back({0, 0, nuc});
   }
+  // the timed steps solve the same restored state again and again: recording them as training pairs of the
+  // learned guess would fill its ring with near-copies, so recording pauses while tuning
+  const int gmode0 = guess_get_mode(*d);
+  if (gmode0 == 1) guess_set_mode(*d, 0);
   Snapshot snap;
-  SNAC_TRY(take(*d, snap));
+  // on every way out: the chosen (or, after an error, the original) settings, solvers built for them and the
+  // state of the snapshot, so that the run goes on as if only the settings had changed
+  auto finish = [&](int prec, int inner, int nuc, int rc) -> int {
+    d->opt.precision = prec;
+    d->tune_inner = inner;
+    d->opt.nu_coarse = nuc;
+    const std::string msg = rc != SNAC_OK ? std::string(snac_last_error()) : std::string();
+    int rc2 = rebuild(*d);
+    if (rc2 == SNAC_OK && !snap.arrays.empty()) rc2 = restore(*d, snap, true);
+    guess_set_mode(*d, gmode0);
+    if (rc != SNAC_OK) {
+      set_error("%s", msg.c_str());
+      return rc;
+    }
+    return rc2;
+  };
+  {
+    const int rc = take(*d, snap);
+    if (rc != SNAC_OK) { guess_set_mode(*d, gmode0); return rc; }
+  }
   // the settings in use: one warm-up step and `steps` timed steps from the snapshot
   auto time_current = [&](double *ms) -> int {
     SNAC_TRY(restore(*d, snap, true));
@@ -131,32 +162,33 @@ int snac_autotune(int steps, snac_tune_result *out) {
     return rc;
   };
   double ms_before = 0.0;
-  SNAC_TRY(time_current(&ms_before));
+  {
+    const int rc = time_current(&ms_before);
+    if (rc != SNAC_OK) return finish(prec0, inner0, nuc0, rc);
+  }
   double best = 1e300;
   int bi = -1, ntimed = 0;
   for (size_t i = 0; i < cand.size(); i++) {
     d->opt.precision = cand[i].prec;
     d->tune_inner = cand[i].inner;
     d->opt.nu_coarse = cand[i].nuc;
-    SNAC_TRY(rebuild(*d));
+    int rc = rebuild(*d);
+    if (rc == SNAC_OK && (int)i == g_fail_candidate) {
+      g_fail_candidate = -1;
+      set_error("snac_autotune: failure injected at candidate %d", (int)i);
+      rc = SNAC_ERR_STATE;
+    }
     double ms = 0.0;
-    const int rc = time_current(&ms);
+    if (rc == SNAC_OK) rc = time_current(&ms);
     ntimed++;
     if (rc == SNAC_ERR_NOT_CONVERGED) continue;  // this candidate does not reach the tolerance
-    SNAC_TRY(rc);
+    if (rc != SNAC_OK) return finish(prec0, inner0, nuc0, rc);
     if (ms < best) { best = ms; bi = (int)i; }
   }
-  if (bi < 0) {  // nothing converged: keep the settings that were in use
-    d->opt.precision = prec0;
-    d->tune_inner = inner0;
-    d->opt.nu_coarse = nuc0;
-  } else {
-    d->opt.precision = cand[bi].prec;
-    d->tune_inner = cand[bi].inner;
-    d->opt.nu_coarse = cand[bi].nuc;
-  }
-  SNAC_TRY(rebuild(*d));
-  SNAC_TRY(restore(*d, snap, true));
+  // nothing converged: keep the settings that were in use
+  const int rc = bi < 0 ? finish(prec0, inner0, nuc0, SNAC_OK)
+                        : finish(cand[bi].prec, cand[bi].inner, cand[bi].nuc, SNAC_OK);
+  SNAC_TRY(rc);
   if (out) {
     out->precision = d->opt.precision;
     out->inner_iters = d->ps ? d->ps->inner_iters : 0;

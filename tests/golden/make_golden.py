@@ -9,7 +9,9 @@ import os
 import shutil
 import sys
 
-src_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_golden.py /path/to/SNaC")
+src_root = sys.argv[1]
 here = os.path.dirname(os.path.abspath(__file__))
 shutil.copyfile(os.path.join(src_root, "tests", "lid_driven_cavity", "data_ldc_re1000.txt"),
                 os.path.join(here, "ldc_re1000_profile.txt"))

@@ -634,6 +634,55 @@ def test_autotune_restores_state(snac_lib, precision):
         assert np.max(np.abs(a - b)) <= 1e-9 * np.max(np.abs(a))
 
 
+@pytest.mark.parametrize("fail_at", [0, 3])
+def test_autotune_error_restores_settings_and_state(snac_lib, fail_at):
+    """A candidate that fails part-way (a host-side injected error after its solvers are rebuilt) makes
+    snac_autotune return that error with the original settings, rebuilt solvers and the snapshot's state:
+    the fields, time and step count are unchanged bit for bit and the next steps run as without the call."""
+    case = cases.channel_4block(nx=(16, 32), ny=(8, 16), nz=16)
+    d = Domain(case, precision=1, use_graph=1)
+    try:
+        ic = cases.channel_initial_condition(case, lambda ib: d.grid(ib, 1, capi.G_XC))
+        for ib, (u, v, w) in ic.items():
+            d.set(ib, capi.U, u)
+            d.set(ib, capi.V, v)
+            d.set(ib, capi.W, w)
+        d.bounduvw(False)
+        d.step(2)
+        keys = (capi.U, capi.V, capi.W, capi.P)
+        before = [d.get(ib, k) for ib in range(len(case.blocks)) for k in keys]
+        st0 = d.stats()
+        assert capi.lib().snac_tune_inject_failure(fail_at) == 0
+        with pytest.raises(capi.SnacError) as ei:
+            d.autotune(1)
+        assert ei.value.code == capi.ERR_STATE and "injected" in str(ei.value)
+        after = [d.get(ib, k) for ib in range(len(case.blocks)) for k in keys]
+        for a, b in zip(before, after):
+            np.testing.assert_array_equal(a, b)
+        st1 = d.stats()
+        assert (st1["istep"], st1["time"], st1["dt"]) == (st0["istep"], st0["time"], st0["dt"])
+        assert d.step(2) == 0
+        assert d.stats()["residual"] <= case.tol
+        # the reference run: the same two steps without the failed tuning call, same settings
+        d2 = Domain(case, precision=1, use_graph=1)
+        try:
+            for ib, (u, v, w) in ic.items():
+                d2.set(ib, capi.U, u)
+                d2.set(ib, capi.V, v)
+                d2.set(ib, capi.W, w)
+            d2.bounduvw(False)
+            d2.step(4)
+            for ib in range(len(case.blocks)):
+                for k in keys[:3]:
+                    a, b = d.get(ib, k), d2.get(ib, k)
+                    assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b))
+        finally:
+            d2.close()
+    finally:
+        capi.lib().snac_tune_inject_failure(-1)
+        d.close()
+
+
 def test_batched_field_copies(snac_lib):
     """snac_set_fields / snac_get_fields move the same bytes as the one-field calls (two streams, one
     synchronisation)."""

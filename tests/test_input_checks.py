@@ -78,3 +78,16 @@ def test_one_cell_periodic_axis_accepted():
         case = dataclasses.replace(case, blocks=[dataclasses.replace(b, ng=(16, 16, 1))])
         rc, lev, _ = check(case)
         assert rc == 0, capi.lib().snac_last_error()
+
+
+@pytest.mark.parametrize("hi", [(65536, 65536, 1), (2147483647 - 63, 1, 1), (1, 1, 2147483647)])
+def test_chkdiv_noalloc_rejects_oversized_block(hi):
+    """The allocation-free divergence check rejects, on the host and before any device work, a block above
+    2^31 - 1 cells or one whose extent along an axis leaves no room for the (n + 2)-long metric arrays in
+    32-bit indices; the placeholder device pointers passed here are never dereferenced."""
+    tot, mx = C.c_double(), C.c_double()
+    L = capi.lib()
+    rc = L.snac_chkdiv_noalloc(capi.iarr((1, 1, 1)), capi.iarr(hi), 8, 8, 8, 8, 8, 8, 1.0, None, C.byref(tot),
+                               C.byref(mx))
+    assert rc == capi.ERR_ARG
+    assert b"exceeds" in L.snac_last_error()
