@@ -208,6 +208,23 @@ int snac_chkdiv(const int lo[3], const int hi[3], const double *dxf, const doubl
 int snac_chkdiv_noalloc(const int lo[3], const int hi[3], const double *dxf, const double *dyf,
                         const double *dzf, const double *u, const double *v, const double *w, double vol,
                         void *stream, double *divtot, double *divmax);
+/* bound.f90:8-66 (bounduvw) for one block on the caller's arrays, with the reference's argument list:
+ * cbc[c][d][s] and bc[c][d][s] are the reference's cbc(s,d,c) and bc(s,d,c) of velocity component c along
+ * direction d, is_bound[d][s] and nb[d][s] its is_bound(s,d) and nb(s,d).  The halo exchange (updthalo,
+ * bound.f90:587-650) is made on the device for every side whose neighbour nb[d][s] is `myrank` itself (a
+ * periodic direction this rank spans alone), in the reference's x, y, z order; sides whose neighbour is another
+ * rank are the caller's MPI exchange (their ghost planes are left untouched), and the MPI datatypes `halos`
+ * of the reference have no counterpart here.  Then set_bc on every face with is_bound, face by face in the
+ * reference's order, the wall-normal component skipped when is_correc.  Metrics (n+2 entries from lo-1) and
+ * u, v, w (halo'd) are host arrays, registered (device mirror) or copied around the call. */
+int snac_bounduvw(const char cbc[3][3][2], const int lo[3], const int hi[3], const double bc[3][3][2], int is_correc,
+                  const int is_bound[3][2], const int nb[3][2], int myrank, const double *dxc, const double *dxf,
+                  const double *dyc, const double *dyf, const double *dzc, const double *dzf, double *u, double *v,
+                  double *w);
+/* bound.f90:68-106 (boundp) for one block, as snac_bounduvw for the centred field p (cbc[d][s], bc[d][s] are
+ * cbc(s,d), bc(s,d)). */
+int snac_boundp(const char cbc[3][2], const int lo[3], const int hi[3], const double bc[3][2], const int is_bound[3][2],
+                const int nb[3][2], int myrank, const double *dxc, const double *dyc, const double *dzc, double *p);
 /* bound.f90:108-248 (set_bc) on one face of one halo'd array */
 int snac_set_bc(char ctype, int ibound, const int lo[3], const int hi[3], int idir, int centered,
                 double rvalue, double dr, double *p);

@@ -437,6 +437,61 @@ void or_set_bc(char ctype, int ibound, const int lo[3], const int hi[3], int idi
   (void)nz;
 }
 
+/* updthalo (bound.f90:587-650) of one block whose neighbour on side s of direction idir is the block itself
+ * (a periodic direction it spans alone, MPI_SENDRECV to its own rank): ghost plane lo-1 receives interior
+ * plane hi and ghost plane hi+1 interior plane lo, each plane including the ghost rows of the other two
+ * directions.  Sides whose neighbour is another rank are left alone (that exchange is not this rank's). */
+static void or_self_halo(const int lo[3], const int hi[3], int idir, const int nb[2], int myrank, double *p) {
+  int nx = NX, ny = NY;
+  int n[3] = {nx, ny, NZ};
+  int d = idir - 1;
+  int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;
+  long st[3] = {1, (long)(nx + 2), (long)(nx + 2) * (ny + 2)};
+  for (int b = 0; b < n[t2] + 2; b++)
+    for (int a = 0; a < n[t1] + 2; a++) {
+      long base = a * st[t1] + b * st[t2];
+      if (nb[0] == myrank) p[base] = p[base + (long)n[d] * st[d]];
+      if (nb[1] == myrank) p[base + (long)(n[d] + 1) * st[d]] = p[base + st[d]];
+    }
+}
+
+/* bound.f90:8-66 (bounduvw) for one block: the halo exchange x, y, z of u, v and w (self-neighbour sides
+ * only, see or_self_halo), then set_bc face by face in the reference's order, the wall-normal component
+ * skipped when is_correc.  cbc[c][d][s], bc[c][d][s] hold cbc(s,d,c), bc(s,d,c); metrics from lo-1. */
+void or_bounduvw_block(const char cbc[3][3][2], const int lo[3], const int hi[3], const double bc[3][3][2],
+                       int is_correc, const int is_bound[3][2], const int nb[3][2], int myrank,
+                       const double *dxc, const double *dxf, const double *dyc, const double *dyf,
+                       const double *dzc, const double *dzf, double *u, double *v, double *w) {
+  double *f[3] = {u, v, w};
+  const double *dc[3] = {dxc, dyc, dzc}, *df[3] = {dxf, dyf, dzf};
+  for (int c = 0; c < 3; c++)
+    for (int d = 1; d <= 3; d++) or_self_halo(lo, hi, d, nb[d - 1], myrank, f[c]);
+  for (int d = 0; d < 3; d++)
+    for (int s = 0; s < 2; s++) {
+      if (!is_bound[d][s]) continue;
+      const int q = s ? hi[d] - lo[d] + 1 : 0;  /* dl(lo-1) or dl(hi) */
+      for (int c = 0; c < 3; c++) {
+        const int centered = c != d;
+        if (!centered && is_correc) continue;
+        or_set_bc(cbc[c][d][s], s, lo, hi, d + 1, centered, bc[c][d][s], centered ? dc[d][q] : df[d][q], f[c]);
+      }
+    }
+}
+
+/* bound.f90:68-106 (boundp) for one block, as or_bounduvw_block for one centred field */
+void or_boundp_block(const char cbc[3][2], const int lo[3], const int hi[3], const double bc[3][2],
+                     const int is_bound[3][2], const int nb[3][2], int myrank, const double *dxc,
+                     const double *dyc, const double *dzc, double *p) {
+  const double *dc[3] = {dxc, dyc, dzc};
+  for (int d = 1; d <= 3; d++) or_self_halo(lo, hi, d, nb[d - 1], myrank, p);
+  for (int d = 0; d < 3; d++)
+    for (int s = 0; s < 2; s++) {
+      if (!is_bound[d][s]) continue;
+      const int q = s ? hi[d] - lo[d] + 1 : 0;
+      or_set_bc(cbc[d][s], s, lo, hi, d + 1, 1, bc[d][s], dc[d][q], p);
+    }
+}
+
 /* solver.f90:44-157 (init_bc_rhs).  fft_axis selects the weight of solver.f90:98-106. */
 void or_init_bc_rhs(const char cbc[3][2], const double bc[3][2], const double dl[3][2],
                     const int is_bound[3][2], const int is_centered[3], const int lo[3],

@@ -111,6 +111,8 @@ def lib():
         L.or_chkdiv_local.argtypes = [ip, ip, dp, dp, dp, dp, dp, dp, d, dp, dp]
         L.or_updt_rhs.argtypes = [ip, ip, ip, dp, dp, dp, dp]
         L.or_set_bc.argtypes = [C.c_char, i, ip, ip, i, i, d, d, dp]
+        L.or_bounduvw_block.argtypes = [C.c_char_p, ip, ip, dp, i, ip, ip, i, dp, dp, dp, dp, dp, dp, dp, dp, dp]
+        L.or_boundp_block.argtypes = [C.c_char_p, ip, ip, dp, ip, ip, i, dp, dp, dp, dp]
         L.or_r2r_lines.argtypes = [i, i, i, C.c_long, C.c_long, dp]
         _lib = L
     return _lib

@@ -101,6 +101,13 @@ void or_updt_rhs(const int lo[3], const int hi[3], const int is_bound[3][2],
                  const double *rhsx, const double *rhsy, const double *rhsz, double *p);
 void or_set_bc(char ctype, int ibound, const int lo[3], const int hi[3], int idir,
                int centered, double rvalue, double dr, double *p);
+void or_bounduvw_block(const char cbc[3][3][2], const int lo[3], const int hi[3], const double bc[3][3][2],
+                       int is_correc, const int is_bound[3][2], const int nb[3][2], int myrank,
+                       const double *dxc, const double *dxf, const double *dyc, const double *dyf,
+                       const double *dzc, const double *dzf, double *u, double *v, double *w);
+void or_boundp_block(const char cbc[3][2], const int lo[3], const int hi[3], const double bc[3][2],
+                     const int is_bound[3][2], const int nb[3][2], int myrank, const double *dxc,
+                     const double *dyc, const double *dzc, double *p);
 void or_init_bc_rhs(const char cbc[3][2], const double bc[3][2], const double dl[3][2],
                     const int is_bound[3][2], const int is_centered[3], const int lo[3],
                     const int hi[3], const int periods[3],

@@ -159,6 +159,51 @@ OneBlock::~OneBlock() {
 size_t OneBlock::halo_bytes() const { return (size_t)(hb.n[0] + 2) * (hb.n[1] + 2) * (hb.n[2] + 2) * sizeof(double); }
 size_t OneBlock::interior_bytes() const { return (size_t)hb.n[0] * hb.n[1] * hb.n[2] * sizeof(double); }
 
+namespace {
+// bound.f90:8-106 for one block on the caller's arrays: self-neighbour halo exchange along each direction,
+// then set_bc face by face.  ent[a] holds one BcEntry per field along axis a (both sides in one entry).
+int bound_block(OneBlock &ob, const int *flds, int nf, const int nb[3][2], int myrank,
+                       const std::vector<BcEntry> (&ent)[3]) {
+  int *dfl = nullptr;
+  {
+    double *q = nullptr;
+    SNAC_TRY(ob.scratch(sizeof(int) * 8, &q));
+    dfl = (int *)q;
+    SNAC_CUDA(cudaMemcpy(dfl, flds, nf * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  for (int a = 0; a < 3; a++) {
+    FaceLink fl[2];
+    int nl = 0;
+    for (int sd = 0; sd < 2; sd++)
+      if (nb[a][sd] == myrank) fl[nl++] = FaceLink{0, 0, sd, 0};
+    const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+    const int maxplane = (ob.hb.n[t1] + 2) * (ob.hb.n[t2] + 2);
+    if (nl) {
+      double *q = nullptr;
+      SNAC_TRY(ob.scratch(sizeof(fl), &q));
+      SNAC_CUDA(cudaMemcpy(q, fl, nl * sizeof(FaceLink), cudaMemcpyHostToDevice));
+      SNAC_TRY(launch_exchange(ob.dblk, (const FaceLink *)q, nl, dfl, nf, a, maxplane, 0));
+    }
+  }
+  for (int a = 0; a < 3; a++) {
+    if (ent[a].empty()) continue;
+    const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+    double *q = nullptr;
+    SNAC_TRY(ob.scratch(ent[a].size() * sizeof(BcEntry), &q));
+    SNAC_CUDA(cudaMemcpy(q, ent[a].data(), ent[a].size() * sizeof(BcEntry), cudaMemcpyHostToDevice));
+    SNAC_TRY(launch_setbc(ob.dblk, (const BcEntry *)q, (int)ent[a].size(), a, (ob.hb.n[t1] + 2) * (ob.hb.n[t2] + 2), 0));
+  }
+  SNAC_CUDA(cudaDeviceSynchronize());
+  return SNAC_OK;
+}
+
+bool bound_args_ok(const int lo[3], const int hi[3], const int is_bound[3][2], const int nb[3][2]) {
+  if (!lo || !hi || !is_bound || !nb) { set_error("null argument"); return false; }
+  return true;
+}
+
+}  // namespace
+
 }  // namespace snac
 
 using namespace snac;
@@ -472,6 +517,84 @@ int snac_set_bc(char ctype, int ibound, const int lo[3], const int hi[3], int id
   cudaDeviceSynchronize();
   cudaFree(de);
   SNAC_TRY(rc);
+  SNAC_TRY(Pa.finish());
+  return SNAC_OK;
+}
+
+int snac_bounduvw(const char cbc[3][3][2], const int lo[3], const int hi[3], const double bc[3][3][2], int is_correc,
+                  const int is_bound[3][2], const int nb[3][2], int myrank, const double *dxc, const double *dxf,
+                  const double *dyc, const double *dyf, const double *dzc, const double *dzf, double *u, double *v,
+                  double *w) {
+  if (!bound_args_ok(lo, hi, is_bound, nb) || !cbc || !bc || !dxc || !dxf || !dyc || !dyf || !dzc || !dzf || !u ||
+      !v || !w) {
+    set_error("snac_bounduvw: null argument");
+    return SNAC_ERR_ARG;
+  }
+  OneBlock ob;
+  SNAC_TRY(ob.setup(lo, hi, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, false));
+  ArgArray Ua, Va, Wa;
+  SNAC_TRY(Ua.bind(u, ob.halo_bytes(), true, true));
+  SNAC_TRY(Va.bind(v, ob.halo_bytes(), true, true));
+  SNAC_TRY(Wa.bind(w, ob.halo_bytes(), true, true));
+  ob.hb.u = (double *)Ua.dev; ob.hb.v = (double *)Va.dev; ob.hb.w = (double *)Wa.dev;
+  SNAC_TRY(ob.upload());
+  const double *dc[3] = {dxc, dyc, dzc}, *df[3] = {dxf, dyf, dzf};
+  std::vector<BcEntry> ent[3];
+  for (int a = 0; a < 3; a++)
+    for (int c = 0; c < 3; c++) {
+      BcEntry e;
+      memset(&e, 0, sizeof(e));
+      e.b = 0;
+      e.f = c;
+      const int centered = c != a;
+      bool any = false;
+      for (int sd = 0; sd < 2; sd++) {
+        if (!is_bound[a][sd] || (!centered && is_correc)) continue;
+        const int q = sd ? ob.hb.n[a] : 0;  // dl(lo-1) or dl(hi)
+        bc_mode(cbc[c][a][sd], sd, centered, bc[c][a][sd], centered ? dc[a][q] : df[a][q], &e.mode[sd],
+                &e.factor[sd], &e.sgn[sd]);
+        any = true;
+      }
+      if (any) ent[a].push_back(e);
+    }
+  const int flds[3] = {0, 1, 2};
+  SNAC_TRY(bound_block(ob, flds, 3, nb, myrank, ent));
+  SNAC_TRY(Ua.finish());
+  SNAC_TRY(Va.finish());
+  SNAC_TRY(Wa.finish());
+  return SNAC_OK;
+}
+
+int snac_boundp(const char cbc[3][2], const int lo[3], const int hi[3], const double bc[3][2], const int is_bound[3][2],
+                const int nb[3][2], int myrank, const double *dxc, const double *dyc, const double *dzc, double *p) {
+  if (!bound_args_ok(lo, hi, is_bound, nb) || !cbc || !bc || !dxc || !dyc || !dzc || !p) {
+    set_error("snac_boundp: null argument");
+    return SNAC_ERR_ARG;
+  }
+  OneBlock ob;
+  SNAC_TRY(ob.setup(lo, hi, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, false));
+  ArgArray Pa;
+  SNAC_TRY(Pa.bind(p, ob.halo_bytes(), true, true));
+  ob.hb.p = (double *)Pa.dev;
+  SNAC_TRY(ob.upload());
+  const double *dc[3] = {dxc, dyc, dzc};
+  std::vector<BcEntry> ent[3];
+  for (int a = 0; a < 3; a++) {
+    BcEntry e;
+    memset(&e, 0, sizeof(e));
+    e.b = 0;
+    e.f = 3;
+    bool any = false;
+    for (int sd = 0; sd < 2; sd++) {
+      if (!is_bound[a][sd]) continue;
+      const int q = sd ? ob.hb.n[a] : 0;
+      bc_mode(cbc[a][sd], sd, 1, bc[a][sd], dc[a][q], &e.mode[sd], &e.factor[sd], &e.sgn[sd]);
+      any = true;
+    }
+    if (any) ent[a].push_back(e);
+  }
+  const int flds[1] = {3};
+  SNAC_TRY(bound_block(ob, flds, 1, nb, myrank, ent));
   SNAC_TRY(Pa.finish());
   return SNAC_OK;
 }

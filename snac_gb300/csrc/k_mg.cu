@@ -281,50 +281,67 @@ __device__ __forceinline__ double cta_sum_parts(const double *part, int s, int s
   return tot;
 }
 
-// partial dot a.b (flat) with the projection of b folded in: for a singular system b -= mean(b) over its
-// active cells first (the mean from the k_sum_active partials; the same rounding as k_sub_mean), written
-// back, and the dot taken with the projected b
-template <typename T>
-__global__ void __launch_bounds__(256) k_cg_dot_proj(MgLevelD L, const int *active, const int *singular,
-                                                     const T *a, T *b, double *part, int stride,
-                                                     const double *part_s, const double *part_n, int nchunk_s) {
-  const int s = blockIdx.y;
-  if (active && !active[s]) return;
-  const long n = L.ncell;
-  const long base = (long)blockIdx.x * FLAT + threadIdx.x, o = n * s;
-  T v = 0;
-  if (singular[s]) {
-    const double na = cta_sum_parts(part_n, s, stride, nchunk_s);
-    const double sm = cta_sum_parts(part_s, s, stride, nchunk_s);
-    const T mean = (T)(na > 0.0 ? sm / na : 0.0);
-#pragma unroll
-    for (int e = 0; e < FLAT / 256; e++) {
-      const long c = base + 256 * e;
-      if (c < n) {
-        T bv = b[o + c];
-        if (!(L.code[c] & 0x8000)) {
-          bv -= mean;
-          b[o + c] = bv;
-        }
-        v = fmat(a[o + c], bv, v);
-      }
-    }
-  } else {
-#pragma unroll
-    for (int e = 0; e < FLAT / 256; e++) {
-      const long c = base + 256 * e;
-      if (c < n) v = fmat(a[o + c], b[o + c], v);
-    }
-  }
-  const double t = block_sum1<T>(v);
-  if (threadIdx.x == 0) part[(long)s * stride + blockIdx.x] = t;
+// convergence of system s from its r.r (k_cg_norms without set_bb; thread 0 only): the system leaves the
+// running loop when its relative residual reaches its tolerance or its right-hand side is zero
+__device__ __forceinline__ bool cg_converged(SysScal &q, double rr, double tol) {
+  q.rr = rr;
+  const double bb = q.bb;
+  const double rel = bb > 0.0 ? sqrt(rr / bb) : 0.0;
+  q.rel = rel;
+  const double ts = q.tol > 0.0 ? q.tol : tol;
+  if (bb == 0.0) { q.zero_rhs = 1; return true; }
+  return rel <= ts;
 }
 
-// rz = sum of the r.z partials; beta = rz / rz_old (0 on the first iteration); one CTA per system
-__global__ void k_cg_beta(const int *active, SysScal *sc, const double *part, int stride, int n) {
+// The start of a Krylov iteration after the V-cycle z = M r, one CTA per system:
+//  * part_rr given: the convergence test of the previous iteration's update, deferred to here (the loop then
+//    needs no launch of its own for it); a system that has converged leaves the loop now, and the z the
+//    V-cycle just made for it is not used;
+//  * a singular system: z -= mean(z) over its active cells (the search directions then carry no constant),
+//    and r.z is taken over the projected z in a fixed order; any other system: r.z from the partials of the
+//    V-cycle's last pass or of k_cg_dot;
+//  * beta = r.z / r.z_old (0 on the first iteration).
+template <typename T>
+__global__ void __launch_bounds__(512) k_cg_beta2(MgLevelD L, int *active, const int *singular, SysScal *sc, T *z,
+                                                  const T *r, const double *part_rz, int nrz, const double *part_rr,
+                                                  int nrr, double tol, int stride) {
   const int s = blockIdx.x;
-  if (active && !active[s]) return;
-  const double rz = cta_sum_parts(part, s, stride, n);
+  if (!active[s]) return;
+  __shared__ int stop;
+  __shared__ double mean_s;
+  if (part_rr) {
+    const double rr = cta_sum_parts(part_rr, s, stride, nrr);
+    if (threadIdx.x == 0) {
+      stop = cg_converged(sc[s], rr, tol) ? 1 : 0;
+      if (stop) active[s] = 0;
+    }
+    __syncthreads();
+    if (stop) return;
+  }
+  double rz;
+  if (singular[s]) {
+    const long n = L.ncell, o = n * (long)s;
+    double v = 0.0, m = 0.0;
+    for (long c = threadIdx.x; c < n; c += blockDim.x)
+      if (!(L.code[c] & 0x8000)) { v += (double)z[o + c]; m += 1.0; }
+    double tv, tm;
+    block_sum2<double>(v, m, tv, tm);
+    if (threadIdx.x == 0) mean_s = tm > 0.0 ? tv / tm : 0.0;
+    __syncthreads();
+    const T mean = (T)mean_s;
+    T acc = 0;
+    for (long c = threadIdx.x; c < n; c += blockDim.x) {
+      T zv = z[o + c];
+      if (!(L.code[c] & 0x8000)) {
+        zv -= mean;
+        z[o + c] = zv;
+      }
+      acc = fmat(r[o + c], zv, acc);
+    }
+    rz = block_sum1<T>(acc);
+  } else {
+    rz = cta_sum_parts(part_rz, s, stride, nrz);
+  }
   if (threadIdx.x == 0) {
     sc[s].beta = sc[s].first ? 0.0 : rz / sc[s].rz;
     sc[s].rz = rz;
@@ -554,9 +571,9 @@ __global__ void k_set_active(int nsys, int *active, const int *src) {
   template __global__ void k_cg_resid<T>(MgLevelD, MgGeom, const T *, const int *, const T *, const T *, T *,        \
                                          double *, double *, int);                                                   \
   template __global__ void k_cg_dot<T>(long, const int *, const T *, const T *, double *, int);                      \
-  template __global__ void k_cg_dot_proj<T>(MgLevelD, const int *, const int *, const T *, T *, double *, int,      \
-                                            const double *, const double *, int);                                    \
   template __global__ void k_cg_p<T>(long, const int *, const SysScal *, const T *, T *);                            \
+  template __global__ void k_cg_beta2<T>(MgLevelD, int *, const int *, SysScal *, T *, const T *, const double *,     \
+                                         int, const double *, int, double, int);                                     \
   template __global__ void k_cg_apply<T, true>(MgLevelD, MgGeom, const T *, const int *, const SysScal *, const T *, \
                                                const T *, T *, T *, double *, int);                                  \
   template __global__ void k_cg_apply<T, false>(MgLevelD, MgGeom, const T *, const int *, const SysScal *,          \
@@ -656,27 +673,20 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
     MgProblem Pz = P;
     if constexpr (sizeof(T) == 8) { Pz.L[0].b = (double *)r; Pz.L[0].x = (double *)z; }
     else { Pz.L[0].bf = (float *)r; Pz.L[0].xf = (float *)z; }
-    // with singular systems r.z is taken after the projection below, by one flat pass over all systems
-    // (cheaper on GB300 than the V-cycle's per-system block reductions of it)
     int nrz = 0;
-    SNAC_TRY(mg_vcycle_impl<T>(Pz, G, 0, shift, W.active, P.any_singular ? nullptr : W.part2, W.stride, &nrz, st));
+    SNAC_TRY(mg_vcycle_impl<T>(Pz, G, 0, shift, W.active, W.part2, W.stride, &nrz, st));
     trace("pcg: V-cycle", st);
-    if (P.any_singular) {
-      // singular systems: z is taken orthogonal to the constant (the null space), so the search
-      // directions carry no constant and x - x0 stays mean-free.  r.z must use the projected z: r's
-      // mean is zero only up to rounding, and the V-cycle's constant drift can be large.
-      // (the subtraction itself is folded into the dot pass that follows)
-      const dim3 gs(gf.x, (unsigned)P.nsing);
-      k_sum_active<T><<<gs, 256, 0, st>>>(L0, P.sing_list, z, W.part0, W.part1, W.stride), ::snac::count_launch();
-      k_cg_dot_proj<T><<<gf, 256, 0, st>>>(L0, W.active, P.singular, r, z, W.part2, W.stride, W.part0, W.part1, nflat),
-          ::snac::count_launch();
-      nrz = nflat;
-    }
     if (nrz == 0) {
       k_cg_dot<T><<<gf, 256, 0, st>>>(n, W.active, r, z, W.part2, W.stride), ::snac::count_launch();
       nrz = nflat;
     }
-    k_cg_beta<<<P.nsys, 256, 0, st>>>(W.active, W.sc, W.part2, W.stride, nrz), ::snac::count_launch();
+    // singular systems: z is taken orthogonal to the constant (the null space), so the search directions
+    // carry no constant and x - x0 stays mean-free; r.z must use the projected z (r's mean is zero only up
+    // to rounding, and the V-cycle's constant drift can be large).  Without a host check the previous
+    // iteration's convergence test is made here too.
+    const bool fold = !check_host && it > 1;
+    k_cg_beta2<T><<<P.nsys, 512, 0, st>>>(L0, W.active, P.singular, W.sc, z, r, W.part2, nrz,
+                                          fold ? W.part0 : nullptr, nflat, tol, W.stride), ::snac::count_launch();
     prof_begin(KID_CG_APPLY, st);
     if constexpr (fusep) {
       if (P.mode3d)
@@ -696,9 +706,11 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
     prof_end(KID_CG_APPLY, st);
     k_cg_alpha<<<P.nsys, 256, 0, st>>>(W.active, W.sc, W.part1, W.stride, nred), ::snac::count_launch();
     k_cg_xr<T><<<gf, 256, 0, st>>>(n, W.active, W.sc, p, q, x, r, W.part0, W.stride, (zero_x && it == 1) ? 1 : 0), ::snac::count_launch();
-    SNAC_CUDA(cudaMemsetAsync(W.d_count, 0, 2 * sizeof(int), st));
-    k_cg_norms<<<P.nsys, 256, 0, st>>>(W.active, nullptr, W.sc, W.part0, nullptr, W.stride, nflat, tol, 0, 0, 0,
-                                       W.d_count, nullptr, 0.0), ::snac::count_launch();
+    if (check_host) {  // the host reads the count before the next iteration
+      SNAC_CUDA(cudaMemsetAsync(W.d_count, 0, 2 * sizeof(int), st));
+      k_cg_norms<<<P.nsys, 256, 0, st>>>(W.active, nullptr, W.sc, W.part0, nullptr, W.stride, nflat, tol, 0, 0, 0,
+                                         W.d_count, nullptr, 0.0), ::snac::count_launch();
+    }
     SNAC_CUDA(cudaGetLastError());
     trace("pcg: iteration", st);
   }

@@ -290,8 +290,8 @@ struct CoarsePlan {
 };
 
 // the layout for levels l0.. : x, b and 1/d of every level (the dense coarsest level only x and b) in
-// shared memory, then the couplings of as many levels as still fit, the finest (most used) first; false
-// when even x, b and 1/d do not fit
+// shared memory, then the couplings of as many levels as still fit, the coarsest first; false when even
+// x, b and 1/d do not fit
 template <typename T>
 static bool coarse_plan(const MgProblem &P, int l0, CoarsePlan *plan, size_t *bytes) {
   const int last = P.nlev - 1;
@@ -315,10 +315,12 @@ static bool coarse_plan(const MgProblem &P, int l0, CoarsePlan *plan, size_t *by
     o += n;
   }
   if (o * sizeof(T) > MG_COARSE_SMEM_MAX) return false;
-  for (int l = l0; l < P.nlev; l++) {
-    if (l == last && dense) break;
+  // couplings of the coarsest levels first: their sweeps have about one cell per thread, so a global load
+  // there is an exposed L2 latency per phase, while the finest level's many cells per thread overlap theirs
+  for (int l = last; l >= l0; l--) {
+    if (l == last && dense) continue;
     const size_t need = 2 * (size_t)P.L[l].ncell;
-    if ((o + need) * sizeof(T) > MG_COARSE_SMEM_MAX) continue;
+    if ((o + need) * sizeof(T) > MG_COARSE_SMEM_MAX) break;
     pl.lev[l].oc = (int)o;
     o += need;
   }
@@ -351,12 +353,85 @@ __device__ __forceinline__ void cta_sweep_xy(int n0, int n1, int per0, int per1,
   __syncthreads();
 }
 
+// The same half-sweep for an even n0 with a fixed cell ownership: thread t owns the column pair (2p, 2p+1),
+// p = t % (n0/2), in the rows j = g, g + G, ... (g = t / (n0/2), G = COARSE_THREADS / (n0/2)), and in each of
+// them updates the one cell of the pair that has the sweep's colour.  The east/west offsets (wrapped on a
+// periodic axis, 0 with a zero coupling at a wall) are fixed per thread, so a cell costs its ten shared loads,
+// four FMAs and a store.  Same terms in the same order as cta_sweep_xy: a missing neighbour contributes a
+// zero coupling times the cell's own value.
+template <typename T>
+__device__ __forceinline__ void cta_sweep_pairs(int n0, int n1, int per0, int per1, T *x, const T *b, const T *id,
+                                                const T *c0, const T *c1, int color) {
+  const int np = n0 >> 1;
+  const int G = COARSE_THREADS / np;
+  const int t = (int)threadIdx.x;
+  if (t < G * np) {
+    const int g = t / np, p = t - g * np;
+    const int we0 = p > 0 ? -1 : (per0 ? n0 - 1 : 0);       // west of the even cell 2p
+    const int ee1 = p < np - 1 ? 1 : (per0 ? 1 - n0 : 0);   // east of the odd cell 2p + 1
+    const bool hw0 = p > 0 || per0;                          // the even cell has a west neighbour
+    const int wrap_n = per1 ? n0 - n0 * n1 : 0, wrap_s = per1 ? n0 * (n1 - 1) : 0;
+    // a missing east/north neighbour has a zero (folded) coupling c0[c] / c1[c]; a missing west/south one
+    // has none to read, so its coupling is taken as zero here
+    for (int j = g; j < n1; j += G) {
+      const int e = (color + j) & 1;
+      const int c = j * n0 + 2 * p + e;
+      const int oe = e ? ee1 : 1, ow = e ? -1 : we0;
+      const int on = j + 1 < n1 ? n0 : wrap_n, os = j > 0 ? -n0 : wrap_s;
+      const T iv = id[c];
+      if (iv != T(0)) {
+        const T cwv = (e || hw0) ? c0[c + ow] : T(0);
+        const T csv = (j > 0 || per1) ? c1[c + os] : T(0);
+        T acc = fmat(c0[c], x[c + oe], T(0));
+        acc = fmat(cwv, x[c + ow], acc);
+        acc = fmat(c1[c], x[c + on], acc);
+        acc = fmat(csv, x[c + os], acc);
+        x[c] = (b[c] - acc) * iv;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// one half-sweep of level (n0, n1): the pair-owned form where it applies, else the walker
+template <typename T>
+__device__ __forceinline__ void cta_sweep(int n0, int n1, int per0, int per1, T *x, const T *b, const T *id,
+                                          const T *c0, const T *c1, int color, int hdj, int hdi) {
+  if (!(n0 & 1) && n0 >= 4 && (n0 >> 1) <= COARSE_THREADS) cta_sweep_pairs<T>(n0, n1, per0, per1, x, b, id, c0, c1, color);
+  else cta_sweep_xy<T>(n0, n1, per0, per1, x, b, id, c0, c1, color, hdj, hdi);
+}
+
+// Coarsest level x = Dinv b by all threads: row r is split into KS contiguous column chunks summed by KS
+// threads (KS = COARSE_THREADS / n), then the chunk sums of each row are added in chunk order.  Every load of
+// the (global, L2-resident) inverse then waits behind a few others instead of n.
+template <typename T>
+__device__ __forceinline__ void cta_dense(int n, const T *__restrict__ M, const T *bv, T *xv, T *red) {
+  const int KS = COARSE_THREADS / n;
+  const int chunk = (n + KS - 1) / KS;
+  const int t = (int)threadIdx.x, k = t / n, r = t - k * n;
+  if (k < KS) {
+    const int ca = k * chunk, cb = min(n, ca + chunk);
+    T acc = 0;
+#pragma unroll 4
+    for (int c = ca; c < cb; c++) acc = fmat(M[(size_t)c * n + r], bv[c], acc);
+    red[k * n + r] = acc;
+  }
+  __syncthreads();
+  if (t < n) {
+    T v = red[t];
+    for (int q = 1; q < KS; q++) v += red[q * n + t];
+    xv[t] = v;
+  }
+  __syncthreads();
+}
+
 template <typename T>
 __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P, CoarsePlan plan, int l0,
                                                                      const T *__restrict__ shift,
                                                                      const int *__restrict__ active,
                                                                      T *__restrict__ xout, const T *__restrict__ bin) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T red[COARSE_THREADS];  // chunk sums of the dense coarsest solve
   const int s = blockIdx.x;
   if (active && !active[s]) return;
   const int last = P.nlev - 1;
@@ -414,7 +489,7 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P
     const T *__restrict__ cc = LA<T>::cc(L);
     const T *__restrict__ w01 = LA<T>::w01(L);
     with_c(l, [&](const T *c0, const T *c1) {
-      for (int it = 0; it < 2 * mg_nu(P, l); it++) cta_sweep_xy<T>(n0, n1, per0, per1, x, b, id, c0, c1, it & 1, E.hdj, E.hdi);
+      for (int it = 0; it < 2 * mg_nu(P, l); it++) cta_sweep<T>(n0, n1, per0, per1, x, b, id, c0, c1, it & 1, E.hdj, E.hdi);
       const int cn0 = C.n[0], cn1 = C.n[1];
       const int e0 = C.coarsened[0] ? 2 : 1, e1 = C.coarsened[1] ? 2 : 1;
       T *bc = B(l + 1), *xc = X(l + 1);
@@ -444,21 +519,15 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P
     const MgLevelD &L = P.L[last];
     const int n = (int)L.ncell;
     if (dense) {
-      const T *__restrict__ M = LA<T>::dinv(L) + (size_t)n * n * s;
-      for (int r = threadIdx.x; r < n; r += blockDim.x) {  // the inverse is stored by columns (as k_dense)
-        T acc = 0;
-#pragma unroll 8
-        for (int c = 0; c < n; c++) acc = fmat(M[(size_t)c * n + r], B(last)[c], acc);
-        X(last)[r] = acc;
-      }
-      __syncthreads();
+      // the inverse is stored by columns (as for k_dense)
+      cta_dense<T>(n, LA<T>::dinv(L) + (size_t)n * n * s, B(last), X(last), red);
     } else {
       const CoarseLev &E = plan.lev[last];
       with_c(last, [&](const T *c0, const T *c1) {
         for (int it = 0; it < 40; it++)
           for (int col = 0; col < 4; col++)
-            cta_sweep_xy<T>(L.n[0], L.n[1], per0, per1, X(last), B(last), ID(last), c0, c1,
-                            (col == 1 || col == 2) ? 1 : 0, E.hdj, E.hdi);
+            cta_sweep<T>(L.n[0], L.n[1], per0, per1, X(last), B(last), ID(last), c0, c1,
+                         (col == 1 || col == 2) ? 1 : 0, E.hdj, E.hdi);
       });
     }
   }
@@ -484,7 +553,7 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P
     __syncthreads();
     with_c(l, [&](const T *c0, const T *c1) {
       for (int it = 0; it < 2 * mg_nu(P, l); it++)
-        cta_sweep_xy<T>(n0, n1, per0, per1, x, B(l), id, c0, c1, 1 - (it & 1), E.hdj, E.hdi);
+        cta_sweep<T>(n0, n1, per0, per1, x, B(l), id, c0, c1, 1 - (it & 1), E.hdj, E.hdi);
     });
   }
   const int n = (int)P.L[l0].ncell;
@@ -635,7 +704,7 @@ static int allow_smem(const void *fn, size_t bytes) {
   std::lock_guard<std::mutex> lk(mu);
   for (auto &e : done)
     if (e.first == fn && e.second == dev) return SNAC_OK;
-  SNAC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MG_COARSE_SMEM_MAX));
+  SNAC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MG_SMEM_OPT_IN));
   done.push_back({fn, dev});
   return SNAC_OK;
 }
@@ -725,7 +794,7 @@ template <typename T>
 int launch_vcycle_coarse3d(const MgProblem &P, const MgGeom &G, int l0, const T *shift, const int *active, T *x,
                            const T *b, cudaStream_t st) {
   const size_t smem = coarse3d_smem_bytes<T>(P, l0);
-  if (smem > MG_COARSE_SMEM_MAX) { set_error("coarse levels exceed the shared-memory budget"); return SNAC_ERR_ARG; }
+  if (smem > MG_COARSE3D_SMEM_MAX) { set_error("coarse levels exceed the shared-memory budget"); return SNAC_ERR_ARG; }
   SNAC_TRY(allow_smem((const void *)k_vcycle_coarse3d<T>, smem));
   prof_begin(KID_COARSE, st);
   k_vcycle_coarse3d<T><<<P.nsys, COARSE_THREADS, smem, st>>>(P, G, l0, shift, active, x, b), ::snac::count_launch();

@@ -73,7 +73,11 @@ size_t coarse3d_smem_bytes(const MgProblem &P, int l0);
 template <typename T>
 int launch_vcycle_coarse3d(const MgProblem &P, const MgGeom &G, int l0, const T *shift, const int *active, T *x,
                            const T *b, cudaStream_t st);
-constexpr size_t MG_COARSE_SMEM_MAX = 226 * 1024;  // dynamic shared memory of the coarse V-cycle CTA (227 KB at most)
+// dynamic shared memory of the one-CTA coarse V-cycles (227 KB at most per CTA): the plane kernel keeps 8 KB
+// of static shared memory for its dense coarsest solve, the 3-D kernel a few bytes
+constexpr size_t MG_SMEM_OPT_IN = 226 * 1024;      // opt-in limit set on every kernel that needs more than 48 KB
+constexpr size_t MG_COARSE_SMEM_MAX = 218 * 1024;
+constexpr size_t MG_COARSE3D_SMEM_MAX = 226 * 1024;
 template <typename T>
 int launch_vcycle_coarse(const MgProblem &P, int l0, const T *shift, const int *active, T *x, const T *b,
                          cudaStream_t st);

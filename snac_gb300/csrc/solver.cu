@@ -628,7 +628,7 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
         size_t bytes;
         if (S.mode3d) bytes = prec ? coarse3d_smem_bytes<double>(P, l) : coarse3d_smem_bytes<float>(P, l);
         else bytes = prec ? coarse_smem_bytes<double>(P, l) : coarse_smem_bytes<float>(P, l);
-        if (bytes <= MG_COARSE_SMEM_MAX) { P.cta_level[prec] = l; break; }
+        if (bytes <= (S.mode3d ? MG_COARSE3D_SMEM_MAX : MG_COARSE_SMEM_MAX)) { P.cta_level[prec] = l; break; }
       }
     }
   }

@@ -85,6 +85,31 @@ def set_bc(ctype, ibound, lo, hi, idir, centered, rvalue, dr, p):
                                  float(rvalue), float(dr), _f(p)))
 
 
+def _cbc(a):
+    """C order of a Fortran cbc(0:1,3[,3]) character array given as nested lists indexed [c][d][s] or [d][s]."""
+    return "".join(np.asarray(a, dtype="U1").ravel()).encode()
+
+
+def bounduvw(cbc, lo, hi, bc, is_correc, is_bound, nb, myrank, dxc, dxf, dyc, dyf, dzc, dzf, u, v, w):
+    """bound.f90:8-66 (bounduvw) for one block: cbc[c][d][s], bc[c][d][s], is_bound[d][s], nb[d][s]."""
+    b = np.ascontiguousarray(bc, dtype=np.float64)
+    ib = np.ascontiguousarray(is_bound, dtype=np.int32)
+    nbr = np.ascontiguousarray(nb, dtype=np.int32)
+    check(capi.lib().snac_bounduvw(_cbc(cbc), iarr(lo), iarr(hi), dptr(b), int(is_correc),
+                                   ib.ctypes.data_as(capi.IP), nbr.ctypes.data_as(capi.IP), int(myrank),
+                                   dptr(dxc), dptr(dxf), dptr(dyc), dptr(dyf), dptr(dzc), dptr(dzf), _f(u), _f(v),
+                                   _f(w)))
+
+
+def boundp(cbc, lo, hi, bc, is_bound, nb, myrank, dxc, dyc, dzc, p):
+    """bound.f90:68-106 (boundp) for one block: cbc[d][s], bc[d][s], is_bound[d][s], nb[d][s]."""
+    b = np.ascontiguousarray(bc, dtype=np.float64)
+    ib = np.ascontiguousarray(is_bound, dtype=np.int32)
+    nbr = np.ascontiguousarray(nb, dtype=np.int32)
+    check(capi.lib().snac_boundp(_cbc(cbc), iarr(lo), iarr(hi), dptr(b), ib.ctypes.data_as(capi.IP),
+                                 nbr.ctypes.data_as(capi.IP), int(myrank), dptr(dxc), dptr(dyc), dptr(dzc), _f(p)))
+
+
 def fft(kind, idir, arr, q=0):
     """fft.f90:85-94 on an interior array arr(n1,n2,n3) along idir (1..3), in place."""
     n = arr.shape

@@ -166,6 +166,50 @@ def test_set_bc(snac_lib, oracle_mod, ctype, centered, idir, ib):
     np.testing.assert_array_equal(got, ref)
 
 
+# bounduvw / boundp with the reference's argument lists: walls on some faces (D and N, both centrings), periodic
+# self-neighbour directions exchanged on the device, and a face whose neighbour is another rank left alone
+BOUND_CASES = {
+    "walls_x_periodic_yz": dict(is_bound=[[1, 1], [0, 0], [0, 0]], nb=[[-1, -1], [0, 0], [0, 0]]),
+    "walls_y_periodic_x_rank_z": dict(is_bound=[[0, 0], [1, 1], [0, 0]], nb=[[0, 0], [-1, -1], [3, 5]]),
+    "box_walls": dict(is_bound=[[1, 1], [1, 1], [1, 1]], nb=[[-1, -1], [-1, -1], [-1, -1]]),
+}
+
+
+@pytest.mark.parametrize("case", sorted(BOUND_CASES))
+@pytest.mark.parametrize("is_correc", [0, 1])
+def test_bounduvw_boundp_block(snac_lib, oracle_mod, case, is_correc):
+    rng = np.random.default_rng(170 + is_correc)
+    cfg = BOUND_CASES[case]
+    dxc, dxf, dyc, dyf, dzc, dzf = metrics(rng)
+    kinds = "DN"
+    cbc = [[[kinds[(c + d + s_) % 2] for s_ in range(2)] for d in range(3)] for c in range(3)]
+    bc = rng.standard_normal((3, 3, 2))
+    is_bound = np.array(cfg["is_bound"], dtype=np.int32)
+    nb = np.array(cfg["nb"], dtype=np.int32)
+    u, v, w = field(rng), field(rng), field(rng)
+    ref = [a.copy(order="F") for a in (u, v, w)]
+    got = [a.copy(order="F") for a in (u, v, w)]
+    cb = hotpath._cbc(cbc)
+    IP = C.POINTER(C.c_int)
+    oracle_mod.lib().or_bounduvw_block(cb, I3(LO), I3(HI), P(np.ascontiguousarray(bc)), is_correc,
+                                       is_bound.ctypes.data_as(IP), nb.ctypes.data_as(IP), 0, P(dxc), P(dxf),
+                                       P(dyc), P(dyf), P(dzc), P(dzf), *(P(a) for a in ref))
+    hotpath.bounduvw(cbc, LO, HI, bc, is_correc, is_bound, nb, 0, dxc, dxf, dyc, dyf, dzc, dzf, *got)
+    for g, r in zip(got, ref):
+        np.testing.assert_array_equal(g, r)
+    # a face exchanged with another rank is untouched (the caller's MPI exchange)
+    if nb[2][0] > 0:
+        np.testing.assert_array_equal(got[0][1:-1, 1:-1, 0], u[1:-1, 1:-1, 0])
+    p = field(rng)
+    pref, pgot = p.copy(order="F"), p.copy(order="F")
+    cbp = [row[:] for row in cbc[0]]
+    bcp = np.ascontiguousarray(bc[0])
+    oracle_mod.lib().or_boundp_block(hotpath._cbc(cbp), I3(LO), I3(HI), P(bcp), is_bound.ctypes.data_as(IP),
+                                     nb.ctypes.data_as(IP), 0, P(dxc), P(dyc), P(dzc), P(pref))
+    hotpath.boundp(cbp, LO, HI, bcp, is_bound, nb, 0, dxc, dyc, dzc, pgot)
+    np.testing.assert_array_equal(pgot, pref)
+
+
 @pytest.mark.parametrize("kind", ["R2HC", "HC2R", "REDFT10", "REDFT01", "REDFT11", "RODFT10", "RODFT01", "RODFT11",
                                   "REDFT00", "RODFT00"])
 @pytest.mark.parametrize("idir,n", [(1, 8), (2, 12), (3, 16), (3, 128), (3, 2)])
