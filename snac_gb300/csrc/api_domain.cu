@@ -1107,7 +1107,8 @@ int snac_bench_smoother(int level, int reps, double *ms_per_launch, double *byte
   int rc = SNAC_OK;
   for (int q = 0; q < 2 + reps && rc == SNAC_OK; q++) {
     if (q == 2) cudaEventRecord(e0, d->st);
-    rc = launch_rbgs_tile2d<float>(P, level, nullptr, 0, 0, L.xpf, L.bf, nullptr, nullptr, nullptr, 0, nullptr, d->st);
+    rc = launch_rbgs_tile2d<float>(P, level, nullptr, 0, 0, L.xpf, L.bf, nullptr, nullptr, nullptr, nullptr, nullptr, 0,
+                                   nullptr, d->st);
   }
   cudaEventRecord(e1, d->st);
   float ms = 0.f;

@@ -147,10 +147,11 @@ __global__ void k_zero(long n, T *x, int nsys, const int *active) {
 }
 
 // V-cycle on level l: x_l <- M b_l (zero initial guess); x and b of each level are the level's own arrays.
-// At level 0 the last smoothing pass may also produce the partials of b.x (= r.z) into part_bx.
+// At level 0 the last smoothing pass may also produce the partials of b.x (= r.z) into part_bx, and for the
+// singular systems those of x and of b into part_x and part_b.
 template <typename T>
 int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, const int *active, double *part_bx,
-                   int part_stride, int *nchunk_bx, cudaStream_t st) {
+                   double *part_x, double *part_b, int part_stride, int *nchunk_bx, cudaStream_t st) {
   const MgLevelD &L = P.L[l];
   T *x = LA<T>::x(L);
   T *b = LA<T>::b(L);
@@ -178,12 +179,12 @@ int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, c
   const MgLevelD &C = P.L[l + 1];
   if ((fuse & 1) && tile2d_ok(P, l, prec)) {
     T *xp = LA<T>::xp(P.L[l]);  // pre-smoothed x (the post-smoother reads it while writing x)
-    SNAC_TRY(launch_rbgs_tile2d<T>(P, l, active, 0, 0, xp, b, (const T *)nullptr, (const T *)nullptr, nullptr, 0,
-                                   nullptr, st));
+    SNAC_TRY(launch_rbgs_tile2d<T>(P, l, active, 0, 0, xp, b, (const T *)nullptr, (const T *)nullptr, nullptr,
+                                   nullptr, nullptr, 0, nullptr, st));
     SNAC_TRY(plane_restrict<T>(P, l, shift, active, xp, b, LA<T>::b(C), LA<T>::x(C), st));
-    SNAC_TRY(mg_vcycle_impl<T>(P, G, l + 1, shift, active, nullptr, 0, nullptr, st));
-    return launch_rbgs_tile2d<T>(P, l, active, 1, 1, x, b, (const T *)xp, (const T *)LA<T>::x(C), part_bx,
-                                 part_stride, nchunk_bx, st);
+    SNAC_TRY(mg_vcycle_impl<T>(P, G, l + 1, shift, active, nullptr, nullptr, nullptr, 0, nullptr, st));
+    return launch_rbgs_tile2d<T>(P, l, active, 1, 1, x, b, (const T *)xp, (const T *)LA<T>::x(C), part_bx, part_x,
+                                 part_b, part_stride, nchunk_bx, st);
   }
   if (l == 0) {  // coarse x is zeroed by the restriction
     const dim3 g((unsigned)((L.ncell + 255) / 256), P.nsys);
@@ -192,7 +193,7 @@ int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, c
   if (!P.mode3d) {  // plane systems: kernels batched over systems
     for (int it = 0; it < 2 * mg_nu(P, l); it++) SNAC_TRY(plane_sweep<T>(P, l, shift, active, it & 1, x, b, st));
     SNAC_TRY(plane_restrict<T>(P, l, shift, active, x, b, LA<T>::b(C), LA<T>::x(C), st));
-    SNAC_TRY(mg_vcycle_impl<T>(P, G, l + 1, shift, active, nullptr, 0, nullptr, st));
+    SNAC_TRY(mg_vcycle_impl<T>(P, G, l + 1, shift, active, nullptr, nullptr, nullptr, 0, nullptr, st));
     SNAC_TRY(plane_prolong<T>(P, l, active, x, LA<T>::x(C), st));
     for (int it = 0; it < 2 * mg_nu(P, l); it++) SNAC_TRY(plane_sweep<T>(P, l, shift, active, 1 - (it & 1), x, b, st));
     return SNAC_OK;
@@ -206,7 +207,7 @@ int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, c
   k_resid_restrict<T><<<grid_cell(P, C), BLK, 0, st>>>(L, C, G, shift, active, x, b, LA<T>::b(C), LA<T>::x(C)), ::snac::count_launch();
   prof_end(KID_RESTRICT, st);
   SNAC_CUDA(cudaGetLastError());
-  SNAC_TRY(mg_vcycle_impl<T>(P, G, l + 1, shift, active, nullptr, 0, nullptr, st));
+  SNAC_TRY(mg_vcycle_impl<T>(P, G, l + 1, shift, active, nullptr, nullptr, nullptr, 0, nullptr, st));
   k_prolong<T><<<grid_cell(P, L), BLK, 0, st>>>(L, C, G, active, x, LA<T>::x(C)), ::snac::count_launch();
   for (int it = 0; it < 2 * mg_nu(P, l); it++) {
     prof_begin(KID_RBGS, st);
@@ -253,10 +254,12 @@ __global__ void __launch_bounds__(256) k_cg_resid(MgLevelD L, MgGeom G, const T 
   }
 }
 
-// partial dot a.b (flat)
+// partial dot a.b (flat); for the singular systems (singular given) also the partial sums of b and of a over
+// the active cells, into part_b and part_a
 template <typename T>
 __global__ void __launch_bounds__(256) k_cg_dot(long n, const int *active, const T *a, const T *b, double *part,
-                                                int stride) {
+                                                int stride, const unsigned short *code, const int *singular,
+                                                double *part_a, double *part_b) {
   const int s = blockIdx.y;
   if (active && !active[s]) return;
   const long base = (long)blockIdx.x * FLAT + threadIdx.x, o = n * s;
@@ -268,6 +271,16 @@ __global__ void __launch_bounds__(256) k_cg_dot(long n, const int *active, const
   }
   const double t = block_sum1<T>(v);
   if (threadIdx.x == 0) part[(long)s * stride + blockIdx.x] = t;
+  if (singular && singular[s]) {
+    T sa = 0, sb = 0;
+    for (int e = 0; e < FLAT / 256; e++) {
+      const long c = base + 256 * e;
+      if (c < n && !(code[c] & 0x8000)) { sa += a[o + c]; sb += b[o + c]; }
+    }
+    double ta, tb;
+    block_sum2<T>(sa, sb, ta, tb);
+    if (threadIdx.x == 0) { part_a[(long)s * stride + blockIdx.x] = ta; part_b[(long)s * stride + blockIdx.x] = tb; }
+  }
 }
 
 // fixed-order sum of the n partials of system s by one CTA (result valid in every thread)
@@ -297,18 +310,17 @@ __device__ __forceinline__ bool cg_converged(SysScal &q, double rr, double tol) 
 //  * part_rr given: the convergence test of the previous iteration's update, deferred to here (the loop then
 //    needs no launch of its own for it); a system that has converged leaves the loop now, and the z the
 //    V-cycle just made for it is not used;
-//  * a singular system: z -= mean(z) over its active cells (the search directions then carry no constant),
-//    and r.z is taken over the projected z in a fixed order; any other system: r.z from the partials of the
-//    V-cycle's last pass or of k_cg_dot;
+//  * r.z from the partials of the V-cycle's last pass or of k_cg_dot; for a singular system z is taken
+//    orthogonal to the constant (its null space): zmean = sum(z)/nact over the active cells, which the new
+//    search direction leaves out (p = z - zmean + beta p), and r.z becomes r.(z - zmean) = r.z - zmean sum(r),
+//    from the partial sums of z and r made by the same pass;
 //  * beta = r.z / r.z_old (0 on the first iteration).
-template <typename T>
-__global__ void __launch_bounds__(512) k_cg_beta2(MgLevelD L, int *active, const int *singular, SysScal *sc, T *z,
-                                                  const T *r, const double *part_rz, int nrz, const double *part_rr,
-                                                  int nrr, double tol, int stride) {
+__global__ void k_cg_beta2(int *active, const int *singular, SysScal *sc, const double *part_rz, const double *part_z,
+                           const double *part_r, int nrz, const double *part_rr, int nrr, double tol, long nact,
+                           int stride) {
   const int s = blockIdx.x;
   if (!active[s]) return;
   __shared__ int stop;
-  __shared__ double mean_s;
   if (part_rr) {
     const double rr = cta_sum_parts(part_rr, s, stride, nrr);
     if (threadIdx.x == 0) {
@@ -318,31 +330,16 @@ __global__ void __launch_bounds__(512) k_cg_beta2(MgLevelD L, int *active, const
     __syncthreads();
     if (stop) return;
   }
-  double rz;
+  double rz = cta_sum_parts(part_rz, s, stride, nrz);
+  double zmean = 0.0;
   if (singular[s]) {
-    const long n = L.ncell, o = n * (long)s;
-    double v = 0.0, m = 0.0;
-    for (long c = threadIdx.x; c < n; c += blockDim.x)
-      if (!(L.code[c] & 0x8000)) { v += (double)z[o + c]; m += 1.0; }
-    double tv, tm;
-    block_sum2<double>(v, m, tv, tm);
-    if (threadIdx.x == 0) mean_s = tm > 0.0 ? tv / tm : 0.0;
-    __syncthreads();
-    const T mean = (T)mean_s;
-    T acc = 0;
-    for (long c = threadIdx.x; c < n; c += blockDim.x) {
-      T zv = z[o + c];
-      if (!(L.code[c] & 0x8000)) {
-        zv -= mean;
-        z[o + c] = zv;
-      }
-      acc = fmat(r[o + c], zv, acc);
-    }
-    rz = block_sum1<T>(acc);
-  } else {
-    rz = cta_sum_parts(part_rz, s, stride, nrz);
+    const double sz = cta_sum_parts(part_z, s, stride, nrz);
+    const double sr = cta_sum_parts(part_r, s, stride, nrz);
+    zmean = nact > 0 ? sz / (double)nact : 0.0;
+    rz -= zmean * sr;
   }
   if (threadIdx.x == 0) {
+    sc[s].zmean = zmean;
     sc[s].beta = sc[s].first ? 0.0 : rz / sc[s].rz;
     sc[s].rz = rz;
     sc[s].first = 0;
@@ -357,22 +354,22 @@ __global__ void k_cg_alpha(const int *active, SysScal *sc, const double *part, i
   if (threadIdx.x == 0) sc[s].alpha = sc[s].rz / pq;
 }
 
-// p = z + beta p (flat; FP64 path)
+// p = (z - zmean) + beta p (flat; FP64 path)
 template <typename T>
 __global__ void __launch_bounds__(256) k_cg_p(long n, const int *active, const SysScal *sc, const T *z, T *p) {
   const int s = blockIdx.y;
   if (active && !active[s]) return;
-  const T beta = (T)sc[s].beta;
+  const T beta = (T)sc[s].beta, zm = (T)sc[s].zmean;
   const long base = (long)blockIdx.x * FLAT + threadIdx.x, o = n * s;
 #pragma unroll
   for (int e = 0; e < FLAT / 256; e++) {
     const long c = base + 256 * e;
-    if (c < n) p[o + c] = fmat(beta, p[o + c], z[o + c]);
+    if (c < n) p[o + c] = fmat(beta, p[o + c], z[o + c] - zm);
   }
 }
 
-// q = A p; partials of p.q.  FUSEP: the new direction p = z + beta p_old is formed on the fly (at the
-// centre and at the neighbours) and written to pn, so p_old and pn must be different arrays.
+// q = A p; partials of p.q.  FUSEP: the new direction p = (z - zmean) + beta p_old is formed on the fly (at
+// the centre and at the neighbours) and written to pn, so p_old and pn must be different arrays.
 template <typename T, bool FUSEP>
 __global__ void __launch_bounds__(256) k_cg_apply(MgLevelD L, MgGeom G, const T *shift, const int *active,
                                                   const SysScal *sc, const T *z, const T *po, T *pn, T *q,
@@ -383,9 +380,9 @@ __global__ void __launch_bounds__(256) k_cg_apply(MgLevelD L, MgGeom G, const T 
   const long off = L.ncell * s;
   const T *__restrict__ zs = z + off;
   const T *__restrict__ ps = po + off;
-  const T beta = FUSEP ? (T)sc[s].beta : T(0);
+  const T beta = FUSEP ? (T)sc[s].beta : T(0), zm = FUSEP ? (T)sc[s].zmean : T(0);
   const T sh = shift[s];
-  auto pv = [&](int e) -> T { return FUSEP ? fmat(beta, ps[e], zs[e]) : ps[e]; };
+  auto pv = [&](int e) -> T { return FUSEP ? fmat(beta, ps[e], zs[e] - zm) : ps[e]; };
   const int i = blockIdx.x * 32 + threadIdx.x;
   T pq = 0;
   for (int qq = 0; qq < RROWS; qq++) {
@@ -570,10 +567,9 @@ __global__ void k_set_active(int nsys, int *active, const int *src) {
   template __global__ void k_zero<T>(long, T *, int, const int *);                                                   \
   template __global__ void k_cg_resid<T>(MgLevelD, MgGeom, const T *, const int *, const T *, const T *, T *,        \
                                          double *, double *, int);                                                   \
-  template __global__ void k_cg_dot<T>(long, const int *, const T *, const T *, double *, int);                      \
+  template __global__ void k_cg_dot<T>(long, const int *, const T *, const T *, double *, int,                      \
+                                       const unsigned short *, const int *, double *, double *);                     \
   template __global__ void k_cg_p<T>(long, const int *, const SysScal *, const T *, T *);                            \
-  template __global__ void k_cg_beta2<T>(MgLevelD, int *, const int *, SysScal *, T *, const T *, const double *,     \
-                                         int, const double *, int, double, int);                                     \
   template __global__ void k_cg_apply<T, true>(MgLevelD, MgGeom, const T *, const int *, const SysScal *, const T *, \
                                                const T *, T *, T *, double *, int);                                  \
   template __global__ void k_cg_apply<T, false>(MgLevelD, MgGeom, const T *, const int *, const SysScal *,          \
@@ -602,7 +598,7 @@ template <> const float *shift_of<float>(const MgProblem &P) { return P.shiftf; 
 
 template <typename T>
 int mg_vcycle(const MgProblem &P, int l, const int *active, cudaStream_t st) {
-  return mg_vcycle_impl<T>(P, geom_of(P), l, shift_of<T>(P), active, nullptr, 0, nullptr, st);
+  return mg_vcycle_impl<T>(P, geom_of(P), l, shift_of<T>(P), active, nullptr, nullptr, nullptr, 0, nullptr, st);
 }
 template int mg_vcycle<double>(const MgProblem &, int, const int *, cudaStream_t);
 template int mg_vcycle<float>(const MgProblem &, int, const int *, cudaStream_t);
@@ -674,19 +670,20 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
     if constexpr (sizeof(T) == 8) { Pz.L[0].b = (double *)r; Pz.L[0].x = (double *)z; }
     else { Pz.L[0].bf = (float *)r; Pz.L[0].xf = (float *)z; }
     int nrz = 0;
-    SNAC_TRY(mg_vcycle_impl<T>(Pz, G, 0, shift, W.active, W.part2, W.stride, &nrz, st));
+    SNAC_TRY(mg_vcycle_impl<T>(Pz, G, 0, shift, W.active, W.part2, W.part3, W.part4, W.stride, &nrz, st));
     trace("pcg: V-cycle", st);
     if (nrz == 0) {
-      k_cg_dot<T><<<gf, 256, 0, st>>>(n, W.active, r, z, W.part2, W.stride), ::snac::count_launch();
+      k_cg_dot<T><<<gf, 256, 0, st>>>(n, W.active, r, z, W.part2, W.stride, L0.code,
+                                      P.any_singular ? P.singular : nullptr, W.part4, W.part3), ::snac::count_launch();
       nrz = nflat;
     }
-    // singular systems: z is taken orthogonal to the constant (the null space), so the search directions
-    // carry no constant and x - x0 stays mean-free; r.z must use the projected z (r's mean is zero only up
-    // to rounding, and the V-cycle's constant drift can be large).  Without a host check the previous
-    // iteration's convergence test is made here too.
+    // singular systems: the search directions carry no constant (z's mean is left out of p), so x - x0 stays
+    // mean-free, and r.z is taken with the projected z (r's mean is zero only up to rounding, and the V-cycle's
+    // constant drift can be large).  Without a host check the previous iteration's convergence test is made
+    // here too.
     const bool fold = !check_host && it > 1;
-    k_cg_beta2<T><<<P.nsys, 512, 0, st>>>(L0, W.active, P.singular, W.sc, z, r, W.part2, nrz,
-                                          fold ? W.part0 : nullptr, nflat, tol, W.stride), ::snac::count_launch();
+    k_cg_beta2<<<P.nsys, 256, 0, st>>>(W.active, P.singular, W.sc, W.part2, W.part3, W.part4, nrz,
+                                       fold ? W.part0 : nullptr, nflat, tol, P.nact0, W.stride), ::snac::count_launch();
     prof_begin(KID_CG_APPLY, st);
     if constexpr (fusep) {
       if (P.mode3d)

@@ -100,7 +100,8 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
                                                          int first_color, int nhalf, T *__restrict__ x,
                                                          const T *__restrict__ b, const T *__restrict__ xin,
                                                          const T *__restrict__ xc, double *__restrict__ part_bx,
-                                                         int part_stride) {
+                                                         const int *__restrict__ singular, double *__restrict__ part_x,
+                                                         double *__restrict__ part_b, int part_stride) {
   static_assert(NW % 2 == 0, "rows w + NW q of a thread must share their colour parity");
   constexpr int SH = NW * R, BY = SH - 2 * TH;
   constexpr int NA = MODE == 1 ? 4 : 2;
@@ -254,7 +255,7 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
     }
     // every thread stores only cells it updated itself: no barrier needed here
     const long off = L.ncell * (long)cur;
-    T bx = 0;
+    T bx = 0, sx = 0, sb = 0;
 #pragma unroll
     for (int q = 0; q < R; q++) {
 #pragma unroll
@@ -263,11 +264,21 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
         const T v = (p ? xo : xe)[tpos + NW * q * TRS];
         x[off + cidx[q] + p] = v;
         bx = fmat(bv[q][p], v, bx);
+        sx += v;
+        sb += bv[q][p];
       }
     }
     if (part_bx) {
       const double t = block_sum1<T>(bx);
       if (threadIdx.x == 0) part_bx[(long)cur * part_stride + blockIdx.x] = t;
+      if (singular && singular[cur]) {  // uniform over the CTA
+        double tx, tb;
+        block_sum2<T>(sx, sb, tx, tb);
+        if (threadIdx.x == 0) {
+          part_x[(long)cur * part_stride + blockIdx.x] = tx;
+          part_b[(long)cur * part_stride + blockIdx.x] = tb;
+        }
+      }
     }
     cur = nxt;
     k ^= 1;
@@ -704,7 +715,17 @@ static int allow_smem(const void *fn, size_t bytes) {
   std::lock_guard<std::mutex> lk(mu);
   for (auto &e : done)
     if (e.first == fn && e.second == dev) return SNAC_OK;
-  SNAC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MG_SMEM_OPT_IN));
+  // the opt-in limit less the kernel's own static shared memory (the coarse kernels keep some)
+  int optin = 0;
+  SNAC_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  SNAC_CUDA(cudaFuncGetAttributes(&fa, fn));
+  const size_t room = (size_t)optin > fa.sharedSizeBytes ? (size_t)optin - fa.sharedSizeBytes : 0;
+  if (bytes > room) {
+    set_error("kernel needs %zu bytes of dynamic shared memory, %zu available", bytes, room);
+    return SNAC_ERR_ARG;
+  }
+  SNAC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min(room, MG_SMEM_OPT_IN)));
   done.push_back({fn, dev});
   return SNAC_OK;
 }
@@ -712,18 +733,21 @@ static int allow_smem(const void *fn, size_t bytes) {
 template <typename T, int NW, int R>
 static int launch_tile(const MgProblem &P, const MgLevelD &L, const MgLevelD &C, int nt, int nhalf, const int *active,
                        int first_color, int mode, T *x, const T *b, const T *xin, const T *xc, double *part_bx,
-                       int part_stride, cudaStream_t st) {
+                       double *part_x, double *part_b, int part_stride, cudaStream_t st) {
+  const int *sing = P.any_singular && part_bx ? P.singular : nullptr;
   const size_t smem = tile_smem_bytes<T>(NW * R, mode);
   const int sb = plane_batch(P, nt, NW == 16 ? 2 : 4);
   const dim3 g((unsigned)nt, (unsigned)((P.nsys + sb - 1) / sb));
   if (mode == 1) {
     SNAC_TRY(allow_smem((const void *)k_rbgs_tile2d<T, NW, R, 1>, smem));
     k_rbgs_tile2d<T, NW, R, 1><<<g, NW * 32, smem, st>>>(L, C, P.periodic[0], P.periodic[1], active, P.nsys, sb,
-                                                         first_color, nhalf, x, b, xin, xc, part_bx, part_stride), ::snac::count_launch();
+                                                         first_color, nhalf, x, b, xin, xc, part_bx, sing, part_x, part_b,
+                                                         part_stride), ::snac::count_launch();
   } else {
     SNAC_TRY(allow_smem((const void *)k_rbgs_tile2d<T, NW, R, 0>, smem));
     k_rbgs_tile2d<T, NW, R, 0><<<g, NW * 32, smem, st>>>(L, C, P.periodic[0], P.periodic[1], active, P.nsys, sb,
-                                                         first_color, nhalf, x, b, xin, xc, part_bx, part_stride), ::snac::count_launch();
+                                                         first_color, nhalf, x, b, xin, xc, part_bx, sing, part_x, part_b,
+                                                         part_stride), ::snac::count_launch();
   }
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -731,7 +755,8 @@ static int launch_tile(const MgProblem &P, const MgLevelD &L, const MgLevelD &C,
 
 template <typename T>
 int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_color, int mode, T *x, const T *b,
-                       const T *xin, const T *xc, double *part_bx, int part_stride, int *nchunk, cudaStream_t st) {
+                       const T *xin, const T *xc, double *part_bx, double *part_x, double *part_b, int part_stride,
+                       int *nchunk, cudaStream_t st) {
   if (mode == 1 && (xin == x || !xin || !xc)) { set_error("tiled post-smoother needs separate input and output"); return SNAC_ERR_ARG; }
   const MgLevelD &L = P.L[l];
   const MgLevelD &C = l + 1 < P.nlev ? P.L[l + 1] : P.L[l];
@@ -741,16 +766,16 @@ int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_c
   prof_begin(KID_RBGS, st);
   int rc;
   if constexpr (sizeof(T) == 8) {
-    rc = launch_tile<T, 8, 2>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
+    rc = launch_tile<T, 8, 2>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_x, part_b, part_stride, st);
   } else {
     if (t.nw == 8 && t.r == 2)
-      rc = launch_tile<T, 8, 2>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
+      rc = launch_tile<T, 8, 2>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_x, part_b, part_stride, st);
     else if (t.nw == 16 && t.r == 2)
-      rc = launch_tile<T, 16, 2>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
+      rc = launch_tile<T, 16, 2>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_x, part_b, part_stride, st);
     else if (t.nw == 8)
-      rc = launch_tile<T, 8, 3>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
+      rc = launch_tile<T, 8, 3>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_x, part_b, part_stride, st);
     else
-      rc = launch_tile<T, 16, 3>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_stride, st);
+      rc = launch_tile<T, 16, 3>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_x, part_b, part_stride, st);
   }
   prof_end(KID_RBGS, st);
   SNAC_TRY(rc);
@@ -811,9 +836,11 @@ template int launch_vcycle_coarse3d<float>(const MgProblem &, const MgGeom &, in
                                            const float *, cudaStream_t);
 
 template int launch_rbgs_tile2d<double>(const MgProblem &, int, const int *, int, int, double *, const double *,
-                                        const double *, const double *, double *, int, int *, cudaStream_t);
+                                        const double *, const double *, double *, double *, double *, int, int *,
+                                        cudaStream_t);
 template int launch_rbgs_tile2d<float>(const MgProblem &, int, const int *, int, int, float *, const float *,
-                                       const float *, const float *, double *, int, int *, cudaStream_t);
+                                       const float *, const float *, double *, double *, double *, int, int *,
+                                       cudaStream_t);
 template size_t coarse_smem_bytes<double>(const MgProblem &, int);
 template size_t coarse_smem_bytes<float>(const MgProblem &, int);
 template int launch_vcycle_coarse<double>(const MgProblem &, int, const double *, const int *, double *,

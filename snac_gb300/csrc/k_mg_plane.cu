@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(256, (RR >= 4 ? 3 : 1)) k_p_resid(MgLevelD L, 
   }
 }
 
-// q = A p; partials of p.q.  FUSEP: p = z + beta p_old is formed on the fly and written to pn.
+// q = A p; partials of p.q.  FUSEP: p = (z - zmean) + beta p_old is formed on the fly and written to pn.
 template <typename T, bool FUSEP>
 __global__ void __launch_bounds__(256) k_p_apply(MgLevelD L, int per0, int per1, const T *__restrict__ shift,
                                                  const int *__restrict__ active, int nsys, int sb,
@@ -228,9 +228,9 @@ __global__ void __launch_bounds__(256) k_p_apply(MgLevelD L, int per0, int per1,
     const long off = L.ncell * (long)s;
     const T *__restrict__ zs = z + off;
     const T *__restrict__ ps = po + off;
-    const T beta = FUSEP ? (T)sc[s].beta : T(0);
+    const T beta = FUSEP ? (T)sc[s].beta : T(0), zm = FUSEP ? (T)sc[s].zmean : T(0);
     const T sh = shift[s];
-    auto pv = [&](int e) -> T { return FUSEP ? fmat(beta, ps[e], zs[e]) : ps[e]; };
+    auto pv = [&](int e) -> T { return FUSEP ? fmat(beta, ps[e], zs[e] - zm) : ps[e]; };
     T pq = 0;
 #pragma unroll
     for (int qq = 0; qq < RROWS; qq++) {

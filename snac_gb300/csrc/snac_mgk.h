@@ -15,6 +15,7 @@ struct SysScal {
   int first, zero_rhs;
   int restart;  // the warm start was worse than zero (rel > 1): the solve restarts from x = 0
   double tol;   // this system's own relative tolerance in the running loop (0: the loop's)
+  double zmean; // singular system: mean of the preconditioned residual z over its active cells (taken out of p)
 };
 
 // Partial sums: one row of `stride` doubles per system; a producer kernel writes one entry per CTA
@@ -22,6 +23,7 @@ struct SysScal {
 struct CgWork {
   void *r, *z, *p, *p2, *q;  // level-0 vectors (type of the running Krylov loop); p/p2 alternate
   double *part0, *part1, *part2;
+  double *part3, *part4;     // singular systems: partial sums of z and of r over the active cells
   int stride;                // partial entries per system (capacity)
   SysScal *sc;               // nsys
   int *active;               // nsys flags of the running loop

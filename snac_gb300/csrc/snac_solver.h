@@ -53,6 +53,7 @@ struct MgProblem {
   int any_singular;                  // some system is singular (pure Neumann, zero shift)
   const int *sing_list;              // device: indices of the singular systems (nsing of them)
   int nsing;
+  long nact0;                        // active cells of one system on level 0
 };
 // smoothing sweeps per side of the V-cycle on level l
 __host__ __device__ inline int mg_nu(const MgProblem &P, int l) { return l >= P.lnu ? P.nu_coarse : P.nu; }
@@ -62,9 +63,12 @@ struct MgGeom;
 // fused kernels (k_mg_fused.cu)
 bool tile2d_ok(const MgProblem &P, int l, int prec);
 int tile2d_max_tiles(const MgLevelD &L);
+// part_bx: partials of b.x of the stored cells (post-smoother, mode 1); for the singular systems also those
+// of x and of b in part_x and part_b
 template <typename T>
 int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_color, int mode, T *x, const T *b,
-                       const T *xin, const T *xc, double *part_bx, int part_stride, int *nchunk, cudaStream_t st);
+                       const T *xin, const T *xc, double *part_bx, double *part_x, double *part_b, int part_stride,
+                       int *nchunk, cudaStream_t st);
 template <typename T>
 size_t coarse_smem_bytes(const MgProblem &P, int l0);
 struct MgGeom;

@@ -637,6 +637,7 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
   P.singular = (const int *)up(singular.data(), singular.size() * sizeof(int));
   P.any_singular = 0;
   for (int v : singular) P.any_singular |= v;
+  P.nact0 = nact;
   {
     std::vector<int> list;
     for (int q = 0; q < S.nsys; q++)
@@ -682,12 +683,13 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
     W->p2 = W == &S.W32 ? S.alloc(nv0 * es) : nullptr;
     W->q = S.alloc(nv0 * es);
     W->stride = stride;
-    for (double **pp : {&W->part0, &W->part1, &W->part2}) *pp = (double *)S.alloc((size_t)stride * S.nsys * sizeof(double));
+    for (double **pp : {&W->part0, &W->part1, &W->part2, &W->part3, &W->part4})
+      *pp = (double *)S.alloc((size_t)stride * S.nsys * sizeof(double));
     W->sc = (SysScal *)S.alloc(S.nsys * sizeof(SysScal));
     W->active = (int *)S.alloc(S.nsys * sizeof(int));
     W->d_count = (int *)S.alloc(2 * sizeof(int));
     SNAC_CUDA(cudaMallocHost(&W->h_count, 2 * sizeof(int)));
-    if (!W->r || !W->z || !W->p || !W->q || (W == &S.W32 && !W->p2) || !W->part0 || !W->part1 || !W->part2 || !W->sc ||
+    if (!W->r || !W->z || !W->p || !W->q || (W == &S.W32 && !W->p2) || !W->part0 || !W->part1 || !W->part2 || !W->part3 || !W->part4 || !W->sc ||
         !W->active || !W->d_count) {
       set_error("device allocation failed for Krylov vectors");
       return SNAC_ERR_NOMEM;
