@@ -51,7 +51,7 @@ const dim3 BLK(32, 8);
 int mg_partial_stride(const MgProblem &P) {
   const MgLevelD &L = P.L[0];
   int m = std::max(nchunk_red(P, L), (int)((L.ncell + FLAT - 1) / FLAT));
-  if (!P.mode3d) m = std::max(m, tile2d_max_tiles(L));
+  if (!P.mode3d) m = std::max(m, tile2d_max_parts(L));
   return m;
 }
 

@@ -11,7 +11,7 @@
 //   can differ from a global sweep, so the output cells are exact after TH.
 //   The pre-smoother starts from x = 0 without reading x; the post-smoother adds
 //   the coarse-grid correction while loading (prolongation fused) and can emit
-//   the partials of b.x (r.z of the Krylov iteration).  Tiles overlap, so a
+//   the partials of b.x (r.z of the Krylov iteration), one per warp.  Tiles overlap, so a
 //   launch never reads the array it writes: the pre-smoother writes xp and the
 //   post-smoother reads xp + correction and writes x.
 // k_vcycle_coarse: one CTA of 1024 threads per system runs the V-cycle from
@@ -66,7 +66,13 @@ __device__ __forceinline__ int wrap(int g, int n) {
 }
 }  // namespace
 
-int tile2d_max_tiles(const MgLevelD &L) { return tiles_for(L, TileShape{8, 2}); }
+// partial sums per system written by the post-smoother: one per warp of every tile, over all tile shapes
+int tile2d_max_parts(const MgLevelD &L) {
+  int m = 0;
+  for (const TileShape &t : SHAPES_F) m = std::max(m, tiles_for(L, t) * t.nw);
+  for (const TileShape &t : SHAPES_D) m = std::max(m, tiles_for(L, t) * t.nw);
+  return m;
+}
 
 bool tile2d_ok(const MgProblem &P, int l, int prec) {
   (void)prec;
@@ -268,16 +274,18 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
         sb += bv[q][p];
       }
     }
-    if (part_bx) {
-      const double t = block_sum1<T>(bx);
-      if (threadIdx.x == 0) part_bx[(long)cur * part_stride + blockIdx.x] = t;
-      if (singular && singular[cur]) {  // uniform over the CTA
-        double tx, tb;
-        block_sum2<T>(sx, sb, tx, tb);
-        if (threadIdx.x == 0) {
-          part_x[(long)cur * part_stride + blockIdx.x] = tx;
-          part_b[(long)cur * part_stride + blockIdx.x] = tb;
+    if (part_bx) {  // one partial per warp (shuffles only: no barrier in the system loop)
+      const long e = (long)cur * part_stride + (long)blockIdx.x * NW + w;
+      double t = (double)bx;
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+      if (lane == 0) part_bx[e] = t;
+      if (singular && singular[cur]) {
+        double tx = (double)sx, tb = (double)sb;
+        for (int o = 16; o > 0; o >>= 1) {
+          tx += __shfl_down_sync(0xffffffffu, tx, o);
+          tb += __shfl_down_sync(0xffffffffu, tb, o);
         }
+        if (lane == 0) { part_x[e] = tx; part_b[e] = tb; }
       }
     }
     cur = nxt;
@@ -762,7 +770,7 @@ int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_c
   const MgLevelD &C = l + 1 < P.nlev ? P.L[l + 1] : P.L[l];
   const TileShape t = choose_shape(L, sizeof(T) == 8 ? 1 : 0);
   const int nt = tiles_for(L, t);
-  if (part_bx && nt > part_stride) { set_error("partial-sum area too small for the tiled smoother"); return SNAC_ERR_ARG; }
+  if (part_bx && nt * t.nw > part_stride) { set_error("partial-sum area too small for the tiled smoother"); return SNAC_ERR_ARG; }
   prof_begin(KID_RBGS, st);
   int rc;
   if constexpr (sizeof(T) == 8) {
@@ -779,7 +787,7 @@ int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_c
   }
   prof_end(KID_RBGS, st);
   SNAC_TRY(rc);
-  if (nchunk) *nchunk = part_bx ? nt : 0;
+  if (nchunk) *nchunk = part_bx ? nt * t.nw : 0;
   return SNAC_OK;
 }
 

@@ -62,7 +62,7 @@ __host__ __device__ inline int mg_nu(const MgProblem &P, int l) { return l >= P.
 struct MgGeom;
 // fused kernels (k_mg_fused.cu)
 bool tile2d_ok(const MgProblem &P, int l, int prec);
-int tile2d_max_tiles(const MgLevelD &L);
+int tile2d_max_parts(const MgLevelD &L);
 // part_bx: partials of b.x of the stored cells (post-smoother, mode 1); for the singular systems also those
 // of x and of b in part_x and part_b
 template <typename T>
