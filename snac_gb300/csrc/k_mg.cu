@@ -307,29 +307,15 @@ __device__ __forceinline__ bool cg_converged(SysScal &q, double rr, double tol) 
 }
 
 // The start of a Krylov iteration after the V-cycle z = M r, one CTA per system:
-//  * part_rr given: the convergence test of the previous iteration's update, deferred to here (the loop then
-//    needs no launch of its own for it); a system that has converged leaves the loop now, and the z the
-//    V-cycle just made for it is not used;
 //  * r.z from the partials of the V-cycle's last pass or of k_cg_dot; for a singular system z is taken
 //    orthogonal to the constant (its null space): zmean = sum(z)/nact over the active cells, which the new
 //    search direction leaves out (p = z - zmean + beta p), and r.z becomes r.(z - zmean) = r.z - zmean sum(r),
 //    from the partial sums of z and r made by the same pass;
 //  * beta = r.z / r.z_old (0 on the first iteration).
-__global__ void k_cg_beta2(int *active, const int *singular, SysScal *sc, const double *part_rz, const double *part_z,
-                           const double *part_r, int nrz, const double *part_rr, int nrr, double tol, long nact,
-                           int stride) {
+__global__ void k_cg_beta2(const int *active, const int *singular, SysScal *sc, const double *part_rz,
+                           const double *part_z, const double *part_r, int nrz, long nact, int stride) {
   const int s = blockIdx.x;
   if (!active[s]) return;
-  __shared__ int stop;
-  if (part_rr) {
-    const double rr = cta_sum_parts(part_rr, s, stride, nrr);
-    if (threadIdx.x == 0) {
-      stop = cg_converged(sc[s], rr, tol) ? 1 : 0;
-      if (stop) active[s] = 0;
-    }
-    __syncthreads();
-    if (stop) return;
-  }
   double rz = cta_sum_parts(part_rz, s, stride, nrz);
   double zmean = 0.0;
   if (singular[s]) {
@@ -344,6 +330,14 @@ __global__ void k_cg_beta2(int *active, const int *singular, SysScal *sc, const 
     sc[s].rz = rz;
     sc[s].first = 0;
   }
+}
+
+// convergence test after an update without a host check (k_cg_norms without the count), one CTA per system
+__global__ void k_cg_conv(int *active, SysScal *sc, const double *part_rr, int nrr, double tol, int stride) {
+  const int s = blockIdx.x;
+  if (!active[s]) return;
+  const double rr = cta_sum_parts(part_rr, s, stride, nrr);
+  if (threadIdx.x == 0 && cg_converged(sc[s], rr, tol)) active[s] = 0;
 }
 
 // alpha = rz / p.q; one CTA per system
@@ -679,11 +673,9 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
     }
     // singular systems: the search directions carry no constant (z's mean is left out of p), so x - x0 stays
     // mean-free, and r.z is taken with the projected z (r's mean is zero only up to rounding, and the V-cycle's
-    // constant drift can be large).  Without a host check the previous iteration's convergence test is made
-    // here too.
-    const bool fold = !check_host && it > 1;
-    k_cg_beta2<<<P.nsys, 256, 0, st>>>(W.active, P.singular, W.sc, W.part2, W.part3, W.part4, nrz,
-                                       fold ? W.part0 : nullptr, nflat, tol, P.nact0, W.stride), ::snac::count_launch();
+    // constant drift can be large)
+    k_cg_beta2<<<P.nsys, 256, 0, st>>>(W.active, P.singular, W.sc, W.part2, W.part3, W.part4, nrz, P.nact0,
+                                       W.stride), ::snac::count_launch();
     prof_begin(KID_CG_APPLY, st);
     if constexpr (fusep) {
       if (P.mode3d)
@@ -707,6 +699,8 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
       SNAC_CUDA(cudaMemsetAsync(W.d_count, 0, 2 * sizeof(int), st));
       k_cg_norms<<<P.nsys, 256, 0, st>>>(W.active, nullptr, W.sc, W.part0, nullptr, W.stride, nflat, tol, 0, 0, 0,
                                          W.d_count, nullptr, 0.0), ::snac::count_launch();
+    } else if (it < maxiter) {  // converged systems leave the loop before the next V-cycle (no count needed)
+      k_cg_conv<<<P.nsys, 256, 0, st>>>(W.active, W.sc, W.part0, nflat, tol, W.stride), ::snac::count_launch();
     }
     SNAC_CUDA(cudaGetLastError());
     trace("pcg: iteration", st);
