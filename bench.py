@@ -148,11 +148,12 @@ KERNEL_WORK = {
 USE_GRAPH = 1  # the mixed path replays its refinement steps as CUDA graphs (bench.py --no-graph: off)
 
 
-def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0):
+def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0, **solver):
+    """solver: snac_options fields passed to the domain (the library defaults when absent)."""
     from snac_gb300 import capi
     from snac_gb300.domain import Domain
     case = case_fn()
-    dom = Domain(case, precision=precision, device=device, use_graph=USE_GRAPH if precision else 0)
+    dom = Domain(case, precision=precision, device=device, use_graph=USE_GRAPH if precision else 0, **solver)
     try:
         init_channel(dom, case)
         dom.step(warmup, allow_not_converged=True)

@@ -109,8 +109,24 @@ typedef struct snac_options {
                          CUDA graph captured once per solver */
   int nu;             /* smoothing sweeps before/after each coarse correction (0 = default 2) */
   int device;         /* CUDA device ordinal */
-  int nu_coarse;      /* smoothing sweeps per side on multigrid levels 2 and coarser (0 = default: 1 with a
+  int nu_coarse;      /* smoothing sweeps per side on multigrid levels mg_lnu and coarser (0 = default: 1 with a
                          transform axis, nu for a 3-D solve) */
+  /* mixed-precision solve (precision 1); 0 selects the default everywhere */
+  int inner_iters;    /* FP32 Krylov iterations per refinement step (default 6) */
+  double inner_tol;   /* relative reduction at which a system's FP32 solve stops (default 1e-7, the FP32 floor) */
+  int inner_adapt;    /* 1 (default): a system's FP32 solve also stops once its outer residual would be within a
+                         tenth of the tolerance; -1: off */
+  int refine_steps;   /* FP32 refinement steps after which the systems still above the tolerance finish with
+                         FP64 conjugate-gradient iterations (default 2); -1: refine in FP32 until converged */
+  /* multigrid kernels (plane systems: tiled smoother, one-CTA coarse V-cycle) */
+  int mg_fuse;        /* bits: 1 tiled FP32 smoother, 2 one-CTA coarse V-cycle FP32, 4 tiled FP64 smoother,
+                         8 one-CTA coarse V-cycle FP64 (default 11); -1: one kernel per sweep */
+  int mg_cta_level;   /* finest level the one-CTA coarse V-cycle may start at (default: the finest that fits) */
+  int mg_tile;        /* FP32 smoother tile, warps x rows per warp: 1 8x2, 2 8x3, 3 16x2, 4 16x3 (default: the
+                         shape with the fewest tile rows) */
+  int mg_waves;       /* waves of CTAs per batched plane launch (default 2) */
+  int mg_red_batch;   /* -1: the reducing plane kernels run one system per CTA (default: batched) */
+  int mg_lnu;         /* first multigrid level that uses nu_coarse (default 2) */
 } snac_options;
 
 typedef struct snac_step_stats {
@@ -327,6 +343,10 @@ typedef struct snac_tune_result {
   double ms_per_step;   /* device time per step of the chosen candidate */
   double ms_before;     /* device time per step of the settings in use before the call */
   int ncand;            /* candidates timed */
+  int mg_tile;          /* chosen FP32 smoother tile of level 0 (as snac_options.mg_tile; 0 without a plane solve) */
+  int mg_waves;         /* chosen waves of CTAs per batched plane launch */
+  int mg_cta_level;     /* first level of the one-CTA coarse V-cycle of the chosen solve */
+  int refine_steps;     /* mixed solve: FP32 refinement steps before FP64 finishing (-1: FP32 to convergence) */
 } snac_tune_result;
 int snac_autotune(int steps, snac_tune_result *out);
 /* No counterpart in the reference: a host-side fault injector for testing snac_autotune's error paths.  The

@@ -48,12 +48,16 @@ class CaseDesc(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("use_graph", C.c_int), ("nu", C.c_int), ("device", C.c_int),
-                ("nu_coarse", C.c_int)]
+                ("nu_coarse", C.c_int), ("inner_iters", C.c_int), ("inner_tol", C.c_double),
+                ("inner_adapt", C.c_int), ("refine_steps", C.c_int), ("mg_fuse", C.c_int),
+                ("mg_cta_level", C.c_int), ("mg_tile", C.c_int), ("mg_waves", C.c_int), ("mg_red_batch", C.c_int),
+                ("mg_lnu", C.c_int)]
 
 
 class TuneResult(C.Structure):
     _fields_ = [("precision", C.c_int), ("inner_iters", C.c_int), ("nu_coarse", C.c_int), ("ms_per_step", C.c_double),
-                ("ms_before", C.c_double), ("ncand", C.c_int)]
+                ("ms_before", C.c_double), ("ncand", C.c_int), ("mg_tile", C.c_int), ("mg_waves", C.c_int),
+                ("mg_cta_level", C.c_int), ("refine_steps", C.c_int)]
 
 
 class StepStats(C.Structure):

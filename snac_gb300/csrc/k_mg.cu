@@ -544,6 +544,11 @@ __global__ void __launch_bounds__(256) k_ir_up(long n, const int *active, const 
   }
 }
 
+__global__ void k_sc_first(int nsys, SysScal *sc) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) sc[s].first = 1;
+}
+
 // active[s] = src ? src[s] : 1
 __global__ void k_set_active(int nsys, int *active, const int *src) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -628,6 +633,12 @@ template int mg_residual<float>(const MgProblem &, CgWork &, const float *, cons
 int mg_restart_bad_guess(const MgProblem &P, CgWork &W, double *x, const double *b, double *r, cudaStream_t st) {
   const long n = P.L[0].ncell;
   k_restart_systems<double><<<dim3((unsigned)((n + 255) / 256), P.nsys), 256, 0, st>>>(n, W.sc, x, b, r), ::snac::count_launch();
+  SNAC_CUDA(cudaGetLastError());
+  return SNAC_OK;
+}
+
+int mg_restart_krylov(const MgProblem &P, CgWork &W, cudaStream_t st) {
+  k_sc_first<<<(P.nsys + 127) / 128, 128, 0, st>>>(P.nsys, W.sc), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

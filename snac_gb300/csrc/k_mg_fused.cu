@@ -39,15 +39,16 @@ constexpr int TSW = 64;            // tile width
 constexpr int TBX = TSW - 2 * TH;  // output columns per tile
 // tile shapes: NW warps x R rows per warp = tile height SH (output rows SH - 2 TH)
 struct TileShape { int nw, r; };
-const TileShape SHAPES_F[] = {{8, 2}, {8, 3}, {16, 2}, {16, 3}};
+const TileShape SHAPES_F[] = {{8, 2}, {8, 3}, {16, 2}, {16, 3}};  // snac_options.mg_tile 1..4
 const TileShape SHAPES_D[] = {{8, 2}};
 inline int tile_by(TileShape t) { return t.nw * t.r - 2 * TH; }
 inline int tiles_for(const MgLevelD &L, TileShape t) {
   return ((L.n[0] + TBX - 1) / TBX) * ((L.n[1] + tile_by(t) - 1) / tile_by(t));
 }
-// the shape that processes the fewest tile rows (ties: the smaller tile; SNAC_MG_TILE_TALL=1: the taller)
-TileShape choose_shape(const MgLevelD &L, int prec) {
-  static const bool tall = [] { const char *e = getenv("SNAC_MG_TILE_TALL"); return e && e[0] == '1'; }();
+// the shape given by `pref` (1..4, FP32 only), else the one that processes the fewest tile rows (ties: the
+// smaller tile)
+TileShape choose_shape(const MgLevelD &L, int prec, int pref) {
+  if (!prec && pref >= 1 && pref <= 4) return SHAPES_F[pref - 1];
   const TileShape *opts = prec ? SHAPES_D : SHAPES_F;
   const int nopt = prec ? 1 : 4;
   TileShape best = opts[0];
@@ -55,7 +56,7 @@ TileShape choose_shape(const MgLevelD &L, int prec) {
   for (int q = 0; q < nopt; q++) {
     const TileShape t = opts[q];
     const long cost = (long)((L.n[1] + tile_by(t) - 1) / tile_by(t)) * t.nw * t.r;
-    if (bestc < 0 || cost < bestc || (tall && cost == bestc)) { bestc = cost; best = t; }
+    if (bestc < 0 || cost < bestc) { bestc = cost; best = t; }
   }
   return best;
 }
@@ -67,6 +68,14 @@ __device__ __forceinline__ int wrap(int g, int n) {
 }  // namespace
 
 // partial sums per system written by the post-smoother: one per warp of every tile, over all tile shapes
+// the FP32 tile shape level l of P uses, as snac_options.mg_tile (1..4)
+int tile2d_shape_index(const MgProblem &P, int l) {
+  const TileShape t = choose_shape(P.L[l], 0, P.tile_shape);
+  for (int q = 0; q < 4; q++)
+    if (SHAPES_F[q].nw == t.nw && SHAPES_F[q].r == t.r) return q + 1;
+  return 0;
+}
+
 int tile2d_max_parts(const MgLevelD &L) {
   int m = 0;
   for (const TileShape &t : SHAPES_F) m = std::max(m, tiles_for(L, t) * t.nw);
@@ -768,7 +777,7 @@ int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_c
   if (mode == 1 && (xin == x || !xin || !xc)) { set_error("tiled post-smoother needs separate input and output"); return SNAC_ERR_ARG; }
   const MgLevelD &L = P.L[l];
   const MgLevelD &C = l + 1 < P.nlev ? P.L[l + 1] : P.L[l];
-  const TileShape t = choose_shape(L, sizeof(T) == 8 ? 1 : 0);
+  const TileShape t = choose_shape(L, sizeof(T) == 8 ? 1 : 0, P.tile_shape);
   const int nt = tiles_for(L, t);
   if (part_bx && nt * t.nw > part_stride) { set_error("partial-sum area too small for the tiled smoother"); return SNAC_ERR_ARG; }
   prof_begin(KID_RBGS, st);

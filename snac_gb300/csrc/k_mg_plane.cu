@@ -33,14 +33,10 @@ int plane_resid_nchunk(const MgLevelD &L, int prec) {
   return ((L.n[0] + 31) / 32) * ((L.n[1] + 8 * rr - 1) / (8 * rr));
 }
 
-// systems per CTA: enough CTAs for about `waves` waves of `per_sm` resident CTAs on every multiprocessor
-// (SNAC_MG_WAVES overrides the default of 2; a large value gives one system per CTA)
+// systems per CTA: enough CTAs for about P.waves waves of `per_sm` resident CTAs on every multiprocessor (a
+// large value gives one system per CTA)
 int plane_batch(const MgProblem &P, long ctas_per_system, int per_sm) {
-  static const long waves = [] {
-    const char *e = getenv("SNAC_MG_WAVES");
-    const long v = e ? atol(e) : 2;
-    return v > 0 ? v : 2;
-  }();
+  const long waves = P.waves > 0 ? P.waves : 2;
   const long target = waves * std::max(1, P.nsm) * per_sm;
   long sb = (ctas_per_system * P.nsys) / std::max(1L, target);
   sb = std::max(1L, std::min(sb, (long)P.nsys));
@@ -309,10 +305,9 @@ int plane_make_invd(MgProblem &P, double *const *out, float *const *outf, cudaSt
   return SNAC_OK;
 }
 
-// the reducing kernels batch systems like the others (SNAC_MG_RED_BATCH=0: one system per CTA)
+// the reducing kernels batch systems like the others (P.red_batch = 0: one system per CTA)
 static int red_batch(const MgProblem &P, long ctas_per_system) {
-  static const int on = [] { const char *e = getenv("SNAC_MG_RED_BATCH"); return !(e && e[0] == '0'); }();
-  return on ? plane_batch(P, ctas_per_system, 8) : 1;
+  return P.red_batch ? plane_batch(P, ctas_per_system, 8) : 1;
 }
 
 template <typename T>

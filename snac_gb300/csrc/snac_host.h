@@ -95,7 +95,7 @@ struct PoissonSolver {
   double *d_lambda = nullptr;        // Helmholtz with a transform: lambda_k / dl^2 (the shift is lambda_k + alphai)
   std::vector<double> lambda;
   int precision = 0;
-  int inner_iters = 5;               // mixed path: FP32 Krylov iterations per refinement step
+  int inner_iters = 6;               // mixed path: FP32 Krylov iterations per refinement step
   int use_graph = 0;                 // mixed path: replay each refinement step's FP32 solve as a CUDA graph
   cudaGraphExec_t inner_exec = nullptr;
   long long inner_nodes = 0;         // kernel launches in that graph
@@ -104,7 +104,9 @@ struct PoissonSolver {
   static constexpr int SPEC_MAX = 8;
   int spec_outer = 0;
   int *d_ocount = nullptr, *h_ocount = nullptr;  // 2 * SPEC_MAX ints (device, pinned host)
-  double inner_tol = 1e-6;           // mixed path: relative tolerance of the FP32 solve
+  double inner_tol = 1e-7;           // mixed path: relative tolerance of the FP32 solve
+  int refine_steps = 2;              // mixed path: FP32 refinement steps before the systems still above the
+                                     // tolerance finish with FP64 PCG (-1: FP32 refinement to convergence)
   bool adapt_inner = true;           // mixed path: each system's inner solve stops once its outer residual
                                      // would be within a tenth of the tolerance (never beyond inner_tol)
   double tol = 1e-12;
@@ -119,6 +121,7 @@ struct PoissonSolver {
   float *box_e32 = nullptr;  // FP32 correction of the mixed path
   std::vector<void *> allocs;
   int last_iters = 0;
+  int last_polish = 0;               // mixed path: FP64 PCG iterations that finished the last solve
   double last_res = 0.0;
   int host_levels = 0;
   long host_coarse_cells = 0;
@@ -151,7 +154,6 @@ struct Domain {
   std::unique_ptr<PoissonSolver> ps;
   std::unique_ptr<PoissonSolver> hs[3 + SNAC_MAX_SCAL];  // IMPDIFF: Helmholtz solvers of u, v, w, scalars
   GuessState *guess = nullptr;       // learned initial guess of the pressure solve (off unless requested)
-  int tune_inner = 0;                // FP32 Krylov iterations per refinement step set by snac_autotune (0: default)
   double dt = 0.0, time = 0.0;
   int istep = 0;
   int last_solve_iters = 0, solves = 0;

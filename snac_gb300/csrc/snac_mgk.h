@@ -47,6 +47,8 @@ int mg_ir_down(const MgProblem &P, const CgWork &Wout, CgWork &W32, const double
                double inner_tol, double outer_tol, cudaStream_t st);
 int mg_ir_up(const MgProblem &P, const CgWork &Wout, const float *e32, double *x, cudaStream_t st);
 int mg_zero_rhs_systems(const MgProblem &P, const CgWork &W, double *x, cudaStream_t st);
+// the next mg_pcg starts a new Krylov sequence (first iteration: beta = 0) for every system of W
+int mg_restart_krylov(const MgProblem &P, CgWork &W, cudaStream_t st);
 // systems whose warm start is worse than zero (set by mg_residual with set_bb): x = 0, r = b
 int mg_restart_bad_guess(const MgProblem &P, CgWork &W, double *x, const double *b, double *r, cudaStream_t st);
 

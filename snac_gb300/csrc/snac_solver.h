@@ -50,6 +50,9 @@ struct MgProblem {
   int fused;                         // bits: 1/4 tiled plane smoother FP32/FP64, 2/8 one-CTA coarse tail FP32/FP64
   int cta_level[2];                  // first level run by k_vcycle_coarse / k_vcycle_coarse3d ([0] FP32, [1] FP64); nlev = none
   int nsm;                           // multiprocessors of the device (sizes the system batches)
+  int tile_shape;                    // FP32 smoother tile: 0 auto, 1..4 = 8x2, 8x3, 16x2, 16x3 (warps x rows)
+  int waves;                         // waves of CTAs per batched plane launch
+  int red_batch;                     // the reducing plane kernels batch systems (0: one system per CTA)
   int any_singular;                  // some system is singular (pure Neumann, zero shift)
   const int *sing_list;              // device: indices of the singular systems (nsing of them)
   int nsing;
@@ -63,6 +66,7 @@ struct MgGeom;
 // fused kernels (k_mg_fused.cu)
 bool tile2d_ok(const MgProblem &P, int l, int prec);
 int tile2d_max_parts(const MgLevelD &L);
+int tile2d_shape_index(const MgProblem &P, int l);
 // part_bx: partials of b.x of the stored cells (post-smoother, mode 1); for the singular systems also those
 // of x and of b in part_x and part_b
 template <typename T>

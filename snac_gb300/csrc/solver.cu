@@ -272,11 +272,11 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
   S.field = field;
   S.helm = field != HF_P;
   S.precision = d.opt.precision;
-  if (d.tune_inner > 0) S.inner_iters = d.tune_inner;
-  // SNAC_MG_ADAPT=0: every inner solve reduces its residual by inner_tol, whatever the outer residual needs
-  if (const char *e = getenv("SNAC_MG_ADAPT")) S.adapt_inner = e[0] != '0';
-  if (const char *e = getenv("SNAC_MG_INNER")) S.inner_iters = std::max(1, atoi(e));
-  if (const char *e = getenv("SNAC_MG_INNER_TOL")) S.inner_tol = atof(e);
+  const snac_options &o = d.opt;
+  if (o.inner_iters > 0) S.inner_iters = o.inner_iters;
+  if (o.inner_tol > 0.0) S.inner_tol = o.inner_tol;
+  S.adapt_inner = o.inner_adapt >= 0;  // -1: every inner solve reduces by inner_tol, whatever the outer needs
+  if (o.refine_steps != 0) S.refine_steps = o.refine_steps;
   S.use_graph = d.opt.use_graph ? 1 : 0;
   S.tol = c.tol;
   S.maxiter = c.maxiter;
@@ -560,9 +560,11 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
   P.nu = d.opt.nu > 0 ? d.opt.nu : 2;
   // levels from 2 down: one sweep per side in plane mode (the tiled levels 0 and 1 keep nu; on the
   // channel this halves the one-CTA coarse V-cycle at the same refinement-step count), nu in 3-D mode
-  P.lnu = 2;
+  P.lnu = o.mg_lnu > 0 ? o.mg_lnu : 2;
   P.nu_coarse = d.opt.nu_coarse > 0 ? d.opt.nu_coarse : (S.mode3d ? P.nu : 1);
-  if (const char *e = getenv("SNAC_MG_LNU")) P.lnu = std::max(0, atoi(e));  // tuning: first level with nu_coarse
+  P.tile_shape = o.mg_tile >= 1 && o.mg_tile <= 4 ? o.mg_tile : 0;
+  P.waves = o.mg_waves > 0 ? o.mg_waves : 2;
+  P.red_batch = o.mg_red_batch == -1 ? 0 : 1;
   auto up = [&](const void *src, size_t bytes) -> void * {
     void *p = S.alloc(bytes ? bytes : 8);
     if (p && bytes) cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
@@ -614,14 +616,11 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
   }
   // fused kernels: tiled plane smoother and a one-CTA coarse tail where its levels fit in shared memory
   {
-    // SNAC_MG_FUSE bit mask: 1 tiled smoother FP32, 2 coarse tail FP32, 4 tiled FP64, 8 coarse tail FP64.
-    // Default 11: the tile's redundant halo updates cost more than they save where FP64 arithmetic bounds.
-    const char *e = getenv("SNAC_MG_UNFUSED");
-    const char *m = getenv("SNAC_MG_FUSE");
-    P.fused = (e && e[0] && e[0] != '0') ? 0 : (m && m[0]) ? (int)strtol(m, nullptr, 0) & 15 : 11;
-    // SNAC_MG_CTA_LEVEL: the finest level the one-CTA coarse tail may start at (default 0: the finest that fits)
-    const char *cl = getenv("SNAC_MG_CTA_LEVEL");
-    const int lmin = cl && cl[0] ? std::max(0, atoi(cl)) : 0;
+    // bit mask: 1 tiled smoother FP32, 2 coarse tail FP32, 4 tiled FP64, 8 coarse tail FP64.  Default 11: the
+    // tile's redundant halo updates cost more than they save where FP64 arithmetic bounds.
+    P.fused = o.mg_fuse == -1 ? 0 : (o.mg_fuse > 0 ? o.mg_fuse & 15 : 11);
+    // the finest level the one-CTA coarse tail may start at (default: the finest that fits)
+    const int lmin = std::max(0, o.mg_cta_level);
     for (int prec = 0; prec < 2; prec++) {
       P.cta_level[prec] = P.nlev;
       for (int l = lmin; l < P.nlev; l++) {
@@ -774,7 +773,7 @@ static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *
   // mixed precision: iterative refinement in FP64 around FP32 Krylov solves (zero initial guess).  The
   // first `spec` refinement steps run without a host round trip (converged systems are skipped on the
   // device by their active flags); the counts of every step are read after step `spec`.
-  int outer = 0, needed = -1;
+  int outer = 0, needed = -1, polish = 0;
   CgWork Wr = S.W64;  // residual-only use of the FP64 work area
   Wr.active = S.active_outer;
   Wr.sc = S.sc_outer;
@@ -816,16 +815,36 @@ static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *
     if (outer == 0 && cnt[1]) SNAC_TRY(mg_zero_rhs_systems(P, Wo, S.box_x, st));
     if (outer == 0) SNAC_TRY(mg_restart_bad_guess(P, Wo, S.box_x, S.box_b, S.r64, st));
     if (cnt[0] == 0) break;
+    if (S.refine_steps > 0 && outer >= S.refine_steps) {
+      // Each FP32 refinement step gains about seven digits at best (the FP32 floor); after refine_steps of
+      // them only a few systems are still above the tolerance -- typically the singular zero-wavenumber one,
+      // the worst conditioned, whose steps gain fewer.  Another FP32 step would cost a full inner solve's
+      // launches for them; FP64 PCG iterations from the current iterate, on those systems only, finish them
+      // (the same stopping test as the plain FP64 path).
+      CgWork Wf = S.W64;
+      Wf.r = S.r64;
+      Wf.active = S.active_outer;
+      Wf.sc = S.sc_outer;
+      Wf.d_count = Wo.d_count;
+      Wf.h_count = outer <= spec ? S.h_ocount + 2 * outer : Wo.h_count;
+      SNAC_TRY(mg_restart_krylov(P, Wf, st));
+      int pit = 0;
+      SNAC_TRY(mg_pcg<double>(P, Wf, S.box_x, S.maxiter, S.tol, false, true, &pit, st));
+      polish = pit;
+      outer++;
+      break;
+    }
     SNAC_TRY(refine_step(S, Wr, st));
   }
   if (needed < 0) needed = outer;
-  S.spec_outer = needed;
+  S.spec_outer = std::min(needed, S.refine_steps > 0 ? S.refine_steps : needed);
   SNAC_CUDA(cudaMemcpyAsync(sc.data(), S.sc_outer, P.nsys * sizeof(SysScal), cudaMemcpyDeviceToHost, st));
   SNAC_CUDA(cudaStreamSynchronize(st));
   for (auto &v : sc) worst = std::max(worst, v.rel);
   *iters_out = needed;
+  S.last_polish = polish;
   *res_out = worst;
-  return (outer >= S.maxiter && worst > S.tol) ? SNAC_ERR_NOT_CONVERGED : SNAC_OK;
+  return (worst > S.tol && (outer >= S.maxiter || polish >= S.maxiter)) ? SNAC_ERR_NOT_CONVERGED : SNAC_OK;
 }
 
 // solve_impdiff_field_3d (solve_helmholtz.f90:109-138): right-hand side alphai V phi + BC planes, the

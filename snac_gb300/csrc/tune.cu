@@ -1,8 +1,9 @@
 // tune.cu -- snac_autotune: the solver settings for the case at hand, chosen by timing RK3 steps.
 //
-// The candidates differ in the solve (plain FP64, or mixed with 4, 5 or 6 FP32 Krylov iterations per
-// refinement step) and in the smoothing sweeps per side on the coarse levels (transform-axis solve); all
-// solve to the same tolerance.  Each candidate rebuilds the
+// The candidates differ in the solve (plain FP64, or mixed with 5, 6 or 7 FP32 Krylov iterations per
+// refinement step, finished in FP64 or refined in FP32 to convergence), the smoothing sweeps per side on the
+// coarse levels and, for the transform-axis solve, the smoother tile shape, the CTA waves per launch and the
+// first level of the one-CTA coarse V-cycle; all solve to the same tolerance.  Each candidate rebuilds the
 // solvers and runs from the same snapshot of the state; the state is restored afterwards, including the
 // solvers' warm starts, so the run continues as if only the settings had changed.
 #include <string>
@@ -119,14 +120,8 @@ int snac_autotune(int steps, snac_tune_result *out) {
   Domain *d = domain();
   if (!d) { set_error("snac_autotune: no domain (call snac_init first)"); return SNAC_ERR_STATE; }
   if (steps < 1) { set_error("snac_autotune: steps must be >= 1"); return SNAC_ERR_ARG; }
-  const int inner0 = d->tune_inner, nuc0 = d->opt.nu_coarse, prec0 = d->opt.precision;
+  const snac_options opt0 = d->opt;
   const bool plane = d->ps && !d->ps->mode3d;
-  struct Cand { int prec, inner, nuc; };  // inner, nuc: 0 = the solver's default
-  std::vector<Cand> cand;
-  for (int nuc : plane ? std::vector<int>{1, 2} : std::vector<int>{0}) {
-    for (int inner : {4, 5, 6}) cand.push_back({1, inner, nuc});
-    cand.push_back({0, 0, nuc});
-  }
   // the timed steps solve the same restored state again and again: recording them as training pairs of the
   // learned guess would fill its ring with near-copies, so recording pauses while tuning
   const int gmode0 = guess_get_mode(*d);
@@ -134,10 +129,8 @@ int snac_autotune(int steps, snac_tune_result *out) {
   Snapshot snap;
   // on every way out: the chosen (or, after an error, the original) settings, solvers built for them and the
   // state of the snapshot, so that the run goes on as if only the settings had changed
-  auto finish = [&](int prec, int inner, int nuc, int rc) -> int {
-    d->opt.precision = prec;
-    d->tune_inner = inner;
-    d->opt.nu_coarse = nuc;
+  auto finish = [&](const snac_options &o, int rc) -> int {
+    d->opt = o;
     const std::string msg = rc != SNAC_OK ? std::string(snac_last_error()) : std::string();
     int rc2 = rebuild(*d);
     if (rc2 == SNAC_OK && !snap.arrays.empty()) rc2 = restore(*d, snap, true);
@@ -164,38 +157,90 @@ int snac_autotune(int steps, snac_tune_result *out) {
   double ms_before = 0.0;
   {
     const int rc = time_current(&ms_before);
-    if (rc != SNAC_OK) return finish(prec0, inner0, nuc0, rc);
+    if (rc != SNAC_OK) return finish(opt0, rc);
   }
+  // Candidates are searched one group at a time, each group varying its settings around the best so far:
+  // the solve (plain FP64, or mixed with 5, 6 or 7 FP32 iterations per refinement step) x the coarse-level
+  // sweeps; then, for the plane systems, the smoother tile shape, the waves of CTAs per batched launch and
+  // the level where the one-CTA coarse V-cycle starts; then, for the mixed solve, FP64 finishing after two
+  // refinement steps against FP32 refinement to convergence.
+  snac_options best_opt = opt0;
   double best = 1e300;
-  int bi = -1, ntimed = 0;
-  for (size_t i = 0; i < cand.size(); i++) {
-    d->opt.precision = cand[i].prec;
-    d->tune_inner = cand[i].inner;
-    d->opt.nu_coarse = cand[i].nuc;
-    int rc = rebuild(*d);
-    if (rc == SNAC_OK && (int)i == g_fail_candidate) {
-      g_fail_candidate = -1;
-      set_error("snac_autotune: failure injected at candidate %d", (int)i);
-      rc = SNAC_ERR_STATE;
+  int ntimed = 0, found = 0;
+  auto try_group = [&](const std::vector<snac_options> &group) -> int {
+    for (const snac_options &o : group) {
+      d->opt = o;
+      int rc = rebuild(*d);
+      if (rc == SNAC_OK && ntimed == g_fail_candidate) {
+        g_fail_candidate = -1;
+        set_error("snac_autotune: failure injected at candidate %d", ntimed);
+        rc = SNAC_ERR_STATE;
+      }
+      double ms = 0.0;
+      if (rc == SNAC_OK) rc = time_current(&ms);
+      ntimed++;
+      if (rc == SNAC_ERR_NOT_CONVERGED) continue;  // this candidate does not reach the tolerance
+      if (rc != SNAC_OK) return rc;
+      if (ms < best) { best = ms; best_opt = o; found = 1; }
     }
-    double ms = 0.0;
-    if (rc == SNAC_OK) rc = time_current(&ms);
-    ntimed++;
-    if (rc == SNAC_ERR_NOT_CONVERGED) continue;  // this candidate does not reach the tolerance
-    if (rc != SNAC_OK) return finish(prec0, inner0, nuc0, rc);
-    if (ms < best) { best = ms; bi = (int)i; }
+    return SNAC_OK;
+  };
+  std::vector<snac_options> g;
+  for (int nuc : plane ? std::vector<int>{1, 2} : std::vector<int>{0}) {
+    for (int inner : {5, 6, 7}) {
+      snac_options o = opt0;
+      o.precision = 1; o.inner_iters = inner; o.nu_coarse = nuc;
+      g.push_back(o);
+    }
+    snac_options o = opt0;
+    o.precision = 0; o.inner_iters = 0; o.nu_coarse = nuc;
+    g.push_back(o);
   }
+  int rc = try_group(g);
+  if (rc == SNAC_OK && found && plane) {
+    g.clear();
+    for (int t = 1; t <= 4; t++) { snac_options o = best_opt; o.mg_tile = t; g.push_back(o); }
+    rc = try_group(g);
+  }
+  if (rc == SNAC_OK && found && plane) {
+    g.clear();
+    for (int w : {1, 2, 4}) { snac_options o = best_opt; o.mg_waves = w; g.push_back(o); }
+    rc = try_group(g);
+  }
+  if (rc == SNAC_OK && found && plane && d->ps) {
+    // the one-CTA coarse V-cycle from the finest level that fits (the default) or one level coarser
+    d->opt = best_opt;
+    rc = rebuild(*d);
+    if (rc == SNAC_OK) {
+      const int prec = best_opt.precision ? 0 : 1;
+      const int l0 = d->ps->P.cta_level[prec];
+      g.clear();
+      if (l0 + 1 < d->ps->P.nlev) {
+        snac_options o = best_opt; o.mg_cta_level = l0 + 1; g.push_back(o);
+        o.mg_cta_level = l0; g.push_back(o);
+      }
+      rc = try_group(g);
+    }
+  }
+  if (rc == SNAC_OK && found && best_opt.precision == 1) {
+    g.clear();
+    for (int r : {2, -1}) { snac_options o = best_opt; o.refine_steps = r; g.push_back(o); }
+    rc = try_group(g);
+  }
+  if (rc != SNAC_OK) return finish(opt0, rc);
   // nothing converged: keep the settings that were in use
-  const int rc = bi < 0 ? finish(prec0, inner0, nuc0, SNAC_OK)
-                        : finish(cand[bi].prec, cand[bi].inner, cand[bi].nuc, SNAC_OK);
-  SNAC_TRY(rc);
+  SNAC_TRY(finish(found ? best_opt : opt0, SNAC_OK));
   if (out) {
     out->precision = d->opt.precision;
     out->inner_iters = d->ps ? d->ps->inner_iters : 0;
     out->nu_coarse = d->ps ? d->ps->P.nu_coarse : 0;
-    out->ms_per_step = bi < 0 ? ms_before : best;
+    out->ms_per_step = found ? best : ms_before;
     out->ms_before = ms_before;
     out->ncand = ntimed;
+    out->mg_tile = d->ps && plane ? tile2d_shape_index(d->ps->P, 0) : 0;
+    out->mg_waves = d->ps ? d->ps->P.waves : 0;
+    out->mg_cta_level = d->ps ? d->ps->P.cta_level[d->opt.precision ? 0 : 1] : 0;
+    out->refine_steps = d->ps ? d->ps->refine_steps : 0;
   }
   return SNAC_OK;
 }

@@ -17,12 +17,20 @@ from .capi import check, dptr
 
 
 class Domain:
-    def __init__(self, case, precision: int = 0, nu: int = 0, device: int = 0, use_graph: int = 0, nu_coarse: int = 0):
+    def __init__(self, case, precision: int = 0, nu: int = 0, device: int = 0, use_graph: int = 0, nu_coarse: int = 0,
+                 **solver):
+        """solver: further snac_options fields (inner_iters, inner_tol, inner_adapt, refine_steps, mg_fuse,
+        mg_cta_level, mg_tile, mg_waves, mg_red_batch, mg_lnu); 0 or absent selects the library default."""
         L = capi.lib()
         self.case = case
         c, arr, keep = capi.fill_descs(case)
         opt = capi.Options(precision=int(precision), use_graph=int(use_graph), nu=int(nu), device=int(device),
                            nu_coarse=int(nu_coarse))
+        names = {f[0] for f in capi.Options._fields_}
+        for k, v in solver.items():
+            if k not in names:
+                raise TypeError(f"unknown solver option {k}")
+            setattr(opt, k, v)
         check(L.snac_init(C.byref(c), arr, C.byref(opt)))
         self._keep = keep
         self.nblocks = len(case.blocks)
@@ -158,7 +166,8 @@ class Domain:
         r = capi.TuneResult()
         check(capi.lib().snac_autotune(int(steps), C.byref(r)))
         return dict(precision=r.precision, inner_iters=r.inner_iters, nu_coarse=r.nu_coarse, ms_per_step=r.ms_per_step,
-                    ms_before=r.ms_before, candidates=r.ncand)
+                    ms_before=r.ms_before, candidates=r.ncand, mg_tile=r.mg_tile, mg_waves=r.mg_waves,
+                    mg_cta_level=r.mg_cta_level, refine_steps=r.refine_steps)
 
     def stats(self):
         s = capi.StepStats()

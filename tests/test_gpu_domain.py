@@ -130,7 +130,7 @@ def test_solve_pressure_matches_oracle(snac_lib, oracle_mod, precision):
 @pytest.mark.parametrize("nu_coarse", [0, 2])
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("which", ["channel", "ldc3d"])
-def test_fused_vcycle_matches_unfused(snac_lib, monkeypatch, precision, which, nu_coarse):
+def test_fused_vcycle_matches_unfused(snac_lib, precision, which, nu_coarse):
     """The tiled smoother / one-CTA coarse tail give the same solves as one kernel per sweep, with the
     default smoothing counts (one sweep per side on levels 2 and coarser with a transform axis) and with
     two sweeps everywhere.
@@ -143,9 +143,7 @@ def test_fused_vcycle_matches_unfused(snac_lib, monkeypatch, precision, which, n
     out = {}
     for mode in ("1", "0"):
         # "1": one kernel per sweep; "0": every fused kernel of both precisions (mask 15)
-        monkeypatch.setenv("SNAC_MG_UNFUSED", mode)
-        monkeypatch.setenv("SNAC_MG_FUSE", "15")
-        d = Domain(case, precision=precision, nu_coarse=nu_coarse)
+        d = Domain(case, precision=precision, nu_coarse=nu_coarse, mg_fuse=-1 if mode == "1" else 15)
         try:
             rng = np.random.default_rng(11)
             for ib in range(len(case.blocks)):
@@ -166,15 +164,13 @@ def test_fused_vcycle_matches_unfused(snac_lib, monkeypatch, precision, which, n
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-def test_fused_vcycle_iterations_multiwave(snac_lib, monkeypatch, precision):
+def test_fused_vcycle_iterations_multiwave(snac_lib, precision):
     """Fused and unfused V-cycles are the same preconditioner, also when the tiled kernels run in
     several waves (tiles of one launch then read and write neighbouring cells at different times)."""
     case = cases.channel_4block(nx=(96, 160), ny=(64, 80), nz=32)
     res = {}
     for mode in ("1", "0"):
-        monkeypatch.setenv("SNAC_MG_UNFUSED", mode)
-        monkeypatch.setenv("SNAC_MG_FUSE", "15")
-        d = Domain(case, precision=precision)
+        d = Domain(case, precision=precision, mg_fuse=-1 if mode == "1" else 15)
         try:
             ic = cases.channel_initial_condition(case, lambda ib: d.grid(ib, 1, capi.G_XC))
             for ib, (u, v, w) in ic.items():
@@ -617,8 +613,11 @@ def test_autotune_restores_state(snac_lib, precision):
             st0 = d.stats()
             if tune:
                 r = d.autotune(2)
-                assert r["candidates"] == 8, r  # (mixed with 4, 5, 6 inner iterations, plain) x (1, 2 sweeps)
-                assert r["precision"] in (0, 1) and r["inner_iters"] in (4, 5, 6) and r["nu_coarse"] in (1, 2), r
+                # (mixed with 5, 6, 7 inner iterations, plain) x (1, 2 sweeps), 4 tile shapes, 3 waves, up to 2
+                # coarse-cycle levels, and for the mixed solve 2 refinement strategies
+                assert 15 <= r["candidates"] <= 19, r
+                assert r["precision"] in (0, 1) and r["inner_iters"] in (5, 6, 7) and r["nu_coarse"] in (1, 2), r
+                assert r["mg_tile"] in (1, 2, 3, 4) and r["mg_waves"] in (1, 2, 4), r
                 assert 0.0 < r["ms_per_step"] <= r["ms_before"] * 1.5, r
                 after = [d.get(ib, k) for ib in range(len(case.blocks)) for k in (capi.U, capi.V, capi.W, capi.P)]
                 for a, b in zip(before, after):
