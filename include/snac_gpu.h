@@ -112,12 +112,13 @@ typedef struct snac_options {
   int nu_coarse;      /* smoothing sweeps per side on multigrid levels mg_lnu and coarser (0 = default: 1 with a
                          transform axis, nu for a 3-D solve) */
   /* mixed-precision solve (precision 1); 0 selects the default everywhere */
-  int inner_iters;    /* FP32 Krylov iterations per refinement step (default 6) */
-  double inner_tol;   /* relative reduction at which a system's FP32 solve stops (default 1e-7, the FP32 floor) */
+  int inner_iters;    /* FP32 Krylov iterations per refinement step (default 5) */
+  double inner_tol;   /* relative reduction at which a system's FP32 solve stops (default 1e-6) */
   int inner_adapt;    /* 1 (default): a system's FP32 solve also stops once its outer residual would be within a
                          tenth of the tolerance; -1: off */
-  int refine_steps;   /* FP32 refinement steps after which the systems still above the tolerance finish with
-                         FP64 conjugate-gradient iterations (default 2); -1: refine in FP32 until converged */
+  int refine_steps;   /* n > 0: FP32 refinement steps after which the systems still above the tolerance finish
+                         with FP64 conjugate-gradient iterations; default (0 or -1): FP32 refinement steps
+                         until converged */
   /* multigrid kernels (plane systems: tiled smoother, one-CTA coarse V-cycle) */
   int mg_fuse;        /* bits: 1 tiled FP32 smoother, 2 one-CTA coarse V-cycle FP32, 4 tiled FP64 smoother,
                          8 one-CTA coarse V-cycle FP64 (default 11); -1: one kernel per sweep */

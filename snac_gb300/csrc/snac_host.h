@@ -95,7 +95,7 @@ struct PoissonSolver {
   double *d_lambda = nullptr;        // Helmholtz with a transform: lambda_k / dl^2 (the shift is lambda_k + alphai)
   std::vector<double> lambda;
   int precision = 0;
-  int inner_iters = 6;               // mixed path: FP32 Krylov iterations per refinement step
+  int inner_iters = 5;               // mixed path: FP32 Krylov iterations per refinement step
   int use_graph = 0;                 // mixed path: replay each refinement step's FP32 solve as a CUDA graph
   cudaGraphExec_t inner_exec = nullptr;
   long long inner_nodes = 0;         // kernel launches in that graph
@@ -104,8 +104,8 @@ struct PoissonSolver {
   static constexpr int SPEC_MAX = 8;
   int spec_outer = 0;
   int *d_ocount = nullptr, *h_ocount = nullptr;  // 2 * SPEC_MAX ints (device, pinned host)
-  double inner_tol = 1e-7;           // mixed path: relative tolerance of the FP32 solve
-  int refine_steps = 2;              // mixed path: FP32 refinement steps before the systems still above the
+  double inner_tol = 1e-6;           // mixed path: relative tolerance of the FP32 solve
+  int refine_steps = -1;             // mixed path: FP32 refinement steps before the systems still above the
                                      // tolerance finish with FP64 PCG (-1: FP32 refinement to convergence)
   bool adapt_inner = true;           // mixed path: each system's inner solve stops once its outer residual
                                      // would be within a tenth of the tolerance (never beyond inner_tol)

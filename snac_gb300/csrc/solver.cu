@@ -276,7 +276,7 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
   if (o.inner_iters > 0) S.inner_iters = o.inner_iters;
   if (o.inner_tol > 0.0) S.inner_tol = o.inner_tol;
   S.adapt_inner = o.inner_adapt >= 0;  // -1: every inner solve reduces by inner_tol, whatever the outer needs
-  if (o.refine_steps != 0) S.refine_steps = o.refine_steps;
+  if (o.refine_steps > 0) S.refine_steps = o.refine_steps;
   S.use_graph = d.opt.use_graph ? 1 : 0;
   S.tol = c.tol;
   S.maxiter = c.maxiter;
@@ -818,9 +818,9 @@ static int solve_box(PoissonSolver &S, cudaStream_t st, int *iters_out, double *
     if (S.refine_steps > 0 && outer >= S.refine_steps) {
       // Each FP32 refinement step gains about seven digits at best (the FP32 floor); after refine_steps of
       // them only a few systems are still above the tolerance -- typically the singular zero-wavenumber one,
-      // the worst conditioned, whose steps gain fewer.  Another FP32 step would cost a full inner solve's
-      // launches for them; FP64 PCG iterations from the current iterate, on those systems only, finish them
-      // (the same stopping test as the plain FP64 path).
+      // the worst conditioned, whose steps gain fewer.  Option: FP64 PCG iterations from the current iterate,
+      // on those systems only, finish them (the same stopping test as the plain FP64 path) instead of another
+      // FP32 step.  On the channel the FP32 step is the faster (its launches replay as a graph, these do not).
       CgWork Wf = S.W64;
       Wf.r = S.r64;
       Wf.active = S.active_outer;

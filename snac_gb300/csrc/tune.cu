@@ -224,7 +224,7 @@ int snac_autotune(int steps, snac_tune_result *out) {
   }
   if (rc == SNAC_OK && found && best_opt.precision == 1) {
     g.clear();
-    for (int r : {2, -1}) { snac_options o = best_opt; o.refine_steps = r; g.push_back(o); }
+    for (int r : {-1, 2}) { snac_options o = best_opt; o.refine_steps = r; g.push_back(o); }
     rc = try_group(g);
   }
   if (rc != SNAC_OK) return finish(opt0, rc);
