@@ -148,14 +148,84 @@ KERNEL_WORK = {
 USE_GRAPH = 1  # the mixed path replays its refinement steps as CUDA graphs (bench.py --no-graph: off)
 
 
-def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0, **solver):
-    """solver: snac_options fields passed to the domain (the library defaults when absent)."""
+def other_configs():
+    """The reference configurations other than the headline channel, at their stated sizes: (case, initial
+    state, description).  The L-shaped box is three 144 x 144 x 96 blocks (5.97 M cells, the configuration's
+    "~6M cells" in three blocks)."""
+    from snac_gb300 import cases
+    return {
+        "c1_ldc64": (lambda: cases.lid_driven_cavity(64), init_rest,
+                     "lid-driven cavity 64^3, Re=1000, CFL 0.5, 3-D multigrid, from rest"),
+        "c2_tgv128": (lambda: cases.taylor_green(128), init_tgv,
+                      "Taylor-Green vortex 128^3, Re=1600, FFT along z (128 systems of 128x128)"),
+        "c4_lbox": (lambda: cases.l_shaped_box(144, 96), init_rest,
+                    "L-shaped closed box, 3 blocks of 144x144x96, lid-driven, Re=2000, 3-D multigrid, from rest"),
+        "c5_dhc512": (lambda: cases.heated_cavity((512, 512, 256)), init_dhc,
+                      "heated cavity 512x512x256, stretched 1.5, Ra=1e8, Pr=0.71, IMPDIFF (u,v,w,T Helmholtz) + "
+                      "3-D pressure multigrid, T noise 1e-3"),
+    }
+
+
+def bench_configs(names, steps, warmup, device):
+    """ms per RK3 step, Mcells/s and max|div u| of the plain FP64 and the mixed path on each configuration."""
+    out = {}
+    cfgs = other_configs()
+    for name in names:
+        case_fn, init, desc = cfgs[name]
+        row = {"workload": desc, "cells": case_fn().ncell}
+        for label, prec in (("mixed", 1), ("plain_fp64", 0)):
+            r = run_gpu_path(case_fn, prec, steps, warmup, device, init=init)
+            row[label] = {"ms_per_step": r["ms"], "mcells_per_s": r["ncell"] / (r["ms"] * 1e-3) / 1e6,
+                          "max_div_u": r["divmax"], "solve_iters_max": r["iters"],
+                          "solve_residual_max": r["residual"], "helm_iters_max": r["helm_iters"],
+                          "setup_s": r["setup_s"], "rc": r["rc"]}
+        row["speedup_mixed_vs_plain"] = row["plain_fp64"]["ms_per_step"] / row["mixed"]["ms_per_step"]
+        out[name] = row
+    return out
+
+
+def init_rest(dom, case):
+    """Zero velocity and pressure (the lid-driven cavities); only the boundary conditions."""
+    from snac_gb300 import capi
+    dom.bounduvw(False)
+    dom.boundp(capi.P)
+
+
+def init_tgv(dom, case):
+    """Taylor-Green vortex with its analytic pressure."""
+    from snac_gb300 import capi, cases
+    for ib, (u, v, w, p) in cases.tgv_initial_condition(case, dom.grid).items():
+        for k, f in ((capi.U, u), (capi.V, v), (capi.W, w), (capi.P, p)):
+            dom.set(ib, k, f)
+    dom.bounduvw(False)
+    dom.boundp(capi.P)
+
+
+def init_dhc(dom, case):
+    """Heated cavity: zero velocity, T = seeded uniform noise of amplitude 1e-3 (splitmix64, seed 0x5EED)."""
+    from snac_gb300 import capi, cases
+    for ib, b in enumerate(case.blocks):
+        n = [int(x) for x in b.ng]
+        t = np.zeros([x + 2 for x in n], order="F")
+        r = cases.splitmix64_uniform_fast(0x5EED, n[0] * n[1] * n[2]).reshape(n, order="F")
+        t[1:-1, 1:-1, 1:-1] = 2e-3 * (r - 0.5)
+        dom.set(ib, capi.S0, t)
+    dom.bounduvw(False)
+    dom.boundp(capi.P)
+    dom.boundp(capi.S0)
+
+
+def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0, init=None, **solver):
+    """solver: snac_options fields passed to the domain (the library defaults when absent); init(dom, case)
+    sets the initial state (default: the channel's)."""
     from snac_gb300 import capi
     from snac_gb300.domain import Domain
     case = case_fn()
+    t0 = time.perf_counter()
     dom = Domain(case, precision=precision, device=device, use_graph=USE_GRAPH if precision else 0, **solver)
+    setup_s = time.perf_counter() - t0
     try:
-        init_channel(dom, case)
+        (init or init_channel)(dom, case)
         dom.step(warmup, allow_not_converged=True)
         L = capi.lib()
         if profile_kid:
@@ -177,7 +247,8 @@ def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0, **sol
         divtot, divmax = dom.chkdiv()
         ke = dom.kinetic_energy()
         return dict(ms=st["device_ms"] / steps, iters=st["iters"], residual=st["residual"], divmax=divmax, ke=ke,
-                    rc=rc, prof=prof, ncell=case.ncell, dt=st["dt"], launches=n1.value - n0.value)
+                    rc=rc, prof=prof, ncell=case.ncell, dt=st["dt"], launches=n1.value - n0.value,
+                    helm_iters=st["helm_iters"], helm_residual=st["helm_residual"], setup_s=setup_s)
     finally:
         dom.close()
 
@@ -317,6 +388,9 @@ def main():
                     help="channel: the benchmark workload; small: the same layout at test size")
     ap.add_argument("--no-graph", action="store_true", help="launch the refinement steps one kernel at a time")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess path (record, train, time)")
+    ap.add_argument("--configs", default="c1_ldc64,c2_tgv128,c4_lbox,c5_dhc512",
+                    help="other reference configurations timed beside the headline (comma list; empty: none)")
+    ap.add_argument("--config-steps", type=int, default=3, help="timed steps per configuration and path")
     ap.add_argument("--only", choices=["mixed", "plain", "learned"], default=None,
                     help="run one path once and print its timing only (used for ncu launch lists; learned: "
                          "1 recorded step and 20 training iterations)")
@@ -429,6 +503,8 @@ def main():
                 "levels": {str(k): {"launch_ms": v[0], "achieved_gbs": v[1] / (v[0] * 1e-3) / 1e9}
                            for k, v in smoother.items()}}
         roof["frac"] = roof["achieved"] / roof["peak"]
+    configs = bench_configs([c for c in args.configs.split(",") if c], args.config_steps, 2, device) \
+        if args.configs else None
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         r = cpu_reference(case_fn, args.steps, args.warmup, budget_s=30.0)
@@ -452,7 +528,7 @@ def main():
             "gpu_launches": mixed["launches"], "gpu_launches_per_step": mixed["launches"] / args.steps,
             "kernels": shares,
             "peaks_measured_here": {"fp64_gflops": f64.value, "fp32_gflops": f32.value},
-            "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
+            "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "configs": configs}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
