@@ -160,9 +160,10 @@ def other_configs():
                       "Taylor-Green vortex 128^3, Re=1600, FFT along z (128 systems of 128x128)"),
         "c4_lbox": (lambda: cases.l_shaped_box(144, 96), init_rest,
                     "L-shaped closed box, 3 blocks of 144x144x96, lid-driven, Re=2000, 3-D multigrid, from rest"),
-        "c5_dhc512": (lambda: cases.heated_cavity((512, 512, 256)), init_dhc,
+        "c5_dhc512": (lambda: cases.heated_cavity((512, 512, 256), dt_f=1e-3), init_dhc,
                       "heated cavity 512x512x256, stretched 1.5, Ra=1e8, Pr=0.71, IMPDIFF (u,v,w,T Helmholtz) + "
-                      "3-D pressure multigrid, T noise 1e-3"),
+                      "3-D pressure multigrid, T noise 1e-3, fixed dt 1e-3 (dt_f of the reference's heated-cavity "
+                      "test: from rest the CFL limit is unbounded and IMPDIFF has no viscous one)"),
     }
 
 

@@ -57,7 +57,9 @@ int mg_partial_stride(const MgProblem &P) {
 
 // ---------------------------------------------------------------- smoothing / transfer
 // one red-black half-sweep: the cells with (i + j + k) % 2 == color
-template <typename T>
+// SEP (3-D mode, FP32): couplings and diagonal from the 1-D factors (offdiag_sep / diag_sep), which leaves the
+// V-cycle reading x, b, cc and the cell codes instead of five per-cell coefficient arrays
+template <typename T, bool SEP>
 __global__ void __launch_bounds__(256) k_rbgs(MgLevelD L, MgGeom G, const T *shift, const int *active, int color,
                                               T *x, const T *b) {
   int k, s;
@@ -67,16 +69,23 @@ __global__ void __launch_bounds__(256) k_rbgs(MgLevelD L, MgGeom G, const T *shi
   const int i = 2 * (int)(blockIdx.x * 32 + threadIdx.x) + ((color + j + k) & 1);
   if (i >= L.n[0] || j >= L.n[1]) return;
   const int c = i + L.n[0] * (j + L.n[1] * k);
-  if (L.code[c] & 0x8000) return;
+  const unsigned cd = L.code[c];
+  if (cd & 0x8000) return;
   const long off = L.ncell * s;
   T *__restrict__ xs = x + off;
-  const T d = diag_of<T>(L, G, shift[s], c);
-  const T acc = offdiag<T>(L, G, [&](int e) { return xs[e]; }, c, i, j, k);
+  T d, acc;
+  if constexpr (SEP) {
+    d = diag_sep(L, shift[s], c, i, j, k);
+    acc = offdiag_sep(L, G, [&](int e) { return xs[e]; }, c, i, j, k, cd);
+  } else {
+    d = diag_of<T>(L, G, shift[s], c);
+    acc = offdiag<T>(L, G, [&](int e) { return xs[e]; }, c, i, j, k);
+  }
   xs[c] = (b[off + c] - acc) * rcpt(d);
 }
 
 // coarse b <- sum over children of (b - A x) on the fine level; coarse x <- 0
-template <typename T>
+template <typename T, bool SEP>
 __global__ void __launch_bounds__(256) k_resid_restrict(MgLevelD F, MgLevelD C, MgGeom G, const T *shift,
                                                         const int *active, const T *xf, const T *bf, T *bc, T *xc) {
   int K, s;
@@ -96,9 +105,15 @@ __global__ void __launch_bounds__(256) k_resid_restrict(MgLevelD F, MgLevelD C, 
         const int i = C.coarsened[0] ? 2 * I + di : I, j = C.coarsened[1] ? 2 * J + dj : J,
                   k = C.coarsened[2] ? 2 * K + dk : K;
         const int c = i + F.n[0] * (j + F.n[1] * k);
-        if (F.code[c] & 0x8000) continue;
-        const T acc = offdiag<T>(F, G, [&](int e) { return xs[e]; }, c, i, j, k);
-        sum += bf[offf + c] - fmat(diag_of<T>(F, G, sh, c), xs[c], acc);
+        const unsigned cd = F.code[c];
+        if (cd & 0x8000) continue;
+        if constexpr (SEP) {
+          const T acc = offdiag_sep(F, G, [&](int e) { return xs[e]; }, c, i, j, k, cd);
+          sum += bf[offf + c] - fmat(diag_sep(F, sh, c, i, j, k), xs[c], acc);
+        } else {
+          const T acc = offdiag<T>(F, G, [&](int e) { return xs[e]; }, c, i, j, k);
+          sum += bf[offf + c] - fmat(diag_of<T>(F, G, sh, c), xs[c], acc);
+        }
       }
   bc[offc + cc] = sum;
   xc[offc + cc] = 0;
@@ -146,6 +161,21 @@ __global__ void k_zero(long n, T *x, int nsys, const int *active) {
   if (c < n) x[n * s + c] = 0;
 }
 
+// the factored-coupling kernels serve the FP32 V-cycles and Krylov iterations of the 3-D mode
+template <typename T>
+inline bool sep_ok(const MgProblem &P) { return sizeof(T) == 4 && P.mode3d && P.sep; }
+
+template <typename T>
+int launch_rbgs3(const MgProblem &P, const MgLevelD &L, const MgGeom &G, const T *shift, const int *active, int color,
+                 T *x, const T *b, cudaStream_t st) {
+  prof_begin(KID_RBGS, st);
+  if (sep_ok<T>(P)) k_rbgs<T, true><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, color, x, b), ::snac::count_launch();
+  else k_rbgs<T, false><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, color, x, b), ::snac::count_launch();
+  prof_end(KID_RBGS, st);
+  SNAC_CUDA(cudaGetLastError());
+  return SNAC_OK;
+}
+
 // V-cycle on level l: x_l <- M b_l (zero initial guess); x and b of each level are the level's own arrays.
 // At level 0 the last smoothing pass may also produce the partials of b.x (= r.z) into part_bx, and for the
 // singular systems those of x and of b into part_x and part_b.
@@ -169,7 +199,7 @@ int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, c
       k_zero<T><<<g, 256, 0, st>>>(L.ncell, x, P.nsys, active), ::snac::count_launch();
       for (int it = 0; it < 40; it++)
         for (int col : {0, 1, 1, 0}) {
-          if (P.mode3d) k_rbgs<T><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, col, x, b), ::snac::count_launch();
+          if (P.mode3d) SNAC_TRY(launch_rbgs3<T>(P, L, G, shift, active, col, x, b, st));
           else SNAC_TRY(plane_sweep<T>(P, l, shift, active, col, x, b, st));
         }
     }
@@ -199,20 +229,19 @@ int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, c
     return SNAC_OK;
   }
   for (int it = 0; it < 2 * mg_nu(P, l); it++) {
-    prof_begin(KID_RBGS, st);
-    k_rbgs<T><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, it & 1, x, b), ::snac::count_launch();
-    prof_end(KID_RBGS, st);
+    SNAC_TRY(launch_rbgs3<T>(P, L, G, shift, active, it & 1, x, b, st));
   }
   prof_begin(KID_RESTRICT, st);
-  k_resid_restrict<T><<<grid_cell(P, C), BLK, 0, st>>>(L, C, G, shift, active, x, b, LA<T>::b(C), LA<T>::x(C)), ::snac::count_launch();
+  if (sep_ok<T>(P))
+    k_resid_restrict<T, true><<<grid_cell(P, C), BLK, 0, st>>>(L, C, G, shift, active, x, b, LA<T>::b(C), LA<T>::x(C)), ::snac::count_launch();
+  else
+    k_resid_restrict<T, false><<<grid_cell(P, C), BLK, 0, st>>>(L, C, G, shift, active, x, b, LA<T>::b(C), LA<T>::x(C)), ::snac::count_launch();
   prof_end(KID_RESTRICT, st);
   SNAC_CUDA(cudaGetLastError());
   SNAC_TRY(mg_vcycle_impl<T>(P, G, l + 1, shift, active, nullptr, nullptr, nullptr, 0, nullptr, st));
   k_prolong<T><<<grid_cell(P, L), BLK, 0, st>>>(L, C, G, active, x, LA<T>::x(C)), ::snac::count_launch();
   for (int it = 0; it < 2 * mg_nu(P, l); it++) {
-    prof_begin(KID_RBGS, st);
-    k_rbgs<T><<<grid_rb(P, L), BLK, 0, st>>>(L, G, shift, active, 1 - (it & 1), x, b), ::snac::count_launch();
-    prof_end(KID_RBGS, st);
+    SNAC_TRY(launch_rbgs3<T>(P, L, G, shift, active, 1 - (it & 1), x, b, st));
   }
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -364,7 +393,7 @@ __global__ void __launch_bounds__(256) k_cg_p(long n, const int *active, const S
 
 // q = A p; partials of p.q.  FUSEP: the new direction p = (z - zmean) + beta p_old is formed on the fly (at
 // the centre and at the neighbours) and written to pn, so p_old and pn must be different arrays.
-template <typename T, bool FUSEP>
+template <typename T, bool FUSEP, bool SEP = false>
 __global__ void __launch_bounds__(256) k_cg_apply(MgLevelD L, MgGeom G, const T *shift, const int *active,
                                                   const SysScal *sc, const T *z, const T *po, T *pn, T *q,
                                                   double *part, int stride) {
@@ -386,9 +415,15 @@ __global__ void __launch_bounds__(256) k_cg_apply(MgLevelD L, MgGeom G, const T 
     const T pc = pv(c);
     if (FUSEP) pn[off + c] = pc;
     T y = 0;
-    if (!(L.code[c] & 0x8000)) {
-      const T acc = offdiag<T>(L, G, pv, c, i, j, k);
-      y = fmat(diag_of<T>(L, G, sh, c), pc, acc);
+    const unsigned cd = L.code[c];
+    if (!(cd & 0x8000)) {
+      if constexpr (SEP) {
+        const T acc = offdiag_sep(L, G, pv, c, i, j, k, cd);
+        y = fmat(diag_sep(L, sh, c, i, j, k), pc, acc);
+      } else {
+        const T acc = offdiag<T>(L, G, pv, c, i, j, k);
+        y = fmat(diag_of<T>(L, G, sh, c), pc, acc);
+      }
     }
     q[off + c] = y;
     pq = fmat(pc, y, pq);
@@ -558,8 +593,8 @@ __global__ void k_set_active(int nsys, int *active, const int *src) {
 // Explicit instantiation of every kernel template for both precisions, so that the
 // device code of each kernel exists whatever host template reaches its launch.
 #define SNAC_MG_KERNELS(T)                                                                                           \
-  template __global__ void k_rbgs<T>(MgLevelD, MgGeom, const T *, const int *, int, T *, const T *);                 \
-  template __global__ void k_resid_restrict<T>(MgLevelD, MgLevelD, MgGeom, const T *, const int *, const T *,        \
+  template __global__ void k_rbgs<T, false>(MgLevelD, MgGeom, const T *, const int *, int, T *, const T *);          \
+  template __global__ void k_resid_restrict<T, false>(MgLevelD, MgLevelD, MgGeom, const T *, const int *, const T *, \
                                                const T *, T *, T *);                                                 \
   template __global__ void k_prolong<T>(MgLevelD, MgLevelD, MgGeom, const int *, T *, const T *);                    \
   template __global__ void k_dense<T>(MgLevelD, const int *, T *, const T *);                                        \
@@ -581,6 +616,11 @@ __global__ void k_set_active(int nsys, int *active, const int *src) {
 SNAC_MG_KERNELS(double)
 SNAC_MG_KERNELS(float)
 #undef SNAC_MG_KERNELS
+template __global__ void k_rbgs<float, true>(MgLevelD, MgGeom, const float *, const int *, int, float *, const float *);
+template __global__ void k_resid_restrict<float, true>(MgLevelD, MgLevelD, MgGeom, const float *, const int *,
+                                                       const float *, const float *, float *, float *);
+template __global__ void k_cg_apply<float, true, true>(MgLevelD, MgGeom, const float *, const int *, const SysScal *,
+                                                       const float *, const float *, float *, float *, double *, int);
 
 // ---------------------------------------------------------------- host drivers
 namespace {
@@ -689,7 +729,10 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
                                        W.stride), ::snac::count_launch();
     prof_begin(KID_CG_APPLY, st);
     if constexpr (fusep) {
-      if (P.mode3d)
+      if (P.mode3d && sep_ok<T>(P))
+        k_cg_apply<T, true, true><<<grid_red(P, L0), BLK, 0, st>>>(L0, G, shift, W.active, W.sc, z, p, pn, q,
+                                                                   W.part1, W.stride), ::snac::count_launch();
+      else if (P.mode3d)
         k_cg_apply<T, true><<<grid_red(P, L0), BLK, 0, st>>>(L0, G, shift, W.active, W.sc, z, p, pn, q, W.part1,
                                                              W.stride), ::snac::count_launch();
       else

@@ -88,6 +88,40 @@ __device__ __forceinline__ T offdiag(const MgLevelD &L, const MgGeom &G, V v, in
   return acc;
 }
 
+// 3-D mode with factored couplings (MgProblem::sep): the couplings of cell c = (i, j, k) formed from the 1-D
+// face factors caf[a] and the widths Wf, in the order of offdiag (+x, -x, +y, -y, +z, -z); a folded face (its
+// code bits non-zero) contributes nothing, an unfolded face always has its neighbour (periodic wrap included).
+// FP32 only: the products round differently from the stored FP32 couplings, which is immaterial for the
+// preconditioner they serve (a coupling is the same value seen from either cell, so it stays symmetric).
+template <typename V>
+__device__ __forceinline__ float offdiag_sep(const MgLevelD &L, const MgGeom &G, V v, int c, int i, int j, int k,
+                                             unsigned cd) {
+  const int n0 = L.n[0], n1 = L.n[1], n2 = L.n[2], st = n0 * n1;
+  const float w0 = L.Wf[0][i], w1 = L.Wf[1][j], w2 = L.Wf[2][k];
+  float acc = 0.f;
+  if (!(G.periodic[0] && n0 == 1)) {
+    const float wt = w1 * w2;
+    if (!((cd >> 2) & 3)) acc = fmat(L.caf[0][i] * wt, v(i + 1 < n0 ? c + 1 : c + 1 - n0), acc);
+    if (!(cd & 3)) acc = fmat(L.caf[0][i > 0 ? i - 1 : n0 - 1] * wt, v(i > 0 ? c - 1 : c + n0 - 1), acc);
+  }
+  if (!(G.periodic[1] && n1 == 1)) {
+    const float wt = w0 * w2;
+    if (!((cd >> 6) & 3)) acc = fmat(L.caf[1][j] * wt, v(j + 1 < n1 ? c + n0 : c + n0 - st), acc);
+    if (!((cd >> 4) & 3)) acc = fmat(L.caf[1][j > 0 ? j - 1 : n1 - 1] * wt, v(j > 0 ? c - n0 : c + st - n0), acc);
+  }
+  if (!(G.periodic[2] && n2 == 1)) {
+    const float wt = w0 * w1;
+    if (!((cd >> 10) & 3)) acc = fmat(L.caf[2][k] * wt, v(k + 1 < n2 ? c + st : c + st - st * n2), acc);
+    if (!((cd >> 8) & 3)) acc = fmat(L.caf[2][k > 0 ? k - 1 : n2 - 1] * wt, v(k > 0 ? c - st : c + st * (n2 - 1)), acc);
+  }
+  return acc;
+}
+// the diagonal with factored couplings: cc, plus the shift times the cell volume W0 W1 W2 when there is one
+__device__ __forceinline__ float diag_sep(const MgLevelD &L, float sh, int c, int i, int j, int k) {
+  const float cc = L.ccf[c];
+  return sh == 0.f ? cc : fmat(sh, L.Wf[0][i] * L.Wf[1][j] * L.Wf[2][k], cc);
+}
+
 // One cell of the plane operator: neighbour indices and couplings in the order +x, -x, +y, -y.  A
 // neighbour that does not exist gets index c and coupling 0, which leaves the FMA chain unchanged.
 template <typename T>

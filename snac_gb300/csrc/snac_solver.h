@@ -33,6 +33,9 @@ struct MgLevelD {
   const float *dinvf;
   const double *invd;                // plane mode: 1 / diagonal per system and cell (0 for inactive cells)
   const float *invdf;
+  // 3-D mode, FP32 V-cycles (MgProblem::sep): the couplings are products of 1-D factors, cp[a] of an unfolded
+  // face between cells q and q+1 along a = caf[a][q] * Wf[b][q_b] * Wf[c][q_c] (b, c the other axes)
+  const float *caf[3];
 };
 
 struct MgProblem {
@@ -57,6 +60,8 @@ struct MgProblem {
   const int *sing_list;              // device: indices of the singular systems (nsing of them)
   int nsing;
   long nact0;                        // active cells of one system on level 0
+  int sep;                           // 3-D mode: every level's couplings factor into 1-D tables (caf), which the
+                                     // FP32 V-cycle and Krylov kernels use instead of the per-cell arrays
 };
 // smoothing sweeps per side of the V-cycle on level l
 __host__ __device__ inline int mg_nu(const MgProblem &P, int l) { return l >= P.lnu ? P.nu_coarse : P.nu; }

@@ -574,10 +574,40 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
     std::vector<float> f(v.begin(), v.end());
     return (float *)up(f.data(), f.size() * sizeof(float));
   };
+  // 3-D mode: factor every level's couplings into 1-D face tables, cp[a](c) = Ca[a][q_a] * W_b * W_c over the
+  // unfolded faces (a tensor-product grid with per-axis spacings makes them so); checked face by face, else
+  // the FP32 kernels keep reading the per-cell couplings
+  std::vector<std::vector<double>> fac[MG_MAXLEV][3];
+  P.sep = S.mode3d ? 1 : 0;
+  for (int l = 0; l < (int)B.L.size() && P.sep; l++) {
+    const HLevel &h = B.L[l];
+    for (int a = 0; a < 3; a++) {
+      fac[l][a].assign(1, std::vector<double>(h.n[a], 0.0));
+      std::vector<double> &F = fac[l][a][0];
+      for (int k = 0; k < h.n[2] && P.sep; k++)
+        for (int j = 0; j < h.n[1] && P.sep; j++)
+          for (int i = 0; i < h.n[0]; i++) {
+            const long c = i + (long)h.n[0] * (j + (long)h.n[1] * k);
+            if (h.code[c] & 0x8000) continue;
+            if ((h.code[c] >> (2 * (2 * a + 1))) & 3) continue;  // folded +a face
+            const double cpv = h.cp[a][c];
+            if (cpv == 0.0) continue;  // one-cell periodic axis
+            const int idx[3] = {i, j, k};
+            double wt = 1.0;
+            for (int b = 0; b < 3; b++)
+              if (b != a) wt *= h.W[b][idx[b]];
+            const double v = cpv / wt;
+            double &f = F[idx[a]];
+            if (f == 0.0) f = v;
+            else if (std::fabs(f - v) > 1e-12 * std::fabs(v)) { P.sep = 0; break; }
+          }
+    }
+  }
   for (int l = 0; l < P.nlev; l++) {
     const HLevel &h = B.L[l];
     MgLevelD &D = P.L[l];
     for (int a = 0; a < 3; a++) { D.n[a] = h.n[a]; D.coarsened[a] = h.coarsened[a]; }
+    for (int a = 0; a < 3; a++) D.caf[a] = P.sep ? upf(fac[l][a][0]) : nullptr;
     D.ncell = h.ncell;
     D.code = (const unsigned short *)up(h.code.data(), h.code.size() * sizeof(unsigned short));
     D.cc = (const double *)up(h.cc.data(), h.cc.size() * sizeof(double));
