@@ -280,6 +280,14 @@ int snac_boundp_all(int field);
  * (skipped when is_correc), the tangential ones mirrored about the face value */
 int snac_inflow_all(int is_correc);                   /* bound.f90:68-106 (SNAC_P, SNAC_PP, scalars) */
 int snac_fillps_all(double dtrk);                 /* fillps.f90 */
+/* solve_impdiff_field (solve_helmholtz.f90:32-138, called at main.f90:919-934 and 961-978) of one field of every
+ * block: field SNAC_U, SNAC_V, SNAC_W or SNAC_S0 + s is replaced by the solution of the IMPDIFF Helmholtz problem
+ * (A + alphai_new V) phi = alphai_new V phi + BC planes, warm-started from the previous solution of that field's
+ * solver, with the transform along FFT_AXIS when there is one.  alphai_old is accepted for the reference's
+ * argument list: the shift of each solve is set from alphai_new alone (the reference adds alphai_new -
+ * alphai_old to the matrix it keeps).  Needs a domain set up with IMPDIFF; SNAC_ERR_NOT_CONVERGED as for
+ * the pressure solve. */
+int snac_impdiff_solve(int field, double alphai_new, double alphai_old);
 int snac_updt_rhs_all(void);                      /* bound.f90:543-585 with the pressure BC planes */
 int snac_solve_pressure(void);                    /* fft + solve_n_helmholtz_2d + fft + normfft, or solve_helmholtz */
 int snac_correc_all(double dtrk);                 /* correc.f90 */
@@ -311,6 +319,11 @@ int snac_out3d_write(const char *fname, int ib, int field);
  * 16 channels x H x W (x rounded to BF16, zero padding, act = ReLU when relu != 0), weights w[16][16][3][3]. */
 int snac_cnn_conv3x3(const float *x, int nplanes, int H, int W, const float *w, const float *bias, int relu,
                      float *y);
+/* No counterpart in the reference: a testing hook for the convolution's bounded wait on its tensor-core
+ * accumulator.  The launches that follow poll the accumulator's mbarrier at most `polls` times (negative:
+ * the default, 2^24); a wait that runs out makes the call return SNAC_ERR_TIMEOUT after the kernel has let the
+ * MMAs in flight finish (with the full bound) and freed its tensor memory, so the context stays usable. */
+int snac_cnn_set_poll_limit(long polls);
 
 /* No counterpart in the reference: forward and backward of the learned-guess network (three 3x3 layers of
  * 16 channels, ReLU between them) on host data, for checking its gradients: x nb x 16 x H x W, target

@@ -695,6 +695,16 @@ void or_boundp(or_domain *d, int kind) {
   }
 }
 
+static int helm_solve(or_domain *d, int hf, int kind, double alphai);
+
+/* solve_impdiff_field (solve_helmholtz.f90:32-138) of one field of every block: field 0..2 = u, v, w,
+ * 3 + s = scalar s; returns non-zero when the solve did not reach the tolerance */
+int or_impdiff_solve(or_domain *d, int field, double alphai) {
+  if (!d->c.impdiff) return -1;
+  if (field < 3) return helm_solve(d, OR_HF_U + field, OR_U + field, alphai);
+  return helm_solve(d, OR_HF_S0 + field - 3, OR_S0 + field - 3, alphai);
+}
+
 void or_fillps_all(or_domain *d, double dtrk) {
   for (int ib = 0; ib < d->nblocks; ib++) {
     or_block *B = &d->b[ib];

@@ -76,6 +76,7 @@ def lib():
         for n in ("or_bounduvw", "or_boundp", "or_inflow"):
             getattr(L, n).argtypes = [C.c_void_p, C.c_int]
         L.or_fillps_all.argtypes = [C.c_void_p, C.c_double]
+        L.or_impdiff_solve.argtypes = [C.c_void_p, C.c_int, C.c_double]
         L.or_updt_rhs_all.argtypes = [C.c_void_p]
         L.or_solve_pressure.argtypes = [C.c_void_p]
         L.or_correc_all.argtypes = [C.c_void_p, C.c_double]

@@ -155,6 +155,7 @@ void   or_time_istep(const or_domain *d, double *time, int *istep);
 int    or_out1d(or_domain *d, int ib, int kind, int idir, double *coord, double *prof, const char *fname);
 void   or_fortran_e15_7(double v, char *out);  /* Fortran Ew.d, w = 15, d = 7 */
 void   or_fillps_all(or_domain *d, double dtrk);
+int    or_impdiff_solve(or_domain *d, int field, double alphai);
 void   or_updt_rhs_all(or_domain *d);
 int    or_solve_pressure(or_domain *d);                   /* pp <- solution, po updated */
 void   or_correc_all(or_domain *d, double dtrk);

@@ -117,6 +117,7 @@ PROTOTYPES = {
     "snac_boundp_all": (C.c_int, [C.c_int]),
     "snac_inflow_all": (C.c_int, [C.c_int]),
     "snac_fillps_all": (C.c_int, [C.c_double]),
+    "snac_impdiff_solve": (C.c_int, [C.c_int, C.c_double, C.c_double]),
     "snac_updt_rhs_all": (C.c_int, []),
     "snac_solve_pressure": (C.c_int, []),
     "snac_correc_all": (C.c_int, [C.c_double]),
@@ -131,6 +132,7 @@ PROTOTYPES = {
     "snac_checkpoint_load": (C.c_int, [C.c_char_p]),
     "snac_out1d": (C.c_int, [C.c_int, C.c_int, C.c_int, DP, DP]),
     "snac_cnn_conv3x3": (C.c_int, [FP, C.c_int, C.c_int, C.c_int, FP, FP, C.c_int, FP]),
+    "snac_cnn_set_poll_limit": (C.c_int, [C.c_long]),
     "snac_guess_grad": (C.c_int, [FP, FP, C.c_int, C.c_int, C.c_int, FP, FP, DP]),
     "snac_guess_mode": (C.c_int, [C.c_int]),
     "snac_guess_train": (C.c_int, [C.c_int, C.c_double, DP, DP, IP]),

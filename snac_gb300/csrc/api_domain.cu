@@ -1080,6 +1080,20 @@ int snac_boundp_all(int field) {
   SNAC_CUDA(cudaStreamSynchronize(d->st));
   return SNAC_OK;
 }
+int snac_impdiff_solve(int field, double alphai_new, double alphai_old) {
+  NEED_DOMAIN
+  (void)alphai_old;  // the shift of this solve is set whole from alphai_new (the reference adds the difference)
+  if (!d->c.impdiff) { set_error("snac_impdiff_solve: the domain was set up without IMPDIFF"); return SNAC_ERR_STATE; }
+  int hf;
+  if (field >= SNAC_U && field <= SNAC_W) hf = HF_U + (field - SNAC_U);
+  else if (field >= SNAC_S0 && field < SNAC_S0 + d->c.nscal) hf = HF_S0 + (field - SNAC_S0);
+  else { set_error("snac_impdiff_solve: field must be SNAC_U, SNAC_V, SNAC_W or a scalar"); return SNAC_ERR_ARG; }
+  if (!d->hs[hf]) { set_error("snac_impdiff_solve: no Helmholtz solver for field %d", field); return SNAC_ERR_STATE; }
+  const int rc = solver_solve_helmholtz(*d, *d->hs[hf], alphai_new);
+  SNAC_CUDA(cudaStreamSynchronize(d->st));
+  return rc;
+}
+
 int snac_fillps_all(double dtrk) {
   NEED_DOMAIN
   SNAC_TRY(launch_fillps(d->d_db, d->d_tiles, d->ntiles, dtrk, d->c.fft_axis, d->st));

@@ -55,9 +55,11 @@ __device__ __forceinline__ int core_off(int r, int k) { return (((r >> 3) * 2 + 
 // [p][co][h][w]) for the first ny output channels (none when y is null) and yb BF16 (act_idx) of all 16
 constexpr int CNN_ROW = (CNN_M + 2) * 16;  // bytes of one staged half-row (130 pixel records)
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+constexpr long MBAR_POLLS = 1L << 24;  // polls of an mbarrier wait before it gives up
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, long limit) {
   uint32_t done = 0;
-  for (long it = 0; it < (1L << 24) && !done; it++) {
+  for (long it = 0; it < limit && !done; it++) {
     asm volatile(
         "{\n .reg .pred pw;\n mbarrier.try_wait.parity.shared::cta.b64 pw, [%1], %2;\n selp.u32 %0, 1, 0, pw;\n}\n"
         : "=r"(done)
@@ -69,7 +71,8 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
 __global__ void __launch_bounds__(CNN_M) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ x, int np, int H, int W,
                                                       const float *__restrict__ wts, const float *__restrict__ bias,
                                                       int relu, float *__restrict__ y, int ny,
-                                                      __nv_bfloat16 *__restrict__ yb, int *__restrict__ err) {
+                                                      __nv_bfloat16 *__restrict__ yb, int *__restrict__ err,
+                                                      long poll_limit) {
   __shared__ __align__(128) unsigned char sa[3 * 2 * CNN_ROW];               // 12.2 KB: rows h-1..h+1, halves
   __shared__ __align__(128) unsigned char sb[CNN_TAPS * CNN_C * CNN_C * 2];  // 4.5 KB of B blocks
   __shared__ float sbias[CNN_C];
@@ -134,7 +137,7 @@ __global__ void __launch_bounds__(CNN_M) k_conv3x3_tc(const __nv_bfloat16 *__res
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar));
     }
-    const bool got = mbar_wait_bounded(bar, phase);
+    const bool got = mbar_wait_bounded(bar, phase, poll_limit);
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (!__syncthreads_and(got ? 1 : 0)) {  // the accumulator did not arrive in time
       if (t == 0) atomicExch(err, 1);
@@ -176,11 +179,15 @@ __global__ void __launch_bounds__(CNN_M) k_conv3x3_tc(const __nv_bfloat16 *__res
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();  // every thread has finished with the staged rows and the accumulator
   }
-  if (failed) mbar_wait_bounded(bar, phase);  // let the MMAs in flight finish (bounded) before freeing TMEM
+  // let the MMAs in flight finish before freeing TMEM: always the full bound, whatever the main wait's limit
+  if (failed) mbar_wait_bounded(bar, phase, MBAR_POLLS);
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(dtmem), "r"(TMEM_COLS));
 }
+
+// polls of the accumulator wait in the launches that follow (snac_cnn_set_poll_limit; testing only)
+static long g_poll_limit = MBAR_POLLS;
 
 int launch_conv3x3_tc(const __nv_bfloat16 *x, int nplanes, int H, int W, const float *wts, const float *bias, int relu,
                       float *y, int ny, __nv_bfloat16 *yb, int *err, cudaStream_t st) {
@@ -189,7 +196,8 @@ int launch_conv3x3_tc(const __nv_bfloat16 *x, int nplanes, int H, int W, const f
   SNAC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   const long total = (long)nplanes * H * ((W + CNN_M - 1) / CNN_M);
   const int grid = (int)std::min<long>(total, (long)nsm * 8);  // persistent CTAs, 8 per SM
-  k_conv3x3_tc<<<grid, CNN_M, 0, st>>>(x, nplanes, H, W, wts, bias, relu, y, ny, yb, err), ::snac::count_launch();
+  k_conv3x3_tc<<<grid, CNN_M, 0, st>>>(x, nplanes, H, W, wts, bias, relu, y, ny, yb, err, g_poll_limit),
+      ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -236,4 +244,9 @@ int snac_cnn_conv3x3(const float *x, int nplanes, int H, int W, const float *wts
   }
   cudaFree(dx); cudaFree(dw); cudaFree(db); cudaFree(dy); cudaFree(derr);
   return rc;
+}
+
+int snac_cnn_set_poll_limit(long polls) {
+  snac::g_poll_limit = polls < 0 ? snac::MBAR_POLLS : polls;
+  return SNAC_OK;
 }

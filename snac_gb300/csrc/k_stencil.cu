@@ -460,16 +460,29 @@ int launch_bulk_partial(const DBlock *dB, const Tile *dT, int ntiles, int sidx, 
   return SNAC_OK;
 }
 
-__global__ void k_reduce_final(const double *part, int n, double *out) {
-  // single warp, fixed order: lane l sums tiles l, l+32, ... then a fixed shuffle tree
-  const int l = threadIdx.x;
+constexpr int RED_THREADS = 1024;
+// one CTA, fixed order: thread t sums tiles t, t + 1024, ... in turn, each warp combines its lanes by a fixed
+// shuffle tree, then warp 0 combines the 32 warp results the same way (deterministic, two levels)
+__global__ void __launch_bounds__(RED_THREADS) k_reduce_final(const double *part, int n, double *out) {
+  __shared__ double ws[RED_THREADS / 32], wm[RED_THREADS / 32];
+  const int t = threadIdx.x, l = t & 31, w = t >> 5;
   double s = 0.0, m = 0.0;
-  for (int q = l; q < n; q += 32) { s += part[2 * q]; m = fmax(m, part[2 * q + 1]); }
+  for (int q = t; q < n; q += RED_THREADS) { s += part[2 * q]; m = fmax(m, part[2 * q + 1]); }
   for (int o = 16; o > 0; o >>= 1) {
     s += __shfl_down_sync(0xffffffffu, s, o);
     m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
   }
-  if (l == 0) { out[0] = s; out[1] = m; }
+  if (l == 0) { ws[w] = s; wm[w] = m; }
+  __syncthreads();
+  if (w == 0) {
+    s = ws[l];
+    m = wm[l];
+    for (int o = 16; o > 0; o >>= 1) {
+      s += __shfl_down_sync(0xffffffffu, s, o);
+      m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    }
+    if (l == 0) { out[0] = s; out[1] = m; }
+  }
 }
 
 int launch_chkdt_partial(const DBlock *dB, const Tile *dT, int ntiles, double *part, cudaStream_t st) {
@@ -491,7 +504,7 @@ int launch_ke_partial(const DBlock *dB, const Tile *dT, int ntiles, double *part
   return SNAC_OK;
 }
 int launch_reduce_final(const double *part, int ntiles, double *out, cudaStream_t st) {
-  k_reduce_final<<<1, 32, 0, st>>>(part, ntiles, out), ::snac::count_launch();
+  k_reduce_final<<<1, RED_THREADS, 0, st>>>(part, ntiles, out), ::snac::count_launch();
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

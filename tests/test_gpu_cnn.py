@@ -45,6 +45,31 @@ def test_conv3x3_tcgen05(snac_lib, shape, relu):
     np.testing.assert_allclose(y, ref, rtol=1e-5, atol=1e-5 * np.max(np.abs(ref)))
 
 
+def test_conv3x3_accumulator_wait_runs_out(snac_lib):
+    """The convolution's wait for its tensor-core accumulator is bounded.  With the bound set to zero polls every
+    wait runs out at once: the call reports SNAC_ERR_TIMEOUT, having let the MMAs in flight finish and freed the
+    tensor memory, and the next call (default bound) on the same context gives the right answer -- which it
+    could not if the tensor memory had not been released."""
+    L = capi.lib()
+    shape = (2, 16, 5, 200)
+    rng = np.random.default_rng(77)
+    x = rng.standard_normal(shape).astype(np.float32)
+    w = (0.2 * rng.standard_normal((16, 16, 3, 3))).astype(np.float32)
+    b = rng.standard_normal(16).astype(np.float32)
+    y = np.zeros(shape, dtype=np.float32)
+    args = (x.ctypes.data_as(capi.FP), shape[0], shape[2], shape[3], w.ctypes.data_as(capi.FP),
+            b.ctypes.data_as(capi.FP), 1, y.ctypes.data_as(capi.FP))
+    try:
+        assert L.snac_cnn_set_poll_limit(0) == 0
+        assert L.snac_cnn_conv3x3(*args) == capi.ERR_TIMEOUT
+        assert b"timed out" in L.snac_last_error()
+    finally:
+        L.snac_cnn_set_poll_limit(-1)
+    assert L.snac_cnn_conv3x3(*args) == 0, L.snac_last_error()
+    ref = conv_ref(x, w, b.astype(np.float64), 1)
+    np.testing.assert_allclose(y, ref, rtol=1e-5, atol=1e-5 * np.max(np.abs(ref)))
+
+
 NPAR = 3 * (16 * 16 * 9 + 16)
 
 

@@ -343,6 +343,42 @@ def test_steps_lshape_impdiff(snac_lib, oracle_mod):
         d.close()
 
 
+@pytest.mark.parametrize("which", ["cavity_3d", "channel_z"])
+def test_impdiff_solve_entry(snac_lib, oracle_mod, which):
+    """snac_impdiff_solve (solve_impdiff_field with the reference's arguments) on each field of a domain: the
+    heated cavity's 3-D Helmholtz solves of u, v, w and T, and the channel's per-wavenumber solves along z,
+    against the oracle's solve of the same field from the same state."""
+    import dataclasses
+    if which == "cavity_3d":
+        case = cases.heated_cavity(n=(16, 16, 8), stretch=1.5, ra=1e6, impdiff=1, tol=1e-12, dt_f=2e-3)
+        fields = (capi.U, capi.V, capi.W, capi.S0)
+    else:
+        case = dataclasses.replace(cases.channel_4block(nx=(16, 32), ny=(8, 16), nz=16), impdiff=1, dt_f=1e-3)
+        fields = (capi.U, capi.V, capi.W)
+    O = oracle_mod.OracleDomain(case)
+    d = Domain(case)
+    try:
+        seed_fields(case, O, d, seed=9, amp=0.3)
+        if capi.S0 in fields:
+            rng = np.random.default_rng(10)
+            t = rng.standard_normal(O.field(0, capi.S0).shape)
+            O.field(0, capi.S0)[...] = t
+            d.set(0, capi.S0, t)
+        for X in (O, d):
+            X.bounduvw(False)
+        alphai = -2.0 * case.visci / 1e-3
+        L = capi.lib()
+        for f in fields:
+            fo = 3 + (f - capi.S0) if f >= capi.S0 else f - capi.U
+            assert oracle_mod.lib().or_impdiff_solve(O.h, fo, alphai) == 0
+            assert L.snac_impdiff_solve(f, alphai, 0.0) == 0, L.snac_last_error()
+            compare_fields(case, O, d, (f,), 1e-10)
+        with pytest.raises(AssertionError):
+            assert L.snac_impdiff_solve(capi.P, alphai, 0.0) == 0
+    finally:
+        d.close()
+
+
 @pytest.mark.parametrize("which", ["duct", "kovasznay"])
 def test_inflow_bitwise(snac_lib, oracle_mod, which):
     """inflow (bound.f90:438-477) after bounduvw: the inflow planes and mirrored ghosts equal the oracle's."""
