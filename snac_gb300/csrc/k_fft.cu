@@ -7,8 +7,20 @@
 // transforms back, applies normfft (main.f90:1017-1019) and writes pp.
 //
 // R2HC/HC2R with a power-of-two length use a shared-memory radix-2 FFT on
-// pairs of real lines packed as one complex line; every other kind (and any
-// length) uses a dense n x n matrix of FFTW's documented definition.
+// pairs of real lines packed as one complex line.  Every kind of any length
+// whose complex transform length factors into 2, 3 and 5 runs as a
+// mixed-radix Stockham FFT (radices 4, 2, 3, 5) in shared memory, with the
+// kinds of FFTW's definitions reduced to complex DFTs of symmetric extensions:
+//   R2HC / HC2R: length n, two real lines packed as one complex line;
+//   REDFT10 (DCT-II): the even extension of length 2n, times exp(-i pi k/2n);
+//   REDFT01 (DCT-III): the length-2n DFT of w_j x_j exp(-i pi j/2n), w = 1, 2, 2, ...;
+//   REDFT11 (DCT-IV): the length-2n DFT of x_j exp(-i pi j/2n), times 2 exp(-i pi (2k+1)/4n);
+//   RODFT10 / RODFT01 / RODFT11 from the DCT of the same type (Wang's relations
+//   DST-II_k = DCT-II((-1)^j x)_{n-1-k}, DST-III_k = (-1)^k DCT-III(x reversed)_k,
+//   DST-IV_k = (-1)^k DCT-IV(x reversed)_k);
+//   REDFT00 (DCT-I): the even extension of length 2(n-1);
+//   RODFT00 (DST-I): the odd extension of length 2(n+1), Y_k = -Im of its DFT at k+1.
+// Other lengths keep the dense n x n matrix of FFTW's documented definition.
 #include <cmath>
 
 #include "snac_host.h"
@@ -136,7 +148,158 @@ struct LineGeom {
   long ncell;          // box cells per system (plane mode)
   int n0;              // box extent along t1
   int field;           // HF_P: pp; HF_U + c: u, v, w; HF_S0 + s: scalar s
+  int N, nst;          // use_fft 2: complex length and number of passes
+  int rad[16];         // use_fft 2: radix of each pass
 };
+
+// ---------------------------------------------------------------- mixed-radix path (use_fft 2)
+// small in-register DFT of size R (2, 3, 4, 5): W_R^m = tw[m * NR] with tw[q] = exp(-2 pi i q / N), NR = N / R
+__device__ __forceinline__ void dft_small(double2 *v, int R, const double2 *__restrict__ tw, int NR) {
+  if (R == 2) {
+    const double2 a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  } else if (R == 4) {
+    const double2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]), t2 = cadd(v[1], v[3]);
+    const double2 dd = csub(v[1], v[3]);
+    const double2 t3 = make_double2(dd.y, -dd.x);  // -i (v1 - v3)
+    v[0] = cadd(t0, t2);
+    v[2] = csub(t0, t2);
+    v[1] = cadd(t1, t3);
+    v[3] = csub(t1, t3);
+  } else {
+    double2 o[5];
+    for (int k = 0; k < R; k++) {
+      double2 acc = v[0];
+      for (int q = 1; q < R; q++) {
+        const double2 w = tw[((q * k) % R) * NR];
+        acc = cadd(acc, cmul(v[q], w));
+      }
+      o[k] = acc;
+    }
+    for (int k = 0; k < R; k++) v[k] = o[k];
+  }
+}
+
+// Stockham autosort FFT (exp(-i...)) of nl complex lines of length N in a, ping-ponging with b; the result
+// ends in a (the pointers are swapped as needed).  Pass with radix R after sub-transforms of size Ns: item j
+// of a line reads x[j + r N/R], applies exp(-2 pi i r (j mod Ns) / (Ns R)), a size-R DFT, and writes
+// y[(j - j mod Ns) R + j mod Ns + r Ns].
+__device__ void fft_stockham(double2 *&a, double2 *&b, int nl, int N, int nst, const int *rad,
+                             const double2 *__restrict__ tw) {
+  int Ns = 1;
+  for (int st = 0; st < nst; st++) {
+    const int R = rad[st], NR = N / R, tscale = N / (Ns * R);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nl * NR; t += blockDim.x) {
+      const int l = t / NR, j = t - l * NR;
+      const double2 *x = a + (size_t)l * N;
+      double2 *y = b + (size_t)l * N;
+      const int jm = j % Ns, tb = jm * tscale;
+      double2 v[5];
+      v[0] = x[j];
+      for (int r = 1; r < R; r++) v[r] = cmul(x[j + r * NR], tw[r * tb]);
+      dft_small(v, R, tw, NR);
+      const int idx = (j - jm) * R + jm;
+      for (int r = 0; r < R; r++) y[idx + r * Ns] = v[r];
+    }
+    double2 *tmp = a;
+    a = b;
+    b = tmp;
+    Ns *= R;
+  }
+  __syncthreads();
+}
+
+// one kind on nl real lines of length n in s (line-major), through the complex buffers A and B (nl lines of
+// g.N each); gt = [tw (N) | pre (n) | post (n)] of this kind.  R2HC/HC2R pack two lines per complex line.
+__device__ void transform_general(const LineGeom &g, int kind, const double2 *__restrict__ gt, double *s, double2 *A,
+                                  double2 *B, int nl) {
+  const int n = g.n, N = g.N;
+  const double2 *__restrict__ tw = gt;
+  const double2 *__restrict__ pre = gt + N;
+  const double2 *__restrict__ post = gt + N + n;
+  const bool pairs = kind == SNAC_R2HC || kind == SNAC_HC2R;
+  const int nc = pairs ? nl >> 1 : nl;  // complex lines
+  __syncthreads();
+  for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
+    const int l = t / N, m = t - l * N;
+    double2 v = make_double2(0.0, 0.0);
+    if (kind == SNAC_R2HC) {
+      v = make_double2(s[(2 * l) * n + m], s[(2 * l + 1) * n + m]);
+    } else if (kind == SNAC_HC2R) {  // conj(Z), Z = A + i B from the two half-complex lines
+      const double *Ah = s + (2 * l) * n, *Bh = s + (2 * l + 1) * n;
+      const int k = m, kk = (2 * k <= n) ? k : n - k;
+      const double ra = Ah[kk], rb = Bh[kk];
+      double ia, ib;
+      if (k == 0 || 2 * k == n) { ia = 0.0; ib = 0.0; }
+      else if (2 * k < n) { ia = Ah[n - k]; ib = Bh[n - k]; }
+      else { ia = -Ah[k]; ib = -Bh[k]; }
+      v = make_double2(ra - ib, -(ia + rb));
+    } else {
+      const double *x = s + l * n;
+      switch (kind) {
+        case SNAC_REDFT10: v.x = m < n ? x[m] : x[2 * n - 1 - m]; break;
+        case SNAC_RODFT10: { const int q = m < n ? m : 2 * n - 1 - m; v.x = (q & 1) ? -x[q] : x[q]; } break;
+        case SNAC_REDFT01: case SNAC_REDFT11:
+          if (m < n) v = make_double2(x[m] * pre[m].x, x[m] * pre[m].y);
+          break;
+        case SNAC_RODFT01: case SNAC_RODFT11:
+          if (m < n) v = make_double2(x[n - 1 - m] * pre[m].x, x[n - 1 - m] * pre[m].y);
+          break;
+        case SNAC_REDFT00: v.x = m < n ? x[m] : x[2 * n - 2 - m]; break;
+        case SNAC_RODFT00:
+          if (m >= 1 && m <= n) v.x = x[m - 1];
+          else if (m >= n + 2) v.x = -x[N - m - 1];
+          break;
+      }
+    }
+    A[t] = v;
+  }
+  fft_stockham(A, B, nc, N, g.nst, g.rad, tw);
+  for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
+    const int l = t / n, k = t - l * n;
+    double y;
+    if (kind == SNAC_R2HC) {
+      const double2 *Z = A + (l >> 1) * N;
+      const double2 Zm = Z[k], Zc = Z[k ? n - k : 0];
+      if (!(l & 1)) y = (2 * k <= n) ? 0.5 * (Zm.x + Zc.x) : 0.5 * (Zc.y - Zm.y);
+      else y = (2 * k <= n) ? 0.5 * (Zm.y + Zc.y) : 0.5 * (Zm.x - Zc.x);
+    } else if (kind == SNAC_HC2R) {
+      const double2 z = A[(l >> 1) * N + k];
+      y = (l & 1) ? -z.y : z.x;
+    } else {
+      const double2 *Z = A + l * N;
+      switch (kind) {
+        case SNAC_REDFT10: { const double2 c = Z[k]; y = c.x * post[k].x - c.y * post[k].y; } break;
+        case SNAC_RODFT10: {
+          const int q = n - 1 - k;
+          const double2 c = Z[q];
+          y = c.x * post[q].x - c.y * post[q].y;
+        } break;
+        case SNAC_REDFT01: y = Z[k].x; break;
+        case SNAC_RODFT01: y = (k & 1) ? -Z[k].x : Z[k].x; break;
+        case SNAC_REDFT11: { const double2 c = Z[k]; y = c.x * post[k].x - c.y * post[k].y; } break;
+        case SNAC_RODFT11: {
+          const double2 c = Z[k];
+          const double v = c.x * post[k].x - c.y * post[k].y;
+          y = (k & 1) ? -v : v;
+        } break;
+        case SNAC_REDFT00: y = Z[k].x; break;
+        default: y = -Z[k + 1].y; break;  // RODFT00
+      }
+    }
+    s[t] = y;
+  }
+  __syncthreads();
+}
+
+// the lines of one CTA in s: the path chosen for this transform (zb: complex buffers behind s)
+__device__ __forceinline__ void transform_lines(const LineGeom &g, const double2 *__restrict__ tw,
+                                                const double *__restrict__ mat, double *s, double2 *zb) {
+  if (g.use_fft == 2) transform_general(g, g.kind, tw, s, zb, zb + (size_t)g.lp * g.N, g.lp);
+  else transform_smem(g.kind, g.n, g.use_fft, g.logn, tw, mat, s, zb, g.lp);
+}
 
 __device__ __forceinline__ double *line_field(const DBlock &B, int field) {
   if (field == HF_P) return B.pp;
@@ -171,7 +334,7 @@ __global__ void k_fft_fwd_box(const DBlock *__restrict__ Bs, const int2 *__restr
   const long fb = hidx(c[0], c[1], c[2], B.n[0], B.n[1]);
   const long fs = g.a == 0 ? 1 : g.a == 1 ? (long)(B.n[0] + 2) : (long)(B.n[0] + 2) * (B.n[1] + 2);
   for (int q = q0; q < n; q += qs) s[l * n + q] = valid ? f[fb + fs * q] : 0.0;
-  transform_smem(g.kind, n, g.use_fft, g.logn, tw, mat, s, zb, g.lp);
+  transform_lines(g, tw, mat, s, zb);
   if (!valid) return;
   const int2 o = boff[lt.x];
   if (x1 < ex.x && x2 < ex.y) {
@@ -208,7 +371,7 @@ __global__ void k_fft_bwd_box(const DBlock *__restrict__ Bs, const int2 *__restr
   const bool inbox = valid && x1 < ex.x && x2 < ex.y;
   const double *__restrict__ bx = box + (long)(x1 + o.x) + (long)g.n0 * (x2 + o.y);
   for (int q = q0; q < n; q += qs) s[l * n + q] = !valid ? 0.0 : inbox ? bx[g.ncell * q] : f[fb + fs * q];
-  transform_smem(g.kind, n, g.use_fft, g.logn, tw, mat, s, zb, g.lp);
+  transform_lines(g, tw, mat, s, zb);
   if (!valid) return;
   const int na = B.n[g.a];
   for (int q = q0; q < na; q += qs) {
@@ -244,21 +407,25 @@ __global__ void k_r2r_strided(double *arr, int m1, long s1, long s2, long sa, in
     const int l = t % g.lp, q = t / g.lp, line = l0 + l;
     s[l * n + q] = line < nlines ? arr[(line % m1) * s1 + (line / m1) * s2 + q * sa] : 0.0;
   }
-  transform_smem(g.kind, n, g.use_fft, g.logn, tw, mat, s, zb, g.lp);
+  transform_lines(g, tw, mat, s, zb);
   for (int t = threadIdx.x; t < g.lp * n; t += blockDim.x) {
     const int l = t % g.lp, q = t / g.lp, line = l0 + l;
     if (line < nlines) arr[(line % m1) * s1 + (line / m1) * s2 + q * sa] = s[l * n + q];
   }
 }
 
-// a power of two from 2 to 16 (the kernels take a thread's line as threadIdx.x mod lp)
-static int lines_per_cta(int n) {
-  const int cap = 6144 / (n > 0 ? n : 1);
+// a power of two from 2 to 16 (the kernels take a thread's line as threadIdx.x mod lp); Nc > 0: the complex
+// length of the mixed-radix path, whose two complex buffers per line bound the lines to about 96 KB a CTA
+static int lines_per_cta(int n, int Nc = 0) {
+  const long per_line = Nc > 0 ? 8L * n + 32L * Nc : 16L * n;
+  const long cap = (Nc > 0 ? 96L * 1024 : 96L * 1024) / (per_line > 0 ? per_line : 1);
   int lp = 2;
   while (lp * 2 <= 16 && lp * 2 <= cap) lp *= 2;
   return lp;
 }
-static size_t smem_bytes(int n, int lp) { return (size_t)lp * n * sizeof(double) * 2; }
+static size_t smem_bytes(int n, int lp, int Nc = 0) {
+  return Nc > 0 ? (size_t)lp * (8 * (size_t)n + 32 * (size_t)Nc) : (size_t)lp * n * sizeof(double) * 2;
+}
 
 static int ilog2(int n) {
   int l = 0;
@@ -314,13 +481,57 @@ static std::vector<double> twiddles(int n) {
 
 static bool pow2(int n) { return n >= 2 && (n & (n - 1)) == 0; }
 
+// complex transform length of a kind of real length n on the mixed-radix path
+static int complex_length(int kind, int n) {
+  switch (kind) {
+    case SNAC_R2HC: case SNAC_HC2R: return n;
+    case SNAC_REDFT00: return n >= 2 ? 2 * (n - 1) : 0;
+    case SNAC_RODFT00: return 2 * (n + 1);
+    default: return 2 * n;
+  }
+}
+// radices 4, 2, 3, 5 of N (4 first: fewer passes); false when another prime divides N
+static bool radices(int N, int *rad, int *nst) {
+  int m = N, k = 0;
+  for (int r : {4, 2, 3, 5})
+    while (m % r == 0 && k < 16) { rad[k++] = r; m /= r; }
+  *nst = k;
+  return m == 1 && N >= 2;
+}
+// [tw (N) | pre (n) | post (n)] of a kind, complex: tw = exp(-2 pi i q/N); the DCT/DST pre- and post-factors
+static std::vector<double> general_tables(int kind, int n, int N) {
+  const double PI = 3.14159265358979323846264338327950288;
+  std::vector<double> t(2 * ((size_t)N + 2 * (size_t)n), 0.0);
+  for (int q = 0; q < N; q++) { t[2 * q] = cos(2.0 * PI * q / N); t[2 * q + 1] = -sin(2.0 * PI * q / N); }
+  double *pre = t.data() + 2 * (size_t)N, *post = pre + 2 * (size_t)n;
+  for (int j = 0; j < n; j++) {
+    const double c = cos(PI * j / (2.0 * n)), sn = -sin(PI * j / (2.0 * n));
+    const double w = (kind == SNAC_REDFT01 || kind == SNAC_RODFT01) ? (j == 0 ? 1.0 : 2.0) : 1.0;
+    pre[2 * j] = w * c;
+    pre[2 * j + 1] = w * sn;
+    if (kind == SNAC_REDFT10 || kind == SNAC_RODFT10) { post[2 * j] = c; post[2 * j + 1] = sn; }
+    if (kind == SNAC_REDFT11 || kind == SNAC_RODFT11) {
+      post[2 * j] = 2.0 * cos(PI * (2 * j + 1) / (4.0 * n));
+      post[2 * j + 1] = -2.0 * sin(PI * (2 * j + 1) / (4.0 * n));
+    }
+  }
+  return t;
+}
+// the mixed-radix path applies to this kind and length
+static bool general_ok(int kind, int n, int *N, int *rad, int *nst) {
+  *N = complex_length(kind, n);
+  if (*N < 2 || !radices(*N, rad, nst)) return false;
+  if ((kind == SNAC_R2HC || kind == SNAC_HC2R) && n < 2) return false;
+  return true;
+}
+
 struct FftLaunch {
   int lp;
   size_t smem;
 };
-static int prep_launch(int n, FftLaunch &L, const void *fn) {
-  L.lp = lines_per_cta(n);
-  L.smem = smem_bytes(n, L.lp);
+static int prep_launch(int n, FftLaunch &L, const void *fn, int Nc = 0) {
+  L.lp = lines_per_cta(n, Nc);
+  L.smem = smem_bytes(n, L.lp, Nc);
   if (L.smem > 48 * 1024) SNAC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
   return SNAC_OK;
 }
@@ -330,7 +541,7 @@ static int ensure_tables(Domain &d, PoissonSolver &S) {
   if (S.tabs_ready) return SNAC_OK;
   const int a = S.fft_axis ? S.fft_axis - 1 : 0;
   const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
-  S.lt_lp = lines_per_cta(S.fft_axis ? S.nfft : 1);
+  S.lt_lp = lines_per_cta(S.fft_axis ? S.nfft : 1, S.use_fft == 2 ? S.nfft_c : 0);
   std::vector<int2> lt, bo, ex;
   std::vector<int4> bo3;
   for (int b = 0; b < d.nblocks; b++) {
@@ -374,6 +585,9 @@ static LineGeom line_geom(const PoissonSolver &S, int kind) {
   g.ncell = S.ncell0;
   g.n0 = S.P.L[0].n[0];
   g.field = S.field;
+  g.N = S.nfft_c;
+  g.nst = S.fft_nst;
+  for (int q = 0; q < 16; q++) g.rad[q] = S.fft_rad[q];
   return g;
 }
 
@@ -381,10 +595,11 @@ int fft_forward_to_box(Domain &d, PoissonSolver &S, cudaStream_t st) {
   SNAC_TRY(ensure_tables(d, S));
   LineGeom g = line_geom(S, S.kind_fwd);
   FftLaunch L;
-  SNAC_TRY(prep_launch(g.n, L, (const void *)k_fft_fwd_box));
+  SNAC_TRY(prep_launch(g.n, L, (const void *)k_fft_fwd_box, S.use_fft == 2 ? S.nfft_c : 0));
   prof_begin(KID_FFT_FWD, st);
-  k_fft_fwd_box<<<S.nlt, 256, L.smem, st>>>(d.d_db, S.d_lt, S.d_boff, S.d_lext, g, (const double2 *)S.d_tw,
-                                            S.d_mat_fwd, S.box_b), ::snac::count_launch();
+  k_fft_fwd_box<<<S.nlt, 256, L.smem, st>>>(d.d_db, S.d_lt, S.d_boff, S.d_lext, g,
+                                            (const double2 *)(S.use_fft == 2 ? S.d_gt_fwd : S.d_tw), S.d_mat_fwd,
+                                            S.box_b), ::snac::count_launch();
   prof_end(KID_FFT_FWD, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -394,10 +609,11 @@ int fft_backward_from_box(Domain &d, PoissonSolver &S, cudaStream_t st) {
   SNAC_TRY(ensure_tables(d, S));
   LineGeom g = line_geom(S, S.kind_bwd);
   FftLaunch L;
-  SNAC_TRY(prep_launch(g.n, L, (const void *)k_fft_bwd_box));
+  SNAC_TRY(prep_launch(g.n, L, (const void *)k_fft_bwd_box, S.use_fft == 2 ? S.nfft_c : 0));
   prof_begin(KID_FFT_BWD, st);
-  k_fft_bwd_box<<<S.nlt, 256, L.smem, st>>>(d.d_db, S.d_lt, S.d_boff, S.d_lext, g, (const double2 *)S.d_tw,
-                                            S.d_mat_bwd, S.box_x, S.normfft), ::snac::count_launch();
+  k_fft_bwd_box<<<S.nlt, 256, L.smem, st>>>(d.d_db, S.d_lt, S.d_boff, S.d_lext, g,
+                                            (const double2 *)(S.use_fft == 2 ? S.d_gt_bwd : S.d_tw), S.d_mat_bwd,
+                                            S.box_x, S.normfft), ::snac::count_launch();
   prof_end(KID_FFT_BWD, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -422,7 +638,22 @@ int box_scatter(Domain &d, PoissonSolver &S, cudaStream_t st) {
 // upload twiddles / matrices of a transform pair
 int fft_setup(PoissonSolver &S) {
   const int n = S.nfft;
+  int Nf = 0, nstf = 0, radf[16], Nb = 0, nstb = 0, radb[16];
   S.use_fft = (S.kind_fwd == SNAC_R2HC && pow2(n)) ? 1 : 0;
+  if (!S.use_fft && general_ok(S.kind_fwd, n, &Nf, radf, &nstf) && general_ok(S.kind_bwd, n, &Nb, radb, &nstb) &&
+      Nf == Nb) {
+    S.use_fft = 2;
+    S.nfft_c = Nf;
+    S.fft_nst = nstf;
+    for (int q = 0; q < 16; q++) S.fft_rad[q] = radf[q];
+    auto tf = general_tables(S.kind_fwd, n, Nf), tb = general_tables(S.kind_bwd, n, Nb);
+    S.d_gt_fwd = (double *)S.alloc(tf.size() * sizeof(double));
+    S.d_gt_bwd = (double *)S.alloc(tb.size() * sizeof(double));
+    if (!S.d_gt_fwd || !S.d_gt_bwd) { set_error("device allocation failed (transform tables)"); return SNAC_ERR_NOMEM; }
+    SNAC_CUDA(cudaMemcpy(S.d_gt_fwd, tf.data(), tf.size() * sizeof(double), cudaMemcpyHostToDevice));
+    SNAC_CUDA(cudaMemcpy(S.d_gt_bwd, tb.data(), tb.size() * sizeof(double), cudaMemcpyHostToDevice));
+    return SNAC_OK;
+  }
   if (S.use_fft) {
     auto tw = twiddles(n);
     S.d_tw = (double *)S.alloc(tw.size() * sizeof(double));
@@ -447,11 +678,19 @@ int r2r_array(int kind, int idir, const int nn[3], int q, double *darr, cudaStre
   LineGeom g;
   g.a = a; g.t1 = t1; g.t2 = t2; g.n = n; g.logn = ilog2(n); g.kind = kind;
   g.use_fft = ((kind == SNAC_R2HC || kind == SNAC_HC2R) && pow2(n)) ? 1 : 0;
-  g.lp = lines_per_cta(n);
+  g.N = 0;
+  g.nst = 0;
+  if (!g.use_fft && general_ok(kind, n, &g.N, g.rad, &g.nst)) g.use_fft = 2;
+  else g.N = 0;
+  g.lp = lines_per_cta(n, g.N);
   g.llp = ilog2(g.lp);
   g.ncell = 0; g.n0 = 0;
   double *dtw = nullptr, *dmat = nullptr;
-  if (g.use_fft) {
+  if (g.use_fft == 2) {
+    auto t = general_tables(kind, n, g.N);
+    SNAC_CUDA(cudaMalloc(&dtw, t.size() * sizeof(double)));
+    SNAC_CUDA(cudaMemcpy(dtw, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice));
+  } else if (g.use_fft) {
     auto tw = twiddles(n);
     SNAC_CUDA(cudaMalloc(&dtw, tw.size() * sizeof(double)));
     SNAC_CUDA(cudaMemcpy(dtw, tw.data(), tw.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -461,7 +700,7 @@ int r2r_array(int kind, int idir, const int nn[3], int q, double *darr, cudaStre
     SNAC_CUDA(cudaMemcpy(dmat, m.data(), m.size() * sizeof(double), cudaMemcpyHostToDevice));
   }
   FftLaunch L;
-  int rc = prep_launch(n, L, (const void *)k_r2r_strided);
+  int rc = prep_launch(n, L, (const void *)k_r2r_strided, g.N);
   const int nlines = nn[t1] * nn[t2];
   if (rc == SNAC_OK) {
     k_r2r_strided<<<(nlines + L.lp - 1) / L.lp, 256, L.smem, st>>>(darr, nn[t1], str[t1], str[t2], str[a], nlines, g,

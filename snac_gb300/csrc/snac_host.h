@@ -80,8 +80,11 @@ struct PoissonSolver {
   int mode3d = 0, ax[3] = {0, 1, 2}, periodic[3] = {0, 0, 0}, nsys = 1, lo_min[3] = {0, 0, 0};
   int fft_axis = 0, nfft = 0, kind_fwd = -1, kind_bwd = -1;
   double normfft = 1.0;
-  int use_fft = 0;                   // 1: radix-2 FFT path for R2HC/HC2R; 0: dense r2r matrices
-  double *d_tw = nullptr;            // FFT twiddles exp(-2 pi i k/n), k < n/2 (complex)
+  int use_fft = 0;                   // 1: radix-2 FFT for power-of-two R2HC/HC2R; 2: mixed-radix (2, 3, 4, 5)
+                                     // FFT of length nfft_c for every kind; 0: dense r2r matrices
+  double *d_tw = nullptr;            // use_fft 1: FFT twiddles exp(-2 pi i k/n), k < n/2 (complex)
+  double *d_gt_fwd = nullptr, *d_gt_bwd = nullptr;  // use_fft 2: tables of the forward / backward kind
+  int nfft_c = 0, fft_nst = 0, fft_rad[16] = {};    // use_fft 2: complex length and its radices
   double *d_mat_fwd = nullptr, *d_mat_bwd = nullptr;  // dense r2r matrices (n x n)
   // transform line tiles (k_fft.cu), built once per solver: (block, first line) per CTA, box offsets of the
   // blocks, per block the solved extents along the two other axes (lines outside them are transformed in

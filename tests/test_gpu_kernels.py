@@ -212,9 +212,13 @@ def test_bounduvw_boundp_block(snac_lib, oracle_mod, case, is_correc):
 
 @pytest.mark.parametrize("kind", ["R2HC", "HC2R", "REDFT10", "REDFT01", "REDFT11", "RODFT10", "RODFT01", "RODFT11",
                                   "REDFT00", "RODFT00"])
-@pytest.mark.parametrize("idir,n", [(1, 8), (2, 12), (3, 16), (3, 128), (3, 2)])
+@pytest.mark.parametrize("idir,n", [(1, 8), (2, 12), (3, 16), (3, 128), (3, 2), (1, 96), (2, 160), (3, 256),
+                                    (1, 15), (2, 7)])
 def test_fft_kinds(snac_lib, oracle_mod, kind, idir, n):
-    """fft.f90:85-94: every FFTW kind along every axis, FFT path (power-of-two R2HC/HC2R) and dense path."""
+    """fft.f90:85-94: every FFTW kind along every axis against the oracle's FFTW definitions: the radix-2 path
+    (power-of-two R2HC/HC2R), the mixed-radix path (every kind whose complex length factors into 2, 3, 5:
+    the DCTs and DSTs through symmetric extensions, odd and non-power-of-two lengths), and the dense path
+    (n = 7: lengths 7 and 14 have a prime factor 7)."""
     if n == 2 and kind in ("REDFT00", "RODFT00"):
         pytest.skip("FFTW's REDFT00 needs n >= 2 points; covered at other sizes")
     rng = np.random.default_rng(90 + n + idir)
