@@ -30,6 +30,18 @@ def test_library_exports_every_declared_symbol():
     assert sorted(capi.PROTOTYPES) == declared_functions()
 
 
+def test_fortran_module_binds_declared_functions():
+    """fortran/mod_snac_gpu.f90 binds only entry points the header declares, one interface each, and covers the
+    reference-signature and per-block boundary calls (the module is not compiled here: no Fortran compiler)."""
+    src = open(os.path.join(ROOT, "fortran", "mod_snac_gpu.f90")).read()
+    bound = re.findall(r"bind\(C,name='(snac_[a-z0-9_]+)'\)", src)
+    assert len(bound) == len(set(bound))
+    assert set(bound) <= set(declared_functions())
+    for n in ("snac_rk_mom", "snac_fillps", "snac_correc", "snac_updt_pressure", "snac_chkdt", "snac_chkdiv",
+              "snac_bounduvw", "snac_boundp", "snac_impdiff_solve", "snac_fft"):
+        assert n in bound, n
+
+
 def test_calls_fail_cleanly_without_device():
     """Without a CUDA device the library reports SNAC_ERR_CUDA instead of computing anything on the CPU."""
     from snac_gb300 import capi
