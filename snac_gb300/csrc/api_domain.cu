@@ -29,6 +29,7 @@ void *Domain::alloc(size_t bytes) {
 }
 Domain::~Domain() {
   if (guess) guess_destroy(guess);
+  tma_destroy(*this);
   ps.reset();
   for (auto &h : hs) h.reset();
   for (void *p : allocs) cudaFree(p);
@@ -653,6 +654,14 @@ static int set_dt_from_cfl(Domain &d) {
   return SNAC_OK;
 }
 
+// fillps on every block: the TMA-staged kernel where its tiled copies apply, else the plain one
+static int fillps_all(Domain &d, double dtrk) {
+  int done = 0;
+  SNAC_TRY(launch_fillps_tma(d, dtrk, &done));
+  if (!done) SNAC_TRY(launch_fillps(d.d_db, d.d_tiles, d.ntiles, dtrk, d.c.fft_axis, d.st));
+  return SNAC_OK;
+}
+
 static int one_stage(Domain &d, int irk) {
   const double dtrk = (RKC[irk][0] + RKC[irk][1]) * d.dt;
   const double alpha = -(1.0 / d.c.visci) * dtrk / 2.0;
@@ -660,7 +669,7 @@ static int one_stage(Domain &d, int irk) {
   SNAC_TRY(rk_mom_all(d, irk));
   SNAC_TRY(bound_uvw(d, 0));
   SNAC_TRY(inflow_all(d, 0));
-  SNAC_TRY(launch_fillps(d.d_db, d.d_tiles, d.ntiles, dtrk, d.c.fft_axis, d.st));
+  SNAC_TRY(fillps_all(d, dtrk));
   SNAC_TRY(updt_rhs_all(d));
   int rc = solver_solve_pressure(d, *d.ps);
   if (rc != SNAC_OK && rc != SNAC_ERR_NOT_CONVERGED) return rc;
@@ -759,6 +768,7 @@ int snac_init(const snac_case *c, const snac_block_desc *blocks, const snac_opti
     d->hs[f].reset(new PoissonSolver());
     rc = solver_create(*d, *d->hs[f], true, f);
   }
+  if (rc == SNAC_OK) rc = tma_setup(*d);  // the TMA-staged fillps where its tiled copies apply
   if (rc != SNAC_OK) { delete d; return rc; }
   g_dom = d;
   return SNAC_OK;
@@ -1096,9 +1106,9 @@ int snac_impdiff_solve(int field, double alphai_new, double alphai_old) {
 
 int snac_fillps_all(double dtrk) {
   NEED_DOMAIN
-  SNAC_TRY(launch_fillps(d->d_db, d->d_tiles, d->ntiles, dtrk, d->c.fft_axis, d->st));
+  SNAC_TRY(fillps_all(*d, dtrk));
   SNAC_CUDA(cudaStreamSynchronize(d->st));
-  return SNAC_OK;
+  return tma_check(*d);
 }
 int snac_updt_rhs_all(void) {
   NEED_DOMAIN
@@ -1208,6 +1218,7 @@ int snac_step(int nsteps) {
   float ms = 0.f;
   SNAC_CUDA(cudaEventElapsedTime(&ms, d->ev0, d->ev1));
   d->device_ms = ms;
+  SNAC_TRY(tma_check(*d));  // a bounded wait of the TMA-staged kernel that ran out
   return rc_all;
 }
 

@@ -132,6 +132,9 @@ struct PoissonSolver {
   void *alloc(size_t bytes);
 };
 
+struct TmaMaps;                     // tensor maps of the TMA-staged kernels (k_tma.cu)
+constexpr int TMA_MAX_BLOCKS = 16;  // blocks the TMA-staged kernels take (more: the plain kernels run)
+
 struct Domain {
   snac_case c{};
   snac_options opt{};
@@ -157,6 +160,10 @@ struct Domain {
   std::unique_ptr<PoissonSolver> ps;
   std::unique_ptr<PoissonSolver> hs[3 + SNAC_MAX_SCAL];  // IMPDIFF: Helmholtz solvers of u, v, w, scalars
   GuessState *guess = nullptr;       // learned initial guess of the pressure solve (off unless requested)
+  TmaMaps *tma = nullptr;            // TMA-staged fillps: tensor maps, tile list, CTAs, error flag (null: n/a)
+  int4 *tma_tiles = nullptr;
+  int tma_ntiles = 0, tma_ctas = 0;
+  int *tma_err = nullptr;
   double dt = 0.0, time = 0.0;
   int istep = 0;
   int last_solve_iters = 0, solves = 0;
@@ -182,6 +189,10 @@ int helm_rhs(Domain &d, PoissonSolver &S, double alphai, cudaStream_t st);
 int helm_shift(PoissonSolver &S, double alphai, cudaStream_t st);
 int helm_io(Domain &d, PoissonSolver &S, double *box, int to_box, cudaStream_t st);
 int solver_solve_pressure(Domain &d, PoissonSolver &S);
+int tma_setup(Domain &d);
+void tma_destroy(Domain &d);
+int launch_fillps_tma(Domain &d, double dt, int *done);
+int tma_check(Domain &d);
 int guess_before(Domain &d, PoissonSolver &S, cudaStream_t st);
 int guess_after(Domain &d, PoissonSolver &S, cudaStream_t st);
 // mode of the learned guess (0 when it was never set up); set only changes an existing guess state
