@@ -128,6 +128,8 @@ typedef struct snac_options {
   int mg_waves;       /* waves of CTAs per batched plane launch (default 2) */
   int mg_red_batch;   /* -1: the reducing plane kernels run one system per CTA (default: batched) */
   int mg_lnu;         /* first multigrid level that uses nu_coarse (default 2) */
+  int tma;            /* -1: the fillps pass reads its fields directly instead of through TMA-staged tiles
+                         (default: TMA where the blocks allow it: even x extents, at most 16 blocks) */
 } snac_options;
 
 typedef struct snac_step_stats {

@@ -156,7 +156,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 // Tensor maps of u, v, w of every block and the tile list; d.tma stays null where the tiled copies do not
 // apply (the plain kernels run then)
 int tma_setup(Domain &d) {
-  if (d.tma) return SNAC_OK;
+  if (d.tma || d.opt.tma == -1) return SNAC_OK;
   if (d.nblocks > TMA_MAX_BLOCKS) return SNAC_OK;
   for (int b = 0; b < d.nblocks; b++)
     if (d.db[b].n[0] & 1) return SNAC_OK;  // row pitch not a multiple of 16 bytes

@@ -343,6 +343,28 @@ def test_steps_lshape_impdiff(snac_lib, oracle_mod):
         d.close()
 
 
+@pytest.mark.parametrize("fft_axis", [0, 3])
+def test_fillps_tma_matches_plain(snac_lib, fft_axis):
+    """fillps through TMA-staged tiles (the uneven four-block channel: every tile kind, partial tiles at the
+    block ends) gives the same bits as the kernel that reads the fields directly."""
+    import dataclasses
+    case = dataclasses.replace(cases.channel_4block(nx=(48, 64), ny=(24, 40), nz=14), fft_axis=fft_axis)
+    out = {}
+    for tma in (0, -1):
+        d = Domain(case, tma=tma)
+        try:
+            rng = np.random.default_rng(12)
+            for ib in range(len(case.blocks)):
+                for k in (capi.U, capi.V, capi.W):
+                    d.set(ib, k, rng.standard_normal(d.shape(ib, k)))
+            d.fillps(0.37)
+            out[tma] = [d.get(ib, capi.PP) for ib in range(len(case.blocks))]
+        finally:
+            d.close()
+    for a, b in zip(out[0], out[-1]):
+        np.testing.assert_array_equal(a[1:-1, 1:-1, 1:-1], b[1:-1, 1:-1, 1:-1])
+
+
 @pytest.mark.parametrize("which", ["cavity_3d", "channel_z"])
 def test_impdiff_solve_entry(snac_lib, oracle_mod, which):
     """snac_impdiff_solve (solve_impdiff_field with the reference's arguments) on each field of a domain: the
