@@ -244,6 +244,24 @@ int snac_bounduvw(const char cbc[3][3][2], const int lo[3], const int hi[3], con
  * cbc(s,d), bc(s,d)). */
 int snac_boundp(const char cbc[3][2], const int lo[3], const int hi[3], const double bc[3][2], const int is_bound[3][2],
                 const int nb[3][2], int myrank, const double *dxc, const double *dyc, const double *dzc, double *p);
+/* post.f90:8-156 for one block, with the reference's argument lists: n the interior extents, the metrics
+ * (n+2 entries from lo-1) and the halo'd velocity ux, uy, uz as host arrays (registered mirrors or copied
+ * around the call); outputs interior (n).  cmpt_vorticity (post.f90:8-53): the three vorticity components at
+ * the cell centres; cmpt_strain_rate (post.f90:55-98): S_ij S_ij; cmpt_rotation_rate (post.f90:100-139):
+ * W_ij W_ij; cmpt_q_criterion (post.f90:141-156): Q = (ens - str) / 2. */
+int snac_cmpt_vorticity(const int n[3], const double *dxc, const double *dyc, const double *dzc, const double *ux,
+                        const double *uy, const double *uz, double *vox, double *voy, double *voz);
+int snac_cmpt_strain_rate(const int n[3], const double *dxc, const double *dyc, const double *dzc, const double *dxf,
+                          const double *dyf, const double *dzf, const double *ux, const double *uy, const double *uz,
+                          double *str);
+int snac_cmpt_rotation_rate(const int n[3], const double *dxc, const double *dyc, const double *dzc, const double *ux,
+                            const double *uy, const double *uz, double *ens);
+int snac_cmpt_q_criterion(const int n[3], const double *ens, const double *str, double *qcr);
+/* No counterpart in the reference (which computes the two rates into arrays first): the Q criterion of one block
+ * straight from the velocity in one pass, the same values as the three calls above. */
+int snac_q_criterion(const int n[3], const double *dxc, const double *dyc, const double *dzc, const double *dxf,
+                     const double *dyf, const double *dzf, const double *ux, const double *uy, const double *uz,
+                     double *qcr);
 /* bound.f90:108-248 (set_bc) on one face of one halo'd array */
 int snac_set_bc(char ctype, int ibound, const int lo[3], const int hi[3], int idir, int centered,
                 double rvalue, double dr, double *p);

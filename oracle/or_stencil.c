@@ -492,6 +492,79 @@ void or_boundp_block(const char cbc[3][2], const int lo[3], const int hi[3], con
     }
 }
 
+/* post.f90:8-156: vorticity, strain rate S_ij S_ij, rotation rate W_ij W_ij and the Q criterion at cell
+ * centres of one block.  n = interior extents; ux, uy, uz halo'd (0:n+1); metrics indexed 0..n+1; outputs
+ * interior (1:n, Fortran order). */
+#define PH(a, i, j, k) a[(i) + (size_t)(n[0] + 2) * ((j) + (size_t)(n[1] + 2) * (k))]
+#define PI_(a, i, j, k) a[((i) - 1) + (size_t)n[0] * (((j) - 1) + (size_t)n[1] * ((k) - 1))]
+void or_cmpt_vorticity(const int n[3], const double *dxc, const double *dyc, const double *dzc, const double *ux,
+                       const double *uy, const double *uz, double *vox, double *voy, double *voz) {
+  for (int k = 1; k <= n[2]; k++)
+    for (int j = 1; j <= n[1]; j++)
+      for (int i = 1; i <= n[0]; i++) {
+        PI_(vox, i, j, k) = 0.25 * ((PH(uz, i, j + 1, k) - PH(uz, i, j, k)) / dyc[j] - (PH(uy, i, j, k + 1) - PH(uy, i, j, k)) / dzc[k] +
+                                    (PH(uz, i, j + 1, k - 1) - PH(uz, i, j, k - 1)) / dyc[j] - (PH(uy, i, j, k) - PH(uy, i, j, k - 1)) / dzc[k - 1] +
+                                    (PH(uz, i, j, k) - PH(uz, i, j - 1, k)) / dyc[j - 1] - (PH(uy, i, j - 1, k + 1) - PH(uy, i, j - 1, k)) / dzc[k] +
+                                    (PH(uz, i, j, k - 1) - PH(uz, i, j - 1, k - 1)) / dyc[j - 1] - (PH(uy, i, j - 1, k) - PH(uy, i, j - 1, k - 1)) / dzc[k - 1]);
+        PI_(voy, i, j, k) = 0.25 * ((PH(ux, i, j, k + 1) - PH(ux, i, j, k)) / dzc[k] - (PH(uz, i + 1, j, k) - PH(uz, i, j, k)) / dxc[i] +
+                                    (PH(ux, i, j, k) - PH(ux, i, j, k - 1)) / dzc[k - 1] - (PH(uz, i + 1, j, k - 1) - PH(uz, i, j, k - 1)) / dxc[i] +
+                                    (PH(ux, i - 1, j, k + 1) - PH(ux, i - 1, j, k)) / dzc[k] - (PH(uz, i, j, k) - PH(uz, i - 1, j, k)) / dxc[i - 1] +
+                                    (PH(ux, i - 1, j, k) - PH(ux, i - 1, j, k - 1)) / dzc[k - 1] - (PH(uz, i, j, k - 1) - PH(uz, i - 1, j, k - 1)) / dxc[i - 1]);
+        PI_(voz, i, j, k) = 0.25 * ((PH(uy, i + 1, j, k) - PH(uy, i, j, k)) / dxc[i] - (PH(ux, i, j + 1, k) - PH(ux, i, j, k)) / dyc[j] +
+                                    (PH(uy, i + 1, j - 1, k) - PH(uy, i, j - 1, k)) / dxc[i] - (PH(ux, i, j, k) - PH(ux, i, j - 1, k)) / dyc[j - 1] +
+                                    (PH(uy, i, j, k) - PH(uy, i - 1, j, k)) / dxc[i - 1] - (PH(ux, i - 1, j + 1, k) - PH(ux, i - 1, j, k)) / dyc[j] +
+                                    (PH(uy, i, j - 1, k) - PH(uy, i - 1, j - 1, k)) / dxc[i - 1] - (PH(ux, i - 1, j, k) - PH(ux, i - 1, j - 1, k)) / dyc[j - 1]);
+      }
+}
+
+static double sq(double a) { return a * a; }
+
+/* sgn = +1: strain rate sum of squares of (du_i/dx_j + du_j/dx_i)/2 terms (post.f90:55-98);
+ * sgn = -1: rotation rate (post.f90:100-139) */
+static void or_rate(const int n[3], const double *dxc, const double *dyc, const double *dzc, const double *dxf,
+                    const double *dyf, const double *dzf, const double *ux, const double *uy, const double *uz,
+                    double sgn, double *out) {
+  for (int k = 1; k <= n[2]; k++)
+    for (int j = 1; j <= n[1]; j++)
+      for (int i = 1; i <= n[0]; i++) {
+        const double a12 = .25 * (sq((PH(ux, i, j + 1, k) - PH(ux, i, j, k)) / dyc[j] + sgn * ((PH(uy, i + 1, j, k) - PH(uy, i, j, k)) / dxc[i])) +
+                                  sq((PH(ux, i, j, k) - PH(ux, i, j - 1, k)) / dyc[j - 1] + sgn * ((PH(uy, i + 1, j - 1, k) - PH(uy, i, j - 1, k)) / dxc[i])) +
+                                  sq((PH(ux, i - 1, j + 1, k) - PH(ux, i - 1, j, k)) / dyc[j] + sgn * ((PH(uy, i, j, k) - PH(uy, i - 1, j, k)) / dxc[i - 1])) +
+                                  sq((PH(ux, i - 1, j, k) - PH(ux, i - 1, j - 1, k)) / dyc[j - 1] + sgn * ((PH(uy, i, j - 1, k) - PH(uy, i - 1, j - 1, k)) / dxc[i - 1]))) * .25;
+        const double a13 = .25 * (sq((PH(ux, i, j, k + 1) - PH(ux, i, j, k)) / dzc[k] + sgn * ((PH(uz, i + 1, j, k) - PH(uz, i, j, k)) / dxc[i])) +
+                                  sq((PH(ux, i, j, k) - PH(ux, i, j, k - 1)) / dzc[k - 1] + sgn * ((PH(uz, i + 1, j, k - 1) - PH(uz, i, j, k - 1)) / dxc[i])) +
+                                  sq((PH(ux, i - 1, j, k + 1) - PH(ux, i - 1, j, k)) / dzc[k] + sgn * ((PH(uz, i, j, k) - PH(uz, i - 1, j, k)) / dxc[i - 1])) +
+                                  sq((PH(ux, i - 1, j, k) - PH(ux, i - 1, j, k - 1)) / dzc[k - 1] + sgn * ((PH(uz, i, j, k - 1) - PH(uz, i - 1, j, k - 1)) / dxc[i - 1]))) * .25;
+        const double a23 = .25 * (sq((PH(uy, i, j, k + 1) - PH(uy, i, j, k)) / dzc[k] + sgn * ((PH(uz, i, j + 1, k) - PH(uz, i, j, k)) / dyc[j])) +
+                                  sq((PH(uy, i, j, k) - PH(uy, i, j, k - 1)) / dzc[k - 1] + sgn * ((PH(uz, i, j + 1, k - 1) - PH(uz, i, j, k - 1)) / dyc[j])) +
+                                  sq((PH(uy, i, j - 1, k + 1) - PH(uy, i, j - 1, k)) / dzc[k] + sgn * ((PH(uz, i, j, k) - PH(uz, i, j - 1, k)) / dyc[j - 1])) +
+                                  sq((PH(uy, i, j - 1, k) - PH(uy, i, j - 1, k - 1)) / dzc[k - 1] + sgn * ((PH(uz, i, j, k - 1) - PH(uz, i, j - 1, k - 1)) / dyc[j - 1]))) * .25;
+        if (sgn > 0) {
+          const double s11 = sq((PH(ux, i, j, k) - PH(ux, i - 1, j, k)) / dxf[i]);
+          const double s22 = sq((PH(uy, i, j, k) - PH(uy, i, j - 1, k)) / dyf[j]);
+          const double s33 = sq((PH(uz, i, j, k) - PH(uz, i, j, k - 1)) / dzf[k]);
+          PI_(out, i, j, k) = s11 + s22 + s33 + 2 * (a12 + a13 + a23);
+        } else {
+          PI_(out, i, j, k) = 2.0 * (a12 + a13 + a23);
+        }
+      }
+}
+void or_cmpt_strain_rate(const int n[3], const double *dxc, const double *dyc, const double *dzc, const double *dxf,
+                         const double *dyf, const double *dzf, const double *ux, const double *uy, const double *uz,
+                         double *str) {
+  or_rate(n, dxc, dyc, dzc, dxf, dyf, dzf, ux, uy, uz, 1.0, str);
+}
+void or_cmpt_rotation_rate(const int n[3], const double *dxc, const double *dyc, const double *dzc, const double *ux,
+                           const double *uy, const double *uz, double *ens) {
+  or_rate(n, dxc, dyc, dzc, dxc, dyc, dzc, ux, uy, uz, -1.0, ens);
+}
+void or_cmpt_q_criterion(const int n[3], const double *ens, const double *str, double *qcr) {
+  const size_t m = (size_t)n[0] * n[1] * n[2];
+  for (size_t q = 0; q < m; q++) qcr[q] = .5 * (ens[q] - str[q]);
+}
+#undef PH
+#undef PI_
+
 /* solver.f90:44-157 (init_bc_rhs).  fft_axis selects the weight of solver.f90:98-106. */
 void or_init_bc_rhs(const char cbc[3][2], const double bc[3][2], const double dl[3][2],
                     const int is_bound[3][2], const int is_centered[3], const int lo[3],

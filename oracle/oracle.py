@@ -112,6 +112,10 @@ def lib():
         L.or_chkdiv_local.argtypes = [ip, ip, dp, dp, dp, dp, dp, dp, d, dp, dp]
         L.or_updt_rhs.argtypes = [ip, ip, ip, dp, dp, dp, dp]
         L.or_set_bc.argtypes = [C.c_char, i, ip, ip, i, i, d, d, dp]
+        L.or_cmpt_vorticity.argtypes = [ip, dp, dp, dp, dp, dp, dp, dp, dp, dp]
+        L.or_cmpt_strain_rate.argtypes = [ip, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
+        L.or_cmpt_rotation_rate.argtypes = [ip, dp, dp, dp, dp, dp, dp, dp]
+        L.or_cmpt_q_criterion.argtypes = [ip, dp, dp, dp]
         L.or_bounduvw_block.argtypes = [C.c_char_p, ip, ip, dp, i, ip, ip, i, dp, dp, dp, dp, dp, dp, dp, dp, dp]
         L.or_boundp_block.argtypes = [C.c_char_p, ip, ip, dp, ip, ip, i, dp, dp, dp, dp]
         L.or_r2r_lines.argtypes = [i, i, i, C.c_long, C.c_long, dp]

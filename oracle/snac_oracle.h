@@ -108,6 +108,14 @@ void or_bounduvw_block(const char cbc[3][3][2], const int lo[3], const int hi[3]
 void or_boundp_block(const char cbc[3][2], const int lo[3], const int hi[3], const double bc[3][2],
                      const int is_bound[3][2], const int nb[3][2], int myrank, const double *dxc,
                      const double *dyc, const double *dzc, double *p);
+void or_cmpt_vorticity(const int n[3], const double *dxc, const double *dyc, const double *dzc, const double *ux,
+                       const double *uy, const double *uz, double *vox, double *voy, double *voz);
+void or_cmpt_strain_rate(const int n[3], const double *dxc, const double *dyc, const double *dzc, const double *dxf,
+                         const double *dyf, const double *dzf, const double *ux, const double *uy, const double *uz,
+                         double *str);
+void or_cmpt_rotation_rate(const int n[3], const double *dxc, const double *dyc, const double *dzc, const double *ux,
+                           const double *uy, const double *uz, double *ens);
+void or_cmpt_q_criterion(const int n[3], const double *ens, const double *str, double *qcr);
 void or_init_bc_rhs(const char cbc[3][2], const double bc[3][2], const double dl[3][2],
                     const int is_bound[3][2], const int is_centered[3], const int lo[3],
                     const int hi[3], const int periods[3],

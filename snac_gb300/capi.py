@@ -97,6 +97,11 @@ PROTOTYPES = {
     "snac_chkdiv_noalloc": (C.c_int, [IP, IP, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_double, C.c_void_p, DP, DP]),
     "snac_set_bc": (C.c_int, [C.c_char, C.c_int, IP, IP, C.c_int, C.c_int, C.c_double, C.c_double, DP]),
+    "snac_cmpt_vorticity": (C.c_int, [IP, DP, DP, DP, DP, DP, DP, DP, DP, DP]),
+    "snac_cmpt_strain_rate": (C.c_int, [IP, DP, DP, DP, DP, DP, DP, DP, DP, DP, DP]),
+    "snac_cmpt_rotation_rate": (C.c_int, [IP, DP, DP, DP, DP, DP, DP, DP]),
+    "snac_cmpt_q_criterion": (C.c_int, [IP, DP, DP, DP]),
+    "snac_q_criterion": (C.c_int, [IP, DP, DP, DP, DP, DP, DP, DP, DP, DP, DP]),
     "snac_bounduvw": (C.c_int, [C.c_char_p, IP, IP, DP, C.c_int, IP, IP, C.c_int, DP, DP, DP, DP, DP, DP, DP, DP,
                                 DP]),
     "snac_boundp": (C.c_int, [C.c_char_p, IP, IP, DP, IP, IP, C.c_int, DP, DP, DP, DP]),

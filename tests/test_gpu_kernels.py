@@ -210,6 +210,32 @@ def test_bounduvw_boundp_block(snac_lib, oracle_mod, case, is_correc):
     np.testing.assert_array_equal(pgot, pref)
 
 
+def test_post_vorticity_strain_rotation_q(snac_lib, oracle_mod):
+    """post.f90:8-156 on the device against the oracle: vorticity, strain and rotation rates, the Q criterion
+    from the two rates and the one-pass Q criterion (the same expressions, so agreement to rounding)."""
+    rng = np.random.default_rng(140)
+    m = metrics(rng)  # dxc, dxf, dyc, dyf, dzc, dzf
+    dxc, dxf, dyc, dyf, dzc, dzf = m
+    u, v, w = (field(rng) for _ in range(3))
+    n = I3(N)
+    L, O = capi.lib(), oracle_mod.lib()
+    ref = [np.zeros(N, order="F") for _ in range(6)]
+    got = [np.zeros(N, order="F") for _ in range(7)]
+    O.or_cmpt_vorticity(n, P(dxc), P(dyc), P(dzc), P(u), P(v), P(w), P(ref[0]), P(ref[1]), P(ref[2]))
+    O.or_cmpt_strain_rate(n, P(dxc), P(dyc), P(dzc), P(dxf), P(dyf), P(dzf), P(u), P(v), P(w), P(ref[3]))
+    O.or_cmpt_rotation_rate(n, P(dxc), P(dyc), P(dzc), P(u), P(v), P(w), P(ref[4]))
+    O.or_cmpt_q_criterion(n, P(ref[4]), P(ref[3]), P(ref[5]))
+    capi.check(L.snac_cmpt_vorticity(n, P(dxc), P(dyc), P(dzc), P(u), P(v), P(w), P(got[0]), P(got[1]), P(got[2])))
+    capi.check(L.snac_cmpt_strain_rate(n, P(dxc), P(dyc), P(dzc), P(dxf), P(dyf), P(dzf), P(u), P(v), P(w),
+                                       P(got[3])))
+    capi.check(L.snac_cmpt_rotation_rate(n, P(dxc), P(dyc), P(dzc), P(u), P(v), P(w), P(got[4])))
+    capi.check(L.snac_cmpt_q_criterion(n, P(got[4]), P(got[3]), P(got[5])))
+    capi.check(L.snac_q_criterion(n, P(dxc), P(dyc), P(dzc), P(dxf), P(dyf), P(dzf), P(u), P(v), P(w), P(got[6])))
+    for g, r in zip(got[:6], ref):
+        close(g, r)
+    close(got[6], ref[5])
+
+
 @pytest.mark.parametrize("kind", ["R2HC", "HC2R", "REDFT10", "REDFT01", "REDFT11", "RODFT10", "RODFT01", "RODFT11",
                                   "REDFT00", "RODFT00"])
 @pytest.mark.parametrize("idir,n", [(1, 8), (2, 12), (3, 16), (3, 128), (3, 2), (1, 96), (2, 160), (3, 256),
