@@ -1,8 +1,8 @@
 // k_tma.cu -- fillps (fillps.f90:27-53) with its 3-D tiles staged through shared memory by TMA.
 //
 // Persistent CTAs walk a list of 32 x 8 x 4 output tiles over all blocks.  For each tile one thread issues
-// three tiled bulk-tensor copies (cp.async.bulk.tensor.3d) of u, v and w, each a 34 x 10 x 6 box of the
-// halo'd field (the tile plus one cell on every side) described by a tensor map per block and field, into
+// three tiled bulk-tensor copies (cp.async.bulk.tensor.3d) of u, v and w, each a 34 x 9 x 5 box of the
+// halo'd field (the tile plus the cells before it) described by a tensor map per block and field, into
 // one of two shared-memory stages; the copies complete on that stage's mbarrier (transaction bytes), so the
 // next tile streams in while the current one is computed.  The divergence of fillps then reads only shared
 // memory: the backward differences u(i)-u(i-1), v(j)-v(j-1), w(k)-w(k-1) of a thread's four cells along z.
@@ -29,9 +29,11 @@ struct TmaMaps {
 namespace {
 
 constexpr int FX = 32, FY = 8, FZ = 4;              // output tile (interior cells); FX x FY threads
-constexpr int BX = FX + 2, BY = FY + 2, BZ = FZ + 2;  // staged box: the tile and one cell on each side
-constexpr int BOX_BYTES = BX * BY * BZ * 8;          // 16,320 bytes of one field's box
-constexpr int BOX_PITCH = 16384;                     // box slot in shared memory (128-byte aligned)
+// staged box: the tile and the cell before it along each axis (fillps takes backward differences); x is one
+// cell wider still, so that the box row is a whole number of 16-byte units
+constexpr int BX = FX + 2, BY = FY + 1, BZ = FZ + 1;
+constexpr int BOX_BYTES = BX * BY * BZ * 8;          // 12,240 bytes of one field's box
+constexpr int BOX_PITCH = 12288;                     // box slot in shared memory (128-byte aligned)
 constexpr int STAGE_BYTES = 3 * BOX_PITCH;           // u, v, w
 constexpr int TMA_SMEM = 2 * STAGE_BYTES + 16;      // two stages and their mbarriers
 constexpr long TMA_POLLS = 1L << 24;
@@ -196,7 +198,7 @@ int tma_setup(Domain &d) {
   d.tma_tiles = dt;
   d.tma_ntiles = (int)tl.size();
   d.tma_err = derr;
-  d.tma_ctas = std::min(d.tma_ntiles, 2 * nsm);
+  d.tma_ctas = std::min(d.tma_ntiles, 3 * nsm);  // 74 KB of stages each: three CTAs per multiprocessor
   return SNAC_OK;
 }
 
