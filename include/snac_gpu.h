@@ -130,6 +130,8 @@ typedef struct snac_options {
   int mg_lnu;         /* first multigrid level that uses nu_coarse (default 2) */
   int tma;            /* -1: the fillps pass reads its fields directly instead of through TMA-staged tiles
                          (default: TMA where the blocks allow it: even x extents, at most 16 blocks) */
+  int pdl;            /* -1: the solver's inner-loop kernels launch without programmatic dependent launch
+                         (default: with it, each kernel's set-up overlapping the previous kernel's tail) */
 } snac_options;
 
 typedef struct snac_step_stats {

@@ -754,6 +754,7 @@ int snac_init(const snac_case *c, const snac_block_desc *blocks, const snac_opti
   snac_finalize();
   auto *d = new Domain();
   if (opt) d->opt = *opt;
+  g_pdl = d->opt.pdl == -1 ? 0 : 1;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { delete d; set_error("no CUDA device"); return SNAC_ERR_CUDA; }
   if (cudaSetDevice(d->opt.device) != cudaSuccess) { delete d; set_error("cannot select device %d", d->opt.device); return SNAC_ERR_CUDA; }

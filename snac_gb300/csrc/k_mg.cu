@@ -343,6 +343,7 @@ __device__ __forceinline__ bool cg_converged(SysScal &q, double rr, double tol) 
 //  * beta = r.z / r.z_old (0 on the first iteration).
 __global__ void k_cg_beta2(const int *active, const int *singular, SysScal *sc, const double *part_rz,
                            const double *part_z, const double *part_r, int nrz, long nact, int stride) {
+  pdl_enter();
   const int s = blockIdx.x;
   if (!active[s]) return;
   double rz = cta_sum_parts(part_rz, s, stride, nrz);
@@ -363,6 +364,7 @@ __global__ void k_cg_beta2(const int *active, const int *singular, SysScal *sc, 
 
 // convergence test after an update without a host check (k_cg_norms without the count), one CTA per system
 __global__ void k_cg_conv(int *active, SysScal *sc, const double *part_rr, int nrr, double tol, int stride) {
+  pdl_enter();
   const int s = blockIdx.x;
   if (!active[s]) return;
   const double rr = cta_sum_parts(part_rr, s, stride, nrr);
@@ -371,6 +373,7 @@ __global__ void k_cg_conv(int *active, SysScal *sc, const double *part_rr, int n
 
 // alpha = rz / p.q; one CTA per system
 __global__ void k_cg_alpha(const int *active, SysScal *sc, const double *part, int stride, int n) {
+  pdl_enter();
   const int s = blockIdx.x;
   if (active && !active[s]) return;
   const double pq = cta_sum_parts(part, s, stride, n);
@@ -437,6 +440,7 @@ __global__ void __launch_bounds__(256) k_cg_apply(MgLevelD L, MgGeom G, const T 
 template <typename T>
 __global__ void __launch_bounds__(256) k_cg_xr(long n, const int *active, const SysScal *sc, const T *p, const T *q,
                                                T *x, T *r, double *part_rr, int stride, int zero_x) {
+  pdl_enter();
   const int s = blockIdx.y;
   if (active && !active[s]) return;
   const T alpha = (T)sc[s].alpha;
@@ -462,6 +466,7 @@ __global__ void __launch_bounds__(256) k_cg_xr(long n, const int *active, const 
 __global__ void k_cg_norms(int *active, const int *src_active, SysScal *sc, const double *part_rr,
                            const double *part_bb, int stride, int n, double tol, int set_bb, int want_scale,
                            long nact, int *count, const SysScal *outer, double outer_tol) {
+  pdl_enter();
   const int s = blockIdx.x;
   if (src_active) {
     if (threadIdx.x == 0) active[s] = src_active[s];
@@ -548,6 +553,7 @@ __global__ void __launch_bounds__(256) k_sub_mean(MgLevelD L, const int *sing_li
 // mixed path: r32 = r64 / scale_s; e32 = 0; partials of r32.r32
 __global__ void __launch_bounds__(256) k_ir_down(long n, const int *active, const SysScal *sc, const double *r,
                                                  float *r32, float *e32, double *part, int stride) {
+  pdl_enter();
   const int s = blockIdx.y;
   if (active && !active[s]) return;
   const double inv = 1.0 / sc[s].scale;
@@ -568,6 +574,7 @@ __global__ void __launch_bounds__(256) k_ir_down(long n, const int *active, cons
 }
 __global__ void __launch_bounds__(256) k_ir_up(long n, const int *active, const SysScal *sc, const float *e32,
                                                double *x) {
+  pdl_enter();
   const int s = blockIdx.y;
   if (active && !active[s]) return;
   const double scale = sc[s].scale;
@@ -725,8 +732,8 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
     // singular systems: the search directions carry no constant (z's mean is left out of p), so x - x0 stays
     // mean-free, and r.z is taken with the projected z (r's mean is zero only up to rounding, and the V-cycle's
     // constant drift can be large)
-    k_cg_beta2<<<P.nsys, 256, 0, st>>>(W.active, P.singular, W.sc, W.part2, W.part3, W.part4, nrz, P.nact0,
-                                       W.stride), ::snac::count_launch();
+    SNAC_CUDA(launch_k(k_cg_beta2, dim3(P.nsys), dim3(256), 0, st, W.active, P.singular, W.sc, W.part2, W.part3,
+                       W.part4, nrz, P.nact0, W.stride));
     prof_begin(KID_CG_APPLY, st);
     if constexpr (fusep) {
       if (P.mode3d && sep_ok<T>(P))
@@ -747,14 +754,15 @@ int mg_pcg(const MgProblem &P, CgWork &W, T *x, int maxiter, double tol, bool ze
         SNAC_TRY((plane_apply<T, false>(P, shift, W.active, W.sc, z, p, nullptr, q, W.part1, W.stride, st)));
     }
     prof_end(KID_CG_APPLY, st);
-    k_cg_alpha<<<P.nsys, 256, 0, st>>>(W.active, W.sc, W.part1, W.stride, nred), ::snac::count_launch();
-    k_cg_xr<T><<<gf, 256, 0, st>>>(n, W.active, W.sc, p, q, x, r, W.part0, W.stride, (zero_x && it == 1) ? 1 : 0), ::snac::count_launch();
+    SNAC_CUDA(launch_k(k_cg_alpha, dim3(P.nsys), dim3(256), 0, st, W.active, W.sc, W.part1, W.stride, nred));
+    SNAC_CUDA(launch_k(k_cg_xr<T>, gf, dim3(256), 0, st, n, W.active, W.sc, p, q, x, r, W.part0, W.stride,
+                       (zero_x && it == 1) ? 1 : 0));
     if (check_host) {  // the host reads the count before the next iteration
       SNAC_CUDA(cudaMemsetAsync(W.d_count, 0, 2 * sizeof(int), st));
       k_cg_norms<<<P.nsys, 256, 0, st>>>(W.active, nullptr, W.sc, W.part0, nullptr, W.stride, nflat, tol, 0, 0, 0,
                                          W.d_count, nullptr, 0.0), ::snac::count_launch();
     } else if (it < maxiter) {  // converged systems leave the loop before the next V-cycle (no count needed)
-      k_cg_conv<<<P.nsys, 256, 0, st>>>(W.active, W.sc, W.part0, nflat, tol, W.stride), ::snac::count_launch();
+      SNAC_CUDA(launch_k(k_cg_conv, dim3(P.nsys), dim3(256), 0, st, W.active, W.sc, W.part0, nflat, tol, W.stride));
     }
     SNAC_CUDA(cudaGetLastError());
     trace("pcg: iteration", st);
@@ -780,7 +788,7 @@ int mg_ir_down(const MgProblem &P, const CgWork &Wout, CgWork &W32, const double
                double inner_tol, double outer_tol, cudaStream_t st) {
   const long n = P.L[0].ncell;
   const dim3 gf = grid_flat(n, P.nsys);
-  k_ir_down<<<gf, 256, 0, st>>>(n, Wout.active, Wout.sc, r64, r32, e32, W32.part0, W32.stride), ::snac::count_launch();
+  SNAC_CUDA(launch_k(k_ir_down, gf, dim3(256), 0, st, n, Wout.active, Wout.sc, r64, r32, e32, W32.part0, W32.stride));
   SNAC_CUDA(cudaMemsetAsync(W32.d_count, 0, 2 * sizeof(int), st));
   k_cg_norms<<<P.nsys, 256, 0, st>>>(W32.active, Wout.active, W32.sc, W32.part0, W32.part0, W32.stride, (int)gf.x,
                                      inner_tol, 1, 0, 0, W32.d_count, outer_tol > 0.0 ? Wout.sc : nullptr, outer_tol),
@@ -790,7 +798,7 @@ int mg_ir_down(const MgProblem &P, const CgWork &Wout, CgWork &W32, const double
 }
 int mg_ir_up(const MgProblem &P, const CgWork &Wout, const float *e32, double *x, cudaStream_t st) {
   const long n = P.L[0].ncell;
-  k_ir_up<<<grid_flat(n, P.nsys), 256, 0, st>>>(n, Wout.active, Wout.sc, e32, x), ::snac::count_launch();
+  SNAC_CUDA(launch_k(k_ir_up, grid_flat(n, P.nsys), dim3(256), 0, st, n, Wout.active, Wout.sc, e32, x));
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

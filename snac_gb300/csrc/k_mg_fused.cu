@@ -214,6 +214,7 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
       if (!active || active[q]) return q;
     return -1;
   };
+  pdl_enter();  // everything above reads constant tables only
   int cur = next_active((int)blockIdx.y), k = 0;
   if (cur >= 0) issue(cur, 0);
   while (cur >= 0) {
@@ -460,6 +461,7 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P
                                                                      T *__restrict__ xout, const T *__restrict__ bin) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T red[COARSE_THREADS];  // chunk sums of the dense coarsest solve
+  pdl_enter();
   const int s = blockIdx.x;
   if (active && !active[s]) return;
   const int last = P.nlev - 1;
@@ -757,14 +759,14 @@ static int launch_tile(const MgProblem &P, const MgLevelD &L, const MgLevelD &C,
   const dim3 g((unsigned)nt, (unsigned)((P.nsys + sb - 1) / sb));
   if (mode == 1) {
     SNAC_TRY(allow_smem((const void *)k_rbgs_tile2d<T, NW, R, 1>, smem));
-    k_rbgs_tile2d<T, NW, R, 1><<<g, NW * 32, smem, st>>>(L, C, P.periodic[0], P.periodic[1], active, P.nsys, sb,
-                                                         first_color, nhalf, x, b, xin, xc, part_bx, sing, part_x, part_b,
-                                                         part_stride), ::snac::count_launch();
+    SNAC_CUDA(launch_k(k_rbgs_tile2d<T, NW, R, 1>, g, dim3(NW * 32), smem, st, L, C, P.periodic[0], P.periodic[1],
+                       active, P.nsys, sb, first_color, nhalf, x, b, xin, xc, part_bx, sing, part_x, part_b,
+                       part_stride));
   } else {
     SNAC_TRY(allow_smem((const void *)k_rbgs_tile2d<T, NW, R, 0>, smem));
-    k_rbgs_tile2d<T, NW, R, 0><<<g, NW * 32, smem, st>>>(L, C, P.periodic[0], P.periodic[1], active, P.nsys, sb,
-                                                         first_color, nhalf, x, b, xin, xc, part_bx, sing, part_x, part_b,
-                                                         part_stride), ::snac::count_launch();
+    SNAC_CUDA(launch_k(k_rbgs_tile2d<T, NW, R, 0>, g, dim3(NW * 32), smem, st, L, C, P.periodic[0], P.periodic[1],
+                       active, P.nsys, sb, first_color, nhalf, x, b, xin, xc, part_bx, sing, part_x, part_b,
+                       part_stride));
   }
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -819,7 +821,7 @@ int launch_vcycle_coarse(const MgProblem &P, int l0, const T *shift, const int *
     }
   SNAC_TRY(allow_smem((const void *)k_vcycle_coarse<T>, smem));
   prof_begin(KID_COARSE, st);
-  k_vcycle_coarse<T><<<P.nsys, COARSE_THREADS, smem, st>>>(P, plan, l0, shift, active, x, b), ::snac::count_launch();
+  SNAC_CUDA(launch_k(k_vcycle_coarse<T>, dim3(P.nsys), dim3(COARSE_THREADS), smem, st, P, plan, l0, shift, active, x, b));
   prof_end(KID_COARSE, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;

@@ -92,6 +92,7 @@ __global__ void __launch_bounds__(256) k_p_restrict(MgLevelD F, MgLevelD C, int 
     }
   }
   const int cq = I + C.n[0] * J;
+  pdl_enter();  // the children's couplings above are constant tables
   for (int s = (int)blockIdx.z; s < nsys; s += (int)gridDim.z) {  // systems strided over the CTA groups
     if (active && !active[s]) continue;
     const long offf = F.ncell * (long)s, offc = C.ncell * (long)s;
@@ -162,6 +163,7 @@ __global__ void __launch_bounds__(256, (RR >= 4 ? 3 : 1)) k_p_resid(MgLevelD L, 
     }
   }
   const long chunk = blockIdx.x + (long)gridDim.x * blockIdx.y;
+  pdl_enter();
   for (int s = (int)blockIdx.z; s < nsys; s += (int)gridDim.z) {  // systems strided over the CTA groups
     if (active && !active[s]) continue;
     const long off = L.ncell * (long)s;
@@ -219,6 +221,7 @@ __global__ void __launch_bounds__(256) k_p_apply(MgLevelD L, int per0, int per1,
     }
   }
   const long chunk = blockIdx.x + (long)gridDim.x * blockIdx.y;
+  pdl_enter();
   for (int s = (int)blockIdx.z; s < nsys; s += (int)gridDim.z) {  // systems strided over the CTA groups
     if (active && !active[s]) continue;
     const long off = L.ncell * (long)s;
@@ -269,13 +272,13 @@ int plane_restrict(const MgProblem &P, int l, const T *shift, const int *active,
   prof_begin(KID_RESTRICT, st);
   const int e0 = C.coarsened[0] ? 2 : 1, e1 = C.coarsened[1] ? 2 : 1;
   if (e0 == 1 && e1 == 2)
-    k_p_restrict<T, 1, 2><<<gz, BLK, 0, st>>>(F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc), ::snac::count_launch();
+    SNAC_CUDA(launch_k(k_p_restrict<T, 1, 2>, gz, BLK, 0, st, F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc));
   else if (e0 == 2 && e1 == 1)
-    k_p_restrict<T, 2, 1><<<gz, BLK, 0, st>>>(F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc), ::snac::count_launch();
+    SNAC_CUDA(launch_k(k_p_restrict<T, 2, 1>, gz, BLK, 0, st, F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc));
   else if (e0 == 2 && e1 == 2)
-    k_p_restrict<T, 2, 2><<<gz, BLK, 0, st>>>(F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc), ::snac::count_launch();
+    SNAC_CUDA(launch_k(k_p_restrict<T, 2, 2>, gz, BLK, 0, st, F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc));
   else
-    k_p_restrict<T, 1, 1><<<gz, BLK, 0, st>>>(F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc), ::snac::count_launch();
+    SNAC_CUDA(launch_k(k_p_restrict<T, 1, 1>, gz, BLK, 0, st, F, C, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, xf, bf, bc, xc));
   prof_end(KID_RESTRICT, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -318,8 +321,8 @@ int plane_resid(const MgProblem &P, const T *shift, const int *active, const T *
   const dim3 g((unsigned)((L.n[0] + 31) / 32), (unsigned)((L.n[1] + 8 * RR - 1) / (8 * RR)), 1);
   const int sb = red_batch(P, (long)g.x * g.y);
   const dim3 gz(g.x, g.y, (unsigned)((P.nsys + sb - 1) / sb));
-  k_p_resid<T, RR><<<gz, BLK, 0, st>>>(L, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, x, b, r, part_rr,
-                                       part_bb, stride), ::snac::count_launch();
+  SNAC_CUDA(launch_k(k_p_resid<T, RR>, gz, BLK, 0, st, L, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, x, b,
+                     r, part_rr, part_bb, stride));
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -331,8 +334,8 @@ int plane_apply(const MgProblem &P, const T *shift, const int *active, const Sys
   const dim3 g((unsigned)((L.n[0] + 31) / 32), (unsigned)((L.n[1] + 8 * RROWS - 1) / (8 * RROWS)), 1);
   const int sb = red_batch(P, (long)g.x * g.y);
   const dim3 gz(g.x, g.y, (unsigned)((P.nsys + sb - 1) / sb));
-  k_p_apply<T, FUSEP><<<gz, BLK, 0, st>>>(L, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb, sc, z, po, pn,
-                                          q, part, stride), ::snac::count_launch();
+  SNAC_CUDA(launch_k(k_p_apply<T, FUSEP>, gz, BLK, 0, st, L, P.periodic[0], P.periodic[1], shift, active, P.nsys, sb,
+                     sc, z, po, pn, q, part, stride));
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

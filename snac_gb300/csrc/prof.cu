@@ -18,6 +18,7 @@ constexpr int PROF_MAX = 8192;
 }  // namespace
 
 static std::atomic<long long> g_launches{0};
+int g_pdl = 1;
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void add_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 bool prof_active() { return g_prof.kid != 0; }

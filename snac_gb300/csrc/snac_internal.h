@@ -14,6 +14,31 @@ namespace snac {
 // every kernel launch site appends ", count_launch()" to its launch expression
 void count_launch();
 
+// Programmatic dependent launch of the solver's inner-loop kernels (snac_options.pdl; on by default): the
+// launch lets the next kernel's CTAs be scheduled while this one drains, and every kernel launched this way
+// calls pdl_enter() before its first access to data an earlier kernel writes (griddepcontrol.wait waits for
+// the previous grid's completion and its memory), so only set-up work on constant tables overlaps.
+extern int g_pdl;
+template <typename... K, typename... A>
+inline cudaError_t launch_k(void (*kern)(K...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A &&...args) {
+  count_launch();
+  if (!g_pdl) {
+    kern<<<grid, block, smem, st>>>(static_cast<K>(args)...);
+    return cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, static_cast<K>(args)...);
+}
+
 void set_error(const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
 // SNAC_DEBUG=1 in the environment: every traced phase syncs the device and logs to stderr
