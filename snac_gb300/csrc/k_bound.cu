@@ -26,6 +26,7 @@ __device__ inline double *field_ptr(const DBlock &B, int f) {
 // copy the friend's interior plane into the ghost plane, for one axis
 __global__ void k_exchange(const DBlock *__restrict__ Bs, const FaceLink *__restrict__ F, const int *__restrict__ flds,
                            int a) {
+  pdl_enter();
   const FaceLink fl = F[blockIdx.y];
   const DBlock &D = Bs[fl.dst];
   const DBlock &S = Bs[fl.src];
@@ -46,6 +47,7 @@ __global__ void k_exchange(const DBlock *__restrict__ Bs, const FaceLink *__rest
 
 // set_bc on both faces of one axis; side 0 then side 1 by the same thread
 __global__ void k_setbc(const DBlock *__restrict__ Bs, const BcEntry *__restrict__ E, int a) {
+  pdl_enter();
   const BcEntry e = E[blockIdx.y];
   const DBlock &B = Bs[e.b];
   const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
@@ -85,7 +87,7 @@ int launch_exchange(const DBlock *dB, const FaceLink *dF, int nlinks, const int 
                     int maxplane, cudaStream_t st) {
   if (nlinks <= 0 || nflds <= 0) return SNAC_OK;
   dim3 g((maxplane + 255) / 256, nlinks, nflds);
-  k_exchange<<<g, 256, 0, st>>>(dB, dF, dflds, a), ::snac::count_launch();
+  SNAC_CUDA(launch_k(k_exchange, g, dim3(256), 0, st, dB, dF, dflds, a));
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -93,7 +95,7 @@ int launch_exchange(const DBlock *dB, const FaceLink *dF, int nlinks, const int 
 int launch_setbc(const DBlock *dB, const BcEntry *dE, int nent, int a, int maxplane, cudaStream_t st) {
   if (nent <= 0) return SNAC_OK;
   dim3 g((maxplane + 255) / 256, nent);
-  k_setbc<<<g, 256, 0, st>>>(dB, dE, a), ::snac::count_launch();
+  SNAC_CUDA(launch_k(k_setbc, g, dim3(256), 0, st, dB, dE, a));
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

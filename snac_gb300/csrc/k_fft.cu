@@ -315,6 +315,7 @@ __device__ __forceinline__ double *line_field(const DBlock &B, int field) {
 __global__ void k_fft_fwd_box(const DBlock *__restrict__ Bs, const int2 *__restrict__ LT, const int2 *__restrict__ boff,
                               const int2 *__restrict__ lext, LineGeom g, const double2 *__restrict__ tw,
                               const double *__restrict__ mat, double *__restrict__ box) {
+  pdl_enter();
   extern __shared__ double smem[];
   const int2 lt = LT[blockIdx.x];
   const DBlock &B = Bs[lt.x];
@@ -350,6 +351,7 @@ __global__ void k_fft_fwd_box(const DBlock *__restrict__ Bs, const int2 *__restr
 __global__ void k_fft_bwd_box(const DBlock *__restrict__ Bs, const int2 *__restrict__ LT, const int2 *__restrict__ boff,
                               const int2 *__restrict__ lext, LineGeom g, const double2 *__restrict__ tw,
                               const double *__restrict__ mat, const double *__restrict__ box, double normfft) {
+  pdl_enter();
   extern __shared__ double smem[];
   const int2 lt = LT[blockIdx.x];
   const DBlock &B = Bs[lt.x];
@@ -597,9 +599,8 @@ int fft_forward_to_box(Domain &d, PoissonSolver &S, cudaStream_t st) {
   FftLaunch L;
   SNAC_TRY(prep_launch(g.n, L, (const void *)k_fft_fwd_box, S.use_fft == 2 ? S.nfft_c : 0));
   prof_begin(KID_FFT_FWD, st);
-  k_fft_fwd_box<<<S.nlt, 256, L.smem, st>>>(d.d_db, S.d_lt, S.d_boff, S.d_lext, g,
-                                            (const double2 *)(S.use_fft == 2 ? S.d_gt_fwd : S.d_tw), S.d_mat_fwd,
-                                            S.box_b), ::snac::count_launch();
+  SNAC_CUDA(launch_k(k_fft_fwd_box, dim3(S.nlt), dim3(256), L.smem, st, d.d_db, S.d_lt, S.d_boff, S.d_lext, g,
+                     (const double2 *)(S.use_fft == 2 ? S.d_gt_fwd : S.d_tw), S.d_mat_fwd, S.box_b));
   prof_end(KID_FFT_FWD, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -611,9 +612,8 @@ int fft_backward_from_box(Domain &d, PoissonSolver &S, cudaStream_t st) {
   FftLaunch L;
   SNAC_TRY(prep_launch(g.n, L, (const void *)k_fft_bwd_box, S.use_fft == 2 ? S.nfft_c : 0));
   prof_begin(KID_FFT_BWD, st);
-  k_fft_bwd_box<<<S.nlt, 256, L.smem, st>>>(d.d_db, S.d_lt, S.d_boff, S.d_lext, g,
-                                            (const double2 *)(S.use_fft == 2 ? S.d_gt_bwd : S.d_tw), S.d_mat_bwd,
-                                            S.box_x, S.normfft), ::snac::count_launch();
+  SNAC_CUDA(launch_k(k_fft_bwd_box, dim3(S.nlt), dim3(256), L.smem, st, d.d_db, S.d_lt, S.d_boff, S.d_lext, g,
+                     (const double2 *)(S.use_fft == 2 ? S.d_gt_bwd : S.d_tw), S.d_mat_bwd, S.box_x, S.normfft));
   prof_end(KID_FFT_BWD, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;

@@ -30,6 +30,7 @@ namespace snac {
 // values, so the write-back is a second, memory-only pass) and dudtrko in place.
 __global__ void __launch_bounds__(TX * TY * TZ)
 k_rk_mom(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, RkMomParams prm) {
+  pdl_enter();
   TILE_SETUP
   const long sy = nx + 2, sz = (long)(nx + 2) * (ny + 2);
   const long c = hidx(i, j, k, nx, ny);
@@ -125,6 +126,7 @@ k_rk_mom(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, RkMomParams 
 
 __global__ void __launch_bounds__(TX * TY * TZ)
 k_rk_mom_writeback(const DBlock *__restrict__ Bs, const Tile *__restrict__ T) {
+  pdl_enter();
   TILE_SETUP
   const long c = hidx(i, j, k, nx, ny), ci = iidx(i, j, k, nx, ny);
   B.u[c] = B.nu[ci];
@@ -135,14 +137,14 @@ k_rk_mom_writeback(const DBlock *__restrict__ Bs, const Tile *__restrict__ T) {
 int launch_rk_mom(const DBlock *dB, const Tile *dT, int ntiles, const RkMomParams &prm, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
   prof_begin(KID_RK_MOM, st);
-  k_rk_mom<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, prm), ::snac::count_launch();
+  SNAC_CUDA(launch_k(k_rk_mom, dim3(ntiles), dim3(TX, TY, TZ), 0, st, dB, dT, prm));
   prof_end(KID_RK_MOM, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
 int launch_rk_mom_writeback(const DBlock *dB, const Tile *dT, int ntiles, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
-  k_rk_mom_writeback<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT), ::snac::count_launch();
+  SNAC_CUDA(launch_k(k_rk_mom_writeback, dim3(ntiles), dim3(TX, TY, TZ), 0, st, dB, dT));
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }
@@ -229,6 +231,7 @@ int launch_bulk_forcing_s(const DBlock *dB, const Tile *dT, int ntiles, int sidx
 // ---------------------------------------------------------------- fillps (fillps.f90:27-53)
 __global__ void __launch_bounds__(TX * TY * TZ)
 k_fillps(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, double rdt, int fft_axis) {
+  pdl_enter();
   TILE_SETUP
   const long sy = nx + 2, sz = (long)(nx + 2) * (ny + 2);
   const long c = hidx(i, j, k, nx, ny);
@@ -247,7 +250,7 @@ k_fillps(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, double rdt, 
 int launch_fillps(const DBlock *dB, const Tile *dT, int ntiles, double dt, int fft_axis, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
   prof_begin(KID_FILLPS, st);
-  k_fillps<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, 1.0 / dt, fft_axis), ::snac::count_launch();
+  SNAC_CUDA(launch_k(k_fillps, dim3(ntiles), dim3(TX, TY, TZ), 0, st, dB, dT, 1.0 / dt, fft_axis));
   prof_end(KID_FILLPS, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -257,6 +260,7 @@ int launch_fillps(const DBlock *dB, const Tile *dT, int ntiles, double dt, int f
 // Tiles cover the halo'd extent: i,j,k here run over -1..n (tile origins shifted by -1).
 __global__ void __launch_bounds__(TX * TY * TZ)
 k_correc(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, double dt) {
+  pdl_enter();
   const Tile t = T[blockIdx.x];
   const DBlock &B = Bs[t.x];
   const int nx = B.n[0], ny = B.n[1], nz = B.n[2];
@@ -273,7 +277,7 @@ k_correc(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, double dt) {
 int launch_correc(const DBlock *dB, const Tile *dT, int ntiles, double dt, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
   prof_begin(KID_CORREC, st);
-  k_correc<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, dt), ::snac::count_launch();
+  SNAC_CUDA(launch_k(k_correc, dim3(ntiles), dim3(TX, TY, TZ), 0, st, dB, dT, dt));
   prof_end(KID_CORREC, st);
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
@@ -282,6 +286,7 @@ int launch_correc(const DBlock *dB, const Tile *dT, int ntiles, double dt, cudaS
 // ---------------------------------------------------------------- updt_pressure (updt_pressure.f90:21-46)
 __global__ void __launch_bounds__(TX * TY * TZ)
 k_updt_pressure(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, double alpha, int impdiff) {
+  pdl_enter();
   TILE_SETUP
   const long c = hidx(i, j, k, nx, ny);
   const double *__restrict__ pp = B.pp;
@@ -299,7 +304,7 @@ k_updt_pressure(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, doubl
 
 int launch_updt_pressure(const DBlock *dB, const Tile *dT, int ntiles, double alpha, int impdiff, cudaStream_t st) {
   if (ntiles <= 0) return SNAC_OK;
-  k_updt_pressure<<<ntiles, dim3(TX, TY, TZ), 0, st>>>(dB, dT, alpha, impdiff), ::snac::count_launch();
+  SNAC_CUDA(launch_k(k_updt_pressure, dim3(ntiles), dim3(TX, TY, TZ), 0, st, dB, dT, alpha, impdiff));
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;
 }

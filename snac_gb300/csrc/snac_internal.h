@@ -19,6 +19,12 @@ void count_launch();
 // calls pdl_enter() before its first access to data an earlier kernel writes (griddepcontrol.wait waits for
 // the previous grid's completion and its memory), so only set-up work on constant tables overlaps.
 extern int g_pdl;
+// A kernel launched by launch_k waits here for the grid before it (and its memory), then lets the next one be
+// scheduled; a no-op for a kernel launched without the programmatic-serialization attribute.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
 template <typename... K, typename... A>
 inline cudaError_t launch_k(void (*kern)(K...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A &&...args) {
   count_launch();

@@ -160,13 +160,6 @@ __device__ __forceinline__ T plane_acc(const PlaneCell<T> &P, V v) {
   return fmat(P.cs, v(P.is), acc);
 }
 
-// A kernel launched by launch_k waits here for the grid before it (and its memory), then lets the next one be
-// scheduled; a no-op for a kernel launched without the programmatic-serialization attribute.
-__device__ __forceinline__ void pdl_enter() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
 // Level kernels run on (32, 8) blocks: grid.z is the system (plane mode) or the k plane (3-D mode).
 __device__ __forceinline__ void zpos(const MgGeom &G, int &k, int &s) {
   if (G.mode3d) { k = blockIdx.z; s = 0; }
