@@ -402,8 +402,7 @@ __device__ __forceinline__ void cta_sweep_pairs(int n0, int n1, int per0, int pe
     const int wrap_n = per1 ? n0 - n0 * n1 : 0, wrap_s = per1 ? n0 * (n1 - 1) : 0;
     // a missing east/north neighbour has a zero (folded) coupling c0[c] / c1[c]; a missing west/south one
     // has none to read, so its coupling is taken as zero here
-#pragma unroll 4
-    for (int j = g; j < n1; j += G) {  // unrolled: the rows' coupling loads (global on the finest level) overlap
+    for (int j = g; j < n1; j += G) {
       const int e = (color + j) & 1;
       const int c = j * n0 + 2 * p + e;
       const int oe = e ? ee1 : 1, ow = e ? -1 : we0;
