@@ -39,7 +39,8 @@ constexpr int TSW = 64;            // tile width
 constexpr int TBX = TSW - 2 * TH;  // output columns per tile
 // tile shapes: NW warps x R rows per warp = tile height SH (output rows SH - 2 TH)
 struct TileShape { int nw, r; };
-const TileShape SHAPES_F[] = {{8, 2}, {8, 3}, {16, 2}, {16, 3}};  // snac_options.mg_tile 1..4
+const TileShape SHAPES_F[] = {{8, 2}, {8, 3}, {16, 2}, {16, 3}, {8, 4}, {16, 4}};  // snac_options.mg_tile 1..6
+constexpr int NSHAPES_F = 6;
 const TileShape SHAPES_D[] = {{8, 2}};
 inline int tile_by(TileShape t) { return t.nw * t.r - 2 * TH; }
 inline int tiles_for(const MgLevelD &L, TileShape t) {
@@ -48,9 +49,9 @@ inline int tiles_for(const MgLevelD &L, TileShape t) {
 // the shape given by `pref` (1..4, FP32 only), else the one that processes the fewest tile rows (ties: the
 // smaller tile)
 TileShape choose_shape(const MgLevelD &L, int prec, int pref) {
-  if (!prec && pref >= 1 && pref <= 4) return SHAPES_F[pref - 1];
+  if (!prec && pref >= 1 && pref <= NSHAPES_F) return SHAPES_F[pref - 1];
   const TileShape *opts = prec ? SHAPES_D : SHAPES_F;
-  const int nopt = prec ? 1 : 4;
+  const int nopt = prec ? 1 : 4;  // the default choice among the first four (the 4-row shapes are tuning options)
   TileShape best = opts[0];
   long bestc = -1;
   for (int q = 0; q < nopt; q++) {
@@ -71,7 +72,7 @@ __device__ __forceinline__ int wrap(int g, int n) {
 // the FP32 tile shape level l of P uses, as snac_options.mg_tile (1..4)
 int tile2d_shape_index(const MgProblem &P, int l) {
   const TileShape t = choose_shape(P.L[l], 0, P.tile_shape);
-  for (int q = 0; q < 4; q++)
+  for (int q = 0; q < NSHAPES_F; q++)
     if (SHAPES_F[q].nw == t.nw && SHAPES_F[q].r == t.r) return q + 1;
   return 0;
 }
@@ -791,10 +792,14 @@ int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_c
       rc = launch_tile<T, 8, 2>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_x, part_b, part_stride, st);
     else if (t.nw == 16 && t.r == 2)
       rc = launch_tile<T, 16, 2>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_x, part_b, part_stride, st);
-    else if (t.nw == 8)
+    else if (t.nw == 8 && t.r == 3)
       rc = launch_tile<T, 8, 3>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_x, part_b, part_stride, st);
-    else
+    else if (t.nw == 16 && t.r == 3)
       rc = launch_tile<T, 16, 3>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_x, part_b, part_stride, st);
+    else if (t.nw == 8)
+      rc = launch_tile<T, 8, 4>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_x, part_b, part_stride, st);
+    else
+      rc = launch_tile<T, 16, 4>(P, L, C, nt, 2 * mg_nu(P, l), active, first_color, mode, x, b, xin, xc, part_bx, part_x, part_b, part_stride, st);
   }
   prof_end(KID_RBGS, st);
   SNAC_TRY(rc);

@@ -199,7 +199,7 @@ int snac_autotune(int steps, snac_tune_result *out) {
   int rc = try_group(g);
   if (rc == SNAC_OK && found && plane) {
     g.clear();
-    for (int t = 1; t <= 4; t++) { snac_options o = best_opt; o.mg_tile = t; g.push_back(o); }
+    for (int t = 1; t <= 6; t++) { snac_options o = best_opt; o.mg_tile = t; g.push_back(o); }
     rc = try_group(g);
   }
   if (rc == SNAC_OK && found && plane) {
