@@ -11,7 +11,9 @@ field: laminar Poiseuille profile scaled to U_b plus seeded uniform noise of
 A "step" is one full RK3 step (3 stages: momentum, halo/BC, divergence,
 transform, 128 batched 2-D solves, back-transform, projection, pressure
 update; chkdt every icheck=10 steps).  `value` is the mixed path (FP32 V-cycles
-inside FP64 refinement); the plain FP64 path and the mixed path with the learned
+inside FP64 refinement, with the solver settings snac_autotune picks after the warm-up steps: tile
+shape, CTA waves, inner iterations, coarse sweeps); the plain FP64 path (library defaults) and the mixed
+path with the learned
 initial guess (pairs recorded from 8 steps, the network trained on the GPU, then
 timed) are reported beside it at the same solver tolerance.  Inputs (~0.5 GB of
 fields + solver vectors) exceed L2.
@@ -216,9 +218,10 @@ def init_dhc(dom, case):
     dom.boundp(capi.S0)
 
 
-def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0, init=None, **solver):
+def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0, init=None, tune=0, **solver):
     """solver: snac_options fields passed to the domain (the library defaults when absent); init(dom, case)
-    sets the initial state (default: the channel's)."""
+    sets the initial state (default: the channel's); tune > 0: snac_autotune with that many timed steps per
+    candidate after the warm-up (its choice is returned in `tuned`, as snac_options fields)."""
     from snac_gb300 import capi
     from snac_gb300.domain import Domain
     case = case_fn()
@@ -228,6 +231,14 @@ def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0, init=
     try:
         (init or init_channel)(dom, case)
         dom.step(warmup, allow_not_converged=True)
+        tuned = None
+        if tune:
+            r = dom.autotune(tune)
+            tuned = dict(precision=r["precision"], inner_iters=r["inner_iters"], nu_coarse=r["nu_coarse"],
+                         mg_tile=r["mg_tile"], mg_waves=r["mg_waves"], mg_cta_level=r["mg_cta_level"],
+                         refine_steps=r["refine_steps"], ms_before=r["ms_before"], ms_tuned=r["ms_per_step"],
+                         candidates=r["candidates"])
+            dom.step(1, allow_not_converged=True)
         L = capi.lib()
         if profile_kid:
             capi.check(L.snac_profile_kernel(profile_kid))
@@ -249,12 +260,12 @@ def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0, init=
         ke = dom.kinetic_energy()
         return dict(ms=st["device_ms"] / steps, iters=st["iters"], residual=st["residual"], divmax=divmax, ke=ke,
                     rc=rc, prof=prof, ncell=case.ncell, dt=st["dt"], launches=n1.value - n0.value,
-                    helm_iters=st["helm_iters"], helm_residual=st["helm_residual"], setup_s=setup_s)
+                    helm_iters=st["helm_iters"], helm_residual=st["helm_residual"], setup_s=setup_s, tuned=tuned)
     finally:
         dom.close()
 
 
-def run_learned_path(case_fn, steps, warmup, device, record=8, train_iters=1500, lr=2e-3):
+def run_learned_path(case_fn, steps, warmup, device, record=8, train_iters=1500, lr=2e-3, **solver):
     """Mixed path with the learned initial guess: pairs recorded from `record` steps after the warm-up, the
     network trained on the GPU, then `steps` timed steps with the guess applied (and one more that measures
     the residual it leaves relative to the previous solution's, per wavenumber system)."""
@@ -262,7 +273,7 @@ def run_learned_path(case_fn, steps, warmup, device, record=8, train_iters=1500,
     from snac_gb300.domain import Domain
     case = case_fn()
     L = capi.lib()
-    dom = Domain(case, precision=1, device=device, use_graph=USE_GRAPH)
+    dom = Domain(case, precision=1, device=device, use_graph=USE_GRAPH, **solver)
     try:
         init_channel(dom, case)
         dom.step(warmup, allow_not_converged=True)
@@ -296,7 +307,7 @@ def bench_smoother(case_fn, device, levels=(0, 1, 2), reps=20):
     from snac_gb300 import capi
     from snac_gb300.domain import Domain
     case = case_fn()
-    dom = Domain(case, precision=1, device=device)
+    dom = Domain(case, precision=1, device=device, **solver)
     out = {}
     try:
         init_channel(dom, case)
@@ -320,14 +331,14 @@ def ncu_traffic(kernel):
         return None
 
 
-def run_e2e(case_fn, precision, steps, device):
+def run_e2e(case_fn, precision, steps, device, **solver):
     """Through the C ABI with host buffers: upload u,v,w,p of every block from pinned host memory in one
     snac_set_fields call, one step, read them back with snac_get_fields."""
     import torch
     from snac_gb300 import capi
     from snac_gb300.domain import Domain
     case = case_fn()
-    dom = Domain(case, precision=precision, device=device, use_graph=USE_GRAPH if precision else 0)
+    dom = Domain(case, precision=precision, device=device, use_graph=USE_GRAPH if precision else 0, **solver)
     try:
         init_channel(dom, case)
         dom.step(1, allow_not_converged=True)
@@ -392,6 +403,9 @@ def main():
     ap.add_argument("--configs", default="c1_ldc64,c2_tgv128,c4_lbox,c5_dhc512",
                     help="other reference configurations timed beside the headline (comma list; empty: none)")
     ap.add_argument("--config-steps", type=int, default=3, help="timed steps per configuration and path")
+    ap.add_argument("--tune", type=int, default=3,
+                    help="snac_autotune with this many timed steps per candidate before the headline path is "
+                         "timed (0: the library defaults)")
     ap.add_argument("--only", choices=["mixed", "plain", "learned"], default=None,
                     help="run one path once and print its timing only (used for ncu launch lists; learned: "
                          "1 recorded step and 20 training iterations)")
@@ -447,25 +461,29 @@ def main():
     plain = run_gpu_path(case_fn, 0, args.steps, args.warmup, device)
     # mixed path, the headline; clocks sampled over its timed region
     sampler.start()
-    mixed = run_gpu_path(case_fn, 1, args.steps, args.warmup, device)
+    mixed = run_gpu_path(case_fn, 1, args.steps, args.warmup, device, tune=args.tune)
     clocks = sampler.stop()
+    # the settings the autotuner chose (tile shape, waves, coarse-cycle level, inner iterations ...) for every
+    # further run of the mixed path
+    opts = {k: mixed["tuned"][k] for k in ("inner_iters", "nu_coarse", "mg_tile", "mg_waves", "mg_cta_level",
+                                           "refine_steps")} if mixed["tuned"] else {}
     # live CUDA-event timing of the kernel classes over timed runs of the mixed path
     shares = {}
     for kid, name in ((10, "pressure_solve"), (2, "smoother"), (9, "coarse_vcycle"), (3, "restriction"),
                       (6, "operator_apply"), (1, "k_rk_mom"), (4, "fft_forward_box")):
-        n, tot = run_gpu_path(case_fn, 1, args.steps, args.warmup, device, profile_kid=kid)["prof"]
+        n, tot = run_gpu_path(case_fn, 1, args.steps, args.warmup, device, profile_kid=kid, **opts)["prof"]
         shares[name] = {"launches_per_step": n / args.steps, "ms_per_step": tot / args.steps,
                         "mean_launch_ms": tot / max(n, 1)}
     prof_mom = (shares["k_rk_mom"]["launches_per_step"] * args.steps, shares["k_rk_mom"]["ms_per_step"] * args.steps)
-    learned = run_learned_path(case_fn, args.steps, args.warmup, device) if not args.no_learned else None
-    smoother = bench_smoother(case_fn, device)
+    learned = run_learned_path(case_fn, args.steps, args.warmup, device, **opts) if not args.no_learned else None
+    smoother = bench_smoother(case_fn, device, **opts)
     ms = mixed["ms"]
     ms = max_over_ranks(ms, device)
     ncell = mixed["ncell"]
     value = world * ncell / (ms * 1e-3) / 1e6
     e2e = None
     if not args.no_e2e:
-        e = run_e2e(case_fn, 1, max(2, min(args.steps, 5)), device)
+        e = run_e2e(case_fn, 1, max(2, min(args.steps, 5)), device, **opts)
         e2e = {"value": world * e["ncell"] / e["s_per_step"] / 1e6, "unit": "Mcells/s",
                "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"],
                "ms_per_step": 1e3 * e["s_per_step"]}
@@ -517,13 +535,14 @@ def main():
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
             "paths": {"mixed": {"ms_per_step": mixed["ms"], "max_div_u": mixed["divmax"],
                                 "solve_iters_max": mixed["iters"], "solve_residual_max": mixed["residual"],
-                                "kinetic_energy": mixed["ke"]},
+                                "kinetic_energy": mixed["ke"], "autotuned": mixed["tuned"]},
                       "plain_fp64": {"ms_per_step": plain["ms"], "max_div_u": plain["divmax"],
                                      "solve_iters_max": plain["iters"], "solve_residual_max": plain["residual"],
                                      "kinetic_energy": plain["ke"]},
                       "speedup_mixed_vs_plain": plain["ms"] / mixed["ms"],
                       "learned_mixed": learned,
-                      "headline_path": "mixed (the learned guess is measured beside it and left off: it lowers "
+                      "headline_path": "mixed, with the settings snac_autotune chose after the warm-up (the "
+                                       "learned guess is measured beside it and left off: it lowers "
                                        "the starting residual but not the refinement-step count)"},
             "roofline": roof if roof else roof_mom, "roofline_rk_mom": roof_mom,
             "gpu_launches": mixed["launches"], "gpu_launches_per_step": mixed["launches"] / args.steps,
