@@ -301,7 +301,7 @@ def run_learned_path(case_fn, steps, warmup, device, record=8, train_iters=1500,
         dom.close()
 
 
-def bench_smoother(case_fn, device, levels=(0, 1, 2), reps=20):
+def bench_smoother(case_fn, device, levels=(0, 1, 2), reps=20, **solver):
     """CUDA-event timing of the FP32 tiled pre-smoother (the dominant kernel) on the bench workload,
     inputs resident in HBM, all systems active: ms and algorithmic bytes per launch per level."""
     from snac_gb300 import capi
