@@ -354,13 +354,31 @@ int snac_cnn_set_poll_limit(long polls);
 int snac_guess_grad(const float *x, const float *target, int nb, int H, int W, const float *params, float *grads,
                     double *loss);
 
-/* No counterpart in the reference: the learned initial guess of the plane-mode pressure solve.  mode 0 off;
- * 1 every pressure solve of snac_step records its (residual of the previous solution, correction) pairs
- * for training; 2 every solve starts from the previous solution plus the network's correction (the
- * multigrid then iterates to the same tolerance).  Not available with the 3-D solve (SNAC_ERR_UNSUPPORTED). */
+/* No counterpart in the reference: the three-level U-Net of the learned guess of the 3-D pressure solve
+ * (about 180k parameters: conv 3x3x3 16->16, pool, 16->32, pool, 32->64, [up | skip] 96->32, [up | skip]
+ * 48->16, head 1x1x1 16->1; BF16 tensor-core operands, FP32 accumulation).  snac_unet_nparams gives the
+ * parameter count.  snac_unet_forward runs it on host data: x nb x 2 x n2 x n1 x n0 (residual, live mask
+ * 0/1), params as the oracle lays them out; out nb x n2 x n1 x n0.  snac_unet_grad also returns the loss
+ * (1/nb) sum_b sum_live (out - t)^2 / sum_live t^2 and its gradient with respect to every parameter.
+ * snac_unet_set_poll_limit is the testing hook of the convolutions' bounded accumulator wait (as
+ * snac_cnn_set_poll_limit). */
+int snac_unet_nparams(void);
+int snac_unet_forward(const float *x, int nb, int n0, int n1, int n2, const float *params, float *out);
+int snac_unet_grad(const float *x, const float *target, int nb, int n0, int n1, int n2, const float *params,
+                   float *grads, double *loss);
+int snac_unet_set_poll_limit(long polls);
+
+/* No counterpart in the reference: the learned initial guess of the pressure solve.  mode 0 off;
+ * 1 every pressure solve of snac_step records training pairs (the residual of the previous solution and
+ * the diagonally scaled correction the solve made: whole wavenumber planes with a transform axis, random
+ * 32^3 crops with the 3-D solve); 2 every solve starts from the previous solution plus the network's
+ * correction, scaled by the step that minimises the residual (the multigrid then iterates to the same
+ * tolerance).  With a transform axis the network is the plane network of snac_guess_grad, with the 3-D
+ * solve the U-Net of snac_unet_forward. */
 int snac_guess_mode(int mode);
-/* trains the network on the recorded pairs on the GPU: iters Adam steps of 16-plane batches at learning
- * rate lr; returns the mean batch loss of the first and last few steps and the number of recorded pairs */
+/* trains the network on the recorded pairs on the GPU: iters Adam steps at learning rate lr (16-plane
+ * batches; 3-D solve: 4 crops); returns the mean batch loss of the first and last few steps and the number
+ * of recorded pairs */
 int snac_guess_train(int iters, double lr, double *loss_first, double *loss_last, int *pairs);
 /* with on != 0 every guided solve also measures |b - A x0| / |b - A x_prev| per non-singular system; returns
  * the median and largest ratio of the last guided solve */

@@ -139,6 +139,10 @@ PROTOTYPES = {
     "snac_cnn_conv3x3": (C.c_int, [FP, C.c_int, C.c_int, C.c_int, FP, FP, C.c_int, FP]),
     "snac_cnn_set_poll_limit": (C.c_int, [C.c_long]),
     "snac_guess_grad": (C.c_int, [FP, FP, C.c_int, C.c_int, C.c_int, FP, FP, DP]),
+    "snac_unet_nparams": (C.c_int, []),
+    "snac_unet_forward": (C.c_int, [FP, C.c_int, C.c_int, C.c_int, C.c_int, FP, FP]),
+    "snac_unet_grad": (C.c_int, [FP, FP, C.c_int, C.c_int, C.c_int, C.c_int, FP, FP, DP]),
+    "snac_unet_set_poll_limit": (C.c_int, [C.c_long]),
     "snac_guess_mode": (C.c_int, [C.c_int]),
     "snac_guess_train": (C.c_int, [C.c_int, C.c_double, DP, DP, IP]),
     "snac_guess_measure": (C.c_int, [C.c_int, DP, DP]),

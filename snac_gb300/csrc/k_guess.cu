@@ -1,4 +1,5 @@
-// k_guess.cu -- the learned initial guess of the plane-mode pressure solve.
+// k_guess.cu -- the learned initial guess of the plane-mode pressure solve (the 3-D solve's U-Net is in
+// k_unet.cu; this file's entry points hand the 3-D case to it).
 //
 // A three-layer convolutional network (3x3, 16 channels, ReLU between layers) maps the residual of the
 // previous solution, r0 = b - A x_prev, of one wavenumber system (normalised by its RMS) and the system's
@@ -420,6 +421,7 @@ struct GuessState {
   // systems the network corrected in the last solve (median and largest)
   int measure = 0;
   double ratio_median = 0.0, ratio_max = 0.0;
+  Guess3 *g3 = nullptr;  // the 3-D solve's U-Net and its recorded crops
   std::vector<void *> mem;
   void *alloc(size_t bytes) {
     void *p = nullptr;
@@ -428,7 +430,10 @@ struct GuessState {
     mem.push_back(p);
     return p;
   }
-  ~GuessState() { for (void *p : mem) cudaFree(p); }
+  ~GuessState() {
+    guess3_destroy(g3);
+    for (void *p : mem) cudaFree(p);
+  }
 };
 
 void guess_destroy(GuessState *g) { delete g; }
@@ -477,7 +482,13 @@ static int guess_setup(PoissonSolver &S, GuessState &g) {
 int guess_before(Domain &d, PoissonSolver &S, cudaStream_t st) {
   GuessState *g = d.guess;
   if (!g || g->mode == 0) return SNAC_OK;
-  if (S.mode3d) { set_error("the learned guess is built for the plane (transform-axis) pressure solve"); return SNAC_ERR_UNSUPPORTED; }
+  if (S.mode3d) {
+    if (!g->g3) g->g3 = guess3_create();
+    double ratio = 0.0;
+    SNAC_TRY(guess3_before(S, *g->g3, g->mode, g->measure, &ratio, st));
+    if (g->mode == 2 && g->measure) g->ratio_median = g->ratio_max = ratio;
+    return SNAC_OK;
+  }
   SNAC_TRY(guess_setup(S, *g));
   const MgProblem &P = S.P;
   const int stride = mg_partial_stride(P);
@@ -522,6 +533,7 @@ int guess_before(Domain &d, PoissonSolver &S, cudaStream_t st) {
 int guess_after(Domain &d, PoissonSolver &S, cudaStream_t st) {
   GuessState *g = d.guess;
   if (!g || g->mode != 1) return SNAC_OK;
+  if (S.mode3d) return g->g3 ? guess3_after(S, *g->g3, st) : SNAC_OK;
   const MgProblem &P = S.P;
   const MgLevelD &L = P.L[0];
   k_gn_target<<<g->nsys, 256, 0, st>>>(S.box_x, g->xprev, g->rms, g->sys, L.code, P.shift, L.w01, L.cc, g->ncell,
@@ -555,7 +567,6 @@ int snac_guess_mode(int mode) {
   Domain *d = domain();
   if (!d) { set_error("snac_guess_mode: no domain (call snac_init first)"); return SNAC_ERR_STATE; }
   if (mode < 0 || mode > 2) { set_error("snac_guess_mode: mode must be 0, 1 or 2"); return SNAC_ERR_ARG; }
-  if (mode && d->ps->mode3d) { set_error("the learned guess is built for the plane (transform-axis) pressure solve"); return SNAC_ERR_UNSUPPORTED; }
   if (!d->guess) d->guess = new GuessState();
   d->guess->mode = mode;
   return SNAC_OK;
@@ -572,6 +583,10 @@ int snac_guess_measure(int on, double *ratio_median, double *ratio_max) {
 
 int snac_guess_train(int iters, double lr, double *loss_first, double *loss_last, int *pairs) {
   Domain *d = domain();
+  if (d && d->guess && d->ps->mode3d) {
+    if (!d->guess->g3) { set_error("snac_guess_train: no recorded pairs"); return SNAC_ERR_STATE; }
+    return guess3_train(*d->guess->g3, iters, lr, loss_first, loss_last, pairs, d->st);
+  }
   if (!d || !d->guess || d->guess->count == 0) { set_error("snac_guess_train: no recorded pairs"); return SNAC_ERR_STATE; }
   GuessState &g = *d->guess;
   cudaStream_t st = d->st;

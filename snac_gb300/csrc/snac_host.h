@@ -71,6 +71,10 @@ __host__ __device__ inline long act_idx(int p, int c, int h, int w, int H, int W
   return ((((long)p * H + h) * 2 + (c >> 3)) * W + w) * 8 + (c & 7);
 }
 void guess_destroy(GuessState *g);
+// the learned guess of the 3-D solve (k_unet.cu): a U-Net, crops of the solves as training pairs
+struct Guess3;
+Guess3 *guess3_create();
+void guess3_destroy(Guess3 *g);
 
 // the device multigrid problem plus its host-side construction data
 struct PoissonSolver {
@@ -195,6 +199,9 @@ int launch_fillps_tma(Domain &d, double dt, int *done);
 int tma_check(Domain &d);
 int guess_before(Domain &d, PoissonSolver &S, cudaStream_t st);
 int guess_after(Domain &d, PoissonSolver &S, cudaStream_t st);
+int guess3_before(PoissonSolver &S, Guess3 &g, int mode, int measure, double *ratio, cudaStream_t st);
+int guess3_after(PoissonSolver &S, Guess3 &g, cudaStream_t st);
+int guess3_train(Guess3 &g, int iters, double lr, double *loss_first, double *loss_last, int *pairs, cudaStream_t st);
 // mode of the learned guess (0 when it was never set up); set only changes an existing guess state
 int guess_get_mode(const Domain &d);
 void guess_set_mode(Domain &d, int mode);
