@@ -169,7 +169,7 @@ def other_configs():
     }
 
 
-def bench_configs(names, steps, warmup, device):
+def bench_configs(names, steps, warmup, device, learned_c4=1500):
     """ms per RK3 step, Mcells/s and max|div u| of the plain FP64 and the mixed path on each configuration."""
     out = {}
     cfgs = other_configs()
@@ -183,6 +183,14 @@ def bench_configs(names, steps, warmup, device):
                           "solve_residual_max": r["residual"], "helm_iters_max": r["helm_iters"],
                           "setup_s": r["setup_s"], "rc": r["rc"]}
         row["speedup_mixed_vs_plain"] = row["plain_fp64"]["ms_per_step"] / row["mixed"]["ms_per_step"]
+        if name == "c4_lbox" and learned_c4:
+            # the configuration's learned guess: 2,000 crops (4 per solve, 3 solves per step) recorded from the
+            # case's own solves, the U-Net trained on them, then guided steps at the same 1e-12 tolerance
+            lr_ = run_learned_path(case_fn, steps, warmup, device, record=167, train_iters=learned_c4, init=init)
+            row["learned_mixed"] = {k: lr_[k] for k in ("ms_per_step", "solve_iters_max", "solve_residual_max",
+                                                       "max_div_u", "pairs", "train_iters", "train_s", "loss_first",
+                                                       "loss_last", "residual_ratio_median")}
+            row["learned_mixed"]["mcells_per_s"] = row["cells"] / (lr_["ms_per_step"] * 1e-3) / 1e6
         out[name] = row
     return out
 
@@ -265,17 +273,19 @@ def run_gpu_path(case_fn, precision, steps, warmup, device, profile_kid=0, init=
         dom.close()
 
 
-def run_learned_path(case_fn, steps, warmup, device, record=8, train_iters=1500, lr=2e-3, **solver):
+def run_learned_path(case_fn, steps, warmup, device, record=8, train_iters=1500, lr=2e-3, init=None, **solver):
     """Mixed path with the learned initial guess: pairs recorded from `record` steps after the warm-up, the
     network trained on the GPU, then `steps` timed steps with the guess applied (and one more that measures
-    the residual it leaves relative to the previous solution's, per wavenumber system)."""
+    the residual it leaves relative to the previous solution's, per wavenumber system; one ratio for the
+    3-D solve).  With a transform axis the network is the plane network, with the 3-D solve the U-Net, whose
+    pairs are four 32^3 crops per solve."""
     from snac_gb300 import capi
     from snac_gb300.domain import Domain
     case = case_fn()
     L = capi.lib()
     dom = Domain(case, precision=1, device=device, use_graph=USE_GRAPH, **solver)
     try:
-        init_channel(dom, case)
+        (init or init_channel)(dom, case)
         dom.step(warmup, allow_not_converged=True)
         capi.check(L.snac_guess_mode(1))
         dom.step(record, allow_not_converged=True)
@@ -403,6 +413,9 @@ def main():
     ap.add_argument("--configs", default="c1_ldc64,c2_tgv128,c4_lbox,c5_dhc512",
                     help="other reference configurations timed beside the headline (comma list; empty: none)")
     ap.add_argument("--config-steps", type=int, default=3, help="timed steps per configuration and path")
+    ap.add_argument("--c4-train", type=int, default=1500,
+                    help="Adam steps of the U-Net guess on the L-shaped box's 2,000 recorded crops (0: no learned "
+                         "path for that configuration)")
     ap.add_argument("--tune", type=int, default=3,
                     help="snac_autotune with this many timed steps per candidate before the headline path is "
                          "timed (0: the library defaults)")
@@ -522,7 +535,7 @@ def main():
                 "levels": {str(k): {"launch_ms": v[0], "achieved_gbs": v[1] / (v[0] * 1e-3) / 1e9}
                            for k, v in smoother.items()}}
         roof["frac"] = roof["achieved"] / roof["peak"]
-    configs = bench_configs([c for c in args.configs.split(",") if c], args.config_steps, 2, device) \
+    configs = bench_configs([c for c in args.configs.split(",") if c], args.config_steps, 2, device, args.c4_train) \
         if args.configs else None
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -139,18 +139,23 @@ __global__ void __launch_bounds__(FX * FY) k_fillps_tma(const __grid_constant__ 
   }
 }
 
-namespace {
-
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+// the driver's cuTensorMapEncodeTiled (null when the driver does not provide it)
+void *tma_encode_fn() {
+  static void *fn = [] {
     void *p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
         q != cudaDriverEntryPointSuccess)
       p = nullptr;
-    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    return p;
   }();
   return fn;
+}
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(tma_encode_fn());
 }
 
 }  // namespace

@@ -9,26 +9,30 @@
 //   D1  conv [up(B) 64 | E1 32] -> 32, ReLU   (half resolution; nearest-neighbour upsampling of B)
 //   D0  conv [up(D1) 32 | E0 16] -> 16, ReLU  (full resolution)
 //   head 1x1x1 16 -> 1 (FP32)
-// Every 3x3x3 convolution is one kernel, k_u3_conv, an implicit GEMM on tcgen05: M = 128 cells of one x-row
-// segment, N = the output channels (16..64), K = 27 taps x 16 channels per channel group.  Activations are
-// BF16 in 16-channel groups, each cell's group stored as two 16-byte records (channels 0-7, 8-15), records of
-// consecutive x adjacent, so the nine (z, y) neighbour rows of a segment staged in shared memory are the A
-// operands of all 27 taps in the no-swizzle K-major core-matrix layout (the x offset of a tap is a 16-byte
-// offset of the descriptor's start address).  A conv input may come from two tensors (the skip connection)
-// and at half resolution (the upsampling is an index halving while staging), so neither a concatenation nor
-// an upsampled copy is ever written.  Stages (segment, channel group) are double-buffered with cp.async: the
-// rows and the weights of stage s+1 load while the 27 MMAs of stage s run; two TMEM accumulators alternate
-// per segment so that a segment's epilogue (tcgen05.ld, bias, ReLU, BF16 store) overlaps the next segment's
-// MMAs.  Every mbarrier wait is bounded; past the bound the kernel records an error, waits (bounded) for the
-// MMAs in flight, frees its TMEM and returns.
+// Every 3x3x3 convolution is one kernel, k_u3_conv, an implicit GEMM on tcgen05 (kind::f16, BF16 operands,
+// FP32 accumulation in TMEM): M = 128 cells of one x-row segment (126 of them outputs), N = 3 x the output
+// channels (the three x taps of every output channel side by side), K = 16 channels per group; one MMA per
+// (dz, dy) row and channel group, so a segment is 9 x groups MMAs.  Activations are BF16 in 16-channel groups,
+// each cell's group one 32-byte record, records of consecutive x adjacent.  Lane 0 of a fifth warp stages each
+// (segment, group) with one 5-D TMA box (128 records x 3 x 3 rows, 32-byte swizzle, zero fill outside the grid)
+// into one of up to four stages, keeps the layer's weights resident in shared memory when they fit (else they
+// stream with each stage as a bulk copy), and issues the MMAs.  Two TMEM accumulators alternate per segment:
+// the four epilogue warps read one back (tcgen05.ld) while the next segment's MMAs run, add the x-shifted tap
+// blocks (rows m, m + 1, m + 2 by warp shuffle, across warps through shared memory), and store bias + ReLU as
+// BF16 or the raw sums as FP32.  A skip connection is a second source tensor of the same convolution; an
+// upsampled input is materialised first (nearest neighbour).  Every mbarrier wait is bounded; past the bound
+// the kernel records an error, waits (bounded) for its copies and MMAs in flight, frees its TMEM and returns.
 // Training: the input gradient of a convolution is the same kernel run on the output gradient with the
 // transposed, tap-flipped weights; the weight gradients are FP32 reductions over cells on the CUDA cores
 // (per-chunk partials summed in a fixed order), Adam updates the FP32 masters.
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <random>
 #include <vector>
 
@@ -39,9 +43,6 @@ namespace snac {
 namespace u3 {
 
 constexpr int M = 128;                 // cells per segment (the MMA's M)
-constexpr int NREC = M + 2;            // staged records per half-row (one halo cell each side)
-constexpr int ROWB = NREC * 16;        // bytes of a staged half-row
-constexpr int ABYTES = 9 * 2 * ROWB;   // nine (dz, dy) rows x two channel halves: 37,440 bytes
 constexpr int TAPS = 27;
 constexpr int NL = 5;                  // convolution layers E0, E1, B, D1, D0
 constexpr int CIN[NL] = {16, 16, 32, 96, 48};
@@ -59,16 +60,24 @@ constexpr int HEAD = woff(NL);         // head: 16 weights then 1 bias
 constexpr int NPAR = HEAD + 17;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
-         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+// shared-memory matrix descriptor (tcgen05), K-major with the 32-byte swizzle (layout type 6 at bit 61): start
+// >> 4, leading-dimension offset unused (16 bytes), stride between 8-row groups >> 4, version 1 at bit 46
+__device__ __forceinline__ uint64_t smem_desc_sw32(uint32_t addr, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFF) | (1ull << 16) | ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46) |
+         (6ull << 61);
 }
 // kind::f16 instruction descriptor: FP32 accumulator, BF16 A and B, both K-major, N >> 3, M >> 4
 __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 // element offset of (row r, k) in a rows x 16 K-major block of 8x8 core matrices (LBO 128 B, SBO 256 B)
-__host__ __device__ __forceinline__ int core_el(int r, int k) { return (((r >> 3) * 2 + (k >> 3)) << 6) + ((r & 7) << 3) + (k & 7); }
+// element offset of (row r, k) in a rows x 16 K-major operand with the 32-byte swizzle: rows 32 bytes apart,
+// the two 16-byte halves of rows 4-7 of every 8-row group swapped (address bit 4 ^= bit 7; the block starts on
+// a 256-byte boundary)
+__host__ __device__ __forceinline__ int sw32_el(int r, int k) { return r * 16 + ((((k >> 3) ^ (r >> 2)) & 1) << 3) + (k & 7); }
+// activations: per 16-channel group g, per cell a 32-byte pair of records (channels 0-7 | 8-15); the index of
+// the 16-byte record gh = 2 g + h of cell `cell` in a tensor of `tot` cells (all volumes)
+__host__ __device__ __forceinline__ long rec16(int gh, long cell, long tot) { return ((long)(gh >> 1) * tot + cell) * 2 + (gh & 1); }
 
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long limit) {
   uint32_t done = 0;
@@ -80,13 +89,6 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long li
   }
   return done != 0;
 }
-__device__ __forceinline__ void cp16(uint32_t dst, const void *src, bool valid) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(valid ? 16u : 0u) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
 // one input tensor of a convolution: grouped BF16 records, `groups` 16-channel groups, on grid n (per
 // volume), at half the convolution's resolution when up = 1
 struct Src {
@@ -115,35 +117,100 @@ __device__ __forceinline__ const __nv_bfloat16 *src_rec(const ConvArgs &a, int g
   const int gs = g < a.s[0].groups ? g : g - a.s[0].groups;
   if (s.up) { x >>= 1; y >>= 1; z >>= 1; }
   const long vol = (long)s.n[0] * s.n[1] * s.n[2];
-  const long rec = (long)(2 * gs + h) * vol * a.nb + (long)b * vol + x + (long)s.n[0] * (y + (long)s.n[1] * z);
+  const long rec = rec16(2 * gs + h, (long)b * vol + x + (long)s.n[0] * (y + (long)s.n[1] * z), vol * a.nb);
   return s.p + rec * 8;
 }
 
-template <int N>
-constexpr int stage_bytes() { return ABYTES + TAPS * N * 32; }
-template <int N>
-constexpr int conv_smem() { return 2 * stage_bytes<N>() + 32; }
-template <int N>
-constexpr uint32_t tmem_cols() { return N <= 16 ? 32u : N <= 32 ? 64u : 128u; }
+// A operand of a stage: one TMA box of 32-byte cell records (16 channels), 128 cells (the segment's and the one
+// before) x 3 x 3 rows, rows ROW bytes apart, written with the 32-byte swizzle; a tap's x offset dx in {0, 1, 2}
+// starts its operand dx records later, so of the 128 MMA rows the first MV = 126 are outputs (the last two would
+// need records past the box: they read the padding after it and are discarded)
+constexpr int MV = M - 2;                              // output cells per segment
+constexpr int ROW = M * 32;                            // 4096 bytes
+constexpr int ABOX = 9 * ROW;                          // bytes one box writes (36,864)
+constexpr int ASTG = ABOX + 1024;                      // with the padding, a multiple of 1024
+constexpr int MAXST = 4;                               // stages at most
+constexpr int SMEM_LIMIT = 227 * 1024;
 
-// y = conv(x) over nb volumes: FWD writes bias + ReLU as grouped BF16, otherwise the raw sums as FP32 planes
+struct TmaConv {
+  CUtensorMap map[2];       // the sources: 5-D maps of 8-byte units {4 per cell record, x, y, z, group x volume}
+  int g0, kb;               // groups of source 0, total groups
+  int n[3], nb;             // output grid per volume, volumes (each source has the same grid)
+  const __nv_bfloat16 *w;   // packed weights [group][tap][N x 16 core layout]
+  const float *bias;        // forward: N biases
+  __nv_bfloat16 *yb;        // forward output (grouped BF16, bias + ReLU)
+  float *yf;                // input-gradient output: planar FP32 [yf_off + n][cell]
+  int yf_off;
+  int resw, nst;            // weights resident for the whole launch; pipeline stages
+  int *err;
+  long poll_limit;
+};
+
+// two accumulators of 3 N columns (the x taps dx = 0, 1, 2 of every output channel)
+template <int N>
+constexpr uint32_t tmem_cols() { return 6 * N <= 128 ? 128u : 6 * N <= 256 ? 256u : 512u; }
+__host__ __device__ constexpr int stage_stride(int N, int resw) {
+  return resw ? ASTG : ((ASTG + TAPS * N * 32 + 1023) / 1024) * 1024;
+}
+// the epilogue's exchange area (two segment parities x 4 warps x 3 N floats) after the stages and resident
+// weights, the mbarriers after it
+__host__ __device__ constexpr int xch_off(int N, int resw, int nst, int kb) {
+  return nst * stage_stride(N, resw) + (resw ? kb * TAPS * N * 32 : 0);
+}
+__host__ __device__ constexpr int bars_off(int N, int resw, int nst, int kb) { return xch_off(N, resw, nst, kb) + 96 * N; }
+__host__ constexpr int conv_smem(int N, int resw, int nst, int kb) { return bars_off(N, resw, nst, kb) + 128; }
+
+__device__ __forceinline__ void bar_init(uint64_t *b, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
+}
+__device__ __forceinline__ void bar_expect(uint64_t *b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bar_arrive(uint64_t *b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+// box of cells x.., rows y.., z.. of group x volume w (innermost coordinate 0: the whole 32-byte record)
+__device__ __forceinline__ void tma_box(uint32_t dst, const CUtensorMap *map, int x, int y, int z, int w, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(dst), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+// y = conv(x) over nb volumes.  Warps 0-3 read the accumulators back (TMEM lanes 32 w .. 32 w + 31) and store
+// them; lane 0 of warp 4 issues the TMA copies of the stages and the MMAs.  FWD writes bias + ReLU as grouped
+// BF16, otherwise the raw sums as FP32 planes.
 template <int N, bool FWD>
-__global__ void __launch_bounds__(128, 1) k_u3_conv(const __grid_constant__ ConvArgs a) {
-  extern __shared__ __align__(128) unsigned char smem[];
+__global__ void __launch_bounds__(160, 1) k_u3_conv(const __grid_constant__ TmaConv a) {
+  extern __shared__ __align__(1024) unsigned char smem[];
   constexpr int SB = TAPS * N * 32;
-  constexpr int STG = stage_bytes<N>();
   constexpr uint32_t TC = tmem_cols<N>();
   constexpr uint32_t ACC1 = TC / 2;  // column of the second accumulator
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + 2 * STG);
-  uint32_t *tbase = reinterpret_cast<uint32_t *>(smem + 2 * STG + 16);
+  const int STG = stage_stride(N, a.resw), NST = a.nst;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + bars_off(N, a.resw, NST, a.kb));
+  uint64_t *full = bars, *empty = bars + MAXST, *accf = bars + 2 * MAXST, *acce = bars + 2 * MAXST + 2,
+           *wbar = bars + 2 * MAXST + 4;
+  uint32_t *tbase = reinterpret_cast<uint32_t *>(bars + 2 * MAXST + 5);
+  unsigned char *wres = smem + NST * STG;
+  float *xch = reinterpret_cast<float *>(smem + xch_off(N, a.resw, NST, a.kb));
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  // the swizzled copies and operands need a 1024-byte aligned window: a misaligned one is reported, nothing runs
+  if (smem_u32(smem) & 1023u) {
+    if (t == 0) atomicExch(a.err, 2);
+    return;
+  }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tbase)), "r"(TC));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (t == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar[0])), "r"(1));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar[1])), "r"(1));
+    for (int q = 0; q < MAXST; q++) { bar_init(&full[q], 1); bar_init(&empty[q], 1); }
+    for (int q = 0; q < 2; q++) { bar_init(&accf[q], 1); bar_init(&acce[q], 4); }
+    bar_init(wbar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -152,147 +219,206 @@ __global__ void __launch_bounds__(128, 1) k_u3_conv(const __grid_constant__ Conv
   const uint32_t tm = *tbase;
   const int n0 = a.n[0], n1 = a.n[1], n2 = a.n[2];
   const long vol = (long)n0 * n1 * n2, tot = vol * a.nb;
-  const int nsx = (n0 + M - 1) / M;
+  const int nsx = (n0 + MV - 1) / MV;
   const long total = (long)nsx * n1 * n2 * a.nb;
   const long nloc = (long)blockIdx.x < total ? (total - 1 - blockIdx.x) / gridDim.x + 1 : 0;
   const long T = nloc * a.kb;
-  long waited = -1, committed = -1;
-  auto wait_upto = [&](long u, long limit) -> bool {
-    while (waited < u) {
-      const long v = waited + 1;
-      if (!mbar_wait(smem_u32(&mbar[v & 1]), (uint32_t)((v >> 1) & 1), limit)) return false;
-      waited = v;
-    }
-    return true;
-  };
   auto seg_of = [&](long k, int &x0, int &y, int &z, int &b) {
     long seg = blockIdx.x + k * gridDim.x;
-    x0 = (int)(seg % nsx) * M; seg /= nsx;
+    x0 = (int)(seg % nsx) * MV; seg /= nsx;
     y = (int)(seg % n1); seg /= n1;
     z = (int)(seg % n2); b = (int)(seg / n2);
   };
-  auto issue = [&](long s) {
-    const long k = s / a.kb;
-    const int g = (int)(s % a.kb);
-    int x0, y, z, b;
-    seg_of(k, x0, y, z, b);
-    unsigned char *A = smem + (s & 1) * STG;
-    const uint32_t A32 = smem_u32(A);
-    for (int e = t; e < 9 * 2 * NREC; e += M) {
-      const int r = e / (2 * NREC), rem = e - r * 2 * NREC;
-      const int h = rem / NREC, q = rem - h * NREC;
-      const int zz = z + r / 3 - 1, yy = y + r % 3 - 1, xx = x0 - 1 + q;
-      const bool in = xx >= 0 && xx < n0 && yy >= 0 && yy < n1 && zz >= 0 && zz < n2;
-      const void *src = in ? (const void *)src_rec(a, g, h, b, xx, yy, zz) : (const void *)a.w;
-      cp16(A32 + (r * 2 + h) * ROWB + q * 16, src, in);
+  bool ok = true;
+  if (warp == 4) {
+    if (lane == 0) {
+      // producer and MMA issuer.  Per buffer: copies issued / waited, commits issued / waited (for the drain)
+      int fiss[MAXST] = {0, 0, 0, 0}, fwt[MAXST] = {0, 0, 0, 0}, eiss[MAXST] = {0, 0, 0, 0}, ewt[MAXST] = {0, 0, 0, 0};
+      int wiss = 0;
+      if (a.resw && T > 0) {
+        bar_expect(wbar, (uint32_t)(a.kb * SB));
+        bulk_copy(smem_u32(wres), a.w, (uint32_t)(a.kb * SB), wbar);
+        wiss = 1;
+      }
+      long issued = 0, s = 0;
+      auto produce = [&](long u) -> bool {
+        const int buf = (int)(u % NST);
+        if (eiss[buf] > ewt[buf]) {  // the buffer's previous stage: its MMAs must be done
+          if (!mbar_wait(smem_u32(&empty[buf]), (uint32_t)(ewt[buf] & 1), a.poll_limit)) return false;
+          ewt[buf]++;
+        }
+        const int g = (int)(u % a.kb);
+        int x0, y, z, b;
+        seg_of(u / a.kb, x0, y, z, b);
+        unsigned char *A = smem + buf * STG;
+        bar_expect(&full[buf], (uint32_t)(ABOX + (a.resw ? 0 : SB)));
+        const int src = g < a.g0 ? 0 : 1, gs = g < a.g0 ? g : g - a.g0;
+        tma_box(smem_u32(A), &a.map[src], x0 - 1, y - 1, z - 1, gs * a.nb + b, &full[buf]);
+        if (!a.resw) bulk_copy(smem_u32(A + ASTG), reinterpret_cast<const unsigned char *>(a.w) + (long)g * SB, SB, &full[buf]);
+        fiss[buf]++;
+        return true;
+      };
+      // stages 0 .. NST-2 in flight before the first MMA; then each iteration queues stage s's MMAs before it
+      // refills the buffer of stage s-1 (whose MMAs run ahead of them), so the tensor pipe never drains
+      while (ok && issued < T && issued < NST - 1) ok = produce(issued++);
+      for (s = 0; s < T && ok; s++) {
+        const int buf = (int)(s % NST);
+        if (!mbar_wait(smem_u32(&full[buf]), (uint32_t)(fwt[buf] & 1), a.poll_limit)) { ok = false; break; }
+        fwt[buf]++;
+        if (wiss == 1) {
+          if (!mbar_wait(smem_u32(wbar), 0u, a.poll_limit)) { ok = false; break; }
+          wiss = 2;
+        }
+        const long k = s / a.kb;
+        const int g = (int)(s % a.kb);
+        if (g == 0 && k >= 2 && !mbar_wait(smem_u32(&acce[k & 1]), (uint32_t)(((k >> 1) - 1) & 1), a.poll_limit)) {
+          ok = false;  // the epilogue of segment k - 2 still holds this accumulator
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        // one MMA per (dz, dy) row r: the row's 128 records (A) times the 3 N rows of its three x taps (B); the
+        // x shift of the taps is applied when the accumulator is read back
+        constexpr uint32_t idesc = idesc_bf16(M, 3 * N);
+        const uint32_t A32 = smem_u32(smem + buf * STG);
+        const uint32_t W32 = a.resw ? smem_u32(wres) + g * SB : A32 + ASTG;
+        const uint32_t dt = tm + ((k & 1) ? ACC1 : 0u);
+#pragma unroll 1
+        for (int r = 0; r < 9; r++) {  // r = (dz + 1) * 3 + (dy + 1)
+          const uint64_t ad = smem_desc_sw32(A32 + r * ROW, 256);
+          const uint64_t bd = smem_desc_sw32(W32 + r * 3 * N * 32, 256);
+          const uint32_t acc = (g > 0 || r > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n .reg .pred pa;\n setp.ne.b32 pa, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, pa;\n}\n" ::"r"(dt),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(&empty[buf])));
+        eiss[buf]++;
+        if (g == a.kb - 1)
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(&accf[k & 1])));
+        while (ok && issued < T && issued < s + NST) ok = produce(issued++);
+      }
+      if (!ok) {
+        atomicExch(a.err, 1);
+        // drain: every copy issued has landed and every MMA issued has finished before the memory goes away
+        for (int q = 0; q < MAXST; q++) {
+          while (fwt[q] < fiss[q] && mbar_wait(smem_u32(&full[q]), (uint32_t)(fwt[q] & 1), MBAR_POLLS)) fwt[q]++;
+          while (ewt[q] < eiss[q] && mbar_wait(smem_u32(&empty[q]), (uint32_t)(ewt[q] & 1), MBAR_POLLS)) ewt[q]++;
+        }
+        if (wiss == 1) mbar_wait(smem_u32(wbar), 0u, MBAR_POLLS);
+      }
     }
-    const unsigned char *wsrc = reinterpret_cast<const unsigned char *>(a.w) + (long)g * SB;
-    for (int e = t; e < SB / 16; e += M) cp16(A32 + ABYTES + e * 16, wsrc + e * 16, true);
-  };
-  auto epilogue = [&](long k) {
-    int x0, y, z, b;
-    seg_of(k, x0, y, z, b);
-    const int x = x0 + warp * 32 + lane;
-    const long cell = (long)b * vol + x + (long)n0 * (y + (long)n1 * z);
-    const uint32_t col = (k & 1) ? ACC1 : 0u;
-#pragma unroll
-    for (int c16 = 0; c16 < N / 16; c16++) {
-      uint32_t rr[16];
-      const uint32_t taddr = tm + ((uint32_t)(warp * 32) << 16) + col + c16 * 16;
+  } else {
+    // epilogue warps: one segment at a time, in order, from the accumulator its MMAs filled
+    for (long k = 0; k < nloc; k++) {
+      const bool got = mbar_wait(smem_u32(&accf[k & 1]), (uint32_t)((k >> 1) & 1), a.poll_limit);
+      // the four epilogue warps decide together (their exchange below has a barrier of its own)
+      uint32_t any_bad;
       asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(rr[0]), "=r"(rr[1]), "=r"(rr[2]), "=r"(rr[3]), "=r"(rr[4]), "=r"(rr[5]), "=r"(rr[6]), "=r"(rr[7]),
-            "=r"(rr[8]), "=r"(rr[9]), "=r"(rr[10]), "=r"(rr[11]), "=r"(rr[12]), "=r"(rr[13]), "=r"(rr[14]),
-            "=r"(rr[15])
-          : "r"(taddr));
-      asm volatile("tcgen05.wait::ld.sync.aligned;");
-      if (x < n0) {
-        if constexpr (FWD) {
+          "{\n .reg .pred pin, pout;\n setp.ne.u32 pin, %1, 0;\n bar.red.or.pred pout, 1, 128, pin;\n"
+          " selp.u32 %0, 1, 0, pout;\n}\n"
+          : "=r"(any_bad)
+          : "r"(got ? 0u : 1u)
+          : "memory");
+      if (any_bad) { ok = false; break; }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      int x0, y, z, b;
+      seg_of(k, x0, y, z, b);
+      // accumulator row m = record x0 - 1 + m; columns dx N + c = its product with tap dx of channel c.  Output
+      // cell x0 + m sums rows m, m + 1, m + 2 of the dx = 0, 1, 2 blocks: the next lanes' values come by shuffle,
+      // those of the next warp's lanes 0 and 1 through shared memory (one exchange per segment)
+      const int m = warp * 32 + lane, x = x0 + m;
+      const long cell = (long)b * vol + x + (long)n0 * (y + (long)n1 * z);
+      const uint32_t col = (k & 1) ? ACC1 : 0u;
+      const uint32_t trow = tm + ((uint32_t)(warp * 32) << 16) + col;
+      float *xw = xch + ((k & 1) * 4 + warp) * 3 * N;  // this warp's exchange slots: lane 0 dx 1, lane 0 dx 2, lane 1 dx 2
+      auto ld16 = [&](uint32_t c, float *v) {
+        uint32_t rr[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(rr[0]), "=r"(rr[1]), "=r"(rr[2]), "=r"(rr[3]), "=r"(rr[4]), "=r"(rr[5]), "=r"(rr[6]), "=r"(rr[7]),
+              "=r"(rr[8]), "=r"(rr[9]), "=r"(rr[10]), "=r"(rr[11]), "=r"(rr[12]), "=r"(rr[13]), "=r"(rr[14]),
+              "=r"(rr[15])
+            : "r"(trow + c));
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-          for (int h = 0; h < 2; h++) {
-            __align__(16) __nv_bfloat16 o[8];
+        for (int e = 0; e < 16; e++) v[e] = __uint_as_float(rr[e]);
+      };
+#pragma unroll 1
+      for (int c16 = 0; c16 < N / 16; c16++) {
+        float v1[16], v2[16];
+        ld16(N + c16 * 16, v1);
+        ld16(2 * N + c16 * 16, v2);
+        if (lane == 0)
+          for (int e = 0; e < 16; e++) { xw[c16 * 16 + e] = v1[e]; xw[N + c16 * 16 + e] = v2[e]; }
+        if (lane == 1)
+          for (int e = 0; e < 16; e++) xw[2 * N + c16 * 16 + e] = v2[e];
+      }
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // the four epilogue warps have published their slots
+      const float *xn = xw + 3 * N;                   // the next warp's slots (read by lanes 30 and 31 of warps 0-2)
+#pragma unroll 1
+      for (int c16 = 0; c16 < N / 16; c16++) {
+        float v0[16], v1[16], v2[16];
+        ld16(c16 * 16, v0);
+        ld16(N + c16 * 16, v1);
+        ld16(2 * N + c16 * 16, v2);
+        float o[16];
 #pragma unroll
-            for (int e = 0; e < 8; e++)
-              o[e] = __float2bfloat16(fmaxf(__uint_as_float(rr[h * 8 + e]) + a.bias[c16 * 16 + h * 8 + e], 0.f));
-            *reinterpret_cast<uint4 *>(a.yb + ((long)(2 * c16 + h) * tot + cell) * 8) = *reinterpret_cast<const uint4 *>(o);
+        for (int e = 0; e < 16; e++) {
+          float s1 = __shfl_down_sync(0xffffffffu, v1[e], 1), s2 = __shfl_down_sync(0xffffffffu, v2[e], 2);
+          if (warp < 3 && lane == 31) { s1 = xn[c16 * 16 + e]; s2 = xn[2 * N + c16 * 16 + e]; }
+          if (warp < 3 && lane == 30) s2 = xn[N + c16 * 16 + e];
+          o[e] = v0[e] + s1 + s2;
+        }
+        if (m < MV && x < n0) {
+          if constexpr (FWD) {
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+              __align__(16) __nv_bfloat16 ob[8];
+#pragma unroll
+              for (int e = 0; e < 8; e++) ob[e] = __float2bfloat16(fmaxf(o[h * 8 + e] + a.bias[c16 * 16 + h * 8 + e], 0.f));
+              *reinterpret_cast<uint4 *>(a.yb + rec16(2 * c16 + h, cell, tot) * 8) = *reinterpret_cast<const uint4 *>(ob);
+            }
+          } else {
+#pragma unroll
+            for (int e = 0; e < 16; e++) a.yf[(long)(a.yf_off + c16 * 16 + e) * tot + cell] = o[e];
           }
-        } else {
-#pragma unroll
-          for (int e = 0; e < 16; e++) a.yf[(long)(a.yf_off + c16 * 16 + e) * tot + cell] = __uint_as_float(rr[e]);
         }
       }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncwarp();
+      if (lane == 0) bar_arrive(&acce[k & 1]);  // this warp is done with the accumulator
     }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-  };
-
-  bool ok = true, failed = false;
-  if (T > 0) { issue(0); cp_commit(); }
-  long pend = -1;
-  for (long s = 0; s < T; s++) {
-    if (s + 1 < T) {
-      if (s >= 1) ok = wait_upto(s - 1, a.poll_limit) && ok;  // stage s+1's buffer was read by stage s-1's MMAs
-      if (ok) issue(s + 1);
-      cp_commit();
-      cp_wait<1>();
-    } else {
-      cp_wait<0>();
-    }
-    // the operands were written by the generic proxy and are read by the tensor core (async proxy)
-    asm volatile("fence.proxy.async.shared::cta;");
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    const int bad = __syncthreads_or(ok ? 0 : 1);
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    if (bad) { failed = true; break; }
-    const long k = s / a.kb;
-    const int g = (int)(s % a.kb);
-    if (t == 0) {
-      constexpr uint32_t idesc = idesc_bf16(M, N);
-      const uint32_t A32 = smem_u32(smem + (s & 1) * STG);
-      const uint32_t dt = tm + ((k & 1) ? ACC1 : 0u);
-#pragma unroll 1
-      for (int q = 0; q < TAPS; q++) {
-        const int r = q / 3, dx = q % 3;  // r = (dz + 1) * 3 + (dy + 1)
-        const uint64_t ad = smem_desc(A32 + r * 2 * ROWB + dx * 16, ROWB, 128);
-        const uint64_t bd = smem_desc(A32 + ABYTES + q * N * 32, 128, 256);
-        const uint32_t acc = (g > 0 || q > 0) ? 1u : 0u;
-        asm volatile(
-            "{\n .reg .pred pa;\n setp.ne.b32 pa, %4, 0;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, pa;\n}\n" ::"r"(dt),
-            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-      }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(&mbar[s & 1])));
-    }
-    committed = s;
-    if (pend >= 0) {  // the previous segment's accumulator (its last stage is s - 1) while stage s multiplies
-      ok = wait_upto(s - 1, a.poll_limit) && ok;
-      ok = __all_sync(0xffffffffu, ok);
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      if (ok) epilogue(pend);
-      pend = -1;
-    }
-    if (g == a.kb - 1) pend = k;
-  }
-  if (!failed && pend >= 0) {
-    ok = wait_upto(T - 1, a.poll_limit) && ok;
-    ok = __all_sync(0xffffffffu, ok);
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    if (ok) epilogue(pend);
-  }
-  if (__syncthreads_or(ok ? 0 : 1)) failed = true;
-  if (failed) {
-    if (t == 0) atomicExch(a.err, 1);
-    cp_wait<0>();
-    wait_upto(committed, MBAR_POLLS);  // let the MMAs in flight finish before the memory goes away
+    if (!ok && lane == 0) atomicExch(a.err, 1);
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(TC));
 }
 
+// nearest-neighbour upsampling of a grouped BF16 tensor (coarse grid c -> fine grid f), record by record
+__global__ void k_u3_upsample(const __nv_bfloat16 *__restrict__ in, int G, int f0, int f1, int f2, int c0, int c1,
+                              int c2, int nb, __nv_bfloat16 *__restrict__ out) {
+  const long vc = (long)c0 * c1 * c2, vf = (long)f0 * f1 * f2;
+  const long total = vf * nb * 2 * G;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const long cell = e % (vf * nb);
+    const int gh = (int)(e / (vf * nb));
+    const int b = (int)(cell / vf);
+    long r = cell % vf;
+    const int x = (int)(r % f0); r /= f0;
+    const int y = (int)(r % f1), z = (int)(r / f1);
+    const long src = rec16(gh, b * vc + (x >> 1) + (long)c0 * ((y >> 1) + (long)c1 * (z >> 1)), vc * nb);
+    *reinterpret_cast<uint4 *>(out + rec16(gh, cell, vf * nb) * 8) = *reinterpret_cast<const uint4 *>(in + src * 8);
+  }
+}
+
 // weights of layer (cin -> cout), FP32 [co][ci][tap], to the packed BF16 blocks of a convolution with N output
 // channels: forward (co = n, ci = 16 g + k), or transposed for the input gradient (input channel co = 16 g + k,
-// output channel ci = n_off + n, tap mirrored)
+// output channel ci = n_off + n, tap mirrored).  Per input group g and (dz, dy) row r one B operand of 3 N rows
+// (the three x taps of every output channel) x 16 channels, 32-byte swizzled
 __global__ void k_u3_pack(const float *__restrict__ w, int cin, int cout, int trans, int n_off, int N, int kb,
                           __nv_bfloat16 *__restrict__ out) {
   const long total = (long)kb * TAPS * N * 16;
@@ -301,7 +427,9 @@ __global__ void k_u3_pack(const float *__restrict__ w, int cin, int cout, int tr
     float v;
     if (!trans) v = w[((long)n * cin + g * 16 + k) * TAPS + q];
     else v = w[((long)(g * 16 + k) * cin + n_off + n) * TAPS + (TAPS - 1 - q)];
-    out[((long)g * TAPS + q) * N * 16 + core_el(n, k)] = __float2bfloat16(v);
+    // block (g, row r = q / 3) of 3 N rows: row dx N + n holds tap (r, dx = q % 3) of output channel n
+    const int r = q / 3, dx = q % 3;
+    out[((long)g * 9 + r) * 3 * N * 16 + sw32_el(dx * N + n, k)] = __float2bfloat16(v);
   }
   (void)cout;
 }
@@ -324,7 +452,7 @@ __global__ void k_u3_pool(const __nv_bfloat16 *__restrict__ in, int G, int f0, i
         for (int dx = 0; dx < 2; dx++) {
           const int x = 2 * X + dx, y = 2 * Y + dy, z = 2 * Z + dz;
           if (x >= f0 || y >= f1 || z >= f2) continue;
-          const uint4 v = *reinterpret_cast<const uint4 *>(in + ((long)gh * vf * nb + b * vf + x + (long)f0 * (y + (long)f1 * z)) * 8);
+          const uint4 v = *reinterpret_cast<const uint4 *>(in + rec16(gh, b * vf + x + (long)f0 * (y + (long)f1 * z), vf * nb) * 8);
           const __nv_bfloat16 *p = reinterpret_cast<const __nv_bfloat16 *>(&v);
 #pragma unroll
           for (int c = 0; c < 8; c++) s[c] += __bfloat162float(p[c]);
@@ -332,7 +460,7 @@ __global__ void k_u3_pool(const __nv_bfloat16 *__restrict__ in, int G, int f0, i
     __align__(16) __nv_bfloat16 o[8];
 #pragma unroll
     for (int c = 0; c < 8; c++) o[c] = __float2bfloat16(s[c] * 0.125f);
-    *reinterpret_cast<uint4 *>(out + ((long)gh * vc * nb + cell) * 8) = *reinterpret_cast<const uint4 *>(o);
+    *reinterpret_cast<uint4 *>(out + rec16(gh, cell, vc * nb) * 8) = *reinterpret_cast<const uint4 *>(o);
   }
 }
 
@@ -346,8 +474,8 @@ __global__ void k_u3_input(const float *__restrict__ r, const unsigned char *__r
     o[1] = __float2bfloat16(l ? 1.f : 0.f);
 #pragma unroll
     for (int e = 2; e < 8; e++) o[e] = __float2bfloat16(0.f);
-    *reinterpret_cast<uint4 *>(x + c * 8) = *reinterpret_cast<const uint4 *>(o);
-    *reinterpret_cast<uint4 *>(x + (tot + c) * 8) = make_uint4(0u, 0u, 0u, 0u);
+    *reinterpret_cast<uint4 *>(x + rec16(0, c, tot) * 8) = *reinterpret_cast<const uint4 *>(o);
+    *reinterpret_cast<uint4 *>(x + rec16(1, c, tot) * 8) = make_uint4(0u, 0u, 0u, 0u);
   }
 }
 
@@ -358,7 +486,7 @@ __global__ void k_u3_head(const __nv_bfloat16 *__restrict__ a4, long tot, const 
     float acc = hw[16];
 #pragma unroll
     for (int h = 0; h < 2; h++) {
-      const uint4 v = *reinterpret_cast<const uint4 *>(a4 + ((long)h * tot + i) * 8);
+      const uint4 v = *reinterpret_cast<const uint4 *>(a4 + rec16(h, i, tot) * 8);
       const __nv_bfloat16 *p = reinterpret_cast<const __nv_bfloat16 *>(&v);
 #pragma unroll
       for (int e = 0; e < 8; e++) acc = fmaf(hw[h * 8 + e], __bfloat162float(p[e]), acc);
@@ -409,7 +537,7 @@ __global__ void __launch_bounds__(256) k_u3_head_back(const float *__restrict__ 
     const float d = dc[i];
 #pragma unroll
     for (int h = 0; h < 2; h++) {
-      const uint4 v = *reinterpret_cast<const uint4 *>(a4 + ((long)h * tot + i) * 8);
+      const uint4 v = *reinterpret_cast<const uint4 *>(a4 + rec16(h, i, tot) * 8);
       const __nv_bfloat16 *p = reinterpret_cast<const __nv_bfloat16 *>(&v);
       __align__(16) __nv_bfloat16 o[8];
 #pragma unroll
@@ -420,7 +548,7 @@ __global__ void __launch_bounds__(256) k_u3_head_back(const float *__restrict__ 
         o[e] = __float2bfloat16(g);
         acc[h * 8 + e] += d * av;
       }
-      *reinterpret_cast<uint4 *>(dzb + ((long)h * tot + i) * 8) = *reinterpret_cast<const uint4 *>(o);
+      *reinterpret_cast<uint4 *>(dzb + rec16(h, i, tot) * 8) = *reinterpret_cast<const uint4 *>(o);
     }
     acc[16] += d;
   }
@@ -462,7 +590,7 @@ __global__ void k_u3_sumchild(const float *__restrict__ gf, int c_off, int G, in
     long r = cell % vc;
     const int X = (int)(r % c0); r /= c0;
     const int Y = (int)(r % c1), Z = (int)(r / c1);
-    const uint4 av = *reinterpret_cast<const uint4 *>(act + ((long)gh * totc + cell) * 8);
+    const uint4 av = *reinterpret_cast<const uint4 *>(act + rec16(gh, cell, totc) * 8);
     const __nv_bfloat16 *ap = reinterpret_cast<const __nv_bfloat16 *>(&av);
     __align__(16) __nv_bfloat16 o[8];
 #pragma unroll
@@ -479,7 +607,7 @@ __global__ void k_u3_sumchild(const float *__restrict__ gf, int c_off, int G, in
       dz[(long)ch * totc + cell] = g;
       o[c] = __float2bfloat16(g);
     }
-    *reinterpret_cast<uint4 *>(dzb + ((long)gh * totc + cell) * 8) = *reinterpret_cast<const uint4 *>(o);
+    *reinterpret_cast<uint4 *>(dzb + rec16(gh, cell, totc) * 8) = *reinterpret_cast<const uint4 *>(o);
   }
 }
 
@@ -498,7 +626,7 @@ __global__ void k_u3_skipadd(const float *__restrict__ gs, int s_off, const floa
     const int x = (int)(r % f0); r /= f0;
     const int y = (int)(r % f1), z = (int)(r / f1);
     const long par = (long)b * vc + (x >> 1) + (long)c0 * ((y >> 1) + (long)c1 * (z >> 1));
-    const uint4 av = *reinterpret_cast<const uint4 *>(act + ((long)gh * totf + cell) * 8);
+    const uint4 av = *reinterpret_cast<const uint4 *>(act + rec16(gh, cell, totf) * 8);
     const __nv_bfloat16 *ap = reinterpret_cast<const __nv_bfloat16 *>(&av);
     __align__(16) __nv_bfloat16 o[8];
 #pragma unroll
@@ -509,7 +637,7 @@ __global__ void k_u3_skipadd(const float *__restrict__ gs, int s_off, const floa
       dz[(long)ch * totf + cell] = g;
       o[c] = __float2bfloat16(g);
     }
-    if (dzb) *reinterpret_cast<uint4 *>(dzb + ((long)gh * totf + cell) * 8) = *reinterpret_cast<const uint4 *>(o);
+    if (dzb) *reinterpret_cast<uint4 *>(dzb + rec16(gh, cell, totf) * 8) = *reinterpret_cast<const uint4 *>(o);
   }
 }
 
@@ -627,6 +755,7 @@ struct UNet3 {
   long cap[3] = {};
   __nv_bfloat16 *in = nullptr, *a0 = nullptr, *p0 = nullptr, *a1 = nullptr, *p1 = nullptr, *a2 = nullptr,
                 *a3 = nullptr, *a4 = nullptr;
+  __nv_bfloat16 *u2 = nullptr, *u3 = nullptr;  // B's output upsampled to level 1, D1's to level 0
   float *c = nullptr;
   // training buffers
   float *dc = nullptr, *dz4 = nullptr, *gd0 = nullptr, *dz3 = nullptr, *gd1 = nullptr, *dz2 = nullptr, *gb = nullptr,
@@ -706,14 +835,15 @@ struct UNet3 {
     for (int l = 0; l < 3; l++) need[l] = cells(nn[l]) * nbv;
     if (need[0] > cap[0] || need[1] > cap[1] || need[2] > cap[2]) {
       void **act[] = {(void **)&in, (void **)&a0, (void **)&p0, (void **)&a1, (void **)&p1, (void **)&a2, (void **)&a3,
-                      (void **)&a4, (void **)&c};
+                      (void **)&a4, (void **)&c, (void **)&u2, (void **)&u3};
       for (void **p : act) release(*p);
       const long c0 = std::max(need[0], cap[0]), c1 = std::max(need[1], cap[1]), c2 = std::max(need[2], cap[2]);
       in = (__nv_bfloat16 *)alloc(c0 * 32); a0 = (__nv_bfloat16 *)alloc(c0 * 32); a4 = (__nv_bfloat16 *)alloc(c0 * 32);
       p0 = (__nv_bfloat16 *)alloc(c1 * 32); a1 = (__nv_bfloat16 *)alloc(c1 * 64); a3 = (__nv_bfloat16 *)alloc(c1 * 64);
       p1 = (__nv_bfloat16 *)alloc(c2 * 64); a2 = (__nv_bfloat16 *)alloc(c2 * 128);
       c = (float *)alloc(c0 * 4);
-      if (!in || !a0 || !a4 || !p0 || !a1 || !a3 || !p1 || !a2 || !c) { set_error("device allocation failed (U-Net activations)"); return SNAC_ERR_NOMEM; }
+      u2 = (__nv_bfloat16 *)alloc(c1 * 128); u3 = (__nv_bfloat16 *)alloc(c0 * 64);
+      if (!in || !a0 || !a4 || !p0 || !a1 || !a3 || !p1 || !a2 || !c || !u2 || !u3) { set_error("device allocation failed (U-Net activations)"); return SNAC_ERR_NOMEM; }
       cap[0] = c0; cap[1] = c1; cap[2] = c2;
     }
     if (training && (need[0] > tcap[0] || need[1] > tcap[1] || need[2] > tcap[2])) {
@@ -742,30 +872,61 @@ struct UNet3 {
     return SNAC_OK;
   }
 
+  // the 5-D tensor map of a grouped BF16 tensor of G groups on level lev, in 8-byte units (four per 32-byte cell
+  // record of 16 channels): {record, x, y, z, group x volume}, boxes of 1 record x 128 cells x 3 x 3 x 1 (a
+  // segment's rows with the cell before; outside the grid: zeros), written with the 32-byte swizzle
+  int encode(CUtensorMap *m, const __nv_bfloat16 *p, int G, int lev) const {
+    auto enc = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(tma_encode_fn());
+    if (!enc) { set_error("U-Net: cuTensorMapEncodeTiled is not available"); return SNAC_ERR_UNSUPPORTED; }
+    const cuuint64_t vol = (cuuint64_t)n[lev][0] * n[lev][1] * n[lev][2];
+    const cuuint64_t gdim[5] = {4, (cuuint64_t)n[lev][0], (cuuint64_t)n[lev][1], (cuuint64_t)n[lev][2],
+                                (cuuint64_t)(G * nb)};
+    const cuuint64_t gstr[4] = {32, 32 * (cuuint64_t)n[lev][0], 32 * (cuuint64_t)n[lev][0] * n[lev][1], 32 * vol};
+    const cuuint32_t box[5] = {4, M, 3, 3, 1}, estr[5] = {1, 1, 1, 1, 1};
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 5, const_cast<__nv_bfloat16 *>(p), gdim, gstr, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) { set_error("U-Net: cuTensorMapEncodeTiled failed (%d)", (int)r); return SNAC_ERR_CUDA; }
+    return SNAC_OK;
+  }
+  // convolution on level lev of the sources (p0: g0 groups, p1: g1 groups, both on level lev)
   template <int N, bool FWD>
-  int conv(const Src &s0, const Src &s1, int lev, const __nv_bfloat16 *w, const float *bias, __nv_bfloat16 *yb,
-           float *yf, int yf_off, cudaStream_t st) {
-    ConvArgs a = {};
-    a.s[0] = s0; a.s[1] = s1;
-    a.kb = s0.groups + s1.groups;
+  int conv(const __nv_bfloat16 *p0, int g0, const __nv_bfloat16 *p1, int g1, int lev, const __nv_bfloat16 *w,
+           const float *bias, __nv_bfloat16 *yb, float *yf, int yf_off, cudaStream_t st) {
+    TmaConv a;
+    memset(&a, 0, sizeof(a));
+    SNAC_TRY(encode(&a.map[0], p0, g0, lev));
+    if (p1) SNAC_TRY(encode(&a.map[1], p1, g1, lev));
+    a.g0 = g0;
+    a.kb = g0 + (p1 ? g1 : 0);
     for (int q = 0; q < 3; q++) a.n[q] = n[lev][q];
     a.nb = nb;
     a.w = w; a.bias = bias; a.yb = yb; a.yf = yf; a.yf_off = yf_off; a.err = err;
     a.poll_limit = g_u3_poll_limit;
-    constexpr int smem = conv_smem<N>();
+    a.resw = conv_smem(N, 1, 2, a.kb) <= SMEM_LIMIT ? 1 : 0;
+    a.nst = MAXST;
+    while (a.nst > 2 && conv_smem(N, a.resw, a.nst, a.kb) > SMEM_LIMIT) a.nst--;
+    const int smem = conv_smem(N, a.resw, a.nst, a.kb);
+    if (smem > SMEM_LIMIT) { set_error("U-Net: convolution stages exceed shared memory"); return SNAC_ERR_UNSUPPORTED; }
     static bool attr = false;  // per template instance; the attribute is per function
     if (!attr) {
-      SNAC_CUDA(cudaFuncSetAttribute(k_u3_conv<N, FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      SNAC_CUDA(cudaFuncSetAttribute(k_u3_conv<N, FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_LIMIT));
       attr = true;
     }
-    int dev = 0, nsm = 0, occ = 0;
+    int dev = 0, nsm = 0;
     SNAC_CUDA(cudaGetDevice(&dev));
     SNAC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    SNAC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_u3_conv<N, FWD>, M, smem));
-    const long total = (long)((a.n[0] + M - 1) / M) * a.n[1] * a.n[2] * nb;
-    const int grid = (int)std::max<long>(1, std::min<long>(total, (long)nsm * std::max(occ, 1)));
-    k_u3_conv<N, FWD><<<grid, M, smem, st>>>(a), ::snac::count_launch();
+    const long total = (long)((a.n[0] + MV - 1) / MV) * a.n[1] * a.n[2] * nb;
+    const int grid = (int)std::max<long>(1, std::min<long>(total, nsm));
+    k_u3_conv<N, FWD><<<grid, 160, smem, st>>>(a), ::snac::count_launch();
     SNAC_CUDA(cudaGetLastError());
+    return SNAC_OK;
+  }
+  int upsample(const __nv_bfloat16 *x, int G, int lc, __nv_bfloat16 *y, cudaStream_t st) {
+    const long total = cells(n[lc - 1]) * nb * 2 * G;
+    const int grid = (int)std::min<long>((total + 255) / 256, 8192);
+    k_u3_upsample<<<grid, 256, 0, st>>>(x, G, n[lc - 1][0], n[lc - 1][1], n[lc - 1][2], n[lc][0], n[lc][1], n[lc][2], nb,
+                                        y), ::snac::count_launch();
     return SNAC_OK;
   }
   Src src(const __nv_bfloat16 *p, int groups, int lev, int up) const {
@@ -784,13 +945,15 @@ struct UNet3 {
   }
   // forward from the BF16 input in `in` to the FP32 head output `c`
   int forward(cudaStream_t st) {
-    SNAC_TRY((conv<16, true>(src(in, 1, 0, 0), none(), 0, wf + wf_off[0], par + woff(0) + 16 * 16 * TAPS, a0, nullptr, 0, st)));
+    SNAC_TRY((conv<16, true>(in, 1, nullptr, 0, 0, wf + wf_off[0], par + woff(0) + 16 * 16 * TAPS, a0, nullptr, 0, st)));
     SNAC_TRY(pool(a0, 1, 0, p0, st));
-    SNAC_TRY((conv<32, true>(src(p0, 1, 1, 0), none(), 1, wf + wf_off[1], par + woff(1) + 16 * 32 * TAPS, a1, nullptr, 0, st)));
+    SNAC_TRY((conv<32, true>(p0, 1, nullptr, 0, 1, wf + wf_off[1], par + woff(1) + 16 * 32 * TAPS, a1, nullptr, 0, st)));
     SNAC_TRY(pool(a1, 2, 1, p1, st));
-    SNAC_TRY((conv<64, true>(src(p1, 2, 2, 0), none(), 2, wf + wf_off[2], par + woff(2) + 32 * 64 * TAPS, a2, nullptr, 0, st)));
-    SNAC_TRY((conv<32, true>(src(a2, 4, 2, 1), src(a1, 2, 1, 0), 1, wf + wf_off[3], par + woff(3) + 96 * 32 * TAPS, a3, nullptr, 0, st)));
-    SNAC_TRY((conv<16, true>(src(a3, 2, 1, 1), src(a0, 1, 0, 0), 0, wf + wf_off[4], par + woff(4) + 48 * 16 * TAPS, a4, nullptr, 0, st)));
+    SNAC_TRY((conv<64, true>(p1, 2, nullptr, 0, 2, wf + wf_off[2], par + woff(2) + 32 * 64 * TAPS, a2, nullptr, 0, st)));
+    SNAC_TRY(upsample(a2, 4, 2, u2, st));
+    SNAC_TRY((conv<32, true>(u2, 4, a1, 2, 1, wf + wf_off[3], par + woff(3) + 96 * 32 * TAPS, a3, nullptr, 0, st)));
+    SNAC_TRY(upsample(a3, 2, 1, u3, st));
+    SNAC_TRY((conv<16, true>(u3, 2, a0, 1, 0, wf + wf_off[4], par + woff(4) + 48 * 16 * TAPS, a4, nullptr, 0, st)));
     const long tot = cells(n[0]) * nb;
     k_u3_head<<<(int)std::min<long>((tot + 255) / 256, 8192), 256, 0, st>>>(a4, tot, par + HEAD, c), ::snac::count_launch();
     SNAC_CUDA(cudaGetLastError());
@@ -825,25 +988,25 @@ struct UNet3 {
     k_u3_sum_rows<<<1, 64, 0, st>>>(part, hb, 17, g + HEAD), ::snac::count_launch();
     // D0: input [up(a3) 2 groups | a0 1 group] at level 0
     SNAC_TRY(wgrad<16>(4, src(a3, 2, 1, 1), src(a0, 1, 0, 0), 0, dz4, st));
-    SNAC_TRY((conv<48, false>(src(dz4b, 1, 0, 0), none(), 0, wt + wt_off[4], nullptr, nullptr, gd0, 0, st)));
+    SNAC_TRY((conv<48, false>(dz4b, 1, nullptr, 0, 0, wt + wt_off[4], nullptr, nullptr, gd0, 0, st)));
     auto grid_of = [](long total) { return (int)std::min<long>((total + 255) / 256, 8192); };
     k_u3_sumchild<<<grid_of(cells(n[1]) * nb * 4), 256, 0, st>>>(gd0, 0, 2, n[0][0], n[0][1], n[0][2], n[1][0], n[1][1],
                                                                 n[1][2], nb, a3, dz3, dz3b), ::snac::count_launch();
     // D1: input [up(a2) 4 groups | a1 2 groups] at level 1
     SNAC_TRY(wgrad<32>(3, src(a2, 4, 2, 1), src(a1, 2, 1, 0), 1, dz3, st));
     for (int ch = 0; ch < 2; ch++)
-      SNAC_TRY((conv<48, false>(src(dz3b, 2, 1, 0), none(), 1, wt + wt_off[3] + (long)ch * 48 * 32 * TAPS, nullptr,
-                                nullptr, gd1, ch * 48, st)));
+      SNAC_TRY((conv<48, false>(dz3b, 2, nullptr, 0, 1, wt + wt_off[3] + (long)ch * 48 * 32 * TAPS, nullptr, nullptr,
+                                gd1, ch * 48, st)));
     k_u3_sumchild<<<grid_of(cells(n[2]) * nb * 8), 256, 0, st>>>(gd1, 0, 4, n[1][0], n[1][1], n[1][2], n[2][0], n[2][1],
                                                                 n[2][2], nb, a2, dz2, dz2b), ::snac::count_launch();
     // B: input p1 (2 groups) at level 2
     SNAC_TRY(wgrad<64>(2, src(p1, 2, 2, 0), none(), 2, dz2, st));
-    SNAC_TRY((conv<32, false>(src(dz2b, 4, 2, 0), none(), 2, wt + wt_off[2], nullptr, nullptr, gb, 0, st)));
+    SNAC_TRY((conv<32, false>(dz2b, 4, nullptr, 0, 2, wt + wt_off[2], nullptr, nullptr, gb, 0, st)));
     k_u3_skipadd<<<grid_of(cells(n[1]) * nb * 4), 256, 0, st>>>(gd1, 64, gb, 2, n[1][0], n[1][1], n[1][2], n[2][0],
                                                                n[2][1], n[2][2], nb, a1, dz1, dz1b), ::snac::count_launch();
     // E1: input p0 (1 group) at level 1
     SNAC_TRY(wgrad<32>(1, src(p0, 1, 1, 0), none(), 1, dz1, st));
-    SNAC_TRY((conv<16, false>(src(dz1b, 2, 1, 0), none(), 1, wt + wt_off[1], nullptr, nullptr, ge1, 0, st)));
+    SNAC_TRY((conv<16, false>(dz1b, 2, nullptr, 0, 1, wt + wt_off[1], nullptr, nullptr, ge1, 0, st)));
     k_u3_skipadd<<<grid_of(cells(n[0]) * nb * 2), 256, 0, st>>>(gd0, 32, ge1, 1, n[0][0], n[0][1], n[0][2], n[1][0],
                                                                n[1][1], n[1][2], nb, a0, dz0, nullptr), ::snac::count_launch();
     // E0: input in (1 group) at level 0
@@ -864,6 +1027,7 @@ struct UNet3 {
     SNAC_CUDA(cudaMemcpy(&e, err, sizeof(int), cudaMemcpyDeviceToHost));
     if (e) {
       SNAC_CUDA(cudaMemset(err, 0, sizeof(int)));
+      if (e == 2) { set_error("U-Net: shared-memory window not 1024-byte aligned"); return SNAC_ERR_CUDA; }
       set_error("tensor-core accumulator wait timed out (U-Net)");
       return SNAC_ERR_TIMEOUT;
     }
@@ -962,8 +1126,8 @@ __global__ void k_g3_input(const double *__restrict__ r, const unsigned short *_
     o[1] = __float2bfloat16(live ? 1.f : 0.f);
 #pragma unroll
     for (int e = 2; e < 8; e++) o[e] = __float2bfloat16(0.f);
-    *reinterpret_cast<uint4 *>(x + c * 8) = *reinterpret_cast<const uint4 *>(o);
-    *reinterpret_cast<uint4 *>(x + (n + c) * 8) = make_uint4(0u, 0u, 0u, 0u);
+    *reinterpret_cast<uint4 *>(x + rec16(0, c, n) * 8) = *reinterpret_cast<const uint4 *>(o);
+    *reinterpret_cast<uint4 *>(x + rec16(1, c, n) * 8) = make_uint4(0u, 0u, 0u, 0u);
   }
 }
 

@@ -73,6 +73,8 @@ __host__ __device__ inline long act_idx(int p, int c, int h, int w, int H, int W
 void guess_destroy(GuessState *g);
 // the learned guess of the 3-D solve (k_unet.cu): a U-Net, crops of the solves as training pairs
 struct Guess3;
+// cuTensorMapEncodeTiled from the driver (k_tma.cu; null when unavailable)
+void *tma_encode_fn();
 Guess3 *guess3_create();
 void guess3_destroy(Guess3 *g);
 
