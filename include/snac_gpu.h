@@ -354,6 +354,16 @@ int snac_cnn_set_poll_limit(long polls);
 int snac_guess_grad(const float *x, const float *target, int nb, int H, int W, const float *params, float *grads,
                     double *loss);
 
+/* No counterpart in the reference (the stand-in for compute-sanitizer and the reference's -fcheck=all debug
+ * build): snac_bounds_checked is 1 in the bounds-check build (libsnac_gb300_checked.so, compiled with
+ * -DSNAC_BOUNDS_CHECK), where the stencil, halo-exchange, boundary-condition and inflow kernels validate the
+ * cells and 1-D table entries they address against their block and skip an access outside it; the entry
+ * points that run kernels then return SNAC_ERR_BOUNDS naming the kernel and the cell.  snac_bounds_selftest
+ * launches a check that fails by design (no access is made) and returns what the host check reports:
+ * SNAC_ERR_BOUNDS in that build, SNAC_ERR_UNSUPPORTED in the normal one. */
+int snac_bounds_checked(void);
+int snac_bounds_selftest(void);
+
 /* No counterpart in the reference: the three-level U-Net of the learned guess of the 3-D pressure solve
  * (about 180k parameters: conv 3x3x3 16->16, pool, 16->32, pool, 32->64, [up | skip] 96->32, [up | skip]
  * 48->16, head 1x1x1 16->1; BF16 tensor-core operands, FP32 accumulation).  snac_unet_nparams gives the

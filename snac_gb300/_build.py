@@ -11,6 +11,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libsnac_gb300.so")
+# the bounds-check build (-DSNAC_BOUNDS_CHECK): device-side index checks that return SNAC_ERR_BOUNDS
+LIB_CHECKED = os.path.join(OUT_DIR, "libsnac_gb300_checked.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no FMA contraction, so the set-up arithmetic (grids, boundary planes, inflow profiles) gives
 # the same bits on x86-64 and aarch64 hosts
@@ -29,8 +31,8 @@ def _nvcc():
     return "nvcc"
 
 
-def _compile(src: str, extra) -> str:
-    obj = os.path.join(OUT_DIR, os.path.basename(src)[:-3] + ".o")
+def _compile(src: str, extra, out_dir=OUT_DIR) -> str:
+    obj = os.path.join(out_dir, os.path.basename(src)[:-3] + ".o")
     cmd = [_nvcc(), *ARCH, *FLAGS, *extra, "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -56,6 +58,26 @@ def build(verbose: bool = False, extra=()) -> str:
     if verbose:
         print("built", LIB)
     return LIB
+
+
+def build_checked(verbose: bool = False) -> str:
+    """The bounds-check library (libsnac_gb300_checked.so), objects in _build/checked."""
+    out_dir = os.path.join(OUT_DIR, "checked")
+    os.makedirs(out_dir, exist_ok=True)
+    srcs = sources()
+    newest = max(os.path.getmtime(p) for p in srcs + [os.path.join(ROOT, "include", "snac_gpu.h")] +
+                 [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")])
+    if os.path.exists(LIB_CHECKED) and os.path.getmtime(LIB_CHECKED) >= newest:
+        return LIB_CHECKED
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        objs = list(ex.map(lambda s: _compile(s, ["-DSNAC_BOUNDS_CHECK"], out_dir), srcs))
+    cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB_CHECKED, *objs, "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    if verbose:
+        print("built", LIB_CHECKED)
+    return LIB_CHECKED
 
 
 if __name__ == "__main__":

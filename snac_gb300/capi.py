@@ -139,6 +139,8 @@ PROTOTYPES = {
     "snac_cnn_conv3x3": (C.c_int, [FP, C.c_int, C.c_int, C.c_int, FP, FP, C.c_int, FP]),
     "snac_cnn_set_poll_limit": (C.c_int, [C.c_long]),
     "snac_guess_grad": (C.c_int, [FP, FP, C.c_int, C.c_int, C.c_int, FP, FP, DP]),
+    "snac_bounds_checked": (C.c_int, []),
+    "snac_bounds_selftest": (C.c_int, []),
     "snac_unet_nparams": (C.c_int, []),
     "snac_unet_forward": (C.c_int, [FP, C.c_int, C.c_int, C.c_int, C.c_int, FP, FP]),
     "snac_unet_grad": (C.c_int, [FP, FP, C.c_int, C.c_int, C.c_int, C.c_int, FP, FP, DP]),
@@ -163,14 +165,16 @@ def lib_path() -> str:
 
 
 def lib(build_if_missing: bool = True):
-    """Load libsnac_gb300.so (compiling it in-tree first when absent)."""
+    """Load libsnac_gb300.so (compiling it in-tree first when absent); with SNAC_BOUNDS_CHECK=1 in the
+    environment, the bounds-check build libsnac_gb300_checked.so instead."""
     global _lib
     if _lib is None:
-        path = _build.LIB
+        checked = os.environ.get("SNAC_BOUNDS_CHECK", "0") not in ("", "0")
+        path = _build.LIB_CHECKED if checked else _build.LIB
         if not os.path.exists(path):
             if not build_if_missing:
                 raise RuntimeError(f"snac_gb300 extension not built: {path}")
-            _build.build()
+            _build.build_checked() if checked else _build.build()
         L = C.CDLL(path)
         for name, (res, args) in PROTOTYPES.items():
             f = getattr(L, name)

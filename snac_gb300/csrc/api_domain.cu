@@ -382,6 +382,7 @@ static int upload_domain(Domain &d) {
     DBlock &B = d.db[b];
     memset(&B, 0, sizeof(B));
     for (int a = 0; a < 3; a++) { B.n[a] = H.ng[a]; B.lo[a] = H.lo[a]; }
+    B.bchk = bounds_flag();
     const size_t nh = (size_t)(H.ng[0] + 2) * (H.ng[1] + 2) * (H.ng[2] + 2) * sizeof(double);
     const size_t ni = (size_t)H.ng[0] * H.ng[1] * H.ng[2] * sizeof(double);
     B.u = (double *)d.alloc(nh); B.v = (double *)d.alloc(nh); B.w = (double *)d.alloc(nh);
@@ -1109,7 +1110,8 @@ int snac_fillps_all(double dtrk) {
   NEED_DOMAIN
   SNAC_TRY(fillps_all(*d, dtrk));
   SNAC_CUDA(cudaStreamSynchronize(d->st));
-  return tma_check(*d);
+  SNAC_TRY(tma_check(*d));
+  return bounds_check(d->st);
 }
 int snac_updt_rhs_all(void) {
   NEED_DOMAIN
@@ -1220,6 +1222,7 @@ int snac_step(int nsteps) {
   SNAC_CUDA(cudaEventElapsedTime(&ms, d->ev0, d->ev1));
   d->device_ms = ms;
   SNAC_TRY(tma_check(*d));  // a bounded wait of the TMA-staged kernel that ran out
+  SNAC_TRY(bounds_check(d->st));
   return rc_all;
 }
 

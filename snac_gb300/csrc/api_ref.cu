@@ -129,6 +129,7 @@ int OneBlock::setup(const int lo_[3], const int hi_[3], const double *dxc, const
   SNAC_CUDA(cudaMalloc(&dax, all.size() * sizeof(double)));
   SNAC_CUDA(cudaMemcpy(dax, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice));
   for (int a = 0; a < 3; a++) hb.ax[a] = dax + off[a];
+  hb.bchk = bounds_flag();
   std::vector<std::array<int, 3>> sz{{hb.n[0] + (halo_tiles ? 2 : 0), hb.n[1] + (halo_tiles ? 2 : 0),
                                       hb.n[2] + (halo_tiles ? 2 : 0)}};
   auto tl = make_tiles(sz, TX, TY, TZ);
@@ -194,7 +195,7 @@ int bound_block(OneBlock &ob, const int *flds, int nf, const int nb[3][2], int m
     SNAC_TRY(launch_setbc(ob.dblk, (const BcEntry *)q, (int)ent[a].size(), a, (ob.hb.n[t1] + 2) * (ob.hb.n[t2] + 2), 0));
   }
   SNAC_CUDA(cudaDeviceSynchronize());
-  return SNAC_OK;
+  return bounds_check(0);
 }
 
 bool bound_args_ok(const int lo[3], const int hi[3], const int is_bound[3][2], const int nb[3][2]) {
@@ -313,6 +314,7 @@ int snac_rk_mom(const double rkpar[2], const int lo[3], const int hi[3], const d
   SNAC_TRY(launch_rk_mom(ob.dblk, ob.dtiles, ob.ntiles, prm, 0));
   SNAC_TRY(launch_rk_mom_writeback(ob.dblk, ob.dtiles, ob.ntiles, 0));
   SNAC_CUDA(cudaDeviceSynchronize());
+  SNAC_TRY(bounds_check(0));
   SNAC_TRY(U.finish()); SNAC_TRY(V.finish()); SNAC_TRY(W.finish());
   SNAC_TRY(RU.finish()); SNAC_TRY(RV.finish()); SNAC_TRY(RW.finish());
   return SNAC_OK;
@@ -357,6 +359,7 @@ int snac_rk_scal(const double rkpar[2], const int lo[3], const int hi[3], const 
     SNAC_CUDA(cudaMemcpy(r, res, 2 * sizeof(double), cudaMemcpyDeviceToHost));
   }
   SNAC_CUDA(cudaDeviceSynchronize());
+  SNAC_TRY(bounds_check(0));
   SNAC_TRY(S.finish());
   SNAC_TRY(RS.finish());
   if (f) *f = (is_forced ? scalf - r[0] / vol_all : 0.0);
@@ -377,6 +380,7 @@ int snac_fillps(const int lo[3], const int hi[3], const double *dxf, const doubl
   SNAC_TRY(ob.upload());
   SNAC_TRY(launch_fillps(ob.dblk, ob.dtiles, ob.ntiles, dt, fft_axis, 0));
   SNAC_CUDA(cudaDeviceSynchronize());
+  SNAC_TRY(bounds_check(0));
   SNAC_TRY(Pp.finish());
   return SNAC_OK;
 }
@@ -395,6 +399,7 @@ int snac_correc(const int lo[3], const int hi[3], const double *dxc, const doubl
   SNAC_TRY(ob.upload());
   SNAC_TRY(launch_correc(ob.dblk, ob.dtiles, ob.ntiles, dt, 0));
   SNAC_CUDA(cudaDeviceSynchronize());
+  SNAC_TRY(bounds_check(0));
   SNAC_TRY(U.finish()); SNAC_TRY(V.finish()); SNAC_TRY(W.finish());
   return SNAC_OK;
 }
@@ -413,6 +418,7 @@ int snac_updt_pressure(const int lo[3], const int hi[3], const double *dxc, cons
   SNAC_TRY(ob.upload());
   SNAC_TRY(launch_updt_pressure(ob.dblk, ob.dtiles, ob.ntiles, alpha, impdiff, 0));
   SNAC_CUDA(cudaDeviceSynchronize());
+  SNAC_TRY(bounds_check(0));
   SNAC_TRY(Pa.finish());
   return SNAC_OK;
 }
@@ -432,6 +438,7 @@ int snac_updt_rhs(const int lo[3], const int hi[3], const int is_bound[3][2], co
   SNAC_TRY(launch_updt_rhs(nx, ny, nz, isb, (const double *)RX.dev, (const double *)RY.dev, (const double *)RZ.dev,
                            (double *)Pa.dev, 0));
   SNAC_CUDA(cudaDeviceSynchronize());
+  SNAC_TRY(bounds_check(0));
   SNAC_TRY(Pa.finish());
   return SNAC_OK;
 }

@@ -39,6 +39,7 @@ __global__ void k_exchange(const DBlock *__restrict__ Bs, const FaceLink *__rest
   cd[t1] = x; cd[t2] = y; cs[t1] = x; cs[t2] = y;
   cd[a] = fl.side ? D.n[a] : -1;
   cs[a] = fl.side ? 0 : S.n[a] - 1;
+  if (!bchk(D, BK_EXCHANGE_DST, cd[0], cd[1], cd[2], -1, 1) || !bchk(S, BK_EXCHANGE_SRC, cs[0], cs[1], cs[2], -1, 1)) return;
   const long id = hidx(cd[0], cd[1], cd[2], D.n[0], D.n[1]);
   const long is = hidx(cs[0], cs[1], cs[2], S.n[0], S.n[1]);
   const int f = flds[blockIdx.z];
@@ -60,6 +61,7 @@ __global__ void k_setbc(const DBlock *__restrict__ Bs, const BcEntry *__restrict
   const int n = B.n[a];
   const long st = a == 0 ? 1 : (a == 1 ? (long)(B.n[0] + 2) : (long)(B.n[0] + 2) * (B.n[1] + 2));
   c[a] = 0;
+  if (!bchk(B, BK_SETBC, c[0], c[1], c[2], -1, 1)) return;  // the plane's cells along a span -1..n
   double *p = field_ptr(B, e.f) + hidx(c[0], c[1], c[2], B.n[0], B.n[1]);  // points at index 0 along a
 #define AT(qq) p[(long)(qq) * st]
   for (int s = 0; s < 2; s++) {
@@ -117,6 +119,8 @@ __global__ void k_inflow(const DBlock *__restrict__ dB, const InflowFace *__rest
   c[t2] = q / n1 - 1;
   const int na = B.n[a];
   const int qn = side ? na - 1 : -1, qt = side ? na : -1, dq = side ? -1 : 1;
+  c[a] = qt;
+  if (!bchk(B, BK_INFLOW, c[0], c[1], c[2], -1, 1)) return;  // qn and qt + dq lie between qt and the interior
   double *f[3] = {B.u, B.v, B.w};
   for (int comp = 0; comp < 3; comp++) {
     const double vin = F.pl[comp][q];

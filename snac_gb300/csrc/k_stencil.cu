@@ -21,7 +21,8 @@ namespace snac {
   const int nx = B.n[0], ny = B.n[1], nz = B.n[2];                  \
   const int i = t.y + (int)threadIdx.x, j = t.z + (int)threadIdx.y, \
             k = t.w + (int)threadIdx.z;                             \
-  if (i >= nx || j >= ny || k >= nz) return;
+  if (i >= nx || j >= ny || k >= nz) return;                        \
+  if (!bchk(B, BK_TILE, i, j, k, 0, 0)) return;
 
 // ---------------------------------------------------------------- rk_mom
 // rk.f90:7-128 with momx/y/z_d (mom.f90:221-327), momx/y/z_a_vv (mom.f90:112-219),

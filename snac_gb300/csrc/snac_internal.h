@@ -90,7 +90,31 @@ struct DBlock {
   double *nu, *nv, *nw;        // interior scratch: new velocity of a stage before write-back
   double *ns;                  // interior scratch for scalars
   const double *ax[3];         // AxisArr tables per axis: ax[a][AX_*(n+2) + q + 1]
+  unsigned long long *bchk;    // bounds-check build: the flag the device checks record into (null otherwise)
 };
+
+// Bounds-check build (compiled with -DSNAC_BOUNDS_CHECK, libsnac_gb300_checked.so): kernels validate the cells
+// and table entries they address against the block's extents; the first failure is recorded in the flag as
+// (kernel id, i, j, k) and the access is skipped, so nothing outside an array is touched; the host turns a
+// set flag into SNAC_ERR_BOUNDS.  In the normal build every check is a constant true.
+enum BchkKernel { BK_TILE = 1, BK_AXIS, BK_EXCHANGE_DST, BK_EXCHANGE_SRC, BK_SETBC, BK_INFLOW, BK_PROBE, BK_NKIND };
+#ifdef SNAC_BOUNDS_CHECK
+__device__ inline void bchk_record(unsigned long long *f, int kid, int i, int j, int k) {
+  if (!f) return;
+  const unsigned long long v = (1ull << 63) | ((unsigned long long)(kid & 0x7FFF) << 48) |
+                               ((unsigned long long)((i + 32768) & 0xFFFF) << 32) |
+                               ((unsigned long long)((j + 32768) & 0xFFFF) << 16) | (unsigned long long)((k + 32768) & 0xFFFF);
+  atomicCAS(f, 0ull, v);
+}
+// (i, j, k) within [lo, n_a - 1 + hi] on every axis of B
+__device__ inline bool bchk(const DBlock &B, int kid, int i, int j, int k, int lo, int hi) {
+  const bool ok = i >= lo && i <= B.n[0] - 1 + hi && j >= lo && j <= B.n[1] - 1 + hi && k >= lo && k <= B.n[2] - 1 + hi;
+  if (!ok) bchk_record(B.bchk, kid, i, j, k);
+  return ok;
+}
+#else
+__device__ __forceinline__ bool bchk(const DBlock &, int, int, int, int, int, int) { return true; }
+#endif
 
 __host__ __device__ inline long hidx(int i, int j, int k, int nx, int ny) {
   return (long)(i + 1) + (long)(nx + 2) * ((long)(j + 1) + (long)(ny + 2) * (long)(k + 1));
@@ -99,8 +123,18 @@ __host__ __device__ inline long iidx(int i, int j, int k, int nx, int ny) {
   return (long)i + (long)nx * ((long)j + (long)ny * (long)k);
 }
 __device__ inline double AX(const DBlock &B, int a, int which, int q) {
+#ifdef SNAC_BOUNDS_CHECK
+  if (a < 0 || a > 2 || which < 0 || which >= AX_NARR || q < -1 || q > B.n[a]) {
+    bchk_record(B.bchk, BK_AXIS, a, which, q);
+    return 0.0;
+  }
+#endif
   return B.ax[a][which * (B.n[a] + 2) + q + 1];
 }
+// the library's bounds flag (null in the normal build) and its host check: SNAC_ERR_BOUNDS with the kernel and
+// cell of the first failure, the flag cleared (bchk.cu)
+unsigned long long *bounds_flag();
+int bounds_check(cudaStream_t st);
 
 // a tile of one block: x = block, y,z,w = i0,j0,k0 (0-based interior)
 typedef int4 Tile;
