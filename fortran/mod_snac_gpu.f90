@@ -139,6 +139,47 @@ module mod_snac_gpu
       integer(c_int), value :: myrank
       real(c_double) :: p(*)
     end function
+    ! open / outflow boundaries of one block (bound.f90:250-541); logical masks passed as 0/1 integers
+    integer(c_int) function snac_set_open_bc_uvw(ibound,lo,hi,idir,visc,dr,u,v,w,p,tr) bind(C,name='snac_set_open_bc_uvw')
+      import
+      integer(c_int), value :: ibound, idir
+      integer(c_int), intent(in) :: lo(3), hi(3)
+      real(c_double), value :: visc, dr
+      real(c_double) :: u(*), v(*), w(*), tr(*)
+      real(c_double), intent(in) :: p(*)
+    end function
+    integer(c_int) function snac_set_open_bc_p(ibound,lo,hi,idir,drc,drf,alpha,p) bind(C,name='snac_set_open_bc_p')
+      import
+      integer(c_int), value :: ibound, idir
+      integer(c_int), intent(in) :: lo(3), hi(3)
+      real(c_double), intent(in) :: drc(0:1)
+      real(c_double), value :: drf, alpha
+      real(c_double) :: p(*)
+    end function
+    integer(c_int) function snac_cmpt_estimated_traction(ibound,lo,hi,idir,visc,dr,u,v,w,p,tr) &
+        bind(C,name='snac_cmpt_estimated_traction')
+      import
+      integer(c_int), value :: ibound, idir
+      integer(c_int), intent(in) :: lo(3), hi(3)
+      real(c_double), value :: visc, dr
+      real(c_double), intent(in) :: u(*), v(*), w(*), p(*)
+      real(c_double) :: tr(*)
+    end function
+    integer(c_int) function snac_outflow(is_outflow_bound,is_estimated_traction,lo,hi,dl,dl_h,visc,u,v,w,p, &
+        tr_x,tr_y,tr_z) bind(C,name='snac_outflow')
+      import
+      integer(c_int), intent(in) :: is_outflow_bound(0:1,3), is_estimated_traction(0:1,3), lo(3), hi(3)
+      real(c_double), intent(in) :: dl(0:1,3), dl_h(0:1,3)
+      real(c_double), value :: visc
+      real(c_double) :: u(*), v(*), w(*), p(*), tr_x(*), tr_y(*), tr_z(*)
+    end function
+    integer(c_int) function snac_outflow_p(is_outflow_bound,lo,hi,dlc,dlf,alpha,p) bind(C,name='snac_outflow_p')
+      import
+      integer(c_int), intent(in) :: is_outflow_bound(0:1,3), lo(3), hi(3)
+      real(c_double), intent(in) :: dlc(0:1,0:1,3), dlf(0:1,3)
+      real(c_double), value :: alpha
+      real(c_double) :: p(*)
+    end function
     ! domain layer (all blocks resident on the GPU after snac_init): the per-stage routines of main.f90:906-1043
     integer(c_int) function snac_rk_mom_all(irk) bind(C,name='snac_rk_mom_all')
       import

@@ -354,6 +354,27 @@ int snac_cnn_set_poll_limit(long polls);
 int snac_guess_grad(const float *x, const float *target, int nb, int H, int W, const float *params, float *grads,
                     double *loss);
 
+/* Open and outflow boundaries of one block (bound.f90:250-541; the reference's main.f90 does not call them).
+ * idir 1..3, ibound 0/1; u, v, w, p halo'd (lo-1:hi+1)^3; a traction plane tr (tr_x, tr_y, tr_z for idir 1, 2,
+ * 3) is (lo_t1-1:hi_t1+1, lo_t2-1:hi_t2+1, 0:1), t1 < t2 the two other axes.  Fortran (ibound, idir) arrays are
+ * [idir-1][ibound] here, dlc(0:1, ibound, idir) is dlc[idir-1][ibound][0:1]. */
+/* set_open_bc_uvw (bound.f90:250-328) */
+int snac_set_open_bc_uvw(int ibound, const int lo[3], const int hi[3], int idir, double visc, double dr, double *u,
+                         double *v, double *w, const double *p, double *tr);
+/* set_open_bc_p (bound.f90:330-375) */
+int snac_set_open_bc_p(int ibound, const int lo[3], const int hi[3], int idir, const double drc[2], double drf,
+                       double alpha, double *p);
+/* cmpt_estimated_traction (bound.f90:377-436) */
+int snac_cmpt_estimated_traction(int ibound, const int lo[3], const int hi[3], int idir, double visc, double dr,
+                                 const double *u, const double *v, const double *w, const double *p, double *tr);
+/* outflow (bound.f90:479-515) */
+int snac_outflow(const int is_outflow_bound[3][2], const int is_estimated_traction[3][2], const int lo[3],
+                 const int hi[3], const double dl[3][2], const double dl_h[3][2], double visc, double *u, double *v,
+                 double *w, double *p, double *tr_x, double *tr_y, double *tr_z);
+/* outflow_p (bound.f90:517-541) */
+int snac_outflow_p(const int is_outflow_bound[3][2], const int lo[3], const int hi[3], const double dlc[3][2][2],
+                   const double dlf[3][2], double alpha, double *p);
+
 /* No counterpart in the reference (the stand-in for compute-sanitizer and the reference's -fcheck=all debug
  * build): snac_bounds_checked is 1 in the bounds-check build (libsnac_gb300_checked.so, compiled with
  * -DSNAC_BOUNDS_CHECK), where the stencil, halo-exchange, boundary-condition and inflow kernels validate the

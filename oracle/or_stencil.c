@@ -632,3 +632,103 @@ void or_init_bc_rhs(const char cbc[3][2], const double bc[3][2], const double dl
   }
 #undef W
 }
+
+/* ---------------------------------------------------------------- open / outflow boundaries
+ * bound.f90:250-328 (set_open_bc_uvw), 330-375 (set_open_bc_p), 377-436 (cmpt_estimated_traction),
+ * 479-515 (outflow), 517-541 (outflow_p).  idir is 1..3 as in the reference; the traction planes tr are
+ * (lo_t1-1:hi_t1+1, lo_t2-1:hi_t2+1, 0:1), t1 < t2 the two other axes.  The plane loops run over every cell of
+ * the halo'd plane, as the reference's whole-array assignments do. */
+static double *cell_at(double *a, const int lo[3], const int hi[3], int ax, int q, int c1, int c2) {
+  int c[3];
+  const int t1 = ax == 0 ? 1 : 0, t2 = ax == 2 ? 1 : 2;
+  c[ax] = q; c[t1] = c1; c[t2] = c2;
+  return &F(a, c[0], c[1], c[2]);
+}
+static double *tr_at(double *tr, const int lo[3], const int hi[3], int ax, int ib, int c1, int c2) {
+  const int t1 = ax == 0 ? 1 : 0, t2 = ax == 2 ? 1 : 2;
+  const int m1 = hi[t1] - lo[t1] + 3, m2 = hi[t2] - lo[t2] + 3;
+  return &tr[(c1 - lo[t1] + 1) + (size_t)m1 * ((c2 - lo[t2] + 1) + (size_t)m2 * ib)];
+}
+#define PLANE_LOOP(ax)                                                               \
+  const int t1_ = (ax) == 0 ? 1 : 0, t2_ = (ax) == 2 ? 1 : 2;                        \
+  for (int c2 = lo[t2_] - 1; c2 <= hi[t2_] + 1; c2++)                                \
+    for (int c1 = lo[t1_] - 1; c1 <= hi[t1_] + 1; c1++)
+
+void or_set_open_bc_uvw(int ibound, const int lo[3], const int hi[3], int idir, double visc, double dr, double *u,
+                        double *v, double *w, const double *p, double *tr) {
+  const int ax = idir - 1;
+  double *f = ax == 0 ? u : (ax == 1 ? v : w);
+  const double norm = ibound == 0 ? 1.0 : -1.0;
+  const int q = ibound == 0 ? lo[ax] - 1 : hi[ax];
+  const double factor = -norm * dr / (2 * visc);
+  PLANE_LOOP(ax) {
+    double *t = tr_at(tr, lo, hi, ax, ibound, c1, c2);
+    if (ibound == 0) {
+      const double fn = *cell_at(f, lo, hi, ax, q + 1, c1, c2);
+      const double m = fmin(0.0, norm * fn);
+      *t = *t + .5 * (m * m);
+      *cell_at(f, lo, hi, ax, q, c1, c2) = fn + factor * (*t + *cell_at((double *)p, lo, hi, ax, q + 1, c1, c2));
+    } else {
+      const double fn = *cell_at(f, lo, hi, ax, q - 1, c1, c2);
+      const double m = fmin(0.0, norm * fn);
+      *t = *t + .5 * (m * m);
+      *cell_at(f, lo, hi, ax, q, c1, c2) = fn + factor * (*t + *cell_at((double *)p, lo, hi, ax, q, c1, c2));
+    }
+  }
+  if (ibound == 1) {
+    PLANE_LOOP(ax) *cell_at(f, lo, hi, ax, hi[ax] + 1, c1, c2) = *cell_at(f, lo, hi, ax, hi[ax], c1, c2);
+  }
+}
+
+void or_set_open_bc_p(int ibound, const int lo[3], const int hi[3], int idir, const double drc[2], double drf,
+                      double alpha, double *p) {
+  const int ax = idir - 1;
+  const int q = ibound == 0 ? lo[ax] : hi[ax];
+  PLANE_LOOP(ax) {
+    const double p0 = *cell_at(p, lo, hi, ax, q, c1, c2);
+    if (ibound == 0) {
+      const double pp = *cell_at(p, lo, hi, ax, q + 1, c1, c2);
+      *cell_at(p, lo, hi, ax, q - 1, c1, c2) = p0 + alpha * drc[0] * drf * p0 - (pp - p0) * drc[0] / drc[1];
+    } else {
+      const double pm = *cell_at(p, lo, hi, ax, q - 1, c1, c2);
+      *cell_at(p, lo, hi, ax, q + 1, c1, c2) = p0 + alpha * drc[1] * drf * p0 + (p0 - pm) * drc[1] / drc[0];
+    }
+  }
+}
+
+void or_cmpt_estimated_traction(int ibound, const int lo[3], const int hi[3], int idir, double visc, double dr,
+                                const double *u, const double *v, const double *w, const double *p, double *tr) {
+  const int ax = idir - 1;
+  double *f = (double *)(ax == 0 ? u : (ax == 1 ? v : w));
+  const int q = ibound == 0 ? lo[ax] - 1 : hi[ax];
+  const double factor = 2. * visc / dr;
+  PLANE_LOOP(ax) {
+    double *t = tr_at(tr, lo, hi, ax, ibound, c1, c2);
+    if (ibound == 0)
+      *t = -*cell_at((double *)p, lo, hi, ax, q + 1, c1, c2) +
+           factor * (*cell_at(f, lo, hi, ax, q + 2, c1, c2) - *cell_at(f, lo, hi, ax, q + 1, c1, c2));
+    else
+      *t = -*cell_at((double *)p, lo, hi, ax, q - 1, c1, c2) +
+           factor * (*cell_at(f, lo, hi, ax, q - 1, c1, c2) - *cell_at(f, lo, hi, ax, q - 2, c1, c2));
+  }
+}
+
+void or_outflow(const int is_outflow_bound[3][2], const int is_estimated_traction[3][2], const int lo[3],
+                const int hi[3], const double dl[3][2], const double dl_h[3][2], double visc, double *u, double *v,
+                double *w, double *p, double *tr_x, double *tr_y, double *tr_z) {
+  double *tr[3] = {tr_x, tr_y, tr_z};
+  for (int ax = 0; ax < 3; ax++)
+    for (int ib = 0; ib < 2; ib++) {
+      if (!is_outflow_bound[ax][ib]) continue;
+      PLANE_LOOP(ax) *tr_at(tr[ax], lo, hi, ax, ib, c1, c2) = 0.0;
+      if (is_estimated_traction[ax][ib]) or_cmpt_estimated_traction(ib, lo, hi, ax + 1, visc, dl_h[ax][ib], u, v, w, p, tr[ax]);
+      or_set_open_bc_uvw(ib, lo, hi, ax + 1, visc, dl[ax][ib], u, v, w, p, tr[ax]);
+    }
+}
+
+void or_outflow_p(const int is_outflow_bound[3][2], const int lo[3], const int hi[3], const double dlc[3][2][2],
+                  const double dlf[3][2], double alpha, double *p) {
+  for (int ax = 0; ax < 3; ax++)
+    for (int ib = 0; ib < 2; ib++)
+      if (is_outflow_bound[ax][ib]) or_set_open_bc_p(ib, lo, hi, ax + 1, dlc[ax][ib], dlf[ax][ib], alpha, p);
+}

@@ -116,6 +116,12 @@ def lib():
         L.or_cmpt_strain_rate.argtypes = [ip, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
         L.or_cmpt_rotation_rate.argtypes = [ip, dp, dp, dp, dp, dp, dp, dp]
         L.or_cmpt_q_criterion.argtypes = [ip, dp, dp, dp]
+        d_ = C.c_double
+        L.or_set_open_bc_uvw.argtypes = [i, ip, ip, i, d_, d_, dp, dp, dp, dp, dp]
+        L.or_set_open_bc_p.argtypes = [i, ip, ip, i, dp, d_, d_, dp]
+        L.or_cmpt_estimated_traction.argtypes = [i, ip, ip, i, d_, d_, dp, dp, dp, dp, dp]
+        L.or_outflow.argtypes = [ip, ip, ip, ip, dp, dp, d_, dp, dp, dp, dp, dp, dp, dp]
+        L.or_outflow_p.argtypes = [ip, ip, ip, dp, dp, d_, dp]
         L.or_bounduvw_block.argtypes = [C.c_char_p, ip, ip, dp, i, ip, ip, i, dp, dp, dp, dp, dp, dp, dp, dp, dp]
         L.or_boundp_block.argtypes = [C.c_char_p, ip, ip, dp, ip, ip, i, dp, dp, dp, dp]
         L.or_r2r_lines.argtypes = [i, i, i, C.c_long, C.c_long, dp]

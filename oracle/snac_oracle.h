@@ -116,6 +116,18 @@ void or_cmpt_strain_rate(const int n[3], const double *dxc, const double *dyc, c
 void or_cmpt_rotation_rate(const int n[3], const double *dxc, const double *dyc, const double *dzc, const double *ux,
                            const double *uy, const double *uz, double *ens);
 void or_cmpt_q_criterion(const int n[3], const double *ens, const double *str, double *qcr);
+/* open / outflow boundaries, bound.f90:250-541 (traction planes (lo_t1-1:hi_t1+1, lo_t2-1:hi_t2+1, 0:1)) */
+void or_set_open_bc_uvw(int ibound, const int lo[3], const int hi[3], int idir, double visc, double dr, double *u,
+                        double *v, double *w, const double *p, double *tr);
+void or_set_open_bc_p(int ibound, const int lo[3], const int hi[3], int idir, const double drc[2], double drf,
+                      double alpha, double *p);
+void or_cmpt_estimated_traction(int ibound, const int lo[3], const int hi[3], int idir, double visc, double dr,
+                                const double *u, const double *v, const double *w, const double *p, double *tr);
+void or_outflow(const int is_outflow_bound[3][2], const int is_estimated_traction[3][2], const int lo[3],
+                const int hi[3], const double dl[3][2], const double dl_h[3][2], double visc, double *u, double *v,
+                double *w, double *p, double *tr_x, double *tr_y, double *tr_z);
+void or_outflow_p(const int is_outflow_bound[3][2], const int lo[3], const int hi[3], const double dlc[3][2][2],
+                  const double dlf[3][2], double alpha, double *p);
 void or_init_bc_rhs(const char cbc[3][2], const double bc[3][2], const double dl[3][2],
                     const int is_bound[3][2], const int is_centered[3], const int lo[3],
                     const int hi[3], const int periods[3],

@@ -139,6 +139,11 @@ PROTOTYPES = {
     "snac_cnn_conv3x3": (C.c_int, [FP, C.c_int, C.c_int, C.c_int, FP, FP, C.c_int, FP]),
     "snac_cnn_set_poll_limit": (C.c_int, [C.c_long]),
     "snac_guess_grad": (C.c_int, [FP, FP, C.c_int, C.c_int, C.c_int, FP, FP, DP]),
+    "snac_set_open_bc_uvw": (C.c_int, [C.c_int, IP, IP, C.c_int, C.c_double, C.c_double, DP, DP, DP, DP, DP]),
+    "snac_set_open_bc_p": (C.c_int, [C.c_int, IP, IP, C.c_int, DP, C.c_double, C.c_double, DP]),
+    "snac_cmpt_estimated_traction": (C.c_int, [C.c_int, IP, IP, C.c_int, C.c_double, C.c_double, DP, DP, DP, DP, DP]),
+    "snac_outflow": (C.c_int, [IP, IP, IP, IP, DP, DP, C.c_double, DP, DP, DP, DP, DP, DP, DP]),
+    "snac_outflow_p": (C.c_int, [IP, IP, IP, DP, DP, C.c_double, DP]),
     "snac_bounds_checked": (C.c_int, []),
     "snac_bounds_selftest": (C.c_int, []),
     "snac_unet_nparams": (C.c_int, []),

@@ -294,3 +294,57 @@ def test_registered_mirrors(snac_lib, oracle_mod):
         close(p, ref)
     finally:
         capi.check(L.snac_unregister(p.ctypes.data))
+
+
+def test_open_and_outflow_bcs(snac_lib, oracle_mod):
+    """bound.f90:250-541 on the device against the oracle: every face of the estimated-traction and zero-traction
+    open BC on the wall-normal velocity, the traction estimate alone, the traction BC on the correction pressure,
+    and the outflow / outflow_p drivers over all six faces (the same operations in the same order, no FMA
+    contraction on either side: bit-identical)."""
+    rng = np.random.default_rng(210)
+    L, O = capi.lib(), oracle_mod.lib()
+    IP = C.POINTER(C.c_int)
+    nh = [n + 2 for n in N]
+
+    def planes(ax):
+        t1, t2 = [q for q in range(3) if q != ax]
+        return np.asfortranarray(rng.standard_normal((nh[t1], nh[t2], 2)))
+
+    for idir in (1, 2, 3):
+        for ib in (0, 1):
+            u, v, w, p = field(rng), field(rng), field(rng), field(rng)
+            tr = planes(idir - 1)
+            ref = [a.copy(order="F") for a in (u, v, w, tr)]
+            got = [a.copy(order="F") for a in (u, v, w, tr)]
+            O.or_set_open_bc_uvw(ib, I3(LO), I3(HI), idir, 1e-3, 0.3, *(P(a) for a in ref[:3]), P(p), P(ref[3]))
+            assert L.snac_set_open_bc_uvw(ib, I3(LO), I3(HI), idir, 1e-3, 0.3, *(P(a) for a in got[:3]), P(p),
+                                          P(got[3])) == 0, L.snac_last_error()
+            for g, r in zip(got, ref):
+                np.testing.assert_array_equal(g, r)
+            t_ref, t_got = tr.copy(order="F"), tr.copy(order="F")
+            O.or_cmpt_estimated_traction(ib, I3(LO), I3(HI), idir, 2e-3, 0.7, P(u), P(v), P(w), P(p), P(t_ref))
+            assert L.snac_cmpt_estimated_traction(ib, I3(LO), I3(HI), idir, 2e-3, 0.7, P(u), P(v), P(w), P(p),
+                                                  P(t_got)) == 0, L.snac_last_error()
+            np.testing.assert_array_equal(t_got, t_ref)
+            drc = np.array([0.4, 0.55])
+            p_ref, p_got = p.copy(order="F"), p.copy(order="F")
+            O.or_set_open_bc_p(ib, I3(LO), I3(HI), idir, P(drc), 0.45, 3.0, P(p_ref))
+            assert L.snac_set_open_bc_p(ib, I3(LO), I3(HI), idir, P(drc), 0.45, 3.0, P(p_got)) == 0
+            np.testing.assert_array_equal(p_got, p_ref)
+    mask = np.array([[1, 1], [0, 1], [1, 0]], dtype=np.int32)
+    est = np.array([[1, 0], [0, 1], [1, 1]], dtype=np.int32)
+    dl, dl_h = rng.random((3, 2)) + 0.1, rng.random((3, 2)) + 0.1
+    dlc, dlf = rng.random((3, 2, 2)) + 0.1, rng.random((3, 2)) + 0.1
+    u, v, w, p = field(rng), field(rng), field(rng), field(rng)
+    trs = [planes(ax) for ax in range(3)]
+    ref = [a.copy(order="F") for a in (u, v, w, p, *trs)]
+    got = [a.copy(order="F") for a in (u, v, w, p, *trs)]
+    O.or_outflow(mask.ctypes.data_as(IP), est.ctypes.data_as(IP), I3(LO), I3(HI), P(dl), P(dl_h), 1.5e-3,
+                 *(P(a) for a in ref))
+    assert L.snac_outflow(mask.ctypes.data_as(IP), est.ctypes.data_as(IP), I3(LO), I3(HI), P(dl), P(dl_h), 1.5e-3,
+                          *(P(a) for a in got)) == 0, L.snac_last_error()
+    for g, r in zip(got, ref):
+        np.testing.assert_array_equal(g, r)
+    O.or_outflow_p(mask.ctypes.data_as(IP), I3(LO), I3(HI), P(dlc), P(dlf), 2.0, P(ref[3]))
+    assert L.snac_outflow_p(mask.ctypes.data_as(IP), I3(LO), I3(HI), P(dlc), P(dlf), 2.0, P(got[3])) == 0
+    np.testing.assert_array_equal(got[3], ref[3])
