@@ -388,7 +388,7 @@ static int upload_domain(Domain &d) {
     B.u = (double *)d.alloc(nh); B.v = (double *)d.alloc(nh); B.w = (double *)d.alloc(nh);
     B.p = (double *)d.alloc(nh); B.pp = (double *)d.alloc(nh);
     B.ru = (double *)d.alloc(ni); B.rv = (double *)d.alloc(ni); B.rw = (double *)d.alloc(ni);
-    B.nu = (double *)d.alloc(ni); B.nv = (double *)d.alloc(ni); B.nw = (double *)d.alloc(ni);
+    B.nu = (double *)d.alloc(nh); B.nv = (double *)d.alloc(nh); B.nw = (double *)d.alloc(nh);
     if (!B.u || !B.v || !B.w || !B.p || !B.pp || !B.ru || !B.nu || !B.nw) { set_error("device allocation failed (fields)"); return SNAC_ERR_NOMEM; }
     for (int q = 0; q < d.c.nscal; q++) {
       B.s[q] = (double *)d.alloc(nh);
@@ -408,8 +408,16 @@ static int upload_domain(Domain &d) {
     d.rhsp_off.push_back(rh);
     rh += H.rhsp[0].size() + H.rhsp[1].size() + H.rhsp[2].size();
   }
-  d.d_db = (DBlock *)d.alloc(d.nblocks * sizeof(DBlock));
-  SNAC_CUDA(cudaMemcpy(d.d_db, d.db.data(), d.nblocks * sizeof(DBlock), cudaMemcpyHostToDevice));
+  for (int par = 0; par < 2; par++) {  // the block table as set up, and with u, v, w and nu, nv, nw swapped
+    std::vector<DBlock> t = d.db;
+    if (par)
+      for (auto &B : t) { std::swap(B.u, B.nu); std::swap(B.v, B.nv); std::swap(B.w, B.nw); }
+    d.d_db_set[par] = (DBlock *)d.alloc(d.nblocks * sizeof(DBlock));
+    if (!d.d_db_set[par]) { set_error("device allocation failed (block table)"); return SNAC_ERR_NOMEM; }
+    SNAC_CUDA(cudaMemcpy(d.d_db_set[par], t.data(), d.nblocks * sizeof(DBlock), cudaMemcpyHostToDevice));
+  }
+  d.uvw_par = 0;
+  d.d_db = d.d_db_set[0];
   auto tl = make_tiles(sz, TX, TY, TZ), th = make_tiles(szh, TX, TY, TZ);
   d.ntiles = (int)tl.size();
   d.ntiles_halo = (int)th.size();
@@ -566,6 +574,16 @@ static int helm_step(Domain &d, PoissonSolver &S, double alphai) {
   return SNAC_OK;
 }
 
+// u, v, w and nu, nv, nw trade places on the host mirror, in the block table the kernels read and in the
+// TMA-staged kernel's tensor maps
+static int swap_uvw(Domain &d) {
+  for (auto &B : d.db) { std::swap(B.u, B.nu); std::swap(B.v, B.nv); std::swap(B.w, B.nw); }
+  d.uvw_par ^= 1;
+  d.d_db = d.d_db_set[d.uvw_par];
+  std::swap(d.tma, d.tma_alt);
+  return SNAC_OK;
+}
+
 static int rk_mom_all(Domain &d, int irk) {
   RkMomParams prm;
   prm.f1 = RKC[irk][0] * d.dt;
@@ -577,8 +595,12 @@ static int rk_mom_all(Domain &d, int irk) {
   prm.boussinesq = d.c.boussinesq && d.c.nscal > 0;  // rk.f90:104-108 with scalars(1)
   if (prm.boussinesq)
     for (int a = 0; a < 3; a++) prm.gb[a] = prm.f12 * d.c.gacc[a] * d.c.beta * 0.5;
+  prm.halo_out = 1;
   SNAC_TRY(launch_rk_mom(d.d_db, d.d_tiles, d.ntiles, prm, d.st));
-  SNAC_TRY(launch_rk_mom_writeback(d.d_db, d.d_tiles, d.ntiles, d.st));
+  // the new interior is in nu, nv, nw: give them the halo of before and let the buffers trade places (the
+  // reference updates u in place, rk.f90:82-101, which leaves the same values)
+  SNAC_TRY(launch_uvw_halo_copy(d.d_db, d.nblocks, std::max(d.maxplane[0], std::max(d.maxplane[1], d.maxplane[2])), d.st));
+  SNAC_TRY(swap_uvw(d));
   if (d.c.impdiff) {  // main.f90:947-995: u, v, w Helmholtz solves with alphai = 1/(-visc*dtrk/2)
     const double alpha = -prm.visc * ((RKC[irk][0] + RKC[irk][1]) * d.dt) / 2.0;
     for (int comp = 0; comp < 3; comp++) SNAC_TRY(helm_step(d, *d.hs[HF_U + comp], 1.0 / alpha));

@@ -310,6 +310,7 @@ int snac_rk_mom(const double rkpar[2], const int lo[3], const int hi[3], const d
   }
   prm.visc = visc;
   prm.impdiff = impdiff;
+  prm.halo_out = 0;  // the caller owns u, v, w: interior scratch, written back
   prm.boussinesq = boussinesq;
   SNAC_TRY(launch_rk_mom(ob.dblk, ob.dtiles, ob.ntiles, prm, 0));
   SNAC_TRY(launch_rk_mom_writeback(ob.dblk, ob.dtiles, ob.ntiles, 0));

@@ -122,7 +122,8 @@ k_rk_mom(const DBlock *__restrict__ Bs, const Tile *__restrict__ T, RkMomParams 
     const double h = 0.5 * prm.f12;
     un = fma(-h, rdu, un); vn = fma(-h, rdv, vn); wn = fma(-h, rdw, wn);
   }
-  B.nu[ci] = un; B.nv[ci] = vn; B.nw[ci] = wn;
+  if (prm.halo_out) { B.nu[c] = un; B.nv[c] = vn; B.nw[c] = wn; }
+  else { B.nu[ci] = un; B.nv[ci] = vn; B.nw[ci] = wn; }
 }
 
 __global__ void __launch_bounds__(TX * TY * TZ)
@@ -147,6 +148,33 @@ int launch_rk_mom_writeback(const DBlock *dB, const Tile *dT, int ntiles, cudaSt
   if (ntiles <= 0) return SNAC_OK;
   SNAC_CUDA(launch_k(k_rk_mom_writeback, dim3(ntiles), dim3(TX, TY, TZ), 0, st, dB, dT));
   SNAC_CUDA(cudaGetLastError());
+  return SNAC_OK;
+}
+
+// The six halo planes of u, v, w into nu, nv, nw, one CTA row per (face, block): the new interior the
+// momentum stage wrote plus the halo of before is exactly the field the reference's in-place update leaves.
+__global__ void k_uvw_halo_copy(const DBlock *__restrict__ Bs) {
+  pdl_enter();
+  const DBlock &B = Bs[blockIdx.y];
+  const int a = blockIdx.z >> 1, side = blockIdx.z & 1;
+  const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+  const int m1 = B.n[t1] + 2, m2 = B.n[t2] + 2;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= m1 * m2) return;
+  int c[3];
+  c[t1] = q % m1 - 1;
+  c[t2] = q / m1 - 1;
+  c[a] = side ? B.n[a] : -1;
+  if (!bchk(B, BK_TILE, c[0], c[1], c[2], -1, 1)) return;
+  const long h = hidx(c[0], c[1], c[2], B.n[0], B.n[1]);
+  B.nu[h] = B.u[h];
+  B.nv[h] = B.v[h];
+  B.nw[h] = B.w[h];
+}
+
+int launch_uvw_halo_copy(const DBlock *dB, int nblocks, int maxplane, cudaStream_t st) {
+  if (nblocks <= 0) return SNAC_OK;
+  SNAC_CUDA(launch_k(k_uvw_halo_copy, dim3((maxplane + 255) / 256, nblocks, 6), dim3(256), 0, st, dB));
   return SNAC_OK;
 }
 

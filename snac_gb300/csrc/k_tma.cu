@@ -169,37 +169,41 @@ int tma_setup(Domain &d) {
     if (d.db[b].n[0] & 1) return SNAC_OK;  // row pitch not a multiple of 16 bytes
   PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
   if (!enc) return SNAC_OK;
-  auto maps = new TmaMaps();
+  // maps of u, v, w as they are now, and of nu, nv, nw, which become u, v, w after the next momentum stage
+  auto maps = new TmaMaps(), alt = new TmaMaps();
   std::vector<int4> tl;
   for (int b = 0; b < d.nblocks; b++) {
     const DBlock &B = d.db[b];
     const cuuint64_t gdim[3] = {(cuuint64_t)B.n[0] + 2, (cuuint64_t)B.n[1] + 2, (cuuint64_t)B.n[2] + 2};
     const cuuint64_t gstr[2] = {gdim[0] * 8, gdim[0] * gdim[1] * 8};
     const cuuint32_t box[3] = {BX, BY, BZ}, estr[3] = {1, 1, 1};
-    double *f[3] = {B.u, B.v, B.w};
-    for (int q = 0; q < 3; q++) {
-      const CUresult r = enc(&maps->m[b][q], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, f[q], gdim, gstr, box, estr,
-                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-      if (r != CUDA_SUCCESS) {
-        delete maps;
-        set_error("cuTensorMapEncodeTiled failed (%d) for block %d field %d", (int)r, b, q);
-        return SNAC_ERR_CUDA;
+    double *f[2][3] = {{B.u, B.v, B.w}, {B.nu, B.nv, B.nw}};
+    for (int s = 0; s < 2; s++)
+      for (int q = 0; q < 3; q++) {
+        const CUresult r = enc(&(s ? alt : maps)->m[b][q], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, f[s][q], gdim, gstr,
+                               box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) {
+          delete maps;
+          delete alt;
+          set_error("cuTensorMapEncodeTiled failed (%d) for block %d field %d", (int)r, b, q);
+          return SNAC_ERR_CUDA;
+        }
       }
-    }
     for (int k = 0; k < B.n[2]; k += FZ)
       for (int j = 0; j < B.n[1]; j += FY)
         for (int i = 0; i < B.n[0]; i += FX) tl.push_back(make_int4(b, i, j, k));
   }
   int4 *dt = (int4 *)d.alloc(tl.size() * sizeof(int4));
   int *derr = (int *)d.alloc(sizeof(int));
-  if (!dt || !derr) { delete maps; set_error("device allocation failed (TMA tiles)"); return SNAC_ERR_NOMEM; }
+  if (!dt || !derr) { delete maps; delete alt; set_error("device allocation failed (TMA tiles)"); return SNAC_ERR_NOMEM; }
   SNAC_CUDA(cudaMemcpy(dt, tl.data(), tl.size() * sizeof(int4), cudaMemcpyHostToDevice));
   int dev = 0, nsm = 0;
   SNAC_CUDA(cudaGetDevice(&dev));
   SNAC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   SNAC_CUDA(cudaFuncSetAttribute((const void *)k_fillps_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, TMA_SMEM));
   d.tma = maps;
+  d.tma_alt = alt;
   d.tma_tiles = dt;
   d.tma_ntiles = (int)tl.size();
   d.tma_err = derr;
@@ -209,7 +213,9 @@ int tma_setup(Domain &d) {
 
 void tma_destroy(Domain &d) {
   delete d.tma;
+  delete d.tma_alt;
   d.tma = nullptr;
+  d.tma_alt = nullptr;
 }
 
 // fillps on every block through the TMA-staged kernel; false in *done when it does not apply

@@ -149,7 +149,11 @@ struct Domain {
   int periods[3] = {0, 0, 0}, is_periodic[3] = {0, 0, 0};
   double vol_all = 0.0;
   std::vector<DBlock> db;
-  DBlock *d_db = nullptr;
+  DBlock *d_db = nullptr;            // the block table the kernels read: d_db_set[uvw_par]
+  // the momentum stage writes the new velocity into nu, nv, nw (halo'd) and the two buffers then trade places:
+  // the two block tables (u, v, w and nu, nv, nw swapped) are uploaded once and uvw_par selects one
+  DBlock *d_db_set[2] = {nullptr, nullptr};
+  int uvw_par = 0;
   Tile *d_tiles = nullptr, *d_tiles_halo = nullptr;
   int ntiles = 0, ntiles_halo = 0;
   FaceLink *d_links[3] = {nullptr, nullptr, nullptr};
@@ -167,6 +171,7 @@ struct Domain {
   std::unique_ptr<PoissonSolver> hs[3 + SNAC_MAX_SCAL];  // IMPDIFF: Helmholtz solvers of u, v, w, scalars
   GuessState *guess = nullptr;       // learned initial guess of the pressure solve (off unless requested)
   TmaMaps *tma = nullptr;            // TMA-staged fillps: tensor maps, tile list, CTAs, error flag (null: n/a)
+  TmaMaps *tma_alt = nullptr;        // the maps of the swapped buffers (uvw_par 1)
   int4 *tma_tiles = nullptr;
   int tma_ntiles = 0, tma_ctas = 0;
   int *tma_err = nullptr;

@@ -87,7 +87,8 @@ struct DBlock {
   double *s[SNAC_MAX_SCAL];    // halo'd scalars
   double *ru, *rv, *rw;        // RK storage dudtrko.. (interior)
   double *rs[SNAC_MAX_SCAL];   // dsdtrko (interior)
-  double *nu, *nv, *nw;        // interior scratch: new velocity of a stage before write-back
+  double *nu, *nv, *nw;        // new velocity of a stage: halo'd in the domain layer (swapped with u, v, w after
+                               // the stage), interior in the per-block path (written back)
   double *ns;                  // interior scratch for scalars
   const double *ax[3];         // AxisArr tables per axis: ax[a][AX_*(n+2) + q + 1]
   unsigned long long *bchk;    // bounds-check build: the flag the device checks record into (null otherwise)
@@ -145,6 +146,7 @@ struct RkMomParams {
   double gb[3];       // f12*gacc*beta*0.5 (Boussinesq)
   double visc;
   int impdiff, boussinesq;
+  int halo_out;       // 1: nu, nv, nw are halo'd (index as u); 0: interior
 };
 
 struct RkScalParams {
@@ -155,6 +157,8 @@ struct RkScalParams {
 // kernel launchers (k_stencil.cu)
 int launch_rk_mom(const DBlock *dB, const Tile *dT, int ntiles, const RkMomParams &prm, cudaStream_t st);
 int launch_rk_mom_writeback(const DBlock *dB, const Tile *dT, int ntiles, cudaStream_t st);
+// the six halo planes of u, v, w copied into nu, nv, nw (before the two trade places)
+int launch_uvw_halo_copy(const DBlock *dB, int nblocks, int maxplane, cudaStream_t st);
 int launch_rk_scal(const DBlock *dB, const Tile *dT, int ntiles, const RkScalParams &prm, double *part,
                    cudaStream_t st);
 int launch_rk_scal_writeback(const DBlock *dB, const Tile *dT, int ntiles, int sidx, cudaStream_t st);
