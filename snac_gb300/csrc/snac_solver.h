@@ -91,6 +91,10 @@ int launch_vcycle_coarse3d(const MgProblem &P, const MgGeom &G, int l0, const T 
 constexpr size_t MG_SMEM_OPT_IN = 226 * 1024;      // opt-in limit set on every kernel that needs more than 48 KB
 constexpr size_t MG_COARSE_SMEM_MAX = 218 * 1024;
 constexpr size_t MG_COARSE3D_SMEM_MAX = 226 * 1024;
+// 3-D mode, default start of the one-CTA coarse V-cycle: the finest level of at most this many cells (about
+// four per thread); a finer level is swept faster by the level-by-level kernels, which spread over the GPU
+// (L-shaped box 288 x 288 x 96: 65.8 ms per step from its 1,944-cell level, 71.7 ms from the 15,552-cell one)
+constexpr long MG_COARSE3D_CELLS = 4096;
 template <typename T>
 int launch_vcycle_coarse(const MgProblem &P, int l0, const T *shift, const int *active, T *x, const T *b,
                          cudaStream_t st);

@@ -649,7 +649,8 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
     // bit mask: 1 tiled smoother FP32, 2 coarse tail FP32, 4 tiled FP64, 8 coarse tail FP64.  Default 11: the
     // tile's redundant halo updates cost more than they save where FP64 arithmetic bounds.
     P.fused = o.mg_fuse == -1 ? 0 : (o.mg_fuse > 0 ? o.mg_fuse & 15 : 11);
-    // the finest level the one-CTA coarse tail may start at (default: the finest that fits)
+    // the finest level the one-CTA coarse tail may start at: the one asked for, or by default the finest that
+    // fits (3-D mode: and has at most MG_COARSE3D_CELLS cells)
     const int lmin = std::max(0, o.mg_cta_level);
     for (int prec = 0; prec < 2; prec++) {
       P.cta_level[prec] = P.nlev;
@@ -657,6 +658,7 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
         size_t bytes;
         if (S.mode3d) bytes = prec ? coarse3d_smem_bytes<double>(P, l) : coarse3d_smem_bytes<float>(P, l);
         else bytes = prec ? coarse_smem_bytes<double>(P, l) : coarse_smem_bytes<float>(P, l);
+        if (S.mode3d && o.mg_cta_level <= 0 && P.L[l].ncell > MG_COARSE3D_CELLS) continue;
         if (bytes <= (S.mode3d ? MG_COARSE3D_SMEM_MAX : MG_COARSE_SMEM_MAX)) { P.cta_level[prec] = l; break; }
       }
     }

@@ -161,9 +161,9 @@ int snac_autotune(int steps, snac_tune_result *out) {
   }
   // Candidates are searched one group at a time, each group varying its settings around the best so far:
   // the solve (plain FP64, or mixed with 5, 6 or 7 FP32 iterations per refinement step) x the coarse-level
-  // sweeps; then, for the plane systems, the smoother tile shape, the waves of CTAs per batched launch and
-  // the level where the one-CTA coarse V-cycle starts; then, for the mixed solve, FP64 finishing after two
-  // refinement steps against FP32 refinement to convergence.
+  // sweeps; then, for the plane systems, the smoother tile shape and the waves of CTAs per batched launch;
+  // then the level where the one-CTA coarse V-cycle starts; then, for the mixed solve, FP64 finishing after
+  // two refinement steps against FP32 refinement to convergence.
   snac_options best_opt = opt0;
   double best = 1e300;
   int ntimed = 0, found = 0;
@@ -207,8 +207,8 @@ int snac_autotune(int steps, snac_tune_result *out) {
     for (int w : {1, 2, 4}) { snac_options o = best_opt; o.mg_waves = w; g.push_back(o); }
     rc = try_group(g);
   }
-  if (rc == SNAC_OK && found && plane && d->ps) {
-    // the one-CTA coarse V-cycle from the finest level that fits (the default) or one level coarser
+  if (rc == SNAC_OK && found && d->ps) {
+    // the one-CTA coarse V-cycle from the default level, one level coarser, or (3-D mode) one level finer
     d->opt = best_opt;
     rc = rebuild(*d);
     if (rc == SNAC_OK) {
@@ -218,6 +218,7 @@ int snac_autotune(int steps, snac_tune_result *out) {
       if (l0 + 1 < d->ps->P.nlev) {
         snac_options o = best_opt; o.mg_cta_level = l0 + 1; g.push_back(o);
         o.mg_cta_level = l0; g.push_back(o);
+        if (!plane && l0 > 0) { o.mg_cta_level = l0 - 1; g.push_back(o); }
       }
       rc = try_group(g);
     }

@@ -691,6 +691,29 @@ def test_autotune_restores_state(snac_lib, precision):
         assert np.max(np.abs(a - b)) <= 1e-9 * np.max(np.abs(a))
 
 
+def test_autotune_3d_solve_searches_the_coarse_level(snac_lib):
+    """With the 3-D solve snac_autotune times the solve group (mixed with 5, 6, 7 inner iterations, plain), the
+    level where the one-CTA coarse V-cycle starts (default, one coarser, one finer) and, for the mixed solve, the
+    two refinement strategies; the state after the call is the state before it, bit for bit."""
+    import dataclasses
+    case = dataclasses.replace(cases.l_shaped_box(16, 8), dt_f=4e-3)
+    d = Domain(case, precision=1, use_graph=1)
+    try:
+        d.bounduvw(False)
+        d.step(2)
+        before = [d.get(ib, k) for ib in range(len(case.blocks)) for k in (capi.U, capi.V, capi.W, capi.P)]
+        r = d.autotune(1)
+        assert 4 <= r["candidates"] <= 9, r
+        assert r["mg_cta_level"] >= 1, r
+        after = [d.get(ib, k) for ib in range(len(case.blocks)) for k in (capi.U, capi.V, capi.W, capi.P)]
+        for a, b in zip(before, after):
+            np.testing.assert_array_equal(a, b)
+        assert d.step(2) == 0
+        assert d.stats()["residual"] <= case.tol and d.chkdiv()[1] < 1e-10
+    finally:
+        d.close()
+
+
 @pytest.mark.parametrize("fail_at", [0, 3])
 def test_autotune_error_restores_settings_and_state(snac_lib, fail_at):
     """A candidate that fails part-way (a host-side injected error after its solvers are rebuilt) makes
