@@ -133,6 +133,9 @@ typedef struct snac_options {
                          (default: TMA where the blocks allow it: even x extents, at most 16 blocks) */
   int pdl;            /* -1: the solver's inner-loop kernels launch without programmatic dependent launch
                          (default: with it, each kernel's set-up overlapping the previous kernel's tail) */
+  int mg_inv;         /* 1: the FP32 tiled smoother forms 1 / diagonal of each system in registers from the cell's
+                         coefficients and the system's shift instead of reading the per-system table (the same
+                         values); default: the table */
 } snac_options;
 
 typedef struct snac_step_stats {

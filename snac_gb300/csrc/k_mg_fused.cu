@@ -117,7 +117,8 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
                                                          const T *__restrict__ b, const T *__restrict__ xin,
                                                          const T *__restrict__ xc, double *__restrict__ part_bx,
                                                          const int *__restrict__ singular, double *__restrict__ part_x,
-                                                         double *__restrict__ part_b, int part_stride) {
+                                                         double *__restrict__ part_b, int part_stride,
+                                                         const T *__restrict__ shift, int inv_inline) {
   static_assert(NW % 2 == 0, "rows w + NW q of a thread must share their colour parity");
   constexpr int SH = NW * R, BY = SH - 2 * TH;
   constexpr int NA = MODE == 1 ? 4 : 2;
@@ -148,6 +149,7 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
   const T *__restrict__ invd = LA<T>::invd(L);
   const bool xhalf = C.coarsened[0] != 0, yhalf = C.coarsened[1] != 0;
   T ce[R][2], cw[R][2], cn[R][2], cs[R][2];
+  T dcc[R][2], dwt[R][2];  // inv_inline: the cell's cc and w01 (1 / diagonal = rcpt(fma(shift, w01, cc)), as the table)
 #pragma unroll
   for (int q = 0; q < R; q++) {
     const int r = w + NW * q;
@@ -178,6 +180,8 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
       cw[q][p] = w_;
       cn[q][p] = n_;
       cs[q][p] = s_;
+      dcc[q][p] = (inv_inline && (live >> (2 * q + p) & 1)) ? LA<T>::cc(L)[cidx[q] + p] : T(0);
+      dwt[q][p] = (inv_inline && (live >> (2 * q + p) & 1)) ? LA<T>::w01(L)[cidx[q] + p] : T(0);
       // unwrapped: each global cell is stored by one tile only (stored cells are never wrapped)
       const int col = 2 * lane + p, ui = i0 + col, uj = j0 + r;
       if (r >= TH && r < TH + BY && col >= TH && col < TH + TBX && ui < n0 && uj < n1 && (live >> (2 * q + p) & 1))
@@ -198,7 +202,7 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
       const bool in = inb >> q & 1;
       T *sq = sk + NW * q * 64;
       cp_async_zfill<2 * sizeof(T)>(sq, b + off + cidx[q], in);
-      cp_async_zfill<2 * sizeof(T)>(sq + SH * 64, invd + off + cidx[q], in);
+      if (!inv_inline) cp_async_zfill<2 * sizeof(T)>(sq + SH * 64, invd + off + cidx[q], in);
       if (MODE == 1) {
         cp_async_zfill<2 * sizeof(T)>(sq + 2 * SH * 64, xin + off + cidx[q], in);
         if (xhalf) cp_async_zfill<sizeof(T)>(sq + 3 * SH * 64, xc + offc + cidxc[q], in);
@@ -229,6 +233,7 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
     __syncthreads();  // the staged inputs are complete and the previous system's sweeps are over
     T bv[R][2], iv[R][2];
     {
+      const T sh = inv_inline ? shift[cur] : T(0);
       const T *sk = stg + (size_t)k * NA * SH * 64 + spos;
 #pragma unroll
       for (int q = 0; q < R; q++) {
@@ -237,7 +242,7 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
         for (int p = 0; p < 2; p++) {
           const bool lv = live >> (2 * q + p) & 1;
           bv[q][p] = lv ? sq[p] : T(0);
-          iv[q][p] = lv ? sq[SH * 64 + p] : T(0);
+          iv[q][p] = lv ? (inv_inline ? rcpt(fmat(sh, dwt[q][p], dcc[q][p])) : sq[SH * 64 + p]) : T(0);
           T x_ = 0;
           if (MODE == 1 && lv) x_ = sq[2 * SH * 64 + p] + sq[3 * SH * 64 + (xhalf ? 0 : p)];
           (p ? xo : xe)[tpos + NW * q * TRS] = x_;
@@ -750,11 +755,19 @@ static int allow_smem(const void *fn, size_t bytes) {
   return SNAC_OK;
 }
 
+// the per-system shifts in the tile's precision (the 1 / diagonal formed in registers needs them)
+template <typename T>
+static const T *shift_of_tile(const MgProblem &P) {
+  if constexpr (sizeof(T) == 8) return P.shift;
+  else return P.shiftf;
+}
+
 template <typename T, int NW, int R>
 static int launch_tile(const MgProblem &P, const MgLevelD &L, const MgLevelD &C, int nt, int nhalf, const int *active,
                        int first_color, int mode, T *x, const T *b, const T *xin, const T *xc, double *part_bx,
                        double *part_x, double *part_b, int part_stride, cudaStream_t st) {
   const int *sing = P.any_singular && part_bx ? P.singular : nullptr;
+  const int inv = sizeof(T) == 4 && P.tile_inv ? 1 : 0;  // FP64 keeps the table (its reciprocal is costly)
   const size_t smem = tile_smem_bytes<T>(NW * R, mode);
   const int sb = plane_batch(P, nt, NW == 16 ? 2 : 4);
   const dim3 g((unsigned)nt, (unsigned)((P.nsys + sb - 1) / sb));
@@ -762,12 +775,12 @@ static int launch_tile(const MgProblem &P, const MgLevelD &L, const MgLevelD &C,
     SNAC_TRY(allow_smem((const void *)k_rbgs_tile2d<T, NW, R, 1>, smem));
     SNAC_CUDA(launch_k(k_rbgs_tile2d<T, NW, R, 1>, g, dim3(NW * 32), smem, st, L, C, P.periodic[0], P.periodic[1],
                        active, P.nsys, sb, first_color, nhalf, x, b, xin, xc, part_bx, sing, part_x, part_b,
-                       part_stride));
+                       part_stride, shift_of_tile<T>(P), inv));
   } else {
     SNAC_TRY(allow_smem((const void *)k_rbgs_tile2d<T, NW, R, 0>, smem));
     SNAC_CUDA(launch_k(k_rbgs_tile2d<T, NW, R, 0>, g, dim3(NW * 32), smem, st, L, C, P.periodic[0], P.periodic[1],
                        active, P.nsys, sb, first_color, nhalf, x, b, xin, xc, part_bx, sing, part_x, part_b,
-                       part_stride));
+                       part_stride, shift_of_tile<T>(P), inv));
   }
   SNAC_CUDA(cudaGetLastError());
   return SNAC_OK;

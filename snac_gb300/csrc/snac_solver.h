@@ -54,6 +54,7 @@ struct MgProblem {
   int cta_level[2];                  // first level run by k_vcycle_coarse / k_vcycle_coarse3d ([0] FP32, [1] FP64); nlev = none
   int nsm;                           // multiprocessors of the device (sizes the system batches)
   int tile_shape;                    // FP32 smoother tile: 0 auto, 1..4 = 8x2, 8x3, 16x2, 16x3 (warps x rows)
+  int tile_inv;                      // FP32 tiled smoother: 1 / diagonal formed in registers instead of read
   int waves;                         // waves of CTAs per batched plane launch
   int red_batch;                     // the reducing plane kernels batch systems (0: one system per CTA)
   int any_singular;                  // some system is singular (pure Neumann, zero shift)

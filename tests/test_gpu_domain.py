@@ -163,6 +163,30 @@ def test_fused_vcycle_matches_unfused(snac_lib, precision, which, nu_coarse):
         assert np.max(np.abs(a - b)) <= 1e-9 * scale
 
 
+def test_tile_smoother_inverse_diagonal_in_registers_is_bitwise(snac_lib):
+    """mg_inv = 1 makes the FP32 tiled smoother form 1 / diagonal from the cell's coefficients and the system's
+    shift instead of reading the per-system table; the table holds exactly those values, so the solves are
+    bit for bit the same."""
+    case = cases.channel_4block(nx=(32, 64), ny=(32, 48), nz=8)
+    out = {}
+    for inv in (0, 1):
+        d = Domain(case, precision=1, mg_inv=inv)
+        try:
+            rng = np.random.default_rng(12)
+            for ib in range(len(case.blocks)):
+                for k in (capi.U, capi.V, capi.W):
+                    d.set(ib, k, rng.standard_normal(d.shape(ib, k)))
+            d.bounduvw(False)
+            d.fillps(0.01)
+            d.updt_rhs()
+            assert d.solve_pressure() == 0
+            out[inv] = [d.get(ib, capi.PP) for ib in range(len(case.blocks))]
+        finally:
+            d.close()
+    for a, b in zip(out[0], out[1]):
+        np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_fused_vcycle_iterations_multiwave(snac_lib, precision):
     """Fused and unfused V-cycles are the same preconditioner, also when the tiled kernels run in
