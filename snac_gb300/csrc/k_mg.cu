@@ -70,9 +70,10 @@ __global__ void __launch_bounds__(256) k_rbgs(MgLevelD L, MgGeom G, const T *shi
   if (i >= L.n[0] || j >= L.n[1]) return;
   const int c = i + L.n[0] * (j + L.n[1] * k);
   const unsigned cd = L.code[c];
-  if (cd & 0x8000) return;
   const long off = L.ncell * s;
   T *__restrict__ xs = x + off;
+  // the operands are read before the cell's code is tested (an inactive cell's neighbours are in range too), so
+  // the loads do not wait for it; only the store depends on it
   T d, acc;
   if constexpr (SEP) {
     d = diag_sep(L, shift[s], c, i, j, k);
@@ -81,7 +82,9 @@ __global__ void __launch_bounds__(256) k_rbgs(MgLevelD L, MgGeom G, const T *shi
     d = diag_of<T>(L, G, shift[s], c);
     acc = offdiag<T>(L, G, [&](int e) { return xs[e]; }, c, i, j, k);
   }
-  xs[c] = (b[off + c] - acc) * rcpt(d);
+  const T bv = b[off + c];
+  if (cd & 0x8000) return;
+  xs[c] = (bv - acc) * rcpt(d);
 }
 
 // coarse b <- sum over children of (b - A x) on the fine level; coarse x <- 0

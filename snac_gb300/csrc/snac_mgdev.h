@@ -98,21 +98,29 @@ __device__ __forceinline__ float offdiag_sep(const MgLevelD &L, const MgGeom &G,
                                              unsigned cd) {
   const int n0 = L.n[0], n1 = L.n[1], n2 = L.n[2], st = n0 * n1;
   const float w0 = L.Wf[0][i], w1 = L.Wf[1][j], w2 = L.Wf[2][k];
+  // every neighbour value and 1-D factor is read before the fold bits are tested (the wrapped indices are in
+  // range for every cell), so these loads do not wait for the cell's code; the FMAs run in the same order
+  const float xe = v(i + 1 < n0 ? c + 1 : c + 1 - n0), xw = v(i > 0 ? c - 1 : c + n0 - 1);
+  const float xn = v(j + 1 < n1 ? c + n0 : c + n0 - st), xs = v(j > 0 ? c - n0 : c + st - n0);
+  const float xt = v(k + 1 < n2 ? c + st : c + st - st * n2), xb = v(k > 0 ? c - st : c + st * (n2 - 1));
+  const float ae = L.caf[0][i], aw = L.caf[0][i > 0 ? i - 1 : n0 - 1];
+  const float an = L.caf[1][j], as = L.caf[1][j > 0 ? j - 1 : n1 - 1];
+  const float at = L.caf[2][k], ab = L.caf[2][k > 0 ? k - 1 : n2 - 1];
   float acc = 0.f;
   if (!(G.periodic[0] && n0 == 1)) {
     const float wt = w1 * w2;
-    if (!((cd >> 2) & 3)) acc = fmat(L.caf[0][i] * wt, v(i + 1 < n0 ? c + 1 : c + 1 - n0), acc);
-    if (!(cd & 3)) acc = fmat(L.caf[0][i > 0 ? i - 1 : n0 - 1] * wt, v(i > 0 ? c - 1 : c + n0 - 1), acc);
+    if (!((cd >> 2) & 3)) acc = fmat(ae * wt, xe, acc);
+    if (!(cd & 3)) acc = fmat(aw * wt, xw, acc);
   }
   if (!(G.periodic[1] && n1 == 1)) {
     const float wt = w0 * w2;
-    if (!((cd >> 6) & 3)) acc = fmat(L.caf[1][j] * wt, v(j + 1 < n1 ? c + n0 : c + n0 - st), acc);
-    if (!((cd >> 4) & 3)) acc = fmat(L.caf[1][j > 0 ? j - 1 : n1 - 1] * wt, v(j > 0 ? c - n0 : c + st - n0), acc);
+    if (!((cd >> 6) & 3)) acc = fmat(an * wt, xn, acc);
+    if (!((cd >> 4) & 3)) acc = fmat(as * wt, xs, acc);
   }
   if (!(G.periodic[2] && n2 == 1)) {
     const float wt = w0 * w1;
-    if (!((cd >> 10) & 3)) acc = fmat(L.caf[2][k] * wt, v(k + 1 < n2 ? c + st : c + st - st * n2), acc);
-    if (!((cd >> 8) & 3)) acc = fmat(L.caf[2][k > 0 ? k - 1 : n2 - 1] * wt, v(k > 0 ? c - st : c + st * (n2 - 1)), acc);
+    if (!((cd >> 10) & 3)) acc = fmat(at * wt, xt, acc);
+    if (!((cd >> 8) & 3)) acc = fmat(ab * wt, xb, acc);
   }
   return acc;
 }
