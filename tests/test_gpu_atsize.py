@@ -7,7 +7,9 @@ kinetic energy within 1e-8, max|div u| <= 1e-10) on the layouts the benchmarks r
   100 steps, with the plain FP64 solve and with FP32 V-cycles inside FP64 refinement (graph replay);
 * the triperiodic Taylor-Green vortex 128^3 (FFT along z, 128 systems of 128x128) from its analytic
   velocity and pressure, 50 steps;
-* the lid-driven cavity 64^3 (3-D multigrid, Re = 1000, CFL 0.5) from rest, 100 steps.
+* the lid-driven cavity 64^3 (3-D multigrid, Re = 1000, CFL 0.5) from rest, 100 steps;
+* the L-shaped closed box, three 144x144x96 blocks (3-D multigrid on a solver box a third inactive), from
+  rest, 10 steps.
 
 The oracle (C restatement with OpenMP on all host cores) runs each case once; the GPU paths are compared
 against it.  Each test prints the measured errors.  These sizes exercise what the small layouts of the
@@ -115,5 +117,24 @@ def test_lid_driven_cavity_64_100_steps(snac_lib, oracle_mod):
         d = _gpu_run(case, fields, 100, precision)
         try:
             _check(case, O, d, f"lid-driven cavity 64^3, precision {precision}")
+        finally:
+            d.close()
+
+
+def test_l_shaped_box_3x144x144x96_10_steps(snac_lib, oracle_mod):
+    """The L-shaped closed box at its benchmark size (three 144x144x96 blocks, 5.97 M cells, 3-D multigrid on
+    the 288x288x96 solver box with a third of it inactive), lid-driven from rest: 10 steps (the oracle's 3-D
+    solve takes about 15 s per step on 16 host cores)."""
+    case = cases.l_shaped_box(144, 96)
+
+    def init(grid):
+        z = np.zeros((146, 146, 98), order="F")
+        return {ib: ((capi.U, z), (capi.V, z), (capi.W, z), (capi.P, z)) for ib in range(3)}
+
+    O, fields = _oracle_run(oracle_mod, "lbox", case, init, 10)
+    for precision in (0, 1):
+        d = _gpu_run(case, fields, 10, precision)
+        try:
+            _check(case, O, d, f"L-shaped box 3x144x144x96, precision {precision}")
         finally:
             d.close()
