@@ -526,11 +526,17 @@ def main():
     roof = None
     if 0 in smoother:
         sm_ms, sm_bytes = smoother[0]
-        name = "k_rbgs_tile2d<float> level 0 pre-smoother"
+        restricting = opts.get("mg_restrict", 0) != -1
+        name = ("k_rbgs_tile2d_restrict<float> level 0 pre-smoother" if restricting
+                else "k_rbgs_tile2d<float> level 0 pre-smoother")
         roof = {"kernel": name, "bound": "hbm", "achieved": sm_bytes / (sm_ms * 1e-3) / 1e9, "peak": hbm_peak,
                 "unit": "GB/s", "frac": None, "traffic": ncu_traffic(name), "peak_source": peak_src,
                 "launch_ms": sm_ms, "bytes_per_launch": sm_bytes,
-                "algorithmic_bytes": "12 B per cell and system: b and 1/diagonal read, x written (FP32)",
+                "algorithmic_bytes": "12 B per cell and system: b and 1/diagonal read, x written (FP32); the "
+                                     "restricting form also writes the coarse right-hand side, 4 B per coarse "
+                                     "cell and system (2 B per cell on the channel's y-halved level 1)"
+                                     if restricting else
+                                     "12 B per cell and system: b and 1/diagonal read, x written (FP32)",
                 "share_of_step": shares["smoother"]["ms_per_step"] / mixed["ms"],
                 "levels": {str(k): {"launch_ms": v[0], "achieved_gbs": v[1] / (v[0] * 1e-3) / 1e9}
                            for k, v in smoother.items()}}

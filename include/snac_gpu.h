@@ -136,6 +136,9 @@ typedef struct snac_options {
   int mg_inv;         /* 1: the FP32 tiled smoother forms 1 / diagonal of each system in registers from the cell's
                          coefficients and the system's shift instead of reading the per-system table (the same
                          values); default: the table */
+  int mg_restrict;    /* -1: the FP32 tiled pre-smoother of levels 0 and 1 leaves the residual restriction to a
+                         separate pass over the level; default: it restricts the residual of its own output cells
+                         (the same values, one pass fewer per level and V-cycle) */
 } snac_options;
 
 typedef struct snac_step_stats {
@@ -172,9 +175,11 @@ int snac_profile_read(int *launches, double *total_ms);
  * (a host-side counter incremented at every launch site). */
 int snac_launch_count(long long *n);
 /* No counterpart in the reference: time `reps` launches of the FP32 tiled pre-smoother on level `level`
- * of the pressure solver of the current domain, all systems active, with CUDA events on the library
- * stream.  Returns the mean time per launch and its algorithmic bytes (b, 1/diagonal read, x written:
- * 12 bytes per cell and system).  The solver's level buffers are overwritten. */
+ * of the pressure solver of the current domain as its V-cycles run it (restricting its residual unless
+ * snac_options.mg_restrict is -1), all systems active, with CUDA events on the library stream.  Returns
+ * the mean time per launch and its algorithmic bytes (b, 1/diagonal read, x written: 12 bytes per cell and
+ * system; with the restriction also 4 bytes per coarse cell and system written).  The solver's level
+ * buffers are overwritten. */
 int snac_bench_smoother(int level, int reps, double *ms_per_launch, double *bytes_per_launch);
 
 /* ---------------------------------------------------------------- host mirrors */

@@ -51,7 +51,8 @@ class Options(C.Structure):
                 ("nu_coarse", C.c_int), ("inner_iters", C.c_int), ("inner_tol", C.c_double),
                 ("inner_adapt", C.c_int), ("refine_steps", C.c_int), ("mg_fuse", C.c_int),
                 ("mg_cta_level", C.c_int), ("mg_tile", C.c_int), ("mg_waves", C.c_int), ("mg_red_batch", C.c_int),
-                ("mg_lnu", C.c_int), ("tma", C.c_int), ("pdl", C.c_int), ("mg_inv", C.c_int)]
+                ("mg_lnu", C.c_int), ("tma", C.c_int), ("pdl", C.c_int), ("mg_inv", C.c_int),
+                ("mg_restrict", C.c_int)]
 
 
 class TuneResult(C.Structure):

@@ -1154,10 +1154,15 @@ int snac_bench_smoother(int level, int reps, double *ms_per_launch, double *byte
   SNAC_CUDA(cudaEventCreate(&e0));
   SNAC_CUDA(cudaEventCreate(&e1));
   int rc = SNAC_OK;
+  const MgLevelD &C = P.L[level + 1];
+  const bool restrict_ = P.tile_restrict != 0;
   for (int q = 0; q < 2 + reps && rc == SNAC_OK; q++) {
     if (q == 2) cudaEventRecord(e0, d->st);
-    rc = launch_rbgs_tile2d<float>(P, level, nullptr, 0, 0, L.xpf, L.bf, nullptr, nullptr, nullptr, nullptr, nullptr, 0,
-                                   nullptr, d->st);
+    if (restrict_)
+      rc = launch_rbgs_tile2d_restrict<float>(P, level, nullptr, L.xpf, L.bf, C.bf, nullptr, d->st);
+    else
+      rc = launch_rbgs_tile2d<float>(P, level, nullptr, 0, 0, L.xpf, L.bf, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                     0, nullptr, d->st);
   }
   cudaEventRecord(e1, d->st);
   float ms = 0.f;
@@ -1168,7 +1173,7 @@ int snac_bench_smoother(int level, int reps, double *ms_per_launch, double *byte
   cudaEventDestroy(e1);
   SNAC_TRY(rc);
   *ms_per_launch = ms / reps;
-  *bytes_per_launch = 12.0 * (double)L.ncell * (double)P.nsys;
+  *bytes_per_launch = (12.0 * (double)L.ncell + (restrict_ ? 4.0 * (double)C.ncell : 0.0)) * (double)P.nsys;
   return SNAC_OK;
 }
 

@@ -212,9 +212,17 @@ int mg_vcycle_impl(const MgProblem &P, const MgGeom &G, int l, const T *shift, c
   const MgLevelD &C = P.L[l + 1];
   if ((fuse & 1) && tile2d_ok(P, l, prec)) {
     T *xp = LA<T>::xp(P.L[l]);  // pre-smoothed x (the post-smoother reads it while writing x)
-    SNAC_TRY(launch_rbgs_tile2d<T>(P, l, active, 0, 0, xp, b, (const T *)nullptr, (const T *)nullptr, nullptr,
-                                   nullptr, nullptr, 0, nullptr, st));
-    SNAC_TRY(plane_restrict<T>(P, l, shift, active, xp, b, LA<T>::b(C), LA<T>::x(C), st));
+    if (!prec && P.tile_restrict) {
+      // the pre-smoother restricts its own residual; the coarse x needs zeroing only where the next level is
+      // swept from x (neither the one-CTA coarse V-cycle nor a tiled pre-smoother, which start from zero)
+      const bool next_from_zero = ((fuse & 2) && l + 1 >= P.cta_level[prec]) || ((fuse & 1) && tile2d_ok(P, l + 1, prec));
+      SNAC_TRY(launch_rbgs_tile2d_restrict<T>(P, l, active, xp, b, LA<T>::b(C), next_from_zero ? nullptr : LA<T>::x(C),
+                                              st));
+    } else {
+      SNAC_TRY(launch_rbgs_tile2d<T>(P, l, active, 0, 0, xp, b, (const T *)nullptr, (const T *)nullptr, nullptr,
+                                     nullptr, nullptr, 0, nullptr, st));
+      SNAC_TRY(plane_restrict<T>(P, l, shift, active, xp, b, LA<T>::b(C), LA<T>::x(C), st));
+    }
     SNAC_TRY(mg_vcycle_impl<T>(P, G, l + 1, shift, active, nullptr, nullptr, nullptr, 0, nullptr, st));
     return launch_rbgs_tile2d<T>(P, l, active, 1, 1, x, b, (const T *)xp, (const T *)LA<T>::x(C), part_bx, part_x,
                                  part_b, part_stride, nchunk_bx, st);

@@ -13,7 +13,14 @@
 //   the coarse-grid correction while loading (prolongation fused) and can emit
 //   the partials of b.x (r.z of the Krylov iteration), one per warp.  Tiles overlap, so a
 //   launch never reads the array it writes: the pre-smoother writes xp and the
-//   post-smoother reads xp + correction and writes x.
+//   post-smoother reads xp + correction and writes x.  The pre-smoother can also form the residual of its
+//   output cells and restrict it to the next level (mode 2): from a zero start the first half-sweep is exact
+//   everywhere in the tile (the cells outside it are still zero too), so after t half-sweeps only cells
+//   within t - 1 of the tile edge differ from a global sweep and the neighbours of the output cells are
+//   exact as well.  The children of a coarse cell (even-aligned pairs) always lie in one tile: along x they
+//   are a thread's own column pair, along y the rows of warps w and w + 1, whose odd warp hands its residuals
+//   over in shared memory; so the separate residual-restriction pass over the level goes away.  The first
+//   half-sweep of a pre-smoother (zero neighbours) is done while its inputs are loaded.
 // k_vcycle_coarse: one CTA of 1024 threads per system runs the V-cycle from
 //   level l0 down to the coarsest solve and back, with x, b and 1/d of every
 //   level in shared memory, and the couplings too where they fit (the top
@@ -36,12 +43,12 @@ namespace snac {
 namespace {
 constexpr int TH = 4;              // tile halo = most half-sweeps per launch (2 nu with nu <= 2)
 constexpr int TSW = 64;            // tile width
-constexpr int TBX = TSW - 2 * TH;  // output columns per tile
 // tile shapes: NW warps x R rows per warp = tile height SH (output rows SH - 2 TH)
 struct TileShape { int nw, r; };
 const TileShape SHAPES_F[] = {{8, 2}, {8, 3}, {16, 2}, {16, 3}, {8, 4}, {16, 4}};  // snac_options.mg_tile 1..6
 constexpr int NSHAPES_F = 6;
 const TileShape SHAPES_D[] = {{8, 2}};
+constexpr int TBX = TSW - 2 * TH;  // output columns per tile
 inline int tile_by(TileShape t) { return t.nw * t.r - 2 * TH; }
 inline int tiles_for(const MgLevelD &L, TileShape t) {
   return ((L.n[0] + TBX - 1) / TBX) * ((L.n[1] + tile_by(t) - 1) / tile_by(t));
@@ -100,32 +107,36 @@ bool tile2d_ok(const MgProblem &P, int l, int prec) {
 constexpr int TRS = 34;
 
 // dynamic shared memory of one tile CTA: the even/odd x tile (SH rows plus a zero pad row above and
-// below) and two stages of the staged inputs (b and 1/d; in mode 1 also the pre-smoothed x and the coarse
-// correction), [stage][array][row][64]
+// below), two stages of the staged inputs (b and 1/d; in mode 1 also the pre-smoothed x and the coarse
+// correction), [stage][array][row][64], and in mode 2 the residuals the odd warps hand over (SH 64 entries)
+// and the owned cells' cc and w01, [2][2R][thread] (2 SH 64 entries)
 template <typename T>
 inline size_t tile_smem_bytes(int sh, int mode) {
-  return (2 * (size_t)(sh + 2) * TRS + 2 * (size_t)(mode == 1 ? 4 : 2) * sh * 64) * sizeof(T);
+  return (2 * (size_t)(sh + 2) * TRS + 2 * (size_t)(mode == 1 ? 4 : 2) * sh * 64 + (mode == 2 ? 3 * (size_t)sh * 64 : 0)) *
+         sizeof(T);
 }
 
 // Every per-cell address, mask and coupling is set up once per CTA and reused for all its systems.  The
 // cells on the tile's outermost ring are updated with zero neighbours from the pads; like any cell within
 // TH of the tile edge they may differ from a global sweep, and none of them is stored.
 template <typename T, int NW, int R, int MODE>
-__global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C, int per0, int per1,
-                                                         const int *__restrict__ active, int nsys, int sb,
-                                                         int first_color, int nhalf, T *__restrict__ x,
-                                                         const T *__restrict__ b, const T *__restrict__ xin,
-                                                         const T *__restrict__ xc, double *__restrict__ part_bx,
-                                                         const int *__restrict__ singular, double *__restrict__ part_x,
-                                                         double *__restrict__ part_b, int part_stride,
-                                                         const T *__restrict__ shift, int inv_inline) {
+__device__ __forceinline__ void rbgs_tile2d(MgLevelD L, MgLevelD C, int per0, int per1, const int *__restrict__ active,
+                                            int nsys, int sb, int first_color, int nhalf, T *__restrict__ x,
+                                            const T *__restrict__ b, const T *__restrict__ xin,
+                                            const T *__restrict__ xc, double *__restrict__ part_bx,
+                                            const int *__restrict__ singular, double *__restrict__ part_x,
+                                            double *__restrict__ part_b, int part_stride, const T *__restrict__ shift,
+                                            int inv_inline, T *__restrict__ bco, T *__restrict__ xcz) {
   static_assert(NW % 2 == 0, "rows w + NW q of a thread must share their colour parity");
   constexpr int SH = NW * R, BY = SH - 2 * TH;
+  static_assert(TBX % 2 == 0 && TH % 2 == 0 && BY % 2 == 0, "coarse cells must not straddle tiles");
   constexpr int NA = MODE == 1 ? 4 : 2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *const xe = reinterpret_cast<T *>(smem_raw);  // [SH + 2][TRS], tile row r at r + 1, pair l at l + 1
   T *const xo = xe + (SH + 2) * TRS;
   T *const stg = xo + (SH + 2) * TRS;
+  T *const res = stg + 2 * NA * SH * 64;          // mode 2: residuals handed from odd to even warps
+  T *const dtab = res + SH * 64;                  // mode 2: cc, w01 of the owned cells, [2][2R][thread]
   const int n0 = L.n[0], n1 = L.n[1];
   const int ntx = (n0 + TBX - 1) / TBX;
   const int i0 = (int)(blockIdx.x % ntx) * TBX - TH, j0 = (int)(blockIdx.x / ntx) * BY - TH;
@@ -140,10 +151,11 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
     gi0 = (g >= 0 && g < n0) ? g : (per0 ? wrap(g, n0) : -1);
   }
   int cidx[R];          // global index of the even cell of the owned pair of row q (0 when outside)
-  int cidxc[R];         // mode 1: index of the coarse cell of that pair
+  int cidxc[R];         // modes 1, 2: index of the coarse cell of that pair
   unsigned live = 0;    // bit 2q+p: active cell
   unsigned inb = 0;     // bit q: the pair of row q lies inside the level (staged from global memory)
   unsigned store = 0;   // bit 2q+p: an output cell of this tile
+  unsigned outq = 0;    // mode 2: bit q: the pair of row q lies in the output region and inside the level
   const T *__restrict__ cp0 = LA<T>::cp(L, 0);
   const T *__restrict__ cp1 = LA<T>::cp(L, 1);
   const T *__restrict__ invd = LA<T>::invd(L);
@@ -182,10 +194,17 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
       cs[q][p] = s_;
       dcc[q][p] = (inv_inline && (live >> (2 * q + p) & 1)) ? LA<T>::cc(L)[cidx[q] + p] : T(0);
       dwt[q][p] = (inv_inline && (live >> (2 * q + p) & 1)) ? LA<T>::w01(L)[cidx[q] + p] : T(0);
+      if (MODE == 2 && !inv_inline) {  // each thread reads back only its own entries: no barrier needed
+        const int dq = (2 * q + p) * NW * 32 + (int)threadIdx.x;
+        const bool lv = live >> (2 * q + p) & 1;
+        dtab[dq] = lv ? LA<T>::cc(L)[cidx[q] + p] : T(0);
+        dtab[2 * R * NW * 32 + dq] = lv ? LA<T>::w01(L)[cidx[q] + p] : T(0);
+      }
       // unwrapped: each global cell is stored by one tile only (stored cells are never wrapped)
       const int col = 2 * lane + p, ui = i0 + col, uj = j0 + r;
-      if (r >= TH && r < TH + BY && col >= TH && col < TH + TBX && ui < n0 && uj < n1 && (live >> (2 * q + p) & 1))
-        store |= 1u << (2 * q + p);
+      const bool outc = r >= TH && r < TH + BY && col >= TH && col < TH + TBX && ui < n0 && uj < n1;
+      if (outc && (live >> (2 * q + p) & 1)) store |= 1u << (2 * q + p);
+      if (p == 0 && outc) outq |= 1u << q;
     }
   }
   // this thread's cells in the tile and the staging area
@@ -232,6 +251,10 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
     }
     __syncthreads();  // the staged inputs are complete and the previous system's sweeps are over
     T bv[R][2], iv[R][2];
+    // the pre-smoother's first half-sweep sees only zero neighbours (x = 0 everywhere, pads included): its
+    // sum of neighbour terms is +0, so (b - 0) / d = b (1/d) exactly, and it is done while loading
+    const int t0 = MODE != 1 && nhalf > 0 ? 1 : 0;
+    const int pfirst = (first_color + par) & 1;  // the column of the pair that half-sweep 0 updates
     {
       const T sh = inv_inline ? shift[cur] : T(0);
       const T *sk = stg + (size_t)k * NA * SH * 64 + spos;
@@ -245,11 +268,12 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
           iv[q][p] = lv ? (inv_inline ? rcpt(fmat(sh, dwt[q][p], dcc[q][p])) : sq[SH * 64 + p]) : T(0);
           T x_ = 0;
           if (MODE == 1 && lv) x_ = sq[2 * SH * 64 + p] + sq[3 * SH * 64 + (xhalf ? 0 : p)];
+          if (MODE != 1 && t0 && p == pfirst) x_ = bv[q][p] * iv[q][p];
           (p ? xo : xe)[tpos + NW * q * TRS] = x_;
         }
       }
     }
-    for (int t = 0; t < nhalf; t++) {
+    for (int t = t0; t < nhalf; t++) {
       __syncthreads();
       if (((first_color + t + par) & 1) == 0) {  // even columns 2 lane: E = odd(lane), W = odd(lane - 1)
 #pragma unroll
@@ -304,9 +328,122 @@ __global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C,
         if (lane == 0) { part_x[e] = tx; part_b[e] = tb; }
       }
     }
+    if constexpr (MODE == 2) {
+      // residual of every owned output cell, term by term as the level kernels form it (the off-diagonal
+      // sum in the order E, W, N, S, then b - (shift w01 + cc) x - sum); 0 for every other cell.  The cells'
+      // cc and w01 (the same for every system) were put in shared memory at set-up
+      __syncthreads();  // the last half-sweep of every thread is complete
+      const T sh = shift[cur];
+      T rv[R][2];
+#pragma unroll
+      for (int q = 0; q < R; q++) {
+#pragma unroll
+        for (int p = 0; p < 2; p++) {
+          rv[q][p] = 0;
+          if (store >> (2 * q + p) & 1) {
+            const T *o = (p ? xo : xe) + tpos + NW * q * TRS;  // the cell's colour array
+            const T *e = (p ? xe : xo) + tpos + NW * q * TRS;  // the other colour
+            T acc = fmat(ce[q][p], p ? e[1] : e[0], T(0));
+            acc = fmat(cw[q][p], p ? e[0] : e[-1], acc);
+            acc = fmat(cn[q][p], o[TRS], acc);
+            acc = fmat(cs[q][p], o[-TRS], acc);
+            const int dq = (2 * q + p) * NW * 32 + (int)threadIdx.x;
+            const T dv = inv_inline ? fmat(sh, dwt[q][p], dcc[q][p]) : fmat(sh, dtab[2 * R * NW * 32 + dq], dtab[dq]);
+            rv[q][p] = bv[q][p] - fmat(dv, o[0], acc);
+          }
+        }
+      }
+      // summed restriction, children in the order (dj outer, di inner) of the level kernels.  The children of
+      // a coarse cell along x are the thread's own pair; along y, rows 2J and 2J + 1 of the tile belong to
+      // warps w and w + 1 (same lane, same q: NW and the tile's first row are even), so the odd warps hand
+      // their residuals over in shared memory and the even warps store the coarse cells
+      T *__restrict__ bcs = bco + C.ncell * (long)cur;
+      T *__restrict__ xcs = xcz ? xcz + C.ncell * (long)cur : nullptr;
+      const bool oddw = w & 1;
+      if (yhalf) {
+        T *const hand = res + (w >> 1) * 32 + lane;  // [q][p][NW / 2][32 lanes]
+        if (oddw) {
+#pragma unroll
+          for (int q = 0; q < R; q++) {
+            hand[q * NW * 32] = rv[q][0];
+            hand[q * NW * 32 + NW * 16] = rv[q][1];
+          }
+        }
+        __syncthreads();
+        if (!oddw) {
+#pragma unroll
+          for (int q = 0; q < R; q++) {
+            if (!(outq >> q & 1)) continue;
+            const T u0 = hand[q * NW * 32], u1 = hand[q * NW * 32 + NW * 16];
+            if (xhalf) {
+              T sum = 0;
+              sum += rv[q][0];
+              sum += rv[q][1];
+              sum += u0;
+              sum += u1;
+              bcs[cidxc[q]] = sum;
+              if (xcs) xcs[cidxc[q]] = T(0);
+            } else {
+              T s0 = 0, s1 = 0;
+              s0 += rv[q][0];
+              s0 += u0;
+              s1 += rv[q][1];
+              s1 += u1;
+              bcs[cidxc[q]] = s0;
+              bcs[cidxc[q] + 1] = s1;
+              if (xcs) { xcs[cidxc[q]] = T(0); xcs[cidxc[q] + 1] = T(0); }
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < R; q++) {
+          if (!(outq >> q & 1)) continue;
+          if (xhalf) {
+            T sum = 0;
+            sum += rv[q][0];
+            sum += rv[q][1];
+            bcs[cidxc[q]] = sum;
+            if (xcs) xcs[cidxc[q]] = T(0);
+          } else {  // no axis halved (not built by the hierarchy; kept general)
+            T s0 = 0, s1 = 0;
+            s0 += rv[q][0];
+            s1 += rv[q][1];
+            bcs[cidxc[q]] = s0;
+            bcs[cidxc[q] + 1] = s1;
+            if (xcs) { xcs[cidxc[q]] = T(0); xcs[cidxc[q] + 1] = T(0); }
+          }
+        }
+      }
+    }
     cur = nxt;
     k ^= 1;
   }
+}
+
+// modes 0 (pre-smoother) and 1 (post-smoother)
+template <typename T, int NW, int R, int MODE>
+__global__ void __launch_bounds__(NW * 32) k_rbgs_tile2d(MgLevelD L, MgLevelD C, int per0, int per1,
+                                                         const int *__restrict__ active, int nsys, int sb,
+                                                         int first_color, int nhalf, T *__restrict__ x,
+                                                         const T *__restrict__ b, const T *__restrict__ xin,
+                                                         const T *__restrict__ xc, double *__restrict__ part_bx,
+                                                         const int *__restrict__ singular, double *__restrict__ part_x,
+                                                         double *__restrict__ part_b, int part_stride,
+                                                         const T *__restrict__ shift, int inv_inline) {
+  rbgs_tile2d<T, NW, R, MODE>(L, C, per0, per1, active, nsys, sb, first_color, nhalf, x, b, xin, xc, part_bx, singular,
+                              part_x, part_b, part_stride, shift, inv_inline, nullptr, nullptr);
+}
+
+// mode 2 (pre-smoother restricting its residual into bco, zeroing xcz when given); with two rows per thread
+// at most 64 registers, so that 2048 threads' worth of CTAs fit on a multiprocessor as in mode 0
+template <typename T, int NW, int R>
+__global__ void __launch_bounds__(NW * 32, R == 2 ? 1024 / (NW * 32) : 1)
+    k_rbgs_tile2d_restrict(MgLevelD L, MgLevelD C, int per0, int per1, const int *__restrict__ active, int nsys, int sb,
+                           int nhalf, T *__restrict__ x, const T *__restrict__ b, const T *__restrict__ shift,
+                           int inv_inline, T *__restrict__ bco, T *__restrict__ xcz) {
+  rbgs_tile2d<T, NW, R, 2>(L, C, per0, per1, active, nsys, sb, 0, nhalf, x, b, nullptr, nullptr, nullptr, nullptr,
+                           nullptr, nullptr, 0, shift, inv_inline, bco, xcz);
 }
 
 // ---------------------------------------------------------------- whole coarse V-cycle in one CTA
@@ -765,13 +902,23 @@ static const T *shift_of_tile(const MgProblem &P) {
 template <typename T, int NW, int R>
 static int launch_tile(const MgProblem &P, const MgLevelD &L, const MgLevelD &C, int nt, int nhalf, const int *active,
                        int first_color, int mode, T *x, const T *b, const T *xin, const T *xc, double *part_bx,
-                       double *part_x, double *part_b, int part_stride, cudaStream_t st) {
+                       double *part_x, double *part_b, int part_stride, cudaStream_t st, T *bco = nullptr,
+                       T *xcz = nullptr) {
   const int *sing = P.any_singular && part_bx ? P.singular : nullptr;
   const int inv = sizeof(T) == 4 && P.tile_inv ? 1 : 0;  // FP64 keeps the table (its reciprocal is costly)
   const size_t smem = tile_smem_bytes<T>(NW * R, mode);
   const int sb = plane_batch(P, nt, NW == 16 ? 2 : 4);
   const dim3 g((unsigned)nt, (unsigned)((P.nsys + sb - 1) / sb));
-  if (mode == 1) {
+  if (mode == 2) {
+    if constexpr (sizeof(T) == 4) {
+      SNAC_TRY(allow_smem((const void *)k_rbgs_tile2d_restrict<T, NW, R>, smem));
+      SNAC_CUDA(launch_k(k_rbgs_tile2d_restrict<T, NW, R>, g, dim3(NW * 32), smem, st, L, C, P.periodic[0],
+                         P.periodic[1], active, P.nsys, sb, nhalf, x, b, shift_of_tile<T>(P), inv, bco, xcz));
+    } else {
+      set_error("the restricting tiled pre-smoother is FP32 only");
+      return SNAC_ERR_ARG;
+    }
+  } else if (mode == 1) {
     SNAC_TRY(allow_smem((const void *)k_rbgs_tile2d<T, NW, R, 1>, smem));
     SNAC_CUDA(launch_k(k_rbgs_tile2d<T, NW, R, 1>, g, dim3(NW * 32), smem, st, L, C, P.periodic[0], P.periodic[1],
                        active, P.nsys, sb, first_color, nhalf, x, b, xin, xc, part_bx, sing, part_x, part_b,
@@ -818,6 +965,41 @@ int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_c
   SNAC_TRY(rc);
   if (nchunk) *nchunk = part_bx ? nt * t.nw : 0;
   return SNAC_OK;
+}
+
+// The FP32 pre-smoother of level l (x = 0 in, 2 nu half-sweeps, xp out) that also writes the restricted
+// residual b_{l+1} of its output cells, and zeroes x_{l+1} when xcz is given: the pre-smoother and
+// plane_restrict of an unfused V-cycle in one pass, with the same values and the same tiles.
+template <typename T>
+int launch_rbgs_tile2d_restrict(const MgProblem &P, int l, const int *active, T *xp, const T *b, T *bc, T *xcz,
+                                cudaStream_t st) {
+  if constexpr (sizeof(T) != 4) {
+    set_error("the restricting tiled pre-smoother is FP32 only");
+    return SNAC_ERR_ARG;
+  } else {
+    if (l + 1 >= P.nlev || !bc) { set_error("restricting pre-smoother: level %d has no coarser level", l); return SNAC_ERR_ARG; }
+    const MgLevelD &L = P.L[l];
+    const MgLevelD &C = P.L[l + 1];
+    const TileShape t = choose_shape(L, 0, P.tile_shape);
+    const int nt = tiles_for(L, t);
+    const int nhalf = 2 * mg_nu(P, l);
+    prof_begin(KID_RBGS, st);
+    int rc;
+    if (t.nw == 8 && t.r == 2)
+      rc = launch_tile<T, 8, 2>(P, L, C, nt, nhalf, active, 0, 2, xp, b, nullptr, nullptr, nullptr, nullptr, nullptr, 0, st, bc, xcz);
+    else if (t.nw == 16 && t.r == 2)
+      rc = launch_tile<T, 16, 2>(P, L, C, nt, nhalf, active, 0, 2, xp, b, nullptr, nullptr, nullptr, nullptr, nullptr, 0, st, bc, xcz);
+    else if (t.nw == 8 && t.r == 3)
+      rc = launch_tile<T, 8, 3>(P, L, C, nt, nhalf, active, 0, 2, xp, b, nullptr, nullptr, nullptr, nullptr, nullptr, 0, st, bc, xcz);
+    else if (t.nw == 16 && t.r == 3)
+      rc = launch_tile<T, 16, 3>(P, L, C, nt, nhalf, active, 0, 2, xp, b, nullptr, nullptr, nullptr, nullptr, nullptr, 0, st, bc, xcz);
+    else if (t.nw == 8)
+      rc = launch_tile<T, 8, 4>(P, L, C, nt, nhalf, active, 0, 2, xp, b, nullptr, nullptr, nullptr, nullptr, nullptr, 0, st, bc, xcz);
+    else
+      rc = launch_tile<T, 16, 4>(P, L, C, nt, nhalf, active, 0, 2, xp, b, nullptr, nullptr, nullptr, nullptr, nullptr, 0, st, bc, xcz);
+    prof_end(KID_RBGS, st);
+    return rc;
+  }
 }
 
 template <typename T>
@@ -878,6 +1060,8 @@ template int launch_rbgs_tile2d<double>(const MgProblem &, int, const int *, int
 template int launch_rbgs_tile2d<float>(const MgProblem &, int, const int *, int, int, float *, const float *,
                                        const float *, const float *, double *, double *, double *, int, int *,
                                        cudaStream_t);
+template int launch_rbgs_tile2d_restrict<float>(const MgProblem &, int, const int *, float *, const float *, float *,
+                                                float *, cudaStream_t);
 template size_t coarse_smem_bytes<double>(const MgProblem &, int);
 template size_t coarse_smem_bytes<float>(const MgProblem &, int);
 template int launch_vcycle_coarse<double>(const MgProblem &, int, const double *, const int *, double *,

@@ -55,6 +55,7 @@ struct MgProblem {
   int nsm;                           // multiprocessors of the device (sizes the system batches)
   int tile_shape;                    // FP32 smoother tile: 0 auto, 1..4 = 8x2, 8x3, 16x2, 16x3 (warps x rows)
   int tile_inv;                      // FP32 tiled smoother: 1 / diagonal formed in registers instead of read
+  int tile_restrict;                 // FP32 tiled pre-smoother also restricts its residual (no separate pass)
   int waves;                         // waves of CTAs per batched plane launch
   int red_batch;                     // the reducing plane kernels batch systems (0: one system per CTA)
   int any_singular;                  // some system is singular (pure Neumann, zero shift)
@@ -79,6 +80,11 @@ template <typename T>
 int launch_rbgs_tile2d(const MgProblem &P, int l, const int *active, int first_color, int mode, T *x, const T *b,
                        const T *xin, const T *xc, double *part_bx, double *part_x, double *part_b, int part_stride,
                        int *nchunk, cudaStream_t st);
+// FP32 pre-smoother of level l (xp out) that also writes the restricted residual bc of level l + 1 and, when
+// xcz is given, zeroes that level's x (the separate restriction pass folded in; the same values)
+template <typename T>
+int launch_rbgs_tile2d_restrict(const MgProblem &P, int l, const int *active, T *xp, const T *b, T *bc, T *xcz,
+                                cudaStream_t st);
 template <typename T>
 size_t coarse_smem_bytes(const MgProblem &P, int l0);
 struct MgGeom;

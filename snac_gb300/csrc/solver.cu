@@ -564,6 +564,7 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
   P.nu_coarse = d.opt.nu_coarse > 0 ? d.opt.nu_coarse : (S.mode3d ? P.nu : 1);
   P.tile_shape = o.mg_tile >= 1 && o.mg_tile <= 6 ? o.mg_tile : 0;
   P.tile_inv = o.mg_inv == 1 ? 1 : 0;
+  P.tile_restrict = o.mg_restrict == -1 ? 0 : 1;
   P.waves = o.mg_waves > 0 ? o.mg_waves : 2;
   P.red_batch = o.mg_red_batch == -1 ? 0 : 1;
   auto up = [&](const void *src, size_t bytes) -> void * {

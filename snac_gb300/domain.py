@@ -20,8 +20,8 @@ class Domain:
     def __init__(self, case, precision: int = 0, nu: int = 0, device: int = 0, use_graph: int = 0, nu_coarse: int = 0,
                  **solver):
         """solver: further snac_options fields (inner_iters, inner_tol, inner_adapt, refine_steps, mg_fuse,
-        mg_cta_level, mg_tile, mg_waves, mg_red_batch, mg_lnu, tma, pdl, mg_inv); 0 or absent selects the library
-        default."""
+        mg_cta_level, mg_tile, mg_waves, mg_red_batch, mg_lnu, tma, pdl, mg_inv, mg_restrict); 0 or absent selects
+        the library default."""
         L = capi.lib()
         self.case = case
         c, arr, keep = capi.fill_descs(case)

@@ -6,6 +6,8 @@ the reference's LDC test layout (3-D solve and FFT along x), the Taylor-Green
 vortex (FFT along z) and the uneven four-block channel.  The reference's own
 golden vector is checked with the reference's tolerance.
 """
+import ctypes as C
+import dataclasses
 import os
 
 import numpy as np
@@ -166,11 +168,11 @@ def test_fused_vcycle_matches_unfused(snac_lib, precision, which, nu_coarse):
 def test_tile_smoother_inverse_diagonal_in_registers_is_bitwise(snac_lib):
     """mg_inv = 1 makes the FP32 tiled smoother form 1 / diagonal from the cell's coefficients and the system's
     shift instead of reading the per-system table; the table holds exactly those values, so the solves are
-    bit for bit the same."""
+    bit for bit the same (levels 0 and 1 tiled: mg_cta_level = 2)."""
     case = cases.channel_4block(nx=(32, 64), ny=(32, 48), nz=8)
     out = {}
     for inv in (0, 1):
-        d = Domain(case, precision=1, mg_inv=inv)
+        d = Domain(case, precision=1, mg_inv=inv, mg_cta_level=2)
         try:
             rng = np.random.default_rng(12)
             for ib in range(len(case.blocks)):
@@ -185,6 +187,47 @@ def test_tile_smoother_inverse_diagonal_in_registers_is_bitwise(snac_lib):
             d.close()
     for a, b in zip(out[0], out[1]):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("which", ["channel", "ldc_fft_x", "tgv", "lbox_fft_z"])
+def test_restricting_pre_smoother_is_bitwise(snac_lib, which):
+    """The FP32 tiled pre-smoother that restricts its own residual (the default) and the pre-smoother followed by
+    the separate restriction pass (mg_restrict = -1) give bit-identical solves and steps: y-only coarsening with
+    periodic x (channel), both axes halved between walls (the reference's cavity along x, four blocks), triperiodic
+    (Taylor-Green), and inactive cells in the plane (the L-shaped box along z).  Levels 0 and 1 run the tiled
+    smoothers (mg_cta_level = 2: these small layouts would otherwise fit the one-CTA V-cycle whole).  The fused
+    form launches fewer kernels per solve."""
+    case = {"channel": lambda: cases.channel_4block(nx=(32, 64), ny=(32, 48), nz=8),
+            "ldc_fft_x": lambda: cases.ldc_reference_test(fft_axis=1),
+            "tgv": lambda: cases.taylor_green(32),
+            "lbox_fft_z": lambda: dataclasses.replace(cases.l_shaped_box(32, 16), fft_axis=3)}[which]()
+    out, launches = {}, {}
+    for mode in (-1, 0):
+        d = Domain(case, precision=1, use_graph=0, mg_restrict=mode, mg_cta_level=2)
+        try:
+            rng = np.random.default_rng(13)
+            for ib in range(len(case.blocks)):
+                for k in (capi.U, capi.V, capi.W):
+                    d.set(ib, k, rng.standard_normal(d.shape(ib, k)))
+            d.bounduvw(False)
+            d.fillps(0.01)
+            d.updt_rhs()
+            n0, n1 = C.c_longlong(), C.c_longlong()
+            capi.check(capi.lib().snac_launch_count(C.byref(n0)))
+            assert d.solve_pressure() == 0
+            capi.check(capi.lib().snac_launch_count(C.byref(n1)))
+            launches[mode] = n1.value - n0.value
+            pp = [d.get(ib, capi.PP) for ib in range(len(case.blocks))]
+            d.bounduvw(False)
+            assert d.step(2) == 0
+            out[mode] = (pp, [d.get(ib, k) for ib in range(len(case.blocks)) for k in (capi.U, capi.V, capi.W, capi.P)],
+                         d.kinetic_energy())
+        finally:
+            d.close()
+    for a, b in zip(out[-1][0] + out[-1][1], out[0][0] + out[0][1]):
+        np.testing.assert_array_equal(a, b)
+    assert out[-1][2] == out[0][2]
+    assert launches[0] < launches[-1], launches
 
 
 @pytest.mark.parametrize("precision", [0, 1])
