@@ -189,21 +189,24 @@ def test_tile_smoother_inverse_diagonal_in_registers_is_bitwise(snac_lib):
         np.testing.assert_array_equal(a, b)
 
 
-@pytest.mark.parametrize("which", ["channel", "ldc_fft_x", "tgv", "lbox_fft_z"])
-def test_restricting_pre_smoother_is_bitwise(snac_lib, which):
+@pytest.mark.parametrize("which,tile", [("channel", 0), ("ldc_fft_x", 0), ("tgv", 0), ("lbox_fft_z", 0),
+                                        ("channel", 1), ("channel", 2), ("channel", 4), ("channel", 5),
+                                        ("channel", 6), ("lbox_fft_z", 2)])
+def test_restricting_pre_smoother_is_bitwise(snac_lib, which, tile):
     """The FP32 tiled pre-smoother that restricts its own residual (the default) and the pre-smoother followed by
     the separate restriction pass (mg_restrict = -1) give bit-identical solves and steps: y-only coarsening with
     periodic x (channel), both axes halved between walls (the reference's cavity along x, four blocks), triperiodic
-    (Taylor-Green), and inactive cells in the plane (the L-shaped box along z).  Levels 0 and 1 run the tiled
-    smoothers (mg_cta_level = 2: these small layouts would otherwise fit the one-CTA V-cycle whole).  The fused
-    form launches fewer kernels per solve."""
+    (Taylor-Green), and inactive cells in the plane (the L-shaped box along z), with the default tile shape and
+    every other one the autotuner may choose (mg_tile 1..6).  Levels 0 and 1 run the tiled smoothers
+    (mg_cta_level = 2: these small layouts would otherwise fit the one-CTA V-cycle whole).  The fused form
+    launches fewer kernels per solve."""
     case = {"channel": lambda: cases.channel_4block(nx=(32, 64), ny=(32, 48), nz=8),
             "ldc_fft_x": lambda: cases.ldc_reference_test(fft_axis=1),
             "tgv": lambda: cases.taylor_green(32),
             "lbox_fft_z": lambda: dataclasses.replace(cases.l_shaped_box(32, 16), fft_axis=3)}[which]()
     out, launches = {}, {}
     for mode in (-1, 0):
-        d = Domain(case, precision=1, use_graph=0, mg_restrict=mode, mg_cta_level=2)
+        d = Domain(case, precision=1, use_graph=0, mg_restrict=mode, mg_cta_level=2, mg_tile=tile)
         try:
             rng = np.random.default_rng(13)
             for ib in range(len(case.blocks)):
