@@ -9,7 +9,9 @@ kinetic energy within 1e-8, max|div u| <= 1e-10) on the layouts the benchmarks r
   velocity and pressure, 50 steps;
 * the lid-driven cavity 64^3 (3-D multigrid, Re = 1000, CFL 0.5) from rest, 100 steps;
 * the L-shaped closed box, three 144x144x96 blocks (3-D multigrid on a solver box a third inactive), from
-  rest, 10 steps.
+  rest, 10 steps;
+* the differentially heated cavity 512x512x256 (IMPDIFF u, v, w, T Helmholtz solves, Boussinesq buoyancy,
+  3-D pressure multigrid), 2 steps.
 
 The oracle (C restatement with OpenMP on all host cores) runs each case once; the GPU paths are compared
 against it.  Each test prints the measured errors.  These sizes exercise what the small layouts of the
@@ -136,5 +138,46 @@ def test_l_shaped_box_3x144x144x96_10_steps(snac_lib, oracle_mod):
         d = _gpu_run(case, fields, 10, precision)
         try:
             _check(case, O, d, f"L-shaped box 3x144x144x96, precision {precision}")
+        finally:
+            d.close()
+
+
+def test_heated_cavity_512x512x256_2_steps(snac_lib, oracle_mod):
+    """The differentially heated cavity at its benchmark size (512x512x256 = 67 M cells, stretched 1.5 toward every
+    wall, Ra = 1e8, Pr = 0.71, Boussinesq buoyancy, IMPDIFF: u, v, w and T Helmholtz solves plus the 3-D pressure
+    solve every stage), from rest with seeded temperature noise of 1e-3, at the reference test's fixed dt = 1e-3:
+    2 steps (the oracle's step takes about a minute on 16 host cores).  The temperature is compared too."""
+    case = cases.heated_cavity((512, 512, 256), dt_f=1e-3)
+
+    def init(grid):
+        n = [int(x) for x in case.blocks[0].ng]
+        z = np.zeros([x + 2 for x in n], order="F")
+        t = np.zeros_like(z)
+        r = cases.splitmix64_uniform_fast(0x5EED, n[0] * n[1] * n[2]).reshape(n, order="F")
+        t[1:-1, 1:-1, 1:-1] = 2e-3 * (r - 0.5)
+        return {0: ((capi.U, z), (capi.V, z), (capi.W, z), (capi.P, z), (capi.S0, t))}
+
+    if "dhc" not in _ORACLE:
+        O = oracle_mod.OracleDomain(case)
+        fields = init(None)
+        for k, f in fields[0]:
+            O.field(0, k)[...] = f
+        O.bounduvw(False)
+        O.boundp(capi.P)
+        O.boundp(capi.S0)
+        O.step(2)
+        _ORACLE["dhc"] = (O, fields)
+    O, fields = _ORACLE["dhc"]
+    for precision in (0, 1):
+        d = Domain(case, precision=precision, use_graph=precision)
+        try:
+            for k, f in fields[0]:
+                d.set(0, k, f)
+            d.bounduvw(False)
+            d.boundp(capi.P)
+            d.boundp(capi.S0)
+            assert d.step(2) == 0
+            err_t = compare_fields(case, O, d, (capi.S0,), 1e-10)
+            _check(case, O, d, f"heated cavity 512x512x256, precision {precision} (temperature {err_t:.2e})")
         finally:
             d.close()
