@@ -30,6 +30,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <mutex>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -128,6 +129,7 @@ __device__ __forceinline__ void rbgs_tile2d(MgLevelD L, MgLevelD C, int per0, in
                                             double *__restrict__ part_b, int part_stride, const T *__restrict__ shift,
                                             int inv_inline, T *__restrict__ bco, T *__restrict__ xcz) {
   static_assert(NW % 2 == 0, "rows w + NW q of a thread must share their colour parity");
+  using V2 = typename std::conditional<sizeof(T) == 4, float2, double2>::type;
   constexpr int SH = NW * R, BY = SH - 2 * TH;
   static_assert(TBX % 2 == 0 && TH % 2 == 0 && BY % 2 == 0, "coarse cells must not straddle tiles");
   constexpr int NA = MODE == 1 ? 4 : 2;
@@ -261,13 +263,18 @@ __device__ __forceinline__ void rbgs_tile2d(MgLevelD L, MgLevelD C, int per0, in
 #pragma unroll
       for (int q = 0; q < R; q++) {
         const T *sq = sk + NW * q * 64;
+        // the staged pairs of b, 1/d and the pre-smoothed x read as vectors (a 2-way bank conflict less per
+        // array; spos is even and every staged array starts on a 16-byte boundary)
+        const V2 b2 = *reinterpret_cast<const V2 *>(sq);
+        const V2 i2 = inv_inline ? V2{} : *reinterpret_cast<const V2 *>(sq + SH * 64);
+        const V2 p2 = MODE == 1 ? *reinterpret_cast<const V2 *>(sq + 2 * SH * 64) : V2{};
 #pragma unroll
         for (int p = 0; p < 2; p++) {
           const bool lv = live >> (2 * q + p) & 1;
-          bv[q][p] = lv ? sq[p] : T(0);
-          iv[q][p] = lv ? (inv_inline ? rcpt(fmat(sh, dwt[q][p], dcc[q][p])) : sq[SH * 64 + p]) : T(0);
+          bv[q][p] = lv ? (p ? b2.y : b2.x) : T(0);
+          iv[q][p] = lv ? (inv_inline ? rcpt(fmat(sh, dwt[q][p], dcc[q][p])) : (p ? i2.y : i2.x)) : T(0);
           T x_ = 0;
-          if (MODE == 1 && lv) x_ = sq[2 * SH * 64 + p] + sq[3 * SH * 64 + (xhalf ? 0 : p)];
+          if (MODE == 1 && lv) x_ = (p ? p2.y : p2.x) + sq[3 * SH * 64 + (xhalf ? 0 : p)];
           if (MODE != 1 && t0 && p == pfirst) x_ = bv[q][p] * iv[q][p];
           (p ? xo : xe)[tpos + NW * q * TRS] = x_;
         }
@@ -454,6 +461,7 @@ constexpr int COARSE_THREADS = 1024;
 struct CoarseLev {
   int ox, ob, oi;  // shared-memory offsets (elements) of x, b, 1/d
   int oc;          // couplings c0 | c1 at oc, oc + ncell; -1: global memory
+  int od;          // the system's diagonal shift w01 + cc (the residual's); -1: formed from global memory
   int hdj, hdi;    // walker steps over the half rows of a colour: COARSE_THREADS / h0, % h0 (h0 = (n0+1)/2)
   int fdj, fdi;    // walker steps over full rows: COARSE_THREADS / n0, % n0
 };
@@ -481,7 +489,7 @@ static bool coarse_plan(const MgProblem &P, int l0, CoarsePlan *plan, size_t *by
     e.ox = (int)o;
     e.ob = (int)o + n;
     o += 2 * (size_t)n;
-    e.oi = e.oc = -1;
+    e.oi = e.oc = e.od = -1;
     if (l == last && dense) continue;
     e.oi = (int)o;
     o += n;
@@ -494,6 +502,14 @@ static bool coarse_plan(const MgProblem &P, int l0, CoarsePlan *plan, size_t *by
     const size_t need = 2 * (size_t)P.L[l].ncell;
     if ((o + need) * sizeof(T) > MG_COARSE_SMEM_MAX) break;
     pl.lev[l].oc = (int)o;
+    o += need;
+  }
+  // then the diagonals the restriction's residual uses, where room is left (coarsest first): formed once per
+  // launch instead of two L2 reads per child in every restriction phase
+  for (int l = last - 1; l >= l0; l--) {
+    const size_t need = (size_t)P.L[l].ncell;
+    if ((o + need) * sizeof(T) > MG_COARSE_SMEM_MAX) break;
+    pl.lev[l].od = (int)o;
     o += need;
   }
   if (plan) *plan = pl;
@@ -633,14 +649,18 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P
     const T *__restrict__ cp0 = LA<T>::cp(L, 0);
     const T *__restrict__ cp1 = LA<T>::cp(L, 1);
     T *id = ID(l);
-    const bool cs = plan.lev[l].oc >= 0;
+    const bool cs = plan.lev[l].oc >= 0, ds = plan.lev[l].od >= 0;
     T *c0 = base + plan.lev[l].oc, *c1 = c0 + n;
+    T *dg = base + plan.lev[l].od;
+    const T *__restrict__ ccl = LA<T>::cc(L);
+    const T *__restrict__ wtl = LA<T>::w01(L);
     for (int c = threadIdx.x; c < n; c += blockDim.x) {
       id[c] = invd[c];
       if (cs) {
         c0[c] = cp0[c];
         c1[c] = cp1[c];
       }
+      if (ds) dg[c] = fmat(sh, wtl[c], ccl[c]);  // the diagonal of the unfused residual, term by term
     }
   }
   {
@@ -674,7 +694,7 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse(MgProblem P
             const int i = C.coarsened[0] ? 2 * I + di : I, j = C.coarsened[1] ? 2 * J + dj : J;
             const int c = i + n0 * j;
             if (id[c] == T(0)) continue;
-            const T dv = fmat(sh, w01[c], cc[c]);  // the diagonal of the unfused residual, term by term
+            const T dv = E.od >= 0 ? base[E.od + c] : fmat(sh, w01[c], cc[c]);  // the unfused residual's diagonal
             const T acc = offdiag_xy<T>(n0, n1, per0, per1, c0, c1, [&](int e) { return x[e]; }, c, i, j);
             sum += b[c] - fmat(dv, x[c], acc);
           }
@@ -869,7 +889,9 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1) k_vcycle_coarse3d(MgProblem
 // ---------------------------------------------------------------- launchers
 // opt in to more than 48 KB of dynamic shared memory, once per kernel and device
 static int allow_smem(const void *fn, size_t bytes) {
-  if (bytes <= 48 * 1024) return SNAC_OK;
+  // the default limit of 48 KB covers static and dynamic shared memory together: the kernels here keep at most
+  // 8 KB of static shared memory, so up to 40 KB of dynamic shared memory needs no opt-in
+  if (bytes <= 40 * 1024) return SNAC_OK;
   static std::mutex mu;
   static std::vector<std::pair<const void *, int>> done;
   int dev = 0;
