@@ -9,6 +9,61 @@ module mod_snac_gpu
   implicit none
   ! field kinds (enum of snac_gpu.h)
   integer(c_int), parameter :: SNAC_U = 0, SNAC_V = 1, SNAC_W = 2, SNAC_P = 3, SNAC_PP = 4, SNAC_S0 = 9
+  integer(c_int), parameter :: SNAC_MAX_SCAL = 4
+  ! the arguments of snac_init: the same members in the same order as the C structs (the C arrays' dimensions
+  ! reversed, so side and direction run fastest as in the reference's block_cbcvel(side,dir,comp))
+  ! one &blocks entry (param.f90:332-360); a friend link 'F' carries the neighbour's 1-based id in the value
+  type, bind(C) :: snac_block_desc
+    integer(c_int)         :: ng(3)
+    real(c_double)         :: lmin(3), lmax(3)
+    integer(c_int)         :: gt(3)
+    real(c_double)         :: gr(3)
+    character(kind=c_char) :: cbcvel(2,3,3)
+    real(c_double)         :: bcvel(2,3,3)
+    character(kind=c_char) :: cbcpre(2,3)
+    real(c_double)         :: bcpre(2,3)
+    character(kind=c_char) :: cbcscal(2,3,SNAC_MAX_SCAL)
+    real(c_double)         :: bcscal(2,3,SNAC_MAX_SCAL)
+    type(c_ptr)            :: grid_file(3)       ! c_loc of grid/grid_?_b_###.bin contents, or c_null_ptr
+    integer(c_int)         :: inflow_type(2,3)
+  end type
+  ! &dns, &scalar and &hypre (param.f90:342-355) plus the build flags
+  type, bind(C) :: snac_case
+    integer(c_int) :: nblocks
+    real(c_double) :: visci, cfl, dtmax, dt_f
+    real(c_double) :: bforce(3), gacc(3), beta
+    integer(c_int) :: nscal
+    real(c_double) :: alphai(SNAC_MAX_SCAL), ssource(SNAC_MAX_SCAL), scalf(SNAC_MAX_SCAL)
+    integer(c_int) :: is_sforced(SNAC_MAX_SCAL)
+    integer(c_int) :: icheck
+    integer(c_int) :: fft_axis                   ! 0: 3-D solve; 1, 2, 3: FFT_AXIS
+    integer(c_int) :: impdiff                    ! _IMPDIFF
+    integer(c_int) :: boussinesq                 ! _BOUSSINESQ_BUOYANCY
+    real(c_double) :: tol                        ! hypre_tol
+    integer(c_int) :: maxiter                    ! hypre_maxiter
+  end type
+  ! library options (no reference counterpart); zero selects each default
+  type, bind(C) :: snac_options
+    integer(c_int) :: precision = 1              ! 0 plain FP64 multigrid-PCG, 1 FP32 V-cycles in FP64 refinement
+    integer(c_int) :: use_graph = 1              ! replay each refinement step as a CUDA graph
+    integer(c_int) :: nu = 0
+    integer(c_int) :: device = 0
+    integer(c_int) :: nu_coarse = 0
+    integer(c_int) :: inner_iters = 0
+    real(c_double) :: inner_tol = 0
+    integer(c_int) :: inner_adapt = 0
+    integer(c_int) :: refine_steps = 0
+    integer(c_int) :: mg_fuse = 0
+    integer(c_int) :: mg_cta_level = 0
+    integer(c_int) :: mg_tile = 0
+    integer(c_int) :: mg_waves = 0
+    integer(c_int) :: mg_red_batch = 0
+    integer(c_int) :: mg_lnu = 0
+    integer(c_int) :: tma = 0
+    integer(c_int) :: pdl = 0
+    integer(c_int) :: mg_inv = 0
+    integer(c_int) :: mg_restrict = 0
+  end type
   interface
     ! rk.f90:7-128 -- u,v,w,p halo'd; dudtrko interior; s1 = scalars(1)%val or c_null_ptr
     integer(c_int) function snac_rk_mom(rkpar,lo,hi,dxc,dxf,dyc,dyf,dzc,dzf,dt,bforce,gacc,beta,s1,visc, &
@@ -179,6 +234,14 @@ module mod_snac_gpu
       real(c_double), intent(in) :: dlc(0:1,0:1,3), dlf(0:1,3)
       real(c_double), value :: alpha
       real(c_double) :: p(*)
+    end function
+    ! domain layer: every block placed, gridded and resident on the GPU, solvers built (initmpi.f90, initgrid.f90,
+    ! solver.f90 set-up); nblocks entries in blocks
+    integer(c_int) function snac_init(c,blocks,opt) bind(C,name='snac_init')
+      import
+      type(snac_case), intent(in) :: c
+      type(snac_block_desc), intent(in) :: blocks(*)
+      type(snac_options), intent(in) :: opt
     end function
     ! domain layer (all blocks resident on the GPU after snac_init): the per-stage routines of main.f90:906-1043
     integer(c_int) function snac_rk_mom_all(irk) bind(C,name='snac_rk_mom_all')
