@@ -123,9 +123,11 @@ typedef struct snac_options {
   int mg_fuse;        /* bits: 1 tiled FP32 smoother, 2 one-CTA coarse V-cycle FP32, 4 tiled FP64 smoother,
                          8 one-CTA coarse V-cycle FP64 (default 11); -1: one kernel per sweep */
   int mg_cta_level;   /* finest level the one-CTA coarse V-cycle may start at (default: the finest that fits;
-                         with the 3-D solve, the finest that fits with at most 4096 cells) */
+                         with the 3-D solve, and for the FP32 plane systems with the tiled smoother on, the
+                         finest that fits with at most 4096 cells) */
   int mg_tile;        /* FP32 smoother tile, warps x rows per warp: 1 8x2, 2 8x3, 3 16x2, 4 16x3, 5 8x4, 6 16x4
-                         (default: the shape among the first four with the fewest tile rows) */
+                         (default: the shape among the first four with the fewest tile rows, the three-row
+                         shapes' rows counted twice for their halved occupancy) */
   int mg_waves;       /* waves of CTAs per batched plane launch (default 2) */
   int mg_red_batch;   /* -1: the reducing plane kernels run one system per CTA (default: batched) */
   int mg_lnu;         /* first multigrid level that uses nu_coarse (default 2) */

@@ -54,8 +54,10 @@ inline int tile_by(TileShape t) { return t.nw * t.r - 2 * TH; }
 inline int tiles_for(const MgLevelD &L, TileShape t) {
   return ((L.n[0] + TBX - 1) / TBX) * ((L.n[1] + tile_by(t) - 1) / tile_by(t));
 }
-// the shape given by `pref` (1..4, FP32 only), else the one that processes the fewest tile rows (ties: the
-// smaller tile)
+// the shape given by `pref` (1..6, FP32 only), else the one that processes the fewest tile rows (ties: the
+// smaller tile), rows of the three-row shapes counted twice: they need more than 64 registers a thread, which
+// halves the warps a multiprocessor holds (channel level 2, 256 x 36: 16 x 3 tiles sweep 48 rows, 16 x 2 tiles
+// 64, and the step takes 17.05 against 16.52 ms)
 TileShape choose_shape(const MgLevelD &L, int prec, int pref) {
   if (!prec && pref >= 1 && pref <= NSHAPES_F) return SHAPES_F[pref - 1];
   const TileShape *opts = prec ? SHAPES_D : SHAPES_F;
@@ -64,7 +66,7 @@ TileShape choose_shape(const MgLevelD &L, int prec, int pref) {
   long bestc = -1;
   for (int q = 0; q < nopt; q++) {
     const TileShape t = opts[q];
-    const long cost = (long)((L.n[1] + tile_by(t) - 1) / tile_by(t)) * t.nw * t.r;
+    const long cost = (long)((L.n[1] + tile_by(t) - 1) / tile_by(t)) * t.nw * t.r * (t.r >= 3 ? 2 : 1);
     if (bestc < 0 || cost < bestc) { bestc = cost; best = t; }
   }
   return best;
@@ -92,15 +94,20 @@ int tile2d_max_parts(const MgLevelD &L) {
   return m;
 }
 
-bool tile2d_ok(const MgProblem &P, int l, int prec) {
-  (void)prec;
+bool tile2d_geometry_ok(const MgProblem &P, int l) {
   if (P.mode3d || l >= P.nlev - 1 || 2 * mg_nu(P, l) > TH) return false;
   const MgLevelD &L = P.L[l];
-  if (!L.xp || !L.xpf || !L.invd || !L.invdf) return false;
   if (L.n[0] & 1) return false;  // column pairs are copied as one aligned unit
   for (int a = 0; a < 2; a++)
     if (P.periodic[a] && L.n[a] > 1 && (L.n[a] & 1)) return false;  // red-black colouring must wrap consistently
   return true;
+}
+
+bool tile2d_ok(const MgProblem &P, int l, int prec) {
+  (void)prec;
+  if (!tile2d_geometry_ok(P, l)) return false;
+  const MgLevelD &L = P.L[l];
+  return L.xp && L.xpf && L.invd && L.invdf;
 }
 
 // shared-memory row of the even/odd x tile: 32 column pairs plus a zero pad on each side, so that the

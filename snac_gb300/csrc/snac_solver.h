@@ -72,6 +72,7 @@ __host__ __device__ inline int mg_nu(const MgProblem &P, int l) { return l >= P.
 struct MgGeom;
 // fused kernels (k_mg_fused.cu)
 bool tile2d_ok(const MgProblem &P, int l, int prec);
+bool tile2d_geometry_ok(const MgProblem &P, int l);  // tile2d_ok before the level's arrays exist
 int tile2d_max_parts(const MgLevelD &L);
 int tile2d_shape_index(const MgProblem &P, int l);
 // part_bx: partials of b.x of the stored cells (post-smoother, mode 1); for the singular systems also those

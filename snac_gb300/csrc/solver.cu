@@ -652,7 +652,7 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
     // tile's redundant halo updates cost more than they save where FP64 arithmetic bounds.
     P.fused = o.mg_fuse == -1 ? 0 : (o.mg_fuse > 0 ? o.mg_fuse & 15 : 11);
     // the finest level the one-CTA coarse tail may start at: the one asked for, or by default the finest that
-    // fits (3-D mode: and has at most MG_COARSE3D_CELLS cells)
+    // fits (3-D mode, and FP32 plane systems with the tiled smoother: and has at most MG_COARSE3D_CELLS cells)
     const int lmin = std::max(0, o.mg_cta_level);
     for (int prec = 0; prec < 2; prec++) {
       P.cta_level[prec] = P.nlev;
@@ -660,7 +660,12 @@ int solver_create(Domain &d, PoissonSolver &S, bool upload, int field) {
         size_t bytes;
         if (S.mode3d) bytes = prec ? coarse3d_smem_bytes<double>(P, l) : coarse3d_smem_bytes<float>(P, l);
         else bytes = prec ? coarse_smem_bytes<double>(P, l) : coarse_smem_bytes<float>(P, l);
-        if (S.mode3d && o.mg_cta_level <= 0 && P.L[l].ncell > MG_COARSE3D_CELLS) continue;
+        // by default the one-CTA cycle takes no level of more than MG_COARSE3D_CELLS cells where that level has
+        // a kernel that spreads over the GPU: always in 3-D mode, and for the FP32 plane systems where the tiled
+        // smoother takes the level (channel 256 x 144: from the 2,304-cell level 16.52 ms per step, from the
+        // 9,216-cell one 16.66 ms)
+        const bool spread = S.mode3d || (prec == 0 && (P.fused & 1) && tile2d_geometry_ok(P, l));
+        if (spread && o.mg_cta_level <= 0 && P.L[l].ncell > MG_COARSE3D_CELLS) continue;
         if (bytes <= (S.mode3d ? MG_COARSE3D_SMEM_MAX : MG_COARSE_SMEM_MAX)) { P.cta_level[prec] = l; break; }
       }
     }

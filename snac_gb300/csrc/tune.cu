@@ -208,7 +208,7 @@ int snac_autotune(int steps, snac_tune_result *out) {
     rc = try_group(g);
   }
   if (rc == SNAC_OK && found && d->ps) {
-    // the one-CTA coarse V-cycle from the default level, one level coarser, or (3-D mode) one level finer
+    // the one-CTA coarse V-cycle from the default level, one level coarser or one level finer
     d->opt = best_opt;
     rc = rebuild(*d);
     if (rc == SNAC_OK) {
@@ -218,7 +218,7 @@ int snac_autotune(int steps, snac_tune_result *out) {
       if (l0 + 1 < d->ps->P.nlev) {
         snac_options o = best_opt; o.mg_cta_level = l0 + 1; g.push_back(o);
         o.mg_cta_level = l0; g.push_back(o);
-        if (!plane && l0 > 0) { o.mg_cta_level = l0 - 1; g.push_back(o); }
+        if (l0 > 1) { o.mg_cta_level = l0 - 1; g.push_back(o); }  // (0 would mean the default again)
       }
       rc = try_group(g);
     }
